@@ -1,0 +1,207 @@
+/*
+ * ekgpu.h -- C ABI of the GB300 RK3 duct substep (RK_DUCT + REM_DIV_CURV).
+ *
+ * Drop-in boundary for the Fortran driver of ekman_bl.  The reference path
+ * has no argument lists: RK_DUCT (src/duct.F90:237-2469) and REM_DIV_CURV
+ * (src/duct.F90:2472-2818) read and write module globals declared in
+ * src/modules.F90:95-316.  Each entry point below replaces one of those
+ * subroutine calls plus the module state it touches; the comment on each
+ * declaration names the reference routine (file:line).  Plain C types only:
+ * every array is a host pointer in the reference's own Fortran layout
+ * (column-major, first index fastest, complex*16 stored as interleaved
+ * (re,im) doubles), so a Fortran caller passes its module arrays through
+ * ISO_C_BINDING with no copy or transpose.
+ *
+ * Layouts (NX, NY, NZ as in grid_def; one MPI rank, so NXP = NX+1,
+ * NX2P = NX/2, NZV = NZ+2):
+ *   spectral field  CU1X(0:NX/2, 0:NZ+1, 0:NY+1) complex*16  -> 2*(NX/2+1)*(NZ+2)*(NY+2) doubles
+ *   physical field  U1X (0:NX+1, 0:NZ+1, 0:NY+1) real*8      -> (NX+2)*(NZ+2)*(NY+2) doubles
+ *   2-D metric      INT_JACOB(0:NZ+2, 0:NY+2)                 -> (NZ+3)*(NY+3) doubles
+ *   face metric     GMAT_11(0:NZ+2, 0:NY+2, 2)                -> 2*(NZ+3)*(NY+3) doubles
+ *   grid points     xpoint(0:NZ+1, 0:NY+1)                    -> (NZ+2)*(NY+2) doubles
+ *
+ * Ownership: the caller owns every host buffer and the library only reads or
+ * writes it during the call.  The library owns device memory, which stays
+ * resident between calls (state never leaves HBM between substeps).
+ * Errors: every entry point returns an ek_status; none calls exit().  A
+ * failed call leaves a message readable through ekgpu_last_error().
+ * Threading: one context per host thread; calls on one context are
+ * serialised on the context's stream.
+ */
+#ifndef EKGPU_H
+#define EKGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum ek_status {
+  EK_OK = 0,
+  EK_ERR_ARG = 1,            /* bad or unsupported argument                     */
+  EK_ERR_CUDA = 2,           /* a CUDA call failed                              */
+  EK_ERR_NOT_CONVERGED = 3,  /* multigrid hit its cycle cap; phi still returned */
+  EK_ERR_NAN = 4,            /* divergence is NaN (reference: STOP 'DIV is a NaN', duct.F90:2811) */
+  EK_ERR_TIMEOUT = 5,        /* a bounded device wait expired                   */
+  EK_ERR_STATE = 6           /* call order violated (e.g. step before metrics)  */
+} ek_status;
+
+/* Boundary-wall index into the *_bc arrays, in input.dat order
+ * (diablo.F90:260-284): LOWER=YMIN, UPPER=YMAX, LEFT=ZMIN, RIGHT=ZMAX. */
+enum { EK_YMIN = 0, EK_YMAX = 1, EK_ZMIN = 2, EK_ZMAX = 3 };
+
+/* Multigrid stopping rule. */
+enum {
+  EK_MG_STOP_RELCHANGE = 0,  /* MUDPACK rule: max|phi_k - phi_{k-1}| / max|phi_k| <= tol (mud2cr.f:301-326) */
+  EK_MG_STOP_RESIDUAL = 1    /* ||b - A phi||_2 / ||b||_2 <= tol, per real 2-D problem                  */
+};
+
+/* Run parameters: the values the Fortran driver reads from input.dat and
+ * grid_def (diablo.F90:242-337, grid_def:7-50).  Fill with
+ * ekgpu_default_params() and override. */
+typedef struct ek_params {
+  int nx, ny, nz;            /* NX (spanwise, Fourier), NY, NZ interior counts          */
+  double lx;                 /* LX, spanwise period: KX(i) = 2*pi*i/LX                 */
+  double nu;                 /* NU                                                      */
+  double delta_t;            /* DELTA_T (fixed; VARIABLE_DT is not supported)           */
+  double f0;                 /* F_0, Coriolis parameter                                 */
+  double wbulk0;             /* WBULK0 (geostrophic wind of the Coriolis term)          */
+  int f_type;                /* F_TYPE: 1 constant PX0, 2 oscillatory                   */
+  double px0, omega0, amp_omega0, time;  /* mean-pressure forcing (duct.F90:411-455)  */
+  int n_th;                  /* N_TH: 0 or 1 scalar                                     */
+  double pr;                 /* PR(1)                                                   */
+  double ri_tau;             /* RI_TAU(1) (buoyancy coefficient)                        */
+  int cont_strat;            /* CONTINUOUS stratification flag CONT_STRAT               */
+  int ic_type;               /* IC_TYPE (only 7, the shipped value, is supported)       */
+  int u_bc[4], v_bc[4], w_bc[4], th_bc[4];            /* BC codes per wall            */
+  double u_bc_c1[4], v_bc_c1[4], w_bc_c1[4], th_bc_c1[4]; /* BC constants *_C1      */
+  int mudpack_bc[4];         /* MUDPACK_BC nxa,nxb,nyc,nyd (only 0 0 2 2 supported)    */
+  int mg_ixp, mg_jyq, mg_iex, mg_jey; /* grid_def iixp,jjyq,iiex,jjey; 0 = choose    */
+  int mg_maxcy;              /* maxcy (reference 6)                                     */
+  int mg_kcycle;             /* mgopt(1): 1 V, 2 W (reference 2)                        */
+  int mg_iprer, mg_ipost;    /* mgopt(2),(3) (reference 2,1)                            */
+  int mg_intpol;             /* mgopt(4): 1 linear, 3 cubic (reference 3)               */
+  int mg_stop;               /* EK_MG_STOP_*                                            */
+  double mg_tol;             /* tolmax: reference REAL*4 10.0**(-6) widened to REAL*8   */
+  int quirk_phi_fp32;        /* Q1: CMPLX(P_TMP2,P_TMP) rounds phi to REAL*4 (duct.F90:2664) */
+  int sponge_type;           /* SPONGE_TYPE (only 0 supported)                          */
+  int les;                   /* LES (only 0 supported)                                  */
+} ek_params;
+
+/* Geometry and background fields of JACOBI_TRANS (diablo.F90:1088-1570);
+ * host pointers in the layouts listed at the top of this file. */
+typedef struct ek_metrics {
+  const double *int_jacob;                  /* INT_JACOB(0:NZ+2,0:NY+2)       */
+  const double *gmat_11, *gmat_12, *gmat_22; /* GMAT_**(0:NZ+2,0:NY+2,2)      */
+  const double *cjob_11, *cjob_12, *cjob_21, *cjob_22; /* CJOB_**(...,2)     */
+  const double *th_bar;                      /* TH_BAR(0:NZ+2,0:NY+2), may be NULL when n_th == 0 */
+} ek_metrics;
+
+/* Per-call multigrid report. */
+typedef struct ek_mg_stats {
+  int nprob;                 /* real 2-D problems solved                         */
+  int min_cycles, max_cycles;/* cycles after FMG, over problems                  */
+  int n_not_converged;       /* problems that hit maxcy                          */
+  double max_relchange;      /* largest final relmax                             */
+  double max_residual;       /* largest final ||b-A phi||/||b|| (residual rule)  */
+} ek_mg_stats;
+
+/* Field selectors for ekgpu_get_field / ekgpu_put_field. */
+enum {
+  EK_F_CU1 = 0, EK_F_CU2, EK_F_CU3, EK_F_CP, EK_F_CTH,   /* state (spectral)   */
+  EK_F_CF1, EK_F_CF2, EK_F_CF3, EK_F_CFTH,              /* RK explicit terms  */
+  EK_F_CR1,                                              /* phi after REM_DIV  */
+  EK_F_NFIELDS
+};
+
+typedef struct ek_ctx ek_ctx;
+
+/* Fill *p with the shipped rundir_unst/input.dat choices that the path
+ * supports (input.dat:1-62), sizes from the caller. */
+int ekgpu_default_params(ek_params *p);
+
+/* Allocate a context and its device state.  Replaces allocate_var
+ * (ALLOCATION.F90:1-217), INIT_FFT (diablo.F90:563, source missing from the
+ * reference tree), the RKW3 constants (diablo.F90:568-576) and INIT_DUCT
+ * (duct.F90:7-232).  Unsupported options give EK_ERR_ARG. */
+int ekgpu_create(const ek_params *p, ek_ctx **ctx);
+
+/* Free the context and its device memory. */
+void ekgpu_destroy(ek_ctx *ctx);
+
+/* Text of the last error on this context (never NULL). */
+const char *ekgpu_last_error(const ek_ctx *ctx);
+
+/* Bind the context to an existing CUDA stream (cudaStream_t passed as a
+ * pointer; NULL returns to the context's own stream). */
+int ekgpu_set_stream(ek_ctx *ctx, void *stream);
+
+/* Upload the metric arrays built by JACOBI_TRANS (diablo.F90:1088-1570). */
+int ekgpu_set_metrics(ek_ctx *ctx, const ek_metrics *m);
+
+/* Host helper: JACOBI_TRANS restated (diablo.F90:1088-1570) from grid
+ * points xpoint/ypoint(0:NZ+1,0:NY+1).  Writes the metric arrays into the
+ * caller's buffers (sizes as in the layout table); th_bar gets the
+ * CONT_STRAT profile -ypoint+ypoint(0,NY+1) when cont_strat != 0. */
+int ekgpu_metrics_from_grid(const ek_params *p, const double *xpoint,
+                            const double *ypoint, double *int_jacob,
+                            double *gmat_11, double *gmat_12, double *gmat_22,
+                            double *cjob_11, double *cjob_12, double *cjob_21,
+                            double *cjob_22, double *th_bar);
+
+/* Copy the Fourier-space state CU1X, CU2X, CU3X, CPX, CTHX in (upload) or
+ * out (download).  Replaces READ_FLOW's fill of the module arrays
+ * (diablo.F90:918-1072) and SAVE_FLOW's read of them (diablo.F90:753-837).
+ * cth may be NULL when n_th == 0.  Upload also zeroes CF*. */
+int ekgpu_upload_state(ek_ctx *ctx, const double *cu1, const double *cu2,
+                       const double *cu3, const double *cp, const double *cth);
+int ekgpu_download_state(ek_ctx *ctx, double *cu1, double *cu2, double *cu3,
+                         double *cp, double *cth);
+
+/* Read or write one spectral field (EK_F_*) in the CU1X layout. */
+int ekgpu_get_field(ek_ctx *ctx, int field, double *out);
+int ekgpu_put_field(ek_ctx *ctx, int field, const double *in);
+
+/* One RK substep rk_step in {1,2,3}: RK_DUCT (duct.F90:237-2469) including
+ * REM_DIV_CURV and the pressure update (duct.F90:2455-2466). */
+int ekgpu_rk_substep(ek_ctx *ctx, int rk_step);
+
+/* nsteps full RK3 steps: the driver loop DO RK_STEP=1,3; CALL RK_DUCT
+ * (diablo.F90:152-154), repeated; advances params.time by DELTA_T per step. */
+int ekgpu_step(ek_ctx *ctx, int nsteps);
+
+/* The projection alone: REM_DIV_CURV (duct.F90:2472-2818) on the current
+ * state, leaving phi in CR1 (as the reference leaves it in CR1X). */
+int ekgpu_rem_div(ek_ctx *ctx);
+
+/* Batched per-kx Poisson: for each problem p, solve the 9-point operator of
+ * dismd2cr (mud2cr.f:501-1270) with coefficients cofcr (duct.F90:3900-3934)
+ * and ce = -kx2[p]*INT_JACOB, right-hand side rhs[p] on the MUDPACK grid
+ * (0:NZ+1,0:NY+1) (what phi_bc, duct.F90:3867, hands to mud2cr), phi zero
+ * initial guess, FMG + k-cycles as MULTIGRID_MUDPACK (mg_solver2d.F90:75-201).
+ * rhs and phi are host arrays of nprob*(NZ+2)*(NY+2) doubles, problem
+ * outermost.  Returns EK_ERR_NOT_CONVERGED (phi still written) when a
+ * problem hits the cycle cap. */
+int ekgpu_poisson_batch(ek_ctx *ctx, const double *rhs, double *phi,
+                        const double *kx2, int nprob, ek_mg_stats *stats);
+
+/* Same solve on device pointers (rhs, phi, kx2 in device memory, same
+ * layout); no host copies.  For callers that keep data resident. */
+int ekgpu_poisson_batch_device(ek_ctx *ctx, const double *rhs_dev,
+                               double *phi_dev, const double *kx2_dev,
+                               int nprob, ek_mg_stats *stats);
+
+/* Mean |div| after the last projection (duct.F90:2790-2806, the value the
+ * reference prints as "Divergence after the projection step"). */
+int ekgpu_last_divergence(ek_ctx *ctx, double *div);
+
+/* Stats of the last multigrid call made by a substep or poisson call. */
+int ekgpu_last_mg_stats(ek_ctx *ctx, ek_mg_stats *stats);
+
+/* Number of kernel launches this context issued since creation. */
+long long ekgpu_launch_count(const ek_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
