@@ -1,0 +1,598 @@
+// C ABI of the GB300 duct substep (include/ekgpu.h) and the host-side
+// orchestration of one RK substep: the same order of operations as
+// RK_DUCT (src/duct.F90:237-2469), with every transform, stencil and solve
+// running on the GPU and the state resident in HBM.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+
+#include "ek_internal.h"
+
+using namespace ek;
+
+struct ek_ctx {
+  Ctx c;
+};
+
+namespace ek {
+void rk_init_attributes();
+void fft_init_attributes();
+}  // namespace ek
+
+namespace {
+
+int fail(Ctx &c, int code, const std::string &m) {
+  c.err = m;
+  return code;
+}
+
+template <typename F>
+int guarded(ek_ctx *h, F &&f) {
+  if (!h) return EK_ERR_ARG;
+  try {
+    return f(h->c);
+  } catch (const CudaError &e) {
+    h->c.err = e.msg;
+    return EK_ERR_CUDA;
+  } catch (const std::bad_alloc &) {
+    h->c.err = "host allocation failed";
+    return EK_ERR_CUDA;
+  }
+}
+
+template <typename T>
+T *dalloc(Ctx &c, size_t n) {
+  void *p = nullptr;
+  EK_CUDA(cudaMalloc(&p, n * sizeof(T)));
+  EK_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), c.stream));
+  c.allocs.push_back(p);
+  return static_cast<T *>(p);
+}
+
+bool supported_bc(const ek_params &p, std::string &why) {
+  auto in = [](int v, std::initializer_list<int> s) { return std::find(s.begin(), s.end(), v) != s.end(); };
+  for (int f = 0; f < 3; ++f) {
+    const int *b = (f == 0) ? p.u_bc : (f == 1) ? p.v_bc : p.w_bc;
+    if (!in(b[EK_YMIN], {0, 1, 6}) || !in(b[EK_YMAX], {0, 1, 6})) { why = "velocity y BC must be 0, 1 or 6"; return false; }
+    if (!in(b[EK_ZMIN], {0, 1, 6}) || !in(b[EK_ZMAX], {0, 1, 6})) { why = "velocity z BC must be 0, 1 or 6"; return false; }
+    if ((f == 1 || f == 2) && b[EK_ZMIN] == 0) { why = "U2/U3 Dirichlet z-min needs the background profiles"; return false; }
+  }
+  if (!in(p.th_bc[EK_YMIN], {0, 1, 5, 6}) || !in(p.th_bc[EK_YMAX], {0, 1, 6}) || !in(p.th_bc[EK_ZMIN], {0, 1, 6}) ||
+      !in(p.th_bc[EK_ZMAX], {0, 1, 6})) {
+    why = "unsupported TH BC";
+    return false;
+  }
+  return true;
+}
+
+void run_rem_div(Ctx &c, double temp4, bool update_p, int *mg_status) {
+  const int P = 2 * (c.d.NKX + 1);
+  MgLevel &F = c.mg.lv[c.mg.ngrid - 1];
+  launch_divergence_rhs(c, F.rhs, P);
+  *mg_status = mg_solve(c, P, c.mg_kx2, nullptr);
+  launch_projection(c, c.mg_phif, P, temp4, update_p);
+}
+
+int substep(Ctx &c, int rk) {
+  const Dims &d = c.d;
+  const ek_params &p = c.p;
+  const bool th = p.n_th > 0;
+  const double TEMP4 = c.H_BAR[rk];
+  const double TEMP5 = c.BETA_BAR[rk] * c.H_BAR[rk];
+  launch_spectral_rhs(c, rk);
+  // to physical space (duct.F90:656-673)
+  {
+    C2rArgs a{};
+    a.j0 = 0; a.j1 = d.NY + 1; a.k0 = 0; a.k1 = d.NZ + 1;
+    a.src = c.CU1; a.dst = c.U1; launch_c2r(c, a);
+    a.src = c.CU2; a.dst = c.U2; launch_c2r(c, a);
+    a.src = c.CU3; a.dst = c.U3; launch_c2r(c, a);
+    if (th) { a.src = c.CTH; a.dst = c.TH; launch_c2r(c, a); }
+  }
+  launch_face_velocity(c);
+  // nonlinear and cross-diffusion terms, fused with their forward FFTs
+  // (duct.F90:683-1121)
+  {
+    R2cArgs a{};
+    a.j0 = d.JS; a.j1 = d.JE; a.k0 = d.ZS; a.k1 = d.ZE;
+    const double *uu[3] = {c.U1, c.U2, c.U3};
+    cplx_t *cf[3] = {c.CF1, c.CF2, c.CF3};
+    for (int f = 0; f < 3; ++f) {
+      a.pro = PRO_PROD; a.a = c.U1; a.b = uu[f]; a.epi = EPI_SUB_IK; a.dst = cf[f];
+      launch_r2c(c, a);
+      a.pro = PRO_FLUX; a.a = uu[f]; a.b = c.U2b; a.visc = p.nu; a.epi = EPI_ADD;
+      launch_r2c(c, a);
+    }
+  }
+  // R = c2r(CR + beta h CF) (duct.F90:1127-1161)
+  {
+    C2rArgs a{};
+    a.j0 = d.JS; a.j1 = d.JE; a.k0 = d.ZS; a.k1 = d.ZE;
+    a.scale2 = TEMP5;
+    a.src = c.CR1; a.src2 = c.CF1; a.dst = c.R1; launch_c2r(c, a);
+    a.src = c.CR2; a.src2 = c.CF2; a.dst = c.R2; launch_c2r(c, a);
+    a.src = c.CR3; a.src2 = c.CF3; a.dst = c.R3; launch_c2r(c, a);
+  }
+  if (th) {
+    // scalar nonlinear terms (duct.F90:1165-1252) and RTH (1304-1326)
+    R2cArgs a{};
+    a.j0 = d.JST; a.j1 = d.JET; a.k0 = d.ZST; a.k1 = d.ZET;
+    a.pro = PRO_PROD; a.a = c.TH; a.b = c.U1; a.epi = EPI_SUB_IK; a.dst = c.CFTH;
+    launch_r2c(c, a);
+    a.pro = PRO_FLUX; a.a = c.TH; a.b = c.U2b; a.visc = p.nu / p.pr; a.epi = EPI_ADD;
+    launch_r2c(c, a);
+    C2rArgs b{};
+    b.j0 = d.JST; b.j1 = d.JET; b.k0 = d.ZST; b.k1 = d.ZET;
+    b.scale2 = TEMP5; b.src = c.CRTH; b.src2 = c.CFTH; b.dst = c.RTH;
+    launch_c2r(c, b);
+    launch_adi(c, 0, rk);
+    launch_th_corners(c);
+  }
+  launch_adi(c, 1, rk);
+  launch_adi(c, 2, rk);
+  launch_adi(c, 3, rk);
+  // back to Fourier space (duct.F90:2421-2451)
+  {
+    R2cArgs a{};
+    a.j0 = 0; a.j1 = d.NY + 1; a.k0 = 0; a.k1 = d.NZ + 1;
+    a.pro = PRO_LOAD; a.epi = EPI_STORE;
+    a.a = c.U1; a.dst = c.CU1; launch_r2c(c, a);
+    a.a = c.U2; a.dst = c.CU2; launch_r2c(c, a);
+    a.a = c.U3; a.dst = c.CU3; launch_r2c(c, a);
+    if (th) { a.a = c.TH; a.dst = c.CTH; launch_r2c(c, a); }
+  }
+  int mg = EK_OK;
+  run_rem_div(c, TEMP4, true, &mg);
+  return finish_divergence(c, nullptr);
+}
+
+__global__ void k_transpose(const double *in, double *out, int P, long npt, int to_inner) {
+  const long n = (long)P * npt;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    if (to_inner) {  // in [p][pt] -> out [pt][p]
+      const int p = (int)(t % P);
+      const long pt = t / P;
+      out[t] = in[(size_t)p * npt + pt];
+    } else {         // in [pt][p] -> out [p][pt]
+      const long pt = t % npt;
+      const int p = (int)(t / npt);
+      out[t] = in[(size_t)pt * P + p];
+    }
+  }
+}
+
+}  // namespace
+
+namespace ek {
+// Sum the recorded per-kernel-class event pairs into kms/kcnt.
+void timing_resolve(Ctx &c) {
+  if (c.trec.empty()) return;
+  EK_CUDA(cudaStreamSynchronize(c.stream));
+  for (const TimerRec &r : c.trec) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    c.kms[r.cls] += ms;
+    c.kcnt[r.cls] += 1;
+    c.evpool.push_back(r.a);
+    c.evpool.push_back(r.b);
+  }
+  c.trec.clear();
+}
+}  // namespace ek
+
+namespace {
+
+int poisson_dev(Ctx &c, const double *rhs_dev, double *phi_dev, const double *kx2_dev, int nprob, ek_mg_stats *st) {
+  if (!c.have_metrics) return fail(c, EK_ERR_STATE, "metrics not set");
+  if (nprob <= 0) return fail(c, EK_ERR_ARG, "nprob must be positive");
+  if (nprob > c.mg_pmax) mg_alloc(c, nprob);
+  const long npt = (long)c.mg.nfx * c.mg.nfy;
+  MgLevel &F = c.mg.lv[c.mg.ngrid - 1];
+  long n = npt * nprob;
+  unsigned blocks = (unsigned)std::min<long>((n + 255) / 256, 65535L * 16);
+  k_transpose<<<blocks, 256, 0, c.stream>>>(rhs_dev, F.rhs, nprob, npt, 1);
+  after_launch(c);
+  const int r = mg_solve(c, nprob, kx2_dev, st);
+  k_transpose<<<blocks, 256, 0, c.stream>>>(c.mg_phif, phi_dev, nprob, npt, 0);
+  after_launch(c);
+  EK_CUDA(cudaStreamSynchronize(c.stream));
+  return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ekgpu_default_params(ek_params *p) {
+  if (!p) return EK_ERR_ARG;
+  std::memset(p, 0, sizeof(*p));
+  p->lx = 4.0 * M_PI;
+  p->nu = 1.0e-3;
+  p->delta_t = 1.0e-3;
+  p->f0 = 1.0e-4;
+  p->wbulk0 = 5.0e-2;
+  p->f_type = 1;
+  p->n_th = 1;
+  p->pr = 1.0;
+  p->ic_type = 7;
+  for (int *b : {p->u_bc, p->v_bc, p->w_bc, p->th_bc}) {
+    b[EK_YMIN] = 0; b[EK_YMAX] = 1; b[EK_ZMIN] = 6; b[EK_ZMAX] = 6;
+  }
+  p->mudpack_bc[0] = 0; p->mudpack_bc[1] = 0; p->mudpack_bc[2] = 2; p->mudpack_bc[3] = 2;
+  p->mg_maxcy = 6; p->mg_kcycle = 2; p->mg_iprer = 2; p->mg_ipost = 1; p->mg_intpol = 3;
+  p->mg_stop = EK_MG_STOP_RELCHANGE;
+  p->mg_tol = (double)powf(10.0f, -6.0f);
+  return EK_OK;
+}
+
+int ekgpu_create(const ek_params *pp, ek_ctx **out) {
+  if (!pp || !out) return EK_ERR_ARG;
+  *out = nullptr;
+  auto h = std::unique_ptr<ek_ctx>(new (std::nothrow) ek_ctx());
+  if (!h) return EK_ERR_ARG;
+  Ctx &c = h->c;
+  c.p = *pp;
+  const ek_params &p = c.p;
+  std::string why;
+  auto reject = [&](const std::string &m) {
+    c.err = m;
+    *out = h.release();
+    return (int)EK_ERR_ARG;
+  };
+  if (p.nx < 8 || p.nx > 1024 || (p.nx & (p.nx - 1))) return reject("NX must be a power of two in [8, 1024]");
+  if (p.ny < 4 || p.nz < 4) return reject("NY and NZ must be >= 4");
+  if (p.ic_type != 7) return reject("only IC_TYPE = 7 boundary rows are supported");
+  if (p.mudpack_bc[0] != 0 || p.mudpack_bc[1] != 0 || p.mudpack_bc[2] != 2 || p.mudpack_bc[3] != 2)
+    return reject("only MUDPACK_BC = 0 0 2 2 is supported");
+  if (p.sponge_type != 0) return reject("SPONGE_TYPE must be 0");
+  if (p.les != 0) return reject("LES is not supported");
+  if (p.f_type != 1 && p.f_type != 2) return reject("F_TYPE must be 1 or 2");
+  if (p.n_th < 0 || p.n_th > 1) return reject("N_TH must be 0 or 1");
+  if (p.mg_kcycle < 1 || p.mg_iprer < 1 || p.mg_ipost < 1 || (p.mg_intpol != 1 && p.mg_intpol != 3) || p.mg_maxcy < 1)
+    return reject("bad multigrid options");
+  if (p.mg_stop != EK_MG_STOP_RELCHANGE && p.mg_stop != EK_MG_STOP_RESIDUAL) return reject("bad mg_stop");
+  if (!supported_bc(p, why)) return reject(why);
+  MgPlan &P = c.mg;
+  if (p.mg_ixp > 0) {
+    P.ixp = p.mg_ixp; P.jyq = p.mg_jyq; P.iex = p.mg_iex; P.jey = p.mg_jey;
+  } else if (!mg_pick_shape(p.nz + 2, P.ixp, P.iex) || !mg_pick_shape(p.ny + 2, P.jyq, P.jey)) {
+    return reject("NZ+2 and NY+2 must have the form p*2^k+1 (MUDPACK)");
+  }
+  if (P.ixp < 2 || P.jyq < 2 || P.ixp * (1 << (P.iex - 1)) + 1 != p.nz + 2 || P.jyq * (1 << (P.jey - 1)) + 1 != p.ny + 2)
+    return reject("Mudpack Multigrid Parameters are not Matching Grid Dimensions.");
+  try {
+    EK_CUDA(cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking));
+    c.stream = c.own_stream;
+    rk_init_attributes();
+    fft_init_attributes();
+    Dims &d = c.d;
+    d.NX = p.nx; d.NY = p.ny; d.NZ = p.nz;
+    d.NKX = p.nx / 3; d.NX2P = p.nx / 2;
+    d.LDX = p.nx + 2; d.LDC = p.nx / 2 + 1;
+    d.NZ2 = p.nz + 2; d.NY2 = p.ny + 2; d.LDM = p.nz + 3;
+    // INIT_DUCT (duct.F90:7-232), IC_TYPE = 7 branches
+    const int *ub = p.u_bc, *wb = p.w_bc, *tb = p.th_bc;
+    d.JS = (wb[EK_YMIN] == 0 || wb[EK_YMIN] == 1 || wb[EK_YMIN] == 6) ? 1 : 2;
+    d.ZS = (ub[EK_ZMIN] == 1 || ub[EK_ZMIN] == 6) ? 1 : 2;
+    d.JE = (wb[EK_YMAX] == 0 || wb[EK_YMAX] == 1 || wb[EK_YMAX] == 6) ? p.ny : p.ny - 1;
+    d.ZE = (ub[EK_ZMAX] == 0 || ub[EK_ZMAX] == 1 || ub[EK_ZMAX] == 6) ? p.nz : p.nz - 1;
+    d.JST = (tb[EK_YMIN] == 0 || tb[EK_YMIN] == 1 || tb[EK_YMIN] == 5 || tb[EK_YMIN] == 6) ? 1 : 2;
+    d.ZST = (tb[EK_ZMIN] == 0 || tb[EK_ZMIN] == 1 || tb[EK_ZMIN] == 6) ? 1 : 2;
+    d.JET = (tb[EK_YMAX] == 0 || tb[EK_YMAX] == 1 || tb[EK_YMAX] == 6) ? p.ny : p.ny - 1;
+    d.ZET = (tb[EK_ZMAX] == 0 || tb[EK_ZMAX] == 1 || tb[EK_ZMAX] == 6) ? p.nz : p.nz - 1;
+    // RKW3 (diablo.F90:568-576)
+    const double dt = p.delta_t;
+    c.H_BAR[1] = dt * (8.0 / 15.0); c.H_BAR[2] = dt * (2.0 / 15.0); c.H_BAR[3] = dt * (5.0 / 15.0);
+    c.BETA_BAR[1] = 1.0; c.BETA_BAR[2] = 25.0 / 8.0; c.BETA_BAR[3] = 9.0 / 4.0;
+    c.ZETA_BAR[1] = 0.0; c.ZETA_BAR[2] = -17.0 / 8.0; c.ZETA_BAR[3] = -5.0 / 4.0;
+    // wavenumbers KX = 2 pi i / LX, KX2 = KX^2
+    c.kx_h.resize(d.NX2P + 1);
+    c.kx2_h.resize(d.NX2P + 1);
+    for (int i = 0; i <= d.NX2P; ++i) {
+      c.kx_h[i] = i * (2.0 * M_PI) / p.lx;
+      c.kx2_h[i] = c.kx_h[i] * c.kx_h[i];
+    }
+    c.kx = dalloc<double>(c, d.NX2P + 1);
+    c.kx2 = dalloc<double>(c, d.NX2P + 1);
+    EK_CUDA(cudaMemcpy(c.kx, c.kx_h.data(), sizeof(double) * (d.NX2P + 1), cudaMemcpyHostToDevice));
+    EK_CUDA(cudaMemcpy(c.kx2, c.kx2_h.data(), sizeof(double) * (d.NX2P + 1), cudaMemcpyHostToDevice));
+    // twiddles
+    const int M = d.NX / 2;
+    std::vector<double2> twm(M / 2 > 0 ? M / 2 : 1), twn(M + 1);
+    for (int t = 0; t < M / 2; ++t) twm[t] = make_double2(cos(-2.0 * M_PI * t / M), sin(-2.0 * M_PI * t / M));
+    for (int k = 0; k <= M; ++k) twn[k] = make_double2(cos(-2.0 * M_PI * k / d.NX), sin(-2.0 * M_PI * k / d.NX));
+    c.tw_m = dalloc<double2>(c, twm.size());
+    c.tw_n = dalloc<double2>(c, twn.size());
+    EK_CUDA(cudaMemcpy(c.tw_m, twm.data(), sizeof(double2) * twm.size(), cudaMemcpyHostToDevice));
+    EK_CUDA(cudaMemcpy(c.tw_n, twn.data(), sizeof(double2) * twn.size(), cudaMemcpyHostToDevice));
+    // fields
+    const size_t nc = d.nspec(), np = d.nphys();
+    for (cplx_t **f : {&c.CU1, &c.CU2, &c.CU3, &c.CP, &c.CTH, &c.CF1, &c.CF2, &c.CF3, &c.CFTH, &c.CR1, &c.CR2, &c.CR3,
+                       &c.CRTH, &c.CS})
+      *f = dalloc<cplx_t>(c, nc);
+    c.CU2b = dalloc<cplx_t>(c, 2 * nc);
+    c.CU3b = c.CU2b + nc;
+    for (double **f : {&c.U1, &c.U2, &c.U3, &c.TH, &c.R1, &c.R2, &c.R3, &c.RTH, &c.PHS, &c.SPH}) *f = dalloc<double>(c, np);
+    c.U2b = dalloc<double>(c, 2 * np);
+    c.U3b = c.U2b + np;
+    c.div_part = dalloc<double>(c, d.NY2);
+    EK_CUDA(cudaStreamSynchronize(c.stream));
+  } catch (const CudaError &e) {
+    c.err = e.msg;
+    *out = h.release();
+    return EK_ERR_CUDA;
+  }
+  *out = h.release();
+  return EK_OK;
+}
+
+void ekgpu_destroy(ek_ctx *h) {
+  if (!h) return;
+  Ctx &c = h->c;
+  if (c.stream) cudaStreamSynchronize(c.stream);
+  for (void *p : c.allocs) cudaFree(p);
+  if (c.mg_pool) cudaFree(c.mg_pool);
+  if (c.mg_done) cudaFree(c.mg_done);
+  if (c.mg.ops_dev) cudaFree(c.mg.ops_dev);
+  for (auto &r : c.trec) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+  for (auto e : c.evpool) cudaEventDestroy(e);
+  if (c.own_stream) cudaStreamDestroy(c.own_stream);
+  delete h;
+}
+
+const char *ekgpu_last_error(const ek_ctx *h) { return h ? h->c.err.c_str() : "null context"; }
+
+int ekgpu_set_stream(ek_ctx *h, void *stream) {
+  return guarded(h, [&](Ctx &c) {
+    EK_CUDA(cudaStreamSynchronize(c.stream));
+    c.stream = stream ? static_cast<cudaStream_t>(stream) : c.own_stream;
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_metrics_from_grid(const ek_params *p, const double *xpoint, const double *ypoint, double *int_jacob,
+                            double *gmat_11, double *gmat_12, double *gmat_22, double *cjob_11, double *cjob_12,
+                            double *cjob_21, double *cjob_22, double *th_bar) {
+  if (!p || !int_jacob || !gmat_11 || !gmat_12 || !gmat_22 || !cjob_11 || !cjob_12 || !cjob_21 || !cjob_22)
+    return EK_ERR_ARG;
+  return metrics_from_grid_host(p, xpoint, ypoint, int_jacob, gmat_11, gmat_12, gmat_22, cjob_11, cjob_12, cjob_21,
+                                cjob_22, th_bar);
+}
+
+int ekgpu_set_metrics(ek_ctx *h, const ek_metrics *m) {
+  return guarded(h, [&](Ctx &c) {
+    if (!m || !m->int_jacob || !m->gmat_11 || !m->gmat_12 || !m->gmat_22 || !m->cjob_11 || !m->cjob_12 ||
+        !m->cjob_21 || !m->cjob_22)
+      return fail(c, EK_ERR_ARG, "metric pointer is NULL");
+    if (c.p.n_th > 0 && !c.p.cont_strat && !m->th_bar) return fail(c, EK_ERR_ARG, "th_bar is required");
+    const Dims &d = c.d;
+    const size_t n2 = (size_t)d.LDM * (d.NY + 3);
+    auto up = [&](double *&dst, const double *src, size_t n) {
+      if (!dst) dst = dalloc<double>(c, n);
+      if (src) EK_CUDA(cudaMemcpy(dst, src, n * sizeof(double), cudaMemcpyHostToDevice));
+      else EK_CUDA(cudaMemset(dst, 0, n * sizeof(double)));
+    };
+    up(c.m.jac, m->int_jacob, n2);
+    up(c.m.g11, m->gmat_11, 2 * n2); up(c.m.g12, m->gmat_12, 2 * n2); up(c.m.g22, m->gmat_22, 2 * n2);
+    up(c.m.c11, m->cjob_11, 2 * n2); up(c.m.c12, m->cjob_12, 2 * n2);
+    up(c.m.c21, m->cjob_21, 2 * n2); up(c.m.c22, m->cjob_22, 2 * n2);
+    up(c.m.thbar, m->th_bar, n2);
+    std::vector<double> jac(m->int_jacob, m->int_jacob + n2), g11(m->gmat_11, m->gmat_11 + 2 * n2),
+        g12(m->gmat_12, m->gmat_12 + 2 * n2), g22(m->gmat_22, m->gmat_22 + 2 * n2), c22(m->cjob_22, m->cjob_22 + 2 * n2);
+    // boundary rows and Thomas factors of every field, substep and direction
+    std::vector<double> w;
+    if (build_bc_sets(c, w, jac, c22) != EK_OK) return fail(c, EK_ERR_ARG, "unsupported boundary condition");
+    if (!w.empty()) {
+      if (c.bc_weights == nullptr) c.bc_weights = dalloc<double>(c, w.size());
+      EK_CUDA(cudaMemcpy(c.bc_weights, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice));
+    }
+    for (int f = 0; f < 4; ++f)
+      for (int rk = 1; rk <= 3; ++rk)
+        for (int dir = 0; dir < 2; ++dir) {
+          std::vector<double> a, ib, u;
+          adi_factor_host(c, f, rk, dir, jac, g11, g22, a, ib, u);
+          AdiFactors &F = c.adi[f][rk][dir];
+          if (!F.a) {
+            F.a = dalloc<double>(c, a.size());
+            F.ib = dalloc<double>(c, ib.size());
+            F.u = dalloc<double>(c, u.size());
+          }
+          EK_CUDA(cudaMemcpy(F.a, a.data(), sizeof(double) * a.size(), cudaMemcpyHostToDevice));
+          EK_CUDA(cudaMemcpy(F.ib, ib.data(), sizeof(double) * ib.size(), cudaMemcpyHostToDevice));
+          EK_CUDA(cudaMemcpy(F.u, u.data(), sizeof(double) * u.size(), cudaMemcpyHostToDevice));
+        }
+    // multigrid plan
+    MgPlan &P = c.mg;
+    mg_build_plan_host(c, jac, g11, g12, g22);
+    mg_build_schedule(P, c.p.mg_kcycle, c.p.mg_iprer, c.p.mg_ipost, c.p.mg_maxcy);
+    const int ncof = P.orth ? 4 : 8;
+    P.lc = 1;
+    for (int l = 1; l <= P.ngrid; ++l) {
+      size_t tot = 0, maxph = 0;
+      for (int k = 1; k <= l; ++k) {
+        const MgLevel &L = P.lv[k - 1];
+        tot += (size_t)(L.nx + 2) * (L.ny + 2) + (size_t)(2 + ncof) * L.nx * L.ny;
+        maxph = std::max(maxph, (size_t)(L.nx + 2) * (L.ny + 2));
+      }
+      if ((tot + maxph) * sizeof(double) <= 96 * 1024) P.lc = l;
+    }
+    const int pmax = std::max(c.mg_pmax, d.NX + 2);
+    mg_alloc(c, pmax);
+    c.have_metrics = true;
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_upload_state(ek_ctx *h, const double *cu1, const double *cu2, const double *cu3, const double *cp,
+                       const double *cth) {
+  return guarded(h, [&](Ctx &c) {
+    if (!cu1 || !cu2 || !cu3 || !cp || (c.p.n_th > 0 && !cth)) return fail(c, EK_ERR_ARG, "state pointer is NULL");
+    const size_t bytes = c.d.nspec() * sizeof(cplx_t);
+    EK_CUDA(cudaMemcpyAsync(c.CU1, cu1, bytes, cudaMemcpyHostToDevice, c.stream));
+    EK_CUDA(cudaMemcpyAsync(c.CU2, cu2, bytes, cudaMemcpyHostToDevice, c.stream));
+    EK_CUDA(cudaMemcpyAsync(c.CU3, cu3, bytes, cudaMemcpyHostToDevice, c.stream));
+    EK_CUDA(cudaMemcpyAsync(c.CP, cp, bytes, cudaMemcpyHostToDevice, c.stream));
+    if (cth) EK_CUDA(cudaMemcpyAsync(c.CTH, cth, bytes, cudaMemcpyHostToDevice, c.stream));
+    for (cplx_t *f : {c.CF1, c.CF2, c.CF3, c.CFTH}) EK_CUDA(cudaMemsetAsync(f, 0, bytes, c.stream));
+    EK_CUDA(cudaStreamSynchronize(c.stream));
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_download_state(ek_ctx *h, double *cu1, double *cu2, double *cu3, double *cp, double *cth) {
+  return guarded(h, [&](Ctx &c) {
+    const size_t bytes = c.d.nspec() * sizeof(cplx_t);
+    if (cu1) EK_CUDA(cudaMemcpyAsync(cu1, c.CU1, bytes, cudaMemcpyDeviceToHost, c.stream));
+    if (cu2) EK_CUDA(cudaMemcpyAsync(cu2, c.CU2, bytes, cudaMemcpyDeviceToHost, c.stream));
+    if (cu3) EK_CUDA(cudaMemcpyAsync(cu3, c.CU3, bytes, cudaMemcpyDeviceToHost, c.stream));
+    if (cp) EK_CUDA(cudaMemcpyAsync(cp, c.CP, bytes, cudaMemcpyDeviceToHost, c.stream));
+    if (cth) EK_CUDA(cudaMemcpyAsync(cth, c.CTH, bytes, cudaMemcpyDeviceToHost, c.stream));
+    EK_CUDA(cudaStreamSynchronize(c.stream));
+    return (int)EK_OK;
+  });
+}
+
+static cplx_t *field_of(Ctx &c, int f) {
+  switch (f) {
+    case EK_F_CU1: return c.CU1; case EK_F_CU2: return c.CU2; case EK_F_CU3: return c.CU3;
+    case EK_F_CP: return c.CP; case EK_F_CTH: return c.CTH; case EK_F_CF1: return c.CF1;
+    case EK_F_CF2: return c.CF2; case EK_F_CF3: return c.CF3; case EK_F_CFTH: return c.CFTH;
+    case EK_F_CR1: return c.CR1;
+    default: return nullptr;
+  }
+}
+
+int ekgpu_get_field(ek_ctx *h, int f, double *out) {
+  return guarded(h, [&](Ctx &c) {
+    cplx_t *src = field_of(c, f);
+    if (!src || !out) return fail(c, EK_ERR_ARG, "bad field");
+    EK_CUDA(cudaMemcpyAsync(out, src, c.d.nspec() * sizeof(cplx_t), cudaMemcpyDeviceToHost, c.stream));
+    EK_CUDA(cudaStreamSynchronize(c.stream));
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_put_field(ek_ctx *h, int f, const double *in) {
+  return guarded(h, [&](Ctx &c) {
+    cplx_t *dst = field_of(c, f);
+    if (!dst || !in) return fail(c, EK_ERR_ARG, "bad field");
+    EK_CUDA(cudaMemcpyAsync(dst, in, c.d.nspec() * sizeof(cplx_t), cudaMemcpyHostToDevice, c.stream));
+    EK_CUDA(cudaStreamSynchronize(c.stream));
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_rk_substep(ek_ctx *h, int rk) {
+  return guarded(h, [&](Ctx &c) {
+    if (!c.have_metrics) return fail(c, EK_ERR_STATE, "metrics not set");
+    if (rk < 1 || rk > 3) return fail(c, EK_ERR_ARG, "rk_step must be 1, 2 or 3");
+    const int st = substep(c, rk);
+    if (st == EK_ERR_NAN) return fail(c, EK_ERR_NAN, "DIV is a NaN");
+    return st;
+  });
+}
+
+int ekgpu_step(ek_ctx *h, int nsteps) {
+  return guarded(h, [&](Ctx &c) {
+    if (!c.have_metrics) return fail(c, EK_ERR_STATE, "metrics not set");
+    if (nsteps < 0) return fail(c, EK_ERR_ARG, "nsteps must be >= 0");
+    for (int n = 0; n < nsteps; ++n) {
+      for (int rk = 1; rk <= 3; ++rk) {
+        const int st = substep(c, rk);
+        if (st == EK_ERR_NAN) return fail(c, EK_ERR_NAN, "DIV is a NaN");
+        if (st != EK_OK) return st;
+      }
+      c.p.time += c.p.delta_t;
+    }
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_rem_div(ek_ctx *h) {
+  return guarded(h, [&](Ctx &c) {
+    if (!c.have_metrics) return fail(c, EK_ERR_STATE, "metrics not set");
+    int mg = EK_OK;
+    run_rem_div(c, 1.0, false, &mg);
+    const int st = finish_divergence(c, nullptr);
+    if (st == EK_ERR_NAN) return fail(c, EK_ERR_NAN, "DIV is a NaN");
+    return st;
+  });
+}
+
+int ekgpu_poisson_batch(ek_ctx *h, const double *rhs, double *phi, const double *kx2, int nprob, ek_mg_stats *stats) {
+  return guarded(h, [&](Ctx &c) {
+    if (!rhs || !phi || !kx2 || nprob <= 0) return fail(c, EK_ERR_ARG, "bad poisson arguments");
+    const size_t n = (size_t)c.mg.nfx * c.mg.nfy * nprob;
+    double *buf = nullptr;
+    EK_CUDA(cudaMalloc(&buf, sizeof(double) * (2 * n + nprob)));
+    int r = EK_OK;
+    try {
+      EK_CUDA(cudaMemcpyAsync(buf, rhs, sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
+      EK_CUDA(cudaMemcpyAsync(buf + 2 * n, kx2, sizeof(double) * nprob, cudaMemcpyHostToDevice, c.stream));
+      r = poisson_dev(c, buf, buf + n, buf + 2 * n, nprob, stats);
+      EK_CUDA(cudaMemcpyAsync(phi, buf + n, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream));
+      EK_CUDA(cudaStreamSynchronize(c.stream));
+    } catch (...) {
+      cudaFree(buf);
+      throw;
+    }
+    cudaFree(buf);
+    return r;
+  });
+}
+
+int ekgpu_poisson_batch_device(ek_ctx *h, const double *rhs_dev, double *phi_dev, const double *kx2_dev, int nprob,
+                               ek_mg_stats *stats) {
+  return guarded(h, [&](Ctx &c) {
+    if (!rhs_dev || !phi_dev || !kx2_dev || nprob <= 0) return fail(c, EK_ERR_ARG, "bad poisson arguments");
+    return poisson_dev(c, rhs_dev, phi_dev, kx2_dev, nprob, stats);
+  });
+}
+
+int ekgpu_last_divergence(ek_ctx *h, double *div) {
+  return guarded(h, [&](Ctx &c) {
+    if (!div) return fail(c, EK_ERR_ARG, "div is NULL");
+    *div = c.last_div;
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_last_mg_stats(ek_ctx *h, ek_mg_stats *s) {
+  return guarded(h, [&](Ctx &c) {
+    if (!s) return fail(c, EK_ERR_ARG, "stats is NULL");
+    *s = c.last_stats;
+    return (int)EK_OK;
+  });
+}
+
+long long ekgpu_launch_count(const ek_ctx *h) { return h ? h->c.launches : -1; }
+
+static const char *kKClassNames[KC_N] = {"spectral_rhs", "fft_c2r", "fft_r2c", "face_velocity", "adi_y", "adi_z",
+                                         "mg_relax", "mg_coarse", "mg_transfer", "mg_check", "mg_setup",
+                                         "projection", "divergence"};
+
+const char *ekgpu_timing_class_name(int k) { return (k >= 0 && k < KC_N) ? kKClassNames[k] : ""; }
+
+int ekgpu_set_timing(ek_ctx *h, int on) {
+  return guarded(h, [&](Ctx &c) {
+    timing_resolve(c);
+    for (int k = 0; k < KC_N; ++k) { c.kms[k] = 0.0; c.kcnt[k] = 0; }
+    c.timing = on != 0;
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_get_timing(ek_ctx *h, double *ms, long long *count, int n) {
+  return guarded(h, [&](Ctx &c) {
+    timing_resolve(c);
+    for (int k = 0; k < n && k < KC_N; ++k) {
+      if (ms) ms[k] = c.kms[k];
+      if (count) count[k] = c.kcnt[k];
+    }
+    return (int)KC_N;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,234 @@
+// Batched x-direction real FFTs of the duct substep, FP64.
+//
+// The reference transforms every field line along x through
+// REAL_FOURIER_TRANS_* (src/mpi_duct.F90:271-717) and the missing
+// FFT_X_TO_FOURIER_OP / FFT_X_TO_PHYSICAL_OP (FFTW 2 rfftw).  Here one warp
+// owns one x-line: a length-NX real transform is done as a length-NX/2
+// complex radix-2 DIF FFT in shared memory plus the split/merge twiddle
+// step.  Forward transforms keep modes 0..NX/3 and scale by 1/NX; the
+// inverse reads modes 0..NX/3 (imaginary part of mode 0 ignored) and zeroes
+// the two padding points x = NX, NX+1, as the reference's copy loops do.
+//
+// The forward kernel fuses its producer and consumer:
+//   prologue PRO_LOAD  x = a
+//            PRO_PROD  x = J a b            (duct.F90:685-691 products)
+//            PRO_FLUX  x = flux stencil of a (duct.F90:735-761 form)
+//   epilogue EPI_STORE dst  = X            (modes > NX/3 set to 0)
+//            EPI_ADD   dst += X            (duct.F90:779-785)
+//            EPI_SUB_IK dst -= i kx X      (duct.F90:712-718)
+// so no product or transform temporary ever reaches HBM.
+#include "ek_internal.h"
+
+namespace ek {
+
+namespace {
+
+constexpr int kWarpsPerBlock = 4;
+
+struct FftConst {
+  Dims d;
+  int M, logM;
+  const double2 *tw_m, *tw_n;
+  const double *kx;
+  Metrics m;
+};
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__device__ __forceinline__ unsigned brev(unsigned v, int logM) { return __brev(v) >> (32 - logM); }
+
+// In-place radix-2 DIF over z[0..M), bit-reversed output.  conj_tw selects
+// the inverse transform.
+__device__ __forceinline__ void dif_fft(double2 *z, int M, const double2 *tw, bool conj_tw, int lane) {
+  for (int s = M >> 1; s >= 1; s >>= 1) {
+    const int stride = (M >> 1) / s;  // twiddle step M/(2s)
+    for (int q = lane; q < (M >> 1); q += 32) {
+      const int t = q & (s - 1);
+      const int a = ((q - t) << 1) + t;
+      const int b = a + s;
+      const double2 u = z[a], v = z[b];
+      z[a] = make_double2(u.x + v.x, u.y + v.y);
+      double2 dlt = make_double2(u.x - v.x, u.y - v.y);
+      if (t != 0) {
+        double2 w = tw[t * stride];
+        if (conj_tw) w.y = -w.y;
+        dlt = cmul(dlt, w);
+      }
+      z[b] = dlt;
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArgs args) {
+  extern __shared__ double2 smem_c[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const Dims &d = fc.d;
+  const int nk = args.k1 - args.k0 + 1;
+  const long nlines = (long)nk * (args.j1 - args.j0 + 1);
+  const long line = (long)blockIdx.x * kWarpsPerBlock + warp;
+  if (line >= nlines) return;
+  const int k = args.k0 + (int)(line % nk);
+  const int j = args.j0 + (int)(line / nk);
+  const int NX = d.NX, M = fc.M;
+  double2 *z = smem_c + (size_t)warp * M;
+  double *zr = reinterpret_cast<double *>(z);
+  const size_t base = d.ip(0, k, j);
+  if (args.pro == PRO_LOAD) {
+    for (int n = lane; n < NX; n += 32) zr[n] = args.a[base + n];
+  } else if (args.pro == PRO_PROD) {
+    const double jac = fc.m.jac[d.m2(k, j)];
+    for (int n = lane; n < NX; n += 32) zr[n] = jac * args.a[base + n] * args.b[base + n];
+  } else {
+    // flux form of the eta/zeta convection plus the GMAT_12 cross diffusion
+    // (duct.F90:735-761; the TH version at 1210-1241 has visc = NU/PR)
+    const double *F = args.a;
+    const double *U2b = args.b;  // U2b, followed in memory by U3b (see launch)
+    const double *U3b = args.b + d.nphys();
+    const double g12a = fc.m.g12[d.m3(k + 1, j, 2)], g12b = fc.m.g12[d.m3(k, j, 2)];
+    const double g12c = fc.m.g12[d.m3(k, j + 1, 1)], g12d = fc.m.g12[d.m3(k, j, 1)];
+    const double qv = 0.25 * args.visc;
+    const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
+    for (int n = lane; n < NX; n += 32) {
+      const size_t c = base + n;
+      const double f = F[c], fkp = F[c + sK], fkm = F[c - sK], fjp = F[c + sJ], fjm = F[c - sJ];
+      const double fpp = F[c + sK + sJ], fpm = F[c + sK - sJ], fmp = F[c - sK + sJ], fmm = F[c - sK - sJ];
+      double s1 = 0.5 * U2b[c + sJ] * (f + fjp) - 0.5 * U2b[c] * (f + fjm);
+      double s2 = 0.5 * U3b[c + sK] * (f + fkp) - 0.5 * U3b[c] * (f + fkm);
+      s1 = -s1 + qv * (g12a * (fpp + fjp - fjm - fpm) - g12b * (fmp + fjp - fjm - fmm));
+      s2 = -s2 + qv * (g12c * (fpp + fkp - fmp - fkm) - g12d * (fkp + fpm - fkm - fmm));
+      zr[n] = s1 + s2;
+    }
+  }
+  __syncwarp();
+  dif_fft(z, M, fc.tw_m, false, lane);
+  // split: X[k] = E + W^k O, E = (Z_k + conj Z_{M-k})/2, O = -i (Z_k - conj Z_{M-k})/2
+  cplx_t *dst = args.dst + d.ic(0, k, j);
+  const double inv = 1.0 / NX;
+  const int NKX = d.NKX;
+  for (int kk = lane; kk <= d.NX2P; kk += 32) {
+    if (kk > NKX) {
+      if (args.epi == EPI_STORE) dst[kk] = cplx_t{0.0, 0.0};
+      continue;
+    }
+    const double2 zk = z[brev(kk & (M - 1), fc.logM)];
+    const double2 zm = z[brev((M - kk) & (M - 1), fc.logM)];
+    const double er = 0.5 * (zk.x + zm.x), ei = 0.5 * (zk.y - zm.y);
+    const double orr = 0.5 * (zk.y + zm.y), oi = -0.5 * (zk.x - zm.x);
+    const double2 w = fc.tw_n[kk];
+    const double xr = (er + (w.x * orr - w.y * oi)) * inv;
+    const double xi = (ei + (w.x * oi + w.y * orr)) * inv;
+    if (args.epi == EPI_STORE) {
+      dst[kk] = cplx_t{xr, xi};
+    } else if (args.epi == EPI_ADD) {
+      const cplx_t o = dst[kk];
+      dst[kk] = cplx_t{o.re + xr, o.im + xi};
+    } else {
+      // CF = CF - CIKXP*CS with CIKXP = (0, kx)
+      const double kv = fc.kx[kk];
+      const cplx_t o = dst[kk];
+      dst[kk] = cplx_t{o.re - (0.0 * xr - kv * xi), o.im - (0.0 * xi + kv * xr)};
+    }
+  }
+}
+
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArgs args) {
+  extern __shared__ double2 smem_c[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const Dims &d = fc.d;
+  const int nk = args.k1 - args.k0 + 1;
+  const long nlines = (long)nk * (args.j1 - args.j0 + 1);
+  const long line = (long)blockIdx.x * kWarpsPerBlock + warp;
+  if (line >= nlines) return;
+  const int k = args.k0 + (int)(line % nk);
+  const int j = args.j0 + (int)(line / nk);
+  const int M = fc.M, NKX = d.NKX;
+  double2 *z = smem_c + (size_t)warp * M;
+  const cplx_t *src = args.src + d.ic(0, k, j);
+  const cplx_t *src2 = args.src2 ? args.src2 + d.ic(0, k, j) : nullptr;
+  auto X = [&](int kk) -> double2 {
+    if (kk > NKX || kk >= M) return make_double2(0.0, 0.0);
+    cplx_t v = src[kk];
+    if (src2) {
+      const cplx_t w = src2[kk];
+      v.re = v.re + args.scale2 * w.re;
+      v.im = v.im + args.scale2 * w.im;
+    }
+    if (kk == 0) v.im = 0.0;
+    return make_double2(v.re, v.im);
+  };
+  // merge: Z'[k] = (X_k + conj X_{M-k}) + i (X_k - conj X_{M-k}) W^{-k}
+  for (int kk = lane; kk < M; kk += 32) {
+    const double2 a = X(kk), b = X(M - kk);
+    const double sr = a.x + b.x, si = a.y - b.y;  // X_k + conj X_{M-k}
+    const double dr = a.x - b.x, di = a.y + b.y;  // X_k - conj X_{M-k}
+    const double2 w = fc.tw_n[kk];              // conj taken below
+    const double tr = dr * w.x + di * w.y, ti = di * w.x - dr * w.y;  // (d)*conj(w)
+    z[kk] = make_double2(sr - ti, si + tr);     // + i*t
+  }
+  __syncwarp();
+  dif_fft(z, M, fc.tw_m, true, lane);
+  const double *zr = reinterpret_cast<const double *>(z);
+  double *dst = args.dst + d.ip(0, k, j);
+  const int NX = d.NX;
+  for (int n = lane; n < NX + 2; n += 32) {
+    double v = 0.0;
+    if (n < NX) {
+      const int m = n >> 1;
+      v = zr[2 * brev(m, fc.logM) + (n & 1)];
+    }
+    dst[n] = v;
+  }
+}
+
+FftConst make_const(Ctx &c) {
+  FftConst f;
+  f.d = c.d;
+  f.M = c.d.NX / 2;
+  int lg = 0;
+  while ((1 << lg) < f.M) ++lg;
+  f.logM = lg;
+  f.tw_m = c.tw_m;
+  f.tw_n = c.tw_n;
+  f.kx = c.kx;
+  f.m = c.m;
+  return f;
+}
+
+}  // namespace
+
+void launch_r2c(Ctx &c, const R2cArgs &a) {
+  const FftConst fc = make_const(c);
+  const long nlines = (long)(a.k1 - a.k0 + 1) * (a.j1 - a.j0 + 1);
+  if (nlines <= 0) return;
+  const unsigned grid = (unsigned)((nlines + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  const size_t smem = sizeof(double2) * fc.M * kWarpsPerBlock;
+  KScope ks(c, KC_R2C);
+  k_r2c<<<grid, 32 * kWarpsPerBlock, smem, c.stream>>>(fc, a);
+  after_launch(c);
+}
+
+void launch_c2r(Ctx &c, const C2rArgs &a) {
+  const FftConst fc = make_const(c);
+  const long nlines = (long)(a.k1 - a.k0 + 1) * (a.j1 - a.j0 + 1);
+  if (nlines <= 0) return;
+  const unsigned grid = (unsigned)((nlines + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  const size_t smem = sizeof(double2) * fc.M * kWarpsPerBlock;
+  KScope ks(c, KC_C2R);
+  k_c2r<<<grid, 32 * kWarpsPerBlock, smem, c.stream>>>(fc, a);
+  after_launch(c);
+}
+
+}  // namespace ek
+
+namespace ek {
+void fft_init_attributes() {
+  static bool done = false;
+  if (done) return;
+  EK_CUDA(cudaFuncSetAttribute(k_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+  EK_CUDA(cudaFuncSetAttribute(k_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+  done = true;
+}
+}  // namespace ek

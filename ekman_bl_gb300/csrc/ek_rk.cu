@@ -1,0 +1,562 @@
+// RK substep kernels of the GB300 duct path, FP64: the fused spectral
+// right-hand side, contravariant face velocities, the CN-ADI line solves
+// and the REM_DIV_CURV divergence / projection stencils.  Each kernel cites
+// the loop nests of src/duct.F90 it replaces.
+#include "ek_internal.h"
+
+namespace ek {
+
+namespace {
+
+__device__ __forceinline__ cplx_t cadd(cplx_t a, cplx_t b) { return {a.re + b.re, a.im + b.im}; }
+__device__ __forceinline__ cplx_t csub(cplx_t a, cplx_t b) { return {a.re - b.re, a.im - b.im}; }
+__device__ __forceinline__ cplx_t cscl(double s, cplx_t a) { return {s * a.re, s * a.im}; }
+__device__ __forceinline__ cplx_t cmul(cplx_t a, cplx_t b) {
+  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+
+struct SpecArgs {
+  Dims d;
+  Metrics m;
+  const double *kx, *kx2;
+  cplx_t *CU1, *CU2, *CU3, *CP, *CTH, *CF1, *CF2, *CF3, *CFTH, *CR1, *CR2, *CR3, *CRTH;
+  double nu, nupr, T3, T4, px, f0, ubc_top, wbulk0, ri;
+  int rk, th, cont_strat, forcing;
+};
+
+// Spectral explicit RHS: duct.F90:299-409 (CR = J CU + zeta h CF_prev, the
+// curvilinear pressure gradient), 411-455 (mean forcing, mode 0),
+// 461-523 (viscous x term, Coriolis on every kx, buoyancy) and 540-633
+// (scalar RHS with the background stratification term).
+__global__ void k_spectral_rhs(SpecArgs a) {
+  const Dims &d = a.d;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y, j = blockIdx.z;
+  if (i > d.NX2P) return;
+  const size_t q = d.ic(i, k, j);
+  const double jac = a.m.jac[d.m2(k, j)];
+  const bool vel = (j >= d.JS && j <= d.JE && k >= d.ZS && k <= d.ZE);
+  const bool sca = a.th && (j >= d.JST && j <= d.JET && k >= d.ZST && k <= d.ZET);
+  if (vel) {
+    const cplx_t cu1 = a.CU1[q], cu2 = a.CU2[q], cu3 = a.CU3[q];
+    cplx_t r1 = cscl(jac, cu1), r2 = cscl(jac, cu2), r3 = cscl(jac, cu3);
+    if (a.rk > 1) {
+      r1 = cadd(r1, cscl(a.T3, a.CF1[q]));
+      r2 = cadd(r2, cscl(a.T3, a.CF2[q]));
+      r3 = cadd(r3, cscl(a.T3, a.CF3[q]));
+    }
+    const cplx_t *CP = a.CP;
+    const cplx_t p0 = CP[q];
+    const cplx_t pkp = CP[d.ic(i, k + 1, j)], pkm = CP[d.ic(i, k - 1, j)];
+    const cplx_t pjp = CP[d.ic(i, k, j + 1)], pjm = CP[d.ic(i, k, j - 1)];
+    const cplx_t cs1 = csub(cadd(csub(cscl(0.5 * a.m.c11[d.m3(k + 1, j, 2)], cadd(p0, pkp)),
+                                      cscl(0.5 * a.m.c11[d.m3(k, j, 2)], cadd(p0, pkm))),
+                                 cscl(0.5 * a.m.c21[d.m3(k, j + 1, 1)], cadd(p0, pjp))),
+                            cscl(0.5 * a.m.c21[d.m3(k, j, 1)], cadd(p0, pjm)));
+    const cplx_t cs2 = csub(cadd(csub(cscl(0.5 * a.m.c12[d.m3(k + 1, j, 2)], cadd(p0, pkp)),
+                                      cscl(0.5 * a.m.c12[d.m3(k, j, 2)], cadd(p0, pkm))),
+                                 cscl(0.5 * a.m.c22[d.m3(k, j + 1, 1)], cadd(p0, pjp))),
+                            cscl(0.5 * a.m.c22[d.m3(k, j, 1)], cadd(p0, pjm)));
+    const cplx_t ik = {0.0, a.kx[i]};
+    r1 = csub(r1, cmul(cscl(jac, cscl(a.T4, ik)), p0));
+    r2 = csub(r2, cscl(a.T4, cs2));
+    r3 = csub(r3, cscl(a.T4, cs1));
+    if (i == 0 && a.forcing) r3.re = r3.re - a.T4 * a.px * jac;
+    a.CR1[q] = r1;
+    a.CR2[q] = r2;
+    a.CR3[q] = r3;
+    const double v = -a.nu * a.kx2[i] * jac;
+    cplx_t f1 = cscl(v, cu1), f2 = cscl(v, cu2), f3 = cscl(v, cu3);
+    f3 = cadd(f3, cscl(jac, cscl(a.f0, cplx_t{cu1.re - a.ubc_top, cu1.im})));
+    f1 = csub(f1, cscl(jac, cscl(a.f0, cplx_t{cu3.re - a.wbulk0, cu3.im})));
+    if (a.th) f2 = csub(f2, cscl(jac * a.ri, a.CTH[q]));
+    a.CF1[q] = f1;
+    a.CF2[q] = f2;
+    a.CF3[q] = f3;
+  }
+  if (sca) {
+    const cplx_t cth = a.CTH[q];
+    cplx_t rt = cscl(jac, cth);
+    if (a.rk > 1) rt = cadd(rt, cscl(a.T3, a.CFTH[q]));
+    a.CRTH[q] = rt;
+    cplx_t ft = cscl(-a.nupr * jac * a.kx2[i], cth);
+    if (a.cont_strat) {
+      ft = cadd(ft, cscl(jac, a.CU2[q]));
+    } else {
+      const double *TB = a.m.thbar;
+      auto tb = [&](int kk, int jj) { return TB[d.m2(kk, jj)]; };
+      const double g = 0.5 * a.m.c12[d.m3(k + 1, j, 2)] * (tb(k, j) + tb(k + 1, j)) -
+                       0.5 * a.m.c12[d.m3(k, j, 2)] * (tb(k, j) + tb(k - 1, j)) +
+                       0.5 * a.m.c22[d.m3(k, j + 1, 1)] * (tb(k, j) + tb(k, j + 1)) -
+                       0.5 * a.m.c22[d.m3(k, j, 1)] * (tb(k, j) + tb(k, j - 1));
+      ft = csub(ft, cscl(g, a.CU2[q]));
+      const double dd =
+          0.25 * a.nupr *
+          (+a.m.g12[d.m3(k + 1, j, 2)] * (tb(k + 1, j + 1) + tb(k, j + 1) - tb(k, j - 1) - tb(k + 1, j - 1)) -
+           a.m.g12[d.m3(k, j, 2)] * (tb(k - 1, j + 1) + tb(k, j + 1) - tb(k, j - 1) - tb(k - 1, j - 1)) +
+           a.m.g12[d.m3(k, j + 1, 1)] * (tb(k + 1, j + 1) + tb(k + 1, j) - tb(k - 1, j + 1) - tb(k - 1, j)) -
+           a.m.g12[d.m3(k, j, 1)] * (tb(k + 1, j) + tb(k + 1, j - 1) - tb(k - 1, j) - tb(k - 1, j - 1)) +
+           4.0 * (a.m.g11[d.m3(k + 1, j, 2)] * (tb(k + 1, j) - tb(k, j)) - a.m.g11[d.m3(k, j, 2)] * (tb(k, j) - tb(k - 1, j))) +
+           4.0 * (a.m.g22[d.m3(k, j + 1, 1)] * (tb(k, j + 1) - tb(k, j)) - a.m.g22[d.m3(k, j, 1)] * (tb(k, j) - tb(k, j - 1))));
+      ft.re = ft.re + dd;
+    }
+    a.CFTH[q] = ft;
+  }
+}
+
+// Contravariant face velocities U2b, U3b (duct.F90:721-732); U3b is stored
+// right after U2b.
+__global__ void k_face_velocity(Dims d, Metrics m, const double *U2, const double *U3, double *U2b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = d.ZS + blockIdx.y, j = d.JS + blockIdx.z;
+  if (i >= d.NX) return;
+  double *U3b = U2b + d.nphys();
+  const size_t c = d.ip(i, k, j);
+  const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
+  U2b[c] = 0.5 * m.c22[d.m3(k, j, 1)] * (U2[c] + U2[c - sJ]) + 0.5 * m.c21[d.m3(k, j, 1)] * (U3[c] + U3[c - sJ]);
+  U3b[c] = 0.5 * m.c11[d.m3(k, j, 2)] * (U3[c] + U3[c - sK]) + 0.5 * m.c12[d.m3(k, j, 2)] * (U2[c] + U2[c - sK]);
+}
+
+// CN-ADI line solves.  One thread per x point I; the Thomas factors of the
+// line (I-independent) were precomputed on the host; shared memory holds
+// the forward-eliminated right-hand side of every thread's line.
+constexpr int kAdiThreads = 32;
+
+struct AdiArgs {
+  Dims d;
+  Metrics m;
+  const double *R, *phi_old, *phs;  // R: c2r(CR); phi_old: field before ADI; phs: y-sweep output
+  double *out;                      // y: phs, z: field
+  const double *fa, *fib, *fu;      // factors [line][row]
+  BcSet bc;
+  const double *bcw;
+  double coef;
+  int js, je, zs, ze;
+};
+
+// y sweep, duct.F90:1640-1739 for U1 (TH 1334-1433, U2 1877-1980, U3 2137-2233):
+// R' = S/2 + J phi + coef d_zeta(G11 d_zeta phi), S = R - J phi; solve the
+// y-tridiagonal of each (I,K) line; the solution goes to phs.
+__global__ void __launch_bounds__(kAdiThreads) k_adi_y(AdiArgs a) {
+  extern __shared__ double g[];  // [row][thread]
+  const Dims &d = a.d;
+  const int t = threadIdx.x;
+  const int i = blockIdx.x * kAdiThreads + t;
+  const int k = a.zs + blockIdx.y;
+  const int nrow = d.NY2;
+  const bool act = (i < d.NX);
+  const size_t sK = d.LDX;
+  const double *fa = a.fa + (size_t)k * nrow, *fib = a.fib + (size_t)k * nrow, *fu = a.fu + (size_t)k * nrow;
+  const double g1 = 0, g0 = 0;
+  (void)g1; (void)g0;
+  // right-hand side of every row
+  for (int r = 0; r < nrow; ++r) {
+    double v = 0.0;
+    if (act) {
+      if (r >= a.js && r <= a.je) {
+        const size_t c = d.ip(i, k, r);
+        const double jac = a.m.jac[d.m2(k, r)];
+        const double ph = a.phi_old[c];
+        const double s = a.R[c] - jac * ph;
+        const double gp = a.m.g11[d.m3(k + 1, r, 2)], gm = a.m.g11[d.m3(k, r, 2)];
+        v = 0.5 * s + jac * ph + a.coef * (gp * (a.phi_old[c + sK] - ph) - gm * (ph - a.phi_old[c - sK]));
+      }
+      for (int b = 0; b < a.bc.n; ++b) {
+        const BcRow &br = a.bc.r[b];
+        if (br.row != r) continue;
+        if (br.kind == 0) v = br.val;
+        else if (br.kind == 1) v = a.phi_old[d.ip(i, k, br.src)];
+        else v = br.val * a.bcw[br.src + k];
+      }
+    }
+    g[r * kAdiThreads + t] = v;
+  }
+  if (!act) return;
+  // forward elimination then back substitution (THOMAS_REAL)
+  double prev = g[t];
+  for (int r = 1; r < nrow; ++r) {
+    prev = g[r * kAdiThreads + t] + fa[r] * prev;
+    g[r * kAdiThreads + t] = prev;
+  }
+  double x = prev * fib[nrow - 1];
+  a.out[d.ip(i, k, nrow - 1)] = x;
+  for (int r = nrow - 2; r >= 0; --r) {
+    x = (g[r * kAdiThreads + t] - fu[r] * x) * fib[r];
+    a.out[d.ip(i, k, r)] = x;
+  }
+}
+
+// z sweep, duct.F90:1741-1854 for U1 (TH 1437-1600, U2 1983-2115,
+// U3 2257-2392): R'' = S/2 + J phi* + coef d_eta(G22 d_eta phi*); solve the
+// z-tridiagonal of each (I,J) line into the field.  Rows J outside the
+// solved range take the y-sweep values.
+__global__ void __launch_bounds__(kAdiThreads) k_adi_z(AdiArgs a) {
+  extern __shared__ double g[];
+  const Dims &d = a.d;
+  const int t = threadIdx.x;
+  const int i = blockIdx.x * kAdiThreads + t;
+  const int j = blockIdx.y;
+  const int nrow = d.NZ2;
+  if (i >= d.NX) return;
+  if (j < a.js || j > a.je) {
+    for (int k = a.zs; k <= a.ze; ++k) a.out[d.ip(i, k, j)] = a.phs[d.ip(i, k, j)];
+    return;
+  }
+  const size_t sJ = (size_t)d.LDX * d.NZ2;
+  const double *fa = a.fa + (size_t)j * nrow, *fib = a.fib + (size_t)j * nrow, *fu = a.fu + (size_t)j * nrow;
+  for (int r = 0; r < nrow; ++r) {
+    double v = 0.0;
+    if (r >= a.zs && r <= a.ze) {
+      const size_t c = d.ip(i, r, j);
+      const double jac = a.m.jac[d.m2(r, j)];
+      const double s = a.R[c] - jac * a.phi_old[c];
+      const double ps = a.phs[c];
+      const double gp = a.m.g22[d.m3(r, j + 1, 1)], gm = a.m.g22[d.m3(r, j, 1)];
+      v = 0.5 * s + jac * ps + a.coef * (+gp * (a.phs[c + sJ] - ps) - gm * (ps - a.phs[c - sJ]));
+    }
+    for (int b = 0; b < a.bc.n; ++b) {
+      const BcRow &br = a.bc.r[b];
+      if (br.row != r) continue;
+      if (br.kind == 0) v = br.val;
+      else if (br.kind == 1) v = a.phs[d.ip(i, br.src, j)];
+      else v = br.val * a.bcw[br.src + j];
+    }
+    g[r * kAdiThreads + t] = v;
+  }
+  double prev = g[t];
+  for (int r = 1; r < nrow; ++r) {
+    prev = g[r * kAdiThreads + t] + fa[r] * prev;
+    g[r * kAdiThreads + t] = prev;
+  }
+  double x = prev * fib[nrow - 1];
+  a.out[d.ip(i, nrow - 1, j)] = x;
+  for (int r = nrow - 2; r >= 0; --r) {
+    x = (g[r * kAdiThreads + t] - fu[r] * x) * fib[r];
+    a.out[d.ip(i, r, j)] = x;
+  }
+}
+
+// Corner copies after the TH solve (duct.F90:1606-1624).
+__global__ void k_th_corners(Dims d, double *TH, int zmax1, int zmin6) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.NX) return;
+  const int NZ = d.NZ, NY = d.NY;
+  if (zmax1) {
+    TH[d.ip(i, NZ + 1, NY + 1)] = TH[d.ip(i, NZ, NY + 1)];
+    TH[d.ip(i, NZ + 1, 0)] = TH[d.ip(i, NZ, 0)];
+    TH[d.ip(i, 0, NY + 1)] = TH[d.ip(i, 1, NY + 1)];
+    TH[d.ip(i, 0, 0)] = TH[d.ip(i, 1, 0)];
+  }
+  if (zmin6) {
+    TH[d.ip(i, NZ + 1, NY + 1)] = TH[d.ip(i, 1, NY + 1)];
+    TH[d.ip(i, NZ + 1, 0)] = TH[d.ip(i, 1, 0)];
+    TH[d.ip(i, 0, NY + 1)] = TH[d.ip(i, NZ, NY + 1)];
+    TH[d.ip(i, 0, 0)] = TH[d.ip(i, NZ, 0)];
+  }
+}
+
+// REM_DIV_CURV face velocities CU2b, CU3b (duct.F90:2511-2522), zero
+// elsewhere (2501-2503); CU3b follows CU2b in memory.
+__global__ void k_rem_faces(Dims d, Metrics m, const cplx_t *CU2, const cplx_t *CU3, cplx_t *CU2b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y, j = blockIdx.z;
+  if (i > d.NX2P) return;
+  cplx_t *CU3b = CU2b + d.nspec();
+  const size_t q = d.ic(i, k, j);
+  if (j >= d.JS && j <= d.JE + 1 && k >= d.ZS && k <= d.ZE + 1) {
+    const size_t sK = d.LDC, sJ = (size_t)d.LDC * d.NZ2;
+    CU2b[q] = cadd(cscl(0.5 * m.c22[d.m3(k, j, 1)], cadd(CU2[q], CU2[q - sJ])),
+                   cscl(0.5 * m.c21[d.m3(k, j, 1)], cadd(CU3[q], CU3[q - sJ])));
+    CU3b[q] = cadd(cscl(0.5 * m.c11[d.m3(k, j, 2)], cadd(CU3[q], CU3[q - sK])),
+                   cscl(0.5 * m.c12[d.m3(k, j, 2)], cadd(CU2[q], CU2[q - sK])));
+  } else {
+    CU2b[q] = cplx_t{0.0, 0.0};
+    CU3b[q] = cplx_t{0.0, 0.0};
+  }
+}
+
+// Divergence (duct.F90:2527-2535) written straight into the multigrid
+// right-hand side: problem p = 2I (real part) or 2I+1 (imaginary part) of
+// mode I, MUDPACK point (K+1, J+1); RHS_TMP is zero outside the range
+// (2631-2651) and phi_bc negates -Re/-Im back.
+__global__ void k_div_rhs(Dims d, const double *kx, const cplx_t *CU1, const cplx_t *CU2b, const double *jacm,
+                          double *rhs, int P) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y, j = blockIdx.z;  // full 0..NZ+1, 0..NY+1
+  if (p >= P) return;
+  const int I = p >> 1;
+  double v = 0.0;
+  if (j >= d.JS && j <= d.JE && k >= d.ZS && k <= d.ZE) {
+    const cplx_t *CU3b = CU2b + d.nspec();
+    const size_t q = d.ic(I, k, j);
+    const size_t sK = d.LDC, sJ = (size_t)d.LDC * d.NZ2;
+    const cplx_t ikj = cmul(cplx_t{0.0, kx[I]}, cplx_t{jacm[d.m2(k, j)], 0.0});
+    const cplx_t dv = cadd(cadd(cmul(ikj, CU1[q]), csub(CU2b[q + sJ], CU2b[q])), csub(CU3b[q + sK], CU3b[q]));
+    v = (p & 1) ? dv.im : dv.re;
+  }
+  const int nfx = d.NZ2;
+  rhs[((size_t)j * nfx + k) * P + p] = v;
+}
+
+// phi back into CR1 (CMPLX(P_TMP2,P_TMP), duct.F90:2662-2666; REAL*4
+// rounding under quirk_phi_fp32), modes above the solved set are zero, and
+// the pressure update CP += CR1/h (duct.F90:2460-2466) when requested.
+__global__ void k_phi_to_cr1(Dims d, const double *phif, int P, cplx_t *CR1, cplx_t *CP, double temp4, int update_p,
+                             int fp32) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y, j = blockIdx.z;
+  if (I > d.NX2P) return;
+  cplx_t v{0.0, 0.0};
+  if (2 * I + 1 < P) {
+    const size_t b = ((size_t)j * d.NZ2 + k) * P + 2 * I;
+    v.re = phif[b];
+    v.im = phif[b + 1];
+    if (fp32) {
+      v.re = (double)(float)v.re;
+      v.im = (double)(float)v.im;
+    }
+  }
+  const size_t q = d.ic(I, k, j);
+  CR1[q] = v;
+  if (update_p && j >= d.JS - 1 && j <= d.JE + 1 && k >= d.ZS - 1 && k <= d.ZE + 1) {
+    const cplx_t o = CP[q];
+    CP[q] = cplx_t{o.re + v.re / temp4, o.im + v.im / temp4};
+  }
+}
+
+// Face-velocity correction (duct.F90:2709-2724).
+__global__ void k_correct_faces(Dims d, Metrics m, const cplx_t *CR1, cplx_t *CU2b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = d.ZS + blockIdx.y, j = d.JS + blockIdx.z;
+  if (i > d.NX2P) return;
+  cplx_t *CU3b = CU2b + d.nspec();
+  const size_t q = d.ic(i, k, j);
+  const size_t sK = d.LDC, sJ = (size_t)d.LDC * d.NZ2;
+  auto P = [&](int dk, int dj) { return CR1[q + (long)dk * (long)sK + (long)dj * (long)sJ]; };
+  CU2b[q] = csub(csub(CU2b[q], cscl(m.g22[d.m3(k, j, 1)], csub(P(0, 0), P(0, -1)))),
+                 cscl(0.25 * m.g12[d.m3(k, j, 1)], csub(csub(cadd(P(1, 0), P(1, -1)), P(-1, 0)), P(-1, -1))));
+  CU3b[q] = csub(csub(CU3b[q], cscl(m.g11[d.m3(k, j, 2)], csub(P(0, 0), P(-1, 0)))),
+                 cscl(0.25 * m.g12[d.m3(k, j, 2)], csub(csub(cadd(P(0, 1), P(-1, 1)), P(0, -1)), P(-1, -1))));
+}
+
+// Cell-centre correction (duct.F90:2729-2750).
+__global__ void k_correct_cells(Dims d, Metrics m, const double *kx, const cplx_t *CR1, cplx_t *CU1, cplx_t *CU2,
+                                cplx_t *CU3) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = d.ZS + blockIdx.y, j = d.JS + blockIdx.z;
+  if (i > d.NX2P) return;
+  const size_t q = d.ic(i, k, j);
+  const size_t sK = d.LDC, sJ = (size_t)d.LDC * d.NZ2;
+  auto P = [&](int dk, int dj) { return CR1[q + (long)dk * (long)sK + (long)dj * (long)sJ]; };
+  const double jac = m.jac[d.m2(k, j)];
+  CU1[q] = csub(CU1[q], cmul(cplx_t{0.0, kx[i]}, P(0, 0)));
+  const cplx_t t2 = csub(cadd(csub(cscl(m.c22[d.m3(k, j + 1, 1)], cadd(P(0, 0), P(0, 1))),
+                                   cscl(m.c22[d.m3(k, j, 1)], cadd(P(0, 0), P(0, -1)))),
+                              cscl(m.c12[d.m3(k + 1, j, 2)], cadd(P(1, 0), P(0, 0)))),
+                         cscl(m.c12[d.m3(k, j, 2)], cadd(P(0, 0), P(-1, 0))));
+  const cplx_t u2 = cscl(0.5, t2);
+  const cplx_t o2 = CU2[q];
+  CU2[q] = cplx_t{o2.re - u2.re / jac, o2.im - u2.im / jac};
+  const cplx_t t3 = csub(cadd(csub(cscl(m.c11[d.m3(k + 1, j, 2)], cadd(P(0, 0), P(1, 0))),
+                                   cscl(m.c11[d.m3(k, j, 2)], cadd(P(0, 0), P(-1, 0)))),
+                              cscl(m.c21[d.m3(k, j + 1, 1)], cadd(P(0, 1), P(0, 0)))),
+                         cscl(m.c21[d.m3(k, j, 1)], cadd(P(0, 0), P(0, -1))));
+  const cplx_t u3 = cscl(0.5, t3);
+  const cplx_t o3 = CU3[q];
+  CU3[q] = cplx_t{o3.re - u3.re / jac, o3.im - u3.im / jac};
+}
+
+// Divergence after the projection (duct.F90:2754-2761) into CS.
+__global__ void k_div_check(Dims d, const double *kx, const double *jacm, const cplx_t *CU1, const cplx_t *CU2b,
+                            cplx_t *CS) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y, j = blockIdx.z;
+  if (i > d.NX2P) return;
+  const size_t q = d.ic(i, k, j);
+  cplx_t v{0.0, 0.0};
+  if (j >= d.JS && j <= d.JE && k >= d.ZS && k <= d.ZE) {
+    const cplx_t *CU3b = CU2b + d.nspec();
+    const size_t sK = d.LDC, sJ = (size_t)d.LDC * d.NZ2;
+    const cplx_t ikj = cmul(cplx_t{0.0, kx[i]}, cplx_t{jacm[d.m2(k, j)], 0.0});
+    v = cadd(cadd(cmul(ikj, CU1[q]), csub(CU2b[q + sJ], CU2b[q])), csub(CU3b[q + sK], CU3b[q]));
+  }
+  CS[q] = v;
+}
+
+// Sum of |div| over I = 1..NXP, K = 2..NZ-1 per line J (duct.F90:2790-2798);
+// one block per J, fixed summation order.
+__global__ void k_div_sum(Dims d, const double *S, double *part) {
+  const int j = 2 + blockIdx.x;
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int k = 2; k <= d.NZ - 1; ++k)
+    for (int i = 1 + threadIdx.x; i <= d.NX + 1; i += blockDim.x) s += fabs(S[d.ip(i, k, j)]);
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+}  // namespace
+
+void launch_spectral_rhs(Ctx &c, int rk) {
+  SpecArgs a;
+  a.d = c.d;
+  a.m = c.m;
+  a.kx = c.kx;
+  a.kx2 = c.kx2;
+  a.CU1 = c.CU1; a.CU2 = c.CU2; a.CU3 = c.CU3; a.CP = c.CP; a.CTH = c.CTH;
+  a.CF1 = c.CF1; a.CF2 = c.CF2; a.CF3 = c.CF3; a.CFTH = c.CFTH;
+  a.CR1 = c.CR1; a.CR2 = c.CR2; a.CR3 = c.CR3; a.CRTH = c.CRTH;
+  const ek_params &p = c.p;
+  a.nu = p.nu;
+  a.nupr = p.nu / p.pr;
+  a.T3 = c.ZETA_BAR[rk] * c.H_BAR[rk];
+  a.T4 = c.H_BAR[rk];
+  a.forcing = (p.f_type == 1 || p.f_type == 2);
+  a.px = (p.f_type == 1) ? p.px0 : (p.px0 + p.amp_omega0 * cos(p.omega0 * p.time));
+  a.f0 = p.f0;
+  a.ubc_top = p.u_bc_c1[EK_YMAX];
+  a.wbulk0 = p.wbulk0;
+  a.ri = p.ri_tau;
+  a.rk = rk;
+  a.th = p.n_th > 0;
+  a.cont_strat = p.cont_strat;
+  dim3 grid((c.d.NX2P + 1 + 63) / 64, c.d.NZ2, c.d.NY2);
+  KScope ks(c, KC_SPECTRAL);
+  k_spectral_rhs<<<grid, 64, 0, c.stream>>>(a);
+  after_launch(c);
+}
+
+void launch_face_velocity(Ctx &c) {
+  const Dims &d = c.d;
+  dim3 grid((d.NX + 127) / 128, d.ZE - d.ZS + 2, d.JE - d.JS + 2);
+  KScope ks(c, KC_FACE);
+  k_face_velocity<<<grid, 128, 0, c.stream>>>(d, c.m, c.U2, c.U3, c.U2b);
+  after_launch(c);
+}
+
+void launch_adi(Ctx &c, int field, int rk) {
+  const Dims &d = c.d;
+  double *phi = (field == 0) ? c.TH : (field == 1) ? c.U1 : (field == 2) ? c.U2 : c.U3;
+  const double *R = (field == 0) ? c.RTH : (field == 1) ? c.R1 : (field == 2) ? c.R2 : c.R3;
+  double coef = c.p.nu * c.H_BAR[rk] / 2.0;
+  if (field == 0) coef = coef / c.p.pr;
+  AdiArgs a;
+  a.d = d;
+  a.m = c.m;
+  a.R = R;
+  a.phi_old = phi;
+  a.phs = c.PHS;
+  a.bcw = c.bc_weights;
+  a.coef = coef;
+  a.js = (field == 0) ? d.JST : d.JS;
+  a.je = (field == 0) ? d.JET : d.JE;
+  a.zs = (field == 0) ? d.ZST : d.ZS;
+  a.ze = (field == 0) ? d.ZET : d.ZE;
+  // y sweep
+  a.out = c.PHS;
+  a.fa = c.adi[field][rk][0].a;
+  a.fib = c.adi[field][rk][0].ib;
+  a.fu = c.adi[field][rk][0].u;
+  a.bc = c.bc[field][0];
+  {
+    const size_t smem = sizeof(double) * kAdiThreads * d.NY2;
+    dim3 grid((d.NX + kAdiThreads - 1) / kAdiThreads, a.ze - a.zs + 1);
+    KScope ks(c, KC_ADI_Y);
+    k_adi_y<<<grid, kAdiThreads, smem, c.stream>>>(a);
+    after_launch(c);
+  }
+  // z sweep
+  a.out = phi;
+  a.fa = c.adi[field][rk][1].a;
+  a.fib = c.adi[field][rk][1].ib;
+  a.fu = c.adi[field][rk][1].u;
+  a.bc = c.bc[field][1];
+  {
+    const size_t smem = sizeof(double) * kAdiThreads * d.NZ2;
+    dim3 grid((d.NX + kAdiThreads - 1) / kAdiThreads, d.NY2);
+    KScope ks(c, KC_ADI_Z);
+    k_adi_z<<<grid, kAdiThreads, smem, c.stream>>>(a);
+    after_launch(c);
+  }
+}
+
+void launch_th_corners(Ctx &c) {
+  const int zmax1 = c.p.th_bc[EK_ZMAX] == 1, zmin6 = c.p.th_bc[EK_ZMIN] == 6;
+  if (!zmax1 && !zmin6) return;
+  KScope ks(c, KC_ADI_Z);
+  k_th_corners<<<(c.d.NX + 127) / 128, 128, 0, c.stream>>>(c.d, c.TH, zmax1, zmin6);
+  after_launch(c);
+}
+
+void launch_divergence_rhs(Ctx &c, double *rhs, int P) {
+  const Dims &d = c.d;
+  KScope ks(c, KC_DIVERGENCE);
+  dim3 g1((d.NX2P + 1 + 63) / 64, d.NZ2, d.NY2);
+  k_rem_faces<<<g1, 64, 0, c.stream>>>(d, c.m, c.CU2, c.CU3, c.CU2b);
+  after_launch(c);
+  dim3 g2((P + 63) / 64, d.NZ2, d.NY2);
+  k_div_rhs<<<g2, 64, 0, c.stream>>>(d, c.kx, c.CU1, c.CU2b, c.m.jac, rhs, P);
+  after_launch(c);
+}
+
+void launch_projection(Ctx &c, const double *phif, int P, double temp4, bool update_p) {
+  const Dims &d = c.d;
+  dim3 g0((d.NX2P + 1 + 63) / 64, d.NZ2, d.NY2);
+  {
+  KScope ks(c, KC_PROJECTION);
+  k_phi_to_cr1<<<g0, 64, 0, c.stream>>>(d, phif, P, c.CR1, c.CP, temp4, update_p ? 1 : 0, c.p.quirk_phi_fp32);
+  after_launch(c);
+  dim3 g1((d.NX2P + 1 + 63) / 64, d.ZE - d.ZS + 1, d.JE - d.JS + 1);
+  k_correct_faces<<<g1, 64, 0, c.stream>>>(d, c.m, c.CR1, c.CU2b);
+  after_launch(c);
+  k_correct_cells<<<g1, 64, 0, c.stream>>>(d, c.m, c.kx, c.CR1, c.CU1, c.CU2, c.CU3);
+  after_launch(c);
+  k_div_check<<<g0, 64, 0, c.stream>>>(d, c.kx, c.m.jac, c.CU1, c.CU2b, c.CS);
+  after_launch(c);
+  }
+  C2rArgs ca{};
+  ca.src = c.CS;
+  ca.dst = c.SPH;
+  ca.j0 = 2;
+  ca.j1 = d.NY - 1;
+  ca.k0 = 2;
+  ca.k1 = d.NZ - 1;
+  launch_c2r(c, ca);
+  KScope ks(c, KC_DIVERGENCE);
+  k_div_sum<<<d.NY - 2, 256, 0, c.stream>>>(d, c.SPH, c.div_part);
+  after_launch(c);
+}
+
+// Mean |div| from the per-line partial sums, in J order (duct.F90:2800).
+int finish_divergence(Ctx &c, double *div_out) {
+  const Dims &d = c.d;
+  std::vector<double> part(d.NY - 2);
+  EK_CUDA(cudaMemcpyAsync(part.data(), c.div_part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, c.stream));
+  EK_CUDA(cudaStreamSynchronize(c.stream));
+  double s = 0.0;
+  for (double v : part) s += v;
+  s = s / ((double)(d.NX + 1) * (double)d.NY * (double)d.NZ);
+  c.last_div = s;
+  if (div_out) *div_out = s;
+  return (s != s) ? EK_ERR_NAN : EK_OK;
+}
+
+}  // namespace ek
+
+namespace ek {
+// The ADI kernels keep one line of right-hand sides per thread in shared
+// memory (32 threads x (NY+2) doubles), more than the default 48 KB for
+// tall grids.
+void rk_init_attributes() {
+  static bool done = false;
+  if (done) return;
+  EK_CUDA(cudaFuncSetAttribute(k_adi_y, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  EK_CUDA(cudaFuncSetAttribute(k_adi_z, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  done = true;
+}
+}  // namespace ek

@@ -1,0 +1,219 @@
+"""Host-side mirror of the reference's duct-substep interface, over the C ABI.
+
+The reference (ekman_bl) exposes its hot path as Fortran subroutines that
+act on module globals: RK_DUCT (src/duct.F90:237-2469), REM_DIV_CURV
+(src/duct.F90:2472-2818) and MULTIGRID_MUDPACK (src/mg_solver2d.F90:75-201).
+`DuctSolver` keeps the same operations and names, with the module state held
+on the GPU by libekgpu.so.  Every call goes through the C ABI of
+include/ekgpu.h; there is no CPU fallback -- if the library or a GPU is
+missing, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .params import STATUS, EkMetrics, EkMgStats, EkParams, as_ptr, spectral_shape
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libekgpu.so")
+_D = C.POINTER(C.c_double)
+_lib = None
+
+EXPORTS = [
+    "ekgpu_default_params", "ekgpu_create", "ekgpu_destroy", "ekgpu_last_error", "ekgpu_set_stream",
+    "ekgpu_set_metrics", "ekgpu_metrics_from_grid", "ekgpu_upload_state", "ekgpu_download_state",
+    "ekgpu_get_field", "ekgpu_put_field", "ekgpu_rk_substep", "ekgpu_step", "ekgpu_rem_div",
+    "ekgpu_poisson_batch", "ekgpu_poisson_batch_device", "ekgpu_last_divergence", "ekgpu_last_mg_stats",
+    "ekgpu_launch_count", "ekgpu_set_timing", "ekgpu_get_timing", "ekgpu_timing_class_name",
+]
+
+
+class EkError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib_path() -> str:
+    return _LIB_PATH
+
+
+def load_library():
+    """Load libekgpu.so (built by ekman_bl_gb300.build); raises if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        raise RuntimeError(f"{_LIB_PATH} is missing: run `python -m ekman_bl_gb300.build` (needs nvcc)")
+    L = C.CDLL(_LIB_PATH)
+    P = C.POINTER(EkParams)
+    V = C.c_void_p
+    L.ekgpu_default_params.argtypes = [P]
+    L.ekgpu_create.argtypes = [P, C.POINTER(V)]
+    L.ekgpu_destroy.argtypes = [V]
+    L.ekgpu_destroy.restype = None
+    L.ekgpu_last_error.argtypes = [V]
+    L.ekgpu_last_error.restype = C.c_char_p
+    L.ekgpu_set_stream.argtypes = [V, V]
+    L.ekgpu_set_metrics.argtypes = [V, C.POINTER(EkMetrics)]
+    L.ekgpu_metrics_from_grid.argtypes = [P, _D, _D] + [_D] * 9
+    L.ekgpu_upload_state.argtypes = [V] + [_D] * 5
+    L.ekgpu_download_state.argtypes = [V] + [_D] * 5
+    L.ekgpu_get_field.argtypes = [V, C.c_int, _D]
+    L.ekgpu_put_field.argtypes = [V, C.c_int, _D]
+    L.ekgpu_rk_substep.argtypes = [V, C.c_int]
+    L.ekgpu_step.argtypes = [V, C.c_int]
+    L.ekgpu_rem_div.argtypes = [V]
+    L.ekgpu_poisson_batch.argtypes = [V, _D, _D, _D, C.c_int, C.POINTER(EkMgStats)]
+    L.ekgpu_poisson_batch_device.argtypes = [V, V, V, V, C.c_int, C.POINTER(EkMgStats)]
+    L.ekgpu_last_divergence.argtypes = [V, _D]
+    L.ekgpu_last_mg_stats.argtypes = [V, C.POINTER(EkMgStats)]
+    L.ekgpu_launch_count.argtypes = [V]
+    L.ekgpu_launch_count.restype = C.c_longlong
+    L.ekgpu_set_timing.argtypes = [V, C.c_int]
+    L.ekgpu_get_timing.argtypes = [V, _D, C.POINTER(C.c_longlong), C.c_int]
+    L.ekgpu_timing_class_name.argtypes = [C.c_int]
+    L.ekgpu_timing_class_name.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def metrics_from_grid(p: EkParams, xpoint: np.ndarray, ypoint: np.ndarray) -> dict:
+    """JACOBI_TRANS (src/diablo.F90:1088-1570) through ekgpu_metrics_from_grid.
+    Arrays in C order: 2-D [J, K] = Fortran (0:NZ+2, 0:NY+2); face [f, J, K]."""
+    L = load_library()
+    n2 = (p.ny + 3, p.nz + 3)
+    out = {"int_jacob": np.zeros(n2), "th_bar": np.zeros(n2)}
+    for k in ("gmat_11", "gmat_12", "gmat_22", "cjob_11", "cjob_12", "cjob_21", "cjob_22"):
+        out[k] = np.zeros((2,) + n2)
+    xp = np.ascontiguousarray(xpoint, np.float64)
+    yp = np.ascontiguousarray(ypoint, np.float64)
+    st = L.ekgpu_metrics_from_grid(C.byref(p), as_ptr(xp), as_ptr(yp), *[as_ptr(out[k]) for k in (
+        "int_jacob", "gmat_11", "gmat_12", "gmat_22", "cjob_11", "cjob_12", "cjob_21", "cjob_22", "th_bar")])
+    if st:
+        raise EkError(st, "ekgpu_metrics_from_grid")
+    return out
+
+
+class DuctSolver:
+    """GPU-resident RK3 duct substep (one context = one set of module arrays)."""
+
+    def __init__(self, p: EkParams, metrics: dict):
+        self.p = p
+        self._L = load_library()
+        h = C.c_void_p()
+        st = self._L.ekgpu_create(C.byref(p), C.byref(h))
+        self._h = h
+        if st:
+            msg = self._L.ekgpu_last_error(h).decode() if h.value else ""
+            self.close()
+            raise EkError(st, msg)
+        self._metrics = {k: np.ascontiguousarray(v, np.float64) for k, v in metrics.items()}
+        m = EkMetrics()
+        for k in ("int_jacob", "gmat_11", "gmat_12", "gmat_22", "cjob_11", "cjob_12", "cjob_21", "cjob_22", "th_bar"):
+            setattr(m, k, as_ptr(self._metrics[k]))
+        self._check(self._L.ekgpu_set_metrics(h, C.byref(m)))
+
+    # -- plumbing -----------------------------------------------------------
+    def _check(self, st, allow=()):
+        if st and st not in allow:
+            raise EkError(st, self._L.ekgpu_last_error(self._h).decode())
+        return st
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._L.ekgpu_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_ptr: int | None):
+        self._check(self._L.ekgpu_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
+
+    # -- state ----------------------------------------------------------------
+    def upload(self, cu1, cu2, cu3, cp, cth):
+        arrs = [np.ascontiguousarray(a, np.complex128) for a in (cu1, cu2, cu3, cp, cth)]
+        self._check(self._L.ekgpu_upload_state(self._h, *[as_ptr(a) for a in arrs]))
+
+    def download(self):
+        shape = spectral_shape(self.p)
+        arrs = [np.zeros(shape, np.complex128) for _ in range(5)]
+        self._check(self._L.ekgpu_download_state(self._h, *[as_ptr(a) for a in arrs]))
+        return arrs
+
+    def get_field(self, f: int):
+        a = np.zeros(spectral_shape(self.p), np.complex128)
+        self._check(self._L.ekgpu_get_field(self._h, f, as_ptr(a)))
+        return a
+
+    def put_field(self, f: int, a):
+        a = np.ascontiguousarray(a, np.complex128)
+        self._check(self._L.ekgpu_put_field(self._h, f, as_ptr(a)))
+
+    # -- the reference operations ---------------------------------------------
+    def rk_duct(self, rk_step: int):
+        """RK_DUCT: one RK3 substep (duct.F90:237-2469)."""
+        return self._check(self._L.ekgpu_rk_substep(self._h, rk_step))
+
+    def step(self, nsteps: int = 1):
+        """nsteps times DO RK_STEP=1,3; CALL RK_DUCT (diablo.F90:152-154)."""
+        return self._check(self._L.ekgpu_step(self._h, nsteps))
+
+    def rem_div_curv(self):
+        """REM_DIV_CURV: projection of the current state (duct.F90:2472-2818)."""
+        return self._check(self._L.ekgpu_rem_div(self._h))
+
+    def multigrid_mudpack(self, rhs: np.ndarray, kx2: np.ndarray):
+        """Batched MULTIGRID_MUDPACK: rhs[nprob, NY+2, NZ+2] (MUDPACK grid,
+        K fastest), one kx^2 per problem; returns (phi, stats, status)."""
+        rhs = np.ascontiguousarray(rhs, np.float64)
+        kx2 = np.ascontiguousarray(kx2, np.float64)
+        phi = np.zeros_like(rhs)
+        st = EkMgStats()
+        code = self._L.ekgpu_poisson_batch(self._h, as_ptr(rhs), as_ptr(phi), as_ptr(kx2), len(kx2), C.byref(st))
+        self._check(code, allow=(3,))
+        return phi, st.as_dict(), code
+
+    def multigrid_mudpack_device(self, rhs_ptr: int, phi_ptr: int, kx2_ptr: int, nprob: int):
+        st = EkMgStats()
+        code = self._L.ekgpu_poisson_batch_device(self._h, C.c_void_p(rhs_ptr), C.c_void_p(phi_ptr),
+                                                   C.c_void_p(kx2_ptr), nprob, C.byref(st))
+        self._check(code, allow=(3,))
+        return st.as_dict(), code
+
+    def divergence(self) -> float:
+        d = C.c_double()
+        self._check(self._L.ekgpu_last_divergence(self._h, C.byref(d)))
+        return d.value
+
+    def mg_stats(self) -> dict:
+        s = EkMgStats()
+        self._check(self._L.ekgpu_last_mg_stats(self._h, C.byref(s)))
+        return s.as_dict()
+
+    def launch_count(self) -> int:
+        return int(self._L.ekgpu_launch_count(self._h))
+
+    def set_timing(self, on: bool):
+        self._check(self._L.ekgpu_set_timing(self._h, 1 if on else 0))
+
+    def timing(self) -> dict:
+        """Per-kernel-class totals {name: (ms, launches)} since set_timing."""
+        n = 32
+        ms = (C.c_double * n)()
+        cnt = (C.c_longlong * n)()
+        k = self._L.ekgpu_get_timing(self._h, ms, cnt, n)
+        if k < 0:
+            self._check(k)
+        return {self._L.ekgpu_timing_class_name(i).decode(): (ms[i], int(cnt[i])) for i in range(k)}

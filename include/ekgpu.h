@@ -200,6 +200,16 @@ int ekgpu_last_mg_stats(ek_ctx *ctx, ek_mg_stats *stats);
 /* Number of kernel launches this context issued since creation. */
 long long ekgpu_launch_count(const ek_ctx *ctx);
 
+/* Optional per-kernel-class timer (CUDA events around every launch on the
+ * context's stream).  ekgpu_set_timing clears the totals; get_timing fills
+ * up to n classes (milliseconds and launch counts) and returns the number
+ * of classes; ekgpu_timing_class_name names class k.  Profiling aid with no
+ * counterpart in the reference (it only prints a wall clock,
+ * diablo.F90:171-176). */
+int ekgpu_set_timing(ek_ctx *ctx, int on);
+int ekgpu_get_timing(ek_ctx *ctx, double *ms, long long *count, int n);
+const char *ekgpu_timing_class_name(int k);
+
 #ifdef __cplusplus
 }
 #endif

@@ -289,13 +289,17 @@ static void to_physical(ekref_ctx *c, const std::vector<cplx> &in, std::vector<d
   }
 }
 
+static bool pow2(int n) { return n >= 2 && (n & (n - 1)) == 0; }
+
 extern "C" void ekref_fft_r2c(int nx, int nkx, long nlines, const double *in, double *out) {
+  if (!pow2(nx)) return;
   FFT f(nx);
   std::vector<std::complex<double>> buf(nx);
   for (long l = 0; l < nlines; ++l)
     r2c_line(f, nkx, in + l * (nx + 2), reinterpret_cast<cplx *>(out) + l * (nx / 2 + 1), buf.data());
 }
 extern "C" void ekref_fft_c2r(int nx, int nkx, long nlines, const double *in, double *out) {
+  if (!pow2(nx)) return;
   FFT f(nx);
   std::vector<std::complex<double>> buf(nx);
   for (long l = 0; l < nlines; ++l)

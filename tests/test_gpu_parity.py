@@ -1,0 +1,119 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle on the same
+seeded inputs.  Tolerances: relative L2 <= 1e-10 after many steps of the
+FP64 path (the bar of the reference's plain method), tighter for single
+operations; multigrid cycle counts must match exactly."""
+import math
+
+import numpy as np
+import pytest
+
+from ekcases import refgrid_case, rel_l2, sheared_case, small_case
+from ekman_bl_gb300 import build as ekbuild
+from ekman_bl_gb300.duct import DuctSolver, metrics_from_grid
+from ekman_bl_gb300.params import (EK_F_CF1, EK_F_CF2, EK_F_CF3, EK_F_CFTH, EK_F_CR1, WORKLOADS,
+                                   workload_setup)
+from oracle import ekref
+
+pytestmark = pytest.mark.gpu
+
+CASES = {"small": small_case, "sheared": sheared_case, "refgrid": refgrid_case}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _build():
+    ekbuild.build()
+
+
+def pair(case, **over):
+    p, xp, yp, st = CASES[case]() if isinstance(case, str) else case
+    for k, v in over.items():
+        setattr(p, k, v)
+    m = metrics_from_grid(p, xp, yp)
+    g = DuctSolver(p, m)
+    o = ekref.Oracle(p, ekref.metrics_from_grid(p, xp, yp))
+    g.upload(*st)
+    o.upload(*st)
+    return p, g, o
+
+
+def compare_state(g, o, tol, fields=True):
+    a, b = g.download(), o.download()
+    for name, x, y in zip(("CU1", "CU2", "CU3", "CP", "CTH"), a, b):
+        e = rel_l2(x, y)
+        assert e <= tol, f"{name}: rel L2 {e:.3e} > {tol:.1e}"
+    return a, b
+
+
+@pytest.mark.parametrize("case", ["small", "sheared", "refgrid"])
+@pytest.mark.parametrize("stop", [0, 1])
+def test_poisson_batch_matches_oracle(case, stop):
+    p, xp, yp, _ = CASES[case]()
+    p.mg_stop = stop
+    if stop == 1:
+        p.mg_tol, p.mg_maxcy = 1e-10, 40
+    m = metrics_from_grid(p, xp, yp)
+    g = DuctSolver(p, m)
+    o = ekref.Oracle(p, ekref.metrics_from_grid(p, xp, yp))
+    rng = np.random.default_rng(11)
+    kx2 = np.array([0.0, 0.3, 1.0, 7.0, 50.0])
+    rhs = rng.standard_normal((len(kx2), p.ny + 2, p.nz + 2))
+    pg, sg, cg = g.multigrid_mudpack(rhs, kx2)
+    po, so, co = o.poisson(rhs, kx2)
+    assert (sg["min_cycles"], sg["max_cycles"], sg["n_not_converged"]) == \
+        (so["min_cycles"], so["max_cycles"], so["n_not_converged"])
+    assert cg == co
+    for q in range(len(kx2)):
+        assert rel_l2(pg[q], po[q]) < 1e-12, q
+
+
+@pytest.mark.parametrize("case", ["small", "sheared", "refgrid"])
+def test_rem_div_matches_oracle(case):
+    p, g, o = pair(case)
+    g.rem_div_curv()
+    o.rem_div()
+    compare_state(g, o, 1e-12)
+    assert rel_l2(g.get_field(EK_F_CR1), o.get_field(EK_F_CR1)) < 1e-12
+    assert g.divergence() == pytest.approx(o.divergence(), rel=1e-6, abs=1e-14)
+
+
+@pytest.mark.parametrize("case", ["small", "sheared", "refgrid"])
+def test_three_substeps_match_oracle(case):
+    p, g, o = pair(case)
+    for rk in (1, 2, 3):
+        g.rk_duct(rk)
+        o.rk_substep(rk)
+        compare_state(g, o, 1e-11)
+        for f in (EK_F_CF1, EK_F_CF2, EK_F_CF3, EK_F_CFTH, EK_F_CR1):
+            assert rel_l2(g.get_field(f), o.get_field(f)) < 1e-11, (rk, f)
+        assert g.mg_stats()["max_cycles"] == o.mg_stats()["max_cycles"]
+
+
+def test_hundred_steps_neutral_64():
+    """The CPU-runnable neutral case (64 x 65 x 65, 100 RK3 steps,
+    dt = 1e-3): FP64 path within 1e-10 relative L2 of the oracle."""
+    w = WORKLOADS["ekman_neutral_64x65x65"]
+    p, g, o = pair(workload_setup(w))
+    g.rem_div_curv()
+    o.rem_div()
+    g.step(100)
+    o.step(100)
+    compare_state(g, o, 1e-10)
+    assert g.divergence() < 1e-8
+
+
+def test_quirk_phi_fp32():
+    """Q1: phi rounded to REAL*4 before the projection (duct.F90:2664)."""
+    p, g, o = pair("small", quirk_phi_fp32=1)
+    g.step(2)
+    o.step(2)
+    compare_state(g, o, 1e-6)
+
+
+def test_nan_state_reports_error():
+    p, g, o = pair("small")
+    cu = g.download()
+    cu[0][3, 3, 1] = np.nan
+    g.upload(*cu)
+    with pytest.raises(Exception) as e:
+        g.step(1)
+    assert "NAN" in str(e.value)
