@@ -1,0 +1,360 @@
+"""Benchmark of the GB300 RK3 duct step (RK_DUCT x 3 with REM_DIV_CURV).
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+Workload: the stratified Ekman layer 256 x 257 x 193 (NX x NY+2 x NZ+2),
+Re = 800, Pr = 0.7, Ri = 0.1, dt = 5e-4, seeded synthetic fields (laminar
+Ekman spiral + 1% Gaussian noise), FP64, every per-kx Poisson problem driven
+to a relative residual of 1e-8 (the singular kx = 0 mode keeps MUDPACK's own
+rule).  Prints one JSON line: RK3 steps/s over K steps after W warm-up steps,
+timed with CUDA events on the solver's stream; the fields are larger than
+the 126 MB L2, so no flush is needed between steps.  For N > 1 each rank
+runs an independent replica on its own GPU (the path does not shard) and
+the value is the sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+WORKLOAD = "ekman_strat_256x257x193"
+MG_TOL = 1e-8
+METRIC = "RK3 steps/s and Poisson solves/s at 1e-8 residual: learned+batched vs plain, 1 GB300"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------------------
+# clocks during the timed region
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.path or not os.path.exists(self.path):
+            return out
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return out
+        sm = [float(r[1]) for r in rows]
+        out["sm_mhz"] = statistics.median(sm)
+        out["sm_max_mhz"] = float(rows[0][2])
+        out["samples"] = len(rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        out["reasons"] = sorted(reasons)
+        return out
+
+
+# ----------------------------------------------------------------------------
+def setup_solver(device_index: int):
+    import torch
+
+    from ekman_bl_gb300 import build as ekbuild
+    from ekman_bl_gb300.duct import DuctSolver, metrics_from_grid
+    from ekman_bl_gb300.params import EK_MG_STOP_RESIDUAL, WORKLOADS, workload_setup
+
+    ekbuild.build()
+    torch.cuda.set_device(device_index)
+    w = WORKLOADS[WORKLOAD]
+    w.mg_tol = MG_TOL
+    p, xp, yp, state = workload_setup(w, EK_MG_STOP_RESIDUAL)
+    solver = DuctSolver(p, metrics_from_grid(p, xp, yp))
+    stream = torch.cuda.Stream()
+    solver.set_stream(stream.cuda_stream)
+    solver.upload(*state)
+    solver.rem_div_curv()   # CREATE_FLOW_DUCT projects the initial field (duct.F90:3189)
+    return w, p, xp, yp, state, solver, stream
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    w, p, xp, yp, state, solver, stream = setup_solver(local)
+    L0 = solver.launch_count()
+
+    # warm-up
+    for _ in range(args.warmup):
+        solver.step(1)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    mg_cycles = []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        n0 = solver.launch_count()
+        with torch.cuda.stream(stream):
+            start.record(stream)
+            for _ in range(args.steps):
+                solver.step(1)
+                mg_cycles.append(solver.mg_stats()["max_cycles"])
+            end.record(stream)
+        torch.cuda.synchronize()
+        launches = solver.launch_count() - n0
+    if world > 1:
+        dist.barrier()
+    ms = start.elapsed_time(end)
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    clocks = clk.summary()
+    value = world * args.steps / (ms_max / 1000.0)
+    div = solver.divergence()
+
+    # per-kernel-class timing of one extra step (events around every launch)
+    solver.set_timing(True)
+    solver.step(1)
+    kt = solver.timing()
+    solver.set_timing(False)
+    ktot = sum(v[0] for v in kt.values())
+
+    # Poisson solves/s: one batched solve of every active kx (real and
+    # imaginary parts together = one complex problem) at 1e-8
+    nkx = p.nx // 3
+    ncomplex = nkx + 1
+    kx2 = torch.tensor([(2 * math.pi * (q // 2) / p.lx) ** 2 for q in range(2 * ncomplex)], dtype=torch.float64,
+                       device="cuda")
+    gen = torch.Generator(device="cpu").manual_seed(7)
+    rhs = torch.randn((2 * ncomplex, p.ny + 2, p.nz + 2), generator=gen, dtype=torch.float64)
+    rhs[:, 0, :] = 0
+    rhs[:, -1, :] = 0
+    rhs[:, :, 0] = 0
+    rhs[:, :, -1] = 0
+    rhs = rhs.cuda()
+    phi = torch.zeros_like(rhs)
+    torch.cuda.synchronize()
+    solver.multigrid_mudpack_device(rhs.data_ptr(), phi.data_ptr(), kx2.data_ptr(), 2 * ncomplex)
+    torch.cuda.synchronize()
+    npois = 3
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for _ in range(npois):
+            pst, _ = solver.multigrid_mudpack_device(rhs.data_ptr(), phi.data_ptr(), kx2.data_ptr(), 2 * ncomplex)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    pois_ms = e0.elapsed_time(e1) / npois
+    solves_per_s = ncomplex / (pois_ms / 1000.0)
+
+    # end to end through the public C ABI with host buffers: H2D of the
+    # state from pinned memory, one RK3 step, D2H of the state
+    shape = (p.ny + 2, p.nz + 2, p.nx // 2 + 1)
+    pinned = [torch.empty(shape, dtype=torch.complex128, pin_memory=True).numpy() for _ in range(5)]
+    cur = solver.download()
+    for a, b in zip(pinned, cur):
+        a[...] = b
+    n_e2e = max(2, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        solver.upload(*pinned)
+        solver.step(1)
+        out = solver.download()
+        for a, b in zip(pinned, out):
+            a[...] = b
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / n_e2e
+    bytes_state = 5 * int(np.prod(shape)) * 16
+
+    result = None
+    if rank == 0:
+        peak, peak_kind = peaks()
+        # dominant kernel class: achieved = its algorithmic HBM bytes (counted
+        # per launch by the library) / its CUDA-event time
+        name, (dms, dcnt, dbytes) = max(kt.items(), key=lambda kv: kv[1][0])
+        roof = None
+        if dcnt > 0 and dms > 0:
+            achieved = dbytes / (dms / 1000.0) / 1e9
+            roof = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
+                    "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                    "traffic": None, "algorithmic_bytes_per_launch": int(dbytes / dcnt),
+                    "avg_launch_us": round(dms * 1000.0 / dcnt, 3), "launches_per_step": dcnt,
+                    "share_of_step": round(dms / ktot, 4)}
+        per_class_gbs = {k: round(v[2] / (v[0] / 1000.0) / 1e9, 1) for k, v in kt.items() if v[0] > 0}
+        result = {
+            "metric": METRIC,
+            "value": round(value, 4),
+            "unit": "RK3 steps/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": round(ms_max / args.steps, 3),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic (seeded laminar Ekman spiral + 1% Gaussian noise; no reference dataset exists)",
+            "config": {"workload": WORKLOAD, "nx": p.nx, "ny_plus_2": p.ny + 2, "nz_plus_2": p.nz + 2,
+                       "re": w.re, "pr": w.pr, "ri": w.ri, "delta_t": p.delta_t, "precision": "fp64 plain",
+                       "poisson": f"MUDPACK FMG + W(2,1), 4-colour GS, relative residual {MG_TOL:g}",
+                       "mg_cycles_per_substep_max": max(mg_cycles) if mg_cycles else None,
+                       "l2": "fields (100 MB each, ~2.5 GB resident) exceed the 126 MB L2; no flush",
+                       "parallelism": f"replicas x{world}"},
+            "poisson_solves_per_s": round(solves_per_s, 2),
+            "poisson_batch": {"complex_problems": ncomplex, "ms": round(pois_ms, 3),
+                              "max_cycles": pst["max_cycles"], "unit": "complex kx problems/s"},
+            "divergence_after_projection": div,
+            "clocks": clocks,
+            "gpu_launches": int(launches),
+            "kernel_ms_per_step": {k: round(v[0], 3) for k, v in kt.items()},
+            "kernel_algorithmic_gbs": per_class_gbs,
+            "kernel_launches_per_step": {k: v[1] for k, v in kt.items()},
+            "e2e": {"value": round(world / e2e_s, 4), "unit": "RK3 steps/s",
+                    "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state,
+                    "steps": n_e2e},
+            "roofline": roof,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            result["cpu_baseline"] = cpu_baseline(args)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    solver.close()
+    return result
+
+
+def cpu_baseline(args, nsteps: int = 1):
+    """The CPU oracle (a restatement of the reference's Fortran; the Fortran
+    itself cannot be built here) on this host's cores, on a bounded sample:
+    nsteps RK3 steps of the same workload after the initial projection."""
+    from ekman_bl_gb300.params import EK_MG_STOP_RESIDUAL, WORKLOADS, workload_setup
+    from oracle import ekref
+
+    cores = os.cpu_count() or 1
+    w = WORKLOADS[WORKLOAD]
+    w.mg_tol = MG_TOL
+    p, xp, yp, state = workload_setup(w, EK_MG_STOP_RESIDUAL)
+    o = ekref.Oracle(p, ekref.metrics_from_grid(p, xp, yp), threads=cores)
+    o.upload(*state)
+    o.rem_div()
+    t0 = time.perf_counter()
+    o.step(nsteps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": round(nsteps / dt, 5), "unit": "RK3 steps/s", "cores": cores, "kind": "port",
+            "sample": f"{nsteps} RK3 step(s) of {WORKLOAD} after the initial projection, "
+                      f"{cores} OpenMP threads ({dt:.1f} s)"}
+
+
+def run_reference(args):
+    """Reference arm: the oracle (CPU restatement of the reference path) on
+    all host cores, same workload/metric; each step a full RK3 step, at most
+    3 timed steps and 1 warm-up so the run stays within minutes."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    from ekman_bl_gb300.params import EK_MG_STOP_RESIDUAL, WORKLOADS, workload_setup
+    from oracle import ekref
+
+    ekref.build()
+    cores = os.cpu_count() or 1
+    w = WORKLOADS[WORKLOAD]
+    w.mg_tol = MG_TOL
+    p, xp, yp, state = workload_setup(w, EK_MG_STOP_RESIDUAL)
+    o = ekref.Oracle(p, ekref.metrics_from_grid(p, xp, yp), threads=cores)
+    o.upload(*state)
+    o.rem_div()
+    for _ in range(min(args.warmup, 1)):
+        o.step(1)
+    nsteps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    o.step(nsteps)
+    dt = time.perf_counter() - t0
+    o.close()
+    v = nsteps / dt
+    sample = f"{nsteps} RK3 step(s) of {WORKLOAD}, {cores} OpenMP threads ({dt:.1f} s)"
+    return {
+        "metric": METRIC, "value": round(v, 5), "unit": "RK3 steps/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": nsteps, "warmup": min(args.warmup, 1), "ms_per_step": round(1000 * dt / nsteps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded laminar Ekman spiral + 1% Gaussian noise)",
+        "config": {"workload": WORKLOAD, "precision": "fp64", "poisson": f"relative residual {MG_TOL:g}"},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(v, 5), "unit": "RK3 steps/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(v, 5), "unit": "RK3 steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gpu":
+        args.warmup = 3
+    res = run_reference(args) if args.impl == "reference" else run_gpu(args)
+    if res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -578,18 +578,19 @@ const char *ekgpu_timing_class_name(int k) { return (k >= 0 && k < KC_N) ? kKCla
 int ekgpu_set_timing(ek_ctx *h, int on) {
   return guarded(h, [&](Ctx &c) {
     timing_resolve(c);
-    for (int k = 0; k < KC_N; ++k) { c.kms[k] = 0.0; c.kcnt[k] = 0; }
+    for (int k = 0; k < KC_N; ++k) { c.kms[k] = 0.0; c.kcnt[k] = 0; c.kbytes[k] = 0.0; }
     c.timing = on != 0;
     return (int)EK_OK;
   });
 }
 
-int ekgpu_get_timing(ek_ctx *h, double *ms, long long *count, int n) {
+int ekgpu_get_timing(ek_ctx *h, double *ms, long long *count, double *bytes, int n) {
   return guarded(h, [&](Ctx &c) {
     timing_resolve(c);
     for (int k = 0; k < n && k < KC_N; ++k) {
       if (ms) ms[k] = c.kms[k];
       if (count) count[k] = c.kcnt[k];
+      if (bytes) bytes[k] = c.kbytes[k];
     }
     return (int)KC_N;
   });

@@ -205,7 +205,9 @@ void launch_r2c(Ctx &c, const R2cArgs &a) {
   if (nlines <= 0) return;
   const unsigned grid = (unsigned)((nlines + kWarpsPerBlock - 1) / kWarpsPerBlock);
   const size_t smem = sizeof(double2) * fc.M * kWarpsPerBlock;
-  KScope ks(c, KC_R2C);
+  const int nops = (a.pro == PRO_LOAD) ? 1 : (a.pro == PRO_PROD) ? 2 : 3;
+  const double epi = (a.epi == EPI_STORE) ? 16.0 * (c.d.NX2P + 1) : 32.0 * (c.d.NKX + 1);
+  KScope ks(c, KC_R2C, nlines * (8.0 * c.d.NX * nops + epi));
   k_r2c<<<grid, 32 * kWarpsPerBlock, smem, c.stream>>>(fc, a);
   after_launch(c);
 }
@@ -216,7 +218,7 @@ void launch_c2r(Ctx &c, const C2rArgs &a) {
   if (nlines <= 0) return;
   const unsigned grid = (unsigned)((nlines + kWarpsPerBlock - 1) / kWarpsPerBlock);
   const size_t smem = sizeof(double2) * fc.M * kWarpsPerBlock;
-  KScope ks(c, KC_C2R);
+  KScope ks(c, KC_C2R, nlines * (16.0 * (c.d.NKX + 1) * (a.src2 ? 2 : 1) + 8.0 * (c.d.NX + 2)));
   k_c2r<<<grid, 32 * kWarpsPerBlock, smem, c.stream>>>(fc, a);
   after_launch(c);
 }

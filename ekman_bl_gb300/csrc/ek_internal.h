@@ -148,6 +148,7 @@ struct Ctx {
   std::vector<cudaEvent_t> evpool;
   double kms[KC_N] = {};
   long long kcnt[KC_N] = {};
+  double kbytes[KC_N] = {};
 };
 
 // Records CUDA events around the launches in its scope when timing is on.
@@ -165,8 +166,10 @@ struct KScope {
     cudaEventCreate(&e);
     return e;
   }
-  KScope(Ctx &ctx, int k) : c(ctx), cls(k) {
+  // bytes: algorithmic HBM bytes the launches in this scope must move
+  KScope(Ctx &ctx, int k, double bytes = 0.0) : c(ctx), cls(k) {
     if (!c.timing) return;
+    c.kbytes[k] += bytes;
     a = get();
     b = get();
     cudaEventRecord(a, c.stream);

@@ -328,44 +328,73 @@ __global__ void k_prolong_y(MgDev g, int level, int intpol, int mode) {
 __device__ __forceinline__ void atomic_max_pos(double *a, double v) {
   atomicMax(reinterpret_cast<unsigned long long *>(a), (unsigned long long)__double_as_longlong(v));
 }
-__global__ void k_check_reduce(MgDev g) {
+// Thread block = 32 consecutive problems x 8 point slices: a warp reads 32
+// problems of one point (coalesced); per-problem partial maxima and sums are
+// combined in shared memory and leave the block with one atomic each.
+constexpr int kChkY = 8;
+__global__ void __launch_bounds__(32 * kChkY) k_check_reduce(MgDev g) {
   if (*g.alldone) return;
   const LvDev L = g.lv[g.ngrid - 1];
   const int P = g.P;
+  const int p = blockIdx.x * 32 + threadIdx.x;
+  const int ty = threadIdx.y;
   const size_t npt = (size_t)L.nx * L.ny;
-  const long n = (long)npt * P;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-    const int p = (int)(t % P);
-    if (g.done[p]) continue;
-    const long pt = t / P;
-    const int i = 1 + (int)(pt % L.nx), j = 1 + (int)(pt / L.nx);
-    const double v = PH(L, P, i, j, p);
-    if (g.stop_rule == 0) {
-      const double old = g.phif[pt * P + p];
-      atomic_max_pos(&g.red[2 * p], fabs(v));
-      atomic_max_pos(&g.red[2 * p + 1], fabs(v - old));
-    } else {
-      const size_t si = P, sj = (size_t)(L.nx + 2) * P;
+  double m0 = 0.0, m1 = 0.0, s2 = 0.0, s3 = 0.0;
+  const bool act = (p < P) && !g.done[p];
+  if (act) {
+    const size_t si = P, sj = (size_t)(L.nx + 2) * P;
+    const double kx2 = g.kx2[p];
+    for (size_t pt = (size_t)blockIdx.y * kChkY + ty; pt < npt; pt += (size_t)gridDim.y * kChkY) {
+      const int i = 1 + (int)(pt % L.nx), j = 1 + (int)(pt / L.nx);
       const double *ph = &PH(L, P, i, j, p);
-      const double *cf = L.cof;
-      double s = cf[pt] * ph[si];
-      s = s + cf[npt + pt] * ph[si + sj];
-      s = s + cf[2 * npt + pt] * ph[sj];
-      s = s + cf[3 * npt + pt] * ph[sj - si];
-      s = s + cf[4 * npt + pt] * ph[-(long)si];
-      s = s + cf[5 * npt + pt] * ph[-(long)(si + sj)];
-      s = s + cf[6 * npt + pt] * ph[-(long)sj];
-      s = s + cf[7 * npt + pt] * ph[si - sj];
-      const double c9v = ((-g.kx2[p] * cf[10 * npt + pt]) - cf[8 * npt + pt]) + cf[9 * npt + pt];
-      s = s + c9v * ph[0];
-      const double b = L.rhs[pt * P + p];
-      const double r = b - s;
-      atomicAdd(&g.red[2 * p], b * b);
-      atomicAdd(&g.red[2 * p + 1], r * r);
+      const double v = ph[0];
+      const double old = g.phif[pt * P + p];
+      m0 = fmax(m0, fabs(v));
+      m1 = fmax(m1, fabs(v - old));
+      if (g.stop_rule == 1) {
+        const double *cf = L.cof;
+        double s = cf[pt] * ph[si];
+        s = s + cf[npt + pt] * ph[si + sj];
+        s = s + cf[2 * npt + pt] * ph[sj];
+        s = s + cf[3 * npt + pt] * ph[sj - si];
+        s = s + cf[4 * npt + pt] * ph[-(long)si];
+        s = s + cf[5 * npt + pt] * ph[-(long)(si + sj)];
+        s = s + cf[6 * npt + pt] * ph[-(long)sj];
+        s = s + cf[7 * npt + pt] * ph[si - sj];
+        const double c9v = ((-kx2 * cf[10 * npt + pt]) - cf[8 * npt + pt]) + cf[9 * npt + pt];
+        s = s + c9v * v;
+        const double b = L.rhs[pt * P + p];
+        const double r = b - s;
+        s2 += b * b;
+        s3 += r * r;
+      }
+      g.phif[pt * P + p] = v;
     }
-    g.phif[pt * P + p] = v;
+  }
+  __shared__ double red[4][kChkY][32];
+  red[0][ty][threadIdx.x] = m0;
+  red[1][ty][threadIdx.x] = m1;
+  red[2][ty][threadIdx.x] = s2;
+  red[3][ty][threadIdx.x] = s3;
+  __syncthreads();
+  if (ty == 0 && act) {
+    for (int y = 1; y < kChkY; ++y) {
+      m0 = fmax(m0, red[0][y][threadIdx.x]);
+      m1 = fmax(m1, red[1][y][threadIdx.x]);
+      s2 += red[2][y][threadIdx.x];
+      s3 += red[3][y][threadIdx.x];
+    }
+    atomic_max_pos(&g.red[4 * p], m0);
+    atomic_max_pos(&g.red[4 * p + 1], m1);
+    if (g.stop_rule == 1) {
+      atomicAdd(&g.red[4 * p + 2], s2);
+      atomicAdd(&g.red[4 * p + 3], s3);
+    }
   }
 }
+
+// Relative change (MUDPACK) or, for the residual rule, relative residual;
+// problems with ce = 0 (kx = 0, singular) keep the relative-change test.
 __global__ void k_check_finish(MgDev g, int iter, int last) {
   if (*g.alldone) return;
   __shared__ int active;
@@ -374,22 +403,32 @@ __global__ void k_check_finish(MgDev g, int iter, int last) {
   for (int p = threadIdx.x; p < g.P; p += blockDim.x) {
     if (g.done[p]) continue;
     g.cycles[p] = iter;
+    double relmax = g.red[4 * p + 1];
+    const double phmax = g.red[4 * p];
+    if (phmax > 0.0) relmax = relmax / phmax;
     bool conv;
     double meas;
     if (g.stop_rule == 0) {
-      double relmax = g.red[2 * p + 1];
-      const double phmax = g.red[2 * p];
-      if (phmax > 0.0) relmax = relmax / phmax;
       meas = relmax;
       conv = (g.tol > 0.0) && (relmax <= g.tol);
+    } else if (g.kx2[p] == 0.0) {
+      // singular mode: MULTIGRID_MUDPACK's own rule (REAL*4 1e-6, <= 6 cycles)
+      meas = relmax;
+      conv = relmax <= (double)1.0e-6f;
+      if (!conv && iter >= 6) {
+        g.done[p] = 2;  // stopped at the reference's cycle cap
+        continue;
+      }
     } else {
-      const double bn = sqrt(g.red[2 * p]);
-      meas = (bn > 0.0) ? sqrt(g.red[2 * p + 1]) / bn : 0.0;
+      const double bn = sqrt(g.red[4 * p + 2]);
+      meas = (bn > 0.0) ? sqrt(g.red[4 * p + 3]) / bn : 0.0;
       conv = meas <= g.tol;
     }
-    g.red[2 * p] = 0.0;
-    g.red[2 * p + 1] = 0.0;
-    g.red[2 * g.P + p] = meas;
+    g.red[4 * p] = 0.0;
+    g.red[4 * p + 1] = 0.0;
+    g.red[4 * p + 2] = 0.0;
+    g.red[4 * p + 3] = 0.0;
+    g.red[4 * g.P + p] = meas;
     if (conv) g.done[p] = 1;
     else atomicAdd(&active, 1);
   }
@@ -655,7 +694,7 @@ void mg_alloc(Ctx &c, int pmax) {
   const size_t phif_off = tot;
   tot += (size_t)P.nfx * P.nfy * pmax;
   const size_t red_off = tot;
-  tot += (size_t)3 * pmax + 8;
+  tot += (size_t)5 * pmax + 8;
   const size_t kx_off = tot;
   tot += pmax;
   EK_CUDA(cudaMalloc(&c.mg_pool, tot * sizeof(double)));
@@ -708,10 +747,10 @@ int mg_solve(Ctx &c, int nprob, const double *kx2_dev, ek_mg_stats *st) {
   const int bs = 256;
   cudaStream_t s = c.stream;
   EK_CUDA(cudaMemsetAsync(c.mg_done, 0, sizeof(int) * (2 * c.mg_pmax + 4), s));
-  EK_CUDA(cudaMemsetAsync(c.mg_red, 0, sizeof(double) * (3 * c.mg_pmax + 8), s));
+  EK_CUDA(cudaMemsetAsync(c.mg_red, 0, sizeof(double) * (5 * c.mg_pmax + 8), s));
   for (int l = 1; l <= PL.ngrid; ++l) {
     const long n = (long)PL.lv[l - 1].nx * PL.lv[l - 1].ny * nprob;
-    KScope ks(c, KC_MG_SETUP);
+    KScope ks(c, KC_MG_SETUP, 8.0 * n);
     k_inv9<<<nblk(n, bs), bs, 0, s>>>(g, l);
     after_launch(c);
   }
@@ -764,7 +803,12 @@ int mg_solve(Ctx &c, int nprob, const double *kx2_dev, ek_mg_stats *st) {
       while (e < nops && is_coarse(PL.ops[e])) ++e;
       A.ops = ops_dev_cached + o;
       A.nops = e - o;
-      KScope ks(c, KC_MG_COARSE);
+      double cb = 0.0;
+      for (int l = 1; l <= lc; ++l) {
+        const MgLevel &Lq = PL.lv[l - 1];
+        cb += 8.0 * nprob * (2.0 * (Lq.nx + 2) * (Lq.ny + 2) + 3.0 * Lq.nx * Lq.ny);
+      }
+      KScope ks(c, KC_MG_COARSE, cb);
       k_coarse<<<nprob, 256, smem, s>>>(A);
       after_launch(c);
       o = e;
@@ -773,7 +817,9 @@ int mg_solve(Ctx &c, int nprob, const double *kx2_dev, ek_mg_stats *st) {
     const MgLevel &L = PL.lv[op.level - 1];
     switch (op.kind) {
       case OP_TRSFC: {
-        KScope ks(c, KC_MG_SETUP);
+        double tb = 8.0 * PL.nfx * PL.nfy * nprob;
+        for (int l = 1; l <= PL.ngrid; ++l) tb += 8.0 * nprob * ((PL.lv[l - 1].nx + 2) * (PL.lv[l - 1].ny + 2) + 2.0 * PL.lv[l - 1].nx * PL.lv[l - 1].ny);
+        KScope ks(c, KC_MG_SETUP, tb);
         for (int l = 1; l <= PL.ngrid; ++l) {
           const size_t n = (size_t)(PL.lv[l - 1].nx + 2) * (PL.lv[l - 1].ny + 2) * nprob;
           k_zero<<<nblk((long)n, bs), bs, 0, s>>>(PL.lv[l - 1].phi, n);
@@ -792,7 +838,7 @@ int mg_solve(Ctx &c, int nprob, const double *kx2_dev, ek_mg_stats *st) {
         break;
       }
       case OP_RELAX: {
-        KScope ks(c, KC_MG_RELAX);
+        KScope ks(c, KC_MG_RELAX, 32.0 * L.nx * L.ny * nprob * op.count);
         const bool onwrite = PL.orth && (L.nx % 4 != 2);
         const int ncol = (L.nx + 3) / 4 + 1;
         for (int sw = 0; sw < op.count; ++sw)
@@ -811,7 +857,8 @@ int mg_solve(Ctx &c, int nprob, const double *kx2_dev, ek_mg_stats *st) {
         break;
       }
       case OP_RESTRICT: {
-        KScope ks(c, KC_MG_TRANSFER);
+        const MgLevel &Cq = PL.lv[op.level - 2];
+        KScope ks(c, KC_MG_TRANSFER, 8.0 * nprob * (4.0 * L.nx * L.ny + 2.0 * (Cq.nx + 2) * (Cq.ny + 2)));
         k_resid<<<nblk((long)L.nx * L.ny * nprob, bs), bs, 0, s>>>(g, op.level);
         after_launch(c);
         const MgLevel &C = PL.lv[op.level - 2];
@@ -821,7 +868,8 @@ int mg_solve(Ctx &c, int nprob, const double *kx2_dev, ek_mg_stats *st) {
       }
       case OP_COR2:
       case OP_PROLONG: {
-        KScope ks(c, KC_MG_TRANSFER);
+        KScope ks(c, KC_MG_TRANSFER, 8.0 * nprob * 4.0 * PL.lv[(op.kind == OP_COR2 ? op.level : op.level + 1) - 1].nx *
+                                         PL.lv[(op.kind == OP_COR2 ? op.level : op.level + 1) - 1].ny);
         const int fine = (op.kind == OP_COR2) ? op.level : op.level + 1;
         const int mode = (op.kind == OP_COR2) ? 0 : 1;
         const MgLevel &F = PL.lv[fine - 1];
@@ -833,10 +881,12 @@ int mg_solve(Ctx &c, int nprob, const double *kx2_dev, ek_mg_stats *st) {
         break;
       }
       case OP_CHECK: {
-        KScope ks(c, KC_MG_CHECK);
+        KScope ks(c, KC_MG_CHECK, 8.0 * nprob * PL.nfx * PL.nfy * (c.p.mg_stop == 1 ? 4.0 : 3.0));
         ++ncheck;
         const MgLevel &F = PL.lv[PL.ngrid - 1];
-        k_check_reduce<<<nblk((long)F.nx * F.ny * nprob, bs), bs, 0, s>>>(g);
+        const long npt = (long)F.nx * F.ny;
+        const int gy = (int)std::min<long>((npt + kChkY - 1) / kChkY, std::max<long>(1, 2048 / ((nprob + 31) / 32)));
+        k_check_reduce<<<dim3((nprob + 31) / 32, gy), dim3(32, kChkY), 0, s>>>(g);
         after_launch(c);
         k_check_finish<<<1, 256, 0, s>>>(g, op.count, ncheck == maxcheck ? 1 : 0);
         after_launch(c);
@@ -852,7 +902,7 @@ int mg_solve(Ctx &c, int nprob, const double *kx2_dev, ek_mg_stats *st) {
   std::vector<double> meas(nprob);
   EK_CUDA(cudaMemcpyAsync(cyc.data(), c.mg_cycles, sizeof(int) * nprob, cudaMemcpyDeviceToHost, s));
   EK_CUDA(cudaMemcpyAsync(done.data(), c.mg_done, sizeof(int) * nprob, cudaMemcpyDeviceToHost, s));
-  EK_CUDA(cudaMemcpyAsync(meas.data(), c.mg_red + 2 * nprob, sizeof(double) * nprob, cudaMemcpyDeviceToHost, s));
+  EK_CUDA(cudaMemcpyAsync(meas.data(), c.mg_red + 4 * nprob, sizeof(double) * nprob, cudaMemcpyDeviceToHost, s));
   EK_CUDA(cudaStreamSynchronize(s));
   ek_mg_stats S{};
   S.nprob = nprob;
@@ -860,7 +910,7 @@ int mg_solve(Ctx &c, int nprob, const double *kx2_dev, ek_mg_stats *st) {
   for (int p = 0; p < nprob; ++p) {
     S.min_cycles = std::min(S.min_cycles, cyc[p]);
     S.max_cycles = std::max(S.max_cycles, cyc[p]);
-    if (!done[p]) S.n_not_converged++;
+    if (done[p] != 1) S.n_not_converged++;
     if (c.p.mg_stop == 0) S.max_relchange = std::max(S.max_relchange, meas[p]);
     else S.max_residual = std::max(S.max_residual, meas[p]);
   }

@@ -426,7 +426,7 @@ void launch_spectral_rhs(Ctx &c, int rk) {
   a.th = p.n_th > 0;
   a.cont_strat = p.cont_strat;
   dim3 grid((c.d.NX2P + 1 + 63) / 64, c.d.NZ2, c.d.NY2);
-  KScope ks(c, KC_SPECTRAL);
+  KScope ks(c, KC_SPECTRAL, 16.0 * c.d.nspec() * (5 + (rk > 1 ? 4 : 0) + 8));
   k_spectral_rhs<<<grid, 64, 0, c.stream>>>(a);
   after_launch(c);
 }
@@ -434,7 +434,7 @@ void launch_spectral_rhs(Ctx &c, int rk) {
 void launch_face_velocity(Ctx &c) {
   const Dims &d = c.d;
   dim3 grid((d.NX + 127) / 128, d.ZE - d.ZS + 2, d.JE - d.JS + 2);
-  KScope ks(c, KC_FACE);
+  KScope ks(c, KC_FACE, 32.0 * d.NX * (d.ZE - d.ZS + 2) * (d.JE - d.JS + 2));
   k_face_velocity<<<grid, 128, 0, c.stream>>>(d, c.m, c.U2, c.U3, c.U2b);
   after_launch(c);
 }
@@ -466,7 +466,7 @@ void launch_adi(Ctx &c, int field, int rk) {
   {
     const size_t smem = sizeof(double) * kAdiThreads * d.NY2;
     dim3 grid((d.NX + kAdiThreads - 1) / kAdiThreads, a.ze - a.zs + 1);
-    KScope ks(c, KC_ADI_Y);
+    KScope ks(c, KC_ADI_Y, 24.0 * d.NX * d.NY2 * (a.ze - a.zs + 1));
     k_adi_y<<<grid, kAdiThreads, smem, c.stream>>>(a);
     after_launch(c);
   }
@@ -479,7 +479,7 @@ void launch_adi(Ctx &c, int field, int rk) {
   {
     const size_t smem = sizeof(double) * kAdiThreads * d.NZ2;
     dim3 grid((d.NX + kAdiThreads - 1) / kAdiThreads, d.NY2);
-    KScope ks(c, KC_ADI_Z);
+    KScope ks(c, KC_ADI_Z, 32.0 * d.NX * d.NZ2 * (a.je - a.js + 1));
     k_adi_z<<<grid, kAdiThreads, smem, c.stream>>>(a);
     after_launch(c);
   }
@@ -488,14 +488,14 @@ void launch_adi(Ctx &c, int field, int rk) {
 void launch_th_corners(Ctx &c) {
   const int zmax1 = c.p.th_bc[EK_ZMAX] == 1, zmin6 = c.p.th_bc[EK_ZMIN] == 6;
   if (!zmax1 && !zmin6) return;
-  KScope ks(c, KC_ADI_Z);
+  KScope ks(c, KC_ADI_Z, 64.0 * c.d.NX);
   k_th_corners<<<(c.d.NX + 127) / 128, 128, 0, c.stream>>>(c.d, c.TH, zmax1, zmin6);
   after_launch(c);
 }
 
 void launch_divergence_rhs(Ctx &c, double *rhs, int P) {
   const Dims &d = c.d;
-  KScope ks(c, KC_DIVERGENCE);
+  KScope ks(c, KC_DIVERGENCE, 16.0 * d.nspec() * 4 + (16.0 * d.nspec() * 3 + 8.0 * P * d.NZ2 * d.NY2));
   dim3 g1((d.NX2P + 1 + 63) / 64, d.NZ2, d.NY2);
   k_rem_faces<<<g1, 64, 0, c.stream>>>(d, c.m, c.CU2, c.CU3, c.CU2b);
   after_launch(c);
@@ -508,7 +508,7 @@ void launch_projection(Ctx &c, const double *phif, int P, double temp4, bool upd
   const Dims &d = c.d;
   dim3 g0((d.NX2P + 1 + 63) / 64, d.NZ2, d.NY2);
   {
-  KScope ks(c, KC_PROJECTION);
+  KScope ks(c, KC_PROJECTION, 16.0 * d.nspec() * (1 + 1 + (update_p ? 2 : 0)) + 16.0 * d.nspec() * (5 + 7 + 4));
   k_phi_to_cr1<<<g0, 64, 0, c.stream>>>(d, phif, P, c.CR1, c.CP, temp4, update_p ? 1 : 0, c.p.quirk_phi_fp32);
   after_launch(c);
   dim3 g1((d.NX2P + 1 + 63) / 64, d.ZE - d.ZS + 1, d.JE - d.JS + 1);
@@ -527,7 +527,7 @@ void launch_projection(Ctx &c, const double *phif, int P, double temp4, bool upd
   ca.k0 = 2;
   ca.k1 = d.NZ - 1;
   launch_c2r(c, ca);
-  KScope ks(c, KC_DIVERGENCE);
+  KScope ks(c, KC_DIVERGENCE, 8.0 * (d.NX + 2) * (d.NZ - 2) * (d.NY - 2));
   k_div_sum<<<d.NY - 2, 256, 0, c.stream>>>(d, c.SPH, c.div_part);
   after_launch(c);
 }

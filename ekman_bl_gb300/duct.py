@@ -74,7 +74,7 @@ def load_library():
     L.ekgpu_launch_count.argtypes = [V]
     L.ekgpu_launch_count.restype = C.c_longlong
     L.ekgpu_set_timing.argtypes = [V, C.c_int]
-    L.ekgpu_get_timing.argtypes = [V, _D, C.POINTER(C.c_longlong), C.c_int]
+    L.ekgpu_get_timing.argtypes = [V, _D, C.POINTER(C.c_longlong), _D, C.c_int]
     L.ekgpu_timing_class_name.argtypes = [C.c_int]
     L.ekgpu_timing_class_name.restype = C.c_char_p
     _lib = L
@@ -209,11 +209,13 @@ class DuctSolver:
         self._check(self._L.ekgpu_set_timing(self._h, 1 if on else 0))
 
     def timing(self) -> dict:
-        """Per-kernel-class totals {name: (ms, launches)} since set_timing."""
+        """Per-kernel-class totals {name: (ms, launches, algorithmic bytes)}
+        since set_timing."""
         n = 32
         ms = (C.c_double * n)()
         cnt = (C.c_longlong * n)()
-        k = self._L.ekgpu_get_timing(self._h, ms, cnt, n)
+        by = (C.c_double * n)()
+        k = self._L.ekgpu_get_timing(self._h, ms, cnt, by, n)
         if k < 0:
             self._check(k)
-        return {self._L.ekgpu_timing_class_name(i).decode(): (ms[i], int(cnt[i])) for i in range(k)}
+        return {self._L.ekgpu_timing_class_name(i).decode(): (ms[i], int(cnt[i]), by[i]) for i in range(k)}

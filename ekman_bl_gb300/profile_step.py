@@ -1,0 +1,50 @@
+"""Run one RK3 step of a named workload for profiling.
+
+    python -m ekman_bl_gb300.profile_step [--workload NAME] [--warmup W] [--tol T]
+
+Sets up the workload, runs W warm-up steps, then exactly one RK3 step, and
+prints the number of kernel launches issued before that step and inside it,
+so that an ncu launch list can bracket the step with -s/-c.  With
+--timing it also prints the per-kernel-class CUDA-event times of the step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+from . import build as ekbuild
+from .duct import DuctSolver, metrics_from_grid
+from .params import EK_MG_STOP_RELCHANGE, EK_MG_STOP_RESIDUAL, WORKLOADS, workload_setup
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="ekman_strat_256x257x193", choices=sorted(WORKLOADS))
+    ap.add_argument("--warmup", type=int, default=1)
+    ap.add_argument("--tol", type=float, default=1e-8, help="relative residual; 0 = MUDPACK's own rule")
+    ap.add_argument("--timing", action="store_true")
+    args = ap.parse_args()
+    ekbuild.build()
+    w = WORKLOADS[args.workload]
+    stop = EK_MG_STOP_RESIDUAL if args.tol > 0 else EK_MG_STOP_RELCHANGE
+    if args.tol > 0:
+        w.mg_tol = args.tol
+    p, xp, yp, state = workload_setup(w, stop)
+    s = DuctSolver(p, metrics_from_grid(p, xp, yp))
+    s.upload(*state)
+    s.rem_div_curv()
+    s.step(args.warmup)
+    before = s.launch_count()
+    if args.timing:
+        s.set_timing(True)
+    s.step(1)
+    inside = s.launch_count() - before
+    out = {"workload": args.workload, "launches_before_step": before, "launches_in_step": inside,
+           "mg": s.mg_stats(), "divergence": s.divergence()}
+    if args.timing:
+        out["timing"] = {k: {"ms": round(v[0], 3), "launches": v[1], "alg_bytes": v[2]} for k, v in s.timing().items()}
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -52,7 +52,10 @@ enum { EK_YMIN = 0, EK_YMAX = 1, EK_ZMIN = 2, EK_ZMAX = 3 };
 /* Multigrid stopping rule. */
 enum {
   EK_MG_STOP_RELCHANGE = 0,  /* MUDPACK rule: max|phi_k - phi_{k-1}| / max|phi_k| <= tol (mud2cr.f:301-326) */
-  EK_MG_STOP_RESIDUAL = 1    /* ||b - A phi||_2 / ||b||_2 <= tol, per real 2-D problem                  */
+  EK_MG_STOP_RESIDUAL = 1    /* ||b - A phi||_2 / ||b||_2 <= tol, per real 2-D problem.  A problem with
+                                kx^2 = 0 (singular: periodic x, Neumann y; its right-hand side need
+                                not be compatible) keeps MULTIGRID_MUDPACK's own rule instead:
+                                REAL*4 1e-6 relative change, at most 6 cycles                      */
 };
 
 /* Run parameters: the values the Fortran driver reads from input.dat and
@@ -202,12 +205,13 @@ long long ekgpu_launch_count(const ek_ctx *ctx);
 
 /* Optional per-kernel-class timer (CUDA events around every launch on the
  * context's stream).  ekgpu_set_timing clears the totals; get_timing fills
- * up to n classes (milliseconds and launch counts) and returns the number
+ * up to n classes (milliseconds, launch counts and the algorithmic HBM bytes
+ * those launches must move, for roofline fractions) and returns the number
  * of classes; ekgpu_timing_class_name names class k.  Profiling aid with no
  * counterpart in the reference (it only prints a wall clock,
  * diablo.F90:171-176). */
 int ekgpu_set_timing(ek_ctx *ctx, int on);
-int ekgpu_get_timing(ek_ctx *ctx, double *ms, long long *count, int n);
+int ekgpu_get_timing(ek_ctx *ctx, double *ms, long long *count, double *bytes, int n);
 const char *ekgpu_timing_class_name(int k);
 
 #ifdef __cplusplus

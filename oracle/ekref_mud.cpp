@@ -361,7 +361,7 @@ void Mud2cr::kcymd2cr(int kcur) {
 }
 
 // mud2cr1 (mud2cr.f:211-338) with swk2 (mudcom.f:32-59).
-MudResult Mud2cr::solve(const double *rhsf, double *phif) {
+MudResult Mud2cr::solve(const double *rhsf, double *phif, bool singular) {
   MudResult r;
   const int nfx = nfx_, nfy = nfy_;
   auto PF = [&](int i, int j) -> double & { return phif[(size_t)(j - 1) * nfx + (i - 1)]; };
@@ -392,11 +392,17 @@ MudResult Mud2cr::solve(const double *rhsf, double *phif) {
       for (int i = 1; i <= nfx; ++i) bnorm += F.C(i, j, 10) * F.C(i, j, 10);
     bnorm = std::sqrt(bnorm);
   }
-  for (int iter = 1; iter <= o_.maxcy; ++iter) {
+  // Under the residual rule a singular problem keeps MULTIGRID_MUDPACK's own
+  // rule: REAL*4 10.0**(-6) relative change, at most 6 cycles
+  // (mg_solver2d.F90:146-199).
+  const bool rel = (o_.stop_rule == 0 || singular);
+  const double tol = (o_.stop_rule == 0) ? o_.tol : (double)1.0e-6f;
+  const int maxcy = (o_.stop_rule == 0 || !singular) ? o_.maxcy : std::min(o_.maxcy, 6);
+  for (int iter = 1; iter <= maxcy; ++iter) {
     r.cycles = iter;
     kcymd2cr(kcur);
-    if (o_.stop_rule == 0) {
-      if (o_.tol > 0.0) {
+    if (rel) {
+      if (tol > 0.0) {
         double relmax = 0.0, phmax = 0.0;
         for (int j = 1; j <= nfy; ++j)
           for (int i = 1; i <= nfx; ++i) {
@@ -406,7 +412,7 @@ MudResult Mud2cr::solve(const double *rhsf, double *phif) {
           }
         if (phmax > 0.0) relmax = relmax / phmax;
         r.relmax = relmax;
-        if (relmax <= o_.tol) { r.converged = true; return r; }
+        if (relmax <= tol) { r.converged = true; return r; }
       }
     } else {
       double rn = 0.0;

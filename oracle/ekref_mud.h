@@ -36,7 +36,9 @@ class Mud2cr {
   void discretize(const CoefFn &coef);
   // intl=1 call: rhsf, phif are (nfx, nfy) column-major; phif is input guess
   // (the reference always passes zeros) and output solution.
-  MudResult solve(const double *rhsf, double *phif);
+  // singular: the problem has ce = 0 (kx = 0, pure Neumann/periodic); under
+  // the residual rule it uses the relative-change test instead.
+  MudResult solve(const double *rhsf, double *phif, bool singular = false);
   // out = A phi at the finest level on (1..nfx, 1..nfy).
   void apply_finest(const double *phif, double *out) const;
   int nfx() const { return nfx_; }

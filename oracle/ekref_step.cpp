@@ -515,7 +515,7 @@ static int mg_batch(ekref_ctx *c, const double *rhs, double *phi, const double *
     for (int p = 0; p < nprob; ++p) {
       mg.discretize(make_cofcr(c, kx2[p]));
       std::fill(phi + p * n, phi + (p + 1) * n, 0.0);  // P_TMP = 0
-      res[p] = mg.solve(rhs + p * n, phi + p * n);
+      res[p] = mg.solve(rhs + p * n, phi + p * n, kx2[p] == 0.0);
     }
   }
   ek_mg_stats s{};
