@@ -19,6 +19,7 @@ struct ek_ctx {
 namespace ek {
 void rk_init_attributes();
 void fft_init_attributes();
+const char *last_global_error();
 }  // namespace ek
 
 namespace {
@@ -342,7 +343,7 @@ void ekgpu_destroy(ek_ctx *h) {
   delete h;
 }
 
-const char *ekgpu_last_error(const ek_ctx *h) { return h ? h->c.err.c_str() : "null context"; }
+const char *ekgpu_last_error(const ek_ctx *h) { return h ? h->c.err.c_str() : ek::last_global_error(); }
 
 int ekgpu_set_stream(ek_ctx *h, void *stream) {
   return guarded(h, [&](Ctx &c) {

@@ -17,6 +17,10 @@
 //            EPI_ADD   dst += X            (duct.F90:779-785)
 //            EPI_SUB_IK dst -= i kx X      (duct.F90:712-718)
 // so no product or transform temporary ever reaches HBM.
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "ek_internal.h"
 
 namespace ek {
@@ -234,3 +238,134 @@ void fft_init_attributes() {
   done = true;
 }
 }  // namespace ek
+
+// ---------------------------------------------------------------------------
+// Context-free batched x-transforms: the FFT_X_TO_FOURIER_OP /
+// FFT_X_TO_PHYSICAL_OP pair that the reference calls (e.g. duct.F90:700 and
+// mpi_duct.F90:308) and whose source (fft.F90) is missing from its tree.
+namespace ek {
+namespace {
+
+thread_local std::string t_last_error;
+
+__global__ void k_twiddles(double2 *tw_m, double2 *tw_n, int nx) {
+  const int M = nx / 2;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t <= M; t += gridDim.x * blockDim.x) {
+    double s, c;
+    if (t < M / 2) {
+      sincospi(-2.0 * t / M, &s, &c);
+      tw_m[t] = make_double2(c, s);
+    }
+    sincospi(-2.0 * t / nx, &s, &c);
+    tw_n[t] = make_double2(c, s);
+  }
+}
+
+bool fft_args_ok(int nx, int nkx, long nlines, const void *in, const void *out) {
+  if (nx < 8 || nx > 1024 || (nx & (nx - 1))) {
+    t_last_error = "nx must be a power of two in [8, 1024]";
+    return false;
+  }
+  if (nkx < 0 || nkx >= nx / 2) {
+    t_last_error = "nkx must be in [0, nx/2)";
+    return false;
+  }
+  if (nlines < 0 || nlines > (1L << 30) || (nlines > 0 && (!in || !out))) {
+    t_last_error = "bad line count or NULL buffer";
+    return false;
+  }
+  return true;
+}
+
+// Twiddle tables of the context-free transforms: cudaMalloc'd once per
+// (device, nx) and kept for the life of the process.
+double2 *cached_twiddles(int nx, cudaStream_t s) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, double2 *> cache;
+  int dev = 0;
+  EK_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find({dev, nx});
+  if (it != cache.end()) return it->second;
+  const int M = nx / 2;
+  double2 *tw = nullptr;
+  EK_CUDA(cudaMalloc(&tw, sizeof(double2) * (M / 2 + M + 1)));
+  k_twiddles<<<4, 256, 0, s>>>(tw, tw + M / 2, nx);
+  EK_CUDA(cudaPeekAtLastError());
+  EK_CUDA(cudaStreamSynchronize(s));
+  cache[{dev, nx}] = tw;
+  return tw;
+}
+
+FftConst standalone_const(int nx, int nkx, long nlines, const double2 *tw) {
+  FftConst f{};
+  Dims &d = f.d;
+  d.NX = nx;
+  d.NKX = nkx;
+  d.NX2P = nx / 2;
+  d.LDX = nx + 2;
+  d.LDC = nx / 2 + 1;
+  d.NZ2 = (int)nlines;  // lines are indexed as (k, j = 0)
+  d.NY2 = 1;
+  f.M = nx / 2;
+  int lg = 0;
+  while ((1 << lg) < f.M) ++lg;
+  f.logM = lg;
+  f.tw_m = tw;
+  f.tw_n = tw + f.M / 2;
+  return f;
+}
+
+int run_standalone(bool forward, int nx, int nkx, long nlines, const double *in, double *out, cudaStream_t s,
+                   const double2 *tw) {
+  if (nlines == 0) return EK_OK;
+  const FftConst fc = standalone_const(nx, nkx, nlines, tw);
+  const unsigned grid = (unsigned)((nlines + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  const size_t smem = sizeof(double2) * fc.M * kWarpsPerBlock;
+  if (forward) {
+    R2cArgs a{};
+    a.a = in;
+    a.dst = reinterpret_cast<cplx_t *>(out);
+    a.pro = PRO_LOAD;
+    a.epi = EPI_STORE;
+    a.k0 = 0; a.k1 = (int)nlines - 1; a.j0 = 0; a.j1 = 0;
+    k_r2c<<<grid, 32 * kWarpsPerBlock, smem, s>>>(fc, a);
+  } else {
+    C2rArgs a{};
+    a.src = reinterpret_cast<const cplx_t *>(in);
+    a.dst = out;
+    a.k0 = 0; a.k1 = (int)nlines - 1; a.j0 = 0; a.j1 = 0;
+    k_c2r<<<grid, 32 * kWarpsPerBlock, smem, s>>>(fc, a);
+  }
+  EK_CUDA(cudaPeekAtLastError());
+  return EK_OK;
+}
+
+int standalone(bool forward, int nx, int nkx, long nlines, const double *in, double *out, void *stream) {
+  if (!fft_args_ok(nx, nkx, nlines, in, out)) return EK_ERR_ARG;
+  try {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    fft_init_attributes();
+    const double2 *tw = cached_twiddles(nx, s);
+    return run_standalone(forward, nx, nkx, nlines, in, out, s, tw);
+  } catch (const CudaError &e) {
+    t_last_error = e.msg;
+    return EK_ERR_CUDA;
+  }
+}
+
+}  // namespace
+
+const char *last_global_error() { return t_last_error.c_str(); }
+
+}  // namespace ek
+
+extern "C" int ekgpu_fft_x_to_fourier(int nx, int nkx, long nlines, const double *in_dev, double *out_dev,
+                                      void *stream) {
+  return ek::standalone(true, nx, nkx, nlines, in_dev, out_dev, stream);
+}
+
+extern "C" int ekgpu_fft_x_to_physical(int nx, int nkx, long nlines, const double *in_dev, double *out_dev,
+                                       void *stream) {
+  return ek::standalone(false, nx, nkx, nlines, in_dev, out_dev, stream);
+}

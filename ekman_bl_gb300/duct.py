@@ -28,6 +28,7 @@ EXPORTS = [
     "ekgpu_get_field", "ekgpu_put_field", "ekgpu_rk_substep", "ekgpu_step", "ekgpu_rem_div",
     "ekgpu_poisson_batch", "ekgpu_poisson_batch_device", "ekgpu_last_divergence", "ekgpu_last_mg_stats",
     "ekgpu_launch_count", "ekgpu_set_timing", "ekgpu_get_timing", "ekgpu_timing_class_name",
+    "ekgpu_fft_x_to_fourier", "ekgpu_fft_x_to_physical",
 ]
 
 
@@ -77,6 +78,8 @@ def load_library():
     L.ekgpu_get_timing.argtypes = [V, _D, C.POINTER(C.c_longlong), _D, C.c_int]
     L.ekgpu_timing_class_name.argtypes = [C.c_int]
     L.ekgpu_timing_class_name.restype = C.c_char_p
+    for n in ("ekgpu_fft_x_to_fourier", "ekgpu_fft_x_to_physical"):
+        getattr(L, n).argtypes = [C.c_int, C.c_int, C.c_long, V, V, V]
     _lib = L
     return L
 
@@ -219,3 +222,13 @@ class DuctSolver:
         if k < 0:
             self._check(k)
         return {self._L.ekgpu_timing_class_name(i).decode(): (ms[i], int(cnt[i]), by[i]) for i in range(k)}
+
+
+def fft_x(forward: bool, nx: int, nkx: int, nlines: int, in_ptr: int, out_ptr: int, stream_ptr: int | None = None):
+    """The context-free x-transforms (ekgpu_fft_x_to_fourier / _to_physical)
+    on device buffers given as raw pointers."""
+    L = load_library()
+    fn = L.ekgpu_fft_x_to_fourier if forward else L.ekgpu_fft_x_to_physical
+    st = fn(nx, nkx, nlines, C.c_void_p(in_ptr), C.c_void_p(out_ptr), C.c_void_p(stream_ptr or 0))
+    if st:
+        raise EkError(st, L.ekgpu_last_error(None).decode())

@@ -131,7 +131,8 @@ int ekgpu_create(const ek_params *p, ek_ctx **ctx);
 /* Free the context and its device memory. */
 void ekgpu_destroy(ek_ctx *ctx);
 
-/* Text of the last error on this context (never NULL). */
+/* Text of the last error on this context (never NULL).  With ctx == NULL:
+ * the last error of a context-free call (ekgpu_fft_*) on this host thread. */
 const char *ekgpu_last_error(const ek_ctx *ctx);
 
 /* Bind the context to an existing CUDA stream (cudaStream_t passed as a
@@ -199,6 +200,19 @@ int ekgpu_last_divergence(ek_ctx *ctx, double *div);
 
 /* Stats of the last multigrid call made by a substep or poisson call. */
 int ekgpu_last_mg_stats(ek_ctx *ctx, ek_mg_stats *stats);
+
+/* Context-free batched x-transforms on device memory: the
+ * FFT_X_TO_FOURIER_OP / FFT_X_TO_PHYSICAL_OP pair the reference calls
+ * (duct.F90:700, mpi_duct.F90:290,308; fft.F90 itself is missing from the
+ * reference tree, FFTW 2.1.5 underneath).  nlines lines, each NX reals with
+ * stride NX+2 doubles (physical) or NX/2+1 complex (spectral).  Forward:
+ * (1/NX) sum_n u_n exp(-2 pi i k n/NX) for k <= nkx, zero above.  Inverse:
+ * the Hermitian sum over k <= nkx (imaginary part of k = 0 ignored), points
+ * x = NX, NX+1 set to 0.  nx a power of two in [8, 1024], nkx < nx/2;
+ * stream is a cudaStream_t or NULL.  The twiddle tables are device scratch
+ * allocated once per (device, nx).  Asynchronous on the stream. */
+int ekgpu_fft_x_to_fourier(int nx, int nkx, long nlines, const double *in_dev, double *out_dev, void *stream);
+int ekgpu_fft_x_to_physical(int nx, int nkx, long nlines, const double *in_dev, double *out_dev, void *stream);
 
 /* Number of kernel launches this context issued since creation. */
 long long ekgpu_launch_count(const ek_ctx *ctx);

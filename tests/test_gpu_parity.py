@@ -117,3 +117,32 @@ def test_nan_state_reports_error():
     with pytest.raises(Exception) as e:
         g.step(1)
     assert "NAN" in str(e.value)
+
+
+@pytest.mark.parametrize("nx", [16, 64, 256, 1024])
+def test_fft_entry_points_match_oracle(nx):
+    """ekgpu_fft_x_to_fourier / _to_physical against the oracle's transform."""
+    torch = pytest.importorskip("torch")
+    from ekman_bl_gb300.duct import fft_x
+    nkx = nx // 3
+    nlines = 37
+    rng = np.random.default_rng(nx)
+    x = np.zeros((nlines, nx + 2))
+    x[:, :nx] = rng.standard_normal((nlines, nx))
+    xd = torch.from_numpy(x).cuda()
+    cd = torch.zeros((nlines, nx // 2 + 1), dtype=torch.complex128, device="cuda")
+    fft_x(True, nx, nkx, nlines, xd.data_ptr(), cd.data_ptr())
+    torch.cuda.synchronize()
+    want = ekref.fft_r2c(x, nkx)
+    assert rel_l2(cd.cpu().numpy(), want) < 1e-14
+    yd = torch.zeros((nlines, nx + 2), dtype=torch.float64, device="cuda")
+    fft_x(False, nx, nkx, nlines, cd.data_ptr(), yd.data_ptr())
+    torch.cuda.synchronize()
+    assert rel_l2(yd.cpu().numpy(), ekref.fft_c2r(want, nkx)) < 1e-14
+
+
+def test_fft_entry_point_rejects_bad_size():
+    from ekman_bl_gb300.duct import EkError, fft_x
+    with pytest.raises(EkError) as e:
+        fft_x(True, 48, 16, 1, 1, 1)
+    assert "power of two" in str(e.value)
