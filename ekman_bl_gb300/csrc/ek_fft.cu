@@ -369,3 +369,68 @@ extern "C" int ekgpu_fft_x_to_physical(int nx, int nkx, long nlines, const doubl
                                        void *stream) {
   return ek::standalone(false, nx, nkx, nlines, in_dev, out_dev, stream);
 }
+
+// ---------------------------------------------------------------------------
+// ekgpu_fft_x_to_fourier_noalloc: the forward transform above with its
+// twiddle scratch in a fixed device array instead of cudaMalloc'd memory.
+namespace ek {
+namespace {
+
+// Largest nx the array holds: (nx/4 + nx/2 + 1) twiddles = 769 for nx = 1024
+// (12.3 KB, resident on every GPU that loads the library until exit).
+constexpr int kNoAllocMaxNx = 1024;
+constexpr int kNoAllocTw = kNoAllocMaxNx / 4 + kNoAllocMaxNx / 2 + 1;
+static __device__ __align__(256) double2 g_noalloc_twiddles[kNoAllocTw];
+
+// Device address of g_noalloc_twiddles, looked up once per device (the host
+// symbol itself is only a stand-in and must never reach a kernel).
+double2 *noalloc_scratch(int &err) {
+  static std::mutex mu;
+  static double2 *addr[128] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 128) {
+    t_last_error = std::string("ekgpu_fft_x_to_fourier_noalloc: cudaGetDevice: ") + cudaGetErrorString(e);
+    err = EK_ERR_CUDA;
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  if (!addr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_twiddles);
+    if (e != cudaSuccess || !p) {
+      t_last_error = std::string("ekgpu_fft_x_to_fourier_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+      err = EK_ERR_CUDA;
+      return nullptr;
+    }
+    addr[dev] = static_cast<double2 *>(p);
+  }
+  return addr[dev];
+}
+
+}  // namespace
+}  // namespace ek
+
+extern "C" int ekgpu_fft_x_to_fourier_noalloc(int nx, int nkx, long nlines, const double *in_dev, double *out_dev,
+                                              void *stream) {
+  using namespace ek;
+  if (nx > kNoAllocMaxNx) {
+    t_last_error = "ekgpu_fft_x_to_fourier_noalloc: nx exceeds the fixed scratch maximum of 1024";
+    return EK_ERR_ARG;
+  }
+  if (!fft_args_ok(nx, nkx, nlines, in_dev, out_dev)) return EK_ERR_ARG;
+  int err = EK_OK;
+  double2 *tw = noalloc_scratch(err);
+  if (!tw) return err;
+  try {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    fft_init_attributes();
+    // the whole table is rewritten on every call, before the transform reads it
+    k_twiddles<<<4, 256, 0, s>>>(tw, tw + nx / 4, nx);
+    EK_CUDA(cudaPeekAtLastError());
+    return run_standalone(true, nx, nkx, nlines, in_dev, out_dev, s, tw);
+  } catch (const CudaError &e) {
+    t_last_error = e.msg;
+    return EK_ERR_CUDA;
+  }
+}

@@ -28,7 +28,7 @@ EXPORTS = [
     "ekgpu_get_field", "ekgpu_put_field", "ekgpu_rk_substep", "ekgpu_step", "ekgpu_rem_div",
     "ekgpu_poisson_batch", "ekgpu_poisson_batch_device", "ekgpu_last_divergence", "ekgpu_last_mg_stats",
     "ekgpu_launch_count", "ekgpu_set_timing", "ekgpu_get_timing", "ekgpu_timing_class_name",
-    "ekgpu_fft_x_to_fourier", "ekgpu_fft_x_to_physical",
+    "ekgpu_fft_x_to_fourier", "ekgpu_fft_x_to_physical", "ekgpu_fft_x_to_fourier_noalloc",
 ]
 
 
@@ -78,7 +78,7 @@ def load_library():
     L.ekgpu_get_timing.argtypes = [V, _D, C.POINTER(C.c_longlong), _D, C.c_int]
     L.ekgpu_timing_class_name.argtypes = [C.c_int]
     L.ekgpu_timing_class_name.restype = C.c_char_p
-    for n in ("ekgpu_fft_x_to_fourier", "ekgpu_fft_x_to_physical"):
+    for n in ("ekgpu_fft_x_to_fourier", "ekgpu_fft_x_to_physical", "ekgpu_fft_x_to_fourier_noalloc"):
         getattr(L, n).argtypes = [C.c_int, C.c_int, C.c_long, V, V, V]
     _lib = L
     return L

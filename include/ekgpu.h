@@ -214,6 +214,26 @@ int ekgpu_last_mg_stats(ek_ctx *ctx, ek_mg_stats *stats);
 int ekgpu_fft_x_to_fourier(int nx, int nkx, long nlines, const double *in_dev, double *out_dev, void *stream);
 int ekgpu_fft_x_to_physical(int nx, int nkx, long nlines, const double *in_dev, double *out_dev, void *stream);
 
+/* ekgpu_fft_x_to_fourier without any device allocation.  No counterpart in
+ * the reference: it exists for callers that are not allowed to allocate
+ * device memory themselves or through this library -- for example a host
+ * application that reserved the GPU's memory up front for its own pool, or
+ * a time-critical loop that cannot pay for cudaMalloc and for the device-wide
+ * synchronisation of cudaFree.  Same arguments and results as
+ * ekgpu_fft_x_to_fourier; the caller still owns in_dev and out_dev.
+ * Limit: nx <= 1024 (larger nx returns EK_ERR_ARG, message via
+ * ekgpu_last_error(NULL)).  Its scratch -- the twiddle table, at most 769
+ * complex doubles (12.3 KB) -- lives in one fixed array in device memory
+ * that every GPU loading this library holds until the process exits.  The
+ * first call on each device looks up that array's device address (a one-
+ * time set-up), so make the first call on a device before any stream
+ * capture.  Every call rewrites the whole table before using it, so nothing
+ * has to start at zero; but all calls share the one table, so calls that
+ * overlap on the GPU (e.g. on two streams) race and must be ordered by the
+ * caller. */
+int ekgpu_fft_x_to_fourier_noalloc(int nx, int nkx, long nlines, const double *in_dev, double *out_dev,
+                                   void *stream);
+
 /* Number of kernel launches this context issued since creation. */
 long long ekgpu_launch_count(const ek_ctx *ctx);
 
