@@ -70,10 +70,9 @@ bool supported_bc(const ek_params &p, std::string &why) {
 
 void run_rem_div(Ctx &c, double temp4, bool update_p, int *mg_status) {
   const int P = 2 * (c.d.NKX + 1);
-  MgLevel &F = c.mg.lv[c.mg.ngrid - 1];
-  launch_divergence_rhs(c, F.rhs, P);
-  *mg_status = mg_solve(c, P, c.mg_kx2, nullptr);
-  launch_projection(c, c.mg_phif, P, temp4, update_p);
+  launch_divergence_rhs(c, c.mgw.rhs[c.mg.ngrid - 1], P);
+  *mg_status = mg_solve(c, P, c.mgw.kx2, c.mg_kx2_host.data(), nullptr);
+  launch_projection(c, c.mgw.phif, P, temp4, update_p);
 }
 
 int substep(Ctx &c, int rk) {
@@ -185,18 +184,18 @@ void timing_resolve(Ctx &c) {
 
 namespace {
 
-int poisson_dev(Ctx &c, const double *rhs_dev, double *phi_dev, const double *kx2_dev, int nprob, ek_mg_stats *st) {
+int poisson_dev(Ctx &c, const double *rhs_dev, double *phi_dev, const double *kx2_dev, const double *kx2_host,
+                int nprob, ek_mg_stats *st) {
   if (!c.have_metrics) return fail(c, EK_ERR_STATE, "metrics not set");
   if (nprob <= 0) return fail(c, EK_ERR_ARG, "nprob must be positive");
-  if (nprob > c.mg_pmax) mg_alloc(c, nprob);
+  if (nprob > c.mgw.pmax) mg_alloc(c, nprob);
   const long npt = (long)c.mg.nfx * c.mg.nfy;
-  MgLevel &F = c.mg.lv[c.mg.ngrid - 1];
   long n = npt * nprob;
   unsigned blocks = (unsigned)std::min<long>((n + 255) / 256, 65535L * 16);
-  k_transpose<<<blocks, 256, 0, c.stream>>>(rhs_dev, F.rhs, nprob, npt, 1);
+  k_transpose<<<blocks, 256, 0, c.stream>>>(rhs_dev, c.mgw.rhs[c.mg.ngrid - 1], nprob, npt, 1);
   after_launch(c);
-  const int r = mg_solve(c, nprob, kx2_dev, st);
-  k_transpose<<<blocks, 256, 0, c.stream>>>(c.mg_phif, phi_dev, nprob, npt, 0);
+  const int r = mg_solve(c, nprob, kx2_dev, kx2_host, st);
+  k_transpose<<<blocks, 256, 0, c.stream>>>(c.mgw.phif, phi_dev, nprob, npt, 0);
   after_launch(c);
   EK_CUDA(cudaStreamSynchronize(c.stream));
   return r;
@@ -254,6 +253,7 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
   if (p.mg_kcycle < 1 || p.mg_iprer < 1 || p.mg_ipost < 1 || (p.mg_intpol != 1 && p.mg_intpol != 3) || p.mg_maxcy < 1)
     return reject("bad multigrid options");
   if (p.mg_stop != EK_MG_STOP_RELCHANGE && p.mg_stop != EK_MG_STOP_RESIDUAL) return reject("bad mg_stop");
+  if (p.mg_fast && p.mg_stop != EK_MG_STOP_RESIDUAL) return reject("mg_fast needs mg_stop = EK_MG_STOP_RESIDUAL");
   if (!supported_bc(p, why)) return reject(why);
   MgPlan &P = c.mg;
   if (p.mg_ixp > 0) {
@@ -334,9 +334,12 @@ void ekgpu_destroy(ek_ctx *h) {
   Ctx &c = h->c;
   if (c.stream) cudaStreamSynchronize(c.stream);
   for (void *p : c.allocs) cudaFree(p);
-  if (c.mg_pool) cudaFree(c.mg_pool);
-  if (c.mg_done) cudaFree(c.mg_done);
+  if (c.mg_cof_pool) cudaFree(c.mg_cof_pool);
+  mg_work_free(c.mgw);
+  mg_work_free(c.mgs);
+  if (c.mgf_pool) cudaFree(c.mgf_pool);
   if (c.mg.ops_dev) cudaFree(c.mg.ops_dev);
+  c.poll.destroy();
   for (auto &r : c.trec) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : c.evpool) cudaEventDestroy(e);
   if (c.own_stream) cudaStreamDestroy(c.own_stream);
@@ -419,7 +422,7 @@ int ekgpu_set_metrics(ek_ctx *h, const ek_metrics *m) {
       }
       if ((tot + maxph) * sizeof(double) <= 96 * 1024) P.lc = l;
     }
-    const int pmax = std::max(c.mg_pmax, d.NX + 2);
+    const int pmax = std::max(c.mgw.pmax, d.NX + 2);
     mg_alloc(c, pmax);
     c.have_metrics = true;
     return (int)EK_OK;
@@ -532,7 +535,7 @@ int ekgpu_poisson_batch(ek_ctx *h, const double *rhs, double *phi, const double 
     try {
       EK_CUDA(cudaMemcpyAsync(buf, rhs, sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
       EK_CUDA(cudaMemcpyAsync(buf + 2 * n, kx2, sizeof(double) * nprob, cudaMemcpyHostToDevice, c.stream));
-      r = poisson_dev(c, buf, buf + n, buf + 2 * n, nprob, stats);
+      r = poisson_dev(c, buf, buf + n, buf + 2 * n, kx2, nprob, stats);
       EK_CUDA(cudaMemcpyAsync(phi, buf + n, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream));
       EK_CUDA(cudaStreamSynchronize(c.stream));
     } catch (...) {
@@ -548,7 +551,7 @@ int ekgpu_poisson_batch_device(ek_ctx *h, const double *rhs_dev, double *phi_dev
                                ek_mg_stats *stats) {
   return guarded(h, [&](Ctx &c) {
     if (!rhs_dev || !phi_dev || !kx2_dev || nprob <= 0) return fail(c, EK_ERR_ARG, "bad poisson arguments");
-    return poisson_dev(c, rhs_dev, phi_dev, kx2_dev, nprob, stats);
+    return poisson_dev(c, rhs_dev, phi_dev, kx2_dev, nullptr, nprob, stats);
   });
 }
 

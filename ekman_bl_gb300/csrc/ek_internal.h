@@ -65,17 +65,32 @@ struct AdiFactors {
 // One multigrid level (MUDPACK level k; index k-1).
 struct MgLevel {
   int nx, ny;
-  double *phi;   // (0:nx+1, 0:ny+1) x P, problem fastest
-  double *rhs;   // (1:nx, 1:ny) x P
-  double *cof;   // 11 x nx x ny: c1..c8, s4, corr9, jac  (kx-independent)
-  double *inv9;  // nx x ny x P: 1/c9 for the current problems
-  size_t phi_off, rhs_off, cof_off;
+  double *cof;  // 11 x nx x ny: c1..c8, s4, corr9, jac  (kx-independent)
+};
+
+// Work arrays of one batched multigrid solve for up to pmax problems,
+// problem fastest: per level phi (0:nx+1, 0:ny+1), rhs (1:nx, 1:ny) and 1/c9
+// (nx x ny); the finest-size scratch; the output iterate (finest interior);
+// per-problem reductions, kx^2, done flags and cycle counts.
+struct MgWork {
+  int pmax = 0;
+  double *pool = nullptr;
+  int *flags = nullptr;
+  std::vector<double *> phi, rhs, inv9;
+  double *scratch = nullptr, *phif = nullptr, *red = nullptr, *kx2 = nullptr;
+  int *done = nullptr, *cycles = nullptr, *alldone = nullptr, *idx = nullptr;
+  std::vector<int> idx_host;  // host copy of idx (a subset's problem numbers)
 };
 
 enum MgOpKind { OP_TRSFC = 0, OP_RELAX = 1, OP_RESTRICT = 2, OP_COR2 = 3, OP_PROLONG = 4, OP_CHECK = 5 };
 struct MgOp {
   int kind, level, count;  // level = MUDPACK level (1 coarsest); RESTRICT: from level to level-1;
                            // COR2: level-1 -> level; PROLONG: level -> level+1
+};
+
+// FP32 arrays of one level for the mixed-precision multigrid (ek_mgfast.cu).
+struct MgLevelF {
+  float *e = nullptr, *r = nullptr, *cp = nullptr, *cof = nullptr;
 };
 
 struct MgPlan {
@@ -99,6 +114,42 @@ enum KClass {
 struct TimerRec {
   int cls;
   cudaEvent_t a, b;
+};
+
+// Early stop of an iteration whose kernels decide on the device when every
+// problem is done (they return at once after that).  After each check kernel
+// the done flag is copied to pinned host memory; the host then waits for the
+// copy made one check earlier, while the GPU still has the latest cycle
+// queued, and stops issuing cycles once that copy reads 1.
+struct StopPoll {
+  int *host = nullptr;  // pinned, kSlots flags
+  cudaEvent_t ev[4] = {};
+  static constexpr int kSlots = 4;
+  int n = 0;
+  void init() {
+    if (host) return;
+    if (cudaHostAlloc(&host, sizeof(int) * kSlots, cudaHostAllocDefault) != cudaSuccess) host = nullptr;
+    for (auto &e : ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  }
+  void destroy() {
+    if (host) cudaFreeHost(host);
+    host = nullptr;
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+  void reset() { n = 0; }
+  // after a check kernel on stream s; returns true when the iteration can stop
+  bool after_check(const int *alldone_dev, cudaStream_t s) {
+    if (!host) return false;
+    const int k = n % kSlots;
+    cudaMemcpyAsync(&host[k], alldone_dev, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaEventRecord(ev[k], s);
+    ++n;
+    if (n < 2) return false;
+    const int k1 = (n - 2) % kSlots;
+    cudaEventSynchronize(ev[k1]);
+    return host[k1] != 0;
+  }
 };
 
 struct Ctx {
@@ -128,16 +179,16 @@ struct Ctx {
   double *bc_weights = nullptr;
   // multigrid
   MgPlan mg;
-  double *mg_pool = nullptr;
-  double *mg_kx2 = nullptr;         // per problem
-  double *mg_scratch = nullptr;     // finest-size scratch x P
-  double *mg_phif = nullptr;        // output iterate per problem (finest interior)
-  double *mg_red = nullptr;         // per-problem reductions
-  int *mg_done = nullptr;           // per problem: 0 active, 1 converged
-  int *mg_cycles = nullptr;         // per problem cycle count
-  int *mg_alldone = nullptr;
-  int mg_pmax = 0;                  // problem capacity
+  double *mg_cof_pool = nullptr;    // the levels' coefficients
+  MgWork mgw;                       // the solves' work arrays
+  MgWork mgs;                       // mixed precision: the kx^2 = 0 problems, solved MUDPACK-exact
+  std::vector<double> mg_kx2_host;  // host copy of mgw.kx2
+  float *mgf_pool = nullptr;        // mixed-precision multigrid
+  std::vector<MgLevelF> mgf_levels;
+  float *mgf_scratch = nullptr;
+  int mgf_pmax = 0;
   ek_mg_stats last_stats{};
+  StopPoll poll;
   // divergence check
   double *div_part = nullptr;
   double last_div = 0.0;
@@ -226,9 +277,18 @@ void launch_divergence_rhs(Ctx &c, double *rhs_finest, int nprob);
 void launch_projection(Ctx &c, const double *phif, int nprob, double temp4, bool update_p);
 int finish_divergence(Ctx &c, double *div_out);
 
-// multigrid (ek_mg.cu)
-int mg_solve(Ctx &c, int nprob, const double *kx2_dev, ek_mg_stats *st);
+// multigrid (ek_mg.cu).  mg_solve: nprob problems whose finest rhs is in
+// c.mgw.rhs[ngrid-1]; the solution is left in c.mgw.phif.  kx2_host may be
+// null (it is then read back from kx2_dev when the mixed-precision solver
+// needs it).
+int mg_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_host, ek_mg_stats *st);
+int mg_solve_exact(Ctx &c, MgWork &w, int nprob, const double *kx2_dev, ek_mg_stats *st, int max_cycles);
+constexpr int kSingularMaxCycles = 6;  // MULTIGRID_MUDPACK's cap for the kx = 0 mode
 void mg_alloc(Ctx &c, int pmax);
+void mg_work_alloc(Ctx &c, MgWork &w, int pmax);
+void mg_work_free(MgWork &w);
+int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_host, ek_mg_stats *st);
+void mgfast_alloc(Ctx &c, int pmax);
 
 #define EK_CUDA(call)                                                                  \
   do {                                                                                 \

@@ -415,7 +415,7 @@ __global__ void k_check_finish(MgDev g, int iter, int last) {
       // singular mode: MULTIGRID_MUDPACK's own rule (REAL*4 1e-6, <= 6 cycles)
       meas = relmax;
       conv = relmax <= (double)1.0e-6f;
-      if (!conv && iter >= 6) {
+      if (!conv && iter >= kSingularMaxCycles) {
         g.done[p] = 2;  // stopped at the reference's cycle cap
         continue;
       }
@@ -673,81 +673,114 @@ unsigned nblk(long n, int bs) {
 
 }  // namespace
 
-void mg_alloc(Ctx &c, int pmax) {
-  MgPlan &P = c.mg;
-  if (c.mg_pool) {
-    cudaFree(c.mg_pool);
-    c.mg_pool = nullptr;
-  }
+void mg_work_free(MgWork &w) {
+  if (w.pool) cudaFree(w.pool);
+  if (w.flags) cudaFree(w.flags);
+  w = MgWork{};
+}
+
+// Work arrays for up to pmax problems; kx2 is left for the caller to fill.
+void mg_work_alloc(Ctx &c, MgWork &w, int pmax) {
+  const MgPlan &P = c.mg;
+  mg_work_free(w);
   size_t tot = 0;
-  for (auto &L : P.lv) {
-    L.phi_off = tot;
+  std::vector<size_t> ph(P.ngrid), rh(P.ngrid), iv(P.ngrid);
+  for (int l = 0; l < P.ngrid; ++l) {
+    const MgLevel &L = P.lv[l];
+    ph[l] = tot;
     tot += (size_t)(L.nx + 2) * (L.ny + 2) * pmax;
-    L.rhs_off = tot;
+    rh[l] = tot;
     tot += (size_t)L.nx * L.ny * pmax;
-    L.cof_off = tot;
-    tot += (size_t)11 * L.nx * L.ny;
-    tot += (size_t)L.nx * L.ny * pmax;  // inv9
+    iv[l] = tot;
+    tot += (size_t)L.nx * L.ny * pmax;
   }
   const size_t scr_off = tot;
   tot += (size_t)(P.nfx + 2) * (P.nfy + 2) * pmax;
   const size_t phif_off = tot;
   tot += (size_t)P.nfx * P.nfy * pmax;
   const size_t red_off = tot;
-  tot += (size_t)5 * pmax + 8;
+  tot += (size_t)6 * pmax + 8;
   const size_t kx_off = tot;
   tot += pmax;
-  EK_CUDA(cudaMalloc(&c.mg_pool, tot * sizeof(double)));
-  for (auto &L : P.lv) {
-    L.phi = c.mg_pool + L.phi_off;
-    L.rhs = c.mg_pool + L.rhs_off;
-    L.cof = c.mg_pool + L.cof_off;
-    L.inv9 = L.cof + (size_t)11 * L.nx * L.ny;
+  EK_CUDA(cudaMalloc(&w.pool, tot * sizeof(double)));
+  EK_CUDA(cudaMalloc(&w.flags, sizeof(int) * (3 * pmax + 4)));
+  w.phi.resize(P.ngrid);
+  w.rhs.resize(P.ngrid);
+  w.inv9.resize(P.ngrid);
+  for (int l = 0; l < P.ngrid; ++l) {
+    w.phi[l] = w.pool + ph[l];
+    w.rhs[l] = w.pool + rh[l];
+    w.inv9[l] = w.pool + iv[l];
   }
-  c.mg_scratch = c.mg_pool + scr_off;
-  c.mg_phif = c.mg_pool + phif_off;
-  c.mg_red = c.mg_pool + red_off;
-  c.mg_kx2 = c.mg_pool + kx_off;
-  // per-problem kx^2 of the projection solves: problem 2I+part is mode I
-  std::vector<double> kx2p(pmax);
-  for (int q = 0; q < pmax; ++q) kx2p[q] = c.kx2_h[std::min(q / 2, c.d.NX2P)];
-  EK_CUDA(cudaMemcpy(c.mg_kx2, kx2p.data(), sizeof(double) * pmax, cudaMemcpyHostToDevice));
-  for (int l = 0; l < P.ngrid; ++l)
+  w.scratch = w.pool + scr_off;
+  w.phif = w.pool + phif_off;
+  w.red = w.pool + red_off;
+  w.kx2 = w.pool + kx_off;
+  w.done = w.flags;
+  w.cycles = w.flags + pmax;
+  w.alldone = w.flags + 2 * pmax;
+  w.idx = w.flags + 2 * pmax + 4;
+  w.pmax = pmax;
+}
+
+// Coefficients of every level, the main work arrays with the projection
+// solves' kx^2 per problem (problem 2I+part is mode I), the operation list.
+void mg_alloc(Ctx &c, int pmax) {
+  MgPlan &P = c.mg;
+  if (c.mg_cof_pool) {
+    cudaFree(c.mg_cof_pool);
+    c.mg_cof_pool = nullptr;
+  }
+  size_t tot = 0;
+  for (auto &L : P.lv) tot += (size_t)11 * L.nx * L.ny;
+  EK_CUDA(cudaMalloc(&c.mg_cof_pool, tot * sizeof(double)));
+  tot = 0;
+  for (int l = 0; l < P.ngrid; ++l) {
+    P.lv[l].cof = c.mg_cof_pool + tot;
+    tot += (size_t)11 * P.lv[l].nx * P.lv[l].ny;
     EK_CUDA(cudaMemcpy(P.lv[l].cof, P.cof_host[l].data(), sizeof(double) * P.cof_host[l].size(), cudaMemcpyHostToDevice));
-  if (c.mg_done) cudaFree(c.mg_done);
-  EK_CUDA(cudaMalloc(&c.mg_done, sizeof(int) * (2 * pmax + 4)));
+  }
+  mg_work_alloc(c, c.mgw, pmax);
+  c.mg_kx2_host.assign(pmax, 0.0);
+  for (int q = 0; q < pmax; ++q) c.mg_kx2_host[q] = c.kx2_h[std::min(q / 2, c.d.NX2P)];
+  EK_CUDA(cudaMemcpy(c.mgw.kx2, c.mg_kx2_host.data(), sizeof(double) * pmax, cudaMemcpyHostToDevice));
   if (P.ops_dev) cudaFree(P.ops_dev);
   EK_CUDA(cudaMalloc(&P.ops_dev, sizeof(MgOp) * P.ops.size()));
   EK_CUDA(cudaMemcpy(P.ops_dev, P.ops.data(), sizeof(MgOp) * P.ops.size(), cudaMemcpyHostToDevice));
-  c.mg_cycles = c.mg_done + pmax;
-  c.mg_alldone = c.mg_done + 2 * pmax;
-  c.mg_pmax = pmax;
+  if (c.p.mg_fast) mgfast_alloc(c, pmax);
 }
 
-// One batched solve: the finest rhs must already be in lv[ngrid-1].rhs
-// (nprob problems, problem fastest); the solution is left in mg_phif.
-int mg_solve(Ctx &c, int nprob, const double *kx2_dev, ek_mg_stats *st) {
+int mg_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_host, ek_mg_stats *st) {
+  if (c.p.mg_fast) return mgfast_solve(c, nprob, kx2_dev, kx2_host, st);
+  return mg_solve_exact(c, c.mgw, nprob, kx2_dev, st, 0);
+}
+
+// One batched MUDPACK-exact solve in the work arrays w: the finest rhs must
+// already be in w.rhs[ngrid-1] (nprob problems, problem fastest); the
+// solution is left in w.phif.  max_cycles > 0 stops issuing the schedule
+// after that many k-cycles (a batch whose problems all stop by then).
+int mg_solve_exact(Ctx &c, MgWork &w, int nprob, const double *kx2_dev, ek_mg_stats *st, int max_cycles) {
   MgPlan &PL = c.mg;
-  if (nprob > c.mg_pmax) return EK_ERR_ARG;
+  if (nprob > w.pmax) return EK_ERR_ARG;
   MgDev g{};
   g.P = nprob;
   g.ngrid = PL.ngrid;
   g.lc = PL.lc;
   g.orth = PL.orth ? 1 : 0;
-  for (int l = 0; l < PL.ngrid; ++l) g.lv[l] = LvDev{PL.lv[l].nx, PL.lv[l].ny, PL.lv[l].phi, PL.lv[l].rhs, PL.lv[l].cof, PL.lv[l].inv9};
-  g.scr = c.mg_scratch;
+  for (int l = 0; l < PL.ngrid; ++l) g.lv[l] = LvDev{PL.lv[l].nx, PL.lv[l].ny, w.phi[l], w.rhs[l], PL.lv[l].cof, w.inv9[l]};
+  g.scr = w.scratch;
   g.kx2 = kx2_dev;
-  g.phif = c.mg_phif;
-  g.red = c.mg_red;
-  g.done = c.mg_done;
-  g.cycles = c.mg_cycles;
-  g.alldone = c.mg_alldone;
+  g.phif = w.phif;
+  g.red = w.red;
+  g.done = w.done;
+  g.cycles = w.cycles;
+  g.alldone = w.alldone;
   g.tol = c.p.mg_tol;
   g.stop_rule = c.p.mg_stop;
   const int bs = 256;
   cudaStream_t s = c.stream;
-  EK_CUDA(cudaMemsetAsync(c.mg_done, 0, sizeof(int) * (2 * c.mg_pmax + 4), s));
-  EK_CUDA(cudaMemsetAsync(c.mg_red, 0, sizeof(double) * (5 * c.mg_pmax + 8), s));
+  EK_CUDA(cudaMemsetAsync(w.flags, 0, sizeof(int) * (2 * w.pmax + 4), s));
+  EK_CUDA(cudaMemsetAsync(w.red, 0, sizeof(double) * (6 * w.pmax + 8), s));
   for (int l = 1; l <= PL.ngrid; ++l) {
     const long n = (long)PL.lv[l - 1].nx * PL.lv[l - 1].ny * nprob;
     KScope ks(c, KC_MG_SETUP, 8.0 * n);
@@ -796,7 +829,11 @@ int mg_solve(Ctx &c, int nprob, const double *kx2_dev, ek_mg_stats *st) {
   int o = 0;
   int ncheck = 0, maxcheck = 0;
   for (const MgOp &op : PL.ops) maxcheck += (op.kind == OP_CHECK);
-  while (o < nops) {
+  if (max_cycles > 0) maxcheck = std::min(maxcheck, max_cycles);
+  c.poll.init();
+  c.poll.reset();
+  bool stop = false;
+  while (o < nops && ncheck < maxcheck && !stop) {
     const MgOp &op = PL.ops[o];
     if (is_coarse(op)) {
       int e = o;
@@ -822,12 +859,12 @@ int mg_solve(Ctx &c, int nprob, const double *kx2_dev, ek_mg_stats *st) {
         KScope ks(c, KC_MG_SETUP, tb);
         for (int l = 1; l <= PL.ngrid; ++l) {
           const size_t n = (size_t)(PL.lv[l - 1].nx + 2) * (PL.lv[l - 1].ny + 2) * nprob;
-          k_zero<<<nblk((long)n, bs), bs, 0, s>>>(PL.lv[l - 1].phi, n);
+          k_zero<<<nblk((long)n, bs), bs, 0, s>>>(w.phi[l - 1], n);
           after_launch(c);
         }
         {
           const size_t n = (size_t)PL.nfx * PL.nfy * nprob;
-          k_zero<<<nblk((long)n, bs), bs, 0, s>>>(c.mg_phif, n);
+          k_zero<<<nblk((long)n, bs), bs, 0, s>>>(w.phif, n);
           after_launch(c);
         }
         for (int l = PL.ngrid; l >= 2; --l) {
@@ -890,6 +927,7 @@ int mg_solve(Ctx &c, int nprob, const double *kx2_dev, ek_mg_stats *st) {
         after_launch(c);
         k_check_finish<<<1, 256, 0, s>>>(g, op.count, ncheck == maxcheck ? 1 : 0);
         after_launch(c);
+        if (c.poll.after_check(w.alldone, s)) stop = true;
         break;
       }
       default:
@@ -900,9 +938,9 @@ int mg_solve(Ctx &c, int nprob, const double *kx2_dev, ek_mg_stats *st) {
   // stats
   std::vector<int> cyc(nprob), done(nprob);
   std::vector<double> meas(nprob);
-  EK_CUDA(cudaMemcpyAsync(cyc.data(), c.mg_cycles, sizeof(int) * nprob, cudaMemcpyDeviceToHost, s));
-  EK_CUDA(cudaMemcpyAsync(done.data(), c.mg_done, sizeof(int) * nprob, cudaMemcpyDeviceToHost, s));
-  EK_CUDA(cudaMemcpyAsync(meas.data(), c.mg_red + 4 * nprob, sizeof(double) * nprob, cudaMemcpyDeviceToHost, s));
+  EK_CUDA(cudaMemcpyAsync(cyc.data(), w.cycles, sizeof(int) * nprob, cudaMemcpyDeviceToHost, s));
+  EK_CUDA(cudaMemcpyAsync(done.data(), w.done, sizeof(int) * nprob, cudaMemcpyDeviceToHost, s));
+  EK_CUDA(cudaMemcpyAsync(meas.data(), w.red + 4 * nprob, sizeof(double) * nprob, cudaMemcpyDeviceToHost, s));
   EK_CUDA(cudaStreamSynchronize(s));
   ek_mg_stats S{};
   S.nprob = nprob;

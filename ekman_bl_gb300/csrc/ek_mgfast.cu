@@ -1,0 +1,770 @@
+// Mixed-precision multigrid for the tolerance-driven projection solves.
+//
+// Same discrete operator as the MUDPACK-exact path (dismd2cr's 9-point
+// coefficients, periodic x with MUDPACK's ghost columns, Neumann y), a
+// different iteration: FP64 iterative refinement around FP32 V-cycles.
+//   r = b - A phi            FP64, with ||r||, ||b|| per problem
+//   stop if ||r|| <= tol ||b||
+//   A e = r                  one FP32 V(1,1) cycle from e = 0 on MUDPACK's
+//                            coarse-level operators, alternating-direction
+//                            zebra line Gauss-Seidel smoother, MUDPACK's
+//                            full-weighting restriction and cubic prolongation
+//   phi = phi + e            FP64
+// GB300 runs FP32 at ~30x its FP64 rate, so only the residual and the update
+// stay on the FP64 pipe.  On a grid stretched in y the strong coupling is
+// along y near the wall and along x far from it; line relaxation in both
+// directions smooths both regions, so each cycle cuts the residual ~10x
+// where MUDPACK's point smoother (W-cycles) gets ~1.3x.
+//
+// Problems with kx^2 = 0 are singular (periodic x, Neumann y).  MUDPACK stops
+// them on its relative-change rule after at most maxcy cycles, usually before
+// they converge, so their result is MUDPACK's particular iterate; they are
+// gathered into a batch of their own and solved by the MUDPACK-exact path,
+// which gives the same result as a solve with mg_fast = 0.
+#include <algorithm>
+
+#include "ek_internal.h"
+
+namespace ek {
+
+namespace {
+
+struct LvF {
+  int nx, ny;
+  float *e, *r, *cof, *cp;  // e: (0:nx+1,0:ny+1)xP; r: nx*ny*P; cof: 11*nx*ny; cp: line-solve scratch nx*ny*P
+};
+struct FastDev {
+  int P, ngrid, orth;
+  LvF lv[24];
+  float *scr;              // finest-size scratch x P (residual / correction)
+  double *phi, *rhs, *cof;  // FP64 finest: phi with ghosts, rhs, coefficients
+  int nfx, nfy;
+  const double *kx2;
+  double *phif;            // output (finest interior, problem fastest)
+  double *red;             // 6 per problem: |b|^2, |r|^2, max|e|, max|phi|, meas
+  int *done, *cycles, *alldone;
+  double tol;
+};
+
+__device__ __forceinline__ float &E(const LvF &L, int P, int i, int j, int p) {
+  return L.e[((size_t)j * (L.nx + 2) + i) * P + p];
+}
+__device__ __forceinline__ void atomic_max_pos(double *a, double v) {
+  atomicMax(reinterpret_cast<unsigned long long *>(a), (unsigned long long)__double_as_longlong(v));
+}
+
+// r = b - A phi at the finest level in FP64; r32 = r; e_finest = 0;
+// per-problem |b|^2 and |r|^2 (block partials, one atomic per block).
+constexpr int kRY = 8;
+__global__ void __launch_bounds__(32 * kRY) k_f_resid64(FastDev g) {
+  if (*g.alldone) return;
+  const int P = g.P;
+  const int p = blockIdx.x * 32 + threadIdx.x;
+  const int ty = threadIdx.y;
+  const int nx = g.nfx, ny = g.nfy;
+  const size_t npt = (size_t)nx * ny;
+  const LvF &F = g.lv[g.ngrid - 1];
+  double sb = 0.0, sr = 0.0;
+  const bool act = (p < P) && !g.done[p];
+  if (act) {
+    const size_t si = P, sj = (size_t)(nx + 2) * P;
+    const double kx2 = g.kx2[p];
+    const double *cf = g.cof;
+    for (size_t pt = (size_t)blockIdx.y * kRY + ty; pt < npt; pt += (size_t)gridDim.y * kRY) {
+      const int i = 1 + (int)(pt % nx), j = 1 + (int)(pt / nx);
+      const double *ph = g.phi + ((size_t)j * (nx + 2) + i) * P + p;
+      double s = cf[pt] * ph[si];
+      if (!g.orth) s = s + cf[npt + pt] * ph[si + sj];
+      s = s + cf[2 * npt + pt] * ph[sj];
+      if (!g.orth) s = s + cf[3 * npt + pt] * ph[sj - si];
+      s = s + cf[4 * npt + pt] * ph[-(long)si];
+      if (!g.orth) s = s + cf[5 * npt + pt] * ph[-(long)(si + sj)];
+      s = s + cf[6 * npt + pt] * ph[-(long)sj];
+      if (!g.orth) s = s + cf[7 * npt + pt] * ph[si - sj];
+      const double c9 = ((-kx2 * cf[10 * npt + pt]) - cf[8 * npt + pt]) + cf[9 * npt + pt];
+      s = s + c9 * ph[0];
+      const double b = g.rhs[pt * P + p];
+      const double r = b - s;
+      sb += b * b;
+      sr += r * r;
+      F.r[pt * P + p] = (float)r;
+    }
+  }
+  // zero the finest correction (with ghosts)
+  if (p < P) {
+    const size_t nph = (size_t)(nx + 2) * (ny + 2);
+    for (size_t q = (size_t)blockIdx.y * kRY + ty; q < nph; q += (size_t)gridDim.y * kRY) F.e[q * P + p] = 0.f;
+  }
+  __shared__ double red[2][kRY][32];
+  red[0][ty][threadIdx.x] = sb;
+  red[1][ty][threadIdx.x] = sr;
+  __syncthreads();
+  if (ty == 0 && act) {
+    for (int y = 1; y < kRY; ++y) {
+      sb += red[0][y][threadIdx.x];
+      sr += red[1][y][threadIdx.x];
+    }
+    atomicAdd(&g.red[6 * p], sb);
+    atomicAdd(&g.red[6 * p + 1], sr);
+  }
+}
+
+// Decide per problem; iter = corrections applied so far.
+__global__ void k_f_check(FastDev g, int iter, int last) {
+  if (*g.alldone) return;
+  __shared__ int active;
+  if (threadIdx.x == 0) active = 0;
+  __syncthreads();
+  for (int p = threadIdx.x; p < g.P; p += blockDim.x) {
+    if (g.done[p]) continue;
+    g.cycles[p] = iter;
+    const double bn = sqrt(g.red[6 * p]);
+    const double meas = (bn > 0.0) ? sqrt(g.red[6 * p + 1]) / bn : 0.0;
+    const bool conv = meas <= g.tol;
+    g.red[6 * p + 4] = meas;
+    for (int k = 0; k < 4; ++k) g.red[6 * p + k] = 0.0;
+    if (conv) g.done[p] = 1;
+    else if (last) g.done[p] = 2;
+    else atomicAdd(&active, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && active == 0) *g.alldone = 1;
+}
+
+// The kx^2 = 0 subset: gather its finest rhs (problem fastest, P problems)
+// into a batch of ns problems, mark it done for the FP32 iteration, and
+// scatter its solutions back.
+__global__ void k_f_gather(const double *src, int P, double *dst, int ns, const int *idx, long npt) {
+  const long n = npt * ns;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int q = (int)(t % ns);
+    dst[t] = src[(t / ns) * P + idx[q]];
+  }
+}
+__global__ void k_f_scatter(const double *src, int ns, double *dst, int P, const int *idx, long npt) {
+  const long n = npt * ns;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int q = (int)(t % ns);
+    dst[(t / ns) * P + idx[q]] = src[t];
+  }
+}
+__global__ void k_f_mark(int *done, const int *idx, int ns) {
+  for (int q = threadIdx.x; q < ns; q += blockDim.x) done[idx[q]] = 1;
+}
+
+// Line Gauss-Seidel.  The 9-point operator couples each point to its eight
+// neighbours; a line solve takes the three couplings along the line into a
+// tridiagonal system and the others from current values.  Zebra order: the
+// lines of one colour do not couple to each other, so all of them (for all
+// problems) are solved in parallel, one thread per (line, problem).
+//
+// y-line at column i: c7 e(i,j-1) + c9 e(i,j) + c3 e(i,j+1) = r(i,j) - c1 e(i+1,j)
+// - c5 e(i-1,j) [- c2, c4, c6, c8 diagonal terms].  Rows j = 1 and ny have
+// c7 = 0 and c3 = 0 after MUDPACK's Neumann folding.  c' is kept in cp, d'
+// overwrites e until the back substitution.
+constexpr int kChunk = 8;
+__device__ __forceinline__ void yline_solve(const LvF &L, int P, int p, int i, float kx2, bool orth) {
+  const int nx = L.nx, ny = L.ny;
+  const size_t npt = (size_t)nx * ny;
+  const size_t si = P, sj = (size_t)(nx + 2) * P;
+  const float *cf = L.cof;
+  float cprev = 0.f, dprev = 0.f;
+  // forward elimination, kChunk rows at a time: every load of a chunk is
+  // issued before the recurrence consumes it
+  for (int j0 = 1; j0 <= ny; j0 += kChunk) {
+    float dv[kChunk], av[kChunk], bv[kChunk], cv[kChunk];
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      const int j = j0 + u;
+      if (j > ny) break;
+      const size_t pt = (size_t)(j - 1) * nx + (i - 1);
+      const float *ep = &L.e[((size_t)j * (nx + 2) + i) * P + p];
+      float d = L.r[pt * P + p] - cf[pt] * ep[si] - cf[4 * npt + pt] * ep[-(long)si];
+      if (orth == false)
+        d = d - cf[npt + pt] * ep[si + sj] - cf[3 * npt + pt] * ep[sj - si] - cf[5 * npt + pt] * ep[-(long)(si + sj)] -
+            cf[7 * npt + pt] * ep[si - sj];
+      dv[u] = d;
+      av[u] = cf[6 * npt + pt];
+      cv[u] = cf[2 * npt + pt];
+      bv[u] = ((-kx2 * cf[10 * npt + pt]) - cf[8 * npt + pt]) + cf[9 * npt + pt];
+    }
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      const int j = j0 + u;
+      if (j > ny) break;
+      const size_t pt = (size_t)(j - 1) * nx + (i - 1);
+      const float m = 1.f / (bv[u] - av[u] * cprev);
+      cprev = cv[u] * m;
+      dprev = (dv[u] - av[u] * dprev) * m;
+      L.cp[pt * P + p] = cprev;
+      L.e[((size_t)j * (nx + 2) + i) * P + p] = dprev;
+    }
+  }
+  // back substitution; periodic ghosts written together with their sources
+  float x = 0.f;
+  for (int j0 = ny; j0 >= 1; j0 -= kChunk) {
+    float dv[kChunk], cv[kChunk];
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      const int j = j0 - u;
+      if (j < 1) break;
+      const size_t pt = (size_t)(j - 1) * nx + (i - 1);
+      dv[u] = L.e[((size_t)j * (nx + 2) + i) * P + p];
+      cv[u] = L.cp[pt * P + p];
+    }
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      const int j = j0 - u;
+      if (j < 1) break;
+      x = dv[u] - cv[u] * x;
+      L.e[((size_t)j * (nx + 2) + i) * P + p] = x;
+      if (i == nx - 1) E(L, P, 0, j, p) = x;
+      if (i == 2) E(L, P, nx + 1, j, p) = x;
+    }
+  }
+}
+
+// x-line at row j: c5 e(i-1,j) + c9 e(i,j) + c1 e(i+1,j) = r(i,j) - c3 e(i,j+1)
+// - c7 e(i,j-1) [- diagonal terms].  The periodic wrap couplings (i = 1 to
+// the ghost e(0) = e(nx-1), i = nx to the ghost e(nx+1) = e(2)) are taken
+// from the ghosts' current values, so the line system stays tridiagonal.
+__device__ __forceinline__ void xline_solve(const LvF &L, int P, int p, int j, float kx2, bool orth) {
+  const int nx = L.nx, ny = L.ny;
+  const size_t npt = (size_t)nx * ny;
+  const size_t si = P, sj = (size_t)(nx + 2) * P;
+  const float *cf = L.cof;
+  float *erow = &L.e[(size_t)j * (nx + 2) * P + p];  // erow[i * P] = e(i, j)
+  float *cprow = &L.cp[(size_t)(j - 1) * nx * P + p];  // cprow[(i-1) * P]
+  const size_t rb = (size_t)(j - 1) * nx;
+  const float g0 = erow[0], g1 = erow[(size_t)(nx + 1) * si];
+  float cprev = 0.f, dprev = 0.f;
+  for (int i0 = 1; i0 <= nx; i0 += kChunk) {
+    float dv[kChunk], av[kChunk], bv[kChunk], cv[kChunk];
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      const int i = i0 + u;
+      if (i > nx) break;
+      const size_t pt = rb + (i - 1);
+      const float *ep = erow + (size_t)i * si;
+      float d = L.r[pt * P + p] - cf[2 * npt + pt] * ep[sj] - cf[6 * npt + pt] * ep[-(long)sj];
+      if (orth == false)
+        d = d - cf[npt + pt] * ep[si + sj] - cf[3 * npt + pt] * ep[sj - si] - cf[5 * npt + pt] * ep[-(long)(si + sj)] -
+            cf[7 * npt + pt] * ep[si - sj];
+      float a = cf[4 * npt + pt], c = cf[pt];
+      if (i == 1) { d -= a * g0; a = 0.f; }
+      if (i == nx) { d -= c * g1; c = 0.f; }
+      dv[u] = d;
+      av[u] = a;
+      cv[u] = c;
+      bv[u] = ((-kx2 * cf[10 * npt + pt]) - cf[8 * npt + pt]) + cf[9 * npt + pt];
+    }
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      const int i = i0 + u;
+      if (i > nx) break;
+      const float m = 1.f / (bv[u] - av[u] * cprev);
+      cprev = cv[u] * m;
+      dprev = (dv[u] - av[u] * dprev) * m;
+      cprow[(size_t)(i - 1) * si] = cprev;
+      erow[(size_t)i * si] = dprev;
+    }
+  }
+  float x = 0.f;
+  for (int i0 = nx; i0 >= 1; i0 -= kChunk) {
+    float dv[kChunk], cv[kChunk];
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      const int i = i0 - u;
+      if (i < 1) break;
+      dv[u] = erow[(size_t)i * si];
+      cv[u] = cprow[(size_t)(i - 1) * si];
+    }
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      const int i = i0 - u;
+      if (i < 1) break;
+      x = dv[u] - cv[u] * x;
+      erow[(size_t)i * si] = x;
+      if (i == nx - 1) erow[0] = x;
+      if (i == 2) erow[(size_t)(nx + 1) * si] = x;
+    }
+  }
+}
+
+// y-lines i = i0, i0+istep, ... (ncol of them), all problems
+__global__ void __launch_bounds__(64) k_f_yline(FastDev g, int level, int i0, int istep, int ncol) {
+  if (*g.alldone) return;
+  const LvF L = g.lv[level - 1];
+  const int P = g.P;
+  const long n = (long)ncol * P;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(t % P);
+    if (g.done[p]) continue;
+    yline_solve(L, P, p, i0 + istep * (int)(t / P), (float)g.kx2[p], g.orth != 0);
+  }
+}
+
+// x-lines j = j0, j0+2, ... (nrow of them), all problems
+__global__ void __launch_bounds__(64) k_f_xline(FastDev g, int level, int j0, int nrow) {
+  if (*g.alldone) return;
+  const LvF L = g.lv[level - 1];
+  const int P = g.P;
+  const long n = (long)nrow * P;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(t % P);
+    if (g.done[p]) continue;
+    xline_solve(L, P, p, j0 + 2 * (int)(t / P), (float)g.kx2[p], g.orth != 0);
+  }
+}
+
+struct LinePhase {
+  int i0, istep, ncol;
+};
+// y-line colour col (1, 2) of a level with nx columns as one or two ordered
+// phases.  With nx odd the colours are odd and even i.  With nx even (only
+// possible on the coarsest level) the periodic wrap couples i = 1 to
+// i = nx-1 and i = nx to i = 2, so i = 1 and i = nx go in phases of their own.
+__host__ __device__ inline int line_phases(int nx, int col, LinePhase *ph) {
+  if (nx % 2 == 1) {
+    ph[0] = (col == 1) ? LinePhase{1, 2, (nx + 1) / 2} : LinePhase{2, 2, (nx - 1) / 2};
+    return 1;
+  }
+  if (col == 1) {
+    ph[0] = LinePhase{3, 2, nx / 2 - 1};
+    ph[1] = LinePhase{1, 1, 1};
+  } else {
+    ph[0] = LinePhase{2, 2, nx / 2 - 1};
+    ph[1] = LinePhase{nx, 1, 1};
+  }
+  return 2;
+}
+
+// The coarsest level: `sweeps` alternating-direction sweeps, one thread per
+// problem (the level has a few tens of points), in the same order as the
+// per-line kernels use.
+__global__ void k_f_coarsest(FastDev g, int sweeps) {
+  if (*g.alldone) return;
+  const LvF L = g.lv[0];
+  const int P = g.P;
+  const bool orth = g.orth != 0;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+    if (g.done[p]) continue;
+    const float kx2 = (float)g.kx2[p];
+    for (int sw = 0; sw < sweeps; ++sw) {
+      for (int col = 1; col <= 2; ++col) {
+        LinePhase ph[2];
+        const int nph = line_phases(L.nx, col, ph);
+        for (int q = 0; q < nph; ++q)
+          for (int c = 0; c < ph[q].ncol; ++c) yline_solve(L, P, p, ph[q].i0 + ph[q].istep * c, kx2, orth);
+      }
+      for (int col = 1; col <= 2; ++col)
+        for (int j = col; j <= L.ny; j += 2) xline_solve(L, P, p, j, kx2, orth);
+    }
+  }
+}
+
+// residual of the correction equation at a level (FP32) into the scratch
+__global__ void k_f_resid32(FastDev g, int level) {
+  if (*g.alldone) return;
+  const LvF L = g.lv[level - 1];
+  const int P = g.P;
+  const int nx = L.nx;
+  const size_t npt = (size_t)nx * L.ny;
+  const size_t si = P, sj = (size_t)(nx + 2) * P;
+  const long n = (long)npt * P;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(t % P);
+    if (g.done[p]) continue;
+    const long pt = t / P;
+    const int i = 1 + (int)(pt % nx), j = 1 + (int)(pt / nx);
+    const float *ep = &L.e[((size_t)j * (nx + 2) + i) * P + p];
+    const float *cf = L.cof;
+    float s = cf[pt] * ep[si] + cf[2 * npt + pt] * ep[sj] + cf[4 * npt + pt] * ep[-(long)si] +
+              cf[6 * npt + pt] * ep[-(long)sj];
+    if (!g.orth)
+      s += cf[npt + pt] * ep[si + sj] + cf[3 * npt + pt] * ep[sj - si] + cf[5 * npt + pt] * ep[-(long)(si + sj)] +
+           cf[7 * npt + pt] * ep[si - sj];
+    const float kx2 = (float)g.kx2[p];
+    const float c9 = ((-kx2 * cf[10 * npt + pt]) - cf[8 * npt + pt]) + cf[9 * npt + pt];
+    s += c9 * ep[0];
+    g.scr[((size_t)j * (nx + 2) + i) * P + p] = L.r[pt * P + p] - s;
+  }
+}
+
+// full weighting (res2, mudcom.f:120-257) to the coarse rhs; e_coarse = 0
+__global__ void k_f_restrict(FastDev g, int level) {
+  if (*g.alldone) return;
+  const LvF F = g.lv[level - 1], C = g.lv[level - 2];
+  const int P = g.P;
+  const int nx = F.nx, ny = F.ny, ncx = C.nx, ncy = C.ny;
+  const int ix = (ncx == nx) ? 0 : 1, jy = (ncy == ny) ? 0 : 1;
+  const long n = (long)(ncx + 2) * (ncy + 2) * P;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(t % P);
+    if (g.done[p]) continue;
+    const long q = t / P;
+    const int ic = (int)(q % (ncx + 2)), jc = (int)(q / (ncx + 2));
+    C.e[q * P + p] = 0.f;
+    if (ic < 1 || ic > ncx || jc < 1 || jc > ncy) continue;
+    const int i = ic + ix * (ic - 1), j = jc + jy * (jc - 1);
+    int im1 = i - 1, ip1 = i + 1, jm1 = j - 1, jp1 = j + 1;
+    if (ic == 1 || ic == ncx) {
+      im1 = max(i - 1, 2);
+      ip1 = min(i + 1, nx - 1);
+      if (i == 1) im1 = nx - 1;
+      if (i == nx) ip1 = 2;
+    }
+    if (jc == 1 || jc == ncy) {
+      jm1 = max(j - 1, 2);
+      jp1 = min(j + 1, ny - 1);
+    }
+    auto R = [&](int a, int b) { return g.scr[((size_t)b * (nx + 2) + a) * P + p]; };
+    C.r[((size_t)(jc - 1) * ncx + (ic - 1)) * P + p] =
+        (R(im1, jm1) + R(ip1, jm1) + R(im1, jp1) + R(ip1, jp1) + 2.f * (R(im1, j) + R(ip1, j) + R(i, jm1) + R(i, jp1)) +
+         4.f * R(i, j)) * .0625f;
+  }
+}
+
+// cubic/linear prolongation (prolon1/prolon2, mudcom.f:261-499) of the
+// coarse correction, stage 1: rows given directly by prolon1, into scratch
+template <typename F>
+__device__ __forceinline__ float prolon1f(int i, int ncx, int nx, bool cubic, F p) {
+  if (ncx == nx) return p(i);
+  if (!cubic) {
+    if (i & 1) return p((i + 1) / 2);
+    return 0.5f * (p(i / 2) + p(i / 2 + 1));
+  }
+  auto q = [&](int ii) { return p((ii + 1) / 2); };
+  if (i & 1) return q(i);
+  if (i >= 4 && i <= nx - 3) return (-q(i - 3) + 9.f * (q(i - 1) + q(i + 1)) - q(i + 3)) * .0625f;
+  if (i == 2) return (-q(nx - 2) + 9.f * (q(1) + q(3)) - q(5)) * .0625f;
+  return (-q(nx - 4) + 9.f * (q(nx - 2) + q(nx)) - q(3)) * .0625f;
+}
+
+__global__ void k_f_prolong_x(FastDev g, int level) {
+  if (*g.alldone) return;
+  const LvF F = g.lv[level - 1], C = g.lv[level - 2];
+  const int P = g.P;
+  const int nx = F.nx, ny = F.ny, ncx = C.nx, ncy = C.ny;
+  const bool ycoarse = ncy < ny;
+  const bool cubic = ncx >= 4;
+  const int nrows = ycoarse ? (ny + 1) / 2 : ny;
+  const long n = (long)nrows * nx * P;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(t % P);
+    if (g.done[p]) continue;
+    const long q = t / P;
+    const int i = 1 + (int)(q % nx), rr = (int)(q / nx);
+    const int j = ycoarse ? 2 * rr + 1 : rr + 1;
+    const int jc = ycoarse ? j / 2 + 1 : j;
+    auto pc = [&](int ic) { return C.e[((size_t)jc * (ncx + 2) + ic) * P + p]; };
+    g.scr[((size_t)j * (nx + 2) + i) * P + p] = prolon1f(i, ncx, nx, cubic, pc);
+  }
+}
+
+// stage 2: the rows between (cubic or linear in y), then e += correction,
+// with the periodic ghosts written together with their sources
+__global__ void k_f_prolong_y(FastDev g, int level) {
+  if (*g.alldone) return;
+  const LvF F = g.lv[level - 1], C = g.lv[level - 2];
+  const int P = g.P;
+  const int nx = F.nx, ny = F.ny, ncy = C.ny;
+  const bool ycoarse = ncy < ny;
+  const bool cubic = ncy >= 4;
+  const long n = (long)nx * ny * P;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(t % P);
+    if (g.done[p]) continue;
+    const long q = t / P;
+    const int i = 1 + (int)(q % nx), j = 1 + (int)(q / nx);
+    auto Q = [&](int jj) { return g.scr[((size_t)jj * (nx + 2) + i) * P + p]; };
+    float v;
+    if (ycoarse && !(j & 1)) {
+      if (!cubic) v = 0.5f * (Q(j - 1) + Q(j + 1));
+      else if (j >= 4 && j <= ny - 3) v = (-Q(j - 3) + 9.f * (Q(j - 1) + Q(j + 1)) - Q(j + 3)) * .0625f;
+      else if (j == 2) v = (5.f * Q(1) + 15.f * Q(3) - 5.f * Q(5) + Q(7)) * .0625f;
+      else v = (5.f * Q(ny) + 15.f * Q(ny - 2) - 5.f * Q(ny - 4) + Q(ny - 6)) * .0625f;
+    } else {
+      v = Q(j);
+    }
+    float &e = E(F, P, i, j, p);
+    const float ne = e + v;
+    e = ne;
+    if (i == nx - 1) E(F, P, 0, j, p) = ne;
+    if (i == 2) E(F, P, nx + 1, j, p) = ne;
+  }
+}
+
+// phi += e at the finest level (FP64), periodic ghosts of phi, and the
+// per-problem max|e| and max|phi| for the singular mode's test.
+__global__ void __launch_bounds__(32 * kRY) k_f_update(FastDev g) {
+  if (*g.alldone) return;
+  const int P = g.P;
+  const int p = blockIdx.x * 32 + threadIdx.x;
+  const int ty = threadIdx.y;
+  const int nx = g.nfx, ny = g.nfy;
+  const size_t npt = (size_t)nx * ny;
+  const LvF &F = g.lv[g.ngrid - 1];
+  double me = 0.0, mp = 0.0;
+  const bool act = (p < P) && !g.done[p];
+  if (act) {
+    for (size_t pt = (size_t)blockIdx.y * kRY + ty; pt < npt; pt += (size_t)gridDim.y * kRY) {
+      const int i = 1 + (int)(pt % nx), j = 1 + (int)(pt / nx);
+      const double e = (double)E(F, P, i, j, p);
+      double *ph = g.phi + ((size_t)j * (nx + 2) + i) * P + p;
+      const double v = *ph + e;
+      *ph = v;
+      g.phif[pt * P + p] = v;
+      if (i == nx - 1) g.phi[((size_t)j * (nx + 2) + 0) * P + p] = v;
+      if (i == 2) g.phi[((size_t)j * (nx + 2) + nx + 1) * P + p] = v;
+      me = fmax(me, fabs(e));
+      mp = fmax(mp, fabs(v));
+    }
+  }
+  __shared__ double red[2][kRY][32];
+  red[0][ty][threadIdx.x] = me;
+  red[1][ty][threadIdx.x] = mp;
+  __syncthreads();
+  if (ty == 0 && act) {
+    for (int y = 1; y < kRY; ++y) {
+      me = fmax(me, red[0][y][threadIdx.x]);
+      mp = fmax(mp, red[1][y][threadIdx.x]);
+    }
+    atomic_max_pos(&g.red[6 * p + 2], me);
+    atomic_max_pos(&g.red[6 * p + 3], mp);
+  }
+}
+
+__global__ void k_f_zero64(double *a, size_t n) {
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) a[t] = 0.0;
+}
+
+unsigned nb(long n, int bs) {
+  long b = (n + bs - 1) / bs;
+  if (b < 1) b = 1;
+  if (b > 65535L * 32) b = 65535L * 32;
+  return (unsigned)b;
+}
+
+}  // namespace
+
+// FP32 copies of the level coefficients and the FP32 work arrays.
+void mgfast_alloc(Ctx &c, int pmax) {
+  MgPlan &PL = c.mg;
+  if (c.mgf_pool) {
+    cudaFree(c.mgf_pool);
+    c.mgf_pool = nullptr;
+  }
+  size_t tot = 0;
+  std::vector<size_t> off(PL.ngrid);
+  for (int l = 0; l < PL.ngrid; ++l) {
+    const MgLevel &L = PL.lv[l];
+    off[l] = tot;
+    tot += (size_t)(L.nx + 2) * (L.ny + 2) * pmax + 2 * (size_t)L.nx * L.ny * pmax + 11 * (size_t)L.nx * L.ny;
+  }
+  const size_t scr_off = tot;
+  tot += (size_t)(PL.nfx + 2) * (PL.nfy + 2) * pmax;
+  EK_CUDA(cudaMalloc(&c.mgf_pool, tot * sizeof(float)));
+  c.mgf_levels.assign(PL.ngrid, {});
+  for (int l = 0; l < PL.ngrid; ++l) {
+    const MgLevel &L = PL.lv[l];
+    float *b = c.mgf_pool + off[l];
+    MgLevelF &F = c.mgf_levels[l];
+    F.e = b;
+    F.r = F.e + (size_t)(L.nx + 2) * (L.ny + 2) * pmax;
+    F.cp = F.r + (size_t)L.nx * L.ny * pmax;
+    F.cof = F.cp + (size_t)L.nx * L.ny * pmax;
+    std::vector<float> cf(PL.cof_host[l].begin(), PL.cof_host[l].end());
+    EK_CUDA(cudaMemcpy(F.cof, cf.data(), sizeof(float) * cf.size(), cudaMemcpyHostToDevice));
+  }
+  c.mgf_scratch = c.mgf_pool + scr_off;
+  c.mgf_pmax = pmax;
+}
+
+// Solve with the mixed-precision iteration; the finest rhs must be in
+// c.mgw.rhs[ngrid-1] (FP64, problem fastest); the solution is left in
+// c.mgw.phif.
+int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_host, ek_mg_stats *st) {
+  MgPlan &PL = c.mg;
+  MgWork &w = c.mgw;
+  if (nprob > c.mgf_pmax || nprob > w.pmax) return EK_ERR_ARG;
+  cudaStream_t s = c.stream;
+  const int bs = 256;
+  const long npt = (long)PL.nfx * PL.nfy;
+  // the singular subset, solved first by the MUDPACK-exact path
+  std::vector<double> kxh;
+  if (!kx2_host) {
+    kxh.resize(nprob);
+    EK_CUDA(cudaMemcpyAsync(kxh.data(), kx2_dev, sizeof(double) * nprob, cudaMemcpyDeviceToHost, s));
+    EK_CUDA(cudaStreamSynchronize(s));
+    kx2_host = kxh.data();
+  }
+  std::vector<int> sing;
+  std::vector<char> is_sing(nprob, 0);
+  for (int p = 0; p < nprob; ++p)
+    if (kx2_host[p] == 0.0) {
+      sing.push_back(p);
+      is_sing[p] = 1;
+    }
+  const int ns = (int)sing.size();
+  ek_mg_stats Ss{};
+  int rs = EK_OK;
+  if (ns > 0) {
+    MgWork &ws = c.mgs;
+    if (ns > ws.pmax) {
+      mg_work_alloc(c, ws, std::max(ns, 2));
+      EK_CUDA(cudaMemsetAsync(ws.kx2, 0, sizeof(double) * ws.pmax, s));
+    }
+    if (ws.idx_host != sing) {
+      EK_CUDA(cudaMemcpyAsync(ws.idx, sing.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s));
+      ws.idx_host = sing;
+    }
+    {
+      KScope ks(c, KC_MG_SETUP, 16.0 * npt * ns);
+      k_f_gather<<<nb(npt * ns, bs), bs, 0, s>>>(w.rhs[PL.ngrid - 1], nprob, ws.rhs[PL.ngrid - 1], ns, ws.idx, npt);
+      after_launch(c);
+    }
+    rs = mg_solve_exact(c, ws, ns, ws.kx2, &Ss, kSingularMaxCycles);
+    if (rs != EK_OK && rs != EK_ERR_NOT_CONVERGED) return rs;
+  }
+  FastDev g{};
+  g.P = nprob;
+  g.ngrid = PL.ngrid;
+  g.orth = PL.orth ? 1 : 0;
+  for (int l = 0; l < PL.ngrid; ++l) {
+    const MgLevelF &F = c.mgf_levels[l];
+    g.lv[l] = LvF{PL.lv[l].nx, PL.lv[l].ny, F.e, F.r, F.cof, F.cp};
+  }
+  g.scr = c.mgf_scratch;
+  g.phi = w.phi[PL.ngrid - 1];
+  g.rhs = w.rhs[PL.ngrid - 1];
+  g.cof = PL.lv[PL.ngrid - 1].cof;
+  g.nfx = PL.nfx;
+  g.nfy = PL.nfy;
+  g.kx2 = kx2_dev;
+  g.phif = w.phif;
+  g.red = w.red;
+  g.done = w.done;
+  g.cycles = w.cycles;
+  g.alldone = w.alldone;
+  g.tol = c.p.mg_tol;
+
+  {
+    KScope ks(c, KC_MG_SETUP, 8.0 * (PL.nfx + 2) * (PL.nfy + 2) * nprob * 2);
+    EK_CUDA(cudaMemsetAsync(w.flags, 0, sizeof(int) * (2 * w.pmax + 4), s));
+    EK_CUDA(cudaMemsetAsync(w.red, 0, sizeof(double) * (6 * w.pmax + 8), s));
+    if (ns > 0) {
+      k_f_mark<<<1, 128, 0, s>>>(w.done, c.mgs.idx, ns);
+      after_launch(c);
+    }
+    const size_t nph = (size_t)(PL.nfx + 2) * (PL.nfy + 2) * nprob;
+    k_f_zero64<<<nb((long)nph, bs), bs, 0, s>>>(g.phi, nph);
+    after_launch(c);
+    const size_t nf = (size_t)PL.nfx * PL.nfy * nprob;
+    k_f_zero64<<<nb((long)nf, bs), bs, 0, s>>>(w.phif, nf);
+    after_launch(c);
+  }
+  const int gx = (nprob + 31) / 32;
+  const int gy = (int)std::min<long>((npt + kRY - 1) / kRY, std::max<long>(1, 2048 / gx));
+  // one alternating-direction zebra sweep at level l: y-lines (colours
+  // 1, 2), then x-lines (rows 1, 3, ... then 2, 4, ...); the post-smoothing
+  // sweep takes the colours in the reverse order.
+  auto relax = [&](int l, bool post) {
+    const MgLevel &L = PL.lv[l - 1];
+    KScope ks(c, KC_MG_RELAX, 4.0 * nprob * L.nx * L.ny * 10);
+    for (int k = 0; k < 2; ++k) {
+      const int col = post ? 2 - k : 1 + k;
+      LinePhase ph[2];
+      const int nph = line_phases(L.nx, col, ph);
+      for (int q = 0; q < nph; ++q) {
+        if (ph[q].ncol <= 0) continue;
+        k_f_yline<<<nb((long)ph[q].ncol * nprob, 64), 64, 0, s>>>(g, l, ph[q].i0, ph[q].istep, ph[q].ncol);
+        after_launch(c);
+      }
+    }
+    for (int k = 0; k < 2; ++k) {
+      const int col = post ? 2 - k : 1 + k;
+      const int nrow = (L.ny - col) / 2 + 1;
+      k_f_xline<<<nb((long)nrow * nprob, 64), 64, 0, s>>>(g, l, col, nrow);
+      after_launch(c);
+    }
+  };
+  const int maxit = c.p.mg_maxcy;
+  c.poll.init();
+  c.poll.reset();
+  for (int it = 0; it <= maxit; ++it) {
+    {
+      KScope ks(c, KC_MG_CHECK, 8.0 * nprob * npt * 3 + 4.0 * nprob * npt);
+      k_f_resid64<<<dim3(gx, gy), dim3(32, kRY), 0, s>>>(g);
+      after_launch(c);
+      k_f_check<<<1, 256, 0, s>>>(g, it, it == maxit ? 1 : 0);
+      after_launch(c);
+    }
+    if (it == maxit || c.poll.after_check(w.alldone, s)) break;
+    // one FP32 V(1,1) cycle on A e = r from e = 0
+    for (int l = PL.ngrid; l >= 1; --l) {
+      const MgLevel &L = PL.lv[l - 1];
+      if (l == 1) {
+        const int sweeps = std::max(8, (L.nx + L.ny) / 2);
+        KScope ks(c, KC_MG_RELAX, 4.0 * nprob * L.nx * L.ny * 10 * sweeps);
+        k_f_coarsest<<<nb(nprob, 64), 64, 0, s>>>(g, sweeps);
+        after_launch(c);
+        break;
+      }
+      relax(l, false);
+      const MgLevel &C = PL.lv[l - 2];
+      KScope ks(c, KC_MG_TRANSFER, 4.0 * nprob * (4.0 * L.nx * L.ny + 2.0 * (C.nx + 2) * (C.ny + 2)));
+      k_f_resid32<<<nb((long)L.nx * L.ny * nprob, bs), bs, 0, s>>>(g, l);
+      after_launch(c);
+      k_f_restrict<<<nb((long)(C.nx + 2) * (C.ny + 2) * nprob, bs), bs, 0, s>>>(g, l);
+      after_launch(c);
+    }
+    for (int l = 2; l <= PL.ngrid; ++l) {
+      const MgLevel &L = PL.lv[l - 1];
+      {
+        KScope ks(c, KC_MG_TRANSFER, 4.0 * nprob * 4.0 * L.nx * L.ny);
+        k_f_prolong_x<<<nb((long)(L.ny + 1) * L.nx * nprob, bs), bs, 0, s>>>(g, l);
+        after_launch(c);
+        k_f_prolong_y<<<nb((long)L.nx * L.ny * nprob, bs), bs, 0, s>>>(g, l);
+        after_launch(c);
+      }
+      relax(l, true);
+    }
+    {
+      KScope ks(c, KC_MG_CHECK, 8.0 * nprob * npt * 3);
+      k_f_update<<<dim3(gx, gy), dim3(32, kRY), 0, s>>>(g);
+      after_launch(c);
+    }
+  }
+  if (ns > 0) {
+    KScope ks(c, KC_MG_SETUP, 16.0 * npt * ns);
+    k_f_scatter<<<nb(npt * ns, bs), bs, 0, s>>>(c.mgs.phif, ns, w.phif, nprob, c.mgs.idx, npt);
+    after_launch(c);
+  }
+  std::vector<int> cyc(nprob), done(nprob);
+  std::vector<double> meas(6 * nprob);
+  EK_CUDA(cudaMemcpyAsync(cyc.data(), w.cycles, sizeof(int) * nprob, cudaMemcpyDeviceToHost, s));
+  EK_CUDA(cudaMemcpyAsync(done.data(), w.done, sizeof(int) * nprob, cudaMemcpyDeviceToHost, s));
+  EK_CUDA(cudaMemcpyAsync(meas.data(), w.red, sizeof(double) * 6 * nprob, cudaMemcpyDeviceToHost, s));
+  EK_CUDA(cudaStreamSynchronize(s));
+  ek_mg_stats S{};
+  S.nprob = nprob;
+  S.min_cycles = (nprob > ns) ? (1 << 30) : Ss.min_cycles;
+  S.max_cycles = Ss.max_cycles;
+  S.n_not_converged = Ss.n_not_converged;
+  S.max_relchange = Ss.max_relchange;
+  S.max_residual = Ss.max_residual;
+  if (ns > 0) S.min_cycles = std::min(S.min_cycles, Ss.min_cycles);
+  for (int p = 0; p < nprob; ++p) {
+    if (is_sing[p]) continue;
+    S.min_cycles = std::min(S.min_cycles, cyc[p]);
+    S.max_cycles = std::max(S.max_cycles, cyc[p]);
+    if (done[p] != 1) S.n_not_converged++;
+    S.max_residual = std::max(S.max_residual, meas[6 * p + 4]);
+  }
+  c.last_stats = S;
+  if (st) *st = S;
+  return S.n_not_converged ? EK_ERR_NOT_CONVERGED : EK_OK;
+}
+
+}  // namespace ek

@@ -42,7 +42,7 @@ class EkParams(C.Structure):
         ("mg_ixp", C.c_int), ("mg_jyq", C.c_int), ("mg_iex", C.c_int), ("mg_jey", C.c_int),
         ("mg_maxcy", C.c_int), ("mg_kcycle", C.c_int), ("mg_iprer", C.c_int), ("mg_ipost", C.c_int),
         ("mg_intpol", C.c_int), ("mg_stop", C.c_int), ("mg_tol", C.c_double),
-        ("quirk_phi_fp32", C.c_int), ("sponge_type", C.c_int), ("les", C.c_int),
+        ("quirk_phi_fp32", C.c_int), ("mg_fast", C.c_int), ("sponge_type", C.c_int), ("les", C.c_int),
     ]
 
 

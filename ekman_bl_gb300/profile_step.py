@@ -23,9 +23,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=1)
     ap.add_argument("--tol", type=float, default=1e-8, help="relative residual; 0 = MUDPACK's own rule")
     ap.add_argument("--timing", action="store_true")
+    ap.add_argument("--nx", type=int, default=0, help="override NX (smaller cases for full ncu captures)")
     args = ap.parse_args()
     ekbuild.build()
     w = WORKLOADS[args.workload]
+    if args.nx:
+        w.nx = args.nx
+
     stop = EK_MG_STOP_RESIDUAL if args.tol > 0 else EK_MG_STOP_RELCHANGE
     if args.tol > 0:
         w.mg_tol = args.tol

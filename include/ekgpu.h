@@ -86,6 +86,10 @@ typedef struct ek_params {
   int mg_stop;               /* EK_MG_STOP_*                                            */
   double mg_tol;             /* tolmax: reference REAL*4 10.0**(-6) widened to REAL*8   */
   int quirk_phi_fp32;        /* Q1: CMPLX(P_TMP2,P_TMP) rounds phi to REAL*4 (duct.F90:2664) */
+  int mg_fast;               /* 0: MUDPACK's own iteration (FP64, point smoother, the parity
+                                default); 1: mixed precision -- FP64 residual and update around FP32
+                                V-cycles with a y-line smoother, same discrete operator, needs
+                                mg_stop = EK_MG_STOP_RESIDUAL; mg_maxcy caps the corrections   */
   int sponge_type;           /* SPONGE_TYPE (only 0 supported)                          */
   int les;                   /* LES (only 0 supported)                                  */
 } ek_params;

@@ -146,3 +146,52 @@ def test_fft_entry_point_rejects_bad_size():
     with pytest.raises(EkError) as e:
         fft_x(True, 48, 16, 1, 1, 1)
     assert "power of two" in str(e.value)
+
+
+@pytest.mark.parametrize("case", ["small", "sheared", "refgrid"])
+def test_mixed_precision_poisson_reaches_tolerance(case):
+    """mg_fast = 1: FP64 refinement around FP32 line-smoothed V-cycles.  The
+    FP64 residual of the returned phi, recomputed with the oracle's operator,
+    must be <= tol for every non-singular problem, and phi must agree with
+    the oracle's FP64 solve at the same tolerance."""
+    p, xp, yp, _ = CASES[case]()
+    p.mg_stop, p.mg_tol, p.mg_maxcy, p.mg_fast = 1, 1e-10, 60, 1
+    g = DuctSolver(p, metrics_from_grid(p, xp, yp))
+    po_ = CASES[case]()[0]
+    po_.mg_stop, po_.mg_tol, po_.mg_maxcy = 1, 1e-12, 200
+    o = ekref.Oracle(po_, ekref.metrics_from_grid(po_, xp, yp))
+    rng = np.random.default_rng(12)
+    # the case's own wavenumbers kx = 2 pi k / LX, k = 1, 2, 5, NX/3
+    kx2 = np.array([(2 * math.pi * k / p.lx) ** 2 for k in (1, 2, 5, p.nx // 3)])
+    rhs = rng.standard_normal((len(kx2), p.ny + 2, p.nz + 2))
+    rhs[:, 0, :] = 0
+    rhs[:, -1, :] = 0
+    pg, sg, cg = g.multigrid_mudpack(rhs, kx2)
+    assert cg == 0 and sg["n_not_converged"] == 0, sg
+    assert sg["max_cycles"] <= 40, sg
+    po, so, co = o.poisson(rhs, kx2)
+    for q in range(len(kx2)):
+        r = rhs[q] - o.mg_apply(kx2[q], pg[q])
+        assert np.linalg.norm(r) / np.linalg.norm(rhs[q]) <= 1.05e-10, q
+        assert rel_l2(pg[q], po[q]) < 1e-6, q
+
+
+def test_mixed_precision_steps_track_oracle():
+    """Three RK3 steps with the mixed-precision projection vs the oracle's
+    FP64 projection at the same 1e-10 residual."""
+    p, xp, yp, st = small_case()
+    p.mg_stop, p.mg_tol, p.mg_maxcy = 1, 1e-10, 60
+    m = metrics_from_grid(p, xp, yp)
+    p.mg_fast = 1
+    g = DuctSolver(p, m)
+    po_ = small_case()[0]
+    po_.mg_stop, po_.mg_tol, po_.mg_maxcy = 1, 1e-10, 200
+    o = ekref.Oracle(po_, ekref.metrics_from_grid(po_, xp, yp))
+    g.upload(*st)
+    o.upload(*st)
+    g.step(3)
+    o.step(3)
+    a, b = g.download(), o.download()
+    for name, x, y in zip(("CU1", "CU2", "CU3", "CP", "CTH"), a, b):
+        assert rel_l2(x, y) < 1e-7, name
+    assert g.divergence() < 1e-7
