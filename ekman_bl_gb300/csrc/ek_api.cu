@@ -340,6 +340,12 @@ void ekgpu_destroy(ek_ctx *h) {
   if (c.mgf_pool) cudaFree(c.mgf_pool);
   if (c.mg.ops_dev) cudaFree(c.mg.ops_dev);
   c.poll.destroy();
+  if (c.aux_stream) {
+    cudaStreamSynchronize(c.aux_stream);
+    cudaStreamDestroy(c.aux_stream);
+  }
+  if (c.ev_fork) cudaEventDestroy(c.ev_fork);
+  if (c.ev_join) cudaEventDestroy(c.ev_join);
   for (auto &r : c.trec) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : c.evpool) cudaEventDestroy(e);
   if (c.own_stream) cudaStreamDestroy(c.own_stream);

@@ -189,6 +189,8 @@ struct Ctx {
   int mgf_pmax = 0;
   ek_mg_stats last_stats{};
   StopPoll poll;
+  cudaStream_t aux_stream = nullptr;  // the kx^2 = 0 batch runs here, beside the FP32 cycles
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // divergence check
   double *div_part = nullptr;
   double last_div = 0.0;
@@ -283,6 +285,8 @@ int finish_divergence(Ctx &c, double *div_out);
 // needs it).
 int mg_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_host, ek_mg_stats *st);
 int mg_solve_exact(Ctx &c, MgWork &w, int nprob, const double *kx2_dev, ek_mg_stats *st, int max_cycles);
+void mg_exact_enqueue(Ctx &c, MgWork &w, int nprob, const double *kx2_dev, int max_cycles, bool poll);
+int mg_exact_stats(Ctx &c, MgWork &w, int nprob, ek_mg_stats *st);
 constexpr int kSingularMaxCycles = 6;  // MULTIGRID_MUDPACK's cap for the kx = 0 mode
 void mg_alloc(Ctx &c, int pmax);
 void mg_work_alloc(Ctx &c, MgWork &w, int pmax);

@@ -760,8 +760,15 @@ int mg_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_host, e
 // solution is left in w.phif.  max_cycles > 0 stops issuing the schedule
 // after that many k-cycles (a batch whose problems all stop by then).
 int mg_solve_exact(Ctx &c, MgWork &w, int nprob, const double *kx2_dev, ek_mg_stats *st, int max_cycles) {
-  MgPlan &PL = c.mg;
   if (nprob > w.pmax) return EK_ERR_ARG;
+  mg_exact_enqueue(c, w, nprob, kx2_dev, max_cycles, true);
+  return mg_exact_stats(c, w, nprob, st);
+}
+
+// The launches of one exact solve on c.stream.  poll: stop issuing cycles
+// once every problem is done (the host waits on the stream's progress).
+void mg_exact_enqueue(Ctx &c, MgWork &w, int nprob, const double *kx2_dev, int max_cycles, bool poll) {
+  MgPlan &PL = c.mg;
   MgDev g{};
   g.P = nprob;
   g.ngrid = PL.ngrid;
@@ -830,8 +837,10 @@ int mg_solve_exact(Ctx &c, MgWork &w, int nprob, const double *kx2_dev, ek_mg_st
   int ncheck = 0, maxcheck = 0;
   for (const MgOp &op : PL.ops) maxcheck += (op.kind == OP_CHECK);
   if (max_cycles > 0) maxcheck = std::min(maxcheck, max_cycles);
-  c.poll.init();
-  c.poll.reset();
+  if (poll) {
+    c.poll.init();
+    c.poll.reset();
+  }
   bool stop = false;
   while (o < nops && ncheck < maxcheck && !stop) {
     const MgOp &op = PL.ops[o];
@@ -927,7 +936,7 @@ int mg_solve_exact(Ctx &c, MgWork &w, int nprob, const double *kx2_dev, ek_mg_st
         after_launch(c);
         k_check_finish<<<1, 256, 0, s>>>(g, op.count, ncheck == maxcheck ? 1 : 0);
         after_launch(c);
-        if (c.poll.after_check(w.alldone, s)) stop = true;
+        if (poll && c.poll.after_check(w.alldone, s)) stop = true;
         break;
       }
       default:
@@ -935,7 +944,11 @@ int mg_solve_exact(Ctx &c, MgWork &w, int nprob, const double *kx2_dev, ek_mg_st
     }
     ++o;
   }
-  // stats
+}
+
+// Per-problem results of an exact solve in w (synchronises c.stream).
+int mg_exact_stats(Ctx &c, MgWork &w, int nprob, ek_mg_stats *st) {
+  cudaStream_t s = c.stream;
   std::vector<int> cyc(nprob), done(nprob);
   std::vector<double> meas(nprob);
   EK_CUDA(cudaMemcpyAsync(cyc.data(), w.cycles, sizeof(int) * nprob, cudaMemcpyDeviceToHost, s));

@@ -317,6 +317,140 @@ __global__ void __launch_bounds__(64) k_f_xline(FastDev g, int level, int j0, in
   }
 }
 
+// Partitioned line solve: one block per (line, 32 problems), lanes over the
+// problems (coalesced, the layout is problem fastest), warps over K segments
+// of the line.  The line's n rows are K segments of <= kSegMax interior rows
+// separated by K-1 separator rows.  Each warp eliminates its segment in
+// registers, expressing every row as x = delta + gamma X0 - beta x(next) with
+// X0, X1 the separators before and after it; the first and last rows in
+// terms of (X0, X1) give a tridiagonal system for the separators, which lane
+// p of warp 0 solves from shared memory; then every warp back-substitutes.
+// XL: x-line (along i, the periodic wrap couplings taken from the ghosts'
+// current values); else y-line (along j).
+constexpr int kSegMax = 16;
+enum { SH_A, SH_B, SH_C, SH_D, SH_YF, SH_VF, SH_WF, SH_YL, SH_VL, SH_WL, SH_S, SH_N };
+template <bool XL>
+__global__ void __launch_bounds__(512) k_f_pline(FastDev g, int level, int l0, int lstep, int mb, int me) {
+  if (*g.alldone) return;
+  extern __shared__ float sh[];
+  const int K = blockDim.y;
+  auto S = [&](int arr, int seg) -> float & { return sh[((size_t)arr * K + seg) * 32 + threadIdx.x]; };
+  const LvF L = g.lv[level - 1];
+  const int P = g.P;
+  const int nx = L.nx, ny = L.ny;
+  const int s = threadIdx.y;
+  const int p = blockIdx.y * 32 + threadIdx.x;
+  const bool act = (p < P) && !g.done[p];
+  const int pp = act ? p : 0;
+  const int line = l0 + lstep * (int)blockIdx.x;
+  const int m = mb + (s < me ? 1 : 0);
+  const int lo = 1 + s * (mb + 1) + min(s, me);
+  const size_t npt = (size_t)nx * ny;
+  const size_t si = P, sj = (size_t)(nx + 2) * P;
+  const float kx2 = (float)g.kx2[pp];
+  const float *cf = L.cof;
+  const bool orth = g.orth != 0;
+  // row k of the line: a x(k-1) + b x(k) + c x(k+1) = d
+  auto row = [&](int k, float &a, float &b, float &c, float &d) {
+    const int i = XL ? k : line, j = XL ? line : k;
+    const size_t pt = (size_t)(j - 1) * nx + (i - 1);
+    const float *ep = &L.e[((size_t)j * (nx + 2) + i) * P + pp];
+    b = ((-kx2 * cf[10 * npt + pt]) - cf[8 * npt + pt]) + cf[9 * npt + pt];
+    float dd = L.r[pt * P + pp];
+    if (XL) {
+      a = cf[4 * npt + pt];
+      c = cf[pt];
+      dd = dd - cf[2 * npt + pt] * ep[sj] - cf[6 * npt + pt] * ep[-(long)sj];
+      if (i == 1) { dd -= a * ep[-(long)si]; a = 0.f; }
+      if (i == nx) { dd -= c * ep[si]; c = 0.f; }
+    } else {
+      a = cf[6 * npt + pt];
+      c = cf[2 * npt + pt];
+      dd = dd - cf[pt] * ep[si] - cf[4 * npt + pt] * ep[-(long)si];
+    }
+    if (!orth)
+      dd = dd - cf[npt + pt] * ep[si + sj] - cf[3 * npt + pt] * ep[sj - si] - cf[5 * npt + pt] * ep[-(long)(si + sj)] -
+           cf[7 * npt + pt] * ep[si - sj];
+    d = dd;
+  };
+  auto store = [&](int k, float x) {
+    const int i = XL ? k : line, j = XL ? line : k;
+    L.e[((size_t)j * (nx + 2) + i) * P + p] = x;
+    if (i == nx - 1) L.e[((size_t)j * (nx + 2)) * P + p] = x;
+    if (i == 2) L.e[((size_t)j * (nx + 2) + nx + 1) * P + p] = x;
+  };
+  float dl[kSegMax], gm[kSegMax], bt[kSegMax];
+  float yl = 0.f, vl = 0.f, wl = 0.f;
+  {
+    float bprev = 0.f, dprev = 0.f, gprev = 1.f;
+#pragma unroll
+    for (int u = 0; u < kSegMax; ++u) {
+      float a, b, c, d;
+      row(lo + min(u, m - 1), a, b, c, d);
+      const float inv = 1.f / (b - a * bprev);
+      bprev = c * inv;
+      dprev = (d - a * dprev) * inv;
+      gprev = -a * gprev * inv;
+      bt[u] = bprev;
+      dl[u] = dprev;
+      gm[u] = gprev;
+      const bool last = (u == m - 1);
+      yl = last ? dprev : yl;
+      vl = last ? gprev : vl;
+      wl = last ? -bprev : wl;
+    }
+  }
+  float yf = yl, vf = vl, wf = wl;
+#pragma unroll
+  for (int u = kSegMax - 2; u >= 0; --u)
+    if (u < m - 1) {
+      yf = dl[u] - bt[u] * yf;
+      vf = gm[u] - bt[u] * vf;
+      wf = -bt[u] * wf;
+    }
+  S(SH_YF, s) = yf; S(SH_VF, s) = vf; S(SH_WF, s) = wf;
+  S(SH_YL, s) = yl; S(SH_VL, s) = vl; S(SH_WL, s) = wl;
+  if (s < K - 1) {
+    float a, b, c, d;
+    row(lo + m, a, b, c, d);
+    S(SH_A, s) = a; S(SH_B, s) = b; S(SH_C, s) = c; S(SH_D, s) = d;
+  }
+  __syncthreads();
+  if (s == 0 && K > 1) {
+    // separators t = 0..K-2: A S(t-1) + B S(t) + C S(t+1) = D
+    float cpv = 0.f, dpv = 0.f;
+    for (int t = 0; t < K - 1; ++t) {
+      const float a = S(SH_A, t), c = S(SH_C, t);
+      const float A = a * S(SH_VL, t);
+      const float B = S(SH_B, t) + a * S(SH_WL, t) + c * S(SH_VF, t + 1);
+      const float C = c * S(SH_WF, t + 1);
+      const float D = S(SH_D, t) - a * S(SH_YL, t) - c * S(SH_YF, t + 1);
+      const float inv = 1.f / (B - A * cpv);
+      cpv = C * inv;
+      dpv = (D - A * dpv) * inv;
+      S(SH_A, t) = cpv;  // c' and d' of the separator system
+      S(SH_D, t) = dpv;
+    }
+    float x = 0.f;
+    for (int t = K - 2; t >= 0; --t) {
+      x = S(SH_D, t) - S(SH_A, t) * x;
+      S(SH_S, t) = x;
+    }
+  }
+  __syncthreads();
+  if (!act) return;
+  const float X0 = (s > 0) ? S(SH_S, s - 1) : 0.f;
+  const float X1 = (s < K - 1) ? S(SH_S, s) : 0.f;
+  float x = 0.f;
+#pragma unroll
+  for (int u = kSegMax - 1; u >= 0; --u)
+    if (u < m) {
+      x = dl[u] + gm[u] * X0 - bt[u] * ((u == m - 1) ? X1 : x);
+      store(lo + u, x);
+    }
+  if (s < K - 1) store(lo + m, X1);
+}
+
 struct LinePhase {
   int i0, istep, ncol;
 };
@@ -579,6 +713,11 @@ void mgfast_alloc(Ctx &c, int pmax) {
   }
   c.mgf_scratch = c.mgf_pool + scr_off;
   c.mgf_pmax = pmax;
+  if (!c.aux_stream) {
+    EK_CUDA(cudaStreamCreateWithFlags(&c.aux_stream, cudaStreamNonBlocking));
+    EK_CUDA(cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming));
+    EK_CUDA(cudaEventCreateWithFlags(&c.ev_join, cudaEventDisableTiming));
+  }
 }
 
 // Solve with the mixed-precision iteration; the finest rhs must be in
@@ -624,8 +763,18 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
       k_f_gather<<<nb(npt * ns, bs), bs, 0, s>>>(w.rhs[PL.ngrid - 1], nprob, ws.rhs[PL.ngrid - 1], ns, ws.idx, npt);
       after_launch(c);
     }
-    rs = mg_solve_exact(c, ws, ns, ws.kx2, &Ss, kSingularMaxCycles);
-    if (rs != EK_OK && rs != EK_ERR_NOT_CONVERGED) return rs;
+    // the exact solve runs on the auxiliary stream, beside the FP32 cycles
+    EK_CUDA(cudaEventRecord(c.ev_fork, s));
+    EK_CUDA(cudaStreamWaitEvent(c.aux_stream, c.ev_fork, 0));
+    c.stream = c.aux_stream;
+    try {
+      mg_exact_enqueue(c, ws, ns, ws.kx2, kSingularMaxCycles, false);
+    } catch (...) {
+      c.stream = s;
+      throw;
+    }
+    c.stream = s;
+    EK_CUDA(cudaEventRecord(c.ev_join, c.aux_stream));
   }
   FastDev g{};
   g.P = nprob;
@@ -666,6 +815,23 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
   }
   const int gx = (nprob + 31) / 32;
   const int gy = (int)std::min<long>((npt + kRY - 1) / kRY, std::max<long>(1, 2048 / gx));
+  // one partitioned line launch: lines l0, l0+lstep, ... (nline of them)
+  // of length n, all problems
+  auto pline = [&](int l, bool xl, int l0, int lstep, int nline, int n) {
+    const int K = std::max(1, (n + kSegMax) / (kSegMax + 1));
+    if (K > 16) {  // lines longer than 271 rows: one thread per line
+      if (xl) k_f_xline<<<nb((long)nline * nprob, 64), 64, 0, s>>>(g, l, l0, nline);
+      else k_f_yline<<<nb((long)nline * nprob, 64), 64, 0, s>>>(g, l, l0, lstep, nline);
+      after_launch(c);
+      return;
+    }
+    const int mb = (n - K + 1) / K, me = (n - K + 1) % K;
+    const dim3 grid((unsigned)nline, (unsigned)((nprob + 31) / 32)), blk(32, K);
+    const size_t smem = sizeof(float) * SH_N * K * 32;
+    if (xl) k_f_pline<true><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);
+    else k_f_pline<false><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);
+    after_launch(c);
+  };
   // one alternating-direction zebra sweep at level l: y-lines (colours
   // 1, 2), then x-lines (rows 1, 3, ... then 2, 4, ...); the post-smoothing
   // sweep takes the colours in the reverse order.
@@ -676,19 +842,15 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
       const int col = post ? 2 - k : 1 + k;
       LinePhase ph[2];
       const int nph = line_phases(L.nx, col, ph);
-      for (int q = 0; q < nph; ++q) {
-        if (ph[q].ncol <= 0) continue;
-        k_f_yline<<<nb((long)ph[q].ncol * nprob, 64), 64, 0, s>>>(g, l, ph[q].i0, ph[q].istep, ph[q].ncol);
-        after_launch(c);
-      }
+      for (int q = 0; q < nph; ++q)
+        if (ph[q].ncol > 0) pline(l, false, ph[q].i0, ph[q].istep, ph[q].ncol, L.ny);
     }
     for (int k = 0; k < 2; ++k) {
       const int col = post ? 2 - k : 1 + k;
-      const int nrow = (L.ny - col) / 2 + 1;
-      k_f_xline<<<nb((long)nrow * nprob, 64), 64, 0, s>>>(g, l, col, nrow);
-      after_launch(c);
+      pline(l, true, col, 2, (L.ny - col) / 2 + 1, L.nx);
     }
   };
+
   const int maxit = c.p.mg_maxcy;
   c.poll.init();
   c.poll.reset();
@@ -737,6 +899,9 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
     }
   }
   if (ns > 0) {
+    EK_CUDA(cudaStreamWaitEvent(s, c.ev_join, 0));
+    rs = mg_exact_stats(c, c.mgs, ns, &Ss);
+    if (rs != EK_OK && rs != EK_ERR_NOT_CONVERGED) return rs;
     KScope ks(c, KC_MG_SETUP, 16.0 * npt * ns);
     k_f_scatter<<<nb(npt * ns, bs), bs, 0, s>>>(c.mgs.phif, ns, w.phif, nprob, c.mgs.idx, npt);
     after_launch(c);
