@@ -4,11 +4,13 @@ python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
 
 Workload: the stratified Ekman layer 256 x 257 x 193 (NX x NY+2 x NZ+2),
 Re = 800, Pr = 0.7, Ri = 0.1, dt = 5e-4, seeded synthetic fields (laminar
-Ekman spiral + 1% Gaussian noise), FP64, every per-kx Poisson problem driven
-to a relative residual of 1e-8 (the singular kx = 0 mode keeps MUDPACK's own
-rule).  Prints one JSON line: RK3 steps/s over K steps after W warm-up steps,
-timed with CUDA events on the solver's stream; the fields are larger than
-the 126 MB L2, so no flush is needed between steps.  For N > 1 each rank
+Ekman spiral + 1% Gaussian noise), FP64 fields, every per-kx Poisson problem
+driven to a relative residual of 1e-8 (the singular kx = 0 mode keeps
+MUDPACK's own rule).  Prints one JSON line: RK3 steps/s of the batched
+mixed-precision projection over K steps after W warm-up steps, timed with
+CUDA events on the solver's stream, and beside it the plain FP64 MUDPACK
+path on the same workload; the fields are larger than the 126 MB L2, so no
+flush is needed between steps.  For N > 1 each rank
 runs an independent replica on its own GPU (the path does not shard) and
 the value is the sum over ranks.
 """
@@ -102,7 +104,7 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------
-def setup_solver(device_index: int):
+def setup_solver(device_index: int, mg_fast: int = 1):
     import torch
 
     from ekman_bl_gb300 import build as ekbuild
@@ -114,6 +116,7 @@ def setup_solver(device_index: int):
     w = WORKLOADS[WORKLOAD]
     w.mg_tol = MG_TOL
     p, xp, yp, state = workload_setup(w, EK_MG_STOP_RESIDUAL)
+    p.mg_fast = mg_fast
     solver = DuctSolver(p, metrics_from_grid(p, xp, yp))
     stream = torch.cuda.Stream()
     solver.set_stream(stream.cuda_stream)
@@ -122,60 +125,44 @@ def setup_solver(device_index: int):
     return w, p, xp, yp, state, solver, stream
 
 
-def run_gpu(args):
+def time_steps(solver, stream, steps, warmup, clocks_gpu=None):
+    """W untimed steps, then exactly `steps` RK3 steps between CUDA events on
+    the solver's stream; returns (ms, max MG cycles per substep, launches,
+    clock summary or None)."""
     import torch
-    import torch.distributed as dist
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    w, p, xp, yp, state, solver, stream = setup_solver(local)
-    L0 = solver.launch_count()
-
-    # warm-up
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         solver.step(1)
     torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
-    mg_cycles = []
-    with ClockSampler(local) as clk:
+    cycles = []
+    sampler = ClockSampler(clocks_gpu) if clocks_gpu is not None else None
+    if sampler:
+        sampler.__enter__()
+    try:
         torch.cuda.synchronize()
         n0 = solver.launch_count()
         with torch.cuda.stream(stream):
             start.record(stream)
-            for _ in range(args.steps):
+            for _ in range(steps):
                 solver.step(1)
-                mg_cycles.append(solver.mg_stats()["max_cycles"])
+                cycles.append(solver.mg_stats()["max_cycles"])
             end.record(stream)
         torch.cuda.synchronize()
         launches = solver.launch_count() - n0
-    if world > 1:
-        dist.barrier()
-    ms = start.elapsed_time(end)
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    clocks = clk.summary()
-    value = world * args.steps / (ms_max / 1000.0)
-    div = solver.divergence()
+    finally:
+        if sampler:
+            sampler.__exit__(None, None, None)
+    return start.elapsed_time(end), max(cycles) if cycles else None, launches, sampler.summary() if sampler else None
 
-    # per-kernel-class timing of one extra step (events around every launch)
-    solver.set_timing(True)
-    solver.step(1)
-    kt = solver.timing()
-    solver.set_timing(False)
-    ktot = sum(v[0] for v in kt.values())
 
-    # Poisson solves/s: one batched solve of every active kx (real and
-    # imaginary parts together = one complex problem) at 1e-8
-    nkx = p.nx // 3
-    ncomplex = nkx + 1
+def time_poisson(solver, stream, p, nrep=3):
+    """One batched solve of every active kx (real and imaginary parts together
+    = one complex problem) at the tolerance; returns (ms per batch, stats)."""
+    import torch
+
+    ncomplex = p.nx // 3 + 1
     kx2 = torch.tensor([(2 * math.pi * (q // 2) / p.lx) ** 2 for q in range(2 * ncomplex)], dtype=torch.float64,
                        device="cuda")
     gen = torch.Generator(device="cpu").manual_seed(7)
@@ -189,16 +176,48 @@ def run_gpu(args):
     torch.cuda.synchronize()
     solver.multigrid_mudpack_device(rhs.data_ptr(), phi.data_ptr(), kx2.data_ptr(), 2 * ncomplex)
     torch.cuda.synchronize()
-    npois = 3
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     with torch.cuda.stream(stream):
         e0.record(stream)
-        for _ in range(npois):
+        for _ in range(nrep):
             pst, _ = solver.multigrid_mudpack_device(rhs.data_ptr(), phi.data_ptr(), kx2.data_ptr(), 2 * ncomplex)
         e1.record(stream)
     torch.cuda.synchronize()
-    pois_ms = e0.elapsed_time(e1) / npois
+    return e0.elapsed_time(e1) / nrep, pst, ncomplex
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+    # the method measured: mixed-precision batched projection (mg_fast = 1)
+    w, p, xp, yp, state, solver, stream = setup_solver(local, mg_fast=1)
+    if world > 1:
+        dist.barrier()
+    ms, mg_cycles, launches, clocks = time_steps(solver, stream, args.steps, args.warmup, clocks_gpu=local)
+    if world > 1:
+        dist.barrier()
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * args.steps / (ms_max / 1000.0)
+    div = solver.divergence()
+
+    # per-kernel-class timing of one extra step (events around every launch)
+    solver.set_timing(True)
+    solver.step(1)
+    kt = solver.timing()
+    solver.set_timing(False)
+    ktot = sum(v[0] for v in kt.values())
+    pois_ms, pst, ncomplex = time_poisson(solver, stream, p)
     solves_per_s = ncomplex / (pois_ms / 1000.0)
 
     # end to end through the public C ABI with host buffers: H2D of the
@@ -220,6 +239,14 @@ def run_gpu(args):
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / n_e2e
     bytes_state = 5 * int(np.prod(shape)) * 16
+    solver.close()
+
+    # the plain FP64 GPU path (MUDPACK's smoother and cycles) at the same
+    # tolerance, same workload, for the method-vs-plain ratio
+    _, _, _, _, _, plain, pstream = setup_solver(local, mg_fast=0)
+    pms, pcyc, _, _ = time_steps(plain, pstream, args.steps, args.warmup)
+    plain_pois_ms, plain_pst, _ = time_poisson(plain, pstream, p)
+    plain.close()
 
     result = None
     if rank == 0:
@@ -236,6 +263,7 @@ def run_gpu(args):
                     "avg_launch_us": round(dms * 1000.0 / dcnt, 3), "launches_per_step": dcnt,
                     "share_of_step": round(dms / ktot, 4)}
         per_class_gbs = {k: round(v[2] / (v[0] / 1000.0) / 1e9, 1) for k, v in kt.items() if v[0] > 0}
+        plain_value = args.steps / (pms / 1000.0)
         result = {
             "metric": METRIC,
             "value": round(value, 4),
@@ -250,11 +278,18 @@ def run_gpu(args):
             "dtype": "f64",
             "data": "synthetic (seeded laminar Ekman spiral + 1% Gaussian noise; no reference dataset exists)",
             "config": {"workload": WORKLOAD, "nx": p.nx, "ny_plus_2": p.ny + 2, "nz_plus_2": p.nz + 2,
-                       "re": w.re, "pr": w.pr, "ri": w.ri, "delta_t": p.delta_t, "precision": "fp64 plain",
-                       "poisson": f"MUDPACK FMG + W(2,1), 4-colour GS, relative residual {MG_TOL:g}",
-                       "mg_cycles_per_substep_max": max(mg_cycles) if mg_cycles else None,
+                       "re": w.re, "pr": w.pr, "ri": w.ri, "delta_t": p.delta_t,
+                       "method": "batched mixed-precision projection (no learned guess)",
+                       "precision": "fp64 fields; Poisson: FP64 residual refinement around FP32 V-cycles",
+                       "poisson": f"relative residual {MG_TOL:g} per problem; kx=0 by MUDPACK's rule",
+                       "mg_corrections_per_substep_max": mg_cycles,
                        "l2": "fields (100 MB each, ~2.5 GB resident) exceed the 126 MB L2; no flush",
                        "parallelism": f"replicas x{world}"},
+            "plain": {"value": round(plain_value, 4), "unit": "RK3 steps/s", "ms_per_step": round(pms / args.steps, 3),
+                      "method": "FP64 MUDPACK FMG + W(2,1), 4-colour GS", "mg_cycles_per_substep_max": pcyc,
+                      "poisson_solves_per_s": round(ncomplex / (plain_pois_ms / 1000.0), 2),
+                      "poisson_max_cycles": plain_pst["max_cycles"]},
+            "speedup_vs_plain": round(value / (world * plain_value), 3),
             "poisson_solves_per_s": round(solves_per_s, 2),
             "poisson_batch": {"complex_problems": ncomplex, "ms": round(pois_ms, 3),
                               "max_cycles": pst["max_cycles"], "unit": "complex kx problems/s"},
@@ -274,7 +309,6 @@ def run_gpu(args):
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
-    solver.close()
     return result
 
 
