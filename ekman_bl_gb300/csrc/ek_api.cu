@@ -68,6 +68,36 @@ bool supported_bc(const ek_params &p, std::string &why) {
   return true;
 }
 
+// Thomas factors of every field, substep and direction for the current
+// DELTA_T (they depend on it through TEMP1 = NU*H_BAR(RK_STEP)/2).
+void build_adi_factors(Ctx &c) {
+  for (int f = 0; f < 4; ++f)
+    for (int rk = 1; rk <= 3; ++rk)
+      for (int dir = 0; dir < 2; ++dir) {
+        std::vector<double> a, ib, u;
+        adi_factor_host(c, f, rk, dir, c.h_jac, c.h_g11, c.h_g22, a, ib, u);
+        AdiFactors &F = c.adi[f][rk][dir];
+        if (!F.a) {
+          F.a = dalloc<double>(c, a.size());
+          F.ib = dalloc<double>(c, ib.size());
+          F.u = dalloc<double>(c, u.size());
+        }
+        EK_CUDA(cudaMemcpyAsync(F.a, a.data(), sizeof(double) * a.size(), cudaMemcpyHostToDevice, c.stream));
+        EK_CUDA(cudaMemcpyAsync(F.ib, ib.data(), sizeof(double) * ib.size(), cudaMemcpyHostToDevice, c.stream));
+        EK_CUDA(cudaMemcpyAsync(F.u, u.data(), sizeof(double) * u.size(), cudaMemcpyHostToDevice, c.stream));
+        EK_CUDA(cudaStreamSynchronize(c.stream));
+      }
+}
+
+// DELTA_T and the H_BAR of COURANT_CURV_MPI (duct.F90:3655-3668)
+void set_delta_t(Ctx &c, double dt) {
+  c.p.delta_t = dt;
+  c.H_BAR[1] = dt * (8.0 / 15.0);
+  c.H_BAR[2] = dt * (2.0 / 15.0);
+  c.H_BAR[3] = dt * (5.0 / 15.0);
+  build_adi_factors(c);
+}
+
 void run_rem_div(Ctx &c, double temp4, bool update_p, int *mg_status) {
   const int P = 2 * (c.d.NKX + 1);
   launch_divergence_rhs(c, c.mgw.rhs[c.mg.ngrid - 1], P);
@@ -133,6 +163,18 @@ int substep(Ctx &c, int rk) {
   launch_adi(c, 1, rk);
   launch_adi(c, 2, rk);
   launch_adi(c, 3, rk);
+  // COURANT_CURV_MPI (duct.F90:2417-2419): the new DELTA_T applies from the
+  // next substep; this one's projection keeps TEMP4
+  if (p.variable_dt && rk == 3 && p.update_dt > 0 && p.time_step % p.update_dt == 0) {
+    launch_courant(c);
+    double dt = 0.0;
+    EK_CUDA(cudaMemcpyAsync(&dt, c.cfl_dt, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    EK_CUDA(cudaStreamSynchronize(c.stream));
+    if (dt > 0.0) {
+      const double nd = (dt >= p.delta_t_set) ? p.delta_t_set : dt;
+      if (nd != p.delta_t) set_delta_t(c, nd);
+    }
+  }
   // back to Fourier space (duct.F90:2421-2451)
   {
     R2cArgs a{};
@@ -224,6 +266,10 @@ int ekgpu_default_params(ek_params *p) {
   p->mg_maxcy = 6; p->mg_kcycle = 2; p->mg_iprer = 2; p->mg_ipost = 1; p->mg_intpol = 3;
   p->mg_stop = EK_MG_STOP_RELCHANGE;
   p->mg_tol = (double)powf(10.0f, -6.0f);
+  p->ny_s_t = 0;
+  p->nz_s_r = 0;
+  p->nz_s_l = 0;
+  p->save_stats_int = 100;
   return EK_OK;
 }
 
@@ -246,7 +292,11 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
   if (p.ic_type != 7) return reject("only IC_TYPE = 7 boundary rows are supported");
   if (p.mudpack_bc[0] != 0 || p.mudpack_bc[1] != 0 || p.mudpack_bc[2] != 2 || p.mudpack_bc[3] != 2)
     return reject("only MUDPACK_BC = 0 0 2 2 is supported");
-  if (p.sponge_type != 0) return reject("SPONGE_TYPE must be 0");
+  if (p.sponge_type < 0 || p.sponge_type > 2) return reject("SPONGE_TYPE must be 0, 1 or 2");
+  if (p.sponge_type != 0 && p.save_stats_int < 1) return reject("SAVE_STATS_INT must be >= 1 with a sponge");
+  if (p.variable_dt && (p.update_dt < 1 || !(p.cfl > 0.0) || !(p.delta_t_set > 0.0)))
+    return reject("VARIABLE_DT needs UPDATE_DT >= 1, CFL > 0 and DELTA_T_SET > 0");
+  if (p.sponge_type != 0 && p.ny_s_t <= p.ny && p.ny_s_t < 0) return reject("NY_S_T must be >= 0");
   if (p.les != 0) return reject("LES is not supported");
   if (p.f_type != 1 && p.f_type != 2) return reject("F_TYPE must be 1 or 2");
   if (p.n_th < 0 || p.n_th > 1) return reject("N_TH must be 0 or 1");
@@ -319,6 +369,11 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
     c.U2b = dalloc<double>(c, 2 * np);
     c.U3b = c.U2b + np;
     c.div_part = dalloc<double>(c, d.NY2);
+    c.cfl_dt = dalloc<double>(c, 1);
+    c.sponge_sig = dalloc<double>(c, d.NY2 + d.NZ2 + 4);
+    c.sponge_sig_out = c.sponge_sig + d.NY2;
+    c.sponge_red = c.sponge_sig_out + d.NZ2;
+    EK_CUDA(cudaMemsetAsync(c.sponge_sig, 0, sizeof(double) * (d.NY2 + d.NZ2 + 4), c.stream));
     EK_CUDA(cudaStreamSynchronize(c.stream));
   } catch (const CudaError &e) {
     c.err = e.msg;
@@ -362,6 +417,40 @@ int ekgpu_set_stream(ek_ctx *h, void *stream) {
   });
 }
 
+int ekgpu_sponge_profiles(const ek_params *p, const double *xpoint, const double *ypoint, double *sponge_sigma,
+                          double *sponge_sigma_out) {
+  if (!p || !xpoint || !ypoint || !sponge_sigma || !sponge_sigma_out) return EK_ERR_ARG;
+  return sponge_profiles_host(p, xpoint, ypoint, sponge_sigma, sponge_sigma_out);
+}
+
+int ekgpu_set_sponge(ek_ctx *h, const double *sponge_sigma, const double *sponge_sigma_out) {
+  return guarded(h, [&](Ctx &c) {
+    if (!sponge_sigma || !sponge_sigma_out) return fail(c, EK_ERR_ARG, "sponge profile is NULL");
+    EK_CUDA(cudaMemcpyAsync(c.sponge_sig, sponge_sigma, sizeof(double) * c.d.NY2, cudaMemcpyHostToDevice, c.stream));
+    EK_CUDA(cudaMemcpyAsync(c.sponge_sig_out, sponge_sigma_out, sizeof(double) * c.d.NZ2, cudaMemcpyHostToDevice,
+                            c.stream));
+    EK_CUDA(cudaStreamSynchronize(c.stream));
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_set_time(ek_ctx *h, double time, int time_step) {
+  return guarded(h, [&](Ctx &c) {
+    c.p.time = time;
+    c.p.time_step = time_step;
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_get_time(ek_ctx *h, double *time, int *time_step, double *delta_t) {
+  return guarded(h, [&](Ctx &c) {
+    if (time) *time = c.p.time;
+    if (time_step) *time_step = c.p.time_step;
+    if (delta_t) *delta_t = c.p.delta_t;
+    return (int)EK_OK;
+  });
+}
+
 int ekgpu_metrics_from_grid(const ek_params *p, const double *xpoint, const double *ypoint, double *int_jacob,
                             double *gmat_11, double *gmat_12, double *gmat_22, double *cjob_11, double *cjob_12,
                             double *cjob_21, double *cjob_22, double *th_bar) {
@@ -398,21 +487,10 @@ int ekgpu_set_metrics(ek_ctx *h, const ek_metrics *m) {
       if (c.bc_weights == nullptr) c.bc_weights = dalloc<double>(c, w.size());
       EK_CUDA(cudaMemcpy(c.bc_weights, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice));
     }
-    for (int f = 0; f < 4; ++f)
-      for (int rk = 1; rk <= 3; ++rk)
-        for (int dir = 0; dir < 2; ++dir) {
-          std::vector<double> a, ib, u;
-          adi_factor_host(c, f, rk, dir, jac, g11, g22, a, ib, u);
-          AdiFactors &F = c.adi[f][rk][dir];
-          if (!F.a) {
-            F.a = dalloc<double>(c, a.size());
-            F.ib = dalloc<double>(c, ib.size());
-            F.u = dalloc<double>(c, u.size());
-          }
-          EK_CUDA(cudaMemcpy(F.a, a.data(), sizeof(double) * a.size(), cudaMemcpyHostToDevice));
-          EK_CUDA(cudaMemcpy(F.ib, ib.data(), sizeof(double) * ib.size(), cudaMemcpyHostToDevice));
-          EK_CUDA(cudaMemcpy(F.u, u.data(), sizeof(double) * u.size(), cudaMemcpyHostToDevice));
-        }
+    c.h_jac = jac;
+    c.h_g11 = g11;
+    c.h_g22 = g22;
+    build_adi_factors(c);
     // multigrid plan
     MgPlan &P = c.mg;
     mg_build_plan_host(c, jac, g11, g12, g22);
@@ -509,6 +587,7 @@ int ekgpu_step(ek_ctx *h, int nsteps) {
     if (!c.have_metrics) return fail(c, EK_ERR_STATE, "metrics not set");
     if (nsteps < 0) return fail(c, EK_ERR_ARG, "nsteps must be >= 0");
     for (int n = 0; n < nsteps; ++n) {
+      c.p.time_step += 1;
       for (int rk = 1; rk <= 3; ++rk) {
         const int st = substep(c, rk);
         if (st == EK_ERR_NAN) return fail(c, EK_ERR_NAN, "DIV is a NaN");

@@ -300,6 +300,52 @@ bool mg_pick_shape(int n, int &p, int &e) {
   return true;
 }
 
+// Sponge profiles (diablo.F90:1489-1556).  b, co_b and xx are REAL*8 there,
+// but REAL(...) of a difference has the default kind (the Makefiles set no
+// -r8), so the spans are rounded to REAL*4 before they divide.
+int sponge_profiles_host(const ek_params *p, const double *xpoint, const double *ypoint, double *sig,
+                         double *sig_out) {
+  const int NY = p->ny, NZ = p->nz;
+  auto X = [&](int k, int j) { return xpoint[(size_t)j * (NZ + 2) + k]; };
+  auto Y = [&](int k, int j) { return ypoint[(size_t)j * (NZ + 2) + k]; };
+  for (int k = 0; k <= NZ + 1; ++k) sig_out[k] = 0.0;
+  const int R = p->nz_s_r, Lft = p->nz_s_l, T = p->ny_s_t;
+  if (p->sponge_type == 1 && R < NZ + 1) {
+    const double b = 1.0 / (double)(float)(X(NZ + 1, NY + 1) - X(R, NY + 1));
+    for (int k = 0; k <= NZ + 1; ++k) {
+      if (k >= R) {
+        const double xx = (X(k, NY + 1) - X(R, NY + 1)) * b;
+        sig_out[k] = xx * xx;
+      } else if (k <= Lft) {
+        const double xx = (X(Lft, NY + 1) - X(k, NY + 1)) * b;
+        sig_out[k] = xx * xx;
+      }
+    }
+  } else if (p->sponge_type == 2 && R < NZ + 1) {
+    const double co_b = 25.0;
+    const double b = std::log(co_b) / (double)(float)(NZ + 1 - R);
+    for (int k = 0; k <= NZ + 1; ++k) {
+      if (k >= R) sig_out[k] = (std::exp(b * std::abs(k - R)) - 1.0) / (co_b - 1.0);
+      else if (k <= Lft) sig_out[k] = (std::exp(b * std::abs(Lft - k)) - 1.0) / (co_b - 1.0);
+    }
+  }
+  for (int j = 0; j <= NY + 1; ++j) sig[j] = 0.0;
+  if (p->sponge_type == 1) {
+    if (T < 0 || T > NY + 1) return EK_ERR_ARG;
+    const double b = 1.0 / (double)(float)(Y(NZ + 1, NY + 1) - Y(NZ + 1, T));
+    for (int j = T; j <= NY + 1; ++j) {
+      const double xx = (Y(NZ + 1, j) - Y(NZ + 1, T)) * b;
+      sig[j] = xx * xx;
+    }
+  } else if (p->sponge_type == 2) {
+    if (T < 0 || T > NY + 1) return EK_ERR_ARG;
+    const double co_b = 30.0;
+    const double b = std::log(co_b) / (double)(float)(NY + 1 - T);
+    for (int j = T; j <= NY + 1; ++j) sig[j] = (std::exp(b * (j - T)) - 1.0) / (co_b - 1.0);
+  }
+  return EK_OK;
+}
+
 // Multigrid plan: level sizes (mud2cr.f:150-158), kx-independent
 // coefficients of dismd2cr (mud2cr.f:544-998) for nxa=nxb=0, nyc=nyd=2 with
 // bndcr's alfa=0, beta=1, gama=0, and cofcr (duct.F90:3900-3934).  Per

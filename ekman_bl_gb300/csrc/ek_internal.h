@@ -191,6 +191,13 @@ struct Ctx {
   StopPoll poll;
   cudaStream_t aux_stream = nullptr;  // the kx^2 = 0 batch runs here, beside the FP32 cycles
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // sponge_th: SPONGE_SIGMA(0:NY+1), SPONGE_SIGMA_OUT(0:NZ+1), and the
+  // mode-0 mean of CU3X over the upper layer with the dynamic-branch flag
+  double *sponge_sig = nullptr, *sponge_sig_out = nullptr, *sponge_red = nullptr;
+  // COURANT_CURV_MPI: device minimum of the CFL time steps; host copies of
+  // the metrics the dt-dependent ADI factors are built from
+  double *cfl_dt = nullptr;
+  std::vector<double> h_jac, h_g11, h_g22;
   // divergence check
   double *div_part = nullptr;
   double last_div = 0.0;
@@ -245,6 +252,9 @@ void adi_factor_host(const Ctx &c, int field, int rk, int dir, const std::vector
                      const std::vector<double> &g11, const std::vector<double> &g22, std::vector<double> &a,
                      std::vector<double> &ib, std::vector<double> &u);
 bool mg_pick_shape(int n, int &p, int &e);
+void launch_courant(Ctx &c);
+int sponge_profiles_host(const ek_params *p, const double *xpoint, const double *ypoint, double *sig,
+                         double *sig_out);
 void mg_build_plan_host(Ctx &c, const std::vector<double> &jac, const std::vector<double> &g11,
                         const std::vector<double> &g12, const std::vector<double> &g22);
 void mg_build_schedule(MgPlan &plan, int kcycle, int iprer, int ipost, int maxcy);

@@ -22,7 +22,35 @@ struct SpecArgs {
   cplx_t *CU1, *CU2, *CU3, *CP, *CTH, *CF1, *CF2, *CF3, *CFTH, *CR1, *CR2, *CR3, *CRTH;
   double nu, nupr, T3, T4, px, f0, ubc_top, wbulk0, ri;
   int rk, th, cont_strat, forcing;
+  // sponge_th
+  const double *sig, *sig_out, *sred;  // sred[1] != 0: dynamic branch active
+  double amp, tgt1, tgt2, tgt3;
+  int sponge, strat_per, reset;
 };
+
+// sponge_th's mean of Re CU3X(0,K,J) over J = NY_sponge..JEND,
+// K = ZSTART..ZEND (duct.F90:3253-3277) and its dynamic-branch test
+// |mean - WBULK0| > WBULK0 * 0.001 (duct.F90:3288).  One block.
+__global__ void k_sponge_mean(Dims d, const cplx_t *CU3, int ny_sponge, double wbulk0, double *red) {
+  __shared__ double s[256];
+  double acc = 0.0;
+  const int nk = d.ZE - d.ZS + 1, nj = d.JE - ny_sponge + 1;
+  for (int t = threadIdx.x; t < nk * nj; t += blockDim.x) {
+    const int k = d.ZS + t % nk, j = ny_sponge + t / nk;
+    acc += CU3[d.ic(0, k, j)].re;
+  }
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double mean = (nk > 0 && nj > 0) ? s[0] / ((double)nk * (double)nj) : 0.0;
+    red[0] = mean;
+    red[1] = (fabs(mean - wbulk0) > wbulk0 * 0.001) ? 1.0 : 0.0;
+  }
+}
 
 // Spectral explicit RHS: duct.F90:299-409 (CR = J CU + zeta h CF_prev, the
 // curvilinear pressure gradient), 411-455 (mean forcing, mode 0),
@@ -37,6 +65,7 @@ __global__ void k_spectral_rhs(SpecArgs a) {
   const double jac = a.m.jac[d.m2(k, j)];
   const bool vel = (j >= d.JS && j <= d.JE && k >= d.ZS && k <= d.ZE);
   const bool sca = a.th && (j >= d.JST && j <= d.JET && k >= d.ZST && k <= d.ZET);
+  cplx_t F1{}, F2{}, F3{}, FT{};
   if (vel) {
     const cplx_t cu1 = a.CU1[q], cu2 = a.CU2[q], cu3 = a.CU3[q];
     cplx_t r1 = cscl(jac, cu1), r2 = cscl(jac, cu2), r3 = cscl(jac, cu3);
@@ -70,9 +99,9 @@ __global__ void k_spectral_rhs(SpecArgs a) {
     f3 = cadd(f3, cscl(jac, cscl(a.f0, cplx_t{cu1.re - a.ubc_top, cu1.im})));
     f1 = csub(f1, cscl(jac, cscl(a.f0, cplx_t{cu3.re - a.wbulk0, cu3.im})));
     if (a.th) f2 = csub(f2, cscl(jac * a.ri, a.CTH[q]));
-    a.CF1[q] = f1;
-    a.CF2[q] = f2;
-    a.CF3[q] = f3;
+    F1 = f1;
+    F2 = f2;
+    F3 = f3;
   }
   if (sca) {
     const cplx_t cth = a.CTH[q];
@@ -100,8 +129,60 @@ __global__ void k_spectral_rhs(SpecArgs a) {
            4.0 * (a.m.g22[d.m3(k, j + 1, 1)] * (tb(k, j + 1) - tb(k, j)) - a.m.g22[d.m3(k, j, 1)] * (tb(k, j) - tb(k, j - 1))));
       ft.re = ft.re + dd;
     }
-    a.CFTH[q] = ft;
+    FT = ft;
   }
+  if (a.sponge) {
+    // sponge_th (duct.F90:3196-3362), in its statement order; each term is
+    // ((amplitude * sigma) * (CU - target)) * J as the Fortran evaluates it
+    cplx_t cu2 = a.CU2[q];
+    if (vel) {
+      const cplx_t cu1 = a.CU1[q], cu3 = a.CU3[q];
+      const cplx_t cth = sca ? a.CTH[q] : cplx_t{};
+      const double sg = a.amp * a.sig[j], so = a.amp * a.sig_out[k];
+      auto damp = [&](cplx_t f, double s, cplx_t u, double tgt, double w) {
+        return csub(f, cscl(w, cscl(s, cplx_t{u.re - tgt, u.im})));
+      };
+      if (i >= 1) {
+        F1 = damp(F1, sg, cu1, 0.0, jac);
+        F2 = damp(F2, sg, cu2, 0.0, jac);
+        F3 = damp(F3, sg, cu3, 0.0, jac);
+        if (sca) FT = damp(FT, sg, cth, 0.0, jac);
+        F1 = damp(F1, so, cu1, 0.0, jac);
+        F2 = damp(F2, so, cu2, 0.0, jac);
+        F3 = damp(F3, so, cu3, 0.0, jac);
+        if (sca) FT = damp(FT, so, cth, 0.0, jac);
+      } else {
+        if (a.sred[1] != 0.0) {
+          F1 = damp(F1, sg, cu1, a.tgt1, jac);
+          F2 = damp(F2, sg, cu2, a.tgt2, jac);
+          F3 = damp(F3, sg, cu3, a.tgt3, jac);
+          if (sca) FT = damp(FT, sg, cth, 0.0, jac);
+        } else {
+          F2 = damp(F2, sg, cu2, a.tgt2, jac);
+          F1 = damp(F1, sg, cu1, a.tgt1, jac);
+        }
+        if (a.strat_per) {
+          // CF2X(0,:,:) -= Sponge_Amp*(CU2X(0,:,:)-target)*INT_JACOB(K,J), with K, J
+          // left at ZEND+1, JEND+1 by the loops before it
+          F2 = damp(F2, a.amp, cu2, a.tgt2, a.m.jac[d.m2(d.ZE + 1, d.JE + 1)]);
+          if (a.reset) cu2 = cplx_t{0.0, 0.0};
+        }
+        const double so2 = (2.0 * a.amp) * a.sig_out[k];
+        F1 = damp(F1, so2, cu1, 0.0, jac);
+        F2 = damp(F2, so2, cu2, 0.0, jac);
+        F3 = damp(F3, so2, cu3, a.tgt3, jac);
+        if (sca) FT = damp(FT, so2, cth, 0.0, jac);
+      }
+    }
+    // CU2X(0,:,:) = 0 on the whole plane, after every use above
+    if (i == 0 && a.strat_per && a.reset) a.CU2[q] = cplx_t{0.0, 0.0};
+  }
+  if (vel) {
+    a.CF1[q] = F1;
+    a.CF2[q] = F2;
+    a.CF3[q] = F3;
+  }
+  if (sca) a.CFTH[q] = FT;
 }
 
 // Contravariant face velocities U2b, U3b (duct.F90:721-732); U3b is stored
@@ -425,9 +506,71 @@ void launch_spectral_rhs(Ctx &c, int rk) {
   a.rk = rk;
   a.th = p.n_th > 0;
   a.cont_strat = p.cont_strat;
+  // sponge_th runs inside the scalar loop (duct.F90:635), so only with N_TH >= 1
+  a.sponge = (p.sponge_type != 0 && p.n_th > 0) ? 1 : 0;
+  a.sig = c.sponge_sig;
+  a.sig_out = c.sponge_sig_out;
+  a.sred = c.sponge_red;
+  a.amp = 0.1 / p.delta_t;
+  a.tgt1 = p.v_bc_c1[EK_YMAX];
+  a.tgt2 = p.u_bc_c1[EK_YMAX];
+  a.tgt3 = p.wbulk0;
+  a.strat_per = (p.v_bc[EK_ZMAX] == 6 && p.u_bc[EK_ZMAX] == 6 && p.w_bc[EK_ZMAX] == 6 && p.ri_tau != 0.0) ? 1 : 0;
+  a.reset = (a.strat_per && p.save_stats_int > 0 && (2 * p.time_step) % p.save_stats_int == 0) ? 1 : 0;
   dim3 grid((c.d.NX2P + 1 + 63) / 64, c.d.NZ2, c.d.NY2);
   KScope ks(c, KC_SPECTRAL, 16.0 * c.d.nspec() * (5 + (rk > 1 ? 4 : 0) + 8));
+  if (a.sponge) {
+    const int nys = (p.ny_s_t > p.ny) ? (2 * p.ny) / 3 : p.ny_s_t;
+    k_sponge_mean<<<1, 256, 0, c.stream>>>(c.d, c.CU3, nys, p.wbulk0, c.sponge_red);
+    after_launch(c);
+  }
   k_spectral_rhs<<<grid, 64, 0, c.stream>>>(a);
+  after_launch(c);
+}
+
+// COURANT_CURV_MPI (duct.F90:3605-3674): the minimum over I = 0..NXP,
+// K = ZSTART..ZEND, J = JSTART..JEND of CFL*DX/|U1|, CFL*J/|U2b|, CFL*J/|U3b|
+// (face velocities as duct.F90:3631-3636), starting from 999.  All terms
+// are positive, so the minimum of their bit patterns is the minimum.
+__global__ void k_courant(Dims d, Metrics m, const double *U1, const double *U2, const double *U3, double cfl,
+                          double dx, unsigned long long *out) {
+  __shared__ unsigned long long s[256];
+  unsigned long long best = (unsigned long long)__double_as_longlong(999.0);
+  const int ni = d.NX + 2, nk = d.ZE - d.ZS + 1, nj = d.JE - d.JS + 1;
+  const long n = (long)ni * nk * nj;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % ni), k = d.ZS + (int)((t / ni) % nk), j = d.JS + (int)(t / ((long)ni * nk));
+    const size_t c = d.ip(i, k, j);
+    const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
+    const double u2b = 0.5 * m.c22[d.m3(k, j, 1)] * (U2[c] + U2[c - sJ]) + 0.5 * m.c21[d.m3(k, j, 1)] * (U3[c] + U3[c - sJ]);
+    const double u3b = 0.5 * m.c11[d.m3(k, j, 2)] * (U3[c] + U3[c - sK]) + 0.5 * m.c12[d.m3(k, j, 2)] * (U2[c] + U2[c - sK]);
+    const double jac = m.jac[d.m2(k, j)];
+    const double dtx = cfl * dx / fabs(U1[c]);
+    const double dty = cfl * jac / fabs(u2b);
+    const double dtz = cfl * jac / fabs(u3b);
+    for (double v : {dtx, dty, dtz}) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+      if (v == v && b < best) best = b;
+    }
+  }
+  s[threadIdx.x] = best;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w && s[threadIdx.x + w] < s[threadIdx.x]) s[threadIdx.x] = s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicMin(out, s[0]);
+}
+
+__global__ void k_set_double(double *a, double v) { *a = v; }
+
+void launch_courant(Ctx &c) {
+  const Dims &d = c.d;
+  KScope ks(c, KC_FACE, 8.0 * 5 * (double)(d.NX + 2) * (d.ZE - d.ZS + 1) * (d.JE - d.JS + 1));
+  k_set_double<<<1, 1, 0, c.stream>>>(c.cfl_dt, 999.0);
+  after_launch(c);
+  k_courant<<<2 * 152, 256, 0, c.stream>>>(d, c.m, c.U1, c.U2, c.U3, c.p.cfl, c.p.lx / c.p.nx,
+                                          reinterpret_cast<unsigned long long *>(c.cfl_dt));
   after_launch(c);
 }
 

@@ -29,6 +29,7 @@ EXPORTS = [
     "ekgpu_poisson_batch", "ekgpu_poisson_batch_device", "ekgpu_last_divergence", "ekgpu_last_mg_stats",
     "ekgpu_launch_count", "ekgpu_set_timing", "ekgpu_get_timing", "ekgpu_timing_class_name",
     "ekgpu_fft_x_to_fourier", "ekgpu_fft_x_to_physical", "ekgpu_fft_x_to_fourier_noalloc",
+    "ekgpu_sponge_profiles", "ekgpu_set_sponge", "ekgpu_set_time", "ekgpu_get_time",
 ]
 
 
@@ -61,6 +62,10 @@ def load_library():
     L.ekgpu_set_stream.argtypes = [V, V]
     L.ekgpu_set_metrics.argtypes = [V, C.POINTER(EkMetrics)]
     L.ekgpu_metrics_from_grid.argtypes = [P, _D, _D] + [_D] * 9
+    L.ekgpu_sponge_profiles.argtypes = [P, _D, _D, _D, _D]
+    L.ekgpu_set_sponge.argtypes = [V, _D, _D]
+    L.ekgpu_set_time.argtypes = [V, C.c_double, C.c_int]
+    L.ekgpu_get_time.argtypes = [V, _D, C.POINTER(C.c_int), _D]
     L.ekgpu_upload_state.argtypes = [V] + [_D] * 5
     L.ekgpu_download_state.argtypes = [V] + [_D] * 5
     L.ekgpu_get_field.argtypes = [V, C.c_int, _D]
@@ -99,6 +104,19 @@ def metrics_from_grid(p: EkParams, xpoint: np.ndarray, ypoint: np.ndarray) -> di
     if st:
         raise EkError(st, "ekgpu_metrics_from_grid")
     return out
+
+
+def sponge_profiles(p: EkParams, xpoint: np.ndarray, ypoint: np.ndarray):
+    """SPONGE_SIGMA(0:NY+1) and SPONGE_SIGMA_OUT(0:NZ+1) of
+    src/diablo.F90:1489-1556 through ekgpu_sponge_profiles."""
+    L = load_library()
+    sig, sig_out = np.zeros(p.ny + 2), np.zeros(p.nz + 2)
+    xp = np.ascontiguousarray(xpoint, np.float64)
+    yp = np.ascontiguousarray(ypoint, np.float64)
+    st = L.ekgpu_sponge_profiles(C.byref(p), as_ptr(xp), as_ptr(yp), as_ptr(sig), as_ptr(sig_out))
+    if st:
+        raise EkError(st, "ekgpu_sponge_profiles")
+    return sig, sig_out
 
 
 class DuctSolver:
@@ -143,6 +161,20 @@ class DuctSolver:
 
     def set_stream(self, stream_ptr: int | None):
         self._check(self._L.ekgpu_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
+
+    def set_sponge(self, sponge_sigma, sponge_sigma_out):
+        """SPONGE_SIGMA(0:NY+1), SPONGE_SIGMA_OUT(0:NZ+1) read by sponge_th."""
+        self._sponge = [np.ascontiguousarray(a, np.float64) for a in (sponge_sigma, sponge_sigma_out)]
+        self._check(self._L.ekgpu_set_sponge(self._h, *[as_ptr(a) for a in self._sponge]))
+
+    def set_time(self, time: float, time_step: int):
+        self._check(self._L.ekgpu_set_time(self._h, float(time), int(time_step)))
+
+    def get_time(self):
+        """(TIME, TIME_STEP, DELTA_T)."""
+        t, n, dt = C.c_double(), C.c_int(), C.c_double()
+        self._check(self._L.ekgpu_get_time(self._h, C.byref(t), C.byref(n), C.byref(dt)))
+        return t.value, n.value, dt.value
 
     # -- state ----------------------------------------------------------------
     def upload(self, cu1, cu2, cu3, cp, cth):

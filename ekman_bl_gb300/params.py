@@ -43,6 +43,9 @@ class EkParams(C.Structure):
         ("mg_maxcy", C.c_int), ("mg_kcycle", C.c_int), ("mg_iprer", C.c_int), ("mg_ipost", C.c_int),
         ("mg_intpol", C.c_int), ("mg_stop", C.c_int), ("mg_tol", C.c_double),
         ("quirk_phi_fp32", C.c_int), ("mg_fast", C.c_int), ("sponge_type", C.c_int), ("les", C.c_int),
+        ("ny_s_t", C.c_int), ("nz_s_r", C.c_int), ("nz_s_l", C.c_int), ("save_stats_int", C.c_int),
+        ("time_step", C.c_int), ("variable_dt", C.c_int), ("update_dt", C.c_int),
+        ("cfl", C.c_double), ("delta_t_set", C.c_double),
     ]
 
 
@@ -88,6 +91,19 @@ def default_params(nx: int, ny: int, nz: int) -> EkParams:
     p.mg_stop = EK_MG_STOP_RELCHANGE
     p.mg_tol = MUDPACK_TOLMAX
     p.quirk_phi_fp32 = 0
+    # sponge extents as grid_def writes them (streamwise sponge off:
+    # NZ_S_R = NZ+2, NZ_S_L = NZ+1-NZ_S_R), SAVE_STATS_INT of input.dat
+    p.sponge_type = 0
+    p.ny_s_t = (2 * ny) // 3
+    p.nz_s_r = nz + 2
+    p.nz_s_l = nz + 1 - p.nz_s_r
+    p.save_stats_int = 100
+    p.time_step = 0
+    # fixed time step (VARIABLE_DT off); CFL, UPDATE_DT of the shipped input.dat
+    p.variable_dt = 0
+    p.update_dt = 1
+    p.cfl = 0.8
+    p.delta_t_set = p.delta_t
     return p
 
 

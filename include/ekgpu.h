@@ -90,8 +90,20 @@ typedef struct ek_params {
                                 default); 1: mixed precision -- FP64 residual and update around FP32
                                 V-cycles with a y-line smoother, same discrete operator, needs
                                 mg_stop = EK_MG_STOP_RESIDUAL; mg_maxcy caps the corrections   */
-  int sponge_type;           /* SPONGE_TYPE (only 0 supported)                          */
+  int sponge_type;           /* SPONGE_TYPE: 0 none, 1 parabolic, 2 exponential profiles;
+                                sponge_th (duct.F90:3196-3362) runs when != 0 and N_TH >= 1 */
   int les;                   /* LES (only 0 supported)                                  */
+  int ny_s_t, nz_s_r, nz_s_l;/* grid_def NY_S_T, NZ_S_R, NZ_S_L: sponge extents         */
+  int save_stats_int;        /* SAVE_STATS_INT (input.dat); sponge_th zeroes mode 0 of CU2X
+                                when MOD(2*TIME_STEP, SAVE_STATS_INT) = 0 in its stratified,
+                                z-periodic branch                                        */
+  int time_step;             /* TIME_STEP of the step being taken; ekgpu_step adds 1 before
+                                each step, as the driver's DO TIME_STEP loop does        */
+  int variable_dt;           /* VARIABLE_DT: COURANT_CURV_MPI (duct.F90:3605-3674) after the
+                                RK_STEP = 3 ADI when MOD(TIME_STEP, UPDATE_DT) = 0       */
+  int update_dt;             /* UPDATE_DT                                               */
+  double cfl;                /* CFL                                                     */
+  double delta_t_set;        /* DELTA_T_SET: the cap of the CFL time step               */
 } ek_params;
 
 /* Geometry and background fields of JACOBI_TRANS (diablo.F90:1088-1570);
@@ -155,6 +167,25 @@ int ekgpu_metrics_from_grid(const ek_params *p, const double *xpoint,
                             double *gmat_11, double *gmat_12, double *gmat_22,
                             double *cjob_11, double *cjob_12, double *cjob_21,
                             double *cjob_22, double *th_bar);
+
+/* Host helper: the sponge profiles of diablo.F90:1489-1556 from the grid
+ * points: SPONGE_SIGMA(0:NY+1) (vertical, from NY_S_T up) and
+ * SPONGE_SIGMA_OUT(0:NZ+1) (streamwise, K >= NZ_S_R and K <= NZ_S_L when
+ * NZ_S_R < NZ+1), parabolic (SPONGE_TYPE 1) or exponential (2); zero for 0. */
+int ekgpu_sponge_profiles(const ek_params *p, const double *xpoint, const double *ypoint,
+                          double *sponge_sigma, double *sponge_sigma_out);
+
+/* Upload SPONGE_SIGMA(0:NY+1) and SPONGE_SIGMA_OUT(0:NZ+1) (the module arrays
+ * that sponge_th reads).  Both default to zero. */
+int ekgpu_set_sponge(ek_ctx *ctx, const double *sponge_sigma, const double *sponge_sigma_out);
+
+/* Set TIME and TIME_STEP for the next substep (a driver that calls
+ * ekgpu_rk_substep itself keeps them in step with its own loop). */
+int ekgpu_set_time(ek_ctx *ctx, double time, int time_step);
+
+/* Read TIME, TIME_STEP and DELTA_T back (DELTA_T changes when VARIABLE_DT
+ * runs COURANT_CURV_MPI). */
+int ekgpu_get_time(ek_ctx *ctx, double *time, int *time_step, double *delta_t);
 
 /* Copy the Fourier-space state CU1X, CU2X, CU3X, CPX, CTHX in (upload) or
  * out (download).  Replaces READ_FLOW's fill of the module arrays

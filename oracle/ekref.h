@@ -40,6 +40,12 @@ int ekref_metrics_from_grid(const ek_params *p, const double *xpoint,
                             double *cjob_11, double *cjob_12, double *cjob_21,
                             double *cjob_22, double *th_bar);
 int ekref_set_metrics(ekref_ctx *ctx, const ek_metrics *m);
+/* SPONGE_SIGMA(0:NY+1), SPONGE_SIGMA_OUT(0:NZ+1) of diablo.F90:1489-1556. */
+int ekref_sponge_profiles(const ek_params *p, const double *xpoint, const double *ypoint,
+                          double *sponge_sigma, double *sponge_sigma_out);
+int ekref_set_sponge(ekref_ctx *ctx, const double *sponge_sigma, const double *sponge_sigma_out);
+int ekref_set_time(ekref_ctx *ctx, double time, int time_step);
+int ekref_get_time(ekref_ctx *ctx, double *time, int *time_step, double *delta_t);
 int ekref_upload_state(ekref_ctx *ctx, const double *cu1, const double *cu2,
                        const double *cu3, const double *cp, const double *cth);
 int ekref_download_state(ekref_ctx *ctx, double *cu1, double *cu2, double *cu3,

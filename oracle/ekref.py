@@ -40,6 +40,10 @@ def lib():
         L.ekref_set_threads.argtypes = [C.c_int]
         L.ekref_metrics_from_grid.argtypes = [P, _D, _D] + [_D] * 9
         L.ekref_set_metrics.argtypes = [C.c_void_p, C.POINTER(EkMetrics)]
+        L.ekref_sponge_profiles.argtypes = [P, _D, _D, _D, _D]
+        L.ekref_set_sponge.argtypes = [C.c_void_p, _D, _D]
+        L.ekref_set_time.argtypes = [C.c_void_p, C.c_double, C.c_int]
+        L.ekref_get_time.argtypes = [C.c_void_p, _D, C.POINTER(C.c_int), _D]
         L.ekref_upload_state.argtypes = [C.c_void_p] + [_D] * 5
         L.ekref_download_state.argtypes = [C.c_void_p] + [_D] * 5
         L.ekref_get_field.argtypes = [C.c_void_p, C.c_int, _D]
@@ -74,6 +78,17 @@ def metrics_from_grid(p: EkParams, xpoint: np.ndarray, ypoint: np.ndarray) -> di
     if st:
         raise RuntimeError(f"ekref_metrics_from_grid failed: {st}")
     return out
+
+
+def sponge_profiles(p: EkParams, xpoint: np.ndarray, ypoint: np.ndarray):
+    """The oracle's SPONGE_SIGMA / SPONGE_SIGMA_OUT (diablo.F90:1489-1556)."""
+    sig, sig_out = np.zeros(p.ny + 2), np.zeros(p.nz + 2)
+    xp = np.ascontiguousarray(xpoint, np.float64)
+    yp = np.ascontiguousarray(ypoint, np.float64)
+    st = lib().ekref_sponge_profiles(C.byref(p), as_ptr(xp), as_ptr(yp), as_ptr(sig), as_ptr(sig_out))
+    if st:
+        raise RuntimeError(f"ekref_sponge_profiles failed: {st}")
+    return sig, sig_out
 
 
 def metrics_struct(m: dict) -> EkMetrics:
@@ -136,6 +151,18 @@ class Oracle:
 
     def step(self, n=1):
         return self._check(lib().ekref_step(self._h, n))
+
+    def set_sponge(self, sponge_sigma, sponge_sigma_out):
+        self._sponge = [np.ascontiguousarray(a, np.float64) for a in (sponge_sigma, sponge_sigma_out)]
+        self._check(lib().ekref_set_sponge(self._h, *[as_ptr(a) for a in self._sponge]))
+
+    def set_time(self, time: float, time_step: int):
+        self._check(lib().ekref_set_time(self._h, float(time), int(time_step)))
+
+    def get_time(self):
+        t, n, dt = C.c_double(), C.c_int(), C.c_double()
+        lib().ekref_get_time(self._h, C.byref(t), C.byref(n), C.byref(dt))
+        return t.value, n.value, dt.value
 
     def rem_div(self):
         return self._check(lib().ekref_rem_div(self._h))

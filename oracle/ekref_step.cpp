@@ -96,6 +96,7 @@ struct ekref_ctx {
   double H_BAR[4], BETA_BAR[4], ZETA_BAR[4];
   std::vector<double> KXP, KX2P;
   std::vector<double> int_jacob, gmat_11, gmat_12, gmat_22, cjob_11, cjob_12, cjob_21, cjob_22, th_bar;
+  std::vector<double> sponge_sigma, sponge_sigma_out;  // (0:NY+1), (0:NZ+1); zero by default
   bool have_metrics = false;
   // spectral fields
   std::vector<cplx> CU1, CU2, CU3, CP, CTH, CF1, CF2, CF3, CFTH, CR1, CR2, CR3, CRTH, CS1, CS2, CU2b, CU3b;
@@ -203,12 +204,173 @@ extern "C" int ekref_create(const ek_params *p, ekref_ctx **out) {
     v->assign(nc, cplx{0.0, 0.0});
   for (auto *v : {&c->U1, &c->U2, &c->U3, &c->TH, &c->R1, &c->R2, &c->R3, &c->RTH, &c->S1, &c->S2, &c->U2b, &c->U3b})
     v->assign(np, 0.0);
+  c->sponge_sigma.assign(NY + 2, 0.0);
+  c->sponge_sigma_out.assign(NZ + 2, 0.0);
+  if (p->sponge_type != 0 && p->save_stats_int < 1)
+    return fail(c.get(), EK_ERR_ARG, "SAVE_STATS_INT must be >= 1 with a sponge"), *out = c.release(), EK_ERR_ARG;
   c->fft = std::make_unique<FFT>(NX);
   *out = c.release();
   return EK_OK;
 }
 
 extern "C" void ekref_destroy(ekref_ctx *c) { delete c; }
+
+// SPONGE_SIGMA / SPONGE_SIGMA_OUT (diablo.F90:1489-1556).  b, co_b and xx are
+// REAL*8; REAL(...) of a difference is default-kind REAL*4 (no -r8 in the
+// Makefiles), so the spans are rounded to float before dividing.
+extern "C" int ekref_sponge_profiles(const ek_params *p, const double *xpoint, const double *ypoint,
+                                     double *SPONGE_SIGMA, double *SPONGE_SIGMA_OUT) {
+  if (!p || !xpoint || !ypoint || !SPONGE_SIGMA || !SPONGE_SIGMA_OUT) return EK_ERR_ARG;
+  const int NY = p->ny, NZ = p->nz, NZ_S_R = p->nz_s_r, NZ_S_L = p->nz_s_l, NY_S_T = p->ny_s_t;
+  auto xpt = [&](int K, int J) { return xpoint[(size_t)J * (NZ + 2) + K]; };
+  auto ypt = [&](int K, int J) { return ypoint[(size_t)J * (NZ + 2) + K]; };
+  double b, co_b, xx;
+  for (int K = 0; K <= NZ + 1; ++K) SPONGE_SIGMA_OUT[K] = 0.0;
+  if (p->sponge_type == 1 && NZ_S_R < NZ + 1) {
+    b = 1.0 / (double)(float)(xpt(NZ + 1, NY + 1) - xpt(NZ_S_R, NY + 1));
+    for (int K = 0; K <= NZ + 1; ++K) {
+      if (K >= NZ_S_R) {
+        xx = (xpt(K, NY + 1) - xpt(NZ_S_R, NY + 1)) * b;
+        SPONGE_SIGMA_OUT[K] = xx * xx;
+      } else if (K <= NZ_S_L) {
+        xx = (xpt(NZ_S_L, NY + 1) - xpt(K, NY + 1)) * b;
+        SPONGE_SIGMA_OUT[K] = xx * xx;
+      }
+    }
+  } else if (p->sponge_type == 2 && NZ_S_R < NZ + 1) {
+    co_b = 25.0;
+    b = std::log(co_b) / (double)(float)(NZ + 1 - NZ_S_R);
+    for (int K = 0; K <= NZ + 1; ++K) {
+      if (K >= NZ_S_R)
+        SPONGE_SIGMA_OUT[K] = (std::exp(b * std::abs(K - NZ_S_R)) - 1.0) / (co_b - 1.0);
+      else if (K <= NZ_S_L)
+        SPONGE_SIGMA_OUT[K] = (std::exp(b * std::abs(NZ_S_L - K)) - 1.0) / (co_b - 1.0);
+    }
+  }
+  for (int J = 0; J <= NY + 1; ++J) SPONGE_SIGMA[J] = 0.0;
+  if (p->sponge_type == 1) {
+    if (NY_S_T < 0 || NY_S_T > NY + 1) return EK_ERR_ARG;
+    b = 1.0 / (double)(float)(ypt(NZ + 1, NY + 1) - ypt(NZ + 1, NY_S_T));
+    for (int J = NY_S_T; J <= NY + 1; ++J) {
+      xx = (ypt(NZ + 1, J) - ypt(NZ + 1, NY_S_T)) * b;
+      SPONGE_SIGMA[J] = xx * xx;
+    }
+  } else if (p->sponge_type == 2) {
+    if (NY_S_T < 0 || NY_S_T > NY + 1) return EK_ERR_ARG;
+    co_b = 30.0;
+    b = std::log(co_b) / (double)(float)(NY + 1 - NY_S_T);
+    for (int J = NY_S_T; J <= NY + 1; ++J) SPONGE_SIGMA[J] = (std::exp(b * (J - NY_S_T)) - 1.0) / (co_b - 1.0);
+  }
+  return EK_OK;
+}
+
+extern "C" int ekref_set_sponge(ekref_ctx *c, const double *s, const double *so) {
+  if (!s || !so) return fail(c, EK_ERR_ARG, "sponge profile is NULL");
+  c->sponge_sigma.assign(s, s + c->NY + 2);
+  c->sponge_sigma_out.assign(so, so + c->NZ + 2);
+  return EK_OK;
+}
+
+extern "C" int ekref_set_time(ekref_ctx *c, double time, int time_step) {
+  c->p.time = time;
+  c->p.time_step = time_step;
+  return EK_OK;
+}
+
+extern "C" int ekref_get_time(ekref_ctx *c, double *time, int *time_step, double *delta_t) {
+  if (time) *time = c->p.time;
+  if (time_step) *time_step = c->p.time_step;
+  if (delta_t) *delta_t = c->p.delta_t;
+  return EK_OK;
+}
+
+// sponge_th(N) (duct.F90:3196-3362), restated loop by loop.
+static void sponge_th(ekref_ctx *c) {
+  const ek_params &p = c->p;
+  const int NX2P = c->NX2P, NY = c->NY, NZ = c->NZ;
+  const int JSTART = c->JSTART, JEND = c->JEND, ZSTART = c->ZSTART, ZEND = c->ZEND;
+  auto &CU1 = c->CU1, &CU2 = c->CU2, &CU3 = c->CU3, &CTH = c->CTH;
+  auto &CF1 = c->CF1, &CF2 = c->CF2, &CF3 = c->CF3, &CFTH = c->CFTH;
+  const std::vector<double> &SPONGE_SIGMA = c->sponge_sigma, &SPONGE_SIGMA_OUT = c->sponge_sigma_out;
+  const double Sponge_Amp = 0.1 / p.delta_t;
+  const double Dynamic_sponge_threshold = 0.001;
+  // F - ((a * s) * (U - t)) * J, complex minus a real target
+  auto term = [](cplx f, double as, cplx u, double t, double jac) {
+    const cplx v{as * (u.re - t), as * u.im};
+    return cplx{f.re - v.re * jac, f.im - v.im * jac};
+  };
+  int i = 0, j = 0, k = 0;
+  // damp fluctuations: top and bottom
+  for (j = JSTART; j <= JEND; ++j)
+    for (k = ZSTART; k <= ZEND; ++k)
+      for (i = 1; i <= NX2P; ++i) {
+        const size_t q = c->ic(i, k, j);
+        const double as = Sponge_Amp * SPONGE_SIGMA[j], J = c->JAC(k, j);
+        CF1[q] = term(CF1[q], as, CU1[q], 0.0, J);
+        CF2[q] = term(CF2[q], as, CU2[q], 0.0, J);
+        CF3[q] = term(CF3[q], as, CU3[q], 0.0, J);
+        CFTH[q] = term(CFTH[q], as, CTH[q], 0.0, J);
+      }
+  // inflow / outflow
+  for (j = JSTART; j <= JEND; ++j)
+    for (k = ZSTART; k <= ZEND; ++k)
+      for (i = 1; i <= NX2P; ++i) {
+        const size_t q = c->ic(i, k, j);
+        const double as = Sponge_Amp * SPONGE_SIGMA_OUT[k], J = c->JAC(k, j);
+        CF1[q] = term(CF1[q], as, CU1[q], 0.0, J);
+        CF2[q] = term(CF2[q], as, CU2[q], 0.0, J);
+        CF3[q] = term(CF3[q], as, CU3[q], 0.0, J);
+        CFTH[q] = term(CFTH[q], as, CTH[q], 0.0, J);
+      }
+  const int NY_sponge = (p.ny_s_t > NY) ? (2 * NY) / 3 : p.ny_s_t;
+  double CU3X_sponge = 0.0;
+  for (j = NY_sponge; j <= JEND; ++j)
+    for (k = ZSTART; k <= ZEND; ++k) CU3X_sponge = CU3X_sponge + CU3[c->ic(0, k, j)].re;
+  CU3X_sponge = CU3X_sponge / (double)((ZEND - ZSTART + 1) * (JEND - NY_sponge + 1));
+  const double CU1X_target = p.v_bc_c1[EK_YMAX], CU2X_target = p.u_bc_c1[EK_YMAX], CU3X_target = p.wbulk0;
+  // damp the mean flow (RANK 0, DYNAMIC_SPONE = .TRUE.)
+  if (std::fabs(CU3X_sponge - CU3X_target) > CU3X_target * Dynamic_sponge_threshold) {
+    for (j = JSTART; j <= JEND; ++j)
+      for (k = ZSTART; k <= ZEND; ++k) {
+        const size_t q = c->ic(0, k, j);
+        const double as = Sponge_Amp * SPONGE_SIGMA[j], J = c->JAC(k, j);
+        CF1[q] = term(CF1[q], as, CU1[q], CU1X_target, J);
+        CF2[q] = term(CF2[q], as, CU2[q], CU2X_target, J);
+        CF3[q] = term(CF3[q], as, CU3[q], CU3X_target, J);
+        CFTH[q] = term(CFTH[q], as, CTH[q], 0.0, J);
+      }
+  } else {
+    for (j = JSTART; j <= JEND; ++j)
+      for (k = ZSTART; k <= ZEND; ++k) {
+        const size_t q = c->ic(0, k, j);
+        const double as = Sponge_Amp * SPONGE_SIGMA[j], J = c->JAC(k, j);
+        CF2[q] = term(CF2[q], as, CU2[q], CU2X_target, J);
+        CF1[q] = term(CF1[q], as, CU1[q], CU1X_target, J);
+      }
+  }
+  // j = JEND+1, k = ZEND+1 here, as after the Fortran DO loops
+  if (p.v_bc[EK_ZMAX] == 6 && p.u_bc[EK_ZMAX] == 6 && p.w_bc[EK_ZMAX] == 6 && p.ri_tau != 0.0) {
+    const double J = c->JAC(k, j);
+    for (int jj = 0; jj <= NY + 1; ++jj)
+      for (int kk = 0; kk <= NZ + 1; ++kk) {
+        const size_t q = c->ic(0, kk, jj);
+        CF2[q] = term(CF2[q], Sponge_Amp, CU2[q], CU2X_target, J);
+      }
+    if ((2 * p.time_step) % p.save_stats_int == 0)
+      for (int jj = 0; jj <= NY + 1; ++jj)
+        for (int kk = 0; kk <= NZ + 1; ++kk) CU2[c->ic(0, kk, jj)] = cplx{0.0, 0.0};
+  }
+  // inflow / outflow of the mean
+  for (j = JSTART; j <= JEND; ++j)
+    for (k = ZSTART; k <= ZEND; ++k) {
+      const size_t q = c->ic(0, k, j);
+      const double as = 2.0 * Sponge_Amp * SPONGE_SIGMA_OUT[k], J = c->JAC(k, j);
+      CF1[q] = term(CF1[q], as, CU1[q], 0.0, J);
+      CF2[q] = term(CF2[q], as, CU2[q], 0.0, J);
+      CF3[q] = term(CF3[q], as, CU3[q], CU3X_target, J);
+      CFTH[q] = term(CFTH[q], as, CTH[q], 0.0, J);
+    }
+}
 
 extern "C" int ekref_set_metrics(ekref_ctx *c, const ek_metrics *m) {
   const size_t n2 = (size_t)(c->NZ + 3) * (c->NY + 3);
@@ -829,6 +991,7 @@ extern "C" int ekref_rk_substep(ekref_ctx *c, int rk) {
         }
       }
   }
+  if (th && p.sponge_type != 0) sponge_th(c);  // duct.F90:635, inside the scalar loop
   // to physical space (duct.F90:656-673)
   to_physical(c, CU1, c->U1, 0, NY + 1, 0, NZ + 1);
   to_physical(c, CU2, c->U2, 0, NY + 1, 0, NZ + 1);
@@ -921,6 +1084,30 @@ extern "C" int ekref_rk_substep(ekref_ctx *c, int rk) {
   adi_field(c, 1, TEMP1, U1, c->R1, JS, JE, ZS, ZE);
   adi_field(c, 2, TEMP1, U2, c->R2, JS, JE, ZS, ZE);
   adi_field(c, 3, TEMP1, U3, c->R3, JS, JE, ZS, ZE);
+  // COURANT_CURV_MPI (duct.F90:2417-2419, 3605-3674)
+  if (p.variable_dt && rk == 3 && p.time_step % p.update_dt == 0) {
+    double dt = 999.0;
+    const double dx = p.lx / (double)c->NX;
+    for (int j = JS; j <= JE; ++j)
+      for (int k = ZS; k <= ZE; ++k)
+        for (int i = 0; i <= NXP; ++i) {
+          const size_t q = c->ip(i, k, j), qj = c->ip(i, k, j - 1), qk = c->ip(i, k - 1, j);
+          const double u2b = 0.5 * c->M3(c->cjob_22, k, j, 1) * (U2[q] + U2[qj]) +
+                             0.5 * c->M3(c->cjob_21, k, j, 1) * (U3[q] + U3[qj]);
+          const double u3b = 0.5 * c->M3(c->cjob_11, k, j, 2) * (U3[q] + U3[qk]) +
+                             0.5 * c->M3(c->cjob_12, k, j, 2) * (U2[q] + U2[qk]);
+          const double dt_x = p.cfl * dx / std::fabs(U1[q]);
+          const double dt_y = p.cfl * c->JAC(k, j) / std::fabs(u2b);
+          const double dt_z = p.cfl * c->JAC(k, j) / std::fabs(u3b);
+          dt = std::min(std::min(std::min(dt, dt_x), dt_y), dt_z);
+        }
+    if (dt > 0.0) {
+      c->p.delta_t = (dt >= p.delta_t_set) ? p.delta_t_set : dt;
+      c->H_BAR[1] = c->p.delta_t * (8.0 / 15.0);
+      c->H_BAR[2] = c->p.delta_t * (2.0 / 15.0);
+      c->H_BAR[3] = c->p.delta_t * (5.0 / 15.0);
+    }
+  }
   // back to Fourier space (duct.F90:2421-2451)
   to_fourier(c, U1, CU1, 0, NY + 1, 0, NZ + 1);
   to_fourier(c, U2, CU2, 0, NY + 1, 0, NZ + 1);
@@ -941,6 +1128,7 @@ extern "C" int ekref_rk_substep(ekref_ctx *c, int rk) {
 
 extern "C" int ekref_step(ekref_ctx *c, int nsteps) {
   for (int n = 0; n < nsteps; ++n) {
+    c->p.time_step += 1;  // DO TIME_STEP = TIME_STEP+1, ... (diablo.F90:109)
     for (int rk = 1; rk <= 3; ++rk) {
       const int st = ekref_rk_substep(c, rk);
       if (st != EK_OK) return st;
