@@ -129,6 +129,7 @@ int substep(Ctx &c, int rk) {
     a.j0 = d.JS; a.j1 = d.JE; a.k0 = d.ZS; a.k1 = d.ZE;
     const double *uu[3] = {c.U1, c.U2, c.U3};
     cplx_t *cf[3] = {c.CF1, c.CF2, c.CF3};
+    a.lowp = 1;
     for (int f = 0; f < 3; ++f) {
       a.pro = PRO_PROD; a.a = c.U1; a.b = uu[f]; a.epi = EPI_SUB_IK; a.dst = cf[f];
       launch_r2c(c, a);
@@ -149,6 +150,7 @@ int substep(Ctx &c, int rk) {
     // scalar nonlinear terms (duct.F90:1165-1252) and RTH (1304-1326)
     R2cArgs a{};
     a.j0 = d.JST; a.j1 = d.JET; a.k0 = d.ZST; a.k1 = d.ZET;
+    a.lowp = 1;
     a.pro = PRO_PROD; a.a = c.TH; a.b = c.U1; a.epi = EPI_SUB_IK; a.dst = c.CFTH;
     launch_r2c(c, a);
     a.pro = PRO_FLUX; a.a = c.TH; a.b = c.U2b; a.visc = p.nu / p.pr; a.epi = EPI_ADD;
@@ -358,6 +360,15 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
     c.tw_n = dalloc<double2>(c, twn.size());
     EK_CUDA(cudaMemcpy(c.tw_m, twm.data(), sizeof(double2) * twm.size(), cudaMemcpyHostToDevice));
     EK_CUDA(cudaMemcpy(c.tw_n, twn.data(), sizeof(double2) * twn.size(), cudaMemcpyHostToDevice));
+    {
+      std::vector<float2> fm(twm.size()), fn(twn.size());
+      for (size_t t = 0; t < twm.size(); ++t) fm[t] = make_float2((float)twm[t].x, (float)twm[t].y);
+      for (size_t t = 0; t < twn.size(); ++t) fn[t] = make_float2((float)twn[t].x, (float)twn[t].y);
+      c.tw_mf = dalloc<float2>(c, fm.size());
+      c.tw_nf = dalloc<float2>(c, fn.size());
+      EK_CUDA(cudaMemcpy(c.tw_mf, fm.data(), sizeof(float2) * fm.size(), cudaMemcpyHostToDevice));
+      EK_CUDA(cudaMemcpy(c.tw_nf, fn.data(), sizeof(float2) * fn.size(), cudaMemcpyHostToDevice));
+    }
     // fields
     const size_t nc = d.nspec(), np = d.nphys();
     for (cplx_t **f : {&c.CU1, &c.CU2, &c.CU3, &c.CP, &c.CTH, &c.CF1, &c.CF2, &c.CF3, &c.CFTH, &c.CR1, &c.CR2, &c.CR3,

@@ -33,30 +33,58 @@ struct FftConst {
   Dims d;
   int M, logM;
   const double2 *tw_m, *tw_n;
+  const float2 *tw_mf, *tw_nf;  // the same tables rounded to FP32
   const double *kx;
   Metrics m;
 };
 
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+// T: the arithmetic type of a transform (double, or float with the fields
+// still stored in FP64); V: its complex pair.
+template <typename T> struct Cx;
+template <> struct Cx<double> {
+  using V = double2;
+  __device__ static V make(double x, double y) { return make_double2(x, y); }
+};
+template <> struct Cx<float> {
+  using V = float2;
+  __device__ static V make(float x, float y) { return make_float2(x, y); }
+};
+template <typename T> __device__ __forceinline__ const typename Cx<T>::V *tw_m(const FftConst &f);
+template <> __device__ __forceinline__ const double2 *tw_m<double>(const FftConst &f) { return f.tw_m; }
+template <> __device__ __forceinline__ const float2 *tw_m<float>(const FftConst &f) { return f.tw_mf; }
+template <typename T> __device__ __forceinline__ const typename Cx<T>::V *tw_n(const FftConst &f);
+template <> __device__ __forceinline__ const double2 *tw_n<double>(const FftConst &f) { return f.tw_n; }
+template <> __device__ __forceinline__ const float2 *tw_n<float>(const FftConst &f) { return f.tw_nf; }
+
+template <typename V>
+__device__ __forceinline__ V cmul(V a, V b) {
+  V r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
 }
 
 __device__ __forceinline__ unsigned brev(unsigned v, int logM) { return __brev(v) >> (32 - logM); }
 
 // In-place radix-2 DIF over z[0..M), bit-reversed output.  conj_tw selects
 // the inverse transform.
-__device__ __forceinline__ void dif_fft(double2 *z, int M, const double2 *tw, bool conj_tw, int lane) {
+template <typename V>
+__device__ __forceinline__ void dif_fft(V *z, int M, const V *tw, bool conj_tw, int lane) {
   for (int s = M >> 1; s >= 1; s >>= 1) {
     const int stride = (M >> 1) / s;  // twiddle step M/(2s)
     for (int q = lane; q < (M >> 1); q += 32) {
       const int t = q & (s - 1);
       const int a = ((q - t) << 1) + t;
       const int b = a + s;
-      const double2 u = z[a], v = z[b];
-      z[a] = make_double2(u.x + v.x, u.y + v.y);
-      double2 dlt = make_double2(u.x - v.x, u.y - v.y);
+      const V u = z[a], v = z[b];
+      V sum, dlt;
+      sum.x = u.x + v.x;
+      sum.y = u.y + v.y;
+      dlt.x = u.x - v.x;
+      dlt.y = u.y - v.y;
+      z[a] = sum;
       if (t != 0) {
-        double2 w = tw[t * stride];
+        V w = tw[t * stride];
         if (conj_tw) w.y = -w.y;
         dlt = cmul(dlt, w);
       }
@@ -66,8 +94,11 @@ __device__ __forceinline__ void dif_fft(double2 *z, int M, const double2 *tw, bo
   }
 }
 
+template <typename T>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArgs args) {
-  extern __shared__ double2 smem_c[];
+  using V = typename Cx<T>::V;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *smem_c = reinterpret_cast<V *>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const Dims &d = fc.d;
   const int nk = args.k1 - args.k0 + 1;
@@ -77,53 +108,56 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
   const int k = args.k0 + (int)(line % nk);
   const int j = args.j0 + (int)(line / nk);
   const int NX = d.NX, M = fc.M;
-  double2 *z = smem_c + (size_t)warp * M;
-  double *zr = reinterpret_cast<double *>(z);
+  V *z = smem_c + (size_t)warp * M;
+  T *zr = reinterpret_cast<T *>(z);
   const size_t base = d.ip(0, k, j);
   if (args.pro == PRO_LOAD) {
-    for (int n = lane; n < NX; n += 32) zr[n] = args.a[base + n];
+    for (int n = lane; n < NX; n += 32) zr[n] = (T)args.a[base + n];
   } else if (args.pro == PRO_PROD) {
-    const double jac = fc.m.jac[d.m2(k, j)];
-    for (int n = lane; n < NX; n += 32) zr[n] = jac * args.a[base + n] * args.b[base + n];
+    const T jac = (T)fc.m.jac[d.m2(k, j)];
+    for (int n = lane; n < NX; n += 32) zr[n] = jac * (T)args.a[base + n] * (T)args.b[base + n];
   } else {
     // flux form of the eta/zeta convection plus the GMAT_12 cross diffusion
     // (duct.F90:735-761; the TH version at 1210-1241 has visc = NU/PR)
     const double *F = args.a;
     const double *U2b = args.b;  // U2b, followed in memory by U3b (see launch)
     const double *U3b = args.b + d.nphys();
-    const double g12a = fc.m.g12[d.m3(k + 1, j, 2)], g12b = fc.m.g12[d.m3(k, j, 2)];
-    const double g12c = fc.m.g12[d.m3(k, j + 1, 1)], g12d = fc.m.g12[d.m3(k, j, 1)];
-    const double qv = 0.25 * args.visc;
+    const T g12a = (T)fc.m.g12[d.m3(k + 1, j, 2)], g12b = (T)fc.m.g12[d.m3(k, j, 2)];
+    const T g12c = (T)fc.m.g12[d.m3(k, j + 1, 1)], g12d = (T)fc.m.g12[d.m3(k, j, 1)];
+    const T qv = (T)(0.25 * args.visc);
+    const T h = (T)0.5;
     const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
     for (int n = lane; n < NX; n += 32) {
       const size_t c = base + n;
-      const double f = F[c], fkp = F[c + sK], fkm = F[c - sK], fjp = F[c + sJ], fjm = F[c - sJ];
-      const double fpp = F[c + sK + sJ], fpm = F[c + sK - sJ], fmp = F[c - sK + sJ], fmm = F[c - sK - sJ];
-      double s1 = 0.5 * U2b[c + sJ] * (f + fjp) - 0.5 * U2b[c] * (f + fjm);
-      double s2 = 0.5 * U3b[c + sK] * (f + fkp) - 0.5 * U3b[c] * (f + fkm);
+      const T f = (T)F[c], fkp = (T)F[c + sK], fkm = (T)F[c - sK], fjp = (T)F[c + sJ], fjm = (T)F[c - sJ];
+      const T fpp = (T)F[c + sK + sJ], fpm = (T)F[c + sK - sJ], fmp = (T)F[c - sK + sJ], fmm = (T)F[c - sK - sJ];
+      T s1 = h * (T)U2b[c + sJ] * (f + fjp) - h * (T)U2b[c] * (f + fjm);
+      T s2 = h * (T)U3b[c + sK] * (f + fkp) - h * (T)U3b[c] * (f + fkm);
       s1 = -s1 + qv * (g12a * (fpp + fjp - fjm - fpm) - g12b * (fmp + fjp - fjm - fmm));
       s2 = -s2 + qv * (g12c * (fpp + fkp - fmp - fkm) - g12d * (fkp + fpm - fkm - fmm));
       zr[n] = s1 + s2;
     }
   }
   __syncwarp();
-  dif_fft(z, M, fc.tw_m, false, lane);
+  dif_fft(z, M, tw_m<T>(fc), false, lane);
   // split: X[k] = E + W^k O, E = (Z_k + conj Z_{M-k})/2, O = -i (Z_k - conj Z_{M-k})/2
   cplx_t *dst = args.dst + d.ic(0, k, j);
-  const double inv = 1.0 / NX;
+  const T inv = (T)(1.0 / NX);
+  const T h = (T)0.5;
   const int NKX = d.NKX;
+  const V *twn = tw_n<T>(fc);
   for (int kk = lane; kk <= d.NX2P; kk += 32) {
     if (kk > NKX) {
       if (args.epi == EPI_STORE) dst[kk] = cplx_t{0.0, 0.0};
       continue;
     }
-    const double2 zk = z[brev(kk & (M - 1), fc.logM)];
-    const double2 zm = z[brev((M - kk) & (M - 1), fc.logM)];
-    const double er = 0.5 * (zk.x + zm.x), ei = 0.5 * (zk.y - zm.y);
-    const double orr = 0.5 * (zk.y + zm.y), oi = -0.5 * (zk.x - zm.x);
-    const double2 w = fc.tw_n[kk];
-    const double xr = (er + (w.x * orr - w.y * oi)) * inv;
-    const double xi = (ei + (w.x * oi + w.y * orr)) * inv;
+    const V zk = z[brev(kk & (M - 1), fc.logM)];
+    const V zm = z[brev((M - kk) & (M - 1), fc.logM)];
+    const T er = h * (zk.x + zm.x), ei = h * (zk.y - zm.y);
+    const T orr = h * (zk.y + zm.y), oi = -h * (zk.x - zm.x);
+    const V w = twn[kk];
+    const double xr = (double)((er + (w.x * orr - w.y * oi)) * inv);
+    const double xi = (double)((ei + (w.x * oi + w.y * orr)) * inv);
     if (args.epi == EPI_STORE) {
       dst[kk] = cplx_t{xr, xi};
     } else if (args.epi == EPI_ADD) {
@@ -138,8 +172,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
   }
 }
 
+template <typename T>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArgs args) {
-  extern __shared__ double2 smem_c[];
+  using V = typename Cx<T>::V;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *smem_c = reinterpret_cast<V *>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const Dims &d = fc.d;
   const int nk = args.k1 - args.k0 + 1;
@@ -149,11 +186,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
   const int k = args.k0 + (int)(line % nk);
   const int j = args.j0 + (int)(line / nk);
   const int M = fc.M, NKX = d.NKX;
-  double2 *z = smem_c + (size_t)warp * M;
+  V *z = smem_c + (size_t)warp * M;
   const cplx_t *src = args.src + d.ic(0, k, j);
   const cplx_t *src2 = args.src2 ? args.src2 + d.ic(0, k, j) : nullptr;
-  auto X = [&](int kk) -> double2 {
-    if (kk > NKX || kk >= M) return make_double2(0.0, 0.0);
+  auto X = [&](int kk) -> V {
+    if (kk > NKX || kk >= M) return Cx<T>::make(0, 0);
     cplx_t v = src[kk];
     if (src2) {
       const cplx_t w = src2[kk];
@@ -161,27 +198,28 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
       v.im = v.im + args.scale2 * w.im;
     }
     if (kk == 0) v.im = 0.0;
-    return make_double2(v.re, v.im);
+    return Cx<T>::make((T)v.re, (T)v.im);
   };
   // merge: Z'[k] = (X_k + conj X_{M-k}) + i (X_k - conj X_{M-k}) W^{-k}
+  const V *twn = tw_n<T>(fc);
   for (int kk = lane; kk < M; kk += 32) {
-    const double2 a = X(kk), b = X(M - kk);
-    const double sr = a.x + b.x, si = a.y - b.y;  // X_k + conj X_{M-k}
-    const double dr = a.x - b.x, di = a.y + b.y;  // X_k - conj X_{M-k}
-    const double2 w = fc.tw_n[kk];              // conj taken below
-    const double tr = dr * w.x + di * w.y, ti = di * w.x - dr * w.y;  // (d)*conj(w)
-    z[kk] = make_double2(sr - ti, si + tr);     // + i*t
+    const V a = X(kk), b = X(M - kk);
+    const T sr = a.x + b.x, si = a.y - b.y;  // X_k + conj X_{M-k}
+    const T dr = a.x - b.x, di = a.y + b.y;  // X_k - conj X_{M-k}
+    const V w = twn[kk];                     // conj taken below
+    const T tr = dr * w.x + di * w.y, ti = di * w.x - dr * w.y;  // (d)*conj(w)
+    z[kk] = Cx<T>::make(sr - ti, si + tr);   // + i*t
   }
   __syncwarp();
-  dif_fft(z, M, fc.tw_m, true, lane);
-  const double *zr = reinterpret_cast<const double *>(z);
+  dif_fft(z, M, tw_m<T>(fc), true, lane);
+  const T *zr = reinterpret_cast<const T *>(z);
   double *dst = args.dst + d.ip(0, k, j);
   const int NX = d.NX;
   for (int n = lane; n < NX + 2; n += 32) {
     double v = 0.0;
     if (n < NX) {
       const int m = n >> 1;
-      v = zr[2 * brev(m, fc.logM) + (n & 1)];
+      v = (double)zr[2 * brev(m, fc.logM) + (n & 1)];
     }
     dst[n] = v;
   }
@@ -196,12 +234,19 @@ FftConst make_const(Ctx &c) {
   f.logM = lg;
   f.tw_m = c.tw_m;
   f.tw_n = c.tw_n;
+  f.tw_mf = c.tw_mf;
+  f.tw_nf = c.tw_nf;
   f.kx = c.kx;
   f.m = c.m;
   return f;
 }
 
 }  // namespace
+
+// FP32 arithmetic for this transform?  fft_fp32 = 1: only the transforms
+// marked low-precision (the nonlinear products and fluxes, whose results
+// enter the step multiplied by the time step); 2: every transform.
+bool fft_lowp(const Ctx &c, int lowp) { return c.p.fft_fp32 >= 2 || (c.p.fft_fp32 == 1 && lowp); }
 
 void launch_r2c(Ctx &c, const R2cArgs &a) {
   const FftConst fc = make_const(c);
@@ -212,7 +257,8 @@ void launch_r2c(Ctx &c, const R2cArgs &a) {
   const int nops = (a.pro == PRO_LOAD) ? 1 : (a.pro == PRO_PROD) ? 2 : 3;
   const double epi = (a.epi == EPI_STORE) ? 16.0 * (c.d.NX2P + 1) : 32.0 * (c.d.NKX + 1);
   KScope ks(c, KC_R2C, nlines * (8.0 * c.d.NX * nops + epi));
-  k_r2c<<<grid, 32 * kWarpsPerBlock, smem, c.stream>>>(fc, a);
+  if (fft_lowp(c, a.lowp)) k_r2c<float><<<grid, 32 * kWarpsPerBlock, smem / 2, c.stream>>>(fc, a);
+  else k_r2c<double><<<grid, 32 * kWarpsPerBlock, smem, c.stream>>>(fc, a);
   after_launch(c);
 }
 
@@ -223,7 +269,8 @@ void launch_c2r(Ctx &c, const C2rArgs &a) {
   const unsigned grid = (unsigned)((nlines + kWarpsPerBlock - 1) / kWarpsPerBlock);
   const size_t smem = sizeof(double2) * fc.M * kWarpsPerBlock;
   KScope ks(c, KC_C2R, nlines * (16.0 * (c.d.NKX + 1) * (a.src2 ? 2 : 1) + 8.0 * (c.d.NX + 2)));
-  k_c2r<<<grid, 32 * kWarpsPerBlock, smem, c.stream>>>(fc, a);
+  if (fft_lowp(c, a.lowp)) k_c2r<float><<<grid, 32 * kWarpsPerBlock, smem / 2, c.stream>>>(fc, a);
+  else k_c2r<double><<<grid, 32 * kWarpsPerBlock, smem, c.stream>>>(fc, a);
   after_launch(c);
 }
 
@@ -233,8 +280,10 @@ namespace ek {
 void fft_init_attributes() {
   static bool done = false;
   if (done) return;
-  EK_CUDA(cudaFuncSetAttribute(k_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-  EK_CUDA(cudaFuncSetAttribute(k_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+  EK_CUDA(cudaFuncSetAttribute(k_r2c<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+  EK_CUDA(cudaFuncSetAttribute(k_c2r<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+  EK_CUDA(cudaFuncSetAttribute(k_r2c<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+  EK_CUDA(cudaFuncSetAttribute(k_c2r<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
   done = true;
 }
 }  // namespace ek
@@ -329,13 +378,13 @@ int run_standalone(bool forward, int nx, int nkx, long nlines, const double *in,
     a.pro = PRO_LOAD;
     a.epi = EPI_STORE;
     a.k0 = 0; a.k1 = (int)nlines - 1; a.j0 = 0; a.j1 = 0;
-    k_r2c<<<grid, 32 * kWarpsPerBlock, smem, s>>>(fc, a);
+    k_r2c<double><<<grid, 32 * kWarpsPerBlock, smem, s>>>(fc, a);
   } else {
     C2rArgs a{};
     a.src = reinterpret_cast<const cplx_t *>(in);
     a.dst = out;
     a.k0 = 0; a.k1 = (int)nlines - 1; a.j0 = 0; a.j1 = 0;
-    k_c2r<<<grid, 32 * kWarpsPerBlock, smem, s>>>(fc, a);
+    k_c2r<double><<<grid, 32 * kWarpsPerBlock, smem, s>>>(fc, a);
   }
   EK_CUDA(cudaPeekAtLastError());
   return EK_OK;

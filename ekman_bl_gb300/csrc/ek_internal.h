@@ -168,6 +168,7 @@ struct Ctx {
   // FFT twiddles
   double2 *tw_m = nullptr;  // exp(-2 pi i t/M), t < M/2   (M = NX/2)
   double2 *tw_n = nullptr;  // exp(-2 pi i k/NX), k <= M
+  float2 *tw_mf = nullptr, *tw_nf = nullptr;  // the same, rounded to FP32
   Metrics m{};
   // spectral fields (complex)
   cplx_t *CU1, *CU2, *CU3, *CP, *CTH, *CF1, *CF2, *CF3, *CFTH, *CR1, *CR2, *CR3, *CRTH, *CS, *CU2b, *CU3b;
@@ -270,6 +271,7 @@ struct R2cArgs {
   int epi;
   int pro;
   int j0, j1, k0, k1;
+  int lowp;               // a nonlinear-term transform (FP32 arithmetic when fft_fp32 = 1)
 };
 void launch_r2c(Ctx &c, const R2cArgs &a);
 struct C2rArgs {
@@ -277,6 +279,7 @@ struct C2rArgs {
   double scale2;
   double *dst;
   int j0, j1, k0, k1;
+  int lowp;                  // as R2cArgs::lowp
 };
 void launch_c2r(Ctx &c, const C2rArgs &a);
 

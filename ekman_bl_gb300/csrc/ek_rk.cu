@@ -198,10 +198,6 @@ __global__ void k_face_velocity(Dims d, Metrics m, const double *U2, const doubl
   U3b[c] = 0.5 * m.c11[d.m3(k, j, 2)] * (U3[c] + U3[c - sK]) + 0.5 * m.c12[d.m3(k, j, 2)] * (U2[c] + U2[c - sK]);
 }
 
-// CN-ADI line solves.  One thread per x point I; the Thomas factors of the
-// line (I-independent) were precomputed on the host; shared memory holds
-// the forward-eliminated right-hand side of every thread's line.
-constexpr int kAdiThreads = 32;
 
 struct AdiArgs {
   Dims d;
@@ -215,105 +211,91 @@ struct AdiArgs {
   int js, je, zs, ze;
 };
 
-// y sweep, duct.F90:1640-1739 for U1 (TH 1334-1433, U2 1877-1980, U3 2137-2233):
-// R' = S/2 + J phi + coef d_zeta(G11 d_zeta phi), S = R - J phi; solve the
-// y-tridiagonal of each (I,K) line; the solution goes to phs.
-__global__ void __launch_bounds__(kAdiThreads) k_adi_y(AdiArgs a) {
-  extern __shared__ double g[];  // [row][thread]
+// CN-ADI line solves: a block owns 32 consecutive x points (lanes) of one
+// line.  Its kAdiWarps warps build the right-hand side of every row in
+// parallel straight into shared memory, together with the line's Thomas
+// factors (precomputed on the host, I-independent); then warp 0 runs the
+// forward elimination and back substitution (THOMAS_REAL) from shared
+// memory, one lane per x point.
+//
+// y sweep (ZS = false), duct.F90:1640-1739 for U1 (TH 1334-1433, U2
+// 1877-1980, U3 2137-2233): R' = S/2 + J phi + coef d_zeta(G11 d_zeta phi),
+// S = R - J phi; the solution of each (I,K) line goes to phs.
+// z sweep (ZS = true), duct.F90:1741-1854 for U1 (TH 1437-1600, U2
+// 1983-2115, U3 2257-2392): R'' = S/2 + J phi* + coef d_eta(G22 d_eta phi*);
+// the solution of each (I,J) line goes into the field; rows J outside the
+// solved range take the y-sweep values.
+constexpr int kAdiWarps = 8;
+template <bool ZS>
+__global__ void __launch_bounds__(32 * kAdiWarps) k_adi(AdiArgs a) {
+  extern __shared__ double sm[];
   const Dims &d = a.d;
-  const int t = threadIdx.x;
-  const int i = blockIdx.x * kAdiThreads + t;
-  const int k = a.zs + blockIdx.y;
-  const int nrow = d.NY2;
+  const int lane = threadIdx.x, w = threadIdx.y;
+  const int i = blockIdx.x * 32 + lane;
+  const int line = ZS ? (int)blockIdx.y : a.zs + (int)blockIdx.y;
+  const int nrow = ZS ? d.NZ2 : d.NY2;
   const bool act = (i < d.NX);
-  const size_t sK = d.LDX;
-  const double *fa = a.fa + (size_t)k * nrow, *fib = a.fib + (size_t)k * nrow, *fu = a.fu + (size_t)k * nrow;
-  const double g1 = 0, g0 = 0;
-  (void)g1; (void)g0;
-  // right-hand side of every row
-  for (int r = 0; r < nrow; ++r) {
+  if (ZS && (line < a.js || line > a.je)) {
+    if (act)
+      for (int k = a.zs + w; k <= a.ze; k += kAdiWarps) a.out[d.ip(i, k, line)] = a.phs[d.ip(i, k, line)];
+    return;
+  }
+  double *g = sm;  // [row][lane]
+  double *sfa = sm + (size_t)nrow * 32, *sfib = sfa + nrow, *sfu = sfib + nrow;
+  {
+    const double *fa = a.fa + (size_t)line * nrow, *fib = a.fib + (size_t)line * nrow, *fu = a.fu + (size_t)line * nrow;
+    for (int r = w * 32 + lane; r < nrow; r += 32 * kAdiWarps) {
+      sfa[r] = fa[r];
+      sfib[r] = fib[r];
+      sfu[r] = fu[r];
+    }
+  }
+  const int r0 = ZS ? a.zs : a.js, r1 = ZS ? a.ze : a.je;
+  for (int r = w; r < nrow; r += kAdiWarps) {
     double v = 0.0;
     if (act) {
-      if (r >= a.js && r <= a.je) {
-        const size_t c = d.ip(i, k, r);
-        const double jac = a.m.jac[d.m2(k, r)];
-        const double ph = a.phi_old[c];
-        const double s = a.R[c] - jac * ph;
-        const double gp = a.m.g11[d.m3(k + 1, r, 2)], gm = a.m.g11[d.m3(k, r, 2)];
-        v = 0.5 * s + jac * ph + a.coef * (gp * (a.phi_old[c + sK] - ph) - gm * (ph - a.phi_old[c - sK]));
+      if (r >= r0 && r <= r1) {
+        if (!ZS) {
+          const int k = line;
+          const size_t c = d.ip(i, k, r), sK = d.LDX;
+          const double jac = a.m.jac[d.m2(k, r)];
+          const double ph = a.phi_old[c];
+          const double s = a.R[c] - jac * ph;
+          const double gp = a.m.g11[d.m3(k + 1, r, 2)], gm = a.m.g11[d.m3(k, r, 2)];
+          v = 0.5 * s + jac * ph + a.coef * (gp * (a.phi_old[c + sK] - ph) - gm * (ph - a.phi_old[c - sK]));
+        } else {
+          const int j = line;
+          const size_t c = d.ip(i, r, j), sJ = (size_t)d.LDX * d.NZ2;
+          const double jac = a.m.jac[d.m2(r, j)];
+          const double s = a.R[c] - jac * a.phi_old[c];
+          const double ps = a.phs[c];
+          const double gp = a.m.g22[d.m3(r, j + 1, 1)], gm = a.m.g22[d.m3(r, j, 1)];
+          v = 0.5 * s + jac * ps + a.coef * (+gp * (a.phs[c + sJ] - ps) - gm * (ps - a.phs[c - sJ]));
+        }
       }
       for (int b = 0; b < a.bc.n; ++b) {
         const BcRow &br = a.bc.r[b];
         if (br.row != r) continue;
         if (br.kind == 0) v = br.val;
-        else if (br.kind == 1) v = a.phi_old[d.ip(i, k, br.src)];
-        else v = br.val * a.bcw[br.src + k];
+        else if (br.kind == 1) v = ZS ? a.phs[d.ip(i, br.src, line)] : a.phi_old[d.ip(i, line, br.src)];
+        else v = br.val * a.bcw[br.src + line];
       }
     }
-    g[r * kAdiThreads + t] = v;
+    g[r * 32 + lane] = v;
   }
-  if (!act) return;
-  // forward elimination then back substitution (THOMAS_REAL)
-  double prev = g[t];
+  __syncthreads();
+  if (w != 0 || !act) return;
+  auto at = [&](int r) { return ZS ? d.ip(i, r, line) : d.ip(i, line, r); };
+  double prev = g[lane];
   for (int r = 1; r < nrow; ++r) {
-    prev = g[r * kAdiThreads + t] + fa[r] * prev;
-    g[r * kAdiThreads + t] = prev;
+    prev = g[r * 32 + lane] + sfa[r] * prev;
+    g[r * 32 + lane] = prev;
   }
-  double x = prev * fib[nrow - 1];
-  a.out[d.ip(i, k, nrow - 1)] = x;
+  double x = prev * sfib[nrow - 1];
+  a.out[at(nrow - 1)] = x;
   for (int r = nrow - 2; r >= 0; --r) {
-    x = (g[r * kAdiThreads + t] - fu[r] * x) * fib[r];
-    a.out[d.ip(i, k, r)] = x;
-  }
-}
-
-// z sweep, duct.F90:1741-1854 for U1 (TH 1437-1600, U2 1983-2115,
-// U3 2257-2392): R'' = S/2 + J phi* + coef d_eta(G22 d_eta phi*); solve the
-// z-tridiagonal of each (I,J) line into the field.  Rows J outside the
-// solved range take the y-sweep values.
-__global__ void __launch_bounds__(kAdiThreads) k_adi_z(AdiArgs a) {
-  extern __shared__ double g[];
-  const Dims &d = a.d;
-  const int t = threadIdx.x;
-  const int i = blockIdx.x * kAdiThreads + t;
-  const int j = blockIdx.y;
-  const int nrow = d.NZ2;
-  if (i >= d.NX) return;
-  if (j < a.js || j > a.je) {
-    for (int k = a.zs; k <= a.ze; ++k) a.out[d.ip(i, k, j)] = a.phs[d.ip(i, k, j)];
-    return;
-  }
-  const size_t sJ = (size_t)d.LDX * d.NZ2;
-  const double *fa = a.fa + (size_t)j * nrow, *fib = a.fib + (size_t)j * nrow, *fu = a.fu + (size_t)j * nrow;
-  for (int r = 0; r < nrow; ++r) {
-    double v = 0.0;
-    if (r >= a.zs && r <= a.ze) {
-      const size_t c = d.ip(i, r, j);
-      const double jac = a.m.jac[d.m2(r, j)];
-      const double s = a.R[c] - jac * a.phi_old[c];
-      const double ps = a.phs[c];
-      const double gp = a.m.g22[d.m3(r, j + 1, 1)], gm = a.m.g22[d.m3(r, j, 1)];
-      v = 0.5 * s + jac * ps + a.coef * (+gp * (a.phs[c + sJ] - ps) - gm * (ps - a.phs[c - sJ]));
-    }
-    for (int b = 0; b < a.bc.n; ++b) {
-      const BcRow &br = a.bc.r[b];
-      if (br.row != r) continue;
-      if (br.kind == 0) v = br.val;
-      else if (br.kind == 1) v = a.phs[d.ip(i, br.src, j)];
-      else v = br.val * a.bcw[br.src + j];
-    }
-    g[r * kAdiThreads + t] = v;
-  }
-  double prev = g[t];
-  for (int r = 1; r < nrow; ++r) {
-    prev = g[r * kAdiThreads + t] + fa[r] * prev;
-    g[r * kAdiThreads + t] = prev;
-  }
-  double x = prev * fib[nrow - 1];
-  a.out[d.ip(i, nrow - 1, j)] = x;
-  for (int r = nrow - 2; r >= 0; --r) {
-    x = (g[r * kAdiThreads + t] - fu[r] * x) * fib[r];
-    a.out[d.ip(i, r, j)] = x;
+    x = (g[r * 32 + lane] - sfu[r] * x) * sfib[r];
+    a.out[at(r)] = x;
   }
 }
 
@@ -607,10 +589,10 @@ void launch_adi(Ctx &c, int field, int rk) {
   a.fu = c.adi[field][rk][0].u;
   a.bc = c.bc[field][0];
   {
-    const size_t smem = sizeof(double) * kAdiThreads * d.NY2;
-    dim3 grid((d.NX + kAdiThreads - 1) / kAdiThreads, a.ze - a.zs + 1);
+    const size_t smem = sizeof(double) * (32 + 3) * d.NY2;
+    dim3 grid((d.NX + 31) / 32, a.ze - a.zs + 1);
     KScope ks(c, KC_ADI_Y, 24.0 * d.NX * d.NY2 * (a.ze - a.zs + 1));
-    k_adi_y<<<grid, kAdiThreads, smem, c.stream>>>(a);
+    k_adi<false><<<grid, dim3(32, kAdiWarps), smem, c.stream>>>(a);
     after_launch(c);
   }
   // z sweep
@@ -620,10 +602,10 @@ void launch_adi(Ctx &c, int field, int rk) {
   a.fu = c.adi[field][rk][1].u;
   a.bc = c.bc[field][1];
   {
-    const size_t smem = sizeof(double) * kAdiThreads * d.NZ2;
-    dim3 grid((d.NX + kAdiThreads - 1) / kAdiThreads, d.NY2);
+    const size_t smem = sizeof(double) * (32 + 3) * d.NZ2;
+    dim3 grid((d.NX + 31) / 32, d.NY2);
     KScope ks(c, KC_ADI_Z, 32.0 * d.NX * d.NZ2 * (a.je - a.js + 1));
-    k_adi_z<<<grid, kAdiThreads, smem, c.stream>>>(a);
+    k_adi<true><<<grid, dim3(32, kAdiWarps), smem, c.stream>>>(a);
     after_launch(c);
   }
 }
@@ -693,13 +675,13 @@ int finish_divergence(Ctx &c, double *div_out) {
 
 namespace ek {
 // The ADI kernels keep one line of right-hand sides per thread in shared
-// memory (32 threads x (NY+2) doubles), more than the default 48 KB for
+// memory ((32 + 3) x (NY+2) doubles), more than the default 48 KB for
 // tall grids.
 void rk_init_attributes() {
   static bool done = false;
   if (done) return;
-  EK_CUDA(cudaFuncSetAttribute(k_adi_y, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  EK_CUDA(cudaFuncSetAttribute(k_adi_z, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  EK_CUDA(cudaFuncSetAttribute(k_adi<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  EK_CUDA(cudaFuncSetAttribute(k_adi<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   done = true;
 }
 }  // namespace ek

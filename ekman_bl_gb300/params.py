@@ -45,7 +45,7 @@ class EkParams(C.Structure):
         ("quirk_phi_fp32", C.c_int), ("mg_fast", C.c_int), ("sponge_type", C.c_int), ("les", C.c_int),
         ("ny_s_t", C.c_int), ("nz_s_r", C.c_int), ("nz_s_l", C.c_int), ("save_stats_int", C.c_int),
         ("time_step", C.c_int), ("variable_dt", C.c_int), ("update_dt", C.c_int),
-        ("cfl", C.c_double), ("delta_t_set", C.c_double),
+        ("cfl", C.c_double), ("delta_t_set", C.c_double), ("fft_fp32", C.c_int),
     ]
 
 

@@ -104,6 +104,8 @@ typedef struct ek_params {
   int update_dt;             /* UPDATE_DT                                               */
   double cfl;                /* CFL                                                     */
   double delta_t_set;        /* DELTA_T_SET: the cap of the CFL time step               */
+  int fft_fp32;              /* x-transforms in FP32 arithmetic (fields stay FP64): 0 none,
+                                1 the nonlinear product/flux transforms, 2 every transform */
 } ek_params;
 
 /* Geometry and background fields of JACOBI_TRANS (diablo.F90:1088-1570);

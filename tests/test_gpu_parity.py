@@ -10,7 +10,7 @@ import pytest
 from ekcases import refgrid_case, rel_l2, sheared_case, small_case
 from ekman_bl_gb300 import build as ekbuild
 from ekman_bl_gb300.duct import DuctSolver, metrics_from_grid
-from ekman_bl_gb300.params import (EK_F_CF1, EK_F_CF2, EK_F_CF3, EK_F_CFTH, EK_F_CR1, WORKLOADS,
+from ekman_bl_gb300.params import (EK_MG_STOP_RESIDUAL, EK_F_CF1, EK_F_CF2, EK_F_CF3, EK_F_CFTH, EK_F_CR1, WORKLOADS,
                                    workload_setup)
 from oracle import ekref
 
@@ -195,3 +195,27 @@ def test_mixed_precision_steps_track_oracle():
     for name, x, y in zip(("CU1", "CU2", "CU3", "CP", "CTH"), a, b):
         assert rel_l2(x, y) < 1e-7, name
     assert g.divergence() < 1e-7
+
+
+def test_mixed_path_hundred_steps_neutral_64():
+    """The mixed-precision path (FP32 V-cycles inside FP64 refinement at
+    1e-10, FP32 arithmetic in the nonlinear-term transforms) against the
+    FP64 oracle after 100 steps of the 64 x 65 x 65 case: velocity and
+    buoyancy within 1e-5 relative L2, divergence below 1e-8."""
+    w = WORKLOADS["ekman_neutral_64x65x65"]
+    p, xp, yp, st = workload_setup(w, EK_MG_STOP_RESIDUAL)
+    p.mg_tol, p.mg_maxcy = 1e-10, 200
+    o = ekref.Oracle(p, ekref.metrics_from_grid(p, xp, yp))
+    q = workload_setup(w, EK_MG_STOP_RESIDUAL)[0]
+    q.mg_tol, q.mg_maxcy, q.mg_fast, q.fft_fp32 = 1e-10, 60, 1, 1
+    g = DuctSolver(q, metrics_from_grid(q, xp, yp))
+    g.upload(*st)
+    o.upload(*st)
+    g.rem_div_curv()
+    o.rem_div()
+    g.step(100)
+    o.step(100)
+    a, b = g.download(), o.download()
+    for name, x, y in zip(("CU1", "CU2", "CU3", "CTH"), (a[0], a[1], a[2], a[4]), (b[0], b[1], b[2], b[4])):
+        assert rel_l2(x, y) < 1e-5, name
+    assert g.divergence() < 1e-8
