@@ -112,14 +112,16 @@ int substep(Ctx &c, int rk) {
   const double TEMP4 = c.H_BAR[rk];
   const double TEMP5 = c.BETA_BAR[rk] * c.H_BAR[rk];
   launch_spectral_rhs(c, rk);
+  // FP32 copies of the physical fields for the nonlinear terms (fft_fp32)
+  const bool f32 = p.fft_fp32 != 0;
   // to physical space (duct.F90:656-673)
   {
     C2rArgs a{};
     a.j0 = 0; a.j1 = d.NY + 1; a.k0 = 0; a.k1 = d.NZ + 1;
-    a.src = c.CU1; a.dst = c.U1; launch_c2r(c, a);
-    a.src = c.CU2; a.dst = c.U2; launch_c2r(c, a);
-    a.src = c.CU3; a.dst = c.U3; launch_c2r(c, a);
-    if (th) { a.src = c.CTH; a.dst = c.TH; launch_c2r(c, a); }
+    a.src = c.CU1; a.dst = c.U1; a.dstf = f32 ? c.U1f : nullptr; launch_c2r(c, a);
+    a.src = c.CU2; a.dst = c.U2; a.dstf = f32 ? c.U2f : nullptr; launch_c2r(c, a);
+    a.src = c.CU3; a.dst = c.U3; a.dstf = f32 ? c.U3f : nullptr; launch_c2r(c, a);
+    if (th) { a.src = c.CTH; a.dst = c.TH; a.dstf = f32 ? c.THf : nullptr; launch_c2r(c, a); }
   }
   launch_face_velocity(c);
   // nonlinear and cross-diffusion terms, fused with their forward FFTs
@@ -128,12 +130,15 @@ int substep(Ctx &c, int rk) {
     R2cArgs a{};
     a.j0 = d.JS; a.j1 = d.JE; a.k0 = d.ZS; a.k1 = d.ZE;
     const double *uu[3] = {c.U1, c.U2, c.U3};
+    const float *uf[3] = {c.U1f, c.U2f, c.U3f};
     cplx_t *cf[3] = {c.CF1, c.CF2, c.CF3};
     a.lowp = 1;
     for (int f = 0; f < 3; ++f) {
       a.pro = PRO_PROD; a.a = c.U1; a.b = uu[f]; a.epi = EPI_SUB_IK; a.dst = cf[f];
+      a.af = f32 ? c.U1f : nullptr; a.bf = f32 ? uf[f] : nullptr;
       launch_r2c(c, a);
       a.pro = PRO_FLUX; a.a = uu[f]; a.b = c.U2b; a.visc = p.nu; a.epi = EPI_ADD;
+      a.af = f32 ? uf[f] : nullptr; a.bf = f32 ? c.U2bf : nullptr;
       launch_r2c(c, a);
     }
   }
@@ -152,8 +157,10 @@ int substep(Ctx &c, int rk) {
     a.j0 = d.JST; a.j1 = d.JET; a.k0 = d.ZST; a.k1 = d.ZET;
     a.lowp = 1;
     a.pro = PRO_PROD; a.a = c.TH; a.b = c.U1; a.epi = EPI_SUB_IK; a.dst = c.CFTH;
+    a.af = f32 ? c.THf : nullptr; a.bf = f32 ? c.U1f : nullptr;
     launch_r2c(c, a);
     a.pro = PRO_FLUX; a.a = c.TH; a.b = c.U2b; a.visc = p.nu / p.pr; a.epi = EPI_ADD;
+    a.af = f32 ? c.THf : nullptr; a.bf = f32 ? c.U2bf : nullptr;
     launch_r2c(c, a);
     C2rArgs b{};
     b.j0 = d.JST; b.j1 = d.JET; b.k0 = d.ZST; b.k1 = d.ZET;
@@ -296,6 +303,7 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
     return reject("only MUDPACK_BC = 0 0 2 2 is supported");
   if (p.sponge_type < 0 || p.sponge_type > 2) return reject("SPONGE_TYPE must be 0, 1 or 2");
   if (p.sponge_type != 0 && p.save_stats_int < 1) return reject("SAVE_STATS_INT must be >= 1 with a sponge");
+  if (p.fft_fp32 < 0 || p.fft_fp32 > 2) return reject("fft_fp32 must be 0, 1 or 2");
   if (p.variable_dt && (p.update_dt < 1 || !(p.cfl > 0.0) || !(p.delta_t_set > 0.0)))
     return reject("VARIABLE_DT needs UPDATE_DT >= 1, CFL > 0 and DELTA_T_SET > 0");
   if (p.sponge_type != 0 && p.ny_s_t <= p.ny && p.ny_s_t < 0) return reject("NY_S_T must be >= 0");
@@ -379,6 +387,11 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
     for (double **f : {&c.U1, &c.U2, &c.U3, &c.TH, &c.R1, &c.R2, &c.R3, &c.RTH, &c.PHS, &c.SPH}) *f = dalloc<double>(c, np);
     c.U2b = dalloc<double>(c, 2 * np);
     c.U3b = c.U2b + np;
+    if (p.fft_fp32) {
+      for (float **f : {&c.U1f, &c.U2f, &c.U3f, &c.THf}) *f = dalloc<float>(c, np);
+      c.U2bf = dalloc<float>(c, 2 * np);
+      c.U3bf = c.U2bf + np;
+    }
     c.div_part = dalloc<double>(c, d.NY2);
     c.cfl_dt = dalloc<double>(c, 1);
     c.sponge_sig = dalloc<double>(c, d.NY2 + d.NZ2 + 4);

@@ -111,11 +111,34 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
   V *z = smem_c + (size_t)warp * M;
   T *zr = reinterpret_cast<T *>(z);
   const size_t base = d.ip(0, k, j);
+  constexpr bool kF = sizeof(T) == 4;
+  const bool fin = kF && args.af != nullptr;  // FP32 copies of the inputs
   if (args.pro == PRO_LOAD) {
     for (int n = lane; n < NX; n += 32) zr[n] = (T)args.a[base + n];
   } else if (args.pro == PRO_PROD) {
     const T jac = (T)fc.m.jac[d.m2(k, j)];
-    for (int n = lane; n < NX; n += 32) zr[n] = jac * (T)args.a[base + n] * (T)args.b[base + n];
+    if (fin)
+      for (int n = lane; n < NX; n += 32) zr[n] = jac * (T)args.af[base + n] * (T)args.bf[base + n];
+    else
+      for (int n = lane; n < NX; n += 32) zr[n] = jac * (T)args.a[base + n] * (T)args.b[base + n];
+  } else if (fin) {
+    // the flux stencil below on the FP32 copies
+    const float *F = args.af, *U2b = args.bf, *U3b = args.bf + d.nphys();
+    const T g12a = (T)fc.m.g12[d.m3(k + 1, j, 2)], g12b = (T)fc.m.g12[d.m3(k, j, 2)];
+    const T g12c = (T)fc.m.g12[d.m3(k, j + 1, 1)], g12d = (T)fc.m.g12[d.m3(k, j, 1)];
+    const T qv = (T)(0.25 * args.visc);
+    const T h = (T)0.5;
+    const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
+    for (int n = lane; n < NX; n += 32) {
+      const size_t c = base + n;
+      const T f = F[c], fkp = F[c + sK], fkm = F[c - sK], fjp = F[c + sJ], fjm = F[c - sJ];
+      const T fpp = F[c + sK + sJ], fpm = F[c + sK - sJ], fmp = F[c - sK + sJ], fmm = F[c - sK - sJ];
+      T s1 = h * (T)U2b[c + sJ] * (f + fjp) - h * (T)U2b[c] * (f + fjm);
+      T s2 = h * (T)U3b[c + sK] * (f + fkp) - h * (T)U3b[c] * (f + fkm);
+      s1 = -s1 + qv * (g12a * (fpp + fjp - fjm - fpm) - g12b * (fmp + fjp - fjm - fmm));
+      s2 = -s2 + qv * (g12c * (fpp + fkp - fmp - fkm) - g12d * (fkp + fpm - fkm - fmm));
+      zr[n] = s1 + s2;
+    }
   } else {
     // flux form of the eta/zeta convection plus the GMAT_12 cross diffusion
     // (duct.F90:735-761; the TH version at 1210-1241 has visc = NU/PR)
@@ -156,8 +179,23 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
     const T er = h * (zk.x + zm.x), ei = h * (zk.y - zm.y);
     const T orr = h * (zk.y + zm.y), oi = -h * (zk.x - zm.x);
     const V w = twn[kk];
-    const double xr = (double)((er + (w.x * orr - w.y * oi)) * inv);
-    const double xi = (double)((ei + (w.x * oi + w.y * orr)) * inv);
+    const T tr = (er + (w.x * orr - w.y * oi)) * inv;
+    const T ti = (ei + (w.x * oi + w.y * orr)) * inv;
+    if (kF) {
+      // the FP32 result enters the FP64 field with one exact widening and
+      // one FP64 add per component
+      const cplx_t o = (args.epi == EPI_STORE) ? cplx_t{0.0, 0.0} : dst[kk];
+      if (args.epi == EPI_STORE) {
+        dst[kk] = cplx_t{f2d_bits((float)tr), f2d_bits((float)ti)};
+      } else if (args.epi == EPI_ADD) {
+        dst[kk] = cplx_t{o.re + f2d_bits((float)tr), o.im + f2d_bits((float)ti)};
+      } else {
+        const T kv = (T)fc.kx[kk];
+        dst[kk] = cplx_t{o.re - f2d_bits((float)(T(0) * tr - kv * ti)), o.im - f2d_bits((float)(T(0) * ti + kv * tr))};
+      }
+      continue;
+    }
+    const double xr = (double)tr, xi = (double)ti;
     if (args.epi == EPI_STORE) {
       dst[kk] = cplx_t{xr, xi};
     } else if (args.epi == EPI_ADD) {
@@ -214,14 +252,21 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
   dif_fft(z, M, tw_m<T>(fc), true, lane);
   const T *zr = reinterpret_cast<const T *>(z);
   double *dst = args.dst + d.ip(0, k, j);
+  float *dstf = args.dstf ? args.dstf + d.ip(0, k, j) : nullptr;
   const int NX = d.NX;
   for (int n = lane; n < NX + 2; n += 32) {
-    double v = 0.0;
+    T v = T(0);
     if (n < NX) {
       const int m = n >> 1;
-      v = (double)zr[2 * brev(m, fc.logM) + (n & 1)];
+      v = zr[2 * brev(m, fc.logM) + (n & 1)];
     }
-    dst[n] = v;
+    if (sizeof(T) == 4) {
+      dst[n] = f2d_bits((float)v);
+      if (dstf) dstf[n] = (float)v;
+    } else {
+      dst[n] = (double)v;
+      if (dstf) dstf[n] = d2f_bits((double)v);
+    }
   }
 }
 

@@ -35,6 +35,37 @@ struct Dims {
   __host__ __device__ size_t nspec() const { return (size_t)LDC * NZ2 * NY2; }
 };
 
+// double <-> float on the integer pipes.  GB300's FP64 pipe (which also
+// executes the F2F conversions) is narrow, so FP32 kernels on FP64 fields
+// would otherwise be bound by their conversions.  Round to nearest even;
+// values below the float normal range become zero, infinities and NaN go
+// through the hardware conversion.
+#ifdef __CUDACC__
+__device__ __forceinline__ float d2f_bits(double x) {
+  const unsigned uh = (unsigned)__double2hiint(x), ul = (unsigned)__double2loint(x);
+  const unsigned sign = uh & 0x80000000u;
+  const int e = (int)((uh >> 20) & 0x7ffu);
+  if (e == 0x7ff) return (float)x;
+  const int fe = e - 896;
+  if (fe <= 0) return __uint_as_float(sign);
+  if (fe >= 0xff) return __uint_as_float(sign | 0x7f800000u);
+  const unsigned mant = ((uh & 0xfffffu) << 3) | (ul >> 29);
+  unsigned r = sign | ((unsigned)fe << 23) | mant;
+  const unsigned dropped = ul & 0x1fffffffu;
+  if (dropped > 0x10000000u || (dropped == 0x10000000u && (mant & 1u))) r += 1u;
+  return __uint_as_float(r);
+}
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned sign = u & 0x80000000u;
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0) return __hiloint2double((int)sign, 0);
+  if (e == 0xff) return (double)f;
+  const unsigned mant = u & 0x7fffffu;
+  return __hiloint2double((int)(sign | ((e + 896u) << 20) | (mant >> 3)), (int)(mant << 29));
+}
+#endif
+
 // Device copies of the JACOBI_TRANS metric arrays.
 struct Metrics {
   double *jac, *g11, *g12, *g22, *c11, *c12, *c21, *c22, *thbar;
@@ -174,6 +205,8 @@ struct Ctx {
   cplx_t *CU1, *CU2, *CU3, *CP, *CTH, *CF1, *CF2, *CF3, *CFTH, *CR1, *CR2, *CR3, *CRTH, *CS, *CU2b, *CU3b;
   // physical fields
   double *U1, *U2, *U3, *TH, *R1, *R2, *R3, *RTH, *U2b, *U3b, *PHS, *SPH;
+  // FP32 copies of the physical fields the nonlinear terms read (fft_fp32)
+  float *U1f = nullptr, *U2f = nullptr, *U3f = nullptr, *THf = nullptr, *U2bf = nullptr, *U3bf = nullptr;
   // ADI: [field 0..3][rk 1..3][dir 0 y, 1 z]
   AdiFactors adi[4][4][2];
   BcSet bc[4][2];
@@ -272,6 +305,7 @@ struct R2cArgs {
   int pro;
   int j0, j1, k0, k1;
   int lowp;               // a nonlinear-term transform (FP32 arithmetic when fft_fp32 = 1)
+  const float *af, *bf;   // FP32 copies of a, b read by the FP32 kernel when given
 };
 void launch_r2c(Ctx &c, const R2cArgs &a);
 struct C2rArgs {
@@ -280,6 +314,7 @@ struct C2rArgs {
   double *dst;
   int j0, j1, k0, k1;
   int lowp;                  // as R2cArgs::lowp
+  float *dstf;               // also write an FP32 copy of dst when given
 };
 void launch_c2r(Ctx &c, const C2rArgs &a);
 

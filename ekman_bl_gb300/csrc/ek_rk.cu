@@ -15,6 +15,21 @@ __device__ __forceinline__ cplx_t cmul(cplx_t a, cplx_t b) {
   return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
 }
 
+// x / b for several x sharing one divisor b: r = RN(1/b) once, then per
+// quotient q0 = RN(x r), e = x - b q0 (exact with an FMA), q = RN(q0 + e r),
+// Markstein's correction step, which rounds the quotient correctly.  Saves
+// the full FP64 division sequence per quotient on a GPU whose FP64 pipe is
+// narrow.
+struct DivBy {
+  double b, r;
+  __device__ explicit DivBy(double bb) : b(bb), r(1.0 / bb) {}
+  __device__ DivBy(double bb, double rr) : b(bb), r(rr) {}
+  __device__ double operator()(double x) const {
+    const double q0 = x * r;
+    return fma(fma(-b, q0, x), r, q0);
+  }
+};
+
 struct SpecArgs {
   Dims d;
   Metrics m;
@@ -187,15 +202,23 @@ __global__ void k_spectral_rhs(SpecArgs a) {
 
 // Contravariant face velocities U2b, U3b (duct.F90:721-732); U3b is stored
 // right after U2b.
-__global__ void k_face_velocity(Dims d, Metrics m, const double *U2, const double *U3, double *U2b) {
+__global__ void k_face_velocity(Dims d, Metrics m, const double *U2, const double *U3, double *U2b, float *U2bf) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int k = d.ZS + blockIdx.y, j = d.JS + blockIdx.z;
   if (i >= d.NX) return;
   double *U3b = U2b + d.nphys();
   const size_t c = d.ip(i, k, j);
   const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
-  U2b[c] = 0.5 * m.c22[d.m3(k, j, 1)] * (U2[c] + U2[c - sJ]) + 0.5 * m.c21[d.m3(k, j, 1)] * (U3[c] + U3[c - sJ]);
-  U3b[c] = 0.5 * m.c11[d.m3(k, j, 2)] * (U3[c] + U3[c - sK]) + 0.5 * m.c12[d.m3(k, j, 2)] * (U2[c] + U2[c - sK]);
+  const double u2b = 0.5 * m.c22[d.m3(k, j, 1)] * (U2[c] + U2[c - sJ]) + 0.5 * m.c21[d.m3(k, j, 1)] * (U3[c] + U3[c - sJ]);
+  const double u3b = 0.5 * m.c11[d.m3(k, j, 2)] * (U3[c] + U3[c - sK]) + 0.5 * m.c12[d.m3(k, j, 2)] * (U2[c] + U2[c - sK]);
+  if (U2bf) {
+    // only the FP32 flux transforms read the face velocities
+    U2bf[c] = d2f_bits(u2b);
+    U2bf[c + d.nphys()] = d2f_bits(u3b);
+  } else {
+    U2b[c] = u2b;
+    U3b[c] = u3b;
+  }
 }
 
 
@@ -364,7 +387,8 @@ __global__ void k_div_rhs(Dims d, const double *kx, const cplx_t *CU1, const cpl
 // phi back into CR1 (CMPLX(P_TMP2,P_TMP), duct.F90:2662-2666; REAL*4
 // rounding under quirk_phi_fp32), modes above the solved set are zero, and
 // the pressure update CP += CR1/h (duct.F90:2460-2466) when requested.
-__global__ void k_phi_to_cr1(Dims d, const double *phif, int P, cplx_t *CR1, cplx_t *CP, double temp4, int update_p,
+__global__ void k_phi_to_cr1(Dims d, const double *phif, int P, cplx_t *CR1, cplx_t *CP, double temp4, double rtemp4,
+                             int update_p,
                              int fp32) {
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int k = blockIdx.y, j = blockIdx.z;
@@ -383,7 +407,8 @@ __global__ void k_phi_to_cr1(Dims d, const double *phif, int P, cplx_t *CR1, cpl
   CR1[q] = v;
   if (update_p && j >= d.JS - 1 && j <= d.JE + 1 && k >= d.ZS - 1 && k <= d.ZE + 1) {
     const cplx_t o = CP[q];
-    CP[q] = cplx_t{o.re + v.re / temp4, o.im + v.im / temp4};
+    const DivBy div(temp4, rtemp4);
+    CP[q] = cplx_t{o.re + div(v.re), o.im + div(v.im)};
   }
 }
 
@@ -419,14 +444,15 @@ __global__ void k_correct_cells(Dims d, Metrics m, const double *kx, const cplx_
                          cscl(m.c12[d.m3(k, j, 2)], cadd(P(0, 0), P(-1, 0))));
   const cplx_t u2 = cscl(0.5, t2);
   const cplx_t o2 = CU2[q];
-  CU2[q] = cplx_t{o2.re - u2.re / jac, o2.im - u2.im / jac};
+  const DivBy div(jac);
+  CU2[q] = cplx_t{o2.re - div(u2.re), o2.im - div(u2.im)};
   const cplx_t t3 = csub(cadd(csub(cscl(m.c11[d.m3(k + 1, j, 2)], cadd(P(0, 0), P(1, 0))),
                                    cscl(m.c11[d.m3(k, j, 2)], cadd(P(0, 0), P(-1, 0)))),
                               cscl(m.c21[d.m3(k, j + 1, 1)], cadd(P(0, 1), P(0, 0)))),
                          cscl(m.c21[d.m3(k, j, 1)], cadd(P(0, 0), P(0, -1))));
   const cplx_t u3 = cscl(0.5, t3);
   const cplx_t o3 = CU3[q];
-  CU3[q] = cplx_t{o3.re - u3.re / jac, o3.im - u3.im / jac};
+  CU3[q] = cplx_t{o3.re - div(u3.re), o3.im - div(u3.im)};
 }
 
 // Divergence after the projection (duct.F90:2754-2761) into CS.
@@ -560,7 +586,7 @@ void launch_face_velocity(Ctx &c) {
   const Dims &d = c.d;
   dim3 grid((d.NX + 127) / 128, d.ZE - d.ZS + 2, d.JE - d.JS + 2);
   KScope ks(c, KC_FACE, 32.0 * d.NX * (d.ZE - d.ZS + 2) * (d.JE - d.JS + 2));
-  k_face_velocity<<<grid, 128, 0, c.stream>>>(d, c.m, c.U2, c.U3, c.U2b);
+  k_face_velocity<<<grid, 128, 0, c.stream>>>(d, c.m, c.U2, c.U3, c.U2b, c.p.fft_fp32 ? c.U2bf : nullptr);
   after_launch(c);
 }
 
@@ -634,7 +660,8 @@ void launch_projection(Ctx &c, const double *phif, int P, double temp4, bool upd
   dim3 g0((d.NX2P + 1 + 63) / 64, d.NZ2, d.NY2);
   {
   KScope ks(c, KC_PROJECTION, 16.0 * d.nspec() * (1 + 1 + (update_p ? 2 : 0)) + 16.0 * d.nspec() * (5 + 7 + 4));
-  k_phi_to_cr1<<<g0, 64, 0, c.stream>>>(d, phif, P, c.CR1, c.CP, temp4, update_p ? 1 : 0, c.p.quirk_phi_fp32);
+  k_phi_to_cr1<<<g0, 64, 0, c.stream>>>(d, phif, P, c.CR1, c.CP, temp4, 1.0 / temp4, update_p ? 1 : 0,
+                                       c.p.quirk_phi_fp32);
   after_launch(c);
   dim3 g1((d.NX2P + 1 + 63) / 64, d.ZE - d.ZS + 1, d.JE - d.JS + 1);
   k_correct_faces<<<g1, 64, 0, c.stream>>>(d, c.m, c.CR1, c.CU2b);

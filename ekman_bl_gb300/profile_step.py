@@ -1,6 +1,6 @@
 """Run one RK3 step of a named workload for profiling.
 
-    python -m ekman_bl_gb300.profile_step [--workload NAME] [--warmup W] [--tol T]
+    python -m ekman_bl_gb300.profile_step [--workload NAME] [--warmup W] [--tol T] [--mixed]
 
 Sets up the workload, runs W warm-up steps, then exactly one RK3 step, and
 prints the number of kernel launches issued before that step and inside it,
@@ -24,6 +24,8 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-8, help="relative residual; 0 = MUDPACK's own rule")
     ap.add_argument("--timing", action="store_true")
     ap.add_argument("--nx", type=int, default=0, help="override NX (smaller cases for full ncu captures)")
+    ap.add_argument("--mixed", action="store_true",
+                    help="mixed-precision method: mg_fast = 1, fft_fp32 = 1 (needs --tol > 0)")
     args = ap.parse_args()
     ekbuild.build()
     w = WORKLOADS[args.workload]
@@ -34,6 +36,8 @@ def main():
     if args.tol > 0:
         w.mg_tol = args.tol
     p, xp, yp, state = workload_setup(w, stop)
+    if args.mixed:
+        p.mg_fast, p.fft_fp32 = 1, 1
     s = DuctSolver(p, metrics_from_grid(p, xp, yp))
     s.upload(*state)
     s.rem_div_curv()
