@@ -118,6 +118,7 @@ def setup_solver(device_index: int, mg_fast: int = 1, fft_fp32: int = 1):
     p, xp, yp, state = workload_setup(w, EK_MG_STOP_RESIDUAL)
     p.mg_fast = mg_fast
     p.fft_fp32 = fft_fp32
+    p.fft_ff = 1 if fft_fp32 else 0
     solver = DuctSolver(p, metrics_from_grid(p, xp, yp))
     stream = torch.cuda.Stream()
     solver.set_stream(stream.cuda_stream)
@@ -281,9 +282,9 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "nx": p.nx, "ny_plus_2": p.ny + 2, "nz_plus_2": p.nz + 2,
                        "re": w.re, "pr": w.pr, "ri": w.ri, "delta_t": p.delta_t,
                        "method": "batched mixed-precision projection (no learned guess)",
-                       "precision": "fp64 fields and state-carrying transforms; FP32 arithmetic in the "
-                                    "nonlinear-term transforms; Poisson: FP64 residual refinement around FP32 "
-                                    "V-cycles",
+                       "precision": "fp64 fields; state-carrying transforms in float-float (~48-bit) "
+                                    "arithmetic, nonlinear-term transforms in FP32; Poisson: FP64 residual "
+                                    "refinement around FP32 V-cycles",
                        "poisson": f"relative residual {MG_TOL:g} per problem; kx=0 by MUDPACK's rule",
                        "mg_corrections_per_substep_max": mg_cycles,
                        "l2": "fields (100 MB each, ~2.5 GB resident) exceed the 126 MB L2; no flush",

@@ -304,6 +304,7 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
   if (p.sponge_type < 0 || p.sponge_type > 2) return reject("SPONGE_TYPE must be 0, 1 or 2");
   if (p.sponge_type != 0 && p.save_stats_int < 1) return reject("SAVE_STATS_INT must be >= 1 with a sponge");
   if (p.fft_fp32 < 0 || p.fft_fp32 > 2) return reject("fft_fp32 must be 0, 1 or 2");
+  if (p.fft_ff < 0 || p.fft_ff > 1) return reject("fft_ff must be 0 or 1");
   if (p.variable_dt && (p.update_dt < 1 || !(p.cfl > 0.0) || !(p.delta_t_set > 0.0)))
     return reject("VARIABLE_DT needs UPDATE_DT >= 1, CFL > 0 and DELTA_T_SET > 0");
   if (p.sponge_type != 0 && p.ny_s_t <= p.ny && p.ny_s_t < 0) return reject("NY_S_T must be >= 0");
@@ -376,6 +377,23 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
       c.tw_nf = dalloc<float2>(c, fn.size());
       EK_CUDA(cudaMemcpy(c.tw_mf, fm.data(), sizeof(float2) * fm.size(), cudaMemcpyHostToDevice));
       EK_CUDA(cudaMemcpy(c.tw_nf, fn.data(), sizeof(float2) * fn.size(), cudaMemcpyHostToDevice));
+      auto split = [](double x) {
+        const float h = (float)x;
+        return std::make_pair(h, (float)(x - (double)h));
+      };
+      std::vector<float4> gm(twm.size()), gn(twn.size());
+      for (size_t t = 0; t < twm.size(); ++t) {
+        const auto a = split(twm[t].x), b = split(twm[t].y);
+        gm[t] = make_float4(a.first, a.second, b.first, b.second);
+      }
+      for (size_t t = 0; t < twn.size(); ++t) {
+        const auto a = split(twn[t].x), b = split(twn[t].y);
+        gn[t] = make_float4(a.first, a.second, b.first, b.second);
+      }
+      c.tw_mff = dalloc<float4>(c, gm.size());
+      c.tw_nff = dalloc<float4>(c, gn.size());
+      EK_CUDA(cudaMemcpy(c.tw_mff, gm.data(), sizeof(float4) * gm.size(), cudaMemcpyHostToDevice));
+      EK_CUDA(cudaMemcpy(c.tw_nff, gn.data(), sizeof(float4) * gn.size(), cudaMemcpyHostToDevice));
     }
     // fields
     const size_t nc = d.nspec(), np = d.nphys();

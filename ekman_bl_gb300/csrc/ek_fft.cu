@@ -34,12 +34,49 @@ struct FftConst {
   int M, logM;
   const double2 *tw_m, *tw_n;
   const float2 *tw_mf, *tw_nf;  // the same tables rounded to FP32
+  const float4 *tw_mff, *tw_nff;  // and split into float-float (re.hi, re.lo, im.hi, im.lo)
   const double *kx;
   Metrics m;
 };
 
-// T: the arithmetic type of a transform (double, or float with the fields
-// still stored in FP64); V: its complex pair.
+// Float-float: an unevaluated sum hi + lo of two floats (about 48
+// significant bits), with the error-free sum (Knuth's TwoSum) and the
+// FMA-based product.  The _rn intrinsics keep the compiler from fusing or
+// reassociating the steps.  On GB300 this runs on the FP32 pipe, ~60x
+// wider than the FP64 one, at roughly ten FP32 instructions per FP64 one.
+struct FF {
+  float hi, lo;
+  FF() = default;
+  __device__ FF(float h, float l) : hi(h), lo(l) {}
+  __device__ explicit FF(double x) {
+    hi = d2f_bits(x);
+    lo = d2f_bits(x - f2d_bits(hi));
+  }
+  __device__ explicit operator double() const { return f2d_bits(hi) + f2d_bits(lo); }
+};
+__device__ __forceinline__ FF ff_norm(float s, float e) {
+  const float h = __fadd_rn(s, e);
+  return FF(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ FF operator+(FF a, FF b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  return ff_norm(s, e);
+}
+__device__ __forceinline__ FF operator-(FF a) { return FF(-a.hi, -a.lo); }
+__device__ __forceinline__ FF operator-(FF a, FF b) { return a + (-b); }
+__device__ __forceinline__ FF operator*(FF a, FF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return ff_norm(p, e);
+}
+
+// T: the arithmetic type of a transform (double; float with the fields still
+// stored in FP64; or FF); V: its complex pair.
 template <typename T> struct Cx;
 template <> struct Cx<double> {
   using V = double2;
@@ -49,12 +86,25 @@ template <> struct Cx<float> {
   using V = float2;
   __device__ static V make(float x, float y) { return make_float2(x, y); }
 };
+struct FF2 {
+  FF x, y;
+};
+template <> struct Cx<FF> {
+  using V = FF2;
+  __device__ static V make(FF x, FF y) { return FF2{x, y}; }
+};
 template <typename T> __device__ __forceinline__ const typename Cx<T>::V *tw_m(const FftConst &f);
 template <> __device__ __forceinline__ const double2 *tw_m<double>(const FftConst &f) { return f.tw_m; }
 template <> __device__ __forceinline__ const float2 *tw_m<float>(const FftConst &f) { return f.tw_mf; }
+template <> __device__ __forceinline__ const FF2 *tw_m<FF>(const FftConst &f) {
+  return reinterpret_cast<const FF2 *>(f.tw_mff);
+}
 template <typename T> __device__ __forceinline__ const typename Cx<T>::V *tw_n(const FftConst &f);
 template <> __device__ __forceinline__ const double2 *tw_n<double>(const FftConst &f) { return f.tw_n; }
 template <> __device__ __forceinline__ const float2 *tw_n<float>(const FftConst &f) { return f.tw_nf; }
+template <> __device__ __forceinline__ const FF2 *tw_n<FF>(const FftConst &f) {
+  return reinterpret_cast<const FF2 *>(f.tw_nff);
+}
 
 template <typename V>
 __device__ __forceinline__ V cmul(V a, V b) {
@@ -118,7 +168,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
   } else if (args.pro == PRO_PROD) {
     const T jac = (T)fc.m.jac[d.m2(k, j)];
     if (fin)
-      for (int n = lane; n < NX; n += 32) zr[n] = jac * (T)args.af[base + n] * (T)args.bf[base + n];
+      for (int n = lane; n < NX; n += 32) zr[n] = jac * (T)(double)args.af[base + n] * (T)(double)args.bf[base + n];
     else
       for (int n = lane; n < NX; n += 32) zr[n] = jac * (T)args.a[base + n] * (T)args.b[base + n];
   } else if (fin) {
@@ -131,10 +181,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
     const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
     for (int n = lane; n < NX; n += 32) {
       const size_t c = base + n;
-      const T f = F[c], fkp = F[c + sK], fkm = F[c - sK], fjp = F[c + sJ], fjm = F[c - sJ];
-      const T fpp = F[c + sK + sJ], fpm = F[c + sK - sJ], fmp = F[c - sK + sJ], fmm = F[c - sK - sJ];
-      T s1 = h * (T)U2b[c + sJ] * (f + fjp) - h * (T)U2b[c] * (f + fjm);
-      T s2 = h * (T)U3b[c + sK] * (f + fkp) - h * (T)U3b[c] * (f + fkm);
+      const T f = (T)(double)F[c], fkp = (T)(double)F[c + sK], fkm = (T)(double)F[c - sK];
+      const T fjp = (T)(double)F[c + sJ], fjm = (T)(double)F[c - sJ];
+      const T fpp = (T)(double)F[c + sK + sJ], fpm = (T)(double)F[c + sK - sJ];
+      const T fmp = (T)(double)F[c - sK + sJ], fmm = (T)(double)F[c - sK - sJ];
+      T s1 = h * (T)(double)U2b[c + sJ] * (f + fjp) - h * (T)(double)U2b[c] * (f + fjm);
+      T s2 = h * (T)(double)U3b[c + sK] * (f + fkp) - h * (T)(double)U3b[c] * (f + fkm);
       s1 = -s1 + qv * (g12a * (fpp + fjp - fjm - fpm) - g12b * (fmp + fjp - fjm - fmm));
       s2 = -s2 + qv * (g12c * (fpp + fkp - fmp - fkm) - g12d * (fkp + fpm - fkm - fmm));
       zr[n] = s1 + s2;
@@ -181,7 +233,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
     const V w = twn[kk];
     const T tr = (er + (w.x * orr - w.y * oi)) * inv;
     const T ti = (ei + (w.x * oi + w.y * orr)) * inv;
-    if (kF) {
+    if constexpr (kF) {
       // the FP32 result enters the FP64 field with one exact widening and
       // one FP64 add per component
       const cplx_t o = (args.epi == EPI_STORE) ? cplx_t{0.0, 0.0} : dst[kk];
@@ -194,7 +246,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
         dst[kk] = cplx_t{o.re - f2d_bits((float)(T(0) * tr - kv * ti)), o.im - f2d_bits((float)(T(0) * ti + kv * tr))};
       }
       continue;
-    }
+    } else {
     const double xr = (double)tr, xi = (double)ti;
     if (args.epi == EPI_STORE) {
       dst[kk] = cplx_t{xr, xi};
@@ -206,6 +258,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
       const double kv = fc.kx[kk];
       const cplx_t o = dst[kk];
       dst[kk] = cplx_t{o.re - (0.0 * xr - kv * xi), o.im - (0.0 * xi + kv * xr)};
+    }
     }
   }
 }
@@ -228,7 +281,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
   const cplx_t *src = args.src + d.ic(0, k, j);
   const cplx_t *src2 = args.src2 ? args.src2 + d.ic(0, k, j) : nullptr;
   auto X = [&](int kk) -> V {
-    if (kk > NKX || kk >= M) return Cx<T>::make(0, 0);
+    if (kk > NKX || kk >= M) return Cx<T>::make(T(0.0), T(0.0));
     cplx_t v = src[kk];
     if (src2) {
       const cplx_t w = src2[kk];
@@ -255,12 +308,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
   float *dstf = args.dstf ? args.dstf + d.ip(0, k, j) : nullptr;
   const int NX = d.NX;
   for (int n = lane; n < NX + 2; n += 32) {
-    T v = T(0);
+    T v = T(0.0);
     if (n < NX) {
       const int m = n >> 1;
       v = zr[2 * brev(m, fc.logM) + (n & 1)];
     }
-    if (sizeof(T) == 4) {
+    if constexpr (sizeof(T) == 4) {
       dst[n] = f2d_bits((float)v);
       if (dstf) dstf[n] = (float)v;
     } else {
@@ -281,6 +334,8 @@ FftConst make_const(Ctx &c) {
   f.tw_n = c.tw_n;
   f.tw_mf = c.tw_mf;
   f.tw_nf = c.tw_nf;
+  f.tw_mff = c.tw_mff;
+  f.tw_nff = c.tw_nff;
   f.kx = c.kx;
   f.m = c.m;
   return f;
@@ -292,6 +347,8 @@ FftConst make_const(Ctx &c) {
 // marked low-precision (the nonlinear products and fluxes, whose results
 // enter the step multiplied by the time step); 2: every transform.
 bool fft_lowp(const Ctx &c, int lowp) { return c.p.fft_fp32 >= 2 || (c.p.fft_fp32 == 1 && lowp); }
+// float-float for the other transforms under fft_ff
+bool fft_ff(const Ctx &c, int lowp) { return c.p.fft_ff && !fft_lowp(c, lowp); }
 
 void launch_r2c(Ctx &c, const R2cArgs &a) {
   const FftConst fc = make_const(c);
@@ -303,6 +360,7 @@ void launch_r2c(Ctx &c, const R2cArgs &a) {
   const double epi = (a.epi == EPI_STORE) ? 16.0 * (c.d.NX2P + 1) : 32.0 * (c.d.NKX + 1);
   KScope ks(c, KC_R2C, nlines * (8.0 * c.d.NX * nops + epi));
   if (fft_lowp(c, a.lowp)) k_r2c<float><<<grid, 32 * kWarpsPerBlock, smem / 2, c.stream>>>(fc, a);
+  else if (fft_ff(c, a.lowp)) k_r2c<FF><<<grid, 32 * kWarpsPerBlock, smem, c.stream>>>(fc, a);
   else k_r2c<double><<<grid, 32 * kWarpsPerBlock, smem, c.stream>>>(fc, a);
   after_launch(c);
 }
@@ -315,6 +373,7 @@ void launch_c2r(Ctx &c, const C2rArgs &a) {
   const size_t smem = sizeof(double2) * fc.M * kWarpsPerBlock;
   KScope ks(c, KC_C2R, nlines * (16.0 * (c.d.NKX + 1) * (a.src2 ? 2 : 1) + 8.0 * (c.d.NX + 2)));
   if (fft_lowp(c, a.lowp)) k_c2r<float><<<grid, 32 * kWarpsPerBlock, smem / 2, c.stream>>>(fc, a);
+  else if (fft_ff(c, a.lowp)) k_c2r<FF><<<grid, 32 * kWarpsPerBlock, smem, c.stream>>>(fc, a);
   else k_c2r<double><<<grid, 32 * kWarpsPerBlock, smem, c.stream>>>(fc, a);
   after_launch(c);
 }
@@ -329,6 +388,8 @@ void fft_init_attributes() {
   EK_CUDA(cudaFuncSetAttribute(k_c2r<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
   EK_CUDA(cudaFuncSetAttribute(k_r2c<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
   EK_CUDA(cudaFuncSetAttribute(k_c2r<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+  EK_CUDA(cudaFuncSetAttribute(k_r2c<FF>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+  EK_CUDA(cudaFuncSetAttribute(k_c2r<FF>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
   done = true;
 }
 }  // namespace ek

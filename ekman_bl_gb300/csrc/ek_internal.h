@@ -200,6 +200,7 @@ struct Ctx {
   double2 *tw_m = nullptr;  // exp(-2 pi i t/M), t < M/2   (M = NX/2)
   double2 *tw_n = nullptr;  // exp(-2 pi i k/NX), k <= M
   float2 *tw_mf = nullptr, *tw_nf = nullptr;  // the same, rounded to FP32
+  float4 *tw_mff = nullptr, *tw_nff = nullptr;  // and as float-float pairs
   Metrics m{};
   // spectral fields (complex)
   cplx_t *CU1, *CU2, *CU3, *CP, *CTH, *CF1, *CF2, *CF3, *CFTH, *CR1, *CR2, *CR3, *CRTH, *CS, *CU2b, *CU3b;

@@ -199,7 +199,8 @@ def test_mixed_precision_steps_track_oracle():
 
 def test_mixed_path_hundred_steps_neutral_64():
     """The mixed-precision path (FP32 V-cycles inside FP64 refinement at
-    1e-10, FP32 arithmetic in the nonlinear-term transforms) against the
+    1e-10, FP32 arithmetic in the nonlinear-term transforms, float-float in
+    the others) against the
     FP64 oracle after 100 steps of the 64 x 65 x 65 case: velocity and
     buoyancy within 1e-5 relative L2, divergence below 1e-8."""
     w = WORKLOADS["ekman_neutral_64x65x65"]
@@ -207,7 +208,7 @@ def test_mixed_path_hundred_steps_neutral_64():
     p.mg_tol, p.mg_maxcy = 1e-10, 200
     o = ekref.Oracle(p, ekref.metrics_from_grid(p, xp, yp))
     q = workload_setup(w, EK_MG_STOP_RESIDUAL)[0]
-    q.mg_tol, q.mg_maxcy, q.mg_fast, q.fft_fp32 = 1e-10, 60, 1, 1
+    q.mg_tol, q.mg_maxcy, q.mg_fast, q.fft_fp32, q.fft_ff = 1e-10, 60, 1, 1, 1
     g = DuctSolver(q, metrics_from_grid(q, xp, yp))
     g.upload(*st)
     o.upload(*st)
@@ -219,3 +220,22 @@ def test_mixed_path_hundred_steps_neutral_64():
     for name, x, y in zip(("CU1", "CU2", "CU3", "CTH"), (a[0], a[1], a[2], a[4]), (b[0], b[1], b[2], b[4])):
         assert rel_l2(x, y) < 1e-5, name
     assert g.divergence() < 1e-8
+
+
+def test_float_float_transforms_hundred_steps():
+    """fft_ff = 1 on the FP64 path: the transforms in float-float arithmetic
+    stay within 1e-10 of the FP64 oracle after 100 steps (measured ~1e-12)."""
+    w = WORKLOADS["ekman_neutral_64x65x65"]
+    p, xp, yp, st = workload_setup(w)
+    o = ekref.Oracle(p, ekref.metrics_from_grid(p, xp, yp))
+    q = workload_setup(w)[0]
+    q.fft_ff = 1
+    g = DuctSolver(q, metrics_from_grid(q, xp, yp))
+    g.upload(*st)
+    o.upload(*st)
+    g.rem_div_curv()
+    o.rem_div()
+    g.step(100)
+    o.step(100)
+    for name, x, y in zip(("CU1", "CU2", "CU3", "CP", "CTH"), g.download(), o.download()):
+        assert rel_l2(x, y) < 1e-10, name
