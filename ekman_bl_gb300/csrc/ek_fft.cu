@@ -39,42 +39,6 @@ struct FftConst {
   Metrics m;
 };
 
-// Float-float: an unevaluated sum hi + lo of two floats (about 48
-// significant bits), with the error-free sum (Knuth's TwoSum) and the
-// FMA-based product.  The _rn intrinsics keep the compiler from fusing or
-// reassociating the steps.  On GB300 this runs on the FP32 pipe, ~60x
-// wider than the FP64 one, at roughly ten FP32 instructions per FP64 one.
-struct FF {
-  float hi, lo;
-  FF() = default;
-  __device__ FF(float h, float l) : hi(h), lo(l) {}
-  __device__ explicit FF(double x) {
-    hi = d2f_bits(x);
-    lo = d2f_bits(x - f2d_bits(hi));
-  }
-  __device__ explicit operator double() const { return f2d_bits(hi) + f2d_bits(lo); }
-};
-__device__ __forceinline__ FF ff_norm(float s, float e) {
-  const float h = __fadd_rn(s, e);
-  return FF(h, __fsub_rn(e, __fsub_rn(h, s)));
-}
-__device__ __forceinline__ FF operator+(FF a, FF b) {
-  const float s = __fadd_rn(a.hi, b.hi);
-  const float bb = __fsub_rn(s, a.hi);
-  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
-  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
-  return ff_norm(s, e);
-}
-__device__ __forceinline__ FF operator-(FF a) { return FF(-a.hi, -a.lo); }
-__device__ __forceinline__ FF operator-(FF a, FF b) { return a + (-b); }
-__device__ __forceinline__ FF operator*(FF a, FF b) {
-  const float p = __fmul_rn(a.hi, b.hi);
-  float e = __fmaf_rn(a.hi, b.hi, -p);
-  e = __fmaf_rn(a.hi, b.lo, e);
-  e = __fmaf_rn(a.lo, b.hi, e);
-  return ff_norm(p, e);
-}
-
 // T: the arithmetic type of a transform (double; float with the fields still
 // stored in FP64; or FF); V: its complex pair.
 template <typename T> struct Cx;

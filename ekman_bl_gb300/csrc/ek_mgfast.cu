@@ -3,15 +3,16 @@
 // Same discrete operator as the MUDPACK-exact path (dismd2cr's 9-point
 // coefficients, periodic x with MUDPACK's ghost columns, Neumann y), a
 // different iteration: FP64 iterative refinement around FP32 V-cycles.
-//   r = b - A phi            FP64, with ||r||, ||b|| per problem
+//   r = b - A phi            float-float (~48 bits, FP32 pipe), ||r||, ||b||
 //   stop if ||r|| <= tol ||b||
 //   A e = r                  one FP32 V(1,1) cycle from e = 0 on MUDPACK's
 //                            coarse-level operators, alternating-direction
 //                            zebra line Gauss-Seidel smoother, MUDPACK's
 //                            full-weighting restriction and cubic prolongation
-//   phi = phi + e            FP64
-// GB300 runs FP32 at ~30x its FP64 rate, so only the residual and the update
-// stay on the FP64 pipe.  On a grid stretched in y the strong coupling is
+//   phi = phi + e            float-float; phi is widened to FP64 at the end
+// GB300 runs FP32 at ~60x its FP64 rate; with float-float refinement the
+// solve never touches the FP64 pipe beyond splitting the rhs and widening
+// the result, and reaches relative residuals down to ~1e-13.  On a grid stretched in y the strong coupling is
 // along y near the wall and along x far from it; line relaxation in both
 // directions smooths both regions, so each cycle cuts the residual ~10x
 // where MUDPACK's point smoother (W-cycles) gets ~1.3x.
@@ -37,11 +38,14 @@ struct FastDev {
   int P, ngrid, orth;
   LvF lv[24];
   float *scr;              // finest-size scratch x P (residual / correction)
-  double *phi, *rhs, *cof;  // FP64 finest: phi with ghosts, rhs, coefficients
+  double *rhs;              // FP64 finest rhs
+  float *phh, *phl;         // float-float finest iterate, with ghosts
+  float *bh, *bl;           // float-float finest rhs
+  const float *cfh, *cfl;   // float-float finest coefficients
   int nfx, nfy;
   const double *kx2;
   double *phif;            // output (finest interior, problem fastest)
-  double *red;             // 6 per problem: |b|^2, |r|^2, max|e|, max|phi|, meas
+  double *red;             // 6 per problem: |b|^2, |r|^2, two unused, meas
   int *done, *cycles, *alldone;
   double tol;
 };
@@ -49,63 +53,70 @@ struct FastDev {
 __device__ __forceinline__ float &E(const LvF &L, int P, int i, int j, int p) {
   return L.e[((size_t)j * (L.nx + 2) + i) * P + p];
 }
-__device__ __forceinline__ void atomic_max_pos(double *a, double v) {
-  atomicMax(reinterpret_cast<unsigned long long *>(a), (unsigned long long)__double_as_longlong(v));
-}
 
-// r = b - A phi at the finest level in FP64; r32 = r; e_finest = 0;
-// per-problem |b|^2 and |r|^2 (block partials, one atomic per block).
+// r = b - A phi at the finest level in float-float (about 48 bits, on the
+// FP32 pipe); r32 = r; e_finest = 0 (ghosts included); per-problem |b|^2 and
+// |r|^2.  Block row jr = j for j = 0..ny+1, lanes over 32 problems.
 constexpr int kRY = 8;
-__global__ void __launch_bounds__(32 * kRY) k_f_resid64(FastDev g) {
+__global__ void __launch_bounds__(32 * kRY) k_f_resid_ff(FastDev g) {
   if (*g.alldone) return;
   const int P = g.P;
   const int p = blockIdx.x * 32 + threadIdx.x;
   const int ty = threadIdx.y;
-  const int nx = g.nfx, ny = g.nfy;
+  const int nx = g.nfx, ny = g.nfy, j = (int)blockIdx.y;
   const size_t npt = (size_t)nx * ny;
   const LvF &F = g.lv[g.ngrid - 1];
-  double sb = 0.0, sr = 0.0;
+  float sb = 0.f, sr = 0.f;
   const bool act = (p < P) && !g.done[p];
   if (act) {
-    const size_t si = P, sj = (size_t)(nx + 2) * P;
-    const double kx2 = g.kx2[p];
-    const double *cf = g.cof;
-    for (size_t pt = (size_t)blockIdx.y * kRY + ty; pt < npt; pt += (size_t)gridDim.y * kRY) {
-      const int i = 1 + (int)(pt % nx), j = 1 + (int)(pt / nx);
-      const double *ph = g.phi + ((size_t)j * (nx + 2) + i) * P + p;
-      double s = cf[pt] * ph[si];
-      if (!g.orth) s = s + cf[npt + pt] * ph[si + sj];
-      s = s + cf[2 * npt + pt] * ph[sj];
-      if (!g.orth) s = s + cf[3 * npt + pt] * ph[sj - si];
-      s = s + cf[4 * npt + pt] * ph[-(long)si];
-      if (!g.orth) s = s + cf[5 * npt + pt] * ph[-(long)(si + sj)];
-      s = s + cf[6 * npt + pt] * ph[-(long)sj];
-      if (!g.orth) s = s + cf[7 * npt + pt] * ph[si - sj];
-      const double c9 = ((-kx2 * cf[10 * npt + pt]) - cf[8 * npt + pt]) + cf[9 * npt + pt];
-      s = s + c9 * ph[0];
-      const double b = g.rhs[pt * P + p];
-      const double r = b - s;
-      sb += b * b;
-      sr += r * r;
-      F.r[pt * P + p] = (float)r;
+    for (int i = ty; i <= nx + 1; i += kRY) F.e[((size_t)j * (nx + 2) + i) * P + p] = 0.f;
+    if (j >= 1 && j <= ny) {
+      const size_t si = P, sj = (size_t)(nx + 2) * P;
+      const FF kx2(g.kx2[p]);
+      for (int i = 1 + ty; i <= nx; i += kRY) {
+        const size_t pt = (size_t)(j - 1) * nx + (i - 1);
+        const size_t q = ((size_t)j * (nx + 2) + i) * P + p;
+        auto PH = [&](long o) { return FF(g.phh[q + o], g.phl[q + o]); };
+        auto CF = [&](int l) { return FF(g.cfh[l * npt + pt], g.cfl[l * npt + pt]); };
+        FF s = CF(0) * PH((long)si);
+        if (!g.orth) s = s + CF(1) * PH((long)(si + sj));
+        s = s + CF(2) * PH((long)sj);
+        if (!g.orth) s = s + CF(3) * PH((long)sj - (long)si);
+        s = s + CF(4) * PH(-(long)si);
+        if (!g.orth) s = s + CF(5) * PH(-(long)(si + sj));
+        s = s + CF(6) * PH(-(long)sj);
+        if (!g.orth) s = s + CF(7) * PH((long)si - (long)sj);
+        const FF c9 = ((-kx2 * CF(10)) - CF(8)) + CF(9);
+        s = s + c9 * PH(0);
+        const FF b(g.bh[pt * P + p], g.bl[pt * P + p]);
+        const FF r = b - s;
+        const float r32 = __fadd_rn(r.hi, r.lo);
+        sb = fmaf(b.hi, b.hi, sb);
+        sr = fmaf(r32, r32, sr);
+        F.r[pt * P + p] = r32;
+      }
     }
   }
-  // zero the finest correction (with ghosts)
-  if (p < P) {
-    const size_t nph = (size_t)(nx + 2) * (ny + 2);
-    for (size_t q = (size_t)blockIdx.y * kRY + ty; q < nph; q += (size_t)gridDim.y * kRY) F.e[q * P + p] = 0.f;
-  }
-  __shared__ double red[2][kRY][32];
+  __shared__ float red[2][kRY][32];
   red[0][ty][threadIdx.x] = sb;
   red[1][ty][threadIdx.x] = sr;
   __syncthreads();
-  if (ty == 0 && act) {
+  if (ty == 0 && act && j >= 1 && j <= ny) {
     for (int y = 1; y < kRY; ++y) {
       sb += red[0][y][threadIdx.x];
       sr += red[1][y][threadIdx.x];
     }
-    atomicAdd(&g.red[6 * p], sb);
-    atomicAdd(&g.red[6 * p + 1], sr);
+    atomicAdd(&g.red[6 * p], (double)sb);
+    atomicAdd(&g.red[6 * p + 1], (double)sr);
+  }
+}
+
+// float-float rhs from the FP64 one (once per solve)
+__global__ void k_f_split(const double *b, float *bh, float *bl, size_t n) {
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const FF v(b[t]);
+    bh[t] = v.hi;
+    bl[t] = v.lo;
   }
 }
 
@@ -497,28 +508,32 @@ __global__ void k_f_coarsest(FastDev g, int sweeps) {
   }
 }
 
+// The elementwise multigrid kernels below use one block per grid row (or
+// coarse row) and 32 problems: lanes over the problems (coalesced, the
+// layout is problem fastest), the block's warps striding along the row.  No
+// index needs a division.
+constexpr int kRowWarps = 8;
+
 // residual of the correction equation at a level (FP32) into the scratch
-__global__ void k_f_resid32(FastDev g, int level) {
+__global__ void __launch_bounds__(32 * kRowWarps) k_f_resid32(FastDev g, int level) {
   if (*g.alldone) return;
   const LvF L = g.lv[level - 1];
   const int P = g.P;
-  const int nx = L.nx;
+  const int p = blockIdx.x * 32 + threadIdx.x;
+  if (p >= P || g.done[p]) return;
+  const int nx = L.nx, j = 1 + (int)blockIdx.y;
   const size_t npt = (size_t)nx * L.ny;
   const size_t si = P, sj = (size_t)(nx + 2) * P;
-  const long n = (long)npt * P;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-    const int p = (int)(t % P);
-    if (g.done[p]) continue;
-    const long pt = t / P;
-    const int i = 1 + (int)(pt % nx), j = 1 + (int)(pt / nx);
+  const float kx2 = (float)g.kx2[p];
+  const float *cf = L.cof;
+  for (int i = 1 + (int)threadIdx.y; i <= nx; i += kRowWarps) {
+    const size_t pt = (size_t)(j - 1) * nx + (i - 1);
     const float *ep = &L.e[((size_t)j * (nx + 2) + i) * P + p];
-    const float *cf = L.cof;
     float s = cf[pt] * ep[si] + cf[2 * npt + pt] * ep[sj] + cf[4 * npt + pt] * ep[-(long)si] +
               cf[6 * npt + pt] * ep[-(long)sj];
     if (!g.orth)
       s += cf[npt + pt] * ep[si + sj] + cf[3 * npt + pt] * ep[sj - si] + cf[5 * npt + pt] * ep[-(long)(si + sj)] +
            cf[7 * npt + pt] * ep[si - sj];
-    const float kx2 = (float)g.kx2[p];
     const float c9 = ((-kx2 * cf[10 * npt + pt]) - cf[8 * npt + pt]) + cf[9 * npt + pt];
     s += c9 * ep[0];
     g.scr[((size_t)j * (nx + 2) + i) * P + p] = L.r[pt * P + p] - s;
@@ -526,19 +541,18 @@ __global__ void k_f_resid32(FastDev g, int level) {
 }
 
 // full weighting (res2, mudcom.f:120-257) to the coarse rhs; e_coarse = 0
-__global__ void k_f_restrict(FastDev g, int level) {
+// (block row jc = 0..ncy+1, ghosts included)
+__global__ void __launch_bounds__(32 * kRowWarps) k_f_restrict(FastDev g, int level) {
   if (*g.alldone) return;
   const LvF F = g.lv[level - 1], C = g.lv[level - 2];
   const int P = g.P;
+  const int p = blockIdx.x * 32 + threadIdx.x;
+  if (p >= P || g.done[p]) return;
   const int nx = F.nx, ny = F.ny, ncx = C.nx, ncy = C.ny;
   const int ix = (ncx == nx) ? 0 : 1, jy = (ncy == ny) ? 0 : 1;
-  const long n = (long)(ncx + 2) * (ncy + 2) * P;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-    const int p = (int)(t % P);
-    if (g.done[p]) continue;
-    const long q = t / P;
-    const int ic = (int)(q % (ncx + 2)), jc = (int)(q / (ncx + 2));
-    C.e[q * P + p] = 0.f;
+  const int jc = (int)blockIdx.y;
+  for (int ic = (int)threadIdx.y; ic <= ncx + 1; ic += kRowWarps) {
+    C.e[((size_t)jc * (ncx + 2) + ic) * P + p] = 0.f;
     if (ic < 1 || ic > ncx || jc < 1 || jc > ncy) continue;
     const int i = ic + ix * (ic - 1), j = jc + jy * (jc - 1);
     int im1 = i - 1, ip1 = i + 1, jm1 = j - 1, jp1 = j + 1;
@@ -575,42 +589,38 @@ __device__ __forceinline__ float prolon1f(int i, int ncx, int nx, bool cubic, F 
   return (-q(nx - 4) + 9.f * (q(nx - 2) + q(nx)) - q(3)) * .0625f;
 }
 
-__global__ void k_f_prolong_x(FastDev g, int level) {
+// block row rr: fine row j = 2 rr + 1 (y coarsened) or rr + 1
+__global__ void __launch_bounds__(32 * kRowWarps) k_f_prolong_x(FastDev g, int level) {
   if (*g.alldone) return;
   const LvF F = g.lv[level - 1], C = g.lv[level - 2];
   const int P = g.P;
+  const int p = blockIdx.x * 32 + threadIdx.x;
+  if (p >= P || g.done[p]) return;
   const int nx = F.nx, ny = F.ny, ncx = C.nx, ncy = C.ny;
   const bool ycoarse = ncy < ny;
   const bool cubic = ncx >= 4;
-  const int nrows = ycoarse ? (ny + 1) / 2 : ny;
-  const long n = (long)nrows * nx * P;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-    const int p = (int)(t % P);
-    if (g.done[p]) continue;
-    const long q = t / P;
-    const int i = 1 + (int)(q % nx), rr = (int)(q / nx);
-    const int j = ycoarse ? 2 * rr + 1 : rr + 1;
-    const int jc = ycoarse ? j / 2 + 1 : j;
-    auto pc = [&](int ic) { return C.e[((size_t)jc * (ncx + 2) + ic) * P + p]; };
+  const int rr = (int)blockIdx.y;
+  const int j = ycoarse ? 2 * rr + 1 : rr + 1;
+  const int jc = ycoarse ? j / 2 + 1 : j;
+  auto pc = [&](int ic) { return C.e[((size_t)jc * (ncx + 2) + ic) * P + p]; };
+  for (int i = 1 + (int)threadIdx.y; i <= nx; i += kRowWarps)
     g.scr[((size_t)j * (nx + 2) + i) * P + p] = prolon1f(i, ncx, nx, cubic, pc);
-  }
 }
 
 // stage 2: the rows between (cubic or linear in y), then e += correction,
-// with the periodic ghosts written together with their sources
-__global__ void k_f_prolong_y(FastDev g, int level) {
+// with the periodic ghosts written together with their sources (block row
+// j - 1)
+__global__ void __launch_bounds__(32 * kRowWarps) k_f_prolong_y(FastDev g, int level) {
   if (*g.alldone) return;
   const LvF F = g.lv[level - 1], C = g.lv[level - 2];
   const int P = g.P;
+  const int p = blockIdx.x * 32 + threadIdx.x;
+  if (p >= P || g.done[p]) return;
   const int nx = F.nx, ny = F.ny, ncy = C.ny;
   const bool ycoarse = ncy < ny;
   const bool cubic = ncy >= 4;
-  const long n = (long)nx * ny * P;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-    const int p = (int)(t % P);
-    if (g.done[p]) continue;
-    const long q = t / P;
-    const int i = 1 + (int)(q % nx), j = 1 + (int)(q / nx);
+  const int j = 1 + (int)blockIdx.y;
+  for (int i = 1 + (int)threadIdx.y; i <= nx; i += kRowWarps) {
     auto Q = [&](int jj) { return g.scr[((size_t)jj * (nx + 2) + i) * P + p]; };
     float v;
     if (ycoarse && !(j & 1)) {
@@ -629,49 +639,44 @@ __global__ void k_f_prolong_y(FastDev g, int level) {
   }
 }
 
-// phi += e at the finest level (FP64), periodic ghosts of phi, and the
-// per-problem max|e| and max|phi| for the singular mode's test.
-__global__ void __launch_bounds__(32 * kRY) k_f_update(FastDev g) {
+// phi += e at the finest level in float-float, with the periodic ghosts of
+// phi (block row j - 1, lanes over 32 problems).
+__global__ void __launch_bounds__(32 * kRY) k_f_update_ff(FastDev g) {
   if (*g.alldone) return;
   const int P = g.P;
   const int p = blockIdx.x * 32 + threadIdx.x;
-  const int ty = threadIdx.y;
-  const int nx = g.nfx, ny = g.nfy;
-  const size_t npt = (size_t)nx * ny;
+  if (p >= P || g.done[p]) return;
+  const int nx = g.nfx, j = 1 + (int)blockIdx.y;
   const LvF &F = g.lv[g.ngrid - 1];
-  double me = 0.0, mp = 0.0;
-  const bool act = (p < P) && !g.done[p];
-  if (act) {
-    for (size_t pt = (size_t)blockIdx.y * kRY + ty; pt < npt; pt += (size_t)gridDim.y * kRY) {
-      const int i = 1 + (int)(pt % nx), j = 1 + (int)(pt / nx);
-      const double e = (double)E(F, P, i, j, p);
-      double *ph = g.phi + ((size_t)j * (nx + 2) + i) * P + p;
-      const double v = *ph + e;
-      *ph = v;
-      g.phif[pt * P + p] = v;
-      if (i == nx - 1) g.phi[((size_t)j * (nx + 2) + 0) * P + p] = v;
-      if (i == 2) g.phi[((size_t)j * (nx + 2) + nx + 1) * P + p] = v;
-      me = fmax(me, fabs(e));
-      mp = fmax(mp, fabs(v));
+  for (int i = 1 + (int)threadIdx.y; i <= nx; i += kRY) {
+    const size_t q = ((size_t)j * (nx + 2) + i) * P + p;
+    const FF v = FF(g.phh[q], g.phl[q]) + FF(E(F, P, i, j, p), 0.f);
+    g.phh[q] = v.hi;
+    g.phl[q] = v.lo;
+    if (i == nx - 1) {
+      g.phh[((size_t)j * (nx + 2)) * P + p] = v.hi;
+      g.phl[((size_t)j * (nx + 2)) * P + p] = v.lo;
     }
-  }
-  __shared__ double red[2][kRY][32];
-  red[0][ty][threadIdx.x] = me;
-  red[1][ty][threadIdx.x] = mp;
-  __syncthreads();
-  if (ty == 0 && act) {
-    for (int y = 1; y < kRY; ++y) {
-      me = fmax(me, red[0][y][threadIdx.x]);
-      mp = fmax(mp, red[1][y][threadIdx.x]);
+    if (i == 2) {
+      g.phh[((size_t)j * (nx + 2) + nx + 1) * P + p] = v.hi;
+      g.phl[((size_t)j * (nx + 2) + nx + 1) * P + p] = v.lo;
     }
-    atomic_max_pos(&g.red[6 * p + 2], me);
-    atomic_max_pos(&g.red[6 * p + 3], mp);
   }
 }
 
-__global__ void k_f_zero64(double *a, size_t n) {
-  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) a[t] = 0.0;
+// the FP64 solution (finest interior, problem fastest) from the float-float
+// iterate, after the last correction
+__global__ void __launch_bounds__(32 * kRY) k_f_phif(FastDev g) {
+  const int P = g.P;
+  const int p = blockIdx.x * 32 + threadIdx.x;
+  if (p >= P) return;
+  const int nx = g.nfx, j = 1 + (int)blockIdx.y;
+  for (int i = 1 + (int)threadIdx.y; i <= nx; i += kRY) {
+    const size_t q = ((size_t)j * (nx + 2) + i) * P + p;
+    g.phif[((size_t)(j - 1) * nx + (i - 1)) * P + p] = (double)FF(g.phh[q], g.phl[q]);
+  }
 }
+
 
 unsigned nb(long n, int bs) {
   long b = (n + bs - 1) / bs;
@@ -697,7 +702,10 @@ void mgfast_alloc(Ctx &c, int pmax) {
     tot += (size_t)(L.nx + 2) * (L.ny + 2) * pmax + 2 * (size_t)L.nx * L.ny * pmax + 11 * (size_t)L.nx * L.ny;
   }
   const size_t scr_off = tot;
-  tot += (size_t)(PL.nfx + 2) * (PL.nfy + 2) * pmax;
+  const size_t nph = (size_t)(PL.nfx + 2) * (PL.nfy + 2), nf = (size_t)PL.nfx * PL.nfy;
+  tot += nph * pmax;
+  const size_t ff_off = tot;
+  tot += 2 * nph * pmax + 2 * nf * pmax + 22 * nf;
   EK_CUDA(cudaMalloc(&c.mgf_pool, tot * sizeof(float)));
   c.mgf_levels.assign(PL.ngrid, {});
   for (int l = 0; l < PL.ngrid; ++l) {
@@ -712,6 +720,23 @@ void mgfast_alloc(Ctx &c, int pmax) {
     EK_CUDA(cudaMemcpy(F.cof, cf.data(), sizeof(float) * cf.size(), cudaMemcpyHostToDevice));
   }
   c.mgf_scratch = c.mgf_pool + scr_off;
+  c.mgf_phh = c.mgf_pool + ff_off;
+  c.mgf_phl = c.mgf_phh + nph * pmax;
+  c.mgf_bh = c.mgf_phl + nph * pmax;
+  c.mgf_bl = c.mgf_bh + nf * pmax;
+  c.mgf_cfh = c.mgf_bl + nf * pmax;
+  c.mgf_cfl = c.mgf_cfh + 11 * nf;
+  {
+    // the finest coefficients split into float-float pairs
+    const std::vector<double> &cf = PL.cof_host[PL.ngrid - 1];
+    std::vector<float> h(cf.size()), l(cf.size());
+    for (size_t t = 0; t < cf.size(); ++t) {
+      h[t] = (float)cf[t];
+      l[t] = (float)(cf[t] - (double)h[t]);
+    }
+    EK_CUDA(cudaMemcpy(c.mgf_cfh, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice));
+    EK_CUDA(cudaMemcpy(c.mgf_cfl, l.data(), sizeof(float) * l.size(), cudaMemcpyHostToDevice));
+  }
   c.mgf_pmax = pmax;
   if (!c.aux_stream) {
     EK_CUDA(cudaStreamCreateWithFlags(&c.aux_stream, cudaStreamNonBlocking));
@@ -785,9 +810,13 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
     g.lv[l] = LvF{PL.lv[l].nx, PL.lv[l].ny, F.e, F.r, F.cof, F.cp};
   }
   g.scr = c.mgf_scratch;
-  g.phi = w.phi[PL.ngrid - 1];
   g.rhs = w.rhs[PL.ngrid - 1];
-  g.cof = PL.lv[PL.ngrid - 1].cof;
+  g.phh = c.mgf_phh;
+  g.phl = c.mgf_phl;
+  g.bh = c.mgf_bh;
+  g.bl = c.mgf_bl;
+  g.cfh = c.mgf_cfh;
+  g.cfl = c.mgf_cfl;
   g.nfx = PL.nfx;
   g.nfy = PL.nfy;
   g.kx2 = kx2_dev;
@@ -807,14 +836,15 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
       after_launch(c);
     }
     const size_t nph = (size_t)(PL.nfx + 2) * (PL.nfy + 2) * nprob;
-    k_f_zero64<<<nb((long)nph, bs), bs, 0, s>>>(g.phi, nph);
-    after_launch(c);
+    EK_CUDA(cudaMemsetAsync(g.phh, 0, sizeof(float) * nph, s));
+    EK_CUDA(cudaMemsetAsync(g.phl, 0, sizeof(float) * nph, s));
     const size_t nf = (size_t)PL.nfx * PL.nfy * nprob;
-    k_f_zero64<<<nb((long)nf, bs), bs, 0, s>>>(w.phif, nf);
+    k_f_split<<<nb((long)nf, bs), bs, 0, s>>>(g.rhs, g.bh, g.bl, nf);
     after_launch(c);
   }
   const int gx = (nprob + 31) / 32;
-  const int gy = (int)std::min<long>((npt + kRY - 1) / kRY, std::max<long>(1, 2048 / gx));
+  const unsigned pch = (unsigned)gx;  // 32-problem chunks of the row kernels
+
   // one partitioned line launch: lines l0, l0+lstep, ... (nline of them)
   // of length n, all problems
   auto pline = [&](int l, bool xl, int l0, int lstep, int nline, int n) {
@@ -834,7 +864,9 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
   };
   // one alternating-direction zebra sweep at level l: y-lines (colours
   // 1, 2), then x-lines (rows 1, 3, ... then 2, 4, ...); the post-smoothing
-  // sweep takes the colours in the reverse order.
+  // sweep takes the colours in the reverse order.  (Post-smoothing with
+  // x-lines only needs 8-9 corrections instead of 6-7 on the 256x257x193
+  // grid, so it costs more than it saves.)
   auto relax = [&](int l, bool post) {
     const MgLevel &L = PL.lv[l - 1];
     KScope ks(c, KC_MG_RELAX, 4.0 * nprob * L.nx * L.ny * 10);
@@ -856,8 +888,8 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
   c.poll.reset();
   for (int it = 0; it <= maxit; ++it) {
     {
-      KScope ks(c, KC_MG_CHECK, 8.0 * nprob * npt * 3 + 4.0 * nprob * npt);
-      k_f_resid64<<<dim3(gx, gy), dim3(32, kRY), 0, s>>>(g);
+      KScope ks(c, KC_MG_CHECK, 4.0 * nprob * (4.0 * npt + 2.0 * (PL.nfx + 2) * (PL.nfy + 2)));
+      k_f_resid_ff<<<dim3(pch, PL.nfy + 2), dim3(32, kRY), 0, s>>>(g);
       after_launch(c);
       k_f_check<<<1, 256, 0, s>>>(g, it, it == maxit ? 1 : 0);
       after_launch(c);
@@ -876,27 +908,33 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
       relax(l, false);
       const MgLevel &C = PL.lv[l - 2];
       KScope ks(c, KC_MG_TRANSFER, 4.0 * nprob * (4.0 * L.nx * L.ny + 2.0 * (C.nx + 2) * (C.ny + 2)));
-      k_f_resid32<<<nb((long)L.nx * L.ny * nprob, bs), bs, 0, s>>>(g, l);
+      k_f_resid32<<<dim3(pch, L.ny), dim3(32, kRowWarps), 0, s>>>(g, l);
       after_launch(c);
-      k_f_restrict<<<nb((long)(C.nx + 2) * (C.ny + 2) * nprob, bs), bs, 0, s>>>(g, l);
+      k_f_restrict<<<dim3(pch, C.ny + 2), dim3(32, kRowWarps), 0, s>>>(g, l);
       after_launch(c);
     }
     for (int l = 2; l <= PL.ngrid; ++l) {
       const MgLevel &L = PL.lv[l - 1];
       {
         KScope ks(c, KC_MG_TRANSFER, 4.0 * nprob * 4.0 * L.nx * L.ny);
-        k_f_prolong_x<<<nb((long)(L.ny + 1) * L.nx * nprob, bs), bs, 0, s>>>(g, l);
+        const MgLevel &Cq = PL.lv[l - 2];
+        k_f_prolong_x<<<dim3(pch, Cq.ny < L.ny ? (L.ny + 1) / 2 : L.ny), dim3(32, kRowWarps), 0, s>>>(g, l);
         after_launch(c);
-        k_f_prolong_y<<<nb((long)L.nx * L.ny * nprob, bs), bs, 0, s>>>(g, l);
+        k_f_prolong_y<<<dim3(pch, L.ny), dim3(32, kRowWarps), 0, s>>>(g, l);
         after_launch(c);
       }
       relax(l, true);
     }
     {
-      KScope ks(c, KC_MG_CHECK, 8.0 * nprob * npt * 3);
-      k_f_update<<<dim3(gx, gy), dim3(32, kRY), 0, s>>>(g);
+      KScope ks(c, KC_MG_CHECK, 4.0 * nprob * npt * 5);
+      k_f_update_ff<<<dim3(pch, PL.nfy), dim3(32, kRY), 0, s>>>(g);
       after_launch(c);
     }
+  }
+  {
+    KScope ks(c, KC_MG_SETUP, 16.0 * nprob * npt);
+    k_f_phif<<<dim3(pch, PL.nfy), dim3(32, kRY), 0, s>>>(g);
+    after_launch(c);
   }
   if (ns > 0) {
     EK_CUDA(cudaStreamWaitEvent(s, c.ev_join, 0));
