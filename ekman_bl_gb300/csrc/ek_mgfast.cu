@@ -338,10 +338,9 @@ __global__ void __launch_bounds__(64) k_f_xline(FastDev g, int level, int j0, in
 // p of warp 0 solves from shared memory; then every warp back-substitutes.
 // XL: x-line (along i, the periodic wrap couplings taken from the ghosts'
 // current values); else y-line (along j).
-constexpr int kSegMax = 16;
 enum { SH_A, SH_B, SH_C, SH_D, SH_YF, SH_VF, SH_WF, SH_YL, SH_VL, SH_WL, SH_S, SH_N };
-template <bool XL>
-__global__ void __launch_bounds__(512) k_f_pline(FastDev g, int level, int l0, int lstep, int mb, int me) {
+template <bool XL, bool ORTH, int kSegMax>
+__global__ void __launch_bounds__(1024) k_f_pline(FastDev g, int level, int l0, int lstep, int mb, int me) {
   if (*g.alldone) return;
   extern __shared__ float sh[];
   const int K = blockDim.y;
@@ -360,7 +359,6 @@ __global__ void __launch_bounds__(512) k_f_pline(FastDev g, int level, int l0, i
   const size_t si = P, sj = (size_t)(nx + 2) * P;
   const float kx2 = (float)g.kx2[pp];
   const float *cf = L.cof;
-  const bool orth = g.orth != 0;
   // row k of the line: a x(k-1) + b x(k) + c x(k+1) = d
   auto row = [&](int k, float &a, float &b, float &c, float &d) {
     const int i = XL ? k : line, j = XL ? line : k;
@@ -372,14 +370,12 @@ __global__ void __launch_bounds__(512) k_f_pline(FastDev g, int level, int l0, i
       a = cf[4 * npt + pt];
       c = cf[pt];
       dd = dd - cf[2 * npt + pt] * ep[sj] - cf[6 * npt + pt] * ep[-(long)sj];
-      if (i == 1) { dd -= a * ep[-(long)si]; a = 0.f; }
-      if (i == nx) { dd -= c * ep[si]; c = 0.f; }
     } else {
       a = cf[6 * npt + pt];
       c = cf[2 * npt + pt];
       dd = dd - cf[pt] * ep[si] - cf[4 * npt + pt] * ep[-(long)si];
     }
-    if (!orth)
+    if (!ORTH)
       dd = dd - cf[npt + pt] * ep[si + sj] - cf[3 * npt + pt] * ep[sj - si] - cf[5 * npt + pt] * ep[-(long)(si + sj)] -
            cf[7 * npt + pt] * ep[si - sj];
     d = dd;
@@ -390,21 +386,43 @@ __global__ void __launch_bounds__(512) k_f_pline(FastDev g, int level, int l0, i
     if (i == nx - 1) L.e[((size_t)j * (nx + 2)) * P + p] = x;
     if (i == 2) L.e[((size_t)j * (nx + 2) + nx + 1) * P + p] = x;
   };
-  float dl[kSegMax], gm[kSegMax], bt[kSegMax];
+  // phase 1: every load of the segment (rows past its end repeat its last
+  // row, so all addresses are valid and no load waits on arithmetic)
+  float av[kSegMax], bv[kSegMax], cv[kSegMax], dv[kSegMax];
+#pragma unroll
+  for (int u = 0; u < kSegMax; ++u) row(lo + min(u, m - 1), av[u], bv[u], cv[u], dv[u]);
+  if (XL) {
+    // the periodic wrap of an x-line: i = 1 couples to the ghost e(0) =
+    // e(nx-1), i = nx to e(nx+1) = e(2), both taken from current values
+    const float *erow = &L.e[(size_t)line * (nx + 2) * P + pp];
+    if (s == 0) {
+      dv[0] -= av[0] * erow[0];
+      av[0] = 0.f;
+    }
+    if (s == K - 1) {
+      const float gh = erow[(size_t)(nx + 1) * si];
+#pragma unroll
+      for (int u = 0; u < kSegMax; ++u) {
+        const bool hit = (u == m - 1);
+        dv[u] = hit ? dv[u] - cv[u] * gh : dv[u];
+        cv[u] = hit ? 0.f : cv[u];
+      }
+    }
+  }
+  // phase 2: elimination in place: cv <- beta, dv <- delta, av <- gamma, where
+  // row u of the segment is x = delta + gamma X0 - beta x(next)
   float yl = 0.f, vl = 0.f, wl = 0.f;
   {
     float bprev = 0.f, dprev = 0.f, gprev = 1.f;
 #pragma unroll
     for (int u = 0; u < kSegMax; ++u) {
-      float a, b, c, d;
-      row(lo + min(u, m - 1), a, b, c, d);
-      const float inv = 1.f / (b - a * bprev);
-      bprev = c * inv;
-      dprev = (d - a * dprev) * inv;
-      gprev = -a * gprev * inv;
-      bt[u] = bprev;
-      dl[u] = dprev;
-      gm[u] = gprev;
+      const float inv = __fdividef(1.f, bv[u] - av[u] * bprev);
+      bprev = cv[u] * inv;
+      dprev = (dv[u] - av[u] * dprev) * inv;
+      gprev = -av[u] * gprev * inv;
+      cv[u] = bprev;
+      dv[u] = dprev;
+      av[u] = gprev;
       const bool last = (u == m - 1);
       yl = last ? dprev : yl;
       vl = last ? gprev : vl;
@@ -415,9 +433,9 @@ __global__ void __launch_bounds__(512) k_f_pline(FastDev g, int level, int l0, i
 #pragma unroll
   for (int u = kSegMax - 2; u >= 0; --u)
     if (u < m - 1) {
-      yf = dl[u] - bt[u] * yf;
-      vf = gm[u] - bt[u] * vf;
-      wf = -bt[u] * wf;
+      yf = dv[u] - cv[u] * yf;
+      vf = av[u] - cv[u] * vf;
+      wf = -cv[u] * wf;
     }
   S(SH_YF, s) = yf; S(SH_VF, s) = vf; S(SH_WF, s) = wf;
   S(SH_YL, s) = yl; S(SH_VL, s) = vl; S(SH_WL, s) = wl;
@@ -436,7 +454,7 @@ __global__ void __launch_bounds__(512) k_f_pline(FastDev g, int level, int l0, i
       const float B = S(SH_B, t) + a * S(SH_WL, t) + c * S(SH_VF, t + 1);
       const float C = c * S(SH_WF, t + 1);
       const float D = S(SH_D, t) - a * S(SH_YL, t) - c * S(SH_YF, t + 1);
-      const float inv = 1.f / (B - A * cpv);
+      const float inv = __fdividef(1.f, B - A * cpv);
       cpv = C * inv;
       dpv = (D - A * dpv) * inv;
       S(SH_A, t) = cpv;  // c' and d' of the separator system
@@ -456,7 +474,7 @@ __global__ void __launch_bounds__(512) k_f_pline(FastDev g, int level, int l0, i
 #pragma unroll
   for (int u = kSegMax - 1; u >= 0; --u)
     if (u < m) {
-      x = dl[u] + gm[u] * X0 - bt[u] * ((u == m - 1) ? X1 : x);
+      x = dv[u] + av[u] * X0 - cv[u] * ((u == m - 1) ? X1 : x);
       store(lo + u, x);
     }
   if (s < K - 1) store(lo + m, X1);
@@ -848,8 +866,10 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
   // one partitioned line launch: lines l0, l0+lstep, ... (nline of them)
   // of length n, all problems
   auto pline = [&](int l, bool xl, int l0, int lstep, int nline, int n) {
-    const int K = std::max(1, (n + kSegMax) / (kSegMax + 1));
-    if (K > 16) {  // lines longer than 271 rows: one thread per line
+    // 8-row segments while a line fits 32 of them (n <= 287), else 16-row
+    const int seg = (n <= 32 * 9 - 1) ? 8 : 16;
+    const int K = std::max(1, (n + seg) / (seg + 1));
+    if (K > 32) {  // lines longer than 543 rows: one thread per line
       if (xl) k_f_xline<<<nb((long)nline * nprob, 64), 64, 0, s>>>(g, l, l0, nline);
       else k_f_yline<<<nb((long)nline * nprob, 64), 64, 0, s>>>(g, l, l0, lstep, nline);
       after_launch(c);
@@ -858,10 +878,18 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
     const int mb = (n - K + 1) / K, me = (n - K + 1) % K;
     const dim3 grid((unsigned)nline, (unsigned)((nprob + 31) / 32)), blk(32, K);
     const size_t smem = sizeof(float) * SH_N * K * 32;
-    if (xl) k_f_pline<true><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);
-    else k_f_pline<false><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);
+#define EK_PLINE(X, O, S) k_f_pline<X, O, S><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me)
+    if (seg == 8) {
+      if (g.orth) { if (xl) EK_PLINE(true, true, 8); else EK_PLINE(false, true, 8); }
+      else { if (xl) EK_PLINE(true, false, 8); else EK_PLINE(false, false, 8); }
+    } else {
+      if (g.orth) { if (xl) EK_PLINE(true, true, 16); else EK_PLINE(false, true, 16); }
+      else { if (xl) EK_PLINE(true, false, 16); else EK_PLINE(false, false, 16); }
+    }
+#undef EK_PLINE
     after_launch(c);
   };
+
   // one alternating-direction zebra sweep at level l: y-lines (colours
   // 1, 2), then x-lines (rows 1, 3, ... then 2, 4, ...); the post-smoothing
   // sweep takes the colours in the reverse order.  (Post-smoothing with

@@ -239,3 +239,21 @@ def test_float_float_transforms_hundred_steps():
     o.step(100)
     for name, x, y in zip(("CU1", "CU2", "CU3", "CP", "CTH"), g.download(), o.download()):
         assert rel_l2(x, y) < 1e-10, name
+
+
+def test_mixed_precision_poisson_tall_grid():
+    """Lines longer than 287 rows take the 16-row-segment line solver: a
+    17 x 321 grid (NZ+2 x NY+2) to 1e-10, checked with the oracle's operator."""
+    p, xp, yp, _ = small_case(nx=16, ny2=321, nz2=17)
+    p.mg_stop, p.mg_tol, p.mg_maxcy, p.mg_fast = 1, 1e-10, 60, 1
+    g = DuctSolver(p, metrics_from_grid(p, xp, yp))
+    o = ekref.Oracle(p, ekref.metrics_from_grid(p, xp, yp))
+    kx2 = np.array([(2 * math.pi * k / p.lx) ** 2 for k in (1, 3)])
+    rhs = np.random.default_rng(5).standard_normal((len(kx2), p.ny + 2, p.nz + 2))
+    rhs[:, 0, :] = 0
+    rhs[:, -1, :] = 0
+    pg, sg, cg = g.multigrid_mudpack(rhs, kx2)
+    assert cg == 0 and sg["n_not_converged"] == 0, sg
+    for q in range(len(kx2)):
+        r = rhs[q] - o.mg_apply(kx2[q], pg[q])
+        assert np.linalg.norm(r) / np.linalg.norm(rhs[q]) <= 1.05e-10, q
