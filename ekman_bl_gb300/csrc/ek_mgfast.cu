@@ -328,28 +328,30 @@ __global__ void __launch_bounds__(64) k_f_xline(FastDev g, int level, int j0, in
   }
 }
 
-// Partitioned line solve: one block per (line, 32 problems), lanes over the
-// problems (coalesced, the layout is problem fastest), warps over K segments
-// of the line.  The line's n rows are K segments of <= kSegMax interior rows
-// separated by K-1 separator rows.  Each warp eliminates its segment in
-// registers, expressing every row as x = delta + gamma X0 - beta x(next) with
-// X0, X1 the separators before and after it; the first and last rows in
-// terms of (X0, X1) give a tridiagonal system for the separators, which lane
-// p of warp 0 solves from shared memory; then every warp back-substitutes.
+// Partitioned line solve: one block per (line, LANES problems), lanes over
+// the problems (coalesced, the layout is problem fastest), threadIdx.y over K
+// segments of the line.  The line's n rows are K segments of <= 8 interior
+// rows separated by K-1 separator rows.  Each thread row eliminates its
+// segment in registers, expressing every row as x = delta + gamma X0 -
+// beta x(next) with X0, X1 the separators before and after it; the first and
+// last rows in terms of (X0, X1) give a tridiagonal system for the
+// separators, which thread row 0 solves from shared memory, one thread per
+// problem; then every segment back-substitutes.
 // XL: x-line (along i, the periodic wrap couplings taken from the ghosts'
 // current values); else y-line (along j).
 enum { SH_A, SH_B, SH_C, SH_D, SH_YF, SH_VF, SH_WF, SH_YL, SH_VL, SH_WL, SH_S, SH_N };
-template <bool XL, bool ORTH, int kSegMax>
+template <bool XL, bool ORTH, int LANES>
 __global__ void __launch_bounds__(1024) k_f_pline(FastDev g, int level, int l0, int lstep, int mb, int me) {
+  constexpr int kSegMax = 8;
   if (*g.alldone) return;
   extern __shared__ float sh[];
   const int K = blockDim.y;
-  auto S = [&](int arr, int seg) -> float & { return sh[((size_t)arr * K + seg) * 32 + threadIdx.x]; };
+  auto S = [&](int arr, int seg) -> float & { return sh[((size_t)arr * K + seg) * LANES + threadIdx.x]; };
   const LvF L = g.lv[level - 1];
   const int P = g.P;
   const int nx = L.nx, ny = L.ny;
   const int s = threadIdx.y;
-  const int p = blockIdx.y * 32 + threadIdx.x;
+  const int p = blockIdx.y * LANES + threadIdx.x;
   const bool act = (p < P) && !g.done[p];
   const int pp = act ? p : 0;
   const int line = l0 + lstep * (int)blockIdx.x;
@@ -866,22 +868,23 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
   // one partitioned line launch: lines l0, l0+lstep, ... (nline of them)
   // of length n, all problems
   auto pline = [&](int l, bool xl, int l0, int lstep, int nline, int n) {
-    // 8-row segments while a line fits 32 of them (n <= 287), else 16-row
-    const int seg = (n <= 32 * 9 - 1) ? 8 : 16;
-    const int K = std::max(1, (n + seg) / (seg + 1));
-    if (K > 32) {  // lines longer than 543 rows: one thread per line
+    // segments of <= 8 rows; 32 problems per block while a line needs at
+    // most 32 segments (n <= 287), else 16 problems and up to 64 segments
+    const int K = std::max(1, (n + 8) / 9);
+    if (K > 64) {  // lines longer than 575 rows: one thread per line
       if (xl) k_f_xline<<<nb((long)nline * nprob, 64), 64, 0, s>>>(g, l, l0, nline);
       else k_f_yline<<<nb((long)nline * nprob, 64), 64, 0, s>>>(g, l, l0, lstep, nline);
       after_launch(c);
       return;
     }
+    const int lanes = (K <= 32) ? 32 : 16;
     const int mb = (n - K + 1) / K, me = (n - K + 1) % K;
-    const dim3 grid((unsigned)nline, (unsigned)((nprob + 31) / 32)), blk(32, K);
-    const size_t smem = sizeof(float) * SH_N * K * 32;
-#define EK_PLINE(X, O, S) k_f_pline<X, O, S><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me)
-    if (seg == 8) {
-      if (g.orth) { if (xl) EK_PLINE(true, true, 8); else EK_PLINE(false, true, 8); }
-      else { if (xl) EK_PLINE(true, false, 8); else EK_PLINE(false, false, 8); }
+    const dim3 grid((unsigned)nline, (unsigned)((nprob + lanes - 1) / lanes)), blk(lanes, K);
+    const size_t smem = sizeof(float) * SH_N * K * lanes;
+#define EK_PLINE(X, O, W) k_f_pline<X, O, W><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me)
+    if (lanes == 32) {
+      if (g.orth) { if (xl) EK_PLINE(true, true, 32); else EK_PLINE(false, true, 32); }
+      else { if (xl) EK_PLINE(true, false, 32); else EK_PLINE(false, false, 32); }
     } else {
       if (g.orth) { if (xl) EK_PLINE(true, true, 16); else EK_PLINE(false, true, 16); }
       else { if (xl) EK_PLINE(true, false, 16); else EK_PLINE(false, false, 16); }
@@ -889,6 +892,7 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
 #undef EK_PLINE
     after_launch(c);
   };
+
 
   // one alternating-direction zebra sweep at level l: y-lines (colours
   // 1, 2), then x-lines (rows 1, 3, ... then 2, 4, ...); the post-smoothing

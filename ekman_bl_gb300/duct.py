@@ -181,9 +181,14 @@ class DuctSolver:
         arrs = [np.ascontiguousarray(a, np.complex128) for a in (cu1, cu2, cu3, cp, cth)]
         self._check(self._L.ekgpu_upload_state(self._h, *[as_ptr(a) for a in arrs]))
 
-    def download(self):
+    def download(self, out=None):
+        """CU1X, CU2X, CU3X, CPX, CTHX; into the five arrays of `out` when
+        given (C-contiguous complex128 of the spectral shape, e.g. pinned)."""
         shape = spectral_shape(self.p)
-        arrs = [np.zeros(shape, np.complex128) for _ in range(5)]
+        arrs = list(out) if out is not None else [np.zeros(shape, np.complex128) for _ in range(5)]
+        for a in arrs:
+            if a.shape != shape or a.dtype != np.complex128 or not a.flags.c_contiguous:
+                raise ValueError("download: out arrays must be C-contiguous complex128 of the spectral shape")
         self._check(self._L.ekgpu_download_state(self._h, *[as_ptr(a) for a in arrs]))
         return arrs
 

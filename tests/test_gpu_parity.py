@@ -242,8 +242,9 @@ def test_float_float_transforms_hundred_steps():
 
 
 def test_mixed_precision_poisson_tall_grid():
-    """Lines longer than 287 rows take the 16-row-segment line solver: a
-    17 x 321 grid (NZ+2 x NY+2) to 1e-10, checked with the oracle's operator."""
+    """Lines longer than 287 rows take the line solver's 16-problem layout
+    (up to 64 segments): a 17 x 321 grid (NZ+2 x NY+2) to 1e-10, checked with
+    the oracle's operator."""
     p, xp, yp, _ = small_case(nx=16, ny2=321, nz2=17)
     p.mg_stop, p.mg_tol, p.mg_maxcy, p.mg_fast = 1, 1e-10, 60, 1
     g = DuctSolver(p, metrics_from_grid(p, xp, yp))
