@@ -151,10 +151,12 @@ class Workload:
 WORKLOADS = {
     "ekman_neutral_64x65x65": Workload("ekman_neutral_64x65x65", 64, 65, 65, 400.0, 1.0, 0.0, 1.0e-3, 100,
                                        1e-10, 0.01, 4.0 * math.pi, 0.4),
+    # cells of 0.35 / 0.3 Ekman depths keep the streamwise advective CFL near
+    # 0.6 at the named time steps (0.25 depths went unstable within 25 steps)
     "ekman_strat_256x257x193": Workload("ekman_strat_256x257x193", 256, 257, 193, 800.0, 0.7, 0.1, 5.0e-4, 200,
-                                        1e-10, 0.01, 64.0, 0.25),
-    "ekman_strat_512x385x257": Workload("ekman_strat_512x385x257", 512, 385, 257, 1000.0, 0.7, 0.1, 5.0e-4, 200,
-                                        1e-8, 0.01, 128.0, 0.25),
+                                        1e-10, 0.01, 64.0, 0.35),
+    "ekman_strat_512x385x257": Workload("ekman_strat_512x385x257", 512, 385, 257, 1000.0, 0.7, 0.1, 3.0e-4, 200,
+                                        1e-8, 0.01, 128.0, 0.3),
 }
 
 
