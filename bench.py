@@ -119,7 +119,7 @@ def setup_solver(device_index: int, mg_fast: int = 1, fft_fp32: int = 1):
     p, xp, yp, state = workload_setup(w, EK_MG_STOP_RESIDUAL)
     p.mg_fast = mg_fast
     p.fft_fp32 = fft_fp32
-    p.fft_ff = 1 if fft_fp32 else 0
+    p.ff_arith = 1 if fft_fp32 else 0
     solver = DuctSolver(p, metrics_from_grid(p, xp, yp))
     stream = torch.cuda.Stream()
     solver.set_stream(stream.cuda_stream)

@@ -304,7 +304,7 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
   if (p.sponge_type < 0 || p.sponge_type > 2) return reject("SPONGE_TYPE must be 0, 1 or 2");
   if (p.sponge_type != 0 && p.save_stats_int < 1) return reject("SAVE_STATS_INT must be >= 1 with a sponge");
   if (p.fft_fp32 < 0 || p.fft_fp32 > 2) return reject("fft_fp32 must be 0, 1 or 2");
-  if (p.fft_ff < 0 || p.fft_ff > 1) return reject("fft_ff must be 0 or 1");
+  if (p.ff_arith < 0 || p.ff_arith > 1) return reject("ff_arith must be 0 or 1");
   if (p.variable_dt && (p.update_dt < 1 || !(p.cfl > 0.0) || !(p.delta_t_set > 0.0)))
     return reject("VARIABLE_DT needs UPDATE_DT >= 1, CFL > 0 and DELTA_T_SET > 0");
   if (p.sponge_type != 0 && p.ny_s_t <= p.ny && p.ny_s_t < 0) return reject("NY_S_T must be >= 0");

@@ -311,8 +311,8 @@ FftConst make_const(Ctx &c) {
 // marked low-precision (the nonlinear products and fluxes, whose results
 // enter the step multiplied by the time step); 2: every transform.
 bool fft_lowp(const Ctx &c, int lowp) { return c.p.fft_fp32 >= 2 || (c.p.fft_fp32 == 1 && lowp); }
-// float-float for the other transforms under fft_ff
-bool fft_ff(const Ctx &c, int lowp) { return c.p.fft_ff && !fft_lowp(c, lowp); }
+// float-float for the other transforms under ff_arith
+bool fft_ff(const Ctx &c, int lowp) { return c.p.ff_arith && !fft_lowp(c, lowp); }
 
 void launch_r2c(Ctx &c, const R2cArgs &a) {
   const FftConst fc = make_const(c);

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/ekgpu.h"
+#include "ek_ffbits.h"
 
 namespace ek {
 
@@ -35,36 +36,7 @@ struct Dims {
   __host__ __device__ size_t nspec() const { return (size_t)LDC * NZ2 * NY2; }
 };
 
-// double <-> float on the integer pipes.  GB300's FP64 pipe (which also
-// executes the F2F conversions) is narrow, so FP32 kernels on FP64 fields
-// would otherwise be bound by their conversions.  Round to nearest even;
-// values below the float normal range become zero, infinities and NaN go
-// through the hardware conversion.
 #ifdef __CUDACC__
-__device__ __forceinline__ float d2f_bits(double x) {
-  const unsigned uh = (unsigned)__double2hiint(x), ul = (unsigned)__double2loint(x);
-  const unsigned sign = uh & 0x80000000u;
-  const int e = (int)((uh >> 20) & 0x7ffu);
-  if (e == 0x7ff) return (float)x;
-  const int fe = e - 896;
-  if (fe <= 0) return __uint_as_float(sign);
-  if (fe >= 0xff) return __uint_as_float(sign | 0x7f800000u);
-  const unsigned mant = ((uh & 0xfffffu) << 3) | (ul >> 29);
-  unsigned r = sign | ((unsigned)fe << 23) | mant;
-  const unsigned dropped = ul & 0x1fffffffu;
-  if (dropped > 0x10000000u || (dropped == 0x10000000u && (mant & 1u))) r += 1u;
-  return __uint_as_float(r);
-}
-__device__ __forceinline__ double f2d_bits(float f) {
-  const unsigned u = __float_as_uint(f);
-  const unsigned sign = u & 0x80000000u;
-  const unsigned e = (u >> 23) & 0xffu;
-  if (e == 0) return __hiloint2double((int)sign, 0);
-  if (e == 0xff) return (double)f;
-  const unsigned mant = u & 0x7fffffu;
-  return __hiloint2double((int)(sign | ((e + 896u) << 20) | (mant >> 3)), (int)(mant << 29));
-}
-
 // Float-float: an unevaluated sum hi + lo of two floats (about 48
 // significant bits), with the error-free sum (Knuth's TwoSum) and the
 // FMA-based product.  The _rn intrinsics keep the compiler from fusing or
@@ -74,6 +46,9 @@ struct FF {
   float hi, lo;
   FF() = default;
   __device__ FF(float h, float l) : hi(h), lo(l) {}
+  // one FP64 add each way: splitting and joining in 64-bit integer
+  // arithmetic costs as much on GB300 (measured), the conversions themselves
+  // run on the integer pipes
   __device__ explicit FF(double x) {
     hi = d2f_bits(x);
     lo = d2f_bits(x - f2d_bits(hi));
@@ -100,7 +75,6 @@ __device__ __forceinline__ FF operator*(FF a, FF b) {
   e = __fmaf_rn(a.lo, b.hi, e);
   return ff_norm(p, e);
 }
-
 #endif
 
 // Device copies of the JACOBI_TRANS metric arrays.

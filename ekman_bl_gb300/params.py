@@ -46,7 +46,7 @@ class EkParams(C.Structure):
         ("ny_s_t", C.c_int), ("nz_s_r", C.c_int), ("nz_s_l", C.c_int), ("save_stats_int", C.c_int),
         ("time_step", C.c_int), ("variable_dt", C.c_int), ("update_dt", C.c_int),
         ("cfl", C.c_double), ("delta_t_set", C.c_double), ("fft_fp32", C.c_int),
-        ("fft_ff", C.c_int),
+        ("ff_arith", C.c_int),
     ]
 
 

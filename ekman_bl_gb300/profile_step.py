@@ -26,7 +26,7 @@ def main():
     ap.add_argument("--nx", type=int, default=0, help="override NX (smaller cases for full ncu captures)")
     ap.add_argument("--mixed", action="store_true",
                     help="mixed-precision method: mg_fast = 1, fft_fp32 = 1 (needs --tol > 0)")
-    ap.add_argument("--ff", action="store_true", help="float-float state-carrying transforms (fft_ff = 1)")
+    ap.add_argument("--ff", action="store_true", help="float-float state-carrying transforms (ff_arith = 1)")
     args = ap.parse_args()
     ekbuild.build()
     w = WORKLOADS[args.workload]
@@ -40,7 +40,7 @@ def main():
     if args.mixed:
         p.mg_fast, p.fft_fp32 = 1, 1
     if args.ff:
-        p.fft_ff = 1
+        p.ff_arith = 1
     s = DuctSolver(p, metrics_from_grid(p, xp, yp))
     s.upload(*state)
     s.rem_div_curv()

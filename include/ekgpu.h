@@ -106,8 +106,8 @@ typedef struct ek_params {
   double delta_t_set;        /* DELTA_T_SET: the cap of the CFL time step               */
   int fft_fp32;              /* x-transforms in FP32 arithmetic (fields stay FP64): 0 none,
                                 1 the nonlinear product/flux transforms, 2 every transform */
-  int fft_ff;                /* 1: the transforms fft_fp32 leaves in FP64 use float-float
-                                arithmetic (~48 bits) on the FP32 pipe instead          */
+  int ff_arith;              /* 1: the x-transforms fft_fp32 leaves in FP64 use float-float
+                                arithmetic (~48 bits) on the FP32 pipe; fields stay FP64  */
 } ek_params;
 
 /* Geometry and background fields of JACOBI_TRANS (diablo.F90:1088-1570);

@@ -208,7 +208,7 @@ def test_mixed_path_hundred_steps_neutral_64():
     p.mg_tol, p.mg_maxcy = 1e-10, 200
     o = ekref.Oracle(p, ekref.metrics_from_grid(p, xp, yp))
     q = workload_setup(w, EK_MG_STOP_RESIDUAL)[0]
-    q.mg_tol, q.mg_maxcy, q.mg_fast, q.fft_fp32, q.fft_ff = 1e-10, 60, 1, 1, 1
+    q.mg_tol, q.mg_maxcy, q.mg_fast, q.fft_fp32, q.ff_arith = 1e-10, 60, 1, 1, 1
     g = DuctSolver(q, metrics_from_grid(q, xp, yp))
     g.upload(*st)
     o.upload(*st)
@@ -223,13 +223,13 @@ def test_mixed_path_hundred_steps_neutral_64():
 
 
 def test_float_float_transforms_hundred_steps():
-    """fft_ff = 1 on the FP64 path: the transforms in float-float arithmetic
+    """ff_arith = 1 on the FP64 path: the transforms in float-float arithmetic
     stay within 1e-10 of the FP64 oracle after 100 steps (measured ~1e-12)."""
     w = WORKLOADS["ekman_neutral_64x65x65"]
     p, xp, yp, st = workload_setup(w)
     o = ekref.Oracle(p, ekref.metrics_from_grid(p, xp, yp))
     q = workload_setup(w)[0]
-    q.fft_ff = 1
+    q.ff_arith = 1
     g = DuctSolver(q, metrics_from_grid(q, xp, yp))
     g.upload(*st)
     o.upload(*st)
