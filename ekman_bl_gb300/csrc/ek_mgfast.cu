@@ -984,12 +984,13 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
   EK_CUDA(cudaStreamSynchronize(s));
   ek_mg_stats S{};
   S.nprob = nprob;
+  // cycle counts over the non-singular problems when there are any: the
+  // kx^2 = 0 ones always run MUDPACK's capped cycles
   S.min_cycles = (nprob > ns) ? (1 << 30) : Ss.min_cycles;
-  S.max_cycles = Ss.max_cycles;
+  S.max_cycles = (nprob > ns) ? 0 : Ss.max_cycles;
   S.n_not_converged = Ss.n_not_converged;
   S.max_relchange = Ss.max_relchange;
   S.max_residual = Ss.max_residual;
-  if (ns > 0) S.min_cycles = std::min(S.min_cycles, Ss.min_cycles);
   for (int p = 0; p < nprob; ++p) {
     if (is_sing[p]) continue;
     S.min_cycles = std::min(S.min_cycles, cyc[p]);

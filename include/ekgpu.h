@@ -122,7 +122,9 @@ typedef struct ek_metrics {
 /* Per-call multigrid report. */
 typedef struct ek_mg_stats {
   int nprob;                 /* real 2-D problems solved                         */
-  int min_cycles, max_cycles;/* cycles after FMG, over problems                  */
+  int min_cycles, max_cycles;/* cycles after FMG (mg_fast: FP32 corrections), over
+                                problems; with mg_fast over the kx^2 != 0 problems
+                                when there are any                              */
   int n_not_converged;       /* problems that hit maxcy                          */
   double max_relchange;      /* largest final relmax                             */
   double max_residual;       /* largest final ||b-A phi||/||b|| (residual rule)  */
