@@ -584,6 +584,30 @@ int ekgpu_download_state(ek_ctx *h, double *cu1, double *cu2, double *cu3, doubl
   });
 }
 
+int ekgpu_save_flow(ek_ctx *h, const char *flow_path, const char *th_path) {
+  return guarded(h, [&](Ctx &c) {
+    if (!flow_path) return fail(c, EK_ERR_ARG, "flow_path is NULL");
+    if (th_path && c.p.n_th < 1) return fail(c, EK_ERR_ARG, "th_path given but n_th == 0");
+    return save_flow(c, flow_path, th_path);
+  });
+}
+
+int ekgpu_read_flow(ek_ctx *h, const char *flow_path, const char *th_path) {
+  return guarded(h, [&](Ctx &c) {
+    if (!flow_path) return fail(c, EK_ERR_ARG, "flow_path is NULL");
+    if (th_path && c.p.n_th < 1) return fail(c, EK_ERR_ARG, "th_path given but n_th == 0");
+    return read_flow(c, flow_path, th_path);
+  });
+}
+
+int ekgpu_save_stats(ek_ctx *h, ek_stats *st) {
+  return guarded(h, [&](Ctx &c) {
+    if (!st) return fail(c, EK_ERR_ARG, "stats is NULL");
+    if (!c.have_metrics) return fail(c, EK_ERR_STATE, "metrics not set");
+    return save_stats(c, st);
+  });
+}
+
 static cplx_t *field_of(Ctx &c, int f) {
   switch (f) {
     case EK_F_CU1: return c.CU1; case EK_F_CU2: return c.CU2; case EK_F_CU3: return c.CU3;

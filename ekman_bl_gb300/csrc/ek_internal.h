@@ -247,6 +247,8 @@ struct Ctx {
   // the metrics the dt-dependent ADI factors are built from
   double *cfl_dt = nullptr;
   std::vector<double> h_jac, h_g11, h_g22;
+  // SAVE_STATS_CURVI planes and sums (ek_stats.cu)
+  double *stats_buf = nullptr;
   // divergence check
   double *div_part = nullptr;
   double last_div = 0.0;
@@ -356,6 +358,12 @@ void mg_work_alloc(Ctx &c, MgWork &w, int pmax);
 void mg_work_free(MgWork &w);
 int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_host, ek_mg_stats *st);
 void mgfast_alloc(Ctx &c, int pmax);
+
+// restart files (ek_io.cpp): SAVE_FLOW / READ_FLOW records from and into the state
+int save_flow(Ctx &c, const char *flow_path, const char *th_path);
+int read_flow(Ctx &c, const char *flow_path, const char *th_path);
+// plane statistics (ek_stats.cu): SAVE_STATS_CURVI's reductions and its state round trip
+int save_stats(Ctx &c, ek_stats *out);
 
 #define EK_CUDA(call)                                                                  \
   do {                                                                                 \

@@ -353,6 +353,7 @@ __global__ void __launch_bounds__(1024) k_f_pline(FastDev g, int level, int l0, 
   const int s = threadIdx.y;
   const int p = blockIdx.y * LANES + threadIdx.x;
   const bool act = (p < P) && !g.done[p];
+  if (!__syncthreads_or(act)) return;  // every problem of the block converged
   const int pp = act ? p : 0;
   const int line = l0 + lstep * (int)blockIdx.x;
   const int m = mb + (s < me ? 1 : 0);

@@ -15,7 +15,7 @@ import os
 
 import numpy as np
 
-from .params import STATUS, EkMetrics, EkMgStats, EkParams, as_ptr, spectral_shape
+from .params import STATUS, EkMetrics, EkMgStats, EkParams, EkStats, as_ptr, spectral_shape, stats_dict, stats_struct
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libekgpu.so")
@@ -30,6 +30,7 @@ EXPORTS = [
     "ekgpu_launch_count", "ekgpu_set_timing", "ekgpu_get_timing", "ekgpu_timing_class_name",
     "ekgpu_fft_x_to_fourier", "ekgpu_fft_x_to_physical", "ekgpu_fft_x_to_fourier_noalloc",
     "ekgpu_sponge_profiles", "ekgpu_set_sponge", "ekgpu_set_time", "ekgpu_get_time",
+    "ekgpu_save_flow", "ekgpu_read_flow", "ekgpu_save_stats",
 ]
 
 
@@ -68,6 +69,9 @@ def load_library():
     L.ekgpu_get_time.argtypes = [V, _D, C.POINTER(C.c_int), _D]
     L.ekgpu_upload_state.argtypes = [V] + [_D] * 5
     L.ekgpu_download_state.argtypes = [V] + [_D] * 5
+    L.ekgpu_save_flow.argtypes = [V, C.c_char_p, C.c_char_p]
+    L.ekgpu_read_flow.argtypes = [V, C.c_char_p, C.c_char_p]
+    L.ekgpu_save_stats.argtypes = [V, C.POINTER(EkStats)]
     L.ekgpu_get_field.argtypes = [V, C.c_int, _D]
     L.ekgpu_put_field.argtypes = [V, C.c_int, _D]
     L.ekgpu_rk_substep.argtypes = [V, C.c_int]
@@ -87,6 +91,24 @@ def load_library():
         getattr(L, n).argtypes = [C.c_int, C.c_int, C.c_long, V, V, V]
     _lib = L
     return L
+
+
+def restart_file_names(kind: str, rank: int = 0, n_th: int = 1, backup_index: int = 0):
+    """The restart file names of SAVE_FLOW, BACKUP_FLOW and READ_FLOW
+    (diablo.F90:781-809, 861-882, 938-950): kind "saved" or "res"
+    (last_saved/), or "backup" (backup/, suffix _mmmm = backup_index mod
+    10000).  Rank digits RRR = (rank+1) mod 1000, scalar digits NN = N mod
+    100.  Returns (flow name, [scalar names])."""
+    r = f"{(rank + 1) % 1000:03d}"
+    if kind in ("saved", "res"):
+        d, ext = "last_saved", "." + kind
+    elif kind == "backup":
+        d, ext = "backup", f".saved_{backup_index % 10000:04d}"
+    else:
+        raise ValueError(f"restart kind {kind!r}: one of saved, res, backup")
+    flow = f"{d}/diablo_{r}{ext}"
+    ths = [f"{d}/diablo_th{n % 100:02d}_{r}{ext}" for n in range(1, n_th + 1)]
+    return flow, ths
 
 
 def metrics_from_grid(p: EkParams, xpoint: np.ndarray, ypoint: np.ndarray) -> dict:
@@ -191,6 +213,71 @@ class DuctSolver:
                 raise ValueError("download: out arrays must be C-contiguous complex128 of the spectral shape")
         self._check(self._L.ekgpu_download_state(self._h, *[as_ptr(a) for a in arrs]))
         return arrs
+
+    # -- restart files ----------------------------------------------------------
+    def write_restart(self, flow_path: str, th_path: str | None = None):
+        """The file writes of SAVE_FLOW / BACKUP_FLOW (diablo.F90:813-833,
+        886-907): records [NX NY NZ TIME TIME_STEP] and [CU1X CU2X CU3X CPX]
+        to flow_path, the header and [CTHX] to th_path."""
+        self._check(self._L.ekgpu_save_flow(self._h, os.fsencode(flow_path),
+                                            None if th_path is None else os.fsencode(th_path)))
+
+    def read_restart(self, flow_path: str, th_path: str | None = None):
+        """The file reads of READ_FLOW (diablo.F90:953-987); sets TIME and
+        TIME_STEP from the headers.  A wrong-dimension file raises EkError
+        (EK_ERR_IO) with the state unchanged."""
+        self._check(self._L.ekgpu_read_flow(self._h, os.fsencode(flow_path),
+                                            None if th_path is None else os.fsencode(th_path)))
+
+    def save_flow(self, final: bool = False, root: str = ".", rank: int = 0):
+        """SAVE_FLOW(FINAL) (diablo.F90:753-837): creates last_saved/ when
+        missing and writes diablo_RRR.saved (.res when final) plus one scalar
+        file per N_TH.  Returns the paths written."""
+        d = os.path.join(root, "last_saved")
+        os.makedirs(d, exist_ok=True)
+        kind = "res" if final else "saved"
+        flow, ths = restart_file_names(kind, rank, self.p.n_th)
+        flow, ths = os.path.join(root, flow), [os.path.join(root, t) for t in ths]
+        self.write_restart(flow, ths[0] if ths else None)
+        return [flow] + ths
+
+    def backup_flow(self, backup_flow_int: int, root: str = ".", rank: int = 0):
+        """BACKUP_FLOW (diablo.F90:841-915): backup/diablo_RRR.saved_mmmm with
+        m = TIME_STEP / BACKUP_FLOW_INT.  Returns the paths written."""
+        os.makedirs(os.path.join(root, "backup"), exist_ok=True)
+        _, step, _ = self.get_time()
+        flow, ths = restart_file_names("backup", rank, self.p.n_th, step // backup_flow_int)
+        flow, ths = os.path.join(root, flow), [os.path.join(root, t) for t in ths]
+        self.write_restart(flow, ths[0] if ths else None)
+        return [flow] + ths
+
+    def read_flow(self, root: str = ".", rank: int = 0, read_th: bool = True):
+        """READ_FLOW (diablo.F90:918-1072): last_saved/diablo_RRR.saved and,
+        when read_th (the scalar is not CREATE_NEW_TH), its scalar file."""
+        flow, ths = restart_file_names("saved", rank, self.p.n_th)
+        th = os.path.join(root, ths[0]) if (read_th and ths) else None
+        self.read_restart(os.path.join(root, flow), th)
+
+    # -- statistics -------------------------------------------------------------
+    def save_stats(self, root: str | None = None, save_stats_int: int | None = None,
+                   xpoint=None, ypoint=None) -> dict:
+        """SAVE_STATS_CURVI (flow_statistics.F90:2-1023): the plane statistics
+        as a dict of scalars and (NY+2, NZ+2) planes.  The state goes through
+        physical space and back and CF1X..CF3X are zeroed, as in the
+        reference.  With root, also appends plane_data/time_bulk.txt and
+        writes plot_binary's data_tec_KKKKK.pln (needs xpoint, ypoint)."""
+        st, arrs = stats_struct(self.p)
+        self._check(self._L.ekgpu_save_stats(self._h, C.byref(st)))
+        out = stats_dict(st, arrs)
+        if root is not None:
+            from .stats_io import write_stats_files
+            time, step, dt = self.get_time()
+            every = save_stats_int if save_stats_int is not None else self.p.save_stats_int
+            th_bar = self._metrics.get("th_bar")
+            if th_bar is None:
+                th_bar = np.zeros((self.p.ny + 3, self.p.nz + 3))
+            out["files"] = write_stats_files(root, time, dt, step, every, xpoint, ypoint, th_bar, out)
+        return out
 
     def get_field(self, f: int):
         a = np.zeros(spectral_shape(self.p), np.complex128)

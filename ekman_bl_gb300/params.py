@@ -20,7 +20,8 @@ EK_MG_STOP_RELCHANGE, EK_MG_STOP_RESIDUAL = 0, 1
  EK_F_CFTH, EK_F_CR1) = range(10)
 
 STATUS = {0: "EK_OK", 1: "EK_ERR_ARG", 2: "EK_ERR_CUDA", 3: "EK_ERR_NOT_CONVERGED",
-          4: "EK_ERR_NAN", 5: "EK_ERR_TIMEOUT", 6: "EK_ERR_STATE"}
+          4: "EK_ERR_NAN", 5: "EK_ERR_TIMEOUT", 6: "EK_ERR_STATE",
+          7: "EK_ERR_IO"}
 
 # REAL*4 literal 10.0**(-6) of mg_solver2d.F90:188, widened to REAL*8.
 MUDPACK_TOLMAX = float(np.float32(10.0) ** np.float32(-6))
@@ -61,6 +62,33 @@ class EkMgStats(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# ek_stats: the scalars, then the (0:NZ+1, 0:NY+1) planes, in header order
+STATS_SCALARS = ("ubulk", "vbulk", "thbulk", "urms_b", "vrms_b", "wrms_b", "u3_probe", "u1_probe")
+STATS_PLANES = ("urms", "vrms", "wrms", "uv", "uw", "wv", "pu", "pv", "tke", "dudy", "dwdy", "dudz", "dwdz",
+                "omega_x", "thrms", "thv", "thw", "dthdy", "dthdz", "rig",
+                "mean_u1", "mean_u2", "mean_u3", "mean_p", "mean_th")
+
+
+class EkStats(C.Structure):
+    _fields_ = [(n, C.c_double) for n in STATS_SCALARS] + [(n, C.POINTER(C.c_double)) for n in STATS_PLANES]
+
+
+def stats_struct(p: "EkParams"):
+    """An EkStats whose planes point into fresh (NY+2, NZ+2) arrays (the
+    Fortran (0:NZ+1, 0:NY+1) layout); returns (struct, arrays)."""
+    arrs = {n: np.zeros((p.ny + 2, p.nz + 2)) for n in STATS_PLANES}
+    st = EkStats()
+    for n, a in arrs.items():
+        setattr(st, n, as_ptr(a))
+    return st, arrs
+
+
+def stats_dict(st: EkStats, arrs: dict) -> dict:
+    out = {n: getattr(st, n) for n in STATS_SCALARS}
+    out.update(arrs)
+    return out
 
 
 def default_params(nx: int, ny: int, nz: int) -> EkParams:

@@ -42,7 +42,8 @@ typedef enum ek_status {
   EK_ERR_NOT_CONVERGED = 3,  /* multigrid hit its cycle cap; phi still returned */
   EK_ERR_NAN = 4,            /* divergence is NaN (reference: STOP 'DIV is a NaN', duct.F90:2811) */
   EK_ERR_TIMEOUT = 5,        /* a bounded device wait expired                   */
-  EK_ERR_STATE = 6           /* call order violated (e.g. step before metrics)  */
+  EK_ERR_STATE = 6,          /* call order violated (e.g. step before metrics)  */
+  EK_ERR_IO = 7              /* restart file missing, unreadable or malformed  */
 } ek_status;
 
 /* Boundary-wall index into the *_bc arrays, in input.dat order
@@ -130,6 +131,28 @@ typedef struct ek_mg_stats {
   double max_residual;       /* largest final ||b-A phi||/||b|| (residual rule)  */
 } ek_mg_stats;
 
+/* Plane statistics of SAVE_STATS_CURVI (flow_statistics.F90:2-1023).  Every
+ * plane is a caller-owned (0:NZ+1, 0:NY+1) array, (NZ+2)*(NY+2) doubles in
+ * the layout of the reference's URMS, UV, ... (K fastest); a NULL plane is
+ * not copied.  Sums over x run over I = 0..NX-1; fluctuations are taken
+ * about DBLE(C*X(0,K,J)), the x-mean.  Planes the reference leaves
+ * unassigned (fresh allocations) are zero. */
+typedef struct ek_stats {
+  double ubulk, vbulk;       /* UBULK, VBULK: cell averages of mode-0 CU3X, CU1X (:80-95)    */
+  double thbulk;             /* the scalar's cell average, printed as THBULK (:540-555)       */
+  double urms_b, vrms_b, wrms_b; /* INT_JACOB-weighted cell averages of URMS.. (:851-879)   */
+  double u3_probe, u1_probe; /* U3X(NXP,2,NY), U1X(NXP,2,NY) of the time_bulk.txt line (:403) */
+  double *urms, *vrms, *wrms;          /* SQRT(SUM (u - <u>)**2 / NX), all K, J            */
+  double *uv, *uw, *wv, *pu, *pv;      /* SUM u'v' / NX etc. on K = 1..NZ (:181-207);
+                                          pu = <w'p'>, pv = <v'p'>, p' about P_MEAN      */
+  double *tke;                         /* TKE: squared mode-0 velocities (:165-174)      */
+  double *dudy, *dwdy, *dudz, *dwdz, *omega_x; /* mode-0 gradients (:216-325)            */
+  double *thrms, *thv, *thw;           /* scalar rms and fluxes (n_th >= 1; :456-503)    */
+  double *dthdy, *dthdz, *rig;         /* scalar gradients, gradient Richardson number   */
+  double *mean_u1, *mean_u2, *mean_u3, *mean_p, *mean_th; /* DBLE(C*X(0,K,J)) after the
+                                          transforms back, as plot_binary writes them   */
+} ek_stats;
+
 /* Field selectors for ekgpu_get_field / ekgpu_put_field. */
 enum {
   EK_F_CU1 = 0, EK_F_CU2, EK_F_CU3, EK_F_CP, EK_F_CTH,   /* state (spectral)   */
@@ -201,6 +224,41 @@ int ekgpu_upload_state(ek_ctx *ctx, const double *cu1, const double *cu2,
                        const double *cu3, const double *cp, const double *cth);
 int ekgpu_download_state(ek_ctx *ctx, double *cu1, double *cu2, double *cu3,
                          double *cp, double *cth);
+
+/* Restart files.  ekgpu_save_flow replaces the file writes of SAVE_FLOW
+ * (diablo.F90:753-837) and BACKUP_FLOW (diablo.F90:841-915); ekgpu_read_flow
+ * the reads of READ_FLOW (diablo.F90:918-1072).  The caller composes the
+ * file names (the reference's last_saved/diablo_001.saved, .res, backup/
+ * diablo_001.saved_mmmm, diablo_th01_001.*), so the Fortran routines keep
+ * their naming and directory logic and pass FNAME and FNAME_TH(N).
+ *
+ * Format: Fortran unformatted sequential, 4-byte record markers in host byte
+ * order, records over 2^31 - 9 bytes split into subrecords (the ifort and
+ * gfortran convention).  flow_path gets the records
+ * [NX NY NZ TIME TIME_STEP] and [CU1X CU2X CU3X CPX]; th_path (may be NULL,
+ * no scalar file) gets [NX NY NZ TIME TIME_STEP] and [CTHX(:,:,:,1)].  The
+ * data stream from HBM through pinned staging with no full host copy.
+ * The environment variable EKGPU_FORTRAN_SUBRECORD=<bytes> lowers the
+ * subrecord limit (to exercise the split on small files).
+ *
+ * Read: flow_path's dimensions must equal the context's (reference: STOP
+ * 'Error: old flowfield wrong dimensions.'; here EK_ERR_IO and the state is
+ * unchanged); th_path NULL skips the scalar (NUM_READ_TH = 0), and is an
+ * error when n_th == 0.  Both files are checked (markers, lengths,
+ * dimensions) before device memory is written, so on any error the state is
+ * left as it was.  TIME and TIME_STEP are taken from the last header read,
+ * CF* are zeroed as by ekgpu_upload_state; IC_TYPE = 7 applies no boundary
+ * conditions after the read (diablo.F90:1062-1069). */
+int ekgpu_save_flow(ek_ctx *ctx, const char *flow_path, const char *th_path);
+int ekgpu_read_flow(ek_ctx *ctx, const char *flow_path, const char *th_path);
+
+/* SAVE_STATS_CURVI (flow_statistics.F90:2-1023) on the resident state:
+ * fills *stats and, as the reference routine does, transforms CU1X, CU2X,
+ * CU3X, CPX, CTHX to physical space and back (which zeroes modes above
+ * NX/3) and zeroes CF1X, CF2X, CF3X (:956-963).  The file output
+ * (plane_data/time_bulk.txt, plot_binary's .pln record) is the caller's;
+ * the TKE budget, the plane dumps and the Tecplot writer are not part of it. */
+int ekgpu_save_stats(ek_ctx *ctx, ek_stats *stats);
 
 /* Read or write one spectral field (EK_F_*) in the CU1X layout. */
 int ekgpu_get_field(ek_ctx *ctx, int field, double *out);
