@@ -59,6 +59,8 @@ int ekref_poisson_batch(ekref_ctx *ctx, const double *rhs, double *phi,
                         const double *kx2, int nprob, ek_mg_stats *stats);
 int ekref_last_divergence(ekref_ctx *ctx, double *div);
 int ekref_last_mg_stats(ekref_ctx *ctx, ek_mg_stats *stats);
+/* SAVE_STATS_CURVI (flow_statistics.F90:2-1023): statistics and state round trip. */
+int ekref_save_stats(ekref_ctx *ctx, ek_stats *stats);
 
 /* Building blocks exposed for unit tests. */
 /* r2c along x of nlines lines of stride nx+2 doubles -> (nx/2+1) complex per

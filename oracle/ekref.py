@@ -13,7 +13,8 @@ import subprocess
 
 import numpy as np
 
-from ekman_bl_gb300.params import EkMetrics, EkMgStats, EkParams, as_ptr, spectral_shape
+from ekman_bl_gb300.params import (EkMetrics, EkMgStats, EkParams, EkStats, as_ptr, spectral_shape, stats_dict,
+                                   stats_struct)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libekref.so")
@@ -58,6 +59,7 @@ def lib():
         L.ekref_fft_c2r.argtypes = [C.c_int, C.c_int, C.c_long, _D, _D]
         L.ekref_thomas_real.argtypes = [C.c_int, C.c_int, _D, _D, _D, _D]
         L.ekref_mg_apply.argtypes = [C.c_void_p, C.c_double, _D, _D]
+        L.ekref_save_stats.argtypes = [C.c_void_p, C.POINTER(EkStats)]
         _lib = L
     return _lib
 
@@ -192,6 +194,12 @@ class Oracle:
         s = EkMgStats()
         lib().ekref_last_mg_stats(self._h, C.byref(s))
         return s.as_dict()
+
+    def save_stats(self) -> dict:
+        """SAVE_STATS_CURVI restated: the statistics and the state round trip."""
+        st, arrs = stats_struct(self.p)
+        self._check(lib().ekref_save_stats(self._h, C.byref(st)))
+        return stats_dict(st, arrs)
 
 
 def fft_r2c(x: np.ndarray, nkx: int) -> np.ndarray:

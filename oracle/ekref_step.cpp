@@ -1137,3 +1137,254 @@ extern "C" int ekref_step(ekref_ctx *c, int nsteps) {
   }
   return EK_OK;
 }
+
+// ---------------------------------------------------------------------------
+// SAVE_STATS_CURVI (flow_statistics.F90:2-1023) with NP = 1 and N_TH <= 1:
+// the plane statistics and the state round trip; the file output
+// (time_bulk.txt, plot_binary, Tecplot, plane dumps) and the TKE budget are
+// left out.  Loops and expression order follow the Fortran; arrays the
+// reference leaves unassigned after ALLOCATE are zero.
+extern "C" int ekref_save_stats(ekref_ctx *c, ek_stats *st) {
+  if (!c->have_metrics) return fail(c, EK_ERR_STATE, "metrics not set");
+  const int NX = c->NX, NY = c->NY, NZ = c->NZ, NZ2 = c->NZ2;
+  const size_t n2 = (size_t)c->NZ2 * c->NY2;
+  const bool th = c->p.n_th > 0;
+  auto pl = [&]() { return std::vector<double>(n2, 0.0); };
+  auto A = [&](std::vector<double> &a, int k, int j) -> double & { return a[(size_t)j * NZ2 + k]; };
+  // CR*X = CU*X (flow_statistics.F90:99-112; the MPI broadcasts are copies)
+  const std::vector<cplx> CR1 = c->CU1, CR2 = c->CU2, CR3 = c->CU3;
+  auto R1 = [&](int k, int j) { return CR1[c->ic(0, k, j)].re; };
+  auto R2 = [&](int k, int j) { return CR2[c->ic(0, k, j)].re; };
+  auto R3 = [&](int k, int j) { return CR3[c->ic(0, k, j)].re; };
+  // UBULK, VBULK (:80-95)
+  double ubulk = 0.0, vbulk = 0.0;
+  for (int J = 1; J <= NY; ++J)
+    for (int K = 1; K <= NZ; ++K) {
+      ubulk = ubulk + 0.25 * (R3(K, J) + R3(K - 1, J) + R3(K - 1, J - 1) + R3(K, J - 1));
+      vbulk = vbulk + 0.25 * (R1(K, J) + R1(K - 1, J) + R1(K - 1, J - 1) + R1(K, J - 1));
+    }
+  const double ncell = (double)(float)(NY * NZ);
+  ubulk = ubulk / ncell;
+  vbulk = vbulk / ncell;
+  std::vector<double> p_mean = pl();
+  for (int k = 1; k <= NZ; ++k)
+    for (int j = 1; j <= NY; ++j) A(p_mean, k, j) = c->CP[c->ic(0, k, j)].re;
+  // to physical space (:156-160); P into the scratch S1
+  to_physical(c, c->CU1, c->U1, 0, NY + 1, 0, NZ + 1);
+  to_physical(c, c->CU2, c->U2, 0, NY + 1, 0, NZ + 1);
+  to_physical(c, c->CU3, c->U3, 0, NY + 1, 0, NZ + 1);
+  to_physical(c, c->CP, c->S1, 0, NY + 1, 0, NZ + 1);
+  const std::vector<double> &U1 = c->U1, &U2 = c->U2, &U3 = c->U3, &PX = c->S1;
+  std::vector<double> tke = pl(), urms = pl(), vrms = pl(), wrms = pl();
+  std::vector<double> uv = pl(), uw = pl(), wv = pl(), pu = pl(), pv = pl();
+  const bool scaled = c->p.amp_omega0 != 0.0;
+  const double fac = scaled ? std::pow(c->p.amp_omega0 / c->p.omega0, -2.0) : 1.0;
+  for (int k = 0; k <= NZ + 1; ++k)
+    for (int j = 0; j <= NY + 1; ++j) {
+      const double e = R1(k, j) * R1(k, j) + R2(k, j) * R2(k, j) + R3(k, j) * R3(k, j);
+      A(tke, k, j) = scaled ? e * fac : e;
+    }
+  const int imax = NX - 1;  // MIN(NXP, NXP_L) on rank 0
+  for (int k = 0; k <= NZ + 1; ++k)
+    for (int j = 0; j <= NY + 1; ++j) {
+      double su = 0.0, sv = 0.0, sw = 0.0;
+      for (int i = 0; i <= imax; ++i) {
+        const double a = U1[c->ip(i, k, j)] - R1(k, j), b = U2[c->ip(i, k, j)] - R2(k, j);
+        const double w = U3[c->ip(i, k, j)] - R3(k, j);
+        su = su + a * a;
+        sv = sv + b * b;
+        sw = sw + w * w;
+      }
+      A(urms, k, j) = su;
+      A(vrms, k, j) = sv;
+      A(wrms, k, j) = sw;
+    }
+  for (int k = 1; k <= NZ; ++k)
+    for (int j = 0; j <= NY + 1; ++j) {
+      double s12 = 0.0, s32 = 0.0, s13 = 0.0, s3p = 0.0, s2p = 0.0;
+      for (int i = 0; i <= imax; ++i) {
+        const size_t q = c->ip(i, k, j);
+        const double a = U1[q] - R1(k, j), b = U2[q] - R2(k, j), w = U3[q] - R3(k, j);
+        const double pp = PX[q] - A(p_mean, k, j);
+        s12 = s12 + a * b;
+        s32 = s32 + w * b;
+        s13 = s13 + a * w;
+        s3p = s3p + w * pp;
+        s2p = s2p + b * pp;
+      }
+      const double nx = (double)(float)NX;
+      A(uv, k, j) = s12 / nx;
+      A(uw, k, j) = s13 / nx;
+      A(wv, k, j) = s32 / nx;
+      A(pu, k, j) = s3p / nx;
+      A(pv, k, j) = s2p / nx;
+    }
+  auto cav = [&](const std::vector<double> &m, int K, int J) {
+    return 0.125 * (c->M3(m, K, J, 1) + c->M3(m, K, J + 1, 1) + c->M3(m, K, J, 2) + c->M3(m, K + 1, J, 2));
+  };
+  std::vector<double> dudy = pl(), dwdy = pl(), dudz = pl(), dwdz = pl(), omx = pl();
+  for (int K = c->ZSTART; K <= c->ZEND; ++K)
+    for (int J = c->JSTART; J <= c->JEND; ++J) {
+      const double a12 = cav(c->cjob_12, K, J), a22 = cav(c->cjob_22, K, J);
+      A(dudy, K, J) = (a12 * (R1(K + 1, J) - R1(K - 1, J)) + a22 * (R1(K, J + 1) - R1(K, J - 1))) / c->JAC(K, J);
+      A(dwdy, K, J) = (a12 * (R3(K + 1, J) - R3(K - 1, J)) + a22 * (R3(K, J + 1) - R3(K, J - 1))) / c->JAC(K, J);
+    }
+  for (int k = 1; k <= NZ; ++k) {
+    A(dudy, k, 0) = A(dudy, k, 1);
+    A(dwdy, k, 0) = A(dwdy, k, 1);
+    A(dudy, k, NY + 1) = A(dudy, k, NY);
+    A(dwdy, k, NY + 1) = A(dwdy, k, NY);
+  }
+  for (int K = 1; K <= NZ; ++K)
+    for (int J = 1; J <= NY; ++J) {
+      const double a21 = cav(c->cjob_21, K, J), a11 = cav(c->cjob_11, K, J);
+      A(dudz, K, J) = (a21 * (R1(K, J + 1) - R1(K, J - 1)) + a11 * (R1(K + 1, J) - R1(K - 1, J))) / c->JAC(K, J);
+      A(dwdz, K, J) = (a21 * (R3(K, J + 1) - R3(K, J - 1)) + a11 * (R3(K + 1, J) - R3(K - 1, J))) / c->JAC(K, J);
+    }
+  for (int k = 1; k <= NZ; ++k) {
+    A(dudz, k, 0) = A(dudz, k, 1);
+    A(dwdz, k, 0) = A(dwdz, k, 1);
+    A(dudz, k, NY + 1) = A(dudz, k, NY);
+    A(dwdz, k, NY + 1) = A(dwdz, k, NY);
+  }
+  for (int j = 1; j <= NY; ++j) {
+    A(dwdz, 1, j) = A(dwdz, 2, j);
+    A(dudz, 1, j) = A(dudz, 2, j);
+  }
+  for (int K = 1; K <= NZ; ++K)
+    for (int J = 1; J <= NY; ++J) {
+      const double a12 = cav(c->cjob_12, K, J), a22 = cav(c->cjob_22, K, J);
+      const double a21 = cav(c->cjob_21, K, J), a11 = cav(c->cjob_11, K, J);
+      A(omx, K, J) = (a12 * (R3(K + 1, J) - R3(K - 1, J)) + a22 * (R3(K, J + 1) - R3(K, J - 1))) / c->JAC(K, J) -
+                     (a21 * (R2(K, J + 1) - R2(K, J - 1)) + a11 * (R2(K + 1, J) - R2(K - 1, J))) / c->JAC(K, J);
+    }
+  for (int k = 1; k <= NZ; ++k) {
+    A(omx, k, 0) = A(omx, k, 1);
+    A(omx, k, NY + 1) = A(omx, k, NY);
+  }
+  // the scalar (:417-555)
+  std::vector<double> thrms = pl(), thv = pl(), thw = pl(), dthdy = pl(), dthdz = pl(), rig = pl();
+  double thbulk = 0.0;
+  if (th) {
+    const std::vector<cplx> CRT = c->CTH;
+    auto T = [&](int k, int j) { return CRT[c->ic(0, k, j)].re; };
+    auto TB = [&](int k, int j) { return c->M2(c->th_bar, k, j); };
+    to_physical(c, c->CTH, c->TH, 0, NY + 1, 0, NZ + 1);
+    const std::vector<double> &THX = c->TH;
+    for (int j = 0; j <= NY + 1; ++j)
+      for (int k = 0; k <= NZ + 1; ++k) {
+        double s = 0.0;
+        for (int i = 0; i <= imax; ++i) {
+          const double a = std::fabs(THX[c->ip(i, k, j)] - T(k, j));
+          s = s + a * a;
+        }
+        A(thrms, k, j) = s;
+      }
+    for (int k = 1; k <= NZ; ++k)
+      for (int j = 1; j <= NY; ++j) {
+        const double a12 = cav(c->cjob_12, k, j), a22 = cav(c->cjob_22, k, j);
+        A(dthdy, k, j) = (a12 * (T(k + 1, j) - T(k - 1, j)) + a22 * (T(k, j + 1) - T(k, j - 1))) / c->JAC(k, j);
+        if (!c->p.cont_strat)
+          A(dthdy, k, j) = A(dthdy, k, j) +
+                           (a12 * (TB(k + 1, j) - TB(k - 1, j)) + a22 * (TB(k, j + 1) - TB(k, j - 1))) / c->JAC(k, j);
+      }
+    for (int j = 1; j <= NY; ++j) {
+      A(dthdy, 0, j) = A(dthdy, 1, j);
+      A(dthdy, NZ + 1, j) = A(dthdy, NZ, j);
+    }
+    for (int k = 0; k <= NZ + 1; ++k) {
+      A(dthdy, k, 0) = 2.0 * A(dthdy, k, 1) - A(dthdy, k, 2);
+      A(dthdy, k, NY + 1) = 2.0 * A(dthdy, k, NY) - A(dthdy, k, NY - 1);
+    }
+    for (int j = 0; j <= NY + 1; ++j)
+      for (int k = 0; k <= NZ + 1; ++k) {
+        double s2 = 0.0, s3 = 0.0;
+        for (int i = 0; i <= imax; ++i) {
+          const size_t q = c->ip(i, k, j);
+          const double t = THX[q] - T(k, j);
+          s2 = s2 + t * (U2[q] - R2(k, j));
+          s3 = s3 + t * (U3[q] - R3(k, j));
+        }
+        A(thv, k, j) = s2 / (double)(float)NX;
+        A(thw, k, j) = s3 / (double)(float)NX;
+      }
+    for (int k = 1; k <= NZ; ++k)
+      for (int j = 1; j <= NY; ++j) {
+        const double a21 = cav(c->cjob_21, k, j), a11 = cav(c->cjob_11, k, j);
+        A(dthdz, k, j) = (a21 * (T(k, j + 1) - T(k, j - 1)) + a11 * (T(k + 1, j) - T(k - 1, j))) / c->JAC(k, j);
+      }
+    for (int j = 1; j <= NY; ++j) {
+      A(dthdz, 0, j) = A(dthdz, 1, j);
+      A(dthdz, NZ + 1, j) = A(dthdz, NZ, j);
+    }
+    for (int k = 0; k <= NZ + 1; ++k) {
+      A(dthdz, k, 0) = 2.0 * A(dthdz, k, 1) - A(dthdz, k, 2);
+      A(dthdz, k, NY + 1) = 2.0 * A(dthdz, k, NY) - A(dthdz, k, NY - 1);
+    }
+    const double ri = c->p.ri_tau;
+    for (int J = 1; J <= NY; ++J)
+      for (int K = 1; K <= NZ; ++K) {
+        thbulk = thbulk + 0.25 * (T(K, J) + T(K - 1, J) + T(K - 1, J - 1) + T(K, J - 1));
+        const double b = c->p.cont_strat ? A(dthdy, K, J) - 1.0 : A(dthdy, K, J);
+        if (A(dwdy, K, J) == 0.0)
+          A(rig, K, J) = -ri * b * 1.0e18;
+        else
+          A(rig, K, J) = -ri * b / (A(dwdy, K, J) * A(dwdy, K, J) + A(dudy, K, J) * A(dudy, K, J));
+      }
+    thbulk = thbulk / ncell;
+    to_fourier(c, c->TH, c->CTH, 0, NY + 1, 0, NZ + 1);  // REAL_FOURIER_TRANS_TH(.true.) (:821)
+  }
+  // rms and their bulk averages (:846-879), scalar rms (:914-920)
+  double ub = 0.0, vb = 0.0, wb = 0.0, area = 0.0;
+  for (int k = 0; k <= NZ + 1; ++k)
+    for (int j = 0; j <= NY + 1; ++j) {
+      A(urms, k, j) = std::sqrt(A(urms, k, j) / (double)NX);
+      A(vrms, k, j) = std::sqrt(A(vrms, k, j) / (double)NX);
+      A(wrms, k, j) = std::sqrt(A(wrms, k, j) / (double)NX);
+    }
+  for (int k = 1; k <= NZ; ++k)
+    for (int j = 1; j <= NY; ++j) {
+      const double J = c->JAC(k, j);
+      area = area + J;
+      ub = ub + 0.25 * (A(urms, k, j) + A(urms, k, j - 1) + A(urms, k - 1, j) + A(urms, k - 1, j - 1)) * J;
+      vb = vb + 0.25 * (A(vrms, k, j) + A(vrms, k, j - 1) + A(vrms, k - 1, j) + A(vrms, k - 1, j - 1)) * J;
+      wb = wb + 0.25 * (A(wrms, k, j) + A(wrms, k, j - 1) + A(wrms, k - 1, j) + A(wrms, k - 1, j - 1)) * J;
+    }
+  if (th)
+    for (int j = 0; j <= NY + 1; ++j)
+      for (int k = 0; k <= NZ + 1; ++k) A(thrms, k, j) = std::sqrt(A(thrms, k, j) / (double)(float)NX);
+  // back to Fourier space and CF1X..CF3X = 0 (:951-963)
+  to_fourier(c, c->U1, c->CU1, 0, NY + 1, 0, NZ + 1);
+  to_fourier(c, c->U2, c->CU2, 0, NY + 1, 0, NZ + 1);
+  to_fourier(c, c->U3, c->CU3, 0, NY + 1, 0, NZ + 1);
+  to_fourier(c, c->S1, c->CP, 0, NY + 1, 0, NZ + 1);
+  for (auto *f : {&c->CF1, &c->CF2, &c->CF3}) std::fill(f->begin(), f->end(), cplx{0.0, 0.0});
+  std::vector<double> m1 = pl(), m2 = pl(), m3 = pl(), mp = pl(), mt = pl();
+  for (int k = 0; k <= NZ + 1; ++k)
+    for (int j = 0; j <= NY + 1; ++j) {
+      A(m1, k, j) = c->CU1[c->ic(0, k, j)].re;
+      A(m2, k, j) = c->CU2[c->ic(0, k, j)].re;
+      A(m3, k, j) = c->CU3[c->ic(0, k, j)].re;
+      A(mp, k, j) = c->CP[c->ic(0, k, j)].re;
+      A(mt, k, j) = th ? c->CTH[c->ic(0, k, j)].re : 0.0;
+    }
+  st->ubulk = ubulk;
+  st->vbulk = vbulk;
+  st->thbulk = thbulk;
+  st->urms_b = ub / area;
+  st->vrms_b = vb / area;
+  st->wrms_b = wb / area;
+  st->u3_probe = U3[c->ip(NX + 1, 2, NY)];
+  st->u1_probe = U1[c->ip(NX + 1, 2, NY)];
+  auto out = [&](double *dst, const std::vector<double> &src) {
+    if (dst) std::copy(src.begin(), src.end(), dst);
+  };
+  out(st->urms, urms); out(st->vrms, vrms); out(st->wrms, wrms);
+  out(st->uv, uv); out(st->uw, uw); out(st->wv, wv); out(st->pu, pu); out(st->pv, pv);
+  out(st->tke, tke); out(st->dudy, dudy); out(st->dwdy, dwdy); out(st->dudz, dudz); out(st->dwdz, dwdz);
+  out(st->omega_x, omx);
+  out(st->thrms, thrms); out(st->thv, thv); out(st->thw, thw); out(st->dthdy, dthdy); out(st->dthdz, dthdz);
+  out(st->rig, rig);
+  out(st->mean_u1, m1); out(st->mean_u2, m2); out(st->mean_u3, m3); out(st->mean_p, mp); out(st->mean_th, mt);
+  return EK_OK;
+}
