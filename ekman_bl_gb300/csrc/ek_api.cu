@@ -9,11 +9,17 @@
 #include <new>
 
 #include "ek_internal.h"
+#include "ek_unet.h"
 
 using namespace ek;
 
 struct ek_ctx {
   Ctx c;
+};
+
+struct ek_unet {
+  std::unique_ptr<ek::UNet> net;
+  std::string err;
 };
 
 namespace ek {
@@ -102,6 +108,8 @@ void run_rem_div(Ctx &c, double temp4, bool update_p, int *mg_status) {
   const int P = 2 * (c.d.NKX + 1);
   launch_divergence_rhs(c, c.mgw.rhs[c.mg.ngrid - 1], P);
   *mg_status = mg_solve(c, P, c.mgw.kx2, c.mg_kx2_host.data(), nullptr);
+  if (c.guess.sink_x)
+    guess_collect(c, P, c.mgw.rhs[c.mg.ngrid - 1], c.mgw.phif, c.mgw.kx2, c.mg_kx2_host, c.stream);
   launch_projection(c, c.mgw.phif, P, temp4, update_p);
 }
 
@@ -434,6 +442,7 @@ void ekgpu_destroy(ek_ctx *h) {
   if (c.mg_cof_pool) cudaFree(c.mg_cof_pool);
   mg_work_free(c.mgw);
   mg_work_free(c.mgs);
+  guess_free(c);
   if (c.mgf_pool) cudaFree(c.mgf_pool);
   if (c.mg.ops_dev) cudaFree(c.mg.ops_dev);
   c.poll.destroy();
@@ -726,7 +735,7 @@ long long ekgpu_launch_count(const ek_ctx *h) { return h ? h->c.launches : -1; }
 
 static const char *kKClassNames[KC_N] = {"spectral_rhs", "fft_c2r", "fft_r2c", "face_velocity", "adi_y", "adi_z",
                                          "mg_relax", "mg_coarse", "mg_transfer", "mg_check", "mg_setup",
-                                         "projection", "divergence"};
+                                         "projection", "divergence", "guess"};
 
 const char *ekgpu_timing_class_name(int k) { return (k >= 0 && k < KC_N) ? kKClassNames[k] : ""; }
 
@@ -752,3 +761,174 @@ int ekgpu_get_timing(ek_ctx *h, double *ms, long long *count, double *bytes, int
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Learned Poisson initial guess: the network object and its use in the solves.
+namespace {
+template <typename F>
+int unet_guarded(ek_unet *u, F &&f) {
+  if (!u || !u->net) return EK_ERR_ARG;
+  try {
+    return f(*u->net);
+  } catch (const CudaError &e) {
+    u->err = e.msg;
+    return EK_ERR_CUDA;
+  } catch (const std::bad_alloc &) {
+    u->err = "host allocation failed";
+    return EK_ERR_CUDA;
+  }
+}
+}  // namespace
+
+int ekgpu_unet_create(int cin, int channels, int max_batch, int h, int w, ek_unet **out) {
+  if (!out) return EK_ERR_ARG;
+  *out = nullptr;
+  if (cin < 1 || channels < 1 || channels > 64 || max_batch < 1 || h < 8 || w < 8 || h % 8 || w % 8)
+    return EK_ERR_ARG;
+  ek_unet *u = new (std::nothrow) ek_unet;
+  if (!u) return EK_ERR_CUDA;
+  try {
+    u->net.reset(new ek::UNet(cin, channels, max_batch, h, w));
+  } catch (const CudaError &) {
+    delete u;
+    return EK_ERR_CUDA;
+  }
+  *out = u;
+  return EK_OK;
+}
+
+void ekgpu_unet_destroy(ek_unet *u) { delete u; }
+
+const char *ekgpu_unet_last_error(const ek_unet *u) { return u ? u->err.c_str() : "null network"; }
+
+long ekgpu_unet_num_params(const ek_unet *u) { return (u && u->net) ? u->net->nparams() : -1; }
+
+int ekgpu_unet_set_params(ek_unet *u, const float *params) {
+  return unet_guarded(u, [&](ek::UNet &n) {
+    if (!params) return (int)EK_ERR_ARG;
+    n.set_params(params);
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_unet_get_params(ek_unet *u, float *params) {
+  return unet_guarded(u, [&](ek::UNet &n) {
+    if (!params) return (int)EK_ERR_ARG;
+    n.get_params(params);
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_unet_forward(ek_unet *u, const float *x_dev, int n, float *y_dev, void *stream) {
+  return unet_guarded(u, [&](ek::UNet &net) {
+    if (!x_dev || !y_dev || n < 1 || n > net.max_n) return (int)EK_ERR_ARG;
+    net.forward(x_dev, n, y_dev, (cudaStream_t)stream);
+    EK_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_unet_train_step(ek_unet *u, const float *x_dev, const float *t_dev, int n, int hv, int wv, double lr,
+                          double *loss, void *stream) {
+  return unet_guarded(u, [&](ek::UNet &net) {
+    if (!x_dev || !t_dev || n < 1 || n > net.max_n || hv < 1 || hv > net.h || wv < 1 || wv > net.w)
+      return (int)EK_ERR_ARG;
+    const double l = net.train_step(x_dev, t_dev, n, hv, wv, lr, (cudaStream_t)stream);
+    if (loss) *loss = l;
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_unet_gradient(ek_unet *u, const float *x_dev, const float *t_dev, int n, int hv, int wv, double *loss,
+                        float *y_dev, float *grad_host, void *stream) {
+  return unet_guarded(u, [&](ek::UNet &net) {
+    if (!x_dev || !t_dev || n < 1 || n > net.max_n || hv < 1 || hv > net.h || wv < 1 || wv > net.w)
+      return (int)EK_ERR_ARG;
+    const double l = net.forward_backward(x_dev, t_dev, n, hv, wv, y_dev, (cudaStream_t)stream);
+    if (loss) *loss = l;
+    if (grad_host)
+      EK_CUDA(cudaMemcpy(grad_host, net.grads(), sizeof(float) * net.nparams(), cudaMemcpyDeviceToHost));
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_guess_geometry(ek_ctx *h, int factor, int *hh, int *ww, int *hv, int *wv) {
+  return guarded(h, [&](Ctx &c) {
+    if (factor < 1 || !hh || !ww || !hv || !wv) return fail(c, EK_ERR_ARG, "bad guess geometry arguments");
+    guess_geometry(c, factor, *hh, *ww, *hv, *wv);
+    return (int)EK_OK;
+  });
+}
+
+static int set_guess_factor(Ctx &c, int factor) {
+  GuessState &G = c.guess;
+  if (G.factor != 0 && G.factor != factor && ((G.sink_x && G.sink_count > 0) || (G.use && G.net)))
+    return fail(c, EK_ERR_STATE, "the guess and the pair sink need the same factor");
+  int h, w, hv, wv;
+  guess_geometry(c, factor, h, w, hv, wv);
+  if (G.factor != factor) G.cap = 0;  // buffers are sized per image
+  G.factor = factor;
+  G.h = h;
+  G.w = w;
+  G.hv = hv;
+  G.wv = wv;
+  return EK_OK;
+}
+
+int ekgpu_set_poisson_guess(ek_ctx *h, ek_unet *net, int factor) {
+  return guarded(h, [&](Ctx &c) {
+    GuessState &G = c.guess;
+    if (!net) {
+      G.use = false;
+      G.net = nullptr;
+      return (int)EK_OK;
+    }
+    if (!net->net || factor < 1) return fail(c, EK_ERR_ARG, "bad network or factor");
+    if (!c.p.mg_fast) return fail(c, EK_ERR_STATE, "the learned guess needs mg_fast = 1");
+    G.use = false;
+    G.net = nullptr;
+    const int st = set_guess_factor(c, factor);
+    if (st != EK_OK) return st;
+    if (net->net->h != G.h || net->net->w != G.w || net->net->cin != 2)
+      return fail(c, EK_ERR_ARG, "network image size or input channels do not match the guess geometry");
+    G.net = net->net.get();
+    G.use = true;
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_set_pair_sink(ek_ctx *h, float *x_dev, float *t_dev, int capacity, int factor) {
+  return guarded(h, [&](Ctx &c) {
+    GuessState &G = c.guess;
+    if (!x_dev || !t_dev || capacity < 1) {
+      G.sink_x = G.sink_t = nullptr;
+      G.sink_cap = G.sink_count = 0;
+      return (int)EK_OK;
+    }
+    if (factor < 1) return fail(c, EK_ERR_ARG, "factor < 1");
+    G.sink_x = nullptr;
+    G.sink_count = 0;
+    const int st = set_guess_factor(c, factor);
+    if (st != EK_OK) return st;
+    G.sink_x = x_dev;
+    G.sink_t = t_dev;
+    G.sink_cap = capacity;
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_pair_count(ek_ctx *h, int *count) {
+  return guarded(h, [&](Ctx &c) {
+    if (!count) return fail(c, EK_ERR_ARG, "count is NULL");
+    *count = c.guess.sink_count;
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_last_guess_stats(ek_ctx *h, double *mean_rho, double *mean_cycles) {
+  return guarded(h, [&](Ctx &c) {
+    if (mean_rho) *mean_rho = c.guess.last_rho;
+    if (mean_cycles) *mean_cycles = c.last_mean_cycles;
+    return (int)EK_OK;
+  });
+}

@@ -151,7 +151,7 @@ struct MgPlan {
 // Kernel classes for the optional per-kernel timer (ekgpu_set_timing).
 enum KClass {
   KC_SPECTRAL = 0, KC_C2R, KC_R2C, KC_FACE, KC_ADI_Y, KC_ADI_Z, KC_MG_RELAX, KC_MG_COARSE,
-  KC_MG_TRANSFER, KC_MG_CHECK, KC_MG_SETUP, KC_PROJECTION, KC_DIVERGENCE, KC_N
+  KC_MG_TRANSFER, KC_MG_CHECK, KC_MG_SETUP, KC_PROJECTION, KC_DIVERGENCE, KC_GUESS, KC_N
 };
 struct TimerRec {
   int cls;
@@ -192,6 +192,27 @@ struct StopPoll {
     cudaEventSynchronize(ev[k1]);
     return host[k1] != 0;
   }
+};
+
+class UNet;
+// Learned initial guess of the Poisson problems (ek_guess.cu): the network
+// (owned by the caller), the image geometry, work buffers, and the optional
+// sink that collects (input, target) training pairs after each solve.
+struct GuessState {
+  UNet *net = nullptr;
+  bool use = false;
+  int factor = 0, h = 0, w = 0, hv = 0, wv = 0;
+  float *x = nullptr, *y = nullptr;
+  double *ss = nullptr;
+  int *idx = nullptr;
+  int cap = 0;
+  std::vector<int> idx_host;
+  float *alpha = nullptr;
+  int alpha_cap = 0;
+  float *sink_x = nullptr, *sink_t = nullptr;
+  int sink_cap = 0, sink_count = 0;
+  long long calls = 0;
+  double last_rho = 1.0;  // mean residual ratio |b - A g|/|b| of the last guess
 };
 
 struct Ctx {
@@ -237,6 +258,7 @@ struct Ctx {
   float *mgf_cfh = nullptr, *mgf_cfl = nullptr;  // float-float finest coefficients
   int mgf_pmax = 0;
   ek_mg_stats last_stats{};
+  double last_mean_cycles = 0.0;  // mixed solver: mean corrections over the kx^2 != 0 problems
   StopPoll poll;
   cudaStream_t aux_stream = nullptr;  // the kx^2 = 0 batch runs here, beside the FP32 cycles
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -247,6 +269,7 @@ struct Ctx {
   // the metrics the dt-dependent ADI factors are built from
   double *cfl_dt = nullptr;
   std::vector<double> h_jac, h_g11, h_g22;
+  GuessState guess;
   // SAVE_STATS_CURVI planes and sums (ek_stats.cu)
   double *stats_buf = nullptr;
   // divergence check
@@ -364,6 +387,13 @@ int save_flow(Ctx &c, const char *flow_path, const char *th_path);
 int read_flow(Ctx &c, const char *flow_path, const char *th_path);
 // plane statistics (ek_stats.cu): SAVE_STATS_CURVI's reductions and its state round trip
 int save_stats(Ctx &c, ek_stats *out);
+// learned guess (ek_guess.cu)
+void guess_geometry(const Ctx &c, int f, int &h, int &w, int &hv, int &wv);
+void guess_predict(Ctx &c, int P, const double *rhs, const double *kx2_dev, const std::vector<int> &nonsing,
+                   float *phh, cudaStream_t s);
+void guess_collect(Ctx &c, int P, const double *rhs, const double *phi, const double *kx2_dev,
+                   const std::vector<double> &kx2_host, cudaStream_t s);
+void guess_free(Ctx &c);
 
 #define EK_CUDA(call)                                                                  \
   do {                                                                                 \

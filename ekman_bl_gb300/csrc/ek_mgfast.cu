@@ -25,6 +25,7 @@
 #include <algorithm>
 
 #include "ek_internal.h"
+#include "ek_unet.h"
 
 namespace ek {
 
@@ -109,6 +110,54 @@ __global__ void __launch_bounds__(32 * kRY) k_f_resid_ff(FastDev g) {
     atomicAdd(&g.red[6 * p], (double)sb);
     atomicAdd(&g.red[6 * p + 1], (double)sr);
   }
+}
+
+// Learned initial guess: after k_f_resid_ff on the unscaled guess g
+// (r = b - A g), <r, b> per problem; then the least-squares factor
+// alpha = <A g, b> / |A g|^2 = (|b|^2 - <r,b>) / (|b|^2 - 2<r,b> + |r|^2),
+// the residual ratio it leaves, |b - alpha A g| / |b|, in red[6p+5], and the
+// accumulators cleared for the iteration.
+__global__ void __launch_bounds__(32 * kRY) k_f_guess_rb(FastDev g) {
+  const int P = g.P;
+  const int p = blockIdx.x * 32 + threadIdx.x;
+  const int ty = threadIdx.y;
+  const int nx = g.nfx, j = 1 + (int)blockIdx.y;
+  const LvF &F = g.lv[g.ngrid - 1];
+  float s = 0.f;
+  const bool act = (p < P) && !g.done[p];
+  if (act)
+    for (int i = 1 + ty; i <= nx; i += kRY) {
+      const size_t pt = (size_t)(j - 1) * nx + (i - 1);
+      s = fmaf(F.r[pt * P + p], g.bh[pt * P + p], s);
+    }
+  __shared__ float red[kRY][32];
+  red[ty][threadIdx.x] = s;
+  __syncthreads();
+  if (ty == 0 && act) {
+    for (int y = 1; y < kRY; ++y) s += red[y][threadIdx.x];
+    atomicAdd(&g.red[6 * p + 2], (double)s);
+  }
+}
+
+__global__ void k_f_guess_alpha(FastDev g, float *alpha) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < g.P; p += gridDim.x * blockDim.x) {
+    double a = 0.0;
+    if (!g.done[p]) {
+      const double bb = g.red[6 * p], rr = g.red[6 * p + 1], rb = g.red[6 * p + 2];
+      const double num = bb - rb, den = bb - 2.0 * rb + rr;
+      if (den > 0.0) a = num / den;
+      const double rho2 = bb > 0.0 ? (bb - a * num) / bb : 0.0;
+      g.red[6 * p + 5] = sqrt(fmax(rho2, 0.0));
+    }
+    alpha[p] = (float)a;
+    for (int k = 0; k < 4; ++k) g.red[6 * p + k] = 0.0;
+  }
+}
+
+__global__ void k_f_guess_scale(FastDev g, const float *alpha) {
+  const size_t n = (size_t)(g.nfx + 2) * (g.nfy + 2) * g.P;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    g.phh[t] *= alpha[t % g.P];
 }
 
 // float-float rhs from the FP64 one (once per solve)
@@ -865,6 +914,32 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
   }
   const int gx = (nprob + 31) / 32;
   const unsigned pch = (unsigned)gx;  // 32-problem chunks of the row kernels
+  // learned initial guess for the kx^2 != 0 problems, scaled by the
+  // least-squares factor (a useless guess gets a factor near zero)
+  const bool guessed = c.guess.net && c.guess.use && nprob > ns;
+  if (guessed) {
+    GuessState &G = c.guess;
+    KScope ks(c, KC_GUESS, G.net->forward_flops(nprob - ns));
+    std::vector<int> nonsing;
+    for (int p = 0; p < nprob; ++p)
+      if (!is_sing[p]) nonsing.push_back(p);
+    guess_predict(c, nprob, g.rhs, kx2_dev, nonsing, g.phh, s);
+    if (G.alpha_cap < nprob) {
+      cudaFree(G.alpha);
+      G.alpha = nullptr;
+      G.alpha_cap = 0;
+      EK_CUDA(cudaMalloc(&G.alpha, sizeof(float) * nprob));
+      G.alpha_cap = nprob;
+    }
+    k_f_resid_ff<<<dim3(pch, PL.nfy + 2), dim3(32, kRY), 0, s>>>(g);
+    after_launch(c);
+    k_f_guess_rb<<<dim3(pch, PL.nfy), dim3(32, kRY), 0, s>>>(g);
+    after_launch(c);
+    k_f_guess_alpha<<<nb(nprob, 128), 128, 0, s>>>(g, G.alpha);
+    after_launch(c);
+    k_f_guess_scale<<<nb((long)(PL.nfx + 2) * (PL.nfy + 2) * nprob, bs), bs, 0, s>>>(g, G.alpha);
+    after_launch(c);
+  }
 
   // one partitioned line launch: lines l0, l0+lstep, ... (nline of them)
   // of length n, all problems
@@ -992,13 +1067,18 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
   S.n_not_converged = Ss.n_not_converged;
   S.max_relchange = Ss.max_relchange;
   S.max_residual = Ss.max_residual;
+  double csum = 0.0, rsum = 0.0;
   for (int p = 0; p < nprob; ++p) {
     if (is_sing[p]) continue;
     S.min_cycles = std::min(S.min_cycles, cyc[p]);
     S.max_cycles = std::max(S.max_cycles, cyc[p]);
     if (done[p] != 1) S.n_not_converged++;
     S.max_residual = std::max(S.max_residual, meas[6 * p + 4]);
+    csum += cyc[p];
+    rsum += guessed ? meas[6 * p + 5] : 1.0;
   }
+  c.last_mean_cycles = (nprob > ns) ? csum / (nprob - ns) : 0.0;
+  c.guess.last_rho = (nprob > ns) ? rsum / (nprob - ns) : 1.0;
   c.last_stats = S;
   if (st) *st = S;
   return S.n_not_converged ? EK_ERR_NOT_CONVERGED : EK_OK;

@@ -31,6 +31,10 @@ EXPORTS = [
     "ekgpu_fft_x_to_fourier", "ekgpu_fft_x_to_physical", "ekgpu_fft_x_to_fourier_noalloc",
     "ekgpu_sponge_profiles", "ekgpu_set_sponge", "ekgpu_set_time", "ekgpu_get_time",
     "ekgpu_save_flow", "ekgpu_read_flow", "ekgpu_save_stats",
+    "ekgpu_unet_create", "ekgpu_unet_destroy", "ekgpu_unet_last_error", "ekgpu_unet_num_params",
+    "ekgpu_unet_set_params", "ekgpu_unet_get_params", "ekgpu_unet_forward", "ekgpu_unet_train_step",
+    "ekgpu_unet_gradient", "ekgpu_guess_geometry", "ekgpu_set_poisson_guess", "ekgpu_set_pair_sink",
+    "ekgpu_pair_count", "ekgpu_last_guess_stats",
 ]
 
 
@@ -72,6 +76,24 @@ def load_library():
     L.ekgpu_save_flow.argtypes = [V, C.c_char_p, C.c_char_p]
     L.ekgpu_read_flow.argtypes = [V, C.c_char_p, C.c_char_p]
     L.ekgpu_save_stats.argtypes = [V, C.POINTER(EkStats)]
+    F = C.POINTER(C.c_float)
+    L.ekgpu_unet_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(V)]
+    L.ekgpu_unet_destroy.argtypes = [V]
+    L.ekgpu_unet_destroy.restype = None
+    L.ekgpu_unet_last_error.argtypes = [V]
+    L.ekgpu_unet_last_error.restype = C.c_char_p
+    L.ekgpu_unet_num_params.argtypes = [V]
+    L.ekgpu_unet_num_params.restype = C.c_long
+    L.ekgpu_unet_set_params.argtypes = [V, F]
+    L.ekgpu_unet_get_params.argtypes = [V, F]
+    L.ekgpu_unet_forward.argtypes = [V, V, C.c_int, V, V]
+    L.ekgpu_unet_train_step.argtypes = [V, V, V, C.c_int, C.c_int, C.c_int, C.c_double, _D, V]
+    L.ekgpu_unet_gradient.argtypes = [V, V, V, C.c_int, C.c_int, C.c_int, _D, V, F, V]
+    L.ekgpu_guess_geometry.argtypes = [V, C.c_int] + [C.POINTER(C.c_int)] * 4
+    L.ekgpu_set_poisson_guess.argtypes = [V, V, C.c_int]
+    L.ekgpu_set_pair_sink.argtypes = [V, V, V, C.c_int, C.c_int]
+    L.ekgpu_pair_count.argtypes = [V, C.POINTER(C.c_int)]
+    L.ekgpu_last_guess_stats.argtypes = [V, _D, _D]
     L.ekgpu_get_field.argtypes = [V, C.c_int, _D]
     L.ekgpu_put_field.argtypes = [V, C.c_int, _D]
     L.ekgpu_rk_substep.argtypes = [V, C.c_int]
@@ -279,6 +301,37 @@ class DuctSolver:
             out["files"] = write_stats_files(root, time, dt, step, every, xpoint, ypoint, th_bar, out)
         return out
 
+    # -- learned initial guess of the Poisson problems ----------------------------
+    def guess_geometry(self, factor: int):
+        """(h, w, hv, wv): the network image size and its valid part."""
+        v = [C.c_int() for _ in range(4)]
+        self._check(self._L.ekgpu_guess_geometry(self._h, factor, *[C.byref(x) for x in v]))
+        return tuple(x.value for x in v)
+
+    def set_poisson_guess(self, net, factor: int = 4):
+        """Start the kx^2 != 0 problems of each mixed solve from net's
+        prediction (None: from zero)."""
+        self._guess_net = net
+        self._check(self._L.ekgpu_set_poisson_guess(self._h, None if net is None else net.handle, factor))
+
+    def set_pair_sink(self, x_ptr: int | None, t_ptr: int | None, capacity: int = 0, factor: int = 4):
+        """Collect (input [h][w][2], target [h][w]) FP32 pairs into device
+        buffers after each projection solve; None stops."""
+        self._check(self._L.ekgpu_set_pair_sink(self._h, C.c_void_p(x_ptr or 0), C.c_void_p(t_ptr or 0),
+                                                capacity, factor))
+
+    def pair_count(self) -> int:
+        n = C.c_int()
+        self._check(self._L.ekgpu_pair_count(self._h, C.byref(n)))
+        return n.value
+
+    def last_guess_stats(self):
+        """(mean |b - A g|/|b| after the scaled guess, mean corrections) of
+        the last mixed solve, over the kx^2 != 0 problems."""
+        r, m = C.c_double(), C.c_double()
+        self._check(self._L.ekgpu_last_guess_stats(self._h, C.byref(r), C.byref(m)))
+        return r.value, m.value
+
     def get_field(self, f: int):
         a = np.zeros(spectral_shape(self.p), np.complex128)
         self._check(self._L.ekgpu_get_field(self._h, f, as_ptr(a)))
@@ -356,3 +409,70 @@ def fft_x(forward: bool, nx: int, nkx: int, nlines: int, in_ptr: int, out_ptr: i
     st = fn(nx, nkx, nlines, C.c_void_p(in_ptr), C.c_void_p(out_ptr), C.c_void_p(stream_ptr or 0))
     if st:
         raise EkError(st, L.ekgpu_last_error(None).decode())
+
+
+class UNet:
+    """The learned-guess network (ekgpu_unet_*): device images are given by
+    address (e.g. torch CUDA tensors' data_ptr()), FP32 NHWC."""
+
+    def __init__(self, cin: int, channels: int, max_batch: int, h: int, w: int):
+        self._L = load_library()
+        hdl = C.c_void_p()
+        st = self._L.ekgpu_unet_create(cin, channels, max_batch, h, w, C.byref(hdl))
+        if st:
+            raise EkError(st, "ekgpu_unet_create")
+        self._h = hdl
+        self.cin, self.channels, self.max_batch, self.h, self.w = cin, channels, max_batch, h, w
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, st):
+        if st:
+            raise EkError(st, self._L.ekgpu_unet_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._L.ekgpu_unet_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def nparams(self) -> int:
+        return int(self._L.ekgpu_unet_num_params(self._h))
+
+    def set_params(self, params: np.ndarray):
+        a = np.ascontiguousarray(params, np.float32)
+        assert a.size == self.nparams()
+        self._check(self._L.ekgpu_unet_set_params(self._h, a.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def get_params(self) -> np.ndarray:
+        a = np.zeros(self.nparams(), np.float32)
+        self._check(self._L.ekgpu_unet_get_params(self._h, a.ctypes.data_as(C.POINTER(C.c_float))))
+        return a
+
+    def forward(self, x_ptr: int, n: int, y_ptr: int, stream: int | None = None):
+        self._check(self._L.ekgpu_unet_forward(self._h, C.c_void_p(x_ptr), n, C.c_void_p(y_ptr),
+                                               C.c_void_p(stream or 0)))
+
+    def train_step(self, x_ptr: int, t_ptr: int, n: int, hv: int, wv: int, lr: float,
+                   stream: int | None = None) -> float:
+        loss = C.c_double()
+        self._check(self._L.ekgpu_unet_train_step(self._h, C.c_void_p(x_ptr), C.c_void_p(t_ptr), n, hv, wv, lr,
+                                                  C.byref(loss), C.c_void_p(stream or 0)))
+        return loss.value
+
+    def gradient(self, x_ptr: int, t_ptr: int, n: int, hv: int, wv: int, y_ptr: int | None = None,
+                 stream: int | None = None):
+        """(loss, flat parameter gradient) without an update."""
+        loss = C.c_double()
+        g = np.zeros(self.nparams(), np.float32)
+        self._check(self._L.ekgpu_unet_gradient(self._h, C.c_void_p(x_ptr), C.c_void_p(t_ptr), n, hv, wv,
+                                                C.byref(loss), C.c_void_p(y_ptr or 0),
+                                                g.ctypes.data_as(C.POINTER(C.c_float)), C.c_void_p(stream or 0)))
+        return loss.value, g

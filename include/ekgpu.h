@@ -260,6 +260,53 @@ int ekgpu_read_flow(ek_ctx *ctx, const char *flow_path, const char *th_path);
  * the TKE budget, the plane dumps and the Tecplot writer are not part of it. */
 int ekgpu_save_stats(ek_ctx *ctx, ek_stats *stats);
 
+/* ---- Learned initial guess of the per-kx Poisson problems -------------------
+ * (No counterpart in the reference: its solves always start from zero.)
+ *
+ * A U-Net (4 levels of two 3x3 convolutions + ReLU, `channels` channels at
+ * every level, 2x2 average pooling, nearest upsampling, skip connections,
+ * a final 3x3 convolution to one channel) with BF16 tensor-core kernels and
+ * FP32 accumulation, trained on the GPU with Adam.  Images are h x w
+ * (multiples of 8), cin input channels, FP32 NHWC on the device.  Parameter
+ * layout: for each of the 15 convolutions in network order (encoder levels
+ * 0..3, decoder levels 2, 1, 0, output), W[cout][9][cin] then b[cout]
+ * (tap = 3*(dy+1) + (dx+1)).  The multigrid stays the solver and the judge
+ * of convergence: the guess only sets the starting iterate, scaled by the
+ * least-squares factor, and the tolerance is unchanged. */
+typedef struct ek_unet ek_unet;
+int ekgpu_unet_create(int cin, int channels, int max_batch, int h, int w, ek_unet **net);
+void ekgpu_unet_destroy(ek_unet *net);
+const char *ekgpu_unet_last_error(const ek_unet *net);
+long ekgpu_unet_num_params(const ek_unet *net);
+int ekgpu_unet_set_params(ek_unet *net, const float *params);   /* host; resets Adam */
+int ekgpu_unet_get_params(ek_unet *net, float *params);         /* host               */
+/* y[n][h][w] = net(x[n][h][w][cin]); device pointers; stream may be NULL */
+int ekgpu_unet_forward(ek_unet *net, const float *x_dev, int n, float *y_dev, void *stream);
+/* one Adam step (beta 0.9/0.999, eps 1e-8) on the mean-square error against
+ * t[n][h][w] over the top-left hv x wv pixels of each image */
+int ekgpu_unet_train_step(ek_unet *net, const float *x_dev, const float *t_dev, int n, int hv, int wv,
+                          double lr, double *loss, void *stream);
+/* forward and backward without an update: loss, prediction (y_dev may be
+ * NULL) and the parameter gradient copied to grad_host (may be NULL) */
+int ekgpu_unet_gradient(ek_unet *net, const float *x_dev, const float *t_dev, int n, int hv, int wv,
+                        double *loss, float *y_dev, float *grad_host, void *stream);
+/* Image geometry of the guess at averaging factor f: the finest multigrid
+ * grid (NZ+2 across, NY+2 down) averaged over f x f blocks is hv x wv,
+ * padded to h x w. */
+int ekgpu_guess_geometry(ek_ctx *ctx, int factor, int *h, int *w, int *hv, int *wv);
+/* Use net (cin = 2: scaled right-hand side, log(1 + kx^2 J)/8) as the
+ * starting iterate of the kx^2 != 0 problems (mg_fast = 1); NULL turns it off.
+ * The caller keeps the network alive while it is set. */
+int ekgpu_set_poisson_guess(ek_ctx *ctx, ek_unet *net, int factor);
+/* After each projection solve, append (input [h][w][2], target [h][w]) pairs
+ * of the kx^2 != 0 problems to the caller's device buffers, at most capacity
+ * pairs; NULL pointers stop collecting. */
+int ekgpu_set_pair_sink(ek_ctx *ctx, float *x_dev, float *t_dev, int capacity, int factor);
+int ekgpu_pair_count(ek_ctx *ctx, int *count);
+/* Last mixed solve: mean of |b - A g|/|b| after the scaled guess (1 without
+ * a guess) and mean number of corrections, over the kx^2 != 0 problems. */
+int ekgpu_last_guess_stats(ek_ctx *ctx, double *mean_rho, double *mean_cycles);
+
 /* Read or write one spectral field (EK_F_*) in the CU1X layout. */
 int ekgpu_get_field(ek_ctx *ctx, int field, double *out);
 int ekgpu_put_field(ek_ctx *ctx, int field, const double *in);
