@@ -205,6 +205,53 @@ def replica_throughput(ms: float, steps: int, device: str = "cuda"):
     return world * steps / (ms_max / 1000.0), ms_max
 
 
+LEARN_FACTOR, LEARN_CHANNELS, LEARN_STEPS, LEARN_ITERS = 4, 32, 3, 300
+
+
+def run_learned(solver, stream, args):
+    """The learned initial guess on the same solver: collect (rhs, solution)
+    pairs from LEARN_STEPS steps of its own projections, train the U-Net on
+    the GPU, then time the same steps with and without the guess.  Returns
+    the measurements (the multigrid tolerance is the same in both)."""
+    import torch
+
+    from ekman_bl_gb300.learned import LearnedGuess
+
+    t0 = time.perf_counter()
+    lg = LearnedGuess(solver, factor=LEARN_FACTOR, channels=LEARN_CHANNELS, seed=0)
+    npairs = lg.collect(LEARN_STEPS)
+    collect_s = time.perf_counter() - t0
+    rep = lg.train(iters=LEARN_ITERS, batch=16, lr=2e-3)
+
+    def run(on):
+        lg.enable(on)
+        ms, cyc, _, _ = time_steps(solver, stream, args.steps, 1)
+        rho, mcyc = solver.last_guess_stats()
+        return ms, cyc, rho, mcyc
+
+    ms_off, cyc_off, _, mc_off = run(False)
+    ms_on, cyc_on, rho, mc_on = run(True)
+    solver.set_timing(True)
+    solver.step(1)
+    kt = solver.timing()
+    solver.set_timing(False)
+    lg.enable(False)
+    g_ms, g_cnt, g_flops = kt.get("guess", (0.0, 0, 0.0))
+    torch.cuda.synchronize()
+    return {"value": round(args.steps / (ms_on / 1000.0), 4), "unit": "RK3 steps/s",
+            "ms_per_step": round(ms_on / args.steps, 3),
+            "same_steps_without_guess_ms_per_step": round(ms_off / args.steps, 3),
+            "mean_corrections_last_substep": {"with": round(mc_on, 3), "without": round(mc_off, 3)},
+            "max_corrections": {"with": cyc_on, "without": cyc_off},
+            "starting_residual_ratio": round(rho, 4),
+            "guess_ms_per_step": round(g_ms, 3),
+            "unet_forward_tflops": round(g_flops / (g_ms / 1000.0) / 1e12, 2) if g_ms > 0 else None,
+            "network": f"U-Net 4 levels x {LEARN_CHANNELS} channels, 3x3, BF16 mma.sync, FP32 accumulate, on the "
+                       f"finest multigrid grid averaged {LEARN_FACTOR}x{LEARN_FACTOR}",
+            "training": {"pairs": npairs, "collect_s": round(collect_s, 2), **{k: (round(v, 5) if isinstance(v, float)
+                                                                                 else v) for k, v in rep.items()}}}
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -251,6 +298,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / n_e2e
     bytes_state = 5 * int(np.prod(shape)) * 16
+    learned = None if args.no_learned else run_learned(solver, stream, args)
     solver.close()
 
     # the plain FP64 GPU path (MUDPACK's smoother and cycles) at the same
@@ -274,7 +322,8 @@ def run_gpu(args):
                     "traffic": None, "algorithmic_bytes_per_launch": int(dbytes / dcnt),
                     "avg_launch_us": round(dms * 1000.0 / dcnt, 3), "launches_per_step": dcnt,
                     "share_of_step": round(dms / ktot, 4)}
-        per_class_gbs = {k: round(v[2] / (v[0] / 1000.0) / 1e9, 1) for k, v in kt.items() if v[0] > 0}
+        per_class_gbs = {k: round(v[2] / (v[0] / 1000.0) / 1e9, 1) for k, v in kt.items()
+                         if v[0] > 0 and k != "guess"}
         plain_value = args.steps / (pms / 1000.0)
         result = {
             "metric": METRIC,
@@ -317,6 +366,7 @@ def run_gpu(args):
                     "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state,
                     "steps": n_e2e},
             "roofline": roof,
+            "learned": learned,
         }
         if world == 1 and not args.no_cpu_baseline:
             result["cpu_baseline"] = cpu_baseline(args)
@@ -396,6 +446,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip training and timing the learned guess")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gpu":
         args.warmup = 3
