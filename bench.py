@@ -264,6 +264,11 @@ def run_gpu(args):
 
     # the method measured: mixed-precision batched projection (mg_fast = 1)
     w, p, xp, yp, state, solver, stream = setup_solver(local, mg_fast=1, fft_fp32=1)
+    # the autotuner picks the line solves' problems-per-block layouts (no
+    # effect on results: each problem's arithmetic is the same in every layout)
+    t_tune = time.perf_counter()
+    tuned = solver.mg_autotune(reps=3)
+    t_tune = time.perf_counter() - t_tune
     if world > 1:
         dist.barrier()
     ms, mg_cycles, launches, clocks = time_steps(solver, stream, args.steps, args.warmup, clocks_gpu=local)
@@ -346,6 +351,8 @@ def run_gpu(args):
                                     "refinement around FP32 V-cycles",
                        "poisson": f"relative residual {MG_TOL:g} per problem; kx=0 by MUDPACK's rule",
                        "mg_corrections_per_substep_max": mg_cycles,
+                       "line_solve_layouts": {f"L{r['level']}{r['dir']}": r["lanes"] for r in tuned},
+                       "autotune_s": round(t_tune, 2),
                        "l2": "fields (407 MB each, ~18 GB resident) exceed the 126 MB L2; no flush",
                        "parallelism": f"replicas x{world}"},
             "plain": {"value": round(plain_value, 4), "unit": "RK3 steps/s", "ms_per_step": round(pms / args.steps, 3),

@@ -932,3 +932,45 @@ int ekgpu_last_guess_stats(ek_ctx *h, double *mean_rho, double *mean_cycles) {
     return (int)EK_OK;
   });
 }
+
+// ---------------------------------------------------------------------------
+// Tile-shape autotuner of the mixed solver's line solves.
+int ekgpu_mg_autotune(ek_ctx *h, int reps, char *report, int report_len) {
+  return guarded(h, [&](Ctx &c) {
+    if (!c.p.mg_fast) return fail(c, EK_ERR_STATE, "the autotuner tunes the mixed solver (mg_fast = 1)");
+    if (!c.have_metrics) return fail(c, EK_ERR_STATE, "metrics not set");
+    std::string rep;
+    const int st = mgfast_autotune(c, reps < 1 ? 1 : reps, rep);
+    if (st != EK_OK) return fail(c, st, "autotune failed");
+    if (report && report_len > 0) {
+      const size_t n = std::min(rep.size(), (size_t)report_len - 1);
+      std::memcpy(report, rep.data(), n);
+      report[n] = 0;
+    }
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_mg_set_lanes(ek_ctx *h, int level, int dir, int lanes) {
+  return guarded(h, [&](Ctx &c) {
+    MgPlan &PL = c.mg;
+    if (level < 2 || level > PL.ngrid || dir < 0 || dir > 1 || !(lanes == 0 || lanes == 8 || lanes == 16 || lanes == 32))
+      return fail(c, EK_ERR_ARG, "level in 2..ngrid, dir 0 (y-lines) or 1 (x-lines), lanes 0, 8, 16 or 32");
+    std::vector<int> &t = dir ? PL.lanes_x : PL.lanes_y;
+    if ((int)t.size() < PL.ngrid + 1) t.resize(PL.ngrid + 1, 0);
+    t[level] = lanes;
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_mg_levels(ek_ctx *h, int *ngrid, int *nx, int *ny, int cap) {
+  return guarded(h, [&](Ctx &c) {
+    const MgPlan &PL = c.mg;
+    if (ngrid) *ngrid = PL.ngrid;
+    for (int l = 0; l < PL.ngrid && l < cap; ++l) {
+      if (nx) nx[l] = PL.lv[l].nx;
+      if (ny) ny[l] = PL.lv[l].ny;
+    }
+    return (int)EK_OK;
+  });
+}

@@ -146,6 +146,9 @@ struct MgPlan {
   // host copies of the kx-independent coefficients per level
   std::vector<std::vector<double>> cof_host;
   size_t coarse_smem = 0;
+  // mixed solver: problems per block of the line solves, per level (index
+  // l = 1..ngrid) and direction; 0 = the default rule (set by ekgpu_mg_autotune)
+  std::vector<int> lanes_y, lanes_x;
 };
 
 // Kernel classes for the optional per-kernel timer (ekgpu_set_timing).
@@ -381,6 +384,7 @@ void mg_work_alloc(Ctx &c, MgWork &w, int pmax);
 void mg_work_free(MgWork &w);
 int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_host, ek_mg_stats *st);
 void mgfast_alloc(Ctx &c, int pmax);
+int mgfast_autotune(Ctx &c, int reps, std::string &report);
 
 // restart files (ek_io.cpp): SAVE_FLOW / READ_FLOW records from and into the state
 int save_flow(Ctx &c, const char *flow_path, const char *th_path);

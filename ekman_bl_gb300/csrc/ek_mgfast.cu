@@ -748,6 +748,73 @@ __global__ void __launch_bounds__(32 * kRY) k_f_phif(FastDev g) {
 }
 
 
+// One partitioned line launch: lines l0, l0+lstep, ... (nline of them) of
+// length n at level l, all problems, `lanes` problems per block (8, 16 or
+// 32; segments of <= 8 rows, at most 64 segments and 1024 threads).  Lines
+// longer than the layout allows fall back to one thread per line.
+void launch_pline(const FastDev &g, int l, bool xl, int l0, int lstep, int nline, int n, int lanes,
+                  cudaStream_t s) {
+  const int K = (n + 8) / 9 > 0 ? (n + 8) / 9 : 1;
+  if (K > 64 || K * lanes > 1024) {
+    const unsigned b = (unsigned)(((long)nline * g.P + 63) / 64);
+    if (xl) k_f_xline<<<b, 64, 0, s>>>(g, l, l0, nline);
+    else k_f_yline<<<b, 64, 0, s>>>(g, l, l0, lstep, nline);
+    return;
+  }
+  const int mb = (n - K + 1) / K, me = (n - K + 1) % K;
+  const dim3 grid((unsigned)nline, (unsigned)((g.P + lanes - 1) / lanes)), blk(lanes, K);
+  const size_t smem = sizeof(float) * SH_N * K * lanes;
+#define EK_PLINE(W)                                                                              \
+  do {                                                                                           \
+    if (g.orth) {                                                                                \
+      if (xl) k_f_pline<true, true, W><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);         \
+      else k_f_pline<false, true, W><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);           \
+    } else {                                                                                     \
+      if (xl) k_f_pline<true, false, W><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);        \
+      else k_f_pline<false, false, W><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);          \
+    }                                                                                            \
+  } while (0)
+  if (lanes == 32) EK_PLINE(32);
+  else if (lanes == 16) EK_PLINE(16);
+  else EK_PLINE(8);
+#undef EK_PLINE
+}
+
+// The layout the solver uses when nothing was tuned: 32 problems per block
+// while a line has at most 32 segments (n <= 287), else 16.
+int default_lanes(int n) { return ((n + 8) / 9 <= 32) ? 32 : 16; }
+
+FastDev make_fastdev(Ctx &c, int nprob, const double *kx2_dev) {
+  const MgPlan &PL = c.mg;
+  MgWork &w = c.mgw;
+  FastDev g{};
+  g.P = nprob;
+  g.ngrid = PL.ngrid;
+  g.orth = PL.orth ? 1 : 0;
+  for (int l = 0; l < PL.ngrid; ++l) {
+    const MgLevelF &F = c.mgf_levels[l];
+    g.lv[l] = LvF{PL.lv[l].nx, PL.lv[l].ny, F.e, F.r, F.cof, F.cp};
+  }
+  g.scr = c.mgf_scratch;
+  g.rhs = w.rhs[PL.ngrid - 1];
+  g.phh = c.mgf_phh;
+  g.phl = c.mgf_phl;
+  g.bh = c.mgf_bh;
+  g.bl = c.mgf_bl;
+  g.cfh = c.mgf_cfh;
+  g.cfl = c.mgf_cfl;
+  g.nfx = PL.nfx;
+  g.nfy = PL.nfy;
+  g.kx2 = kx2_dev;
+  g.phif = w.phif;
+  g.red = w.red;
+  g.done = w.done;
+  g.cycles = w.cycles;
+  g.alldone = w.alldone;
+  g.tol = c.p.mg_tol;
+  return g;
+}
+
 unsigned nb(long n, int bs) {
   long b = (n + bs - 1) / bs;
   if (b < 1) b = 1;
@@ -871,31 +938,7 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
     c.stream = s;
     EK_CUDA(cudaEventRecord(c.ev_join, c.aux_stream));
   }
-  FastDev g{};
-  g.P = nprob;
-  g.ngrid = PL.ngrid;
-  g.orth = PL.orth ? 1 : 0;
-  for (int l = 0; l < PL.ngrid; ++l) {
-    const MgLevelF &F = c.mgf_levels[l];
-    g.lv[l] = LvF{PL.lv[l].nx, PL.lv[l].ny, F.e, F.r, F.cof, F.cp};
-  }
-  g.scr = c.mgf_scratch;
-  g.rhs = w.rhs[PL.ngrid - 1];
-  g.phh = c.mgf_phh;
-  g.phl = c.mgf_phl;
-  g.bh = c.mgf_bh;
-  g.bl = c.mgf_bl;
-  g.cfh = c.mgf_cfh;
-  g.cfl = c.mgf_cfl;
-  g.nfx = PL.nfx;
-  g.nfy = PL.nfy;
-  g.kx2 = kx2_dev;
-  g.phif = w.phif;
-  g.red = w.red;
-  g.done = w.done;
-  g.cycles = w.cycles;
-  g.alldone = w.alldone;
-  g.tol = c.p.mg_tol;
+  FastDev g = make_fastdev(c, nprob, kx2_dev);
 
   {
     KScope ks(c, KC_MG_SETUP, 8.0 * (PL.nfx + 2) * (PL.nfy + 2) * nprob * 2);
@@ -941,31 +984,12 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
     after_launch(c);
   }
 
-  // one partitioned line launch: lines l0, l0+lstep, ... (nline of them)
-  // of length n, all problems
+  // one partitioned line launch, in the layout tuned for (level, direction)
   auto pline = [&](int l, bool xl, int l0, int lstep, int nline, int n) {
-    // segments of <= 8 rows; 32 problems per block while a line needs at
-    // most 32 segments (n <= 287), else 16 problems and up to 64 segments
-    const int K = std::max(1, (n + 8) / 9);
-    if (K > 64) {  // lines longer than 575 rows: one thread per line
-      if (xl) k_f_xline<<<nb((long)nline * nprob, 64), 64, 0, s>>>(g, l, l0, nline);
-      else k_f_yline<<<nb((long)nline * nprob, 64), 64, 0, s>>>(g, l, l0, lstep, nline);
-      after_launch(c);
-      return;
-    }
-    const int lanes = (K <= 32) ? 32 : 16;
-    const int mb = (n - K + 1) / K, me = (n - K + 1) % K;
-    const dim3 grid((unsigned)nline, (unsigned)((nprob + lanes - 1) / lanes)), blk(lanes, K);
-    const size_t smem = sizeof(float) * SH_N * K * lanes;
-#define EK_PLINE(X, O, W) k_f_pline<X, O, W><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me)
-    if (lanes == 32) {
-      if (g.orth) { if (xl) EK_PLINE(true, true, 32); else EK_PLINE(false, true, 32); }
-      else { if (xl) EK_PLINE(true, false, 32); else EK_PLINE(false, false, 32); }
-    } else {
-      if (g.orth) { if (xl) EK_PLINE(true, true, 16); else EK_PLINE(false, true, 16); }
-      else { if (xl) EK_PLINE(true, false, 16); else EK_PLINE(false, false, 16); }
-    }
-#undef EK_PLINE
+    int lanes = default_lanes(n);
+    const std::vector<int> &tab = xl ? PL.lanes_x : PL.lanes_y;
+    if (l < (int)tab.size() && tab[l] > 0) lanes = tab[l];
+    launch_pline(g, l, xl, l0, lstep, nline, n, lanes, s);
     after_launch(c);
   };
 
@@ -1082,6 +1106,87 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
   c.last_stats = S;
   if (st) *st = S;
   return S.n_not_converged ? EK_ERR_NOT_CONVERGED : EK_OK;
+}
+
+
+// Tile-shape autotuner of the line solves: for every level of the mixed
+// solver and both line directions, time one full zebra sweep (both colours)
+// in each valid problems-per-block layout (8, 16, 32) on the solver's own
+// arrays, `reps` times, and keep the fastest.  The level arrays are work
+// space that every solve re-initialises, so the timing runs leave no trace.
+int mgfast_autotune(Ctx &c, int reps, std::string &report) {
+  MgPlan &PL = c.mg;
+  MgWork &w = c.mgw;
+  const int nprob = 2 * (c.d.NKX + 1);
+  if (!c.p.mg_fast || nprob > c.mgf_pmax) return EK_ERR_STATE;
+  cudaStream_t s = c.stream;
+  FastDev g = make_fastdev(c, nprob, w.kx2);
+  EK_CUDA(cudaMemsetAsync(w.flags, 0, sizeof(int) * (2 * w.pmax + 4), s));  // every problem active
+  PL.lanes_y.assign(PL.ngrid + 1, 0);
+  PL.lanes_x.assign(PL.ngrid + 1, 0);
+  cudaEvent_t e0, e1;
+  EK_CUDA(cudaEventCreate(&e0));
+  EK_CUDA(cudaEventCreate(&e1));
+  report = "[";
+  bool first = true;
+  try {
+    for (int l = 2; l <= PL.ngrid; ++l) {
+      const MgLevel &L = PL.lv[l - 1];
+      for (int dir = 0; dir < 2; ++dir) {
+        const bool xl = dir == 1;
+        const int n = xl ? L.nx : L.ny;
+        const int K = (n + 8) / 9;
+        auto sweep = [&](int lanes) {
+          if (xl) {
+            for (int col = 1; col <= 2; ++col) launch_pline(g, l, true, col, 2, (L.ny - col) / 2 + 1, L.nx, lanes, s);
+          } else {
+            for (int col = 1; col <= 2; ++col) {
+              LinePhase ph[2];
+              const int nph = line_phases(L.nx, col, ph);
+              for (int q = 0; q < nph; ++q)
+                if (ph[q].ncol > 0) launch_pline(g, l, false, ph[q].i0, ph[q].istep, ph[q].ncol, L.ny, lanes, s);
+            }
+          }
+        };
+        int best = 0;
+        float best_ms = 0.f;
+        std::string row;
+        for (int lanes : {32, 16, 8}) {
+          if (K > 64 || K * lanes > 1024) continue;
+          sweep(lanes);  // warm-up
+          after_launch(c);
+          EK_CUDA(cudaEventRecord(e0, s));
+          for (int r = 0; r < reps; ++r) sweep(lanes);
+          EK_CUDA(cudaEventRecord(e1, s));
+          after_launch(c);
+          EK_CUDA(cudaEventSynchronize(e1));
+          float ms = 0.f;
+          EK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+          ms /= (float)reps;
+          row += (row.empty() ? "" : ", ") + std::string("\"") + std::to_string(lanes) + "\": " +
+                 std::to_string(1000.0 * ms);
+          if (best == 0 || ms < best_ms) {
+            best = lanes;
+            best_ms = ms;
+          }
+        }
+        (xl ? PL.lanes_x : PL.lanes_y)[l] = best;
+        report += std::string(first ? "" : ", ") + "{\"level\": " + std::to_string(l) + ", \"dir\": \"" +
+                  (xl ? "x" : "y") + "\", \"n\": " + std::to_string(n) + ", \"us\": {" + row +
+                  "}, \"lanes\": " + std::to_string(best) + "}";
+        first = false;
+      }
+    }
+  } catch (...) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    throw;
+  }
+  report += "]";
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  EK_CUDA(cudaStreamSynchronize(s));
+  return EK_OK;
 }
 
 }  // namespace ek

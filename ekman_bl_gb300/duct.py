@@ -34,7 +34,7 @@ EXPORTS = [
     "ekgpu_unet_create", "ekgpu_unet_destroy", "ekgpu_unet_last_error", "ekgpu_unet_num_params",
     "ekgpu_unet_set_params", "ekgpu_unet_get_params", "ekgpu_unet_forward", "ekgpu_unet_train_step",
     "ekgpu_unet_gradient", "ekgpu_guess_geometry", "ekgpu_set_poisson_guess", "ekgpu_set_pair_sink",
-    "ekgpu_pair_count", "ekgpu_last_guess_stats",
+    "ekgpu_pair_count", "ekgpu_last_guess_stats", "ekgpu_mg_autotune", "ekgpu_mg_set_lanes", "ekgpu_mg_levels",
 ]
 
 
@@ -94,6 +94,9 @@ def load_library():
     L.ekgpu_set_pair_sink.argtypes = [V, V, V, C.c_int, C.c_int]
     L.ekgpu_pair_count.argtypes = [V, C.POINTER(C.c_int)]
     L.ekgpu_last_guess_stats.argtypes = [V, _D, _D]
+    L.ekgpu_mg_autotune.argtypes = [V, C.c_int, C.c_char_p, C.c_int]
+    L.ekgpu_mg_set_lanes.argtypes = [V, C.c_int, C.c_int, C.c_int]
+    L.ekgpu_mg_levels.argtypes = [V, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]
     L.ekgpu_get_field.argtypes = [V, C.c_int, _D]
     L.ekgpu_put_field.argtypes = [V, C.c_int, _D]
     L.ekgpu_rk_substep.argtypes = [V, C.c_int]
@@ -300,6 +303,25 @@ class DuctSolver:
                 th_bar = np.zeros((self.p.ny + 3, self.p.nz + 3))
             out["files"] = write_stats_files(root, time, dt, step, every, xpoint, ypoint, th_bar, out)
         return out
+
+    # -- line-solver layouts (tile-shape autotuner) -------------------------------
+    def mg_autotune(self, reps: int = 3) -> list:
+        """Time every valid layout of the mixed solver's line solves per level
+        and direction and keep the fastest; returns the timings."""
+        import json
+        buf = C.create_string_buffer(1 << 16)
+        self._check(self._L.ekgpu_mg_autotune(self._h, reps, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
+    def mg_set_lanes(self, level: int, direction: int, lanes: int):
+        self._check(self._L.ekgpu_mg_set_lanes(self._h, level, direction, lanes))
+
+    def mg_levels(self):
+        """[(nx, ny)] of the multigrid levels, coarsest first."""
+        n = C.c_int()
+        nx, ny = (C.c_int * 32)(), (C.c_int * 32)()
+        self._check(self._L.ekgpu_mg_levels(self._h, C.byref(n), nx, ny, 32))
+        return [(nx[i], ny[i]) for i in range(n.value)]
 
     # -- learned initial guess of the Poisson problems ----------------------------
     def guess_geometry(self, factor: int):

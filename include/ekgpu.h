@@ -260,6 +260,20 @@ int ekgpu_read_flow(ek_ctx *ctx, const char *flow_path, const char *th_path);
  * the TKE budget, the plane dumps and the Tecplot writer are not part of it. */
 int ekgpu_save_stats(ek_ctx *ctx, ek_stats *stats);
 
+/* ---- Tile-shape autotuner of the mixed solver's line solves ----------------
+ * (No counterpart in the reference.)  For every multigrid level l = 2..ngrid
+ * and both line directions, time one zebra sweep in each valid layout (8, 16
+ * or 32 problems per block) `reps` times on the context's own work arrays,
+ * and use the fastest from then on.  The arithmetic of each problem is the
+ * same in every layout, so tuning changes no result.  report (may be NULL)
+ * receives the timings as JSON text.  Needs mg_fast = 1 and metrics. */
+int ekgpu_mg_autotune(ek_ctx *ctx, int reps, char *report, int report_len);
+/* Set one layout by hand (lanes 0 restores the default rule; dir 0 y-lines,
+ * 1 x-lines), e.g. to replay a table tuned earlier. */
+int ekgpu_mg_set_lanes(ek_ctx *ctx, int level, int dir, int lanes);
+/* The multigrid levels: ngrid and the sizes nx[l-1] x ny[l-1], l = 1..ngrid. */
+int ekgpu_mg_levels(ek_ctx *ctx, int *ngrid, int *nx, int *ny, int cap);
+
 /* ---- Learned initial guess of the per-kx Poisson problems -------------------
  * (No counterpart in the reference: its solves always start from zero.)
  *

@@ -1,0 +1,77 @@
+"""Tile-shape autotuner of the mixed solver's line solves.
+
+Each problem's arithmetic is the same in every layout (8, 16 or 32 problems
+per block): the separator system of a line is solved by the problem's own
+lane.  So a solve in any forced layout, and after autotuning, must equal the
+default-layout solve bit for bit, with the same cycle counts.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from ekcases import small_case
+from ekman_bl_gb300.params import EK_MG_STOP_RESIDUAL
+
+pytestmark = pytest.mark.gpu
+
+
+def mixed_solver():
+    from ekman_bl_gb300.duct import DuctSolver, metrics_from_grid
+    p, xp, yp, st = small_case(nx=32, ny2=129, nz2=65, mg_stop=EK_MG_STOP_RESIDUAL)
+    p.mg_tol, p.mg_maxcy, p.mg_fast = 1e-10, 60, 1
+    g = DuctSolver(p, metrics_from_grid(p, xp, yp))
+    g.upload(*st)
+    return p, g
+
+
+def batch(p, seed=3):
+    kx2 = np.array([(2 * math.pi * k / p.lx) ** 2 for k in (1, 2, 3, 5, 8, 10)])
+    rhs = np.random.default_rng(seed).standard_normal((len(kx2), p.ny + 2, p.nz + 2))
+    rhs[:, 0, :] = 0
+    rhs[:, -1, :] = 0
+    return rhs, kx2
+
+
+def test_layouts_give_identical_solves():
+    p, g = mixed_solver()
+    rhs, kx2 = batch(p)
+    phi0, st0, c0 = g.multigrid_mudpack(rhs, kx2)
+    assert c0 == 0
+    ngrid = len(g.mg_levels())
+    for lanes in (8, 16, 32):
+        for lev in range(2, ngrid + 1):
+            for d in (0, 1):
+                g.mg_set_lanes(lev, d, lanes)
+        phi, st, c = g.multigrid_mudpack(rhs, kx2)
+        assert c == 0 and st["max_cycles"] == st0["max_cycles"] and st["min_cycles"] == st0["min_cycles"]
+        assert np.array_equal(phi, phi0), lanes
+
+
+def test_autotune_picks_valid_layouts_and_changes_nothing():
+    p, g = mixed_solver()
+    rhs, kx2 = batch(p, seed=4)
+    phi0, st0, _ = g.multigrid_mudpack(rhs, kx2)
+    a0 = g.download()
+    rep = g.mg_autotune(reps=2)
+    levels = g.mg_levels()
+    assert len(rep) == 2 * (len(levels) - 1)
+    for row in rep:
+        assert row["lanes"] in (8, 16, 32) and str(row["lanes"]) in row["us"]
+        assert all(v > 0 for v in row["us"].values())
+        nx, ny = levels[row["level"] - 1]
+        assert row["n"] == (nx if row["dir"] == "x" else ny)
+    # the state is untouched, and a solve after tuning is the same solve
+    for x, y in zip(g.download(), a0):
+        assert np.array_equal(x, y)
+    phi, st, c = g.multigrid_mudpack(rhs, kx2)
+    assert c == 0 and st["max_cycles"] == st0["max_cycles"]
+    assert np.array_equal(phi, phi0)
+
+
+def test_autotune_needs_the_mixed_solver():
+    from ekman_bl_gb300.duct import DuctSolver, EkError, metrics_from_grid
+    p, xp, yp, st = small_case()
+    g = DuctSolver(p, metrics_from_grid(p, xp, yp))
+    with pytest.raises(EkError):
+        g.mg_autotune()
