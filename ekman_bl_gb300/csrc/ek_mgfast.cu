@@ -497,27 +497,48 @@ __global__ void __launch_bounds__(1024) k_f_pline(FastDev g, int level, int l0, 
     S(SH_A, s) = a; S(SH_B, s) = b; S(SH_C, s) = c; S(SH_D, s) = d;
   }
   __syncthreads();
-  if (s == 0 && K > 1) {
-    // separators t = 0..K-2: A S(t-1) + B S(t) + C S(t+1) = D
-    float cpv = 0.f, dpv = 0.f;
-    for (int t = 0; t < K - 1; ++t) {
-      const float a = S(SH_A, t), c = S(SH_C, t);
-      const float A = a * S(SH_VL, t);
-      const float B = S(SH_B, t) + a * S(SH_WL, t) + c * S(SH_VF, t + 1);
-      const float C = c * S(SH_WF, t + 1);
-      const float D = S(SH_D, t) - a * S(SH_YL, t) - c * S(SH_YF, t + 1);
-      const float inv = __fdividef(1.f, B - A * cpv);
-      cpv = C * inv;
-      dpv = (D - A * dpv) * inv;
-      S(SH_A, t) = cpv;  // c' and d' of the separator system
-      S(SH_D, t) = dpv;
+  // the K-1 separator unknowns, A S(t-1) + B S(t) + C S(t+1) = D, by
+  // parallel cyclic reduction: thread row t owns separator t; after the
+  // steps of stride 1, 2, 4, ... each row couples to nothing and S(t) = D/B
+  const int nsep = K - 1;
+  float eA = 0.f, eB = 1.f, eC = 0.f, eD = 0.f;
+  if (s < nsep) {
+    const float a = S(SH_A, s), c = S(SH_C, s);
+    eA = (s > 0) ? a * S(SH_VL, s) : 0.f;
+    eB = S(SH_B, s) + a * S(SH_WL, s) + c * S(SH_VF, s + 1);
+    eC = (s < nsep - 1) ? c * S(SH_WF, s + 1) : 0.f;
+    eD = S(SH_D, s) - a * S(SH_YL, s) - c * S(SH_YF, s + 1);
+  }
+  for (int d = 1; d < nsep; d <<= 1) {
+    __syncthreads();
+    if (s < nsep) {
+      S(SH_A, s) = eA;
+      S(SH_B, s) = eB;
+      S(SH_C, s) = eC;
+      S(SH_D, s) = eD;
     }
-    float x = 0.f;
-    for (int t = K - 2; t >= 0; --t) {
-      x = S(SH_D, t) - S(SH_A, t) * x;
-      S(SH_S, t) = x;
+    __syncthreads();
+    if (s < nsep) {
+      float nA = 0.f, nC = 0.f, nB = eB, nD = eD;
+      if (s - d >= 0) {
+        const float al = __fdividef(eA, S(SH_B, s - d));
+        nA = -al * S(SH_A, s - d);
+        nB -= al * S(SH_C, s - d);
+        nD -= al * S(SH_D, s - d);
+      }
+      if (s + d < nsep) {
+        const float ga = __fdividef(eC, S(SH_B, s + d));
+        nC = -ga * S(SH_C, s + d);
+        nB -= ga * S(SH_A, s + d);
+        nD -= ga * S(SH_D, s + d);
+      }
+      eA = nA;
+      eB = nB;
+      eC = nC;
+      eD = nD;
     }
   }
+  if (s < nsep) S(SH_S, s) = __fdividef(eD, eB);
   __syncthreads();
   if (!act) return;
   const float X0 = (s > 0) ? S(SH_S, s - 1) : 0.f;
