@@ -351,7 +351,7 @@ def run_gpu(args):
                                     "refinement around FP32 V-cycles",
                        "poisson": f"relative residual {MG_TOL:g} per problem; kx=0 by MUDPACK's rule",
                        "mg_corrections_per_substep_max": mg_cycles,
-                       "line_solve_layouts": {f"L{r['level']}{r['dir']}": r["lanes"] for r in tuned},
+                       "line_solve_layouts": {f"L{r['level']}{r['dir']}": f"{r['lanes']}x{r['seg']}" for r in tuned},
                        "autotune_s": round(t_tune, 2),
                        "l2": "fields (407 MB each, ~18 GB resident) exceed the 126 MB L2; no flush",
                        "parallelism": f"replicas x{world}"},

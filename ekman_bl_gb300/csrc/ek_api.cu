@@ -951,14 +951,18 @@ int ekgpu_mg_autotune(ek_ctx *h, int reps, char *report, int report_len) {
   });
 }
 
-int ekgpu_mg_set_lanes(ek_ctx *h, int level, int dir, int lanes) {
+int ekgpu_mg_set_layout(ek_ctx *h, int level, int dir, int lanes, int seg) {
   return guarded(h, [&](Ctx &c) {
     MgPlan &PL = c.mg;
-    if (level < 2 || level > PL.ngrid || dir < 0 || dir > 1 || !(lanes == 0 || lanes == 8 || lanes == 16 || lanes == 32))
-      return fail(c, EK_ERR_ARG, "level in 2..ngrid, dir 0 (y-lines) or 1 (x-lines), lanes 0, 8, 16 or 32");
+    if (level < 2 || level > PL.ngrid || dir < 0 || dir > 1 || !(lanes == 0 || lanes == 8 || lanes == 16 || lanes == 32) ||
+        !(seg == 0 || seg == 4 || seg == 8))
+      return fail(c, EK_ERR_ARG, "level in 2..ngrid, dir 0 (y-lines) or 1 (x-lines), lanes 0/8/16/32, seg 0/4/8");
     std::vector<int> &t = dir ? PL.lanes_x : PL.lanes_y;
+    std::vector<int> &u = dir ? PL.seg_x : PL.seg_y;
     if ((int)t.size() < PL.ngrid + 1) t.resize(PL.ngrid + 1, 0);
+    if ((int)u.size() < PL.ngrid + 1) u.resize(PL.ngrid + 1, 0);
     t[level] = lanes;
+    u[level] = seg;
     return (int)EK_OK;
   });
 }

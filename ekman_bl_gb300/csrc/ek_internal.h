@@ -146,9 +146,10 @@ struct MgPlan {
   // host copies of the kx-independent coefficients per level
   std::vector<std::vector<double>> cof_host;
   size_t coarse_smem = 0;
-  // mixed solver: problems per block of the line solves, per level (index
-  // l = 1..ngrid) and direction; 0 = the default rule (set by ekgpu_mg_autotune)
-  std::vector<int> lanes_y, lanes_x;
+  // mixed solver: layout of the line solves per level (index l = 1..ngrid)
+  // and direction -- problems per block and rows per segment; 0 = the
+  // default rule (set by ekgpu_mg_autotune)
+  std::vector<int> lanes_y, lanes_x, seg_y, seg_x;
 };
 
 // Kernel classes for the optional per-kernel timer (ekgpu_set_timing).

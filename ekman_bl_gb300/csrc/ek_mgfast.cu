@@ -389,9 +389,9 @@ __global__ void __launch_bounds__(64) k_f_xline(FastDev g, int level, int j0, in
 // XL: x-line (along i, the periodic wrap couplings taken from the ghosts'
 // current values); else y-line (along j).
 enum { SH_A, SH_B, SH_C, SH_D, SH_YF, SH_VF, SH_WF, SH_YL, SH_VL, SH_WL, SH_S, SH_N };
-template <bool XL, bool ORTH, int LANES>
+template <bool XL, bool ORTH, int LANES, int SEG>
 __global__ void __launch_bounds__(1024) k_f_pline(FastDev g, int level, int l0, int lstep, int mb, int me) {
-  constexpr int kSegMax = 8;
+  constexpr int kSegMax = SEG;
   if (*g.alldone) return;
   extern __shared__ float sh[];
   const int K = blockDim.y;
@@ -770,13 +770,22 @@ __global__ void __launch_bounds__(32 * kRY) k_f_phif(FastDev g) {
 
 
 // One partitioned line launch: lines l0, l0+lstep, ... (nline of them) of
-// length n at level l, all problems, `lanes` problems per block (8, 16 or
-// 32; segments of <= 8 rows, at most 64 segments and 1024 threads).  Lines
-// longer than the layout allows fall back to one thread per line.
-void launch_pline(const FastDev &g, int l, bool xl, int l0, int lstep, int nline, int n, int lanes,
+// length n at level l, all problems, in the layout (lanes, seg): `lanes`
+// problems per block (8, 16 or 32), segments of at most `seg` rows (4 or 8)
+// separated by single rows, at most 128 segments and 1024 threads.  Lines
+// the layout cannot hold fall back to one thread per line.
+// K segments of at most seg rows and K-1 separator rows cover n rows when
+// K (seg + 1) >= n + 1
+int pline_segments(int n, int seg) { return std::max(1, (n + seg + 1) / (seg + 1)); }
+bool pline_fits(int n, int lanes, int seg) {
+  const int K = pline_segments(n, seg);
+  return K <= 128 && K * lanes <= 1024;
+}
+
+void launch_pline(const FastDev &g, int l, bool xl, int l0, int lstep, int nline, int n, int lanes, int seg,
                   cudaStream_t s) {
-  const int K = (n + 8) / 9 > 0 ? (n + 8) / 9 : 1;
-  if (K > 64 || K * lanes > 1024) {
+  const int K = pline_segments(n, seg);
+  if (!pline_fits(n, lanes, seg)) {
     const unsigned b = (unsigned)(((long)nline * g.P + 63) / 64);
     if (xl) k_f_xline<<<b, 64, 0, s>>>(g, l, l0, nline);
     else k_f_yline<<<b, 64, 0, s>>>(g, l, l0, lstep, nline);
@@ -785,25 +794,31 @@ void launch_pline(const FastDev &g, int l, bool xl, int l0, int lstep, int nline
   const int mb = (n - K + 1) / K, me = (n - K + 1) % K;
   const dim3 grid((unsigned)nline, (unsigned)((g.P + lanes - 1) / lanes)), blk(lanes, K);
   const size_t smem = sizeof(float) * SH_N * K * lanes;
-#define EK_PLINE(W)                                                                              \
-  do {                                                                                           \
-    if (g.orth) {                                                                                \
-      if (xl) k_f_pline<true, true, W><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);         \
-      else k_f_pline<false, true, W><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);           \
-    } else {                                                                                     \
-      if (xl) k_f_pline<true, false, W><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);        \
-      else k_f_pline<false, false, W><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);          \
-    }                                                                                            \
+#define EK_PLINE(W, S)                                                                             \
+  do {                                                                                             \
+    if (g.orth) {                                                                                  \
+      if (xl) k_f_pline<true, true, W, S><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);        \
+      else k_f_pline<false, true, W, S><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);          \
+    } else {                                                                                       \
+      if (xl) k_f_pline<true, false, W, S><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);       \
+      else k_f_pline<false, false, W, S><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);         \
+    }                                                                                              \
   } while (0)
-  if (lanes == 32) EK_PLINE(32);
-  else if (lanes == 16) EK_PLINE(16);
-  else EK_PLINE(8);
+  if (seg == 4) {
+    if (lanes == 32) EK_PLINE(32, 4);
+    else if (lanes == 16) EK_PLINE(16, 4);
+    else EK_PLINE(8, 4);
+  } else {
+    if (lanes == 32) EK_PLINE(32, 8);
+    else if (lanes == 16) EK_PLINE(16, 8);
+    else EK_PLINE(8, 8);
+  }
 #undef EK_PLINE
 }
 
-// The layout the solver uses when nothing was tuned: 32 problems per block
-// while a line has at most 32 segments (n <= 287), else 16.
-int default_lanes(int n) { return ((n + 8) / 9 <= 32) ? 32 : 16; }
+// The layout the solver uses when nothing was tuned: 8-row segments, 32
+// problems per block while a line has at most 32 segments (n <= 287), else 16.
+int default_lanes(int n) { return (pline_segments(n, 8) <= 32) ? 32 : 16; }
 
 FastDev make_fastdev(Ctx &c, int nprob, const double *kx2_dev) {
   const MgPlan &PL = c.mg;
@@ -1007,10 +1022,12 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
 
   // one partitioned line launch, in the layout tuned for (level, direction)
   auto pline = [&](int l, bool xl, int l0, int lstep, int nline, int n) {
-    int lanes = default_lanes(n);
-    const std::vector<int> &tab = xl ? PL.lanes_x : PL.lanes_y;
-    if (l < (int)tab.size() && tab[l] > 0) lanes = tab[l];
-    launch_pline(g, l, xl, l0, lstep, nline, n, lanes, s);
+    int lanes = default_lanes(n), seg = 8;
+    const std::vector<int> &tl = xl ? PL.lanes_x : PL.lanes_y;
+    const std::vector<int> &ts = xl ? PL.seg_x : PL.seg_y;
+    if (l < (int)tl.size() && tl[l] > 0) lanes = tl[l];
+    if (l < (int)ts.size() && ts[l] > 0) seg = ts[l];
+    launch_pline(g, l, xl, l0, lstep, nline, n, lanes, seg, s);
     after_launch(c);
   };
 
@@ -1132,8 +1149,8 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
 
 // Tile-shape autotuner of the line solves: for every level of the mixed
 // solver and both line directions, time one full zebra sweep (both colours)
-// in each valid problems-per-block layout (8, 16, 32) on the solver's own
-// arrays, `reps` times, and keep the fastest.  The level arrays are work
+// in each valid layout -- 8, 16 or 32 problems per block, segments of 8 or 4
+// rows -- on the solver's own arrays, `reps` times, and keep the fastest.  The level arrays are work
 // space that every solve re-initialises, so the timing runs leave no trace.
 int mgfast_autotune(Ctx &c, int reps, std::string &report) {
   MgPlan &PL = c.mg;
@@ -1145,6 +1162,8 @@ int mgfast_autotune(Ctx &c, int reps, std::string &report) {
   EK_CUDA(cudaMemsetAsync(w.flags, 0, sizeof(int) * (2 * w.pmax + 4), s));  // every problem active
   PL.lanes_y.assign(PL.ngrid + 1, 0);
   PL.lanes_x.assign(PL.ngrid + 1, 0);
+  PL.seg_y.assign(PL.ngrid + 1, 0);
+  PL.seg_x.assign(PL.ngrid + 1, 0);
   cudaEvent_t e0, e1;
   EK_CUDA(cudaEventCreate(&e0));
   EK_CUDA(cudaEventCreate(&e1));
@@ -1156,45 +1175,48 @@ int mgfast_autotune(Ctx &c, int reps, std::string &report) {
       for (int dir = 0; dir < 2; ++dir) {
         const bool xl = dir == 1;
         const int n = xl ? L.nx : L.ny;
-        const int K = (n + 8) / 9;
-        auto sweep = [&](int lanes) {
+        auto sweep = [&](int lanes, int seg) {
           if (xl) {
-            for (int col = 1; col <= 2; ++col) launch_pline(g, l, true, col, 2, (L.ny - col) / 2 + 1, L.nx, lanes, s);
+            for (int col = 1; col <= 2; ++col)
+              launch_pline(g, l, true, col, 2, (L.ny - col) / 2 + 1, L.nx, lanes, seg, s);
           } else {
             for (int col = 1; col <= 2; ++col) {
               LinePhase ph[2];
               const int nph = line_phases(L.nx, col, ph);
               for (int q = 0; q < nph; ++q)
-                if (ph[q].ncol > 0) launch_pline(g, l, false, ph[q].i0, ph[q].istep, ph[q].ncol, L.ny, lanes, s);
+                if (ph[q].ncol > 0) launch_pline(g, l, false, ph[q].i0, ph[q].istep, ph[q].ncol, L.ny, lanes, seg, s);
             }
           }
         };
-        int best = 0;
+        int best = 0, best_seg = 8;
         float best_ms = 0.f;
         std::string row;
-        for (int lanes : {32, 16, 8}) {
-          if (K > 64 || K * lanes > 1024) continue;
-          sweep(lanes);  // warm-up
-          after_launch(c);
-          EK_CUDA(cudaEventRecord(e0, s));
-          for (int r = 0; r < reps; ++r) sweep(lanes);
-          EK_CUDA(cudaEventRecord(e1, s));
-          after_launch(c);
-          EK_CUDA(cudaEventSynchronize(e1));
-          float ms = 0.f;
-          EK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-          ms /= (float)reps;
-          row += (row.empty() ? "" : ", ") + std::string("\"") + std::to_string(lanes) + "\": " +
-                 std::to_string(1000.0 * ms);
-          if (best == 0 || ms < best_ms) {
-            best = lanes;
-            best_ms = ms;
+        for (int seg : {8, 4})
+          for (int lanes : {32, 16, 8}) {
+            if (!pline_fits(n, lanes, seg)) continue;
+            sweep(lanes, seg);  // warm-up
+            after_launch(c);
+            EK_CUDA(cudaEventRecord(e0, s));
+            for (int r = 0; r < reps; ++r) sweep(lanes, seg);
+            EK_CUDA(cudaEventRecord(e1, s));
+            after_launch(c);
+            EK_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            EK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            ms /= (float)reps;
+            row += (row.empty() ? "" : ", ") + std::string("\"") + std::to_string(lanes) + "x" + std::to_string(seg) +
+                   "\": " + std::to_string(1000.0 * ms);
+            if (best == 0 || ms < best_ms) {
+              best = lanes;
+              best_seg = seg;
+              best_ms = ms;
+            }
           }
-        }
         (xl ? PL.lanes_x : PL.lanes_y)[l] = best;
+        (xl ? PL.seg_x : PL.seg_y)[l] = best_seg;
         report += std::string(first ? "" : ", ") + "{\"level\": " + std::to_string(l) + ", \"dir\": \"" +
                   (xl ? "x" : "y") + "\", \"n\": " + std::to_string(n) + ", \"us\": {" + row +
-                  "}, \"lanes\": " + std::to_string(best) + "}";
+                  "}, \"lanes\": " + std::to_string(best) + ", \"seg\": " + std::to_string(best_seg) + "}";
         first = false;
       }
     }

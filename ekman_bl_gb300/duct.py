@@ -34,7 +34,7 @@ EXPORTS = [
     "ekgpu_unet_create", "ekgpu_unet_destroy", "ekgpu_unet_last_error", "ekgpu_unet_num_params",
     "ekgpu_unet_set_params", "ekgpu_unet_get_params", "ekgpu_unet_forward", "ekgpu_unet_train_step",
     "ekgpu_unet_gradient", "ekgpu_guess_geometry", "ekgpu_set_poisson_guess", "ekgpu_set_pair_sink",
-    "ekgpu_pair_count", "ekgpu_last_guess_stats", "ekgpu_mg_autotune", "ekgpu_mg_set_lanes", "ekgpu_mg_levels",
+    "ekgpu_pair_count", "ekgpu_last_guess_stats", "ekgpu_mg_autotune", "ekgpu_mg_set_layout", "ekgpu_mg_levels",
 ]
 
 
@@ -95,7 +95,7 @@ def load_library():
     L.ekgpu_pair_count.argtypes = [V, C.POINTER(C.c_int)]
     L.ekgpu_last_guess_stats.argtypes = [V, _D, _D]
     L.ekgpu_mg_autotune.argtypes = [V, C.c_int, C.c_char_p, C.c_int]
-    L.ekgpu_mg_set_lanes.argtypes = [V, C.c_int, C.c_int, C.c_int]
+    L.ekgpu_mg_set_layout.argtypes = [V, C.c_int, C.c_int, C.c_int, C.c_int]
     L.ekgpu_mg_levels.argtypes = [V, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]
     L.ekgpu_get_field.argtypes = [V, C.c_int, _D]
     L.ekgpu_put_field.argtypes = [V, C.c_int, _D]
@@ -313,8 +313,10 @@ class DuctSolver:
         self._check(self._L.ekgpu_mg_autotune(self._h, reps, buf, len(buf)))
         return json.loads(buf.value.decode())
 
-    def mg_set_lanes(self, level: int, direction: int, lanes: int):
-        self._check(self._L.ekgpu_mg_set_lanes(self._h, level, direction, lanes))
+    def mg_set_layout(self, level: int, direction: int, lanes: int, seg: int = 8):
+        """Problems per block (8/16/32) and segment rows (4/8) of the line
+        solves at one level and direction (0 y-lines, 1 x-lines); 0 = default."""
+        self._check(self._L.ekgpu_mg_set_layout(self._h, level, direction, lanes, seg))
 
     def mg_levels(self):
         """[(nx, ny)] of the multigrid levels, coarsest first."""

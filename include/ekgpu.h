@@ -262,15 +262,17 @@ int ekgpu_save_stats(ek_ctx *ctx, ek_stats *stats);
 
 /* ---- Tile-shape autotuner of the mixed solver's line solves ----------------
  * (No counterpart in the reference.)  For every multigrid level l = 2..ngrid
- * and both line directions, time one zebra sweep in each valid layout (8, 16
- * or 32 problems per block) `reps` times on the context's own work arrays,
- * and use the fastest from then on.  The arithmetic of each problem is the
- * same in every layout, so tuning changes no result.  report (may be NULL)
- * receives the timings as JSON text.  Needs mg_fast = 1 and metrics. */
+ * and both line directions, time one zebra sweep in each valid layout -- 8,
+ * 16 or 32 problems per block, line segments of 8 or 4 rows -- `reps` times
+ * on the context's own work arrays, and use the fastest from then on.  Each
+ * problem's arithmetic does not depend on the problems per block; the
+ * segment length changes the order of the line elimination (results agree
+ * to the solve tolerance, not bit for bit).  report (may be NULL) receives
+ * the timings as JSON text.  Needs mg_fast = 1 and metrics. */
 int ekgpu_mg_autotune(ek_ctx *ctx, int reps, char *report, int report_len);
-/* Set one layout by hand (lanes 0 restores the default rule; dir 0 y-lines,
- * 1 x-lines), e.g. to replay a table tuned earlier. */
-int ekgpu_mg_set_lanes(ek_ctx *ctx, int level, int dir, int lanes);
+/* Set one layout by hand (0 restores the default: lanes by line length,
+ * seg 8; dir 0 y-lines, 1 x-lines), e.g. to replay a table tuned earlier. */
+int ekgpu_mg_set_layout(ek_ctx *ctx, int level, int dir, int lanes, int seg);
 /* The multigrid levels: ngrid and the sizes nx[l-1] x ny[l-1], l = 1..ngrid. */
 int ekgpu_mg_levels(ek_ctx *ctx, int *ngrid, int *nx, int *ny, int cap);
 

@@ -1,9 +1,10 @@
 """Tile-shape autotuner of the mixed solver's line solves.
 
-Each problem's arithmetic is the same in every layout (8, 16 or 32 problems
-per block): the separator system of a line is solved by the problem's own
-lane.  So a solve in any forced layout, and after autotuning, must equal the
-default-layout solve bit for bit, with the same cycle counts.
+Each problem's arithmetic does not depend on the problems per block (8, 16
+or 32): a line's segments and separators are all the problem's own lane.  So
+with 8-row segments every layout gives the default solve bit for bit.  With
+4-row segments the elimination order changes: the solve then meets the same
+tolerance in the same number of cycles and agrees to that tolerance.
 """
 import math
 
@@ -42,10 +43,25 @@ def test_layouts_give_identical_solves():
     for lanes in (8, 16, 32):
         for lev in range(2, ngrid + 1):
             for d in (0, 1):
-                g.mg_set_lanes(lev, d, lanes)
+                g.mg_set_layout(lev, d, lanes, 8)
         phi, st, c = g.multigrid_mudpack(rhs, kx2)
         assert c == 0 and st["max_cycles"] == st0["max_cycles"] and st["min_cycles"] == st0["min_cycles"]
         assert np.array_equal(phi, phi0), lanes
+
+
+def test_short_segments_meet_the_tolerance():
+    p, g = mixed_solver()
+    rhs, kx2 = batch(p, seed=5)
+    phi0, st0, _ = g.multigrid_mudpack(rhs, kx2)
+    ngrid = len(g.mg_levels())
+    for lanes in (8, 16):
+        for lev in range(2, ngrid + 1):
+            for d in (0, 1):
+                g.mg_set_layout(lev, d, lanes, 4)
+        phi, st, c = g.multigrid_mudpack(rhs, kx2)
+        assert c == 0 and st["n_not_converged"] == 0 and st["max_residual"] <= p.mg_tol
+        assert abs(st["max_cycles"] - st0["max_cycles"]) <= 1
+        assert np.linalg.norm(phi - phi0) <= 1e-8 * np.linalg.norm(phi0)
 
 
 def test_autotune_picks_valid_layouts_and_changes_nothing():
@@ -57,7 +73,8 @@ def test_autotune_picks_valid_layouts_and_changes_nothing():
     levels = g.mg_levels()
     assert len(rep) == 2 * (len(levels) - 1)
     for row in rep:
-        assert row["lanes"] in (8, 16, 32) and str(row["lanes"]) in row["us"]
+        assert row["lanes"] in (8, 16, 32) and row["seg"] in (4, 8)
+        assert f'{row["lanes"]}x{row["seg"]}' in row["us"]
         assert all(v > 0 for v in row["us"].values())
         nx, ny = levels[row["level"] - 1]
         assert row["n"] == (nx if row["dir"] == "x" else ny)
@@ -65,8 +82,8 @@ def test_autotune_picks_valid_layouts_and_changes_nothing():
     for x, y in zip(g.download(), a0):
         assert np.array_equal(x, y)
     phi, st, c = g.multigrid_mudpack(rhs, kx2)
-    assert c == 0 and st["max_cycles"] == st0["max_cycles"]
-    assert np.array_equal(phi, phi0)
+    assert c == 0 and st["max_residual"] <= p.mg_tol
+    assert np.linalg.norm(phi - phi0) <= 1e-8 * np.linalg.norm(phi0)
 
 
 def test_autotune_needs_the_mixed_solver():
