@@ -389,13 +389,15 @@ __global__ void __launch_bounds__(64) k_f_xline(FastDev g, int level, int j0, in
 // XL: x-line (along i, the periodic wrap couplings taken from the ghosts'
 // current values); else y-line (along j).
 enum { SH_A, SH_B, SH_C, SH_D, SH_YF, SH_VF, SH_WF, SH_YL, SH_VL, SH_WL, SH_S, SH_N };
+// 4-row segments are capped at 48 registers, so that two or three blocks
+// share an SM (their per-thread arrays are half as large)
 template <bool XL, bool ORTH, int LANES, int SEG>
-__global__ void __launch_bounds__(1024) k_f_pline(FastDev g, int level, int l0, int lstep, int mb, int me) {
+__global__ void __launch_bounds__(1024) __maxnreg__(SEG == 4 ? 48 : 64) k_f_pline(FastDev g, int level, int l0, int lstep, int mb, int me) {
   constexpr int kSegMax = SEG;
   if (*g.alldone) return;
   extern __shared__ float sh[];
   const int K = blockDim.y;
-  auto S = [&](int arr, int seg) -> float & { return sh[((size_t)arr * K + seg) * LANES + threadIdx.x]; };
+  auto S = [&](int arr, int seg) -> float & { return sh[(arr * K + seg) * LANES + threadIdx.x]; };
   const LvF L = g.lv[level - 1];
   const int P = g.P;
   const int nx = L.nx, ny = L.ny;
@@ -407,36 +409,39 @@ __global__ void __launch_bounds__(1024) k_f_pline(FastDev g, int level, int l0, 
   const int line = l0 + lstep * (int)blockIdx.x;
   const int m = mb + (s < me ? 1 : 0);
   const int lo = 1 + s * (mb + 1) + min(s, me);
-  const size_t npt = (size_t)nx * ny;
-  const size_t si = P, sj = (size_t)(nx + 2) * P;
+  // 32-bit offsets: the host checks that (nx+2)(ny+2)P and 11 nx ny fit
+  const unsigned npt = (unsigned)nx * (unsigned)ny;
+  const unsigned si = (unsigned)P, sj = (unsigned)(nx + 2) * (unsigned)P;
   const float kx2 = (float)g.kx2[pp];
   const float *cf = L.cof;
   // row k of the line: a x(k-1) + b x(k) + c x(k+1) = d
   auto row = [&](int k, float &a, float &b, float &c, float &d) {
     const int i = XL ? k : line, j = XL ? line : k;
-    const size_t pt = (size_t)(j - 1) * nx + (i - 1);
-    const float *ep = &L.e[((size_t)j * (nx + 2) + i) * P + pp];
-    b = ((-kx2 * cf[10 * npt + pt]) - cf[8 * npt + pt]) + cf[9 * npt + pt];
-    float dd = L.r[pt * P + pp];
+    const unsigned pt = (unsigned)((j - 1) * nx + (i - 1));
+    const float *ep = L.e + ((unsigned)(j * (nx + 2) + i) * si + (unsigned)pp);
+    const float *cp = cf + pt;
+    b = ((-kx2 * cp[10 * npt]) - cp[8 * npt]) + cp[9 * npt];
+    float dd = L.r[pt * si + (unsigned)pp];
     if (XL) {
-      a = cf[4 * npt + pt];
-      c = cf[pt];
-      dd = dd - cf[2 * npt + pt] * ep[sj] - cf[6 * npt + pt] * ep[-(long)sj];
+      a = cp[4 * npt];
+      c = cp[0];
+      dd = dd - cp[2 * npt] * ep[sj] - cp[6 * npt] * *(ep - sj);
     } else {
-      a = cf[6 * npt + pt];
-      c = cf[2 * npt + pt];
-      dd = dd - cf[pt] * ep[si] - cf[4 * npt + pt] * ep[-(long)si];
+      a = cp[6 * npt];
+      c = cp[2 * npt];
+      dd = dd - cp[0] * ep[si] - cp[4 * npt] * *(ep - si);
     }
     if (!ORTH)
-      dd = dd - cf[npt + pt] * ep[si + sj] - cf[3 * npt + pt] * ep[sj - si] - cf[5 * npt + pt] * ep[-(long)(si + sj)] -
-           cf[7 * npt + pt] * ep[si - sj];
+      dd = dd - cp[npt] * ep[si + sj] - cp[3 * npt] * ep[sj - si] - cp[5 * npt] * *(ep - (si + sj)) -
+           cp[7 * npt] * *(ep - (sj - si));
     d = dd;
   };
   auto store = [&](int k, float x) {
     const int i = XL ? k : line, j = XL ? line : k;
-    L.e[((size_t)j * (nx + 2) + i) * P + p] = x;
-    if (i == nx - 1) L.e[((size_t)j * (nx + 2)) * P + p] = x;
-    if (i == 2) L.e[((size_t)j * (nx + 2) + nx + 1) * P + p] = x;
+    float *erow = L.e + (unsigned)(j * (nx + 2)) * si + (unsigned)p;
+    erow[(unsigned)i * si] = x;
+    if (i == nx - 1) erow[0] = x;
+    if (i == 2) erow[(unsigned)(nx + 1) * si] = x;
   };
   // phase 1: every load of the segment (rows past its end repeat its last
   // row, so all addresses are valid and no load waits on arithmetic)
@@ -446,13 +451,13 @@ __global__ void __launch_bounds__(1024) k_f_pline(FastDev g, int level, int l0, 
   if (XL) {
     // the periodic wrap of an x-line: i = 1 couples to the ghost e(0) =
     // e(nx-1), i = nx to e(nx+1) = e(2), both taken from current values
-    const float *erow = &L.e[(size_t)line * (nx + 2) * P + pp];
+    const float *erow = L.e + (unsigned)(line * (nx + 2)) * si + (unsigned)pp;
     if (s == 0) {
       dv[0] -= av[0] * erow[0];
       av[0] = 0.f;
     }
     if (s == K - 1) {
-      const float gh = erow[(size_t)(nx + 1) * si];
+      const float gh = erow[(unsigned)(nx + 1) * si];
 #pragma unroll
       for (int u = 0; u < kSegMax; ++u) {
         const bool hit = (u == m - 1);
@@ -785,6 +790,9 @@ bool pline_fits(int n, int lanes, int seg) {
 void launch_pline(const FastDev &g, int l, bool xl, int l0, int lstep, int nline, int n, int lanes, int seg,
                   cudaStream_t s) {
   const int K = pline_segments(n, seg);
+  // the kernel indexes with 32-bit offsets
+  if ((size_t)(g.nfx + 2) * (g.nfy + 2) * g.P >= (1ull << 31) || 11ull * g.nfx * g.nfy >= (1ull << 31))
+    throw CudaError("line solve: grid x problems beyond 32-bit offsets");
   if (!pline_fits(n, lanes, seg)) {
     const unsigned b = (unsigned)(((long)nline * g.P + 63) / 64);
     if (xl) k_f_xline<<<b, 64, 0, s>>>(g, l, l0, nline);
