@@ -529,6 +529,8 @@ int ekgpu_set_metrics(ek_ctx *h, const ek_metrics *m) {
     up(c.m.c11, m->cjob_11, 2 * n2); up(c.m.c12, m->cjob_12, 2 * n2);
     up(c.m.c21, m->cjob_21, 2 * n2); up(c.m.c22, m->cjob_22, 2 * n2);
     up(c.m.thbar, m->th_bar, n2);
+    if (!c.m.pg) c.m.pg = dalloc<double>(c, 11 * n2);
+    launch_metric_tables(c);
     std::vector<double> jac(m->int_jacob, m->int_jacob + n2), g11(m->gmat_11, m->gmat_11 + 2 * n2),
         g12(m->gmat_12, m->gmat_12 + 2 * n2), g22(m->gmat_22, m->gmat_22 + 2 * n2), c22(m->cjob_22, m->cjob_22 + 2 * n2);
     // boundary rows and Thomas factors of every field, substep and direction

@@ -80,6 +80,11 @@ __device__ __forceinline__ FF operator*(FF a, FF b) {
 // Device copies of the JACOBI_TRANS metric arrays.
 struct Metrics {
   double *jac, *g11, *g12, *g22, *c11, *c12, *c21, *c22, *thbar;
+  // per-cell coefficient planes (metric-only, built by launch_metric_tables):
+  // pg[0..4] the pressure-gradient weights of the CJOB_12/CJOB_22 combination
+  // and pg[5..9] of the CJOB_11/CJOB_21 one, for (p0, p(k+1), p(k-1),
+  // p(j+1), p(j-1)), each with its 0.5; pg[10] = 1/INT_JACOB
+  double *pg = nullptr;
 };
 
 // Boundary rows of one ADI direction (a row of a tridiagonal line replaced
@@ -364,6 +369,7 @@ void launch_c2r(Ctx &c, const C2rArgs &a);
 
 // RK pieces (ek_rk.cu)
 void launch_spectral_rhs(Ctx &c, int rk);
+void launch_metric_tables(Ctx &c);
 void launch_face_velocity(Ctx &c);
 void launch_adi(Ctx &c, int field, int rk);
 void launch_th_corners(Ctx &c);

@@ -621,10 +621,16 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_f_resid32(FastDev g, int lev
   const size_t npt = (size_t)nx * L.ny;
   const size_t si = P, sj = (size_t)(nx + 2) * P;
   const float kx2 = (float)g.kx2[p];
-  const float *cf = L.cof;
+  // restrict-qualified copies: the stores cannot alias the loads, so the
+  // unrolled iterations' loads are issued together
+  const float *__restrict__ cf = L.cof;
+  const float *__restrict__ ee = L.e;
+  const float *__restrict__ rr = L.r;
+  float *__restrict__ scr = g.scr;
+#pragma unroll 4
   for (int i = 1 + (int)threadIdx.y; i <= nx; i += kRowWarps) {
     const size_t pt = (size_t)(j - 1) * nx + (i - 1);
-    const float *ep = &L.e[((size_t)j * (nx + 2) + i) * P + p];
+    const float *ep = &ee[((size_t)j * (nx + 2) + i) * P + p];
     float s = cf[pt] * ep[si] + cf[2 * npt + pt] * ep[sj] + cf[4 * npt + pt] * ep[-(long)si] +
               cf[6 * npt + pt] * ep[-(long)sj];
     if (!g.orth)
@@ -632,7 +638,7 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_f_resid32(FastDev g, int lev
            cf[7 * npt + pt] * ep[si - sj];
     const float c9 = ((-kx2 * cf[10 * npt + pt]) - cf[8 * npt + pt]) + cf[9 * npt + pt];
     s += c9 * ep[0];
-    g.scr[((size_t)j * (nx + 2) + i) * P + p] = L.r[pt * P + p] - s;
+    scr[((size_t)j * (nx + 2) + i) * P + p] = rr[pt * P + p] - s;
   }
 }
 
@@ -647,8 +653,12 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_f_restrict(FastDev g, int le
   const int nx = F.nx, ny = F.ny, ncx = C.nx, ncy = C.ny;
   const int ix = (ncx == nx) ? 0 : 1, jy = (ncy == ny) ? 0 : 1;
   const int jc = (int)blockIdx.y;
+  const float *__restrict__ scr = g.scr;
+  float *__restrict__ ce = C.e;
+  float *__restrict__ cr = C.r;
+#pragma unroll 4
   for (int ic = (int)threadIdx.y; ic <= ncx + 1; ic += kRowWarps) {
-    C.e[((size_t)jc * (ncx + 2) + ic) * P + p] = 0.f;
+    ce[((size_t)jc * (ncx + 2) + ic) * P + p] = 0.f;
     if (ic < 1 || ic > ncx || jc < 1 || jc > ncy) continue;
     const int i = ic + ix * (ic - 1), j = jc + jy * (jc - 1);
     int im1 = i - 1, ip1 = i + 1, jm1 = j - 1, jp1 = j + 1;
@@ -662,8 +672,8 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_f_restrict(FastDev g, int le
       jm1 = max(j - 1, 2);
       jp1 = min(j + 1, ny - 1);
     }
-    auto R = [&](int a, int b) { return g.scr[((size_t)b * (nx + 2) + a) * P + p]; };
-    C.r[((size_t)(jc - 1) * ncx + (ic - 1)) * P + p] =
+    auto R = [&](int a, int b) { return scr[((size_t)b * (nx + 2) + a) * P + p]; };
+    cr[((size_t)(jc - 1) * ncx + (ic - 1)) * P + p] =
         (R(im1, jm1) + R(ip1, jm1) + R(im1, jp1) + R(ip1, jp1) + 2.f * (R(im1, j) + R(ip1, j) + R(i, jm1) + R(i, jp1)) +
          4.f * R(i, j)) * .0625f;
   }
@@ -698,9 +708,12 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_f_prolong_x(FastDev g, int l
   const int rr = (int)blockIdx.y;
   const int j = ycoarse ? 2 * rr + 1 : rr + 1;
   const int jc = ycoarse ? j / 2 + 1 : j;
-  auto pc = [&](int ic) { return C.e[((size_t)jc * (ncx + 2) + ic) * P + p]; };
+  const float *__restrict__ ce = C.e;
+  float *__restrict__ scr = g.scr;
+  auto pc = [&](int ic) { return ce[((size_t)jc * (ncx + 2) + ic) * P + p]; };
+#pragma unroll 4
   for (int i = 1 + (int)threadIdx.y; i <= nx; i += kRowWarps)
-    g.scr[((size_t)j * (nx + 2) + i) * P + p] = prolon1f(i, ncx, nx, cubic, pc);
+    scr[((size_t)j * (nx + 2) + i) * P + p] = prolon1f(i, ncx, nx, cubic, pc);
 }
 
 // stage 2: the rows between (cubic or linear in y), then e += correction,
@@ -716,8 +729,12 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_f_prolong_y(FastDev g, int l
   const bool ycoarse = ncy < ny;
   const bool cubic = ncy >= 4;
   const int j = 1 + (int)blockIdx.y;
+  const float *__restrict__ scr = g.scr;
+  float *__restrict__ ef = F.e;
+  const size_t rowj = (size_t)j * (nx + 2) * P + p;
+#pragma unroll 4
   for (int i = 1 + (int)threadIdx.y; i <= nx; i += kRowWarps) {
-    auto Q = [&](int jj) { return g.scr[((size_t)jj * (nx + 2) + i) * P + p]; };
+    auto Q = [&](int jj) { return scr[((size_t)jj * (nx + 2) + i) * P + p]; };
     float v;
     if (ycoarse && !(j & 1)) {
       if (!cubic) v = 0.5f * (Q(j - 1) + Q(j + 1));
@@ -727,11 +744,10 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_f_prolong_y(FastDev g, int l
     } else {
       v = Q(j);
     }
-    float &e = E(F, P, i, j, p);
-    const float ne = e + v;
-    e = ne;
-    if (i == nx - 1) E(F, P, 0, j, p) = ne;
-    if (i == 2) E(F, P, nx + 1, j, p) = ne;
+    const float ne = ef[rowj + (size_t)i * P] + v;
+    ef[rowj + (size_t)i * P] = ne;
+    if (i == nx - 1) ef[rowj] = ne;
+    if (i == 2) ef[rowj + (size_t)(nx + 1) * P] = ne;
   }
 }
 
@@ -744,18 +760,23 @@ __global__ void __launch_bounds__(32 * kRY) k_f_update_ff(FastDev g) {
   if (p >= P || g.done[p]) return;
   const int nx = g.nfx, j = 1 + (int)blockIdx.y;
   const LvF &F = g.lv[g.ngrid - 1];
+  const float *__restrict__ ef = F.e;
+  float *__restrict__ ph = g.phh;
+  float *__restrict__ pl = g.phl;
+  const size_t rowj = (size_t)j * (nx + 2) * P + p;
+#pragma unroll 4
   for (int i = 1 + (int)threadIdx.y; i <= nx; i += kRY) {
-    const size_t q = ((size_t)j * (nx + 2) + i) * P + p;
-    const FF v = FF(g.phh[q], g.phl[q]) + FF(E(F, P, i, j, p), 0.f);
-    g.phh[q] = v.hi;
-    g.phl[q] = v.lo;
+    const size_t q = rowj + (size_t)i * P;
+    const FF v = FF(ph[q], pl[q]) + FF(ef[q], 0.f);
+    ph[q] = v.hi;
+    pl[q] = v.lo;
     if (i == nx - 1) {
-      g.phh[((size_t)j * (nx + 2)) * P + p] = v.hi;
-      g.phl[((size_t)j * (nx + 2)) * P + p] = v.lo;
+      ph[rowj] = v.hi;
+      pl[rowj] = v.lo;
     }
     if (i == 2) {
-      g.phh[((size_t)j * (nx + 2) + nx + 1) * P + p] = v.hi;
-      g.phl[((size_t)j * (nx + 2) + nx + 1) * P + p] = v.lo;
+      ph[rowj + (size_t)(nx + 1) * P] = v.hi;
+      pl[rowj + (size_t)(nx + 1) * P] = v.lo;
     }
   }
 }

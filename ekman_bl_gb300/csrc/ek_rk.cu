@@ -71,6 +71,39 @@ __global__ void k_sponge_mean(Dims d, const cplx_t *CU3, int ny_sponge, double w
 // curvilinear pressure gradient), 411-455 (mean forcing, mode 0),
 // 461-523 (viscous x term, Coriolis on every kx, buoyancy) and 540-633
 // (scalar RHS with the background stratification term).
+// sum_t G[t] P[t] over the five pressure points (p0, p(k+1), p(k-1),
+// p(j+1), p(j-1)) with the weights of coefficient planes g0..g0+4
+__device__ __forceinline__ cplx_t pg_dot(const double *pg, size_t n2, int g0, size_t mm, cplx_t p0, cplx_t pkp,
+                                         cplx_t pkm, cplx_t pjp, cplx_t pjm) {
+  const double w0 = pg[(g0 + 0) * n2 + mm], w1 = pg[(g0 + 1) * n2 + mm], w2 = pg[(g0 + 2) * n2 + mm];
+  const double w3 = pg[(g0 + 3) * n2 + mm], w4 = pg[(g0 + 4) * n2 + mm];
+  cplx_t r;
+  r.re = fma(w4, pjm.re, fma(w3, pjp.re, fma(w2, pkm.re, fma(w1, pkp.re, w0 * p0.re))));
+  r.im = fma(w4, pjm.im, fma(w3, pjp.im, fma(w2, pkm.im, fma(w1, pkp.im, w0 * p0.im))));
+  return r;
+}
+
+// The pressure-gradient weights and 1/J per cell, K = 1..NZ, J = 1..NY: the
+// metric combinations that the spectral right-hand side and the projection
+// would otherwise rebuild for every kx mode
+__global__ void k_metric_tables(Dims d, Metrics m) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  const size_t n2 = (size_t)d.LDM * (d.NY + 3);
+  if (k > d.NZ + 2 || j > d.NY + 2) return;
+  const size_t mm = d.m2(k, j);
+  double w[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (k >= 1 && k <= d.NZ && j >= 1 && j <= d.NY) {
+    const double e = 0.5 * m.c12[d.m3(k + 1, j, 2)], f = 0.5 * m.c12[d.m3(k, j, 2)];
+    const double g = 0.5 * m.c22[d.m3(k, j + 1, 1)], h = 0.5 * m.c22[d.m3(k, j, 1)];
+    const double a = 0.5 * m.c11[d.m3(k + 1, j, 2)], b = 0.5 * m.c11[d.m3(k, j, 2)];
+    const double c = 0.5 * m.c21[d.m3(k, j + 1, 1)], dd = 0.5 * m.c21[d.m3(k, j, 1)];
+    w[0] = ((e - f) + g) - h; w[1] = e; w[2] = -f; w[3] = g; w[4] = -h;
+    w[5] = ((a - b) + c) - dd; w[6] = a; w[7] = -b; w[8] = c; w[9] = -dd;
+    w[10] = 1.0 / m.jac[mm];
+  }
+  for (int t = 0; t < 11; ++t) m.pg[t * n2 + mm] = w[t];
+}
+
 __global__ void k_spectral_rhs(SpecArgs a) {
   const Dims &d = a.d;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -93,14 +126,11 @@ __global__ void k_spectral_rhs(SpecArgs a) {
     const cplx_t p0 = CP[q];
     const cplx_t pkp = CP[d.ic(i, k + 1, j)], pkm = CP[d.ic(i, k - 1, j)];
     const cplx_t pjp = CP[d.ic(i, k, j + 1)], pjm = CP[d.ic(i, k, j - 1)];
-    const cplx_t cs1 = csub(cadd(csub(cscl(0.5 * a.m.c11[d.m3(k + 1, j, 2)], cadd(p0, pkp)),
-                                      cscl(0.5 * a.m.c11[d.m3(k, j, 2)], cadd(p0, pkm))),
-                                 cscl(0.5 * a.m.c21[d.m3(k, j + 1, 1)], cadd(p0, pjp))),
-                            cscl(0.5 * a.m.c21[d.m3(k, j, 1)], cadd(p0, pjm)));
-    const cplx_t cs2 = csub(cadd(csub(cscl(0.5 * a.m.c12[d.m3(k + 1, j, 2)], cadd(p0, pkp)),
-                                      cscl(0.5 * a.m.c12[d.m3(k, j, 2)], cadd(p0, pkm))),
-                                 cscl(0.5 * a.m.c22[d.m3(k, j + 1, 1)], cadd(p0, pjp))),
-                            cscl(0.5 * a.m.c22[d.m3(k, j, 1)], cadd(p0, pjm)));
+    // the curvilinear pressure gradient (duct.F90:371-409) from the
+    // per-cell weight planes
+    const size_t n2 = (size_t)d.LDM * (d.NY + 3), mm = d.m2(k, j);
+    const cplx_t cs1 = pg_dot(a.m.pg, n2, 5, mm, p0, pkp, pkm, pjp, pjm);
+    const cplx_t cs2 = pg_dot(a.m.pg, n2, 0, mm, p0, pkp, pkm, pjp, pjm);
     const cplx_t ik = {0.0, a.kx[i]};
     r1 = csub(r1, cmul(cscl(jac, cscl(a.T4, ik)), p0));
     r2 = csub(r2, cscl(a.T4, cs2));
@@ -436,23 +466,17 @@ __global__ void k_correct_cells(Dims d, Metrics m, const double *kx, const cplx_
   const size_t q = d.ic(i, k, j);
   const size_t sK = d.LDC, sJ = (size_t)d.LDC * d.NZ2;
   auto P = [&](int dk, int dj) { return CR1[q + (long)dk * (long)sK + (long)dj * (long)sJ]; };
-  const double jac = m.jac[d.m2(k, j)];
-  CU1[q] = csub(CU1[q], cmul(cplx_t{0.0, kx[i]}, P(0, 0)));
-  const cplx_t t2 = csub(cadd(csub(cscl(m.c22[d.m3(k, j + 1, 1)], cadd(P(0, 0), P(0, 1))),
-                                   cscl(m.c22[d.m3(k, j, 1)], cadd(P(0, 0), P(0, -1)))),
-                              cscl(m.c12[d.m3(k + 1, j, 2)], cadd(P(1, 0), P(0, 0)))),
-                         cscl(m.c12[d.m3(k, j, 2)], cadd(P(0, 0), P(-1, 0))));
-  const cplx_t u2 = cscl(0.5, t2);
+  const size_t n2 = (size_t)d.LDM * (d.NY + 3), mm = d.m2(k, j);
+  const cplx_t p00 = P(0, 0), p10 = P(1, 0), pm0 = P(-1, 0), p01 = P(0, 1), p0m = P(0, -1);
+  const cplx_t o1 = CU1[q];
+  CU1[q] = cplx_t{fma(kx[i], p00.im, o1.re), fma(-kx[i], p00.re, o1.im)};  // CU1 -= i kx phi
+  const double rj = m.pg[10 * n2 + mm];
+  const cplx_t u2 = pg_dot(m.pg, n2, 0, mm, p00, p10, pm0, p01, p0m);  // 0.5 (CJOB_22, CJOB_12 terms)
   const cplx_t o2 = CU2[q];
-  const DivBy div(jac);
-  CU2[q] = cplx_t{o2.re - div(u2.re), o2.im - div(u2.im)};
-  const cplx_t t3 = csub(cadd(csub(cscl(m.c11[d.m3(k + 1, j, 2)], cadd(P(0, 0), P(1, 0))),
-                                   cscl(m.c11[d.m3(k, j, 2)], cadd(P(0, 0), P(-1, 0)))),
-                              cscl(m.c21[d.m3(k, j + 1, 1)], cadd(P(0, 1), P(0, 0)))),
-                         cscl(m.c21[d.m3(k, j, 1)], cadd(P(0, 0), P(0, -1))));
-  const cplx_t u3 = cscl(0.5, t3);
+  CU2[q] = cplx_t{fma(-u2.re, rj, o2.re), fma(-u2.im, rj, o2.im)};
+  const cplx_t u3 = pg_dot(m.pg, n2, 5, mm, p00, p10, pm0, p01, p0m);  // 0.5 (CJOB_11, CJOB_21 terms)
   const cplx_t o3 = CU3[q];
-  CU3[q] = cplx_t{o3.re - div(u3.re), o3.im - div(u3.im)};
+  CU3[q] = cplx_t{fma(-u3.re, rj, o3.re), fma(-u3.im, rj, o3.im)};
 }
 
 // Divergence after the projection (duct.F90:2754-2761) into CS.
@@ -490,6 +514,13 @@ __global__ void k_div_sum(Dims d, const double *S, double *part) {
 }
 
 }  // namespace
+
+void launch_metric_tables(Ctx &c) {
+  const Dims &d = c.d;
+  k_metric_tables<<<dim3((unsigned)((d.NZ + 3 + 63) / 64), (unsigned)(d.NY + 3)), 64, 0, c.stream>>>(d, c.m);
+  after_launch(c);
+  EK_CUDA(cudaStreamSynchronize(c.stream));
+}
 
 void launch_spectral_rhs(Ctx &c, int rk) {
   SpecArgs a;
