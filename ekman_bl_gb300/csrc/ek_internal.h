@@ -281,6 +281,8 @@ struct Ctx {
   GuessState guess;
   // SAVE_STATS_CURVI planes and sums (ek_stats.cu)
   double *stats_buf = nullptr;
+  // per-cell right-hand-side weights of the two ADI sweeps (k_adi_tab)
+  double *adi_tab = nullptr;
   // divergence check
   double *div_part = nullptr;
   double last_div = 0.0;

@@ -262,7 +262,36 @@ struct AdiArgs {
   const double *bcw;
   double coef;
   int js, je, zs, ze;
+  const double *tab;  // per-cell right-hand-side weights of this sweep (k_adi_tab)
 };
+
+// Right-hand-side weights of one ADI sweep per cell (tab[t * n2 + m2(k, j)]),
+// so that the line kernel forms each row with four or five multiply-adds
+// instead of rebuilding the metric terms for every x point:
+//   y sweep: v = 0.5 R + t0 phi + t1 phi(k+1) + t2 phi(k-1)
+//            t0 = 0.5 J - c (G11(k+1) + G11(k)), t1 = c G11(k+1), t2 = c G11(k)
+//   z sweep: v = 0.5 R + t3 phi + t0 phs + t1 phs(j+1) + t2 phs(j-1)
+//            t0 = J - c (G22(j+1) + G22(j)), t1 = c G22(j+1), t2 = c G22(j), t3 = -0.5 J
+// (c = NU H/2 [/PR]; the same algebra as duct.F90:1640-1660, 1877-1905, ...)
+template <bool ZS>
+__global__ void k_adi_tab(Dims d, Metrics m, double coef, double *tab) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (k > d.NZ + 1 || j > d.NY + 1 || k < 1 || j < 1) return;
+  const size_t n2 = (size_t)d.LDM * (d.NY + 3), mm = d.m2(k, j);
+  const double jac = m.jac[mm];
+  if (!ZS) {
+    const double gp = m.g11[d.m3(k + 1, j, 2)], gm = m.g11[d.m3(k, j, 2)];
+    tab[mm] = 0.5 * jac - coef * (gp + gm);
+    tab[n2 + mm] = coef * gp;
+    tab[2 * n2 + mm] = coef * gm;
+  } else {
+    const double gp = m.g22[d.m3(k, j + 1, 1)], gm = m.g22[d.m3(k, j, 1)];
+    tab[mm] = jac - coef * (gp + gm);
+    tab[n2 + mm] = coef * gp;
+    tab[2 * n2 + mm] = coef * gm;
+    tab[3 * n2 + mm] = -0.5 * jac;
+  }
+}
 
 // CN-ADI line solves: a block owns 32 consecutive x points (lanes) of one
 // line.  Its kAdiWarps warps build the right-hand side of every row in
@@ -308,22 +337,18 @@ __global__ void __launch_bounds__(32 * kAdiWarps) k_adi(AdiArgs a) {
     double v = 0.0;
     if (act) {
       if (r >= r0 && r <= r1) {
+        const size_t n2 = (size_t)d.LDM * (d.NY + 3);
         if (!ZS) {
           const int k = line;
-          const size_t c = d.ip(i, k, r), sK = d.LDX;
-          const double jac = a.m.jac[d.m2(k, r)];
-          const double ph = a.phi_old[c];
-          const double s = a.R[c] - jac * ph;
-          const double gp = a.m.g11[d.m3(k + 1, r, 2)], gm = a.m.g11[d.m3(k, r, 2)];
-          v = 0.5 * s + jac * ph + a.coef * (gp * (a.phi_old[c + sK] - ph) - gm * (ph - a.phi_old[c - sK]));
+          const size_t c = d.ip(i, k, r), sK = d.LDX, mm = d.m2(k, r);
+          v = fma(0.5, a.R[c],
+                  fma(a.tab[mm], a.phi_old[c], fma(a.tab[n2 + mm], a.phi_old[c + sK], a.tab[2 * n2 + mm] * a.phi_old[c - sK])));
         } else {
           const int j = line;
-          const size_t c = d.ip(i, r, j), sJ = (size_t)d.LDX * d.NZ2;
-          const double jac = a.m.jac[d.m2(r, j)];
-          const double s = a.R[c] - jac * a.phi_old[c];
-          const double ps = a.phs[c];
-          const double gp = a.m.g22[d.m3(r, j + 1, 1)], gm = a.m.g22[d.m3(r, j, 1)];
-          v = 0.5 * s + jac * ps + a.coef * (+gp * (a.phs[c + sJ] - ps) - gm * (ps - a.phs[c - sJ]));
+          const size_t c = d.ip(i, r, j), sJ = (size_t)d.LDX * d.NZ2, mm = d.m2(r, j);
+          v = fma(0.5, a.R[c],
+                  fma(a.tab[3 * n2 + mm], a.phi_old[c],
+                      fma(a.tab[mm], a.phs[c], fma(a.tab[n2 + mm], a.phs[c + sJ], a.tab[2 * n2 + mm] * a.phs[c - sJ]))));
         }
       }
       for (int b = 0; b < a.bc.n; ++b) {
@@ -639,6 +664,19 @@ void launch_adi(Ctx &c, int field, int rk) {
   a.je = (field == 0) ? d.JET : d.JE;
   a.zs = (field == 0) ? d.ZST : d.ZS;
   a.ze = (field == 0) ? d.ZET : d.ZE;
+  const size_t n2 = (size_t)d.LDM * (d.NY + 3);
+  if (!c.adi_tab) {
+    EK_CUDA(cudaMalloc(&c.adi_tab, sizeof(double) * 8 * n2));
+    c.allocs.push_back(c.adi_tab);
+  }
+  a.tab = c.adi_tab;
+  {
+    const dim3 tg((unsigned)((d.NZ + 2 + 63) / 64), (unsigned)(d.NY + 2));
+    k_adi_tab<false><<<tg, 64, 0, c.stream>>>(d, c.m, coef, c.adi_tab);
+    after_launch(c);
+    k_adi_tab<true><<<tg, 64, 0, c.stream>>>(d, c.m, coef, c.adi_tab + 4 * n2);
+    after_launch(c);
+  }
   // y sweep
   a.out = c.PHS;
   a.fa = c.adi[field][rk][0].a;
@@ -653,6 +691,7 @@ void launch_adi(Ctx &c, int field, int rk) {
     after_launch(c);
   }
   // z sweep
+  a.tab = c.adi_tab + 4 * n2;
   a.out = phi;
   a.fa = c.adi[field][rk][1].a;
   a.fib = c.adi[field][rk][1].ib;
