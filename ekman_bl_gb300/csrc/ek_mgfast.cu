@@ -1206,14 +1206,19 @@ int mgfast_autotune(Ctx &c, int reps, std::string &report) {
         const int n = xl ? L.nx : L.ny;
         auto sweep = [&](int lanes, int seg) {
           if (xl) {
-            for (int col = 1; col <= 2; ++col)
+            for (int col = 1; col <= 2; ++col) {
               launch_pline(g, l, true, col, 2, (L.ny - col) / 2 + 1, L.nx, lanes, seg, s);
+              after_launch(c);
+            }
           } else {
             for (int col = 1; col <= 2; ++col) {
               LinePhase ph[2];
               const int nph = line_phases(L.nx, col, ph);
               for (int q = 0; q < nph; ++q)
-                if (ph[q].ncol > 0) launch_pline(g, l, false, ph[q].i0, ph[q].istep, ph[q].ncol, L.ny, lanes, seg, s);
+                if (ph[q].ncol > 0) {
+                  launch_pline(g, l, false, ph[q].i0, ph[q].istep, ph[q].ncol, L.ny, lanes, seg, s);
+                  after_launch(c);
+                }
             }
           }
         };
@@ -1224,11 +1229,9 @@ int mgfast_autotune(Ctx &c, int reps, std::string &report) {
           for (int lanes : {32, 16, 8}) {
             if (!pline_fits(n, lanes, seg)) continue;
             sweep(lanes, seg);  // warm-up
-            after_launch(c);
             EK_CUDA(cudaEventRecord(e0, s));
             for (int r = 0; r < reps; ++r) sweep(lanes, seg);
             EK_CUDA(cudaEventRecord(e1, s));
-            after_launch(c);
             EK_CUDA(cudaEventSynchronize(e1));
             float ms = 0.f;
             EK_CUDA(cudaEventElapsedTime(&ms, e0, e1));

@@ -27,6 +27,9 @@ def main():
     ap.add_argument("--mixed", action="store_true",
                     help="mixed-precision method: mg_fast = 1, fft_fp32 = 1 (needs --tol > 0)")
     ap.add_argument("--ff", action="store_true", help="float-float state-carrying transforms (ff_arith = 1)")
+    ap.add_argument("--autotune", action="store_true", help="tune the line-solve layouts first, as bench.py does")
+    ap.add_argument("--guess", action="store_true",
+                    help="train the learned initial guess on one warm-up step (50 Adam steps) and use it (needs --mixed)")
     args = ap.parse_args()
     ekbuild.build()
     w = WORKLOADS[args.workload]
@@ -43,7 +46,15 @@ def main():
         p.ff_arith = 1
     s = DuctSolver(p, metrics_from_grid(p, xp, yp))
     s.upload(*state)
+    if args.autotune:
+        s.mg_autotune(reps=3)
     s.rem_div_curv()
+    if args.guess:
+        from .learned import LearnedGuess
+        lg = LearnedGuess(s, factor=4, channels=32, seed=0)
+        lg.collect(1)
+        lg.train(iters=50, batch=16, lr=2e-3)
+        lg.enable()
     s.step(args.warmup)
     before = s.launch_count()
     if args.timing:
