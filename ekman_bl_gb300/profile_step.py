@@ -28,6 +28,7 @@ def main():
                     help="mixed-precision method: mg_fast = 1, fft_fp32 = 1 (needs --tol > 0)")
     ap.add_argument("--ff", action="store_true", help="float-float state-carrying transforms (ff_arith = 1)")
     ap.add_argument("--autotune", action="store_true", help="tune the line-solve layouts first, as bench.py does")
+    ap.add_argument("--layout", default="", help="LANESxSEG for every line solve (e.g. 8x8) instead of tuning")
     ap.add_argument("--guess", action="store_true",
                     help="train the learned initial guess on one warm-up step (50 Adam steps) and use it (needs --mixed)")
     args = ap.parse_args()
@@ -48,6 +49,11 @@ def main():
     s.upload(*state)
     if args.autotune:
         s.mg_autotune(reps=3)
+    if args.layout:
+        lanes, seg = (int(v) for v in args.layout.split("x"))
+        for lev in range(2, len(s.mg_levels()) + 1):
+            for d in (0, 1):
+                s.mg_set_layout(lev, d, lanes, seg)
     s.rem_div_curv()
     if args.guess:
         from .learned import LearnedGuess
