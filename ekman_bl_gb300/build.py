@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libekgpu.so")
-SOURCES = ["ek_api.cu", "ek_fft.cu", "ek_rk.cu", "ek_mg.cu", "ek_mgfast.cu", "ek_host.cpp", "ek_io.cpp", "ek_stats.cu", "ek_unet.cu", "ek_guess.cu"]
+SOURCES = ["ek_api.cu", "ek_fft.cu", "ek_rk.cu", "ek_mg.cu", "ek_mgfast.cu", "ek_host.cpp", "ek_io.cpp", "ek_stats.cu", "ek_unet.cu", "ek_guess.cu", "ek_les.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

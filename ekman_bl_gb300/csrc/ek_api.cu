@@ -25,6 +25,7 @@ struct ek_unet {
 namespace ek {
 void rk_init_attributes();
 void fft_init_attributes();
+void les_init_attributes();
 const char *last_global_error();
 }  // namespace ek
 
@@ -116,6 +117,7 @@ void run_rem_div(Ctx &c, double temp4, bool update_p, int *mg_status) {
 int substep(Ctx &c, int rk) {
   const Dims &d = c.d;
   const ek_params &p = c.p;
+  if (p.les && !c.les.have_metrics) return fail(c, EK_ERR_STATE, "LES metrics not set (ekgpu_set_les_metrics)");
   const bool th = p.n_th > 0;
   const double TEMP4 = c.H_BAR[rk];
   const double TEMP5 = c.BETA_BAR[rk] * c.H_BAR[rk];
@@ -131,6 +133,10 @@ int substep(Ctx &c, int rk) {
     a.src = c.CU3; a.dst = c.U3; a.dstf = f32 ? c.U3f : nullptr; launch_c2r(c, a);
     if (th) { a.src = c.CTH; a.dst = c.TH; a.dstf = f32 ? c.THf : nullptr; launch_c2r(c, a); }
   }
+  // les_chan / les_chan_th (duct.F90:641-654): NU_T and the stress terms
+  // that the transforms below add to CF1..CF3 and CFTH
+  const bool les = les_active(c);
+  if (les) launch_les(c, rk);
   launch_face_velocity(c);
   // nonlinear and cross-diffusion terms, fused with their forward FFTs
   // (duct.F90:683-1121)
@@ -144,9 +150,11 @@ int substep(Ctx &c, int rk) {
     for (int f = 0; f < 3; ++f) {
       a.pro = PRO_PROD; a.a = c.U1; a.b = uu[f]; a.epi = EPI_SUB_IK; a.dst = cf[f];
       a.af = f32 ? c.U1f : nullptr; a.bf = f32 ? uf[f] : nullptr;
+      a.extra = les ? c.les.t[f] : nullptr;  // + J tau_1f
       launch_r2c(c, a);
       a.pro = PRO_FLUX; a.a = uu[f]; a.b = c.U2b; a.visc = p.nu; a.epi = EPI_ADD;
       a.af = f32 ? uf[f] : nullptr; a.bf = f32 ? c.U2bf : nullptr;
+      a.extra = les ? c.les.ext[f] : nullptr;  // + NU_T cross term - stress divergence
       launch_r2c(c, a);
     }
   }
@@ -166,9 +174,11 @@ int substep(Ctx &c, int rk) {
     a.lowp = 1;
     a.pro = PRO_PROD; a.a = c.TH; a.b = c.U1; a.epi = EPI_SUB_IK; a.dst = c.CFTH;
     a.af = f32 ? c.THf : nullptr; a.bf = f32 ? c.U1f : nullptr;
+    a.extra = les ? c.les.tth : nullptr;  // + J (-KAPPA_T dTH/dx)
     launch_r2c(c, a);
     a.pro = PRO_FLUX; a.a = c.TH; a.b = c.U2b; a.visc = p.nu / p.pr; a.epi = EPI_ADD;
     a.af = f32 ? c.THf : nullptr; a.bf = f32 ? c.U2bf : nullptr;
+    a.extra = les ? c.les.ext[3] : nullptr;  // + KAPPA_T cross term
     launch_r2c(c, a);
     C2rArgs b{};
     b.j0 = d.JST; b.j1 = d.JET; b.k0 = d.ZST; b.k1 = d.ZET;
@@ -287,6 +297,9 @@ int ekgpu_default_params(ek_params *p) {
   p->nz_s_r = 0;
   p->nz_s_l = 0;
   p->save_stats_int = 100;
+  p->les_model_type = 2;
+  p->les_model_type_th = 1;
+  p->create_new_flow = 1;
   return EK_OK;
 }
 
@@ -316,7 +329,10 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
   if (p.variable_dt && (p.update_dt < 1 || !(p.cfl > 0.0) || !(p.delta_t_set > 0.0)))
     return reject("VARIABLE_DT needs UPDATE_DT >= 1, CFL > 0 and DELTA_T_SET > 0");
   if (p.sponge_type != 0 && p.ny_s_t <= p.ny && p.ny_s_t < 0) return reject("NY_S_T must be >= 0");
-  if (p.les != 0) return reject("LES is not supported");
+  if (p.les != 0) {
+    if (p.les_model_type != 2) return reject("LES: only LES_MODEL_TYPE = 2 (dynamic Smagorinsky) is supported");
+    if (p.n_th > 0 && p.les_model_type_th != 1) return reject("LES: only LES_MODEL_TYPE_TH = 1 is supported");
+  }
   if (p.f_type != 1 && p.f_type != 2) return reject("F_TYPE must be 1 or 2");
   if (p.n_th < 0 || p.n_th > 1) return reject("N_TH must be 0 or 1");
   if (p.mg_kcycle < 1 || p.mg_iprer < 1 || p.mg_ipost < 1 || (p.mg_intpol != 1 && p.mg_intpol != 3) || p.mg_maxcy < 1)
@@ -337,6 +353,7 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
     c.stream = c.own_stream;
     rk_init_attributes();
     fft_init_attributes();
+    if (p.les) les_init_attributes();
     Dims &d = c.d;
     d.NX = p.nx; d.NY = p.ny; d.NZ = p.nz;
     d.NKX = p.nx / 3; d.NX2P = p.nx / 2;
@@ -413,6 +430,7 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
     for (double **f : {&c.U1, &c.U2, &c.U3, &c.TH, &c.R1, &c.R2, &c.R3, &c.RTH, &c.PHS, &c.SPH}) *f = dalloc<double>(c, np);
     c.U2b = dalloc<double>(c, 2 * np);
     c.U3b = c.U2b + np;
+    if (p.les) les_alloc(c);
     if (p.fft_fp32) {
       for (float **f : {&c.U1f, &c.U2f, &c.U3f, &c.THf}) *f = dalloc<float>(c, np);
       c.U2bf = dalloc<float>(c, 2 * np);
@@ -509,6 +527,50 @@ int ekgpu_metrics_from_grid(const ek_params *p, const double *xpoint, const doub
     return EK_ERR_ARG;
   return metrics_from_grid_host(p, xpoint, ypoint, int_jacob, gmat_11, gmat_12, gmat_22, cjob_11, cjob_12, cjob_21,
                                 cjob_22, th_bar);
+}
+
+int ekgpu_les_metrics_from_grid(const ek_params *p, const double *xpoint, const double *ypoint, double *gmat_11_y,
+                                double *gmat_12_y, double *gmat_22_y, double *gmat_11_z, double *gmat_12_z,
+                                double *gmat_22_z) {
+  if (!p) return EK_ERR_ARG;
+  return les_metrics_from_grid_host(p, xpoint, ypoint, gmat_11_y, gmat_12_y, gmat_22_y, gmat_11_z, gmat_12_z, gmat_22_z);
+}
+
+int ekgpu_set_les_metrics(ek_ctx *h, const double *gmat_11_y, const double *gmat_12_y, const double *gmat_22_y,
+                          const double *gmat_11_z, const double *gmat_12_z, const double *gmat_22_z) {
+  return guarded(h, [&](Ctx &c) {
+    if (!c.p.les) return fail(c, EK_ERR_STATE, "LES is off (ek_params.les = 0)");
+    if (!gmat_11_y || !gmat_12_y || !gmat_22_y || !gmat_11_z || !gmat_12_z || !gmat_22_z)
+      return fail(c, EK_ERR_ARG, "LES metric pointer is NULL");
+    const size_t n3 = 2 * (size_t)c.d.LDM * (c.d.NY + 3);
+    auto up = [&](double *&dst, const double *src) {
+      if (!dst) dst = dalloc<double>(c, n3);
+      EK_CUDA(cudaMemcpy(dst, src, n3 * sizeof(double), cudaMemcpyHostToDevice));
+    };
+    up(c.m.g11y, gmat_11_y); up(c.m.g12y, gmat_12_y); up(c.m.g22y, gmat_22_y);
+    up(c.m.g11z, gmat_11_z); up(c.m.g12z, gmat_12_z); up(c.m.g22z, gmat_22_z);
+    c.les.have_metrics = true;
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_les_set_first_time(ek_ctx *h, int first_time) {
+  return guarded(h, [&](Ctx &c) {
+    if (!c.p.les) return fail(c, EK_ERR_STATE, "LES is off (ek_params.les = 0)");
+    c.les.first_time = first_time != 0;
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_les_get(ek_ctx *h, double *nu_t, double *c_dyn) {
+  return guarded(h, [&](Ctx &c) {
+    if (!c.p.les) return fail(c, EK_ERR_STATE, "LES is off (ek_params.les = 0)");
+    EK_CUDA(cudaStreamSynchronize(c.stream));
+    if (nu_t) EK_CUDA(cudaMemcpy(nu_t, c.les.nut, sizeof(double) * c.d.nphys(), cudaMemcpyDeviceToHost));
+    if (c_dyn)
+      EK_CUDA(cudaMemcpy(c_dyn, c.les.cdyn, sizeof(double) * (size_t)c.d.NZ2 * c.d.NY2, cudaMemcpyDeviceToHost));
+    return (int)EK_OK;
+  });
 }
 
 int ekgpu_set_metrics(ek_ctx *h, const ek_metrics *m) {
@@ -671,6 +733,7 @@ int ekgpu_step(ek_ctx *h, int nsteps) {
         if (st != EK_OK) return st;
       }
       c.p.time += c.p.delta_t;
+      c.les.first_time = false;  // FIRST_TIME = .FALSE. after the first step (diablo.F90:157)
     }
     return (int)EK_OK;
   });
@@ -737,7 +800,7 @@ long long ekgpu_launch_count(const ek_ctx *h) { return h ? h->c.launches : -1; }
 
 static const char *kKClassNames[KC_N] = {"spectral_rhs", "fft_c2r", "fft_r2c", "face_velocity", "adi_y", "adi_z",
                                          "mg_relax", "mg_coarse", "mg_transfer", "mg_check", "mg_setup",
-                                         "projection", "divergence", "guess"};
+                                         "projection", "divergence", "guess", "les"};
 
 const char *ekgpu_timing_class_name(int k) { return (k >= 0 && k < KC_N) ? kKClassNames[k] : ""; }
 

@@ -13,6 +13,7 @@
 //   prologue PRO_LOAD  x = a
 //            PRO_PROD  x = J a b            (duct.F90:685-691 products)
 //            PRO_FLUX  x = flux stencil of a (duct.F90:735-761 form)
+//            (with LES, + J tau or + the eddy-viscosity terms: ek_les.cu)
 //   epilogue EPI_STORE dst  = X            (modes > NX/3 set to 0)
 //            EPI_ADD   dst += X            (duct.F90:779-785)
 //            EPI_SUB_IK dst -= i kx X      (duct.F90:712-718)
@@ -177,6 +178,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
       zr[n] = s1 + s2;
     }
   }
+  if (args.extra && args.pro != PRO_LOAD) {
+    // LES additions: jac * tau for a product, the precomputed terms for a flux
+    const T es = (args.pro == PRO_PROD) ? (T)fc.m.jac[d.m2(k, j)] : (T)1.0;
+    for (int n = lane; n < NX; n += 32) zr[n] = zr[n] + es * (T)args.extra[base + n];
+  }
   __syncwarp();
   dif_fft(z, M, tw_m<T>(fc), false, lane);
   // split: X[k] = E + W^k O, E = (Z_k + conj Z_{M-k})/2, O = -i (Z_k - conj Z_{M-k})/2
@@ -251,6 +257,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
       const cplx_t w = src2[kk];
       v.re = v.re + args.scale2 * w.re;
       v.im = v.im + args.scale2 * w.im;
+    }
+    if (args.ik) {  // CIKXP * v
+      const double kv = fc.kx[kk], re = v.re;
+      v.re = -(kv * v.im);
+      v.im = kv * re;
     }
     if (kk == 0) v.im = 0.0;
     return Cx<T>::make((T)v.re, (T)v.im);

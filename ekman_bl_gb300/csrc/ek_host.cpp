@@ -10,32 +10,26 @@
 
 namespace ek {
 
-// JACOBI_TRANS (src/diablo.F90:1088-1570).  Same statement order as the
-// Fortran; arrays start zero-filled as a fresh ALLOCATE.
-int metrics_from_grid_host(const ek_params *p, const double *xpoint, const double *ypoint, double *int_jacob,
-                           double *gmat_11, double *gmat_12, double *gmat_22, double *cjob_11, double *cjob_12,
-                           double *cjob_21, double *cjob_22, double *th_bar) {
-  const int NY = p->ny, NZ = p->nz;
-  if (NY < 3 || NZ < 3 || !xpoint || !ypoint) return EK_ERR_ARG;
-  const int LD = NZ + 3;
-  const size_t N2 = (size_t)LD * (NY + 3);
-  const int n1 = NZ + 1, m1 = NY + 1;  // extents of the temporaries (1:NZ+1, 1:NY+1, 2)
-  std::vector<double> xz(2 * n1 * m1, 0.0), yz(xz), xe(xz), ye(xz), zx(xz), zy(xz), ex(xz), ey(xz), ij(xz);
-  auto T = [&](std::vector<double> &v, int k, int j, int f) -> double & {
+namespace {
+
+// The face derivatives of the grid (x_zeta, y_zeta, x_eta, y_eta on faces
+// 1 and 2), their one-sided extrapolations and the AINT truncation to 1e-8
+// (diablo.F90:1164-1229), in arrays (1:NZ+1, 1:NY+1, 2).
+struct GridDeriv {
+  int n1, m1;
+  std::vector<double> xz, yz, xe, ye;
+  GridDeriv(int nz, int ny) : n1(nz + 1), m1(ny + 1), xz(2 * (size_t)(nz + 1) * (ny + 1), 0.0), yz(xz), xe(xz), ye(xz) {}
+  double &operator()(std::vector<double> &v, int k, int j, int f) {
     return v[((size_t)(f - 1) * m1 + (j - 1)) * n1 + (k - 1)];
-  };
+  }
+};
+
+void grid_derivatives(const ek_params *p, const double *xpoint, const double *ypoint, GridDeriv &g) {
+  const int NY = p->ny, NZ = p->nz;
+  auto &xz = g.xz, &yz = g.yz, &xe = g.xe, &ye = g.ye;
+  auto T = [&](std::vector<double> &v, int k, int j, int f) -> double & { return g(v, k, j, f); };
   auto XP = [&](int k, int j) { return xpoint[(size_t)j * (NZ + 2) + k]; };
   auto YP = [&](int k, int j) { return ypoint[(size_t)j * (NZ + 2) + k]; };
-  auto M2 = [&](double *a, int k, int j) -> double & { return a[(size_t)j * LD + k]; };
-  auto M3 = [&](double *a, int k, int j, int f) -> double & { return a[(size_t)(f - 1) * N2 + (size_t)j * LD + k]; };
-  std::memset(int_jacob, 0, sizeof(double) * N2);
-  for (double *a : {gmat_11, gmat_12, gmat_22, cjob_11, cjob_12, cjob_21, cjob_22}) std::memset(a, 0, sizeof(double) * 2 * N2);
-  if (th_bar) {
-    std::memset(th_bar, 0, sizeof(double) * N2);
-    if (p->cont_strat)
-      for (int j = 0; j <= NY + 1; ++j)
-        for (int k = 0; k <= NZ + 1; ++k) M2(th_bar, k, j) = (-YP(k, j) + YP(0, NY + 1));
-  }
   for (int j = 1; j <= NY; ++j)
     for (int k = 1; k <= NZ; ++k) {
       T(xz, k, j, 1) = XP(k + 1, j) - XP(k, j);
@@ -75,6 +69,38 @@ int metrics_from_grid_host(const ek_params *p, const double *xpoint, const doubl
     for (int k = 1; k <= NZ + 1; ++k)
       for (int f = 1; f <= 2; ++f)
         for (auto *v : {&xz, &xe, &yz, &ye}) T(*v, k, j, f) = std::trunc(T(*v, k, j, f) * 100000000.0) * 1.0e-8;
+}
+
+}  // namespace
+
+// JACOBI_TRANS (src/diablo.F90:1088-1570).  Same statement order as the
+// Fortran; arrays start zero-filled as a fresh ALLOCATE.
+int metrics_from_grid_host(const ek_params *p, const double *xpoint, const double *ypoint, double *int_jacob,
+                           double *gmat_11, double *gmat_12, double *gmat_22, double *cjob_11, double *cjob_12,
+                           double *cjob_21, double *cjob_22, double *th_bar) {
+  const int NY = p->ny, NZ = p->nz;
+  if (NY < 3 || NZ < 3 || !xpoint || !ypoint) return EK_ERR_ARG;
+  const int LD = NZ + 3;
+  const size_t N2 = (size_t)LD * (NY + 3);
+  const int n1 = NZ + 1, m1 = NY + 1;  // extents of the temporaries (1:NZ+1, 1:NY+1, 2)
+  std::vector<double> ij(2 * (size_t)n1 * m1, 0.0);
+  auto T = [&](std::vector<double> &v, int k, int j, int f) -> double & {
+    return v[((size_t)(f - 1) * m1 + (j - 1)) * n1 + (k - 1)];
+  };
+  auto YP = [&](int k, int j) { return ypoint[(size_t)j * (NZ + 2) + k]; };
+  auto M2 = [&](double *a, int k, int j) -> double & { return a[(size_t)j * LD + k]; };
+  auto M3 = [&](double *a, int k, int j, int f) -> double & { return a[(size_t)(f - 1) * N2 + (size_t)j * LD + k]; };
+  std::memset(int_jacob, 0, sizeof(double) * N2);
+  for (double *a : {gmat_11, gmat_12, gmat_22, cjob_11, cjob_12, cjob_21, cjob_22}) std::memset(a, 0, sizeof(double) * 2 * N2);
+  if (th_bar) {
+    std::memset(th_bar, 0, sizeof(double) * N2);
+    if (p->cont_strat)
+      for (int j = 0; j <= NY + 1; ++j)
+        for (int k = 0; k <= NZ + 1; ++k) M2(th_bar, k, j) = (-YP(k, j) + YP(0, NY + 1));
+  }
+  GridDeriv gd(NZ, NY);
+  grid_derivatives(p, xpoint, ypoint, gd);
+  auto &xz = gd.xz, &yz = gd.yz, &xe = gd.xe, &ye = gd.ye;
   for (int j = 1; j <= NY + 1; ++j)
     for (int k = 1; k <= NZ + 1; ++k)
       for (int f = 1; f <= 2; ++f) {
@@ -132,6 +158,65 @@ int metrics_from_grid_host(const ek_params *p, const double *xpoint, const doubl
   }
   return EK_OK;
 }
+
+
+// The LES metric variants GMAT_*_y / GMAT_*_z of JACOBI_TRANS
+// (diablo.F90:1379-1467): the zeta_x/eta_x products doubled (_z) or the
+// zeta_y/eta_y products doubled (_y); the K = 0 column and then the J = 0
+// row extrapolated linearly; the (0,0) corner averaged for GMAT_11_* and
+// GMAT_22_* (the reference writes the GMAT_22_* corner twice, first from
+// GMAT_12_*, and keeps GMAT_12_*(0,0) from the row extrapolation); index
+// NZ+2 / NY+2 copies.
+int les_metrics_from_grid_host(const ek_params *p, const double *xpoint, const double *ypoint, double *g11y,
+                               double *g12y, double *g22y, double *g11z, double *g12z, double *g22z) {
+  const int NY = p->ny, NZ = p->nz;
+  if (NY < 3 || NZ < 3 || !xpoint || !ypoint || !g11y || !g12y || !g22y || !g11z || !g12z || !g22z) return EK_ERR_ARG;
+  const int LD = NZ + 3;
+  const size_t N2 = (size_t)LD * (NY + 3);
+  auto M3 = [&](double *a, int k, int j, int f) -> double & { return a[(size_t)(f - 1) * N2 + (size_t)j * LD + k]; };
+  double *all6[6] = {g11z, g12z, g22z, g11y, g12y, g22y};
+  for (double *a : all6) std::memset(a, 0, sizeof(double) * 2 * N2);
+  GridDeriv gd(NZ, NY);
+  grid_derivatives(p, xpoint, ypoint, gd);
+  for (int j = 1; j <= NY + 1; ++j)
+    for (int k = 1; k <= NZ + 1; ++k)
+      for (int f = 1; f <= 2; ++f) {
+        const double xz = gd(gd.xz, k, j, f), yz = gd(gd.yz, k, j, f), xe = gd(gd.xe, k, j, f), ye = gd(gd.ye, k, j, f);
+        const double J = xz * ye - xe * yz;
+        const double zx = ye / J, ex = -yz / J, zy = -xe / J, ey = xz / J;
+        M3(g11z, k, j, f) = (2.0 * zx * zx + zy * zy) * J;
+        M3(g12z, k, j, f) = (2.0 * zx * ex + zy * ey) * J;
+        M3(g22z, k, j, f) = (2.0 * ex * ex + ey * ey) * J;
+        M3(g11y, k, j, f) = (zx * zx + 2.0 * zy * zy) * J;
+        M3(g12y, k, j, f) = (zx * ex + 2.0 * zy * ey) * J;
+        M3(g22y, k, j, f) = (ex * ex + 2.0 * ey * ey) * J;
+      }
+  for (int j = 0; j <= NY + 1; ++j)
+    for (int f = 1; f <= 2; ++f)
+      for (double *a : all6) M3(a, 0, j, f) = 2.0 * M3(a, 1, j, f) - M3(a, 2, j, f);
+  for (int k = 0; k <= NZ + 1; ++k)
+    for (int f = 1; f <= 2; ++f)
+      for (double *a : all6) M3(a, k, 0, f) = 2.0 * M3(a, k, 1, f) - M3(a, k, 2, f);
+  for (int f = 1; f <= 2; ++f) {
+    auto corner = [&](double *s) {
+      return 0.5 * (2.0 * M3(s, 0, 1, f) - M3(s, 0, 2, f) + 2.0 * M3(s, 1, 0, f) - M3(s, 2, 0, f));
+    };
+    M3(g11z, 0, 0, f) = corner(g11z);
+    M3(g22z, 0, 0, f) = corner(g22z);
+    M3(g11y, 0, 0, f) = corner(g11y);
+    M3(g22y, 0, 0, f) = corner(g22y);
+  }
+  for (int f = 1; f <= 2; ++f) {
+    for (int k = 0; k <= NZ + 1; ++k)
+      for (double *a : all6) M3(a, k, NY + 2, f) = M3(a, k, NY + 1, f);
+    for (int j = 0; j <= NY + 1; ++j)
+      for (double *a : all6) M3(a, NZ + 2, j, f) = M3(a, NZ + 1, j, f);
+    for (double *a : all6) M3(a, NZ + 2, NY + 2, f) = M3(a, NZ + 1, NY + 1, f);
+  }
+  return EK_OK;
+}
+
+static void bc_lhs(int field, int dir, const ek_params &p, const Dims &d, int row, double &L, double &D, double &U);
 
 // Boundary rows of APPLY_BC_{TH,1,2,3}_{LOWER,UPPER,LEFT,RIGHT}
 // (src/boundary.F90:124-1763) for the supported codes with IC_TYPE = 7.
@@ -202,6 +287,11 @@ int build_bc_sets(Ctx &c, std::vector<double> &w, const std::vector<double> &jac
       else z.r[z.n++] = BcRow{NZ + 1, 0, 0, c1[EK_ZMAX]};
     } else if (zr == 6) z.r[z.n++] = BcRow{NZ + 1, 1, 1, 0.0};
     else return EK_ERR_ARG;
+    // the boundary rows' matrix entries, for the solvers that build rows on the device
+    for (int dir = 0; dir < 2; ++dir) {
+      BcSet &bs = c.bc[f][dir];
+      for (int t = 0; t < bs.n; ++t) bc_lhs(f, dir, p, d, bs.r[t].row, bs.r[t].l, bs.r[t].dg, bs.r[t].u);
+    }
   }
   return EK_OK;
 }

@@ -85,6 +85,8 @@ struct Metrics {
   // and pg[5..9] of the CJOB_11/CJOB_21 one, for (p0, p(k+1), p(k-1),
   // p(j+1), p(j-1)), each with its 0.5; pg[10] = 1/INT_JACOB
   double *pg = nullptr;
+  // LES variants GMAT_*_y / GMAT_*_z (face layout; null without LES)
+  double *g11y = nullptr, *g12y = nullptr, *g22y = nullptr, *g11z = nullptr, *g12z = nullptr, *g22z = nullptr;
 };
 
 // Boundary rows of one ADI direction (a row of a tridiagonal line replaced
@@ -95,6 +97,7 @@ struct BcRow {
   int kind;
   int src;
   double val;
+  double l, dg, u;  // the row's matrix entries (APPLY_BC_*), for solvers that build rows on the device
 };
 struct BcSet {
   int n;
@@ -160,7 +163,7 @@ struct MgPlan {
 // Kernel classes for the optional per-kernel timer (ekgpu_set_timing).
 enum KClass {
   KC_SPECTRAL = 0, KC_C2R, KC_R2C, KC_FACE, KC_ADI_Y, KC_ADI_Z, KC_MG_RELAX, KC_MG_COARSE,
-  KC_MG_TRANSFER, KC_MG_CHECK, KC_MG_SETUP, KC_PROJECTION, KC_DIVERGENCE, KC_GUESS, KC_N
+  KC_MG_TRANSFER, KC_MG_CHECK, KC_MG_SETUP, KC_PROJECTION, KC_DIVERGENCE, KC_GUESS, KC_LES, KC_N
 };
 struct TimerRec {
   int cls;
@@ -224,6 +227,19 @@ struct GuessState {
   double last_rho = 1.0;  // mean residual ratio |b - A g|/|b| of the last guess
 };
 
+// LES (les_chan LES_MODEL_TYPE 2, les_chan_th LES_MODEL_TYPE_TH 1) state
+// and work fields (ek_les.cu).  Physical layout unless noted.
+struct LesState {
+  bool have_metrics = false;
+  bool first_time = true;       // FIRST_TIME: recompute C_DYN in every substep
+  double *nut = nullptr;        // NU_T, zero outside the velocity interior
+  double *cdyn = nullptr;       // C_DYN(0:NZ+1, 0:NY+1), K fastest
+  double *t[3] = {};            // d(U1,U2,U3)/dx, then tau_11, tau_12, tau_13 in place
+  double *t23 = nullptr;        // tau_23
+  double *tth = nullptr;        // d(TH)/dx, then the scalar flux -KAPPA_T d(TH)/dx in place
+  double *ext[4] = {};          // flux-transform additions of U1, U2, U3, TH
+};
+
 struct Ctx {
   ek_params p{};
   Dims d{};
@@ -283,6 +299,8 @@ struct Ctx {
   double *stats_buf = nullptr;
   // per-cell right-hand-side weights of the two ADI sweeps (k_adi_tab)
   double *adi_tab = nullptr;
+  LesState les;
+  double *adi_scr = nullptr;  // LES ADI: the modified upper diagonals (one field)
   // divergence check
   double *div_part = nullptr;
   double last_div = 0.0;
@@ -338,6 +356,8 @@ void adi_factor_host(const Ctx &c, int field, int rk, int dir, const std::vector
                      std::vector<double> &ib, std::vector<double> &u);
 bool mg_pick_shape(int n, int &p, int &e);
 void launch_courant(Ctx &c);
+int les_metrics_from_grid_host(const ek_params *p, const double *xpoint, const double *ypoint, double *g11y,
+                               double *g12y, double *g22y, double *g11z, double *g12z, double *g22z);
 int sponge_profiles_host(const ek_params *p, const double *xpoint, const double *ypoint, double *sig,
                          double *sig_out);
 void mg_build_plan_host(Ctx &c, const std::vector<double> &jac, const std::vector<double> &g11,
@@ -350,6 +370,7 @@ enum { PRO_LOAD = 0, PRO_PROD = 1, PRO_FLUX = 2 };
 enum { EPI_STORE = 0, EPI_ADD = 1, EPI_SUB_IK = 2 };
 struct R2cArgs {
   const double *a, *b;    // PRO_LOAD: a; PRO_PROD: jac*a*b; PRO_FLUX: field a
+  const double *extra;    // when set: PRO_PROD adds jac*extra, PRO_FLUX adds extra
   double visc;            // PRO_FLUX viscosity
   cplx_t *dst;
   int epi;
@@ -362,6 +383,7 @@ void launch_r2c(Ctx &c, const R2cArgs &a);
 struct C2rArgs {
   const cplx_t *src, *src2;  // x = src (+ scale2*src2)
   double scale2;
+  int ik;                    // 1: x = i kx src (the x derivative)
   double *dst;
   int j0, j1, k0, k1;
   int lowp;                  // as R2cArgs::lowp
@@ -374,6 +396,11 @@ void launch_spectral_rhs(Ctx &c, int rk);
 void launch_metric_tables(Ctx &c);
 void launch_face_velocity(Ctx &c);
 void launch_adi(Ctx &c, int field, int rk);
+
+// LES (ek_les.cu)
+bool les_active(const Ctx &c);
+void les_alloc(Ctx &c);
+void launch_les(Ctx &c, int rk);
 void launch_th_corners(Ctx &c);
 void launch_divergence_rhs(Ctx &c, double *rhs_finest, int nprob);
 void launch_projection(Ctx &c, const double *phif, int nprob, double temp4, bool update_p);

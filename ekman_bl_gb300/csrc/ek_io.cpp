@@ -341,6 +341,9 @@ int read_flow(Ctx &c, const char *flow_path, const char *th_path) {
     // TIME and TIME_STEP: the last header read wins, as in READ_FLOW
     c.p.time = all.back()->h.time;
     c.p.time_step = all.back()->h.time_step;
+    // a run started from a restart file begins with FIRST_TIME (diablo.F90:88):
+    // with LES, C_DYN is recomputed in each substep of its first step
+    c.les.first_time = true;
   } catch (const IoError &e) {
     c.err = e.msg;
     return EK_ERR_IO;

@@ -37,6 +37,8 @@ struct SpecArgs {
   cplx_t *CU1, *CU2, *CU3, *CP, *CTH, *CF1, *CF2, *CF3, *CFTH, *CR1, *CR2, *CR3, *CRTH;
   double nu, nupr, T3, T4, px, f0, ubc_top, wbulk0, ri;
   int rk, th, cont_strat, forcing;
+  const double *nut;  // LES: NU_T of the previous substep (KAPPA_T = NU_T/PR), else null
+  double pr;
   // sponge_th
   const double *sig, *sig_out, *sred;  // sred[1] != 0: dynamic branch active
   double amp, tgt1, tgt2, tgt3;
@@ -164,8 +166,11 @@ __global__ void k_spectral_rhs(SpecArgs a) {
                        0.5 * a.m.c22[d.m3(k, j + 1, 1)] * (tb(k, j) + tb(k, j + 1)) -
                        0.5 * a.m.c22[d.m3(k, j, 1)] * (tb(k, j) + tb(k, j - 1));
       ft = csub(ft, cscl(g, a.CU2[q]));
+      // with LES the coefficient is NU/PR + KAPPA_T at the physical point whose
+      // x index is the mode index (duct.F90:610-618)
+      const double kap = a.nut ? a.nupr + a.nut[d.ip(i, k, j)] / a.pr : a.nupr;
       const double dd =
-          0.25 * a.nupr *
+          0.25 * kap *
           (+a.m.g12[d.m3(k + 1, j, 2)] * (tb(k + 1, j + 1) + tb(k, j + 1) - tb(k, j - 1) - tb(k + 1, j - 1)) -
            a.m.g12[d.m3(k, j, 2)] * (tb(k - 1, j + 1) + tb(k, j + 1) - tb(k, j - 1) - tb(k - 1, j - 1)) +
            a.m.g12[d.m3(k, j + 1, 1)] * (tb(k + 1, j + 1) + tb(k + 1, j) - tb(k - 1, j + 1) - tb(k - 1, j)) -
@@ -263,6 +268,12 @@ struct AdiArgs {
   double coef;
   int js, je, zs, ze;
   const double *tab;  // per-cell right-hand-side weights of this sweep (k_adi_tab)
+  // LES (k_adi_les): viscosity nu = nut * nscale, the LES metric of the
+  // right-hand-side term (lg_r) and of the matrix (lg_m), TEMP2 = H/2, and
+  // two scratch fields for the eliminated diagonal and the upper diagonal
+  const double *nut, *lg_r, *lg_m;
+  double nscale, temp2;
+  double *scr_b, *scr_u;
 };
 
 // Right-hand-side weights of one ADI sweep per cell (tab[t * n2 + m2(k, j)]),
@@ -374,6 +385,113 @@ __global__ void __launch_bounds__(32 * kAdiWarps) k_adi(AdiArgs a) {
   for (int r = nrow - 2; r >= 0; --r) {
     x = (g[r * 32 + lane] - sfu[r] * x) * sfib[r];
     a.out[at(r)] = x;
+  }
+}
+
+// CN-ADI line solves with the LES eddy viscosity (duct.F90:1373-1386,
+// 1437-1450, 1489-1500, 1559-1569 for TH; 1667-1680, 1720-1731, 1771-1784,
+// 1821-1832 for U1; 1916-1929, 1963-1973, 2013-2026, 2081-2091 for U2 with
+// GMAT_*_y; 2177-2190, 2224-2234, 2300-2313, 2358-2368 for U3 with GMAT_*_z):
+// the matrix rows depend on x through NU_T, so each thread owns one system
+// (one x point of one line), builds every row -- the right-hand side of
+// k_adi plus the NU_T terms, the tridiagonal row, or the boundary row -- and
+// runs THOMAS_REAL (boundary.F90:53-84) on it.  The forward sweep parks the
+// eliminated diagonal and the upper diagonal in two scratch fields and the
+// modified right-hand side in the output; the back substitution reads them
+// back.  Consecutive threads take consecutive x points, so every access is
+// coalesced.
+template <bool ZS>
+__global__ void __launch_bounds__(128) k_adi_les(AdiArgs a) {
+  const Dims &d = a.d;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int line = ZS ? (int)blockIdx.y : a.zs + (int)blockIdx.y;
+  if (i >= d.NX) return;
+  if (ZS && (line < a.js || line > a.je)) {
+    for (int k = a.zs; k <= a.ze; ++k) a.out[d.ip(i, k, line)] = a.phs[d.ip(i, k, line)];
+    return;
+  }
+  const int nrow = ZS ? d.NZ2 : d.NY2;
+  const int r0 = ZS ? a.zs : a.js, r1 = ZS ? a.ze : a.je;
+  const size_t n2 = (size_t)d.LDM * (d.NY + 3);
+  const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
+  const size_t sA = ZS ? sK : sJ;  // along the line
+  const size_t sX = ZS ? sJ : sK;  // across: the direction of the explicit term
+  const double h2 = 0.5 * a.temp2;
+  const double *nut = a.nut, *R = a.R, *po = a.phi_old, *ps = a.phs;
+  const double *gb = ZS ? a.m.g11 : a.m.g22;  // base matrix metric
+  const int fm = ZS ? 2 : 1;                  // its face
+  auto at = [&](int r) { return ZS ? d.ip(i, r, line) : d.ip(i, line, r); };
+  auto mrow = [&](int r, int &k, int &j) {
+    k = ZS ? r : line;
+    j = ZS ? line : r;
+  };
+  double Bp = 1.0, gp = 0.0, Up = 0.0;
+  for (int r = 0; r < nrow; ++r) {
+    double L = 0.0, D = 1.0, U = 0.0, V = 0.0;
+    const size_t c = at(r);
+    if (r >= r0 && r <= r1) {
+      int k, j;
+      mrow(r, k, j);
+      const size_t mm = d.m2(k, j);
+      const double nu0 = nut[c] * a.nscale;
+      const double nxp = nut[c + sX] * a.nscale, nxm = nut[c - sX] * a.nscale;
+      const double nap = nut[c + sA] * a.nscale, nam = nut[c - sA] * a.nscale;
+      // right-hand side: k_adi's rows plus the NU_T term across the line
+      double gxp, gxm;  // LES metric on the two faces across
+      if (!ZS) {
+        V = fma(0.5, R[c], fma(a.tab[mm], po[c], fma(a.tab[n2 + mm], po[c + sK], a.tab[2 * n2 + mm] * po[c - sK])));
+        gxp = a.lg_r[d.m3(k + 1, j, 2)];
+        gxm = a.lg_r[d.m3(k, j, 2)];
+        V += a.temp2 * ((0.5 * (nxp + nu0)) * (gxp * (po[c + sK] - po[c])) - (0.5 * (nu0 + nxm)) * (gxm * (po[c] - po[c - sK])));
+      } else {
+        V = fma(0.5, R[c],
+                fma(a.tab[3 * n2 + mm], po[c], fma(a.tab[mm], ps[c], fma(a.tab[n2 + mm], ps[c + sJ], a.tab[2 * n2 + mm] * ps[c - sJ]))));
+        gxp = a.lg_r[d.m3(k, j + 1, 1)];
+        gxm = a.lg_r[d.m3(k, j, 1)];
+        V += a.temp2 * ((0.5 * (nxp + nu0)) * (gxp * (ps[c + sJ] - ps[c])) - (0.5 * (nxm + nu0)) * (gxm * (ps[c] - ps[c - sJ])));
+      }
+      // tridiagonal row: base coefficients plus the NU_T face terms
+      const size_t fl = d.m3(k, j, fm);
+      const size_t fu = ZS ? d.m3(k + 1, j, fm) : d.m3(k, j + 1, fm);
+      const double glo = gb[fl], gup = gb[fu];
+      const double llo = a.lg_m[fl], lup = a.lg_m[fu];
+      const double tl = (h2 * (nu0 + nam)) * llo, tu = (h2 * (nu0 + nap)) * lup;
+      L = -a.coef * glo - tl;
+      D = a.m.jac[mm] + a.coef * (gup + glo) + tu + tl;
+      U = -a.coef * gup - tu;
+    }
+    for (int b = 0; b < a.bc.n; ++b) {
+      const BcRow &br = a.bc.r[b];
+      if (br.row != r) continue;
+      L = br.l;
+      D = br.dg;
+      U = br.u;
+      if (br.kind == 0) V = br.val;
+      else if (br.kind == 1) V = ZS ? ps[d.ip(i, br.src, line)] : po[d.ip(i, line, br.src)];
+      else V = br.val * a.bcw[br.src + line];
+    }
+    double B, g;
+    if (r == 0) {
+      B = D;
+      g = V;
+    } else {
+      const double am = -L / Bp;
+      B = D + am * Up;
+      g = V + am * gp;
+    }
+    a.out[c] = g;
+    a.scr_b[c] = B;
+    a.scr_u[c] = U;
+    Bp = B;
+    gp = g;
+    Up = U;
+  }
+  double x = gp / Bp;
+  a.out[at(nrow - 1)] = x;
+  for (int r = nrow - 2; r >= 0; --r) {
+    const size_t c = at(r);
+    x = (a.out[c] - a.scr_u[c] * x) / a.scr_b[c];
+    a.out[c] = x;
   }
 }
 
@@ -570,6 +688,8 @@ void launch_spectral_rhs(Ctx &c, int rk) {
   a.rk = rk;
   a.th = p.n_th > 0;
   a.cont_strat = p.cont_strat;
+  a.nut = p.les ? c.les.nut : nullptr;
+  a.pr = p.pr;
   // sponge_th runs inside the scalar loop (duct.F90:635), so only with N_TH >= 1
   a.sponge = (p.sponge_type != 0 && p.n_th > 0) ? 1 : 0;
   a.sig = c.sponge_sig;
@@ -676,6 +796,43 @@ void launch_adi(Ctx &c, int field, int rk) {
     after_launch(c);
     k_adi_tab<true><<<tg, 64, 0, c.stream>>>(d, c.m, coef, c.adi_tab + 4 * n2);
     after_launch(c);
+  }
+  if (les_active(c)) {
+    // LES: x-dependent rows, one thread per system
+    const size_t np = d.nphys();
+    if (!c.adi_scr) {
+      EK_CUDA(cudaMalloc(&c.adi_scr, sizeof(double) * 2 * np));
+      c.allocs.push_back(c.adi_scr);
+    }
+    a.scr_b = c.adi_scr;
+    a.scr_u = c.adi_scr + np;
+    a.nut = c.les.nut;
+    a.nscale = (field == 0) ? 1.0 / c.p.pr : 1.0;
+    a.temp2 = c.H_BAR[rk] / 2.0;
+    const double *l11 = (field == 2) ? c.m.g11y : (field == 3) ? c.m.g11z : c.m.g11;
+    const double *l22 = (field == 2) ? c.m.g22y : (field == 3) ? c.m.g22z : c.m.g22;
+    a.out = c.PHS;
+    a.bc = c.bc[field][0];
+    a.lg_r = l11;
+    a.lg_m = l22;
+    {
+      dim3 grid((d.NX + 127) / 128, a.ze - a.zs + 1);
+      KScope ks(c, KC_ADI_Y, 96.0 * d.NX * d.NY2 * (a.ze - a.zs + 1));
+      k_adi_les<false><<<grid, 128, 0, c.stream>>>(a);
+      after_launch(c);
+    }
+    a.tab = c.adi_tab + 4 * n2;
+    a.out = phi;
+    a.bc = c.bc[field][1];
+    a.lg_r = l22;
+    a.lg_m = l11;
+    {
+      dim3 grid((d.NX + 127) / 128, d.NY2);
+      KScope ks(c, KC_ADI_Z, 96.0 * d.NX * d.NZ2 * (a.je - a.js + 1));
+      k_adi_les<true><<<grid, 128, 0, c.stream>>>(a);
+      after_launch(c);
+    }
+    return;
   }
   // y sweep
   a.out = c.PHS;

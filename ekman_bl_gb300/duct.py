@@ -35,7 +35,10 @@ EXPORTS = [
     "ekgpu_unet_set_params", "ekgpu_unet_get_params", "ekgpu_unet_forward", "ekgpu_unet_train_step",
     "ekgpu_unet_gradient", "ekgpu_guess_geometry", "ekgpu_set_poisson_guess", "ekgpu_set_pair_sink",
     "ekgpu_pair_count", "ekgpu_last_guess_stats", "ekgpu_mg_autotune", "ekgpu_mg_set_layout", "ekgpu_mg_levels",
+    "ekgpu_les_metrics_from_grid", "ekgpu_set_les_metrics", "ekgpu_les_set_first_time", "ekgpu_les_get",
 ]
+
+LES_METRICS = ("gmat_11_y", "gmat_12_y", "gmat_22_y", "gmat_11_z", "gmat_12_z", "gmat_22_z")
 
 
 class EkError(RuntimeError):
@@ -97,6 +100,10 @@ def load_library():
     L.ekgpu_mg_autotune.argtypes = [V, C.c_int, C.c_char_p, C.c_int]
     L.ekgpu_mg_set_layout.argtypes = [V, C.c_int, C.c_int, C.c_int, C.c_int]
     L.ekgpu_mg_levels.argtypes = [V, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]
+    L.ekgpu_les_metrics_from_grid.argtypes = [P, _D, _D] + [_D] * 6
+    L.ekgpu_set_les_metrics.argtypes = [V] + [_D] * 6
+    L.ekgpu_les_set_first_time.argtypes = [V, C.c_int]
+    L.ekgpu_les_get.argtypes = [V, _D, _D]
     L.ekgpu_get_field.argtypes = [V, C.c_int, _D]
     L.ekgpu_put_field.argtypes = [V, C.c_int, _D]
     L.ekgpu_rk_substep.argtypes = [V, C.c_int]
@@ -150,6 +157,19 @@ def metrics_from_grid(p: EkParams, xpoint: np.ndarray, ypoint: np.ndarray) -> di
         "int_jacob", "gmat_11", "gmat_12", "gmat_22", "cjob_11", "cjob_12", "cjob_21", "cjob_22", "th_bar")])
     if st:
         raise EkError(st, "ekgpu_metrics_from_grid")
+    return out
+
+
+def les_metrics_from_grid(p: EkParams, xpoint: np.ndarray, ypoint: np.ndarray) -> dict:
+    """GMAT_*_y / GMAT_*_z of JACOBI_TRANS's LES branch (src/diablo.F90:1379-1467)
+    through ekgpu_les_metrics_from_grid; face layout [f, J, K] like GMAT_11."""
+    L = load_library()
+    out = {k: np.zeros((2, p.ny + 3, p.nz + 3)) for k in LES_METRICS}
+    xp = np.ascontiguousarray(xpoint, np.float64)
+    yp = np.ascontiguousarray(ypoint, np.float64)
+    st = L.ekgpu_les_metrics_from_grid(C.byref(p), as_ptr(xp), as_ptr(yp), *[as_ptr(out[k]) for k in LES_METRICS])
+    if st:
+        raise EkError(st, "ekgpu_les_metrics_from_grid")
     return out
 
 
@@ -216,6 +236,24 @@ class DuctSolver:
 
     def set_time(self, time: float, time_step: int):
         self._check(self._L.ekgpu_set_time(self._h, float(time), int(time_step)))
+
+    # -- LES (les_chan / les_chan_th) ----------------------------------------
+    def set_les_metrics(self, m: dict):
+        """Upload GMAT_*_y / GMAT_*_z (les_metrics_from_grid)."""
+        self._les_metrics = [np.ascontiguousarray(m[k], np.float64) for k in LES_METRICS]
+        self._check(self._L.ekgpu_set_les_metrics(self._h, *[as_ptr(a) for a in self._les_metrics]))
+
+    def les_set_first_time(self, flag: bool):
+        """FIRST_TIME: recompute C_DYN in every substep until cleared."""
+        self._check(self._L.ekgpu_les_set_first_time(self._h, int(bool(flag))))
+
+    def les_state(self):
+        """(NU_T in the physical layout [J, K, I], C_DYN [J, K])."""
+        p = self.p
+        nu = np.zeros((p.ny + 2, p.nz + 2, p.nx + 2))
+        cd = np.zeros((p.ny + 2, p.nz + 2))
+        self._check(self._L.ekgpu_les_get(self._h, as_ptr(nu), as_ptr(cd)))
+        return nu, cd
 
     def get_time(self):
         """(TIME, TIME_STEP, DELTA_T)."""

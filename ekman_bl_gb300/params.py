@@ -47,7 +47,8 @@ class EkParams(C.Structure):
         ("ny_s_t", C.c_int), ("nz_s_r", C.c_int), ("nz_s_l", C.c_int), ("save_stats_int", C.c_int),
         ("time_step", C.c_int), ("variable_dt", C.c_int), ("update_dt", C.c_int),
         ("cfl", C.c_double), ("delta_t_set", C.c_double), ("fft_fp32", C.c_int),
-        ("ff_arith", C.c_int),
+        ("ff_arith", C.c_int), ("les_model_type", C.c_int), ("les_model_type_th", C.c_int),
+        ("create_new_flow", C.c_int),
     ]
 
 
@@ -133,6 +134,8 @@ def default_params(nx: int, ny: int, nz: int) -> EkParams:
     p.update_dt = 1
     p.cfl = 0.8
     p.delta_t_set = p.delta_t
+    # LES off; the shipped model choice (input.dat:11) when it is switched on
+    p.les, p.les_model_type, p.les_model_type_th, p.create_new_flow = 0, 2, 1, 1
     return p
 
 

@@ -93,7 +93,10 @@ typedef struct ek_params {
                                 mg_stop = EK_MG_STOP_RESIDUAL; mg_maxcy caps the corrections   */
   int sponge_type;           /* SPONGE_TYPE: 0 none, 1 parabolic, 2 exponential profiles;
                                 sponge_th (duct.F90:3196-3362) runs when != 0 and N_TH >= 1 */
-  int les;                   /* LES (only 0 supported)                                  */
+  int les;                   /* LES: dynamic-Smagorinsky subgrid terms of les_chan /
+                                les_chan_th (les_chan.F90, les_chan_th.F90) in every substep
+                                with TIME_STEP > 1 or create_new_flow = 0; needs
+                                ekgpu_set_les_metrics                                   */
   int ny_s_t, nz_s_r, nz_s_l;/* grid_def NY_S_T, NZ_S_R, NZ_S_L: sponge extents         */
   int save_stats_int;        /* SAVE_STATS_INT (input.dat); sponge_th zeroes mode 0 of CU2X
                                 when MOD(2*TIME_STEP, SAVE_STATS_INT) = 0 in its stratified,
@@ -109,6 +112,11 @@ typedef struct ek_params {
                                 1 the nonlinear product/flux transforms, 2 every transform */
   int ff_arith;              /* 1: the x-transforms fft_fp32 leaves in FP64 use float-float
                                 arithmetic (~48 bits) on the FP32 pipe; fields stay FP64  */
+  int les_model_type;        /* LES_MODEL_TYPE: only 2 (dynamic Smagorinsky, C_DYN from the
+                                test filter every 5 steps) is supported                   */
+  int les_model_type_th;     /* LES_MODEL_TYPE_TH: only 1 (KAPPA_T = NU_T/PR) is supported */
+  int create_new_flow;       /* CREATE_NEW_FLOW (input.dat): 1 leaves the subgrid terms out of
+                                the run's first step (TIME_STEP = 1)                     */
 } ek_params;
 
 /* Geometry and background fields of JACOBI_TRANS (diablo.F90:1088-1570);
@@ -203,6 +211,32 @@ int ekgpu_metrics_from_grid(const ek_params *p, const double *xpoint,
  * NZ_S_R < NZ+1), parabolic (SPONGE_TYPE 1) or exponential (2); zero for 0. */
 int ekgpu_sponge_profiles(const ek_params *p, const double *xpoint, const double *ypoint,
                           double *sponge_sigma, double *sponge_sigma_out);
+
+/* LES (ek_params.les = 1; les_chan.F90 with LES_MODEL_TYPE 2 and
+ * les_chan_th.F90 with LES_MODEL_TYPE_TH 1, called from RK_DUCT at
+ * duct.F90:641-654).
+ * ekgpu_les_metrics_from_grid: host helper, the GMAT_*_y / GMAT_*_z arrays
+ *   of JACOBI_TRANS's LES branch (diablo.F90:1379-1467) from the grid
+ *   points, each (0:NZ+2,0:NY+2,2) like GMAT_11.
+ * ekgpu_set_les_metrics: upload them (replaces allocation_les_var's arrays
+ *   filled by JACOBI_TRANS); needed before the first substep with LES.
+ * ekgpu_les_set_first_time: set FIRST_TIME (diablo.F90:88,157), which makes
+ *   every substep recompute C_DYN.  It is 1 after ekgpu_create and after
+ *   ekgpu_read_flow, and ekgpu_step clears it after each step; a driver that
+ *   calls ekgpu_rk_substep itself clears it after its first step.
+ * ekgpu_les_get: copy NU_T (physical layout) and C_DYN ((0:NZ+1,0:NY+1),
+ *   (NZ+2)*(NY+2) doubles) out; either pointer may be NULL.
+ * The subgrid terms act in every substep with TIME_STEP > 1, or in every
+ * substep when create_new_flow = 0 (the IF of duct.F90:641).  NU_T and C_DYN
+ * start at zero (diablo.F90:541-557). */
+int ekgpu_les_metrics_from_grid(const ek_params *p, const double *xpoint, const double *ypoint,
+                                double *gmat_11_y, double *gmat_12_y, double *gmat_22_y,
+                                double *gmat_11_z, double *gmat_12_z, double *gmat_22_z);
+int ekgpu_set_les_metrics(ek_ctx *ctx, const double *gmat_11_y, const double *gmat_12_y,
+                          const double *gmat_22_y, const double *gmat_11_z, const double *gmat_12_z,
+                          const double *gmat_22_z);
+int ekgpu_les_set_first_time(ek_ctx *ctx, int first_time);
+int ekgpu_les_get(ek_ctx *ctx, double *nu_t, double *c_dyn);
 
 /* Upload SPONGE_SIGMA(0:NY+1) and SPONGE_SIGMA_OUT(0:NZ+1) (the module arrays
  * that sponge_th reads).  Both default to zero. */

@@ -62,6 +62,19 @@ int ekref_last_mg_stats(ekref_ctx *ctx, ek_mg_stats *stats);
 /* SAVE_STATS_CURVI (flow_statistics.F90:2-1023): statistics and state round trip. */
 int ekref_save_stats(ekref_ctx *ctx, ek_stats *stats);
 
+/* LES (les_chan.F90 LES_MODEL_TYPE 2, les_chan_th.F90 LES_MODEL_TYPE_TH 1):
+ * the GMAT_*_y / GMAT_*_z metrics of JACOBI_TRANS (diablo.F90:1379-1467), in
+ * the face-metric layout; the context's copy of them; FIRST_TIME; and the
+ * NU_T (physical layout) and C_DYN ((0:NZ+1,0:NY+1)) arrays. */
+int ekref_les_metrics_from_grid(const ek_params *p, const double *xpoint, const double *ypoint,
+                                double *gmat_11_y, double *gmat_12_y, double *gmat_22_y,
+                                double *gmat_11_z, double *gmat_12_z, double *gmat_22_z);
+int ekref_set_les_metrics(ekref_ctx *ctx, const double *gmat_11_y, const double *gmat_12_y,
+                          const double *gmat_22_y, const double *gmat_11_z, const double *gmat_12_z,
+                          const double *gmat_22_z);
+int ekref_les_set_first_time(ekref_ctx *ctx, int first_time);
+int ekref_les_get(ekref_ctx *ctx, double *nu_t, double *c_dyn);
+
 /* Building blocks exposed for unit tests. */
 /* r2c along x of nlines lines of stride nx+2 doubles -> (nx/2+1) complex per
  * line, modes above nkx zeroed; c2r the inverse (x >= nx set to 0). */

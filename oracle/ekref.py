@@ -60,6 +60,10 @@ def lib():
         L.ekref_thomas_real.argtypes = [C.c_int, C.c_int, _D, _D, _D, _D]
         L.ekref_mg_apply.argtypes = [C.c_void_p, C.c_double, _D, _D]
         L.ekref_save_stats.argtypes = [C.c_void_p, C.POINTER(EkStats)]
+        L.ekref_les_metrics_from_grid.argtypes = [P, _D, _D] + [_D] * 6
+        L.ekref_set_les_metrics.argtypes = [C.c_void_p] + [_D] * 6
+        L.ekref_les_set_first_time.argtypes = [C.c_void_p, C.c_int]
+        L.ekref_les_get.argtypes = [C.c_void_p, _D, _D]
         _lib = L
     return _lib
 
@@ -79,6 +83,21 @@ def metrics_from_grid(p: EkParams, xpoint: np.ndarray, ypoint: np.ndarray) -> di
                                        as_ptr(out["cjob_22"]), as_ptr(out["th_bar"]))
     if st:
         raise RuntimeError(f"ekref_metrics_from_grid failed: {st}")
+    return out
+
+
+LES_METRICS = ("gmat_11_y", "gmat_12_y", "gmat_22_y", "gmat_11_z", "gmat_12_z", "gmat_22_z")
+
+
+def les_metrics_from_grid(p: EkParams, xpoint: np.ndarray, ypoint: np.ndarray) -> dict:
+    """GMAT_*_y / GMAT_*_z of JACOBI_TRANS (diablo.F90:1379-1467), face layout [f, J, K]."""
+    n3 = (2, p.ny + 3, p.nz + 3)
+    out = {k: np.zeros(n3) for k in LES_METRICS}
+    xp = np.ascontiguousarray(xpoint, np.float64)
+    yp = np.ascontiguousarray(ypoint, np.float64)
+    st = lib().ekref_les_metrics_from_grid(C.byref(p), as_ptr(xp), as_ptr(yp), *[as_ptr(out[k]) for k in LES_METRICS])
+    if st:
+        raise RuntimeError(f"ekref_les_metrics_from_grid failed: {st}")
     return out
 
 
@@ -194,6 +213,21 @@ class Oracle:
         s = EkMgStats()
         lib().ekref_last_mg_stats(self._h, C.byref(s))
         return s.as_dict()
+
+    def set_les_metrics(self, m: dict):
+        self._les = [np.ascontiguousarray(m[k], np.float64) for k in LES_METRICS]
+        self._check(lib().ekref_set_les_metrics(self._h, *[as_ptr(a) for a in self._les]))
+
+    def les_set_first_time(self, flag: bool):
+        self._check(lib().ekref_les_set_first_time(self._h, int(bool(flag))))
+
+    def les_state(self):
+        """(NU_T in the physical layout [J, K, I], C_DYN [J, K])."""
+        p = self.p
+        nu = np.zeros((p.ny + 2, p.nz + 2, p.nx + 2))
+        cd = np.zeros((p.ny + 2, p.nz + 2))
+        self._check(lib().ekref_les_get(self._h, as_ptr(nu), as_ptr(cd)))
+        return nu, cd
 
     def save_stats(self) -> dict:
         """SAVE_STATS_CURVI restated: the statistics and the state round trip."""

@@ -16,105 +16,9 @@
 #include <omp.h>
 #endif
 
-#include "ekref.h"
-#include "ekref_mud.h"
+#include "ekref_ctx.h"
 
-namespace {
-
-struct cplx {
-  double re, im;
-};
-inline cplx cadd(cplx a, cplx b) { return {a.re + b.re, a.im + b.im}; }
-inline cplx csub(cplx a, cplx b) { return {a.re - b.re, a.im - b.im}; }
-inline cplx cscale(double s, cplx a) { return {s * a.re, s * a.im}; }
-inline cplx cmul(cplx a, cplx b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
-
-// Radix-2 complex FFT, sign = -1 forward, +1 inverse (unnormalised).
-struct FFT {
-  int n = 0;
-  std::vector<std::complex<double>> tw;
-  std::vector<int> rev;
-  explicit FFT(int n_) : n(n_), tw(n_ / 2), rev(n_) {
-    for (int k = 0; k < n / 2; ++k) tw[k] = std::polar(1.0, -2.0 * M_PI * k / n);
-    int lg = 0;
-    while ((1 << lg) < n) ++lg;
-    for (int i = 0; i < n; ++i) {
-      int r = 0;
-      for (int b = 0; b < lg; ++b) r |= ((i >> b) & 1) << (lg - 1 - b);
-      rev[i] = r;
-    }
-  }
-  void run(std::complex<double> *a, int sign) const {
-    for (int i = 0; i < n; ++i)
-      if (i < rev[i]) std::swap(a[i], a[rev[i]]);
-    for (int len = 2; len <= n; len <<= 1) {
-      const int step = n / len;
-      for (int s = 0; s < n; s += len)
-        for (int k = 0; k < len / 2; ++k) {
-          std::complex<double> w = tw[k * step];
-          if (sign > 0) w = std::conj(w);
-          const std::complex<double> u = a[s + k], v = a[s + k + len / 2] * w;
-          a[s + k] = u + v;
-          a[s + k + len / 2] = u - v;
-        }
-    }
-  }
-};
-
-void r2c_line(const FFT &f, int nkx, const double *in, cplx *out, std::complex<double> *buf) {
-  const int n = f.n;
-  for (int i = 0; i < n; ++i) buf[i] = std::complex<double>(in[i], 0.0);
-  f.run(buf, -1);
-  const double s = 1.0 / n;
-  for (int k = 0; k <= n / 2; ++k)
-    out[k] = (k <= nkx) ? cplx{buf[k].real() * s, buf[k].imag() * s} : cplx{0.0, 0.0};
-}
-
-void c2r_line(const FFT &f, int nkx, const cplx *in, double *out, std::complex<double> *buf) {
-  const int n = f.n;
-  for (int i = 0; i < n; ++i) buf[i] = 0.0;
-  buf[0] = std::complex<double>(in[0].re, 0.0);
-  for (int k = 1; k <= nkx && k < n / 2; ++k) {
-    buf[k] = std::complex<double>(in[k].re, in[k].im);
-    buf[n - k] = std::complex<double>(in[k].re, -in[k].im);
-  }
-  f.run(buf, +1);
-  for (int i = 0; i < n; ++i) out[i] = buf[i].real();
-  out[n] = 0.0;
-  out[n + 1] = 0.0;
-}
-
-}  // namespace
-
-struct ekref_ctx {
-  ek_params p{};
-  std::string err;
-  int NX, NY, NZ, NKX, NX2P, NXP;
-  int LDX, LDC;      // physical and spectral line lengths (NX+2, NX/2+1)
-  int NZ2, NY2;      // NZ+2, NY+2 lines
-  int JSTART, JEND, ZSTART, ZEND, JSTART_TH, JEND_TH, ZSTART_TH, ZEND_TH;
-  double H_BAR[4], BETA_BAR[4], ZETA_BAR[4];
-  std::vector<double> KXP, KX2P;
-  std::vector<double> int_jacob, gmat_11, gmat_12, gmat_22, cjob_11, cjob_12, cjob_21, cjob_22, th_bar;
-  std::vector<double> sponge_sigma, sponge_sigma_out;  // (0:NY+1), (0:NZ+1); zero by default
-  bool have_metrics = false;
-  // spectral fields
-  std::vector<cplx> CU1, CU2, CU3, CP, CTH, CF1, CF2, CF3, CFTH, CR1, CR2, CR3, CRTH, CS1, CS2, CU2b, CU3b;
-  // physical fields
-  std::vector<double> U1, U2, U3, TH, R1, R2, R3, RTH, S1, S2, U2b, U3b;
-  std::unique_ptr<FFT> fft;
-  ekref::MudOpts mud{};
-  double last_div = 0.0;
-  ek_mg_stats last_stats{};
-
-  size_t ip(int i, int k, int j) const { return ((size_t)j * NZ2 + k) * LDX + i; }
-  size_t ic(int i, int k, int j) const { return ((size_t)j * NZ2 + k) * LDC + i; }
-  double M2(const std::vector<double> &a, int k, int j) const { return a[(size_t)j * (NZ + 3) + k]; }
-  double M3(const std::vector<double> &a, int k, int j, int f) const {
-    return a[(size_t)(f - 1) * (NZ + 3) * (NY + 3) + (size_t)j * (NZ + 3) + k];
-  }
-  double JAC(int k, int j) const { return M2(int_jacob, k, j); }
-};
+using namespace ekref_detail;
 
 static int fail(ekref_ctx *c, int code, const std::string &m) {
   c->err = m;
@@ -208,6 +112,13 @@ extern "C" int ekref_create(const ek_params *p, ekref_ctx **out) {
   c->sponge_sigma_out.assign(NZ + 2, 0.0);
   if (p->sponge_type != 0 && p->save_stats_int < 1)
     return fail(c.get(), EK_ERR_ARG, "SAVE_STATS_INT must be >= 1 with a sponge"), *out = c.release(), EK_ERR_ARG;
+  if (p->les) {
+    if (p->les_model_type != 2 || (p->n_th > 0 && p->les_model_type_th != 1))
+      return fail(c.get(), EK_ERR_ARG, "LES: only LES_MODEL_TYPE 2 with LES_MODEL_TYPE_TH 1"), *out = c.release(), EK_ERR_ARG;
+    if (wb[EK_YMIN] == 3)
+      return fail(c.get(), EK_ERR_ARG, "LES: the wall model (W_BC_YMIN = 3) is not restated"), *out = c.release(), EK_ERR_ARG;
+    les_alloc(c.get());
+  }
   c->fft = std::make_unique<FFT>(NX);
   *out = c.release();
   return EK_OK;
@@ -430,7 +341,7 @@ extern "C" int ekref_download_state(ekref_ctx *c, double *cu1, double *cu2, doub
 
 // ---------------------------------------------------------------------------
 // x-transforms (mpi_duct.F90:271-717 with NP = 1; MPI transposes are copies)
-static void to_fourier(ekref_ctx *c, const std::vector<double> &in, std::vector<cplx> &out, int j0, int j1, int k0, int k1) {
+void to_fourier(ekref_ctx *c, const std::vector<double> &in, std::vector<cplx> &out, int j0, int j1, int k0, int k1) {
   const FFT &f = *c->fft;
 #pragma omp parallel
   {
@@ -440,7 +351,7 @@ static void to_fourier(ekref_ctx *c, const std::vector<double> &in, std::vector<
       for (int k = k0; k <= k1; ++k) r2c_line(f, c->NKX, &in[c->ip(0, k, j)], &out[c->ic(0, k, j)], buf.data());
   }
 }
-static void to_physical(ekref_ctx *c, const std::vector<cplx> &in, std::vector<double> &out, int j0, int j1, int k0, int k1) {
+void to_physical(ekref_ctx *c, const std::vector<cplx> &in, std::vector<double> &out, int j0, int j1, int k0, int k1) {
   const FFT &f = *c->fft;
 #pragma omp parallel
   {
@@ -570,7 +481,11 @@ static void bc_z(ekref_ctx *c, int var, int J, Rows &r, const std::vector<double
 // One ADI-CN field update (e.g. U1: duct.F90:1640-1854).  coef = TEMP1 (or
 // TEMP1/PR for TH).  phi is U1X/U2X/U3X/THX, R the matching R*X.
 static void adi_field(ekref_ctx *c, int var, double coef, std::vector<double> &phi, std::vector<double> &R,
-                      int js, int je, int zs, int ze) {
+                      int js, int je, int zs, int ze, const LesAdi *les) {
+  // half-sum of the eddy viscosity over a face, times TEMP2 (duct.F90:1667-1854)
+  auto nuf = [&](int i, int k1, int j1, int k2, int j2) {
+    return 0.5 * ((*les->nu)[c->ip(i, k1, j1)] + (*les->nu)[c->ip(i, k2, j2)]);
+  };
   const int NXP = c->NXP, NY = c->NY, NZ = c->NZ;
   std::vector<double> &S = c->S1;
   // S = R - J*phi ; R = 0.5*S + J*phi + coef*d_zeta(G11 d_zeta phi)
@@ -586,6 +501,13 @@ static void adi_field(ekref_ctx *c, int var, double coef, std::vector<double> &p
         R[c->ip(i, k, j)] = 0.5 * S[c->ip(i, k, j)] + jac * phi[c->ip(i, k, j)] +
                             coef * (g1 * (phi[c->ip(i, k + 1, j)] - phi[c->ip(i, k, j)]) -
                                     g0 * (phi[c->ip(i, k, j)] - phi[c->ip(i, k - 1, j)]));
+      }
+      if (les) {  // e.g. duct.F90:1667-1680
+        const double l1 = c->M3(*les->g11, k + 1, j, 2), l0 = c->M3(*les->g11, k, j, 2);
+        for (int i = 0; i <= NXP; ++i)
+          R[c->ip(i, k, j)] = R[c->ip(i, k, j)] +
+                              les->temp2 * (nuf(i, k + 1, j, k, j) * (l1 * (phi[c->ip(i, k + 1, j)] - phi[c->ip(i, k, j)])) -
+                                            nuf(i, k, j, k - 1, j) * (l0 * (phi[c->ip(i, k, j)] - phi[c->ip(i, k - 1, j)])));
       }
     }
   // y-systems, one per K (THOMAS_REAL over I)
@@ -606,6 +528,15 @@ static void adi_field(ekref_ctx *c, int var, double coef, std::vector<double> &p
           U[j * ldy + i] = -coef * gu;
           V[j * ldy + i] = R[c->ip(i, k, j)];
         }
+        if (les) {  // e.g. duct.F90:1720-1731
+          const double ml = c->M3(*les->g22, k, j, 1), mu = c->M3(*les->g22, k, j + 1, 1);
+          for (int i = 0; i <= NXP; ++i) {
+            const double nl = les->temp2 * nuf(i, k, j, k, j - 1), nu = les->temp2 * nuf(i, k, j, k, j + 1);
+            L[j * ldy + i] = L[j * ldy + i] - nl * ml;
+            D[j * ldy + i] = D[j * ldy + i] + nu * mu + nl * ml;
+            U[j * ldy + i] = U[j * ldy + i] - nu * mu;
+          }
+        }
       }
       bc_y(c, var, k, rows, phi);
       thomas_real(L.data(), D.data(), U.data(), V.data(), NY + 1, NXP);
@@ -623,6 +554,13 @@ static void adi_field(ekref_ctx *c, int var, double coef, std::vector<double> &p
         R[c->ip(i, k, j)] = 0.5 * S[c->ip(i, k, j)] + jac * phi[c->ip(i, k, j)] +
                             coef * (+g1 * (phi[c->ip(i, k, j + 1)] - phi[c->ip(i, k, j)]) -
                                     g0 * (phi[c->ip(i, k, j)] - phi[c->ip(i, k, j - 1)]));
+      if (les) {  // e.g. duct.F90:1771-1784
+        const double l1 = c->M3(*les->g22, k, j + 1, 1), l0 = c->M3(*les->g22, k, j, 1);
+        for (int i = 0; i <= NXP; ++i)
+          R[c->ip(i, k, j)] = R[c->ip(i, k, j)] +
+                              les->temp2 * (nuf(i, k, j + 1, k, j) * (l1 * (phi[c->ip(i, k, j + 1)] - phi[c->ip(i, k, j)])) -
+                                            nuf(i, k, j - 1, k, j) * (l0 * (phi[c->ip(i, k, j)] - phi[c->ip(i, k, j - 1)])));
+      }
     }
   // z-systems, one per J
 #pragma omp parallel
@@ -640,6 +578,15 @@ static void adi_field(ekref_ctx *c, int var, double coef, std::vector<double> &p
           D[k * ldy + i] = dd;
           U[k * ldy + i] = -coef * gu;
           V[k * ldy + i] = R[c->ip(i, k, j)];
+        }
+        if (les) {  // e.g. duct.F90:1821-1832
+          const double ml = c->M3(*les->g11, k, j, 2), mu = c->M3(*les->g11, k + 1, j, 2);
+          for (int i = 0; i <= NXP; ++i) {
+            const double nl = les->temp2 * nuf(i, k, j, k - 1, j), nu = les->temp2 * nuf(i, k + 1, j, k, j);
+            L[k * ldy + i] = L[k * ldy + i] - nl * ml;
+            D[k * ldy + i] = D[k * ldy + i] + nu * mu + nl * ml;
+            U[k * ldy + i] = U[k * ldy + i] - nu * mu;
+          }
         }
       }
       bc_z(c, var, j, rows, phi);
@@ -878,12 +825,14 @@ static void add_c(ekref_ctx *c, std::vector<cplx> &CF, const std::vector<cplx> &
 extern "C" int ekref_rk_substep(ekref_ctx *c, int rk) {
   if (!c->have_metrics) return fail(c, EK_ERR_STATE, "metrics not set");
   if (rk < 1 || rk > 3) return fail(c, EK_ERR_ARG, "rk_step must be 1..3");
+  if (c->p.les && !c->have_les_metrics) return fail(c, EK_ERR_STATE, "LES metrics not set");
   const ek_params &p = c->p;
   const int NX2P = c->NX2P, NXP = c->NXP, NY = c->NY, NZ = c->NZ;
   const int JS = c->JSTART, JE = c->JEND, ZS = c->ZSTART, ZE = c->ZEND;
   const int JST = c->JSTART_TH, JET = c->JEND_TH, ZST = c->ZSTART_TH, ZET = c->ZEND_TH;
   const double NU = p.nu;
   const double TEMP1 = NU * c->H_BAR[rk] / 2.0;
+  const double TEMP2 = c->H_BAR[rk] / 2.0;
   const double TEMP3 = c->ZETA_BAR[rk] * c->H_BAR[rk];
   const double TEMP4 = c->H_BAR[rk];
   const double TEMP5 = c->BETA_BAR[rk] * c->H_BAR[rk];
@@ -978,8 +927,11 @@ extern "C" int ekref_rk_substep(ekref_ctx *c, int rk) {
                              0.5 * c->M3(c->cjob_22, k, j + 1, 1) * (TB(k, j) + TB(k, j + 1)) -
                              0.5 * c->M3(c->cjob_22, k, j, 1) * (TB(k, j) + TB(k, j - 1));
             CFTH[q] = csub(CFTH[q], cscale(g, CU2[q]));
+            // with LES the coefficient takes KAPPA_T at the physical point
+            // whose x index equals the mode index (duct.F90:610-618)
+            const double kap = p.les ? (nupr + c->KAPPA_T[c->ip(i, k, j)]) : nupr;
             const double d =
-                0.25 * nupr *
+                0.25 * kap *
                 (+c->M3(c->gmat_12, k + 1, j, 2) * (TB(k + 1, j + 1) + TB(k, j + 1) - TB(k, j - 1) - TB(k + 1, j - 1)) -
                  c->M3(c->gmat_12, k, j, 2) * (TB(k - 1, j + 1) + TB(k, j + 1) - TB(k, j - 1) - TB(k - 1, j - 1)) +
                  c->M3(c->gmat_12, k, j + 1, 1) * (TB(k + 1, j + 1) + TB(k + 1, j) - TB(k - 1, j + 1) - TB(k - 1, j)) -
@@ -992,11 +944,18 @@ extern "C" int ekref_rk_substep(ekref_ctx *c, int rk) {
       }
   }
   if (th && p.sponge_type != 0) sponge_th(c);  // duct.F90:635, inside the scalar loop
-  // to physical space (duct.F90:656-673)
-  to_physical(c, CU1, c->U1, 0, NY + 1, 0, NZ + 1);
-  to_physical(c, CU2, c->U2, 0, NY + 1, 0, NZ + 1);
-  to_physical(c, CU3, c->U3, 0, NY + 1, 0, NZ + 1);
-  if (th) to_physical(c, CTH, c->TH, 0, NY + 1, 0, NZ + 1);
+  const bool les = c->les_active();
+  if (les) {
+    // les_chan / les_chan_th (duct.F90:641-654) leave the fields in physical space
+    les_chan(c, rk);
+    if (th) les_chan_th(c);
+  } else {
+    // to physical space (duct.F90:656-673)
+    to_physical(c, CU1, c->U1, 0, NY + 1, 0, NZ + 1);
+    to_physical(c, CU2, c->U2, 0, NY + 1, 0, NZ + 1);
+    to_physical(c, CU3, c->U3, 0, NY + 1, 0, NZ + 1);
+    if (th) to_physical(c, CTH, c->TH, 0, NY + 1, 0, NZ + 1);
+  }
   auto &U1 = c->U1, &U2 = c->U2, &U3 = c->U3, &TH = c->TH, &S1 = c->S1;
 
   // nonlinear terms (duct.F90:683-1121)
@@ -1036,6 +995,7 @@ extern "C" int ekref_rk_substep(ekref_ctx *c, int rk) {
   flux_terms(c, U3, NU, JS, JE, ZS, ZE);
   to_fourier(c, S1, CS1, JS, JE, ZS, ZE);
   add_c(c, CF3, CS1, JS, JE, ZS, ZE);
+  if (les) les_cross_terms(c);  // duct.F90:990-1120
   // CR += TEMP5*CF (duct.F90:1127-1149), R to physical
 #pragma omp parallel for schedule(static)
   for (int j = JS; j <= JE; ++j)
@@ -1056,6 +1016,7 @@ extern "C" int ekref_rk_substep(ekref_ctx *c, int rk) {
     flux_terms(c, TH, NU / p.pr, JST, JET, ZST, ZET);
     to_fourier(c, S1, CS1, JST, JET, ZST, ZET);
     add_c(c, CFTH, CS1, JST, JET, ZST, ZET);
+    if (les) les_cross_terms_th(c);  // duct.F90:1266-1311
 #pragma omp parallel for schedule(static)
     for (int j = JST; j <= JET; ++j)
       for (int k = ZST; k <= ZET; ++k)
@@ -1065,7 +1026,8 @@ extern "C" int ekref_rk_substep(ekref_ctx *c, int rk) {
         }
     to_physical(c, CRTH, c->RTH, JST, JET, ZST, ZET);
     // ADI for TH (duct.F90:1334-1625), then corner copies (1610-1624)
-    adi_field(c, 0, TEMP1 / p.pr, TH, c->RTH, JST, JET, ZST, ZET);
+    const LesAdi la{&c->KAPPA_T, &c->gmat_11, &c->gmat_22, TEMP2};
+    adi_field(c, 0, TEMP1 / p.pr, TH, c->RTH, JST, JET, ZST, ZET, les ? &la : nullptr);
     if (p.th_bc[EK_ZMAX] == 1)
       for (int i = 0; i <= NXP; ++i) {
         TH[c->ip(i, NZ + 1, NY + 1)] = TH[c->ip(i, NZ, NY + 1)];
@@ -1081,9 +1043,11 @@ extern "C" int ekref_rk_substep(ekref_ctx *c, int rk) {
         TH[c->ip(i, 0, 0)] = TH[c->ip(i, NZ, 0)];
       }
   }
-  adi_field(c, 1, TEMP1, U1, c->R1, JS, JE, ZS, ZE);
-  adi_field(c, 2, TEMP1, U2, c->R2, JS, JE, ZS, ZE);
-  adi_field(c, 3, TEMP1, U3, c->R3, JS, JE, ZS, ZE);
+  const LesAdi l1{&c->NU_T, &c->gmat_11, &c->gmat_22, TEMP2}, l2{&c->NU_T, &c->g11y, &c->g22y, TEMP2},
+      l3{&c->NU_T, &c->g11z, &c->g22z, TEMP2};
+  adi_field(c, 1, TEMP1, U1, c->R1, JS, JE, ZS, ZE, les ? &l1 : nullptr);
+  adi_field(c, 2, TEMP1, U2, c->R2, JS, JE, ZS, ZE, les ? &l2 : nullptr);
+  adi_field(c, 3, TEMP1, U3, c->R3, JS, JE, ZS, ZE, les ? &l3 : nullptr);
   // COURANT_CURV_MPI (duct.F90:2417-2419, 3605-3674)
   if (p.variable_dt && rk == 3 && p.time_step % p.update_dt == 0) {
     double dt = 999.0;
@@ -1134,6 +1098,7 @@ extern "C" int ekref_step(ekref_ctx *c, int nsteps) {
       if (st != EK_OK) return st;
     }
     c->p.time += c->p.delta_t;
+    c->first_time = false;  // diablo.F90:157
   }
   return EK_OK;
 }

@@ -38,10 +38,13 @@ def test_exports_every_declared_symbol(lib):
 @pytest.mark.parametrize("field,value,msg", [
     ("nx", 48, "power of two"), ("ic_type", 5, "IC_TYPE"), ("sponge_type", 3, "SPONGE"),
     ("save_stats_int", 0, "SAVE_STATS_INT"),
-    ("les", 1, "LES"), ("f_type", 0, "F_TYPE"), ("mg_ixp", 3, "Mudpack")])
+    ("les_model_type", 1, "LES_MODEL_TYPE"), ("les_model_type_th", 2, "LES_MODEL_TYPE_TH"),
+    ("f_type", 0, "F_TYPE"), ("mg_ixp", 3, "Mudpack")])
 def test_create_rejects_unsupported(lib, field, value, msg):
     p = default_params(16, 15, 15)
     setattr(p, field, value)
+    if field.startswith("les_"):
+        p.les = 1
     if field == "save_stats_int":
         p.sponge_type = 2
     if field == "mg_ixp":  # grid_def shape that does not match NZ+2 = 17
