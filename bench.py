@@ -4,7 +4,7 @@ python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
 
 Workload: the stratified Ekman layer 512 x 385 x 257 (NX x NY+2 x NZ+2;
 NY = 384 rounded up to MUDPACK form), Re = 1000, Pr = 0.7, Ri = 0.1,
-dt = 5e-4, seeded synthetic fields (laminar Ekman spiral + 1% Gaussian
+dt = 3e-4, seeded synthetic fields (laminar Ekman spiral + 1% Gaussian
 noise), FP64 fields, every per-kx Poisson problem (171 complex ones) driven
 to a relative residual of 1e-8 (the singular kx = 0 mode keeps MUDPACK's
 own rule).  Prints one JSON line: RK3 steps/s of the batched
@@ -14,6 +14,12 @@ path on the same workload; the fields are larger than the 126 MB L2, so no
 flush is needed between steps.  For N > 1 each rank
 runs an independent replica on its own GPU (the path does not shard) and
 the value is the sum over ranks.
+
+The line also carries "les": the LES case 1024 x 513 x 385 (dynamic
+Smagorinsky, les_chan / les_chan_th) timed over one C_DYN period of five
+steps with the same mixed-precision method, the plain FP64 path beside it,
+the LES kernels' share and roofline, and one oracle LES substep on the host
+cores (skip with --no-les).
 """
 from __future__ import annotations
 
@@ -105,22 +111,24 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------
-def setup_solver(device_index: int, mg_fast: int = 1, fft_fp32: int = 1):
+def setup_solver(device_index: int, mg_fast: int = 1, fft_fp32: int = 1, workload: str = WORKLOAD):
     import torch
 
     from ekman_bl_gb300 import build as ekbuild
-    from ekman_bl_gb300.duct import DuctSolver, metrics_from_grid
+    from ekman_bl_gb300.duct import DuctSolver, les_metrics_from_grid, metrics_from_grid
     from ekman_bl_gb300.params import EK_MG_STOP_RESIDUAL, WORKLOADS, workload_setup
 
     ekbuild.build()
     torch.cuda.set_device(device_index)
-    w = WORKLOADS[WORKLOAD]
+    w = WORKLOADS[workload]
     w.mg_tol = MG_TOL
     p, xp, yp, state = workload_setup(w, EK_MG_STOP_RESIDUAL)
     p.mg_fast = mg_fast
     p.fft_fp32 = fft_fp32
     p.ff_arith = 1 if fft_fp32 else 0
     solver = DuctSolver(p, metrics_from_grid(p, xp, yp))
+    if p.les:
+        solver.set_les_metrics(les_metrics_from_grid(p, xp, yp))
     stream = torch.cuda.Stream()
     solver.set_stream(stream.cuda_stream)
     solver.upload(*state)
@@ -252,6 +260,77 @@ def run_learned(solver, stream, args):
                                                                                  else v) for k, v in rep.items()}}}
 
 
+LES_WORKLOAD = "ekman_les_1024x513x385"
+LES_STEPS = 5  # one C_DYN period: RK_STEP 1 of every fifth step recomputes it
+
+
+def run_les(args, local):
+    """The LES case (dynamic Smagorinsky, les_chan / les_chan_th): RK3
+    steps/s of the mixed-precision method and of the plain FP64 path over
+    one C_DYN period after the FIRST_TIME step, the LES kernels' share and
+    roofline, and the oracle's LES substep on the host cores beside it."""
+    import torch
+
+    peak, peak_kind = peaks()
+    w, p, _, _, _, solver, stream = setup_solver(local, 1, 1, workload=LES_WORKLOAD)
+    solver.mg_autotune(reps=2)
+    ms, cyc, launches, clocks = time_steps(solver, stream, LES_STEPS, 1, clocks_gpu=local)
+    solver.set_timing(True)
+    solver.step(LES_STEPS)
+    kt = solver.timing()
+    solver.set_timing(False)
+    solver.close()
+    per = {k: (v[0] / LES_STEPS, v[1] / LES_STEPS, v[2] / LES_STEPS) for k, v in kt.items()}
+    ktot = sum(v[0] for v in per.values())
+    les_ms, les_cnt, les_bytes = per.get("les", (0.0, 0, 0.0))
+    roof = None
+    if les_ms > 0:
+        achieved = les_bytes / (les_ms / 1000.0) / 1e9
+        roof = {"bound": "hbm", "kernel": "les (line, scalar-flux and flux-addition kernels)",
+                "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "peak_kind": peak_kind, "share_of_step": round(les_ms / ktot, 4)}
+    _, _, _, _, _, plain, pstream = setup_solver(local, 0, 0, workload=LES_WORKLOAD)
+    pms, pcyc, _, _ = time_steps(plain, pstream, 2, 1)
+    plain.close()
+    torch.cuda.synchronize()
+    out = {"workload": LES_WORKLOAD, "nx": p.nx, "ny_plus_2": p.ny + 2, "nz_plus_2": p.nz + 2,
+           "model": "dynamic Smagorinsky (LES_MODEL_TYPE 2), KAPPA_T = NU_T/PR (LES_MODEL_TYPE_TH 1)",
+           "value": round(LES_STEPS / (ms / 1000.0), 4), "unit": "RK3 steps/s",
+           "ms_per_step": round(ms / LES_STEPS, 3), "steps": LES_STEPS, "warmup": 1,
+           "mg_corrections_per_substep_max": cyc, "gpu_launches": int(launches), "clocks": clocks,
+           "plain": {"value": round(2 / (pms / 1000.0), 4), "ms_per_step": round(pms / 2, 3), "steps": 2,
+                     "mg_cycles_per_substep_max": pcyc},
+           "speedup_vs_plain": round((LES_STEPS / ms) / (2 / pms), 3),
+           "kernel_ms_per_step": {k: round(v[0], 3) for k, v in per.items()},
+           "roofline": roof}
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = les_cpu_baseline()
+    return out
+
+
+def les_cpu_baseline():
+    """The oracle's LES path on the host cores, bounded sample: one substep
+    (RK_STEP 1 of the FIRST_TIME step, C_DYN recomputed) of the LES case."""
+    from ekman_bl_gb300.params import EK_MG_STOP_RESIDUAL, WORKLOADS, workload_setup
+    from oracle import ekref
+
+    cores = os.cpu_count() or 1
+    w = WORKLOADS[LES_WORKLOAD]
+    w.mg_tol = MG_TOL
+    p, xp, yp, state = workload_setup(w, EK_MG_STOP_RESIDUAL)
+    o = ekref.Oracle(p, ekref.metrics_from_grid(p, xp, yp), threads=cores)
+    o.set_les_metrics(ekref.les_metrics_from_grid(p, xp, yp))
+    o.upload(*state)
+    o.set_time(0.0, 1)
+    t0 = time.perf_counter()
+    o.rk_substep(1)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": round(1.0 / (3.0 * dt), 5), "unit": "RK3 steps/s (3 x the substep time)", "cores": cores,
+            "kind": "port", "sample": f"1 substep (RK_STEP 1, C_DYN recomputed) of {LES_WORKLOAD}, "
+                                      f"{cores} OpenMP threads ({dt:.1f} s)"}
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -312,6 +391,7 @@ def run_gpu(args):
     pms, pcyc, _, _ = time_steps(plain, pstream, args.steps, args.warmup)
     plain_pois_ms, plain_pst, _ = time_poisson(plain, pstream, p)
     plain.close()
+    les = None if args.no_les else run_les(args, local)
 
     result = None
     if rank == 0:
@@ -374,6 +454,7 @@ def run_gpu(args):
                     "steps": n_e2e},
             "roofline": roof,
             "learned": learned,
+            "les": les,
         }
         if world == 1 and not args.no_cpu_baseline:
             result["cpu_baseline"] = cpu_baseline(args)
@@ -454,6 +535,7 @@ def main():
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip training and timing the learned guess")
+    ap.add_argument("--no-les", action="store_true", help="skip the LES case")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gpu":
         args.warmup = 3

@@ -330,7 +330,8 @@ void launch_les(Ctx &c, int rk) {
   const unsigned nlines = (unsigned)((d.ZE - d.ZS + 1) * (d.JE - d.JS + 1));
   const bool dyn = (p.time_step % 5 == 0 && rk == 1) || L.first_time;
   {
-    KScope ks(c, KC_LES, 8.0 * (double)d.NX * nlines * (dyn ? 22 : 19));
+    // algorithmic bytes: read d(U1,U2,U3)/dx and U1..U3, write NU_T and four stresses
+    KScope ks(c, KC_LES, 8.0 * 11.0 * (double)d.NX * nlines);
     if (dyn) k_les_line<true><<<nlines, kLineThreads, les_line_smem(d), c.stream>>>(la);
     else k_les_line<false><<<nlines, kLineThreads, 0, c.stream>>>(la);
     after_launch(c);
@@ -350,7 +351,8 @@ void launch_les(Ctx &c, int rk) {
     ea.e1 = L.ext[0]; ea.e2 = L.ext[1]; ea.e3 = L.ext[2]; ea.eth = L.ext[3];
     ea.inv_pr = 1.0 / p.pr;
     ea.th = th ? 1 : 0;
-    KScope ks(c, KC_LES, 8.0 * (double)d.NX * d.NZ2 * d.NY2 * 16);
+    // read U1..U3, TH, NU_T and three stresses, write four additions (interior points)
+    KScope ks(c, KC_LES, 8.0 * 12.0 * (double)d.NX * nlines);
     dim3 grid((d.NX + 127) / 128, d.NZ2, d.NY2);
     k_les_extra<<<grid, 128, 0, c.stream>>>(ea);
     after_launch(c);

@@ -817,7 +817,8 @@ void launch_adi(Ctx &c, int field, int rk) {
     a.lg_m = l22;
     {
       dim3 grid((d.NX + 127) / 128, a.ze - a.zs + 1);
-      KScope ks(c, KC_ADI_Y, 96.0 * d.NX * d.NY2 * (a.ze - a.zs + 1));
+      // algorithmic: read R, the field and NU_T, write the result
+      KScope ks(c, KC_ADI_Y, 32.0 * d.NX * d.NY2 * (a.ze - a.zs + 1));
       k_adi_les<false><<<grid, 128, 0, c.stream>>>(a);
       after_launch(c);
     }
@@ -828,7 +829,8 @@ void launch_adi(Ctx &c, int field, int rk) {
     a.lg_m = l11;
     {
       dim3 grid((d.NX + 127) / 128, d.NY2);
-      KScope ks(c, KC_ADI_Z, 96.0 * d.NX * d.NZ2 * (a.je - a.js + 1));
+      // read R, the old field, the y-sweep result and NU_T, write the result
+      KScope ks(c, KC_ADI_Z, 40.0 * d.NX * d.NZ2 * (a.je - a.js + 1));
       k_adi_les<true><<<grid, 128, 0, c.stream>>>(a);
       after_launch(c);
     }

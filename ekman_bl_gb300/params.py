@@ -156,6 +156,8 @@ class Workload:
     lx_d: float          # spanwise period, in Ekman depths
     cell_d: float        # y-z cell size (uniform z, mean y), in Ekman depths
     seed: int = 0
+    les: int = 0         # dynamic-Smagorinsky LES; the synthetic field stands in for a
+                         # restart file (CREATE_NEW_FLOW = .FALSE.)
 
     def params(self, mg_stop: int = EK_MG_STOP_RELCHANGE) -> EkParams:
         p = default_params(self.nx, self.ny2 - 2, self.nz2 - 2)
@@ -169,6 +171,8 @@ class Workload:
         p.mg_tol = MUDPACK_TOLMAX if mg_stop == EK_MG_STOP_RELCHANGE else self.mg_tol
         if mg_stop == EK_MG_STOP_RESIDUAL:
             p.mg_maxcy = 60
+        if self.les:
+            p.les, p.create_new_flow = 1, 0
         return p
 
     @property
@@ -177,8 +181,8 @@ class Workload:
 
 
 # The reference's named cases (CPU-runnable neutral case, the stratified
-# plain-path case, the large stratified case), with the vertical size rounded
-# up to MUDPACK's p*2^k+1.
+# plain-path case, the large stratified case, the LES case), with the
+# vertical size rounded up to MUDPACK's p*2^k+1.
 WORKLOADS = {
     "ekman_neutral_64x65x65": Workload("ekman_neutral_64x65x65", 64, 65, 65, 400.0, 1.0, 0.0, 1.0e-3, 100,
                                        1e-10, 0.01, 4.0 * math.pi, 0.4),
@@ -188,6 +192,10 @@ WORKLOADS = {
                                         1e-10, 0.01, 64.0, 0.35),
     "ekman_strat_512x385x257": Workload("ekman_strat_512x385x257", 512, 385, 257, 1000.0, 0.7, 0.1, 3.0e-4, 200,
                                         1e-8, 0.01, 128.0, 0.3),
+    # the LES case: twice the spanwise and about 1.3 and 1.5 times the vertical
+    # and streamwise points of the large stratified case at the same cell sizes
+    "ekman_les_1024x513x385": Workload("ekman_les_1024x513x385", 1024, 513, 385, 1000.0, 0.7, 0.1, 3.0e-4, 500,
+                                       1e-8, 0.01, 256.0, 0.3, les=1),
 }
 
 
