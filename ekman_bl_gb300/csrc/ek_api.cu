@@ -151,10 +151,12 @@ int substep(Ctx &c, int rk) {
       a.pro = PRO_PROD; a.a = c.U1; a.b = uu[f]; a.epi = EPI_SUB_IK; a.dst = cf[f];
       a.af = f32 ? c.U1f : nullptr; a.bf = f32 ? uf[f] : nullptr;
       a.extra = les ? c.les.t[f] : nullptr;  // + J tau_1f
+      a.extraf = les ? c.les.tf[f] : nullptr;
       launch_r2c(c, a);
       a.pro = PRO_FLUX; a.a = uu[f]; a.b = c.U2b; a.visc = p.nu; a.epi = EPI_ADD;
       a.af = f32 ? uf[f] : nullptr; a.bf = f32 ? c.U2bf : nullptr;
       a.extra = les ? c.les.ext[f] : nullptr;  // + NU_T cross term - stress divergence
+      a.extraf = les ? c.les.extf[f] : nullptr;
       launch_r2c(c, a);
     }
   }
@@ -175,10 +177,12 @@ int substep(Ctx &c, int rk) {
     a.pro = PRO_PROD; a.a = c.TH; a.b = c.U1; a.epi = EPI_SUB_IK; a.dst = c.CFTH;
     a.af = f32 ? c.THf : nullptr; a.bf = f32 ? c.U1f : nullptr;
     a.extra = les ? c.les.tth : nullptr;  // + J (-KAPPA_T dTH/dx)
+    a.extraf = les ? c.les.tthf : nullptr;
     launch_r2c(c, a);
     a.pro = PRO_FLUX; a.a = c.TH; a.b = c.U2b; a.visc = p.nu / p.pr; a.epi = EPI_ADD;
     a.af = f32 ? c.THf : nullptr; a.bf = f32 ? c.U2bf : nullptr;
     a.extra = les ? c.les.ext[3] : nullptr;  // + KAPPA_T cross term
+    a.extraf = les ? c.les.extf[3] : nullptr;
     launch_r2c(c, a);
     C2rArgs b{};
     b.j0 = d.JST; b.j1 = d.JET; b.k0 = d.ZST; b.k1 = d.ZET;
@@ -550,6 +554,7 @@ int ekgpu_set_les_metrics(ek_ctx *h, const double *gmat_11_y, const double *gmat
     up(c.m.g11y, gmat_11_y); up(c.m.g12y, gmat_12_y); up(c.m.g22y, gmat_22_y);
     up(c.m.g11z, gmat_11_z); up(c.m.g12z, gmat_12_z); up(c.m.g22z, gmat_22_z);
     c.les.have_metrics = true;
+    c.les.tab_ok = false;
     return (int)EK_OK;
   });
 }
@@ -593,6 +598,7 @@ int ekgpu_set_metrics(ek_ctx *h, const ek_metrics *m) {
     up(c.m.thbar, m->th_bar, n2);
     if (!c.m.pg) c.m.pg = dalloc<double>(c, 11 * n2);
     launch_metric_tables(c);
+    c.les.tab_ok = false;
     std::vector<double> jac(m->int_jacob, m->int_jacob + n2), g11(m->gmat_11, m->gmat_11 + 2 * n2),
         g12(m->gmat_12, m->gmat_12 + 2 * n2), g22(m->gmat_22, m->gmat_22 + 2 * n2), c22(m->cjob_22, m->cjob_22 + 2 * n2);
     // boundary rows and Thomas factors of every field, substep and direction

@@ -178,10 +178,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
       zr[n] = s1 + s2;
     }
   }
-  if (args.extra && args.pro != PRO_LOAD) {
+  if (args.pro != PRO_LOAD && (args.extra || args.extraf)) {
     // LES additions: jac * tau for a product, the precomputed terms for a flux
     const T es = (args.pro == PRO_PROD) ? (T)fc.m.jac[d.m2(k, j)] : (T)1.0;
-    for (int n = lane; n < NX; n += 32) zr[n] = zr[n] + es * (T)args.extra[base + n];
+    if (kF && args.extraf)
+      for (int n = lane; n < NX; n += 32) zr[n] = zr[n] + es * (T)args.extraf[base + n];
+    else if (args.extra)
+      for (int n = lane; n < NX; n += 32) zr[n] = zr[n] + es * (T)args.extra[base + n];
   }
   __syncwarp();
   dif_fft(z, M, tw_m<T>(fc), false, lane);
@@ -279,7 +282,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
   __syncwarp();
   dif_fft(z, M, tw_m<T>(fc), true, lane);
   const T *zr = reinterpret_cast<const T *>(z);
-  double *dst = args.dst + d.ip(0, k, j);
+  double *dst = args.dst ? args.dst + d.ip(0, k, j) : nullptr;
   float *dstf = args.dstf ? args.dstf + d.ip(0, k, j) : nullptr;
   const int NX = d.NX;
   for (int n = lane; n < NX + 2; n += 32) {
@@ -289,10 +292,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
       v = zr[2 * brev(m, fc.logM) + (n & 1)];
     }
     if constexpr (sizeof(T) == 4) {
-      dst[n] = f2d_bits((float)v);
+      if (dst) dst[n] = f2d_bits((float)v);
       if (dstf) dstf[n] = (float)v;
     } else {
-      dst[n] = (double)v;
+      if (dst) dst[n] = (double)v;
       if (dstf) dstf[n] = d2f_bits((double)v);
     }
   }

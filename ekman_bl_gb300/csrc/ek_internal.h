@@ -232,12 +232,16 @@ struct GuessState {
 struct LesState {
   bool have_metrics = false;
   bool first_time = true;       // FIRST_TIME: recompute C_DYN in every substep
-  double *nut = nullptr;        // NU_T, zero outside the velocity interior
+  bool lowp = false;            // stresses in FP32 (fft_fp32 >= 1): the f-suffixed buffers
+  bool tab_ok = false;          // tabf matches the metrics
+  double *nut = nullptr;        // NU_T, zero outside the velocity interior (both precisions)
   double *cdyn = nullptr;       // C_DYN(0:NZ+1, 0:NY+1), K fastest
   double *t[3] = {};            // d(U1,U2,U3)/dx, then tau_11, tau_12, tau_13 in place
   double *t23 = nullptr;        // tau_23
   double *tth = nullptr;        // d(TH)/dx, then the scalar flux -KAPPA_T d(TH)/dx in place
   double *ext[4] = {};          // flux-transform additions of U1, U2, U3, TH
+  float *tf[3] = {}, *t23f = nullptr, *tthf = nullptr, *extf[4] = {}, *nutf = nullptr;
+  float *tabf = nullptr;        // per-cell FP32 weights of the FP32 kernels
 };
 
 struct Ctx {
@@ -300,7 +304,8 @@ struct Ctx {
   // per-cell right-hand-side weights of the two ADI sweeps (k_adi_tab)
   double *adi_tab = nullptr;
   LesState les;
-  double *adi_scr = nullptr;  // LES ADI: the modified upper diagonals (one field)
+  double *adi_scr = nullptr;      // LES ADI: 1/B and the upper diagonal of the eliminated rows (two fields)
+  double *adi_les_tab = nullptr;  // LES ADI: per-cell row weights of the two sweeps (k_adi_les_tab)
   // divergence check
   double *div_part = nullptr;
   double last_div = 0.0;
@@ -371,6 +376,7 @@ enum { EPI_STORE = 0, EPI_ADD = 1, EPI_SUB_IK = 2 };
 struct R2cArgs {
   const double *a, *b;    // PRO_LOAD: a; PRO_PROD: jac*a*b; PRO_FLUX: field a
   const double *extra;    // when set: PRO_PROD adds jac*extra, PRO_FLUX adds extra
+  const float *extraf;    // the same term in FP32, read by the FP32 kernel instead of extra
   double visc;            // PRO_FLUX viscosity
   cplx_t *dst;
   int epi;
@@ -387,7 +393,7 @@ struct C2rArgs {
   double *dst;
   int j0, j1, k0, k1;
   int lowp;                  // as R2cArgs::lowp
-  float *dstf;               // also write an FP32 copy of dst when given
+  float *dstf;               // also write an FP32 copy of dst when given (dst may then be null)
 };
 void launch_c2r(Ctx &c, const C2rArgs &a);
 

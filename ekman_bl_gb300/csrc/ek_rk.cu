@@ -268,11 +268,10 @@ struct AdiArgs {
   double coef;
   int js, je, zs, ze;
   const double *tab;  // per-cell right-hand-side weights of this sweep (k_adi_tab)
-  // LES (k_adi_les): viscosity nu = nut * nscale, the LES metric of the
-  // right-hand-side term (lg_r) and of the matrix (lg_m), TEMP2 = H/2, and
-  // two scratch fields for the eliminated diagonal and the upper diagonal
-  const double *nut, *lg_r, *lg_m;
-  double nscale, temp2;
+  // LES (k_adi_les): NU_T, the per-cell row weights of this sweep
+  // (k_adi_les_tab) and two scratch fields for the reciprocal of the
+  // eliminated diagonal and the upper diagonal
+  const double *nut, *ltab;
   double *scr_b, *scr_u;
 };
 
@@ -388,18 +387,47 @@ __global__ void __launch_bounds__(32 * kAdiWarps) k_adi(AdiArgs a) {
   }
 }
 
+// Per-cell weights of one LES ADI sweep (seven planes, ltab[t * n2 + m2(k, j)]):
+//   t0 = -c Gb(lo), t1 = -c Gb(up), t2 = J + c (Gb(up) + Gb(lo))   the plain row
+//   t3 = h Gm(lo),  t4 = h Gm(up)     eddy-viscosity face weights of the row
+//   t5 = h Gr(+),   t6 = h Gr(-)      and of the explicit term across the line
+// with c = NU H/2 [/PR], h = TEMP2/2 [/PR] (KAPPA_T = NU_T/PR for TH); Gb the
+// plain metric of the line direction (GMAT_22 for y, GMAT_11 for z), Gm the
+// LES metric of the line direction and Gr that of the other direction
+// (GMAT_*, GMAT_*_y for U2, GMAT_*_z for U3).  Faces: y lines lo = (k,j,1),
+// up = (k,j+1,1), across (k+1,j,2) / (k,j,2); z lines lo = (k,j,2),
+// up = (k+1,j,2), across (k,j+1,1) / (k,j,1).
+template <bool ZS>
+__global__ void k_adi_les_tab(Dims d, Metrics m, const double *gb, const double *gm, const double *gr, double c,
+                              double h, double *tab) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (k < 1 || k > d.NZ || j < 1 || j > d.NY) return;
+  const size_t n2 = (size_t)d.LDM * (d.NY + 3), mm = d.m2(k, j);
+  const size_t lo = ZS ? d.m3(k, j, 2) : d.m3(k, j, 1), up = ZS ? d.m3(k + 1, j, 2) : d.m3(k, j + 1, 1);
+  const size_t xp = ZS ? d.m3(k, j + 1, 1) : d.m3(k + 1, j, 2), xm = ZS ? d.m3(k, j, 1) : d.m3(k, j, 2);
+  tab[mm] = -c * gb[lo];
+  tab[n2 + mm] = -c * gb[up];
+  tab[2 * n2 + mm] = m.jac[mm] + c * (gb[up] + gb[lo]);
+  tab[3 * n2 + mm] = h * gm[lo];
+  tab[4 * n2 + mm] = h * gm[up];
+  tab[5 * n2 + mm] = h * gr[xp];
+  tab[6 * n2 + mm] = h * gr[xm];
+}
+
 // CN-ADI line solves with the LES eddy viscosity (duct.F90:1373-1386,
 // 1437-1450, 1489-1500, 1559-1569 for TH; 1667-1680, 1720-1731, 1771-1784,
 // 1821-1832 for U1; 1916-1929, 1963-1973, 2013-2026, 2081-2091 for U2 with
 // GMAT_*_y; 2177-2190, 2224-2234, 2300-2313, 2358-2368 for U3 with GMAT_*_z):
 // the matrix rows depend on x through NU_T, so each thread owns one system
-// (one x point of one line), builds every row -- the right-hand side of
-// k_adi plus the NU_T terms, the tridiagonal row, or the boundary row -- and
-// runs THOMAS_REAL (boundary.F90:53-84) on it.  The forward sweep parks the
-// eliminated diagonal and the upper diagonal in two scratch fields and the
-// modified right-hand side in the output; the back substitution reads them
-// back.  Consecutive threads take consecutive x points, so every access is
-// coalesced.
+// (one x point of one line) and builds every row -- the right-hand side of
+// k_adi plus the NU_T term across the line, the tridiagonal row from the
+// per-cell weights and the two face sums of NU_T, or the boundary row -- then
+// runs the elimination of THOMAS_REAL (boundary.F90:53-84) with one
+// reciprocal per row: the forward sweep parks 1/B and the upper diagonal in
+// two scratch fields and the modified right-hand side in the output, the
+// back substitution reads them back.  Consecutive threads take consecutive x
+// points, so every access is coalesced; the work is FP64 arithmetic, about
+// two dozen operations and one reciprocal per row.
 template <bool ZS>
 __global__ void __launch_bounds__(128) k_adi_les(AdiArgs a) {
   const Dims &d = a.d;
@@ -416,49 +444,27 @@ __global__ void __launch_bounds__(128) k_adi_les(AdiArgs a) {
   const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
   const size_t sA = ZS ? sK : sJ;  // along the line
   const size_t sX = ZS ? sJ : sK;  // across: the direction of the explicit term
-  const double h2 = 0.5 * a.temp2;
-  const double *nut = a.nut, *R = a.R, *po = a.phi_old, *ps = a.phs;
-  const double *gb = ZS ? a.m.g11 : a.m.g22;  // base matrix metric
-  const int fm = ZS ? 2 : 1;                  // its face
+  const double *nut = a.nut, *R = a.R, *po = a.phi_old, *ps = a.phs, *lt = a.ltab, *tb = a.tab;
+  const double *px = ZS ? ps : po;  // field of the explicit term across the line
   auto at = [&](int r) { return ZS ? d.ip(i, r, line) : d.ip(i, line, r); };
-  auto mrow = [&](int r, int &k, int &j) {
-    k = ZS ? r : line;
-    j = ZS ? line : r;
-  };
-  double Bp = 1.0, gp = 0.0, Up = 0.0;
+  double rBp = 1.0, gp = 0.0, Up = 0.0;
   for (int r = 0; r < nrow; ++r) {
     double L = 0.0, D = 1.0, U = 0.0, V = 0.0;
     const size_t c = at(r);
     if (r >= r0 && r <= r1) {
-      int k, j;
-      mrow(r, k, j);
-      const size_t mm = d.m2(k, j);
-      const double nu0 = nut[c] * a.nscale;
-      const double nxp = nut[c + sX] * a.nscale, nxm = nut[c - sX] * a.nscale;
-      const double nap = nut[c + sA] * a.nscale, nam = nut[c - sA] * a.nscale;
-      // right-hand side: k_adi's rows plus the NU_T term across the line
-      double gxp, gxm;  // LES metric on the two faces across
-      if (!ZS) {
-        V = fma(0.5, R[c], fma(a.tab[mm], po[c], fma(a.tab[n2 + mm], po[c + sK], a.tab[2 * n2 + mm] * po[c - sK])));
-        gxp = a.lg_r[d.m3(k + 1, j, 2)];
-        gxm = a.lg_r[d.m3(k, j, 2)];
-        V += a.temp2 * ((0.5 * (nxp + nu0)) * (gxp * (po[c + sK] - po[c])) - (0.5 * (nu0 + nxm)) * (gxm * (po[c] - po[c - sK])));
-      } else {
-        V = fma(0.5, R[c],
-                fma(a.tab[3 * n2 + mm], po[c], fma(a.tab[mm], ps[c], fma(a.tab[n2 + mm], ps[c + sJ], a.tab[2 * n2 + mm] * ps[c - sJ]))));
-        gxp = a.lg_r[d.m3(k, j + 1, 1)];
-        gxm = a.lg_r[d.m3(k, j, 1)];
-        V += a.temp2 * ((0.5 * (nxp + nu0)) * (gxp * (ps[c + sJ] - ps[c])) - (0.5 * (nxm + nu0)) * (gxm * (ps[c] - ps[c - sJ])));
-      }
-      // tridiagonal row: base coefficients plus the NU_T face terms
-      const size_t fl = d.m3(k, j, fm);
-      const size_t fu = ZS ? d.m3(k + 1, j, fm) : d.m3(k, j + 1, fm);
-      const double glo = gb[fl], gup = gb[fu];
-      const double llo = a.lg_m[fl], lup = a.lg_m[fu];
-      const double tl = (h2 * (nu0 + nam)) * llo, tu = (h2 * (nu0 + nap)) * lup;
-      L = -a.coef * glo - tl;
-      D = a.m.jac[mm] + a.coef * (gup + glo) + tu + tl;
-      U = -a.coef * gup - tu;
+      const size_t mm = ZS ? d.m2(r, line) : d.m2(line, r);
+      const double nu0 = nut[c], nap = nut[c + sA], nam = nut[c - sA];
+      const double nxp = nut[c + sX], nxm = nut[c - sX];
+      const double f0 = px[c], fxp = px[c + sX], fxm = px[c - sX];
+      if (!ZS) V = fma(0.5, R[c], fma(tb[mm], f0, fma(tb[n2 + mm], fxp, tb[2 * n2 + mm] * fxm)));
+      else V = fma(0.5, R[c], fma(tb[3 * n2 + mm], po[c], fma(tb[mm], f0, fma(tb[n2 + mm], fxp, tb[2 * n2 + mm] * fxm))));
+      const double tp = lt[5 * n2 + mm] * (nxp + nu0), tm = lt[6 * n2 + mm] * (nu0 + nxm);
+      V = fma(tp, fxp - f0, fma(-tm, f0 - fxm, V));
+      const double slo = nu0 + nam, sup = nu0 + nap;
+      const double ml = lt[3 * n2 + mm], mu = lt[4 * n2 + mm];
+      L = fma(-ml, slo, lt[mm]);
+      U = fma(-mu, sup, lt[n2 + mm]);
+      D = fma(mu, sup, fma(ml, slo, lt[2 * n2 + mm]));
     }
     for (int b = 0; b < a.bc.n; ++b) {
       const BcRow &br = a.bc.r[b];
@@ -475,22 +481,23 @@ __global__ void __launch_bounds__(128) k_adi_les(AdiArgs a) {
       B = D;
       g = V;
     } else {
-      const double am = -L / Bp;
-      B = D + am * Up;
-      g = V + am * gp;
+      const double am = -L * rBp;
+      B = fma(am, Up, D);
+      g = fma(am, gp, V);
     }
+    const double rB = __drcp_rn(B);
     a.out[c] = g;
-    a.scr_b[c] = B;
+    a.scr_b[c] = rB;
     a.scr_u[c] = U;
-    Bp = B;
+    rBp = rB;
     gp = g;
     Up = U;
   }
-  double x = gp / Bp;
+  double x = gp * rBp;
   a.out[at(nrow - 1)] = x;
   for (int r = nrow - 2; r >= 0; --r) {
     const size_t c = at(r);
-    x = (a.out[c] - a.scr_u[c] * x) / a.scr_b[c];
+    x = fma(-a.scr_u[c], x, a.out[c]) * a.scr_b[c];
     a.out[c] = x;
   }
 }
@@ -803,18 +810,26 @@ void launch_adi(Ctx &c, int field, int rk) {
     if (!c.adi_scr) {
       EK_CUDA(cudaMalloc(&c.adi_scr, sizeof(double) * 2 * np));
       c.allocs.push_back(c.adi_scr);
+      EK_CUDA(cudaMalloc(&c.adi_les_tab, sizeof(double) * 14 * n2));
+      c.allocs.push_back(c.adi_les_tab);
     }
     a.scr_b = c.adi_scr;
     a.scr_u = c.adi_scr + np;
     a.nut = c.les.nut;
-    a.nscale = (field == 0) ? 1.0 / c.p.pr : 1.0;
-    a.temp2 = c.H_BAR[rk] / 2.0;
+    // KAPPA_T = NU_T/PR for TH: the 1/PR goes into the eddy-viscosity weights
+    const double h = 0.5 * (c.H_BAR[rk] / 2.0) * ((field == 0) ? 1.0 / c.p.pr : 1.0);
     const double *l11 = (field == 2) ? c.m.g11y : (field == 3) ? c.m.g11z : c.m.g11;
     const double *l22 = (field == 2) ? c.m.g22y : (field == 3) ? c.m.g22z : c.m.g22;
+    {
+      const dim3 tg((unsigned)((d.NZ + 2 + 63) / 64), (unsigned)(d.NY + 2));
+      k_adi_les_tab<false><<<tg, 64, 0, c.stream>>>(d, c.m, c.m.g22, l22, l11, coef, h, c.adi_les_tab);
+      after_launch(c);
+      k_adi_les_tab<true><<<tg, 64, 0, c.stream>>>(d, c.m, c.m.g11, l11, l22, coef, h, c.adi_les_tab + 7 * n2);
+      after_launch(c);
+    }
     a.out = c.PHS;
     a.bc = c.bc[field][0];
-    a.lg_r = l11;
-    a.lg_m = l22;
+    a.ltab = c.adi_les_tab;
     {
       dim3 grid((d.NX + 127) / 128, a.ze - a.zs + 1);
       // algorithmic: read R, the field and NU_T, write the result
@@ -825,8 +840,7 @@ void launch_adi(Ctx &c, int field, int rk) {
     a.tab = c.adi_tab + 4 * n2;
     a.out = phi;
     a.bc = c.bc[field][1];
-    a.lg_r = l22;
-    a.lg_m = l11;
+    a.ltab = c.adi_les_tab + 7 * n2;
     {
       dim3 grid((d.NX + 127) / 128, d.NY2);
       // read R, the old field, the y-sweep result and NU_T, write the result
