@@ -379,13 +379,14 @@ __global__ void __launch_bounds__(64) k_f_xline(FastDev g, int level, int j0, in
 
 // Partitioned line solve: one block per (line, LANES problems), lanes over
 // the problems (coalesced, the layout is problem fastest), threadIdx.y over K
-// segments of the line.  The line's n rows are K segments of <= 8 interior
+// segments of the line.  The line's n rows are K segments of <= SEG interior
 // rows separated by K-1 separator rows.  Each thread row eliminates its
 // segment in registers, expressing every row as x = delta + gamma X0 -
 // beta x(next) with X0, X1 the separators before and after it; the first and
 // last rows in terms of (X0, X1) give a tridiagonal system for the
-// separators, which thread row 0 solves from shared memory, one thread per
-// problem; then every segment back-substitutes.
+// separators, solved from shared memory by parallel cyclic reduction (one
+// thread row per separator, log2(K) combine steps); then every segment
+// back-substitutes.
 // XL: x-line (along i, the periodic wrap couplings taken from the ghosts'
 // current values); else y-line (along j).
 enum { SH_A, SH_B, SH_C, SH_D, SH_YF, SH_VF, SH_WF, SH_YL, SH_VL, SH_WL, SH_S, SH_N };
