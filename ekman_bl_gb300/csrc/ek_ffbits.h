@@ -6,9 +6,11 @@
 //   d2f_bits(x)   RN(x) to float
 //   f2d_bits(f)   f widened exactly to double
 //
-// Both equal the hardware conversion bit for bit in the float normal range;
-// values below it become zero, infinities and NaN take the hardware
-// conversion.  (Splitting a double into a float-float pair, or joining one,
+// Both equal the hardware conversion bit for bit in the float normal range
+// and for infinities; values below it become zero, and a NaN stays a quiet
+// NaN of the same sign.  Nothing falls back to the hardware conversion: a
+// compiler may turn such a branch into a select and issue the conversion for
+// every value.  (Splitting a double into a float-float pair, or joining one,
 // in 64-bit integer arithmetic was measured to cost as much as the one FP64
 // add it saves, so those stay FP64.)  The header compiles as plain C++ too,
 // so the CPU tests can check it.
@@ -67,7 +69,10 @@ EK_HD float d2f_bits(double x) {
   const uint32_t uh = (uint32_t)(u >> 32), ul = (uint32_t)u;
   const uint32_t sign = uh & 0x80000000u;
   const int e = (int)((uh >> 20) & 0x7ffu);
-  if (e == 0x7ff) return (float)x;
+  if (e == 0x7ff) {  // infinity, or NaN (quiet, with the payload's top bits)
+    const bool nan = ((uh & 0xfffffu) | ul) != 0u;
+    return ffrom(sign | 0x7f800000u | (nan ? (0x400000u | ((uh & 0xfffffu) << 2) | (ul >> 30)) : 0u));
+  }
   const int fe = e - 896;
   if (fe <= 0) return ffrom(sign);
   if (fe >= 0xff) return ffrom(sign | 0x7f800000u);
@@ -83,9 +88,9 @@ EK_HD double f2d_bits(float f) {
   const uint32_t sign = u & 0x80000000u;
   const uint32_t e = (u >> 23) & 0xffu;
   if (e == 0) return dfrom((uint64_t)sign << 32);
-  if (e == 0xff) return (double)f;
   const uint32_t mant = u & 0x7fffffu;
-  return dfrom(((uint64_t)(sign | ((e + 896u) << 20) | (mant >> 3)) << 32) | ((uint64_t)(mant << 29)));
+  const uint32_t de = (e == 0xff) ? 0x7ffu : e + 896u;  // infinity and NaN keep their class and payload
+  return dfrom(((uint64_t)(sign | (de << 20) | (mant >> 3)) << 32) | ((uint64_t)(mant << 29)));
 }
 
 }  // namespace ek

@@ -233,7 +233,7 @@ struct LesState {
   bool have_metrics = false;
   bool first_time = true;       // FIRST_TIME: recompute C_DYN in every substep
   bool lowp = false;            // stresses in FP32 (fft_fp32 >= 1): the f-suffixed buffers
-  bool tab_ok = false;          // tabf matches the metrics
+  bool tab_ok = false;          // delta and tabf match the metrics
   double *nut = nullptr;        // NU_T, zero outside the velocity interior (both precisions)
   double *cdyn = nullptr;       // C_DYN(0:NZ+1, 0:NY+1), K fastest
   double *t[3] = {};            // d(U1,U2,U3)/dx, then tau_11, tau_12, tau_13 in place
@@ -242,6 +242,7 @@ struct LesState {
   double *ext[4] = {};          // flux-transform additions of U1, U2, U3, TH
   float *tf[3] = {}, *t23f = nullptr, *tthf = nullptr, *extf[4] = {}, *nutf = nullptr;
   float *tabf = nullptr;        // per-cell FP32 weights of the FP32 kernels
+  double *delta = nullptr;      // DELTA_Y(K, J), metric layout
 };
 
 struct Ctx {

@@ -73,6 +73,14 @@ __global__ void k_les_tab(Dims d, Metrics m, float *tab) {
   }
 }
 
+// DELTA_Y(K, J) = (beta DX(1) INT_JACOB(K, J))^(1/3), beta = 1
+// (les_chan.F90:343-348), once per metric set.
+__global__ void k_les_delta(Dims d, Metrics m, double dx1, double *delta) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (k > d.NZ + 1 || j > d.NY + 1) return;
+  delta[d.m2(k, j)] = pow(dx1 * m.jac[d.m2(k, j)], 1.0 / 3.0);
+}
+
 struct LesLineArgs {
   Dims d;
   Metrics m;
@@ -83,7 +91,7 @@ struct LesLineArgs {
   float *f0, *f1, *f2, *f23;      // FP32: the same
   double *nut, *cdyn;
   float *nutf;
-  double dx1;  // DX(1) = LX/NX
+  const double *delta;  // DELTA(K, J)
 };
 
 template <typename T>
@@ -176,7 +184,7 @@ __global__ void __launch_bounds__(kLineThreads) k_les_line(LesLineArgs a) {
     }
     rJ = a.tabf[kTabRJ * n2 + mm];
   }
-  const double delta64 = pow(a.dx1 * a.m.jac[mm], 1.0 / 3.0);  // (beta DX(1) INT_JACOB)^(1/3), beta = 1
+  const double delta64 = a.delta[mm];  // DELTA(K, J), k_les_delta
   const T delta = cvt<T>(delta64);
   const T d2 = delta * delta;
   const size_t base = d.ip(0, k, j), sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
@@ -336,12 +344,14 @@ __global__ void k_les_extra(LesExtraArgs a) {
   if (!vel && !sca) return;
   constexpr bool kF = sizeof(T) == 4;
   const size_t c = d.ip(i, k, j), sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
-  const size_t n2 = (size_t)d.LDM * (d.NY + 3), mm = d.m2(k, j);
+  const size_t mm = d.m2(k, j);
+  const int n2 = d.LDM * (d.NY + 3);  // plane stride of the weight tables (32-bit products)
   const T *nut;
   if constexpr (kF) nut = a.nutf; else nut = a.nut;
   auto faces = [&](int v, T *G) {
     if constexpr (kF) {
-      for (int t = 0; t < 4; ++t) G[t] = a.tabf[(kTabG12 + 4 * v + t) * n2 + mm];
+      const float *tb = a.tabf + mm;
+      for (int t = 0; t < 4; ++t) G[t] = tb[(kTabG12 + 4 * v + t) * n2];
     } else {
       const double *g = (v == 0) ? a.m.g12 : (v == 1) ? a.m.g12y : a.m.g12z;
       G[0] = g[d.m3(k + 1, j, 2)];
@@ -352,20 +362,25 @@ __global__ void k_les_extra(LesExtraArgs a) {
   };
   T G[4];
   if (vel) {
-    auto tau = [&](const T *S, int kk, int jj) {
+    // the stress at (k + dk, j + dj) through the ghost map, addressed from c
+    // with small-integer offsets (64-bit index products are emulated)
+    auto tau = [&](const T *S, int dk, int dj) {
+      int kk = k + dk, jj = j + dj;
       kk = (kk == 0) ? 1 : (kk == d.NZ + 1) ? d.NZ : kk;
       jj = (jj == 0) ? 1 : (jj == d.NY + 1) ? d.NY : jj;
       const bool in = (jj >= d.JS && jj <= d.JE && kk >= d.ZS && kk <= d.ZE);
-      return in ? S[d.ip(i, kk, jj)] : T(0.0);
+      const long long ok = (kk == k) ? 0LL : (kk > k ? (long long)sK : -(long long)sK);
+      const long long oj = (jj == j) ? 0LL : (jj > j ? (long long)sJ : -(long long)sJ);
+      const long long off = ok + oj;
+      return in ? S[(long long)c + off] : T(0.0);
     };
     auto w = [&](int t) -> T {
-      if constexpr (kF) return a.tabf[t * n2 + mm];
-      else return a.m.pg[t * n2 + mm];
+      if constexpr (kF) return a.tabf[mm + t * n2];
+      else return a.m.pg[mm + t * n2];
     };
     auto div = [&](const T *S, int g0) {
-      return fma(w(g0 + 4), tau(S, k, j - 1),
-                 fma(w(g0 + 3), tau(S, k, j + 1),
-                     fma(w(g0 + 2), tau(S, k - 1, j), fma(w(g0 + 1), tau(S, k + 1, j), w(g0) * tau(S, k, j)))));
+      return fma(w(g0 + 4), tau(S, 0, -1),
+                 fma(w(g0 + 3), tau(S, 0, 1), fma(w(g0 + 2), tau(S, -1, 0), fma(w(g0 + 1), tau(S, 1, 0), w(g0) * tau(S, 0, 0)))));
     };
     const T *U1, *U2, *U3, *t12, *t13, *t23;
     T *e1, *e2, *e3;
@@ -407,6 +422,7 @@ void les_alloc(Ctx &c) {
   };
   field(L.nut, np);
   field(L.cdyn, (size_t)c.d.NZ2 * c.d.NY2);
+  field(L.delta, (size_t)c.d.LDM * (c.d.NY + 3));
   if (L.lowp) {
     for (float *&t : L.tf) field(t, np);
     field(L.t23f, np);
@@ -432,10 +448,14 @@ void launch_les(Ctx &c, int rk) {
   LesState &L = c.les;
   const bool th = p.n_th > 0;
   const bool lowp = L.lowp;
-  if (lowp && !L.tab_ok) {
+  if (!L.tab_ok) {
     const dim3 tg((unsigned)((d.NZ + 2 + 63) / 64), (unsigned)(d.NY + 2));
-    k_les_tab<<<tg, 64, 0, c.stream>>>(d, c.m, L.tabf);
+    k_les_delta<<<tg, 64, 0, c.stream>>>(d, c.m, p.lx / p.nx, L.delta);
     after_launch(c);
+    if (lowp) {
+      k_les_tab<<<tg, 64, 0, c.stream>>>(d, c.m, L.tabf);
+      after_launch(c);
+    }
     L.tab_ok = true;
   }
   {
@@ -467,7 +487,7 @@ void launch_les(Ctx &c, int rk) {
   la.t0 = L.t[0]; la.t1 = L.t[1]; la.t2 = L.t[2]; la.t23 = L.t23;
   la.f0 = L.tf[0]; la.f1 = L.tf[1]; la.f2 = L.tf[2]; la.f23 = L.t23f;
   la.nut = L.nut; la.nutf = L.nutf; la.cdyn = L.cdyn;
-  la.dx1 = p.lx / p.nx;
+  la.delta = L.delta;
   const unsigned nlines = (unsigned)((d.ZE - d.ZS + 1) * (d.JE - d.JS + 1));
   const bool dyn = (p.time_step % 5 == 0 && rk == 1) || L.first_time;
   const double wb = lowp ? 4.0 : 8.0;  // bytes per value of the work fields

@@ -440,31 +440,33 @@ __global__ void __launch_bounds__(128) k_adi_les(AdiArgs a) {
   }
   const int nrow = ZS ? d.NZ2 : d.NY2;
   const int r0 = ZS ? a.zs : a.js, r1 = ZS ? a.ze : a.je;
-  const size_t n2 = (size_t)d.LDM * (d.NY + 3);
+  const int n2 = d.LDM * (d.NY + 3);  // plane stride of the weight tables
   const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
   const size_t sA = ZS ? sK : sJ;  // along the line
   const size_t sX = ZS ? sJ : sK;  // across: the direction of the explicit term
-  const double *nut = a.nut, *R = a.R, *po = a.phi_old, *ps = a.phs, *lt = a.ltab, *tb = a.tab;
+  const double *nut = a.nut, *R = a.R, *po = a.phi_old, *ps = a.phs;
   const double *px = ZS ? ps : po;  // field of the explicit term across the line
-  auto at = [&](int r) { return ZS ? d.ip(i, r, line) : d.ip(i, line, r); };
+  // addresses advance along the line: the point by sA, the cell by 1 (z) or LDM (y)
+  const size_t c0 = ZS ? d.ip(i, 0, line) : d.ip(i, line, 0);
+  const int m0 = ZS ? line * d.LDM : line, mstep = ZS ? 1 : d.LDM;
   double rBp = 1.0, gp = 0.0, Up = 0.0;
-  for (int r = 0; r < nrow; ++r) {
+  size_t c = c0;
+  for (int r = 0; r < nrow; ++r, c += sA) {
     double L = 0.0, D = 1.0, U = 0.0, V = 0.0;
-    const size_t c = at(r);
     if (r >= r0 && r <= r1) {
-      const size_t mm = ZS ? d.m2(r, line) : d.m2(line, r);
+      const double *lt = a.ltab + (m0 + r * mstep), *tb = a.tab + (m0 + r * mstep);
       const double nu0 = nut[c], nap = nut[c + sA], nam = nut[c - sA];
       const double nxp = nut[c + sX], nxm = nut[c - sX];
       const double f0 = px[c], fxp = px[c + sX], fxm = px[c - sX];
-      if (!ZS) V = fma(0.5, R[c], fma(tb[mm], f0, fma(tb[n2 + mm], fxp, tb[2 * n2 + mm] * fxm)));
-      else V = fma(0.5, R[c], fma(tb[3 * n2 + mm], po[c], fma(tb[mm], f0, fma(tb[n2 + mm], fxp, tb[2 * n2 + mm] * fxm))));
-      const double tp = lt[5 * n2 + mm] * (nxp + nu0), tm = lt[6 * n2 + mm] * (nu0 + nxm);
+      if (!ZS) V = fma(0.5, R[c], fma(tb[0], f0, fma(tb[n2], fxp, tb[2 * n2] * fxm)));
+      else V = fma(0.5, R[c], fma(tb[3 * n2], po[c], fma(tb[0], f0, fma(tb[n2], fxp, tb[2 * n2] * fxm))));
+      const double tp = lt[5 * n2] * (nxp + nu0), tm = lt[6 * n2] * (nu0 + nxm);
       V = fma(tp, fxp - f0, fma(-tm, f0 - fxm, V));
       const double slo = nu0 + nam, sup = nu0 + nap;
-      const double ml = lt[3 * n2 + mm], mu = lt[4 * n2 + mm];
-      L = fma(-ml, slo, lt[mm]);
-      U = fma(-mu, sup, lt[n2 + mm]);
-      D = fma(mu, sup, fma(ml, slo, lt[2 * n2 + mm]));
+      const double ml = lt[3 * n2], mu = lt[4 * n2];
+      L = fma(-ml, slo, lt[0]);
+      U = fma(-mu, sup, lt[n2]);
+      D = fma(mu, sup, fma(ml, slo, lt[2 * n2]));
     }
     for (int b = 0; b < a.bc.n; ++b) {
       const BcRow &br = a.bc.r[b];
@@ -493,10 +495,11 @@ __global__ void __launch_bounds__(128) k_adi_les(AdiArgs a) {
     gp = g;
     Up = U;
   }
+  c -= sA;  // the last row
   double x = gp * rBp;
-  a.out[at(nrow - 1)] = x;
+  a.out[c] = x;
   for (int r = nrow - 2; r >= 0; --r) {
-    const size_t c = at(r);
+    c -= sA;
     x = fma(-a.scr_u[c], x, a.out[c]) * a.scr_b[c];
     a.out[c] = x;
   }

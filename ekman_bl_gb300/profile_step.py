@@ -1,6 +1,6 @@
 """Run one RK3 step of a named workload for profiling.
 
-    python -m ekman_bl_gb300.profile_step [--workload NAME] [--warmup W] [--tol T] [--mixed]
+    python -m ekman_bl_gb300.profile_step [--workload NAME] [--warmup W] [--tol T] [--mixed] [--les]
 
 Sets up the workload, runs W warm-up steps, then exactly one RK3 step, and
 prints the number of kernel launches issued before that step and inside it,
@@ -13,7 +13,7 @@ import argparse
 import json
 
 from . import build as ekbuild
-from .duct import DuctSolver, metrics_from_grid
+from .duct import DuctSolver, les_metrics_from_grid, metrics_from_grid
 from .params import EK_MG_STOP_RELCHANGE, EK_MG_STOP_RESIDUAL, WORKLOADS, workload_setup
 
 
@@ -29,6 +29,8 @@ def main():
     ap.add_argument("--ff", action="store_true", help="float-float state-carrying transforms (ff_arith = 1)")
     ap.add_argument("--autotune", action="store_true", help="tune the line-solve layouts first, as bench.py does")
     ap.add_argument("--layout", default="", help="LANESxSEG for every line solve (e.g. 8x8) instead of tuning")
+    ap.add_argument("--les", action="store_true",
+                    help="dynamic-Smagorinsky LES on (CREATE_NEW_FLOW = .FALSE.: subgrid terms from the first step)")
     ap.add_argument("--guess", action="store_true",
                     help="train the learned initial guess on one warm-up step (50 Adam steps) and use it (needs --mixed)")
     args = ap.parse_args()
@@ -45,7 +47,11 @@ def main():
         p.mg_fast, p.fft_fp32 = 1, 1
     if args.ff:
         p.ff_arith = 1
+    if args.les:
+        p.les, p.create_new_flow = 1, 0
     s = DuctSolver(p, metrics_from_grid(p, xp, yp))
+    if p.les:
+        s.set_les_metrics(les_metrics_from_grid(p, xp, yp))
     s.upload(*state)
     if args.autotune:
         s.mg_autotune(reps=3)

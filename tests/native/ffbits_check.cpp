@@ -24,6 +24,17 @@ int main(int argc, char **argv) {
     if (ek::fbits(ek::d2f_bits(x)) != ek::fbits(h_ref)) ++bad_d2f;
     if (ek::dbits(ek::f2d_bits(h_ref)) != ek::dbits((double)h_ref)) ++bad_f2d;
   }
+  // infinities both ways; NaN stays NaN with its sign
+  for (double x : {INFINITY, -INFINITY}) {
+    if (ek::fbits(ek::d2f_bits(x)) != ek::fbits((float)x)) ++bad_d2f;
+    if (ek::dbits(ek::f2d_bits((float)x)) != ek::dbits(x)) ++bad_f2d;
+  }
+  for (double x : {NAN, -NAN}) {
+    const float f = ek::d2f_bits(x);
+    if (!std::isnan(f) || std::signbit(f) != std::signbit(x)) ++bad_d2f;
+    const double y = ek::f2d_bits((float)x);
+    if (!std::isnan(y) || std::signbit(y) != std::signbit(x)) ++bad_f2d;
+  }
   std::printf("n=%ld d2f=%ld f2d=%ld\n", n, bad_d2f, bad_f2d);
   return (bad_d2f | bad_f2d) ? 1 : 0;
 }
