@@ -472,6 +472,7 @@ void ekgpu_destroy(ek_ctx *h) {
     cudaStreamSynchronize(c.aux_stream);
     cudaStreamDestroy(c.aux_stream);
   }
+  sing_graph_reset(c);
   if (c.ev_fork) cudaEventDestroy(c.ev_fork);
   if (c.ev_join) cudaEventDestroy(c.ev_join);
   for (auto &r : c.trec) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
@@ -599,6 +600,7 @@ int ekgpu_set_metrics(ek_ctx *h, const ek_metrics *m) {
     if (!c.m.pg) c.m.pg = dalloc<double>(c, 11 * n2);
     launch_metric_tables(c);
     c.les.tab_ok = false;
+    sing_graph_reset(c);  // the multigrid plan is rebuilt below
     std::vector<double> jac(m->int_jacob, m->int_jacob + n2), g11(m->gmat_11, m->gmat_11 + 2 * n2),
         g12(m->gmat_12, m->gmat_12 + 2 * n2), g22(m->gmat_22, m->gmat_22 + 2 * n2), c22(m->cjob_22, m->cjob_22 + 2 * n2);
     // boundary rows and Thomas factors of every field, substep and direction

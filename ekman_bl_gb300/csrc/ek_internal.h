@@ -290,8 +290,15 @@ struct Ctx {
   ek_mg_stats last_stats{};
   double last_mean_cycles = 0.0;  // mixed solver: mean corrections over the kx^2 != 0 problems
   StopPoll poll;
-  cudaStream_t aux_stream = nullptr;  // the kx^2 = 0 batch runs here, beside the FP32 cycles
+  cudaStream_t aux_stream = nullptr;  // the kx^2 = 0 batch runs here, beside the FP32 cycles (high priority)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // the kx^2 = 0 batch's exact solve captured as one CUDA graph: valid for
+  // sing_ns problems in the work arrays and plan recorded in sing_key
+  cudaGraph_t sing_graph = nullptr;
+  cudaGraphExec_t sing_exec = nullptr;
+  int sing_ns = 0;
+  const void *sing_key[3] = {};
+  long long sing_launches = 0;
   // sponge_th: SPONGE_SIGMA(0:NY+1), SPONGE_SIGMA_OUT(0:NZ+1), and the
   // mode-0 mean of CU3X over the upper layer with the dynamic-branch flag
   double *sponge_sig = nullptr, *sponge_sig_out = nullptr, *sponge_red = nullptr;
@@ -403,6 +410,8 @@ void launch_spectral_rhs(Ctx &c, int rk);
 void launch_metric_tables(Ctx &c);
 void launch_face_velocity(Ctx &c);
 void launch_adi(Ctx &c, int field, int rk);
+void mg_exact_attributes();
+void sing_graph_reset(Ctx &c);
 
 // LES (ek_les.cu)
 bool les_active(const Ctx &c);

@@ -765,6 +765,15 @@ int mg_solve_exact(Ctx &c, MgWork &w, int nprob, const double *kx2_dev, ek_mg_st
   return mg_exact_stats(c, w, nprob, st);
 }
 
+// k_coarse's shared-memory limit, set once (outside any stream capture).
+void mg_exact_attributes() {
+  static bool attr_set = false;
+  if (!attr_set) {
+    EK_CUDA(cudaFuncSetAttribute(k_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_set = true;
+  }
+}
+
 // The launches of one exact solve on c.stream.  poll: stop issuing cycles
 // once every problem is done (the host waits on the stream's progress).
 void mg_exact_enqueue(Ctx &c, MgWork &w, int nprob, const double *kx2_dev, int max_cycles, bool poll) {
@@ -815,11 +824,7 @@ void mg_exact_enqueue(Ctx &c, MgWork &w, int nprob, const double *kx2_dev, int m
   off += maxph;
   A.total = off;
   const size_t smem = sizeof(double) * off;
-  static bool attr_set = false;
-  if (!attr_set) {
-    EK_CUDA(cudaFuncSetAttribute(k_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr_set = true;
-  }
+  mg_exact_attributes();
   const MgOp *ops_dev_cached = PL.ops_dev;
   const int lc = PL.lc;
   auto is_coarse = [&](const MgOp &o) {

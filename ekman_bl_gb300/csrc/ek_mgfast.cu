@@ -942,10 +942,23 @@ void mgfast_alloc(Ctx &c, int pmax) {
   }
   c.mgf_pmax = pmax;
   if (!c.aux_stream) {
-    EK_CUDA(cudaStreamCreateWithFlags(&c.aux_stream, cudaStreamNonBlocking));
+    // highest priority: the kx^2 = 0 solve is a long chain of small launches
+    // that would otherwise queue behind the FP32 cycles' full-GPU kernels
+    int lo = 0, hi = 0;
+    EK_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    EK_CUDA(cudaStreamCreateWithPriority(&c.aux_stream, cudaStreamNonBlocking, hi));
     EK_CUDA(cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming));
     EK_CUDA(cudaEventCreateWithFlags(&c.ev_join, cudaEventDisableTiming));
   }
+  mg_exact_attributes();
+}
+
+void sing_graph_reset(Ctx &c) {
+  if (c.sing_exec) cudaGraphExecDestroy(c.sing_exec);
+  if (c.sing_graph) cudaGraphDestroy(c.sing_graph);
+  c.sing_exec = nullptr;
+  c.sing_graph = nullptr;
+  c.sing_ns = 0;
 }
 
 // Solve with the mixed-precision iteration; the finest rhs must be in
@@ -994,14 +1007,47 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
     // the exact solve runs on the auxiliary stream, beside the FP32 cycles
     EK_CUDA(cudaEventRecord(c.ev_fork, s));
     EK_CUDA(cudaStreamWaitEvent(c.aux_stream, c.ev_fork, 0));
-    c.stream = c.aux_stream;
-    try {
-      mg_exact_enqueue(c, ws, ns, ws.kx2, kSingularMaxCycles, false);
-    } catch (...) {
+    if (c.timing) {
+      // the per-kernel timer records events around each launch: no graph
+      c.stream = c.aux_stream;
+      try {
+        mg_exact_enqueue(c, ws, ns, ws.kx2, kSingularMaxCycles, false);
+      } catch (...) {
+        c.stream = s;
+        throw;
+      }
       c.stream = s;
-      throw;
+    } else {
+      // its ~1,500 launches (a fixed schedule: no host polling) as one CUDA
+      // graph, captured the first time and again when the work arrays or the
+      // plan change
+      const void *key[3] = {ws.pool, PL.ops_dev, PL.lv.empty() ? nullptr : PL.lv[0].cof};
+      if (!c.sing_exec || c.sing_ns != ns || key[0] != c.sing_key[0] || key[1] != c.sing_key[1] ||
+          key[2] != c.sing_key[2]) {
+        sing_graph_reset(c);
+        const long long l0 = c.launches;
+        EK_CUDA(cudaStreamBeginCapture(c.aux_stream, cudaStreamCaptureModeThreadLocal));
+        c.stream = c.aux_stream;
+        try {
+          mg_exact_enqueue(c, ws, ns, ws.kx2, kSingularMaxCycles, false);
+        } catch (...) {
+          c.stream = s;
+          cudaGraph_t g = nullptr;
+          cudaStreamEndCapture(c.aux_stream, &g);
+          if (g) cudaGraphDestroy(g);
+          throw;
+        }
+        c.stream = s;
+        EK_CUDA(cudaStreamEndCapture(c.aux_stream, &c.sing_graph));
+        EK_CUDA(cudaGraphInstantiate(&c.sing_exec, c.sing_graph, 0));
+        c.sing_launches = c.launches - l0;
+        c.launches = l0;
+        c.sing_ns = ns;
+        for (int t = 0; t < 3; ++t) c.sing_key[t] = key[t];
+      }
+      EK_CUDA(cudaGraphLaunch(c.sing_exec, c.aux_stream));
+      c.launches += c.sing_launches;
     }
-    c.stream = s;
     EK_CUDA(cudaEventRecord(c.ev_join, c.aux_stream));
   }
   FastDev g = make_fastdev(c, nprob, kx2_dev);
