@@ -314,6 +314,7 @@ struct Ctx {
   LesState les;
   double *adi_scr = nullptr;      // LES ADI: 1/B and the upper diagonal of the eliminated rows (two fields)
   double *adi_les_tab = nullptr;  // LES ADI: per-cell row weights of the two sweeps (k_adi_les_tab)
+  float2 *adi_ff_tab = nullptr;   // LES ADI, float-float: both sweeps' weights as float pairs
   // divergence check
   double *div_part = nullptr;
   double last_div = 0.0;

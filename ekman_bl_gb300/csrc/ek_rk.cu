@@ -273,6 +273,10 @@ struct AdiArgs {
   // eliminated diagonal and the upper diagonal
   const double *nut, *ltab;
   double *scr_b, *scr_u;
+  // the float-float variant (k_adi_les_ff): NU_T in FP32 and the weights of
+  // both tables split into float-float planes (0..3 right-hand side, 4..10 row)
+  const float *nutf;
+  const float2 *ftab;
 };
 
 // Right-hand-side weights of one ADI sweep per cell (tab[t * n2 + m2(k, j)]),
@@ -502,6 +506,118 @@ __global__ void __launch_bounds__(128) k_adi_les(AdiArgs a) {
     c -= sA;
     x = fma(-a.scr_u[c], x, a.out[c]) * a.scr_b[c];
     a.out[c] = x;
+  }
+}
+
+// Float-float reciprocal: the FP32 reciprocal and one Newton step in
+// float-float (about 46 bits).
+__device__ __forceinline__ FF ff_rcp(FF b) {
+  const float r0 = __frcp_rn(b.hi);
+  float e = __fmaf_rn(-b.hi, r0, 1.0f);
+  e = __fmaf_rn(-b.lo, r0, e);
+  return ff_norm(r0, __fmul_rn(r0, e));
+}
+__device__ __forceinline__ FF ff2(float2 v) { return FF(v.x, v.y); }
+__device__ __forceinline__ FF ff1(float v) { return FF(v, 0.0f); }
+
+// The weights of one sweep's two tables split into float-float planes.
+__global__ void k_adi_ff_tab(int n2, const double *rhs_tab, const double *row_tab, float2 *ftab) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n2) return;
+  for (int p = 0; p < 11; ++p) {
+    const double v = (p < 4) ? rhs_tab[(size_t)p * n2 + m] : row_tab[(size_t)(p - 4) * n2 + m];
+    const FF f(v);
+    ftab[(size_t)p * n2 + m] = make_float2(f.hi, f.lo);
+  }
+}
+
+// k_adi_les in float-float arithmetic, for the mixed-precision method: the
+// rows, the elimination and the back substitution run on the FP32 pipe at
+// about 46 significant bits; the FP64 pipe only splits the five FP64 inputs
+// of a row and joins the result.  The eliminated rows go to the scratch
+// fields (and the modified right-hand side into the output) as float pairs
+// in the same 8-byte slots.
+template <bool ZS>
+__global__ void __launch_bounds__(128) k_adi_les_ff(AdiArgs a) {
+  const Dims &d = a.d;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int line = ZS ? (int)blockIdx.y : a.zs + (int)blockIdx.y;
+  if (i >= d.NX) return;
+  if (ZS && (line < a.js || line > a.je)) {
+    for (int k = a.zs; k <= a.ze; ++k) a.out[d.ip(i, k, line)] = a.phs[d.ip(i, k, line)];
+    return;
+  }
+  const int nrow = ZS ? d.NZ2 : d.NY2;
+  const int r0 = ZS ? a.zs : a.js, r1 = ZS ? a.ze : a.je;
+  const int n2 = d.LDM * (d.NY + 3);
+  const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
+  const size_t sA = ZS ? sK : sJ;
+  const size_t sX = ZS ? sJ : sK;
+  const float *nut = a.nutf;
+  const double *R = a.R, *po = a.phi_old, *ps = a.phs;
+  const double *px = ZS ? ps : po;
+  float2 *gout = reinterpret_cast<float2 *>(a.out);
+  float2 *sb = reinterpret_cast<float2 *>(a.scr_b), *su = reinterpret_cast<float2 *>(a.scr_u);
+  const size_t c0 = ZS ? d.ip(i, 0, line) : d.ip(i, line, 0);
+  const int m0 = ZS ? line * d.LDM : line, mstep = ZS ? 1 : d.LDM;
+  FF rBp(1.0f, 0.0f), gp(0.0f, 0.0f), Up(0.0f, 0.0f);
+  size_t c = c0;
+  for (int r = 0; r < nrow; ++r, c += sA) {
+    FF L(0.0f, 0.0f), D(1.0f, 0.0f), U(0.0f, 0.0f), V(0.0f, 0.0f);
+    if (r >= r0 && r <= r1) {
+      const float2 *t = a.ftab + (m0 + r * mstep);
+      const float nu0 = nut[c], nap = nut[c + sA], nam = nut[c - sA], nxp = nut[c + sX], nxm = nut[c - sX];
+      const FF f0(px[c]), fxp(px[c + sX]), fxm(px[c - sX]), rr(R[c]);
+      FF v = FF(0.5f * rr.hi, 0.5f * rr.lo);
+      if (!ZS) {
+        v = v + ff2(t[0]) * f0 + ff2(t[n2]) * fxp + ff2(t[2 * n2]) * fxm;
+      } else {
+        const FF p0(po[c]);
+        v = v + ff2(t[3 * n2]) * p0 + ff2(t[0]) * f0 + ff2(t[n2]) * fxp + ff2(t[2 * n2]) * fxm;
+      }
+      const FF tp = ff2(t[9 * n2]) * (ff1(nxp) + ff1(nu0)), tm = ff2(t[10 * n2]) * (ff1(nu0) + ff1(nxm));
+      V = v + tp * (fxp - f0) - tm * (f0 - fxm);
+      const FF slo = ff1(nu0) + ff1(nam), sup = ff1(nu0) + ff1(nap);
+      const FF ml = ff2(t[7 * n2]), mu = ff2(t[8 * n2]);
+      L = ff2(t[4 * n2]) - ml * slo;
+      U = ff2(t[5 * n2]) - mu * sup;
+      D = ff2(t[6 * n2]) + mu * sup + ml * slo;
+    }
+    for (int b = 0; b < a.bc.n; ++b) {
+      const BcRow &br = a.bc.r[b];
+      if (br.row != r) continue;
+      L = FF(br.l);
+      D = FF(br.dg);
+      U = FF(br.u);
+      if (br.kind == 0) V = FF(br.val);
+      else if (br.kind == 1) V = FF(ZS ? ps[d.ip(i, br.src, line)] : po[d.ip(i, line, br.src)]);
+      else V = FF(br.val * a.bcw[br.src + line]);
+    }
+    FF B, g;
+    if (r == 0) {
+      B = D;
+      g = V;
+    } else {
+      const FF am = -(L * rBp);
+      B = D + am * Up;
+      g = V + am * gp;
+    }
+    const FF rB = ff_rcp(B);
+    gout[c] = make_float2(g.hi, g.lo);
+    sb[c] = make_float2(rB.hi, rB.lo);
+    su[c] = make_float2(U.hi, U.lo);
+    rBp = rB;
+    gp = g;
+    Up = U;
+  }
+  c -= sA;
+  FF x = gp * rBp;
+  a.out[c] = (double)x;
+  for (int r = nrow - 2; r >= 0; --r) {
+    c -= sA;
+    const FF gg = ff2(gout[c]);
+    x = (gg - ff2(su[c]) * x) * ff2(sb[c]);
+    a.out[c] = (double)x;
   }
 }
 
@@ -830,25 +946,43 @@ void launch_adi(Ctx &c, int field, int rk) {
       k_adi_les_tab<true><<<tg, 64, 0, c.stream>>>(d, c.m, c.m.g11, l11, l22, coef, h, c.adi_les_tab + 7 * n2);
       after_launch(c);
     }
+    // the mixed-precision method (FP32 LES kernels) eliminates in float-float
+    const bool ff = c.les.lowp;
+    if (ff) {
+      if (!c.adi_ff_tab) {
+        EK_CUDA(cudaMalloc(&c.adi_ff_tab, sizeof(float2) * 22 * n2));
+        c.allocs.push_back(c.adi_ff_tab);
+      }
+      const unsigned nb = (unsigned)((n2 + 127) / 128);
+      k_adi_ff_tab<<<nb, 128, 0, c.stream>>>((int)n2, c.adi_tab, c.adi_les_tab, c.adi_ff_tab);
+      after_launch(c);
+      k_adi_ff_tab<<<nb, 128, 0, c.stream>>>((int)n2, c.adi_tab + 4 * n2, c.adi_les_tab + 7 * n2, c.adi_ff_tab + 11 * n2);
+      after_launch(c);
+      a.nutf = c.les.nutf;
+    }
     a.out = c.PHS;
     a.bc = c.bc[field][0];
     a.ltab = c.adi_les_tab;
+    a.ftab = c.adi_ff_tab;
     {
       dim3 grid((d.NX + 127) / 128, a.ze - a.zs + 1);
       // algorithmic: read R, the field and NU_T, write the result
       KScope ks(c, KC_ADI_Y, 32.0 * d.NX * d.NY2 * (a.ze - a.zs + 1));
-      k_adi_les<false><<<grid, 128, 0, c.stream>>>(a);
+      if (ff) k_adi_les_ff<false><<<grid, 128, 0, c.stream>>>(a);
+      else k_adi_les<false><<<grid, 128, 0, c.stream>>>(a);
       after_launch(c);
     }
     a.tab = c.adi_tab + 4 * n2;
     a.out = phi;
     a.bc = c.bc[field][1];
     a.ltab = c.adi_les_tab + 7 * n2;
+    a.ftab = c.adi_ff_tab ? c.adi_ff_tab + 11 * n2 : nullptr;
     {
       dim3 grid((d.NX + 127) / 128, d.NY2);
       // read R, the old field, the y-sweep result and NU_T, write the result
       KScope ks(c, KC_ADI_Z, 40.0 * d.NX * d.NZ2 * (a.je - a.js + 1));
-      k_adi_les<true><<<grid, 128, 0, c.stream>>>(a);
+      if (ff) k_adi_les_ff<true><<<grid, 128, 0, c.stream>>>(a);
+      else k_adi_les<true><<<grid, 128, 0, c.stream>>>(a);
       after_launch(c);
     }
     return;
