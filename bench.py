@@ -44,6 +44,18 @@ MG_TOL = 1e-8
 METRIC = "RK3 steps/s and Poisson solves/s at 1e-8 residual: learned+batched vs plain, 1 GB300"
 
 
+def profiled_traffic(kernel_class: str):
+    """DRAM bytes per launch of a kernel class from its committed ncu summary
+    (profiles/<class>_traffic_512x385x257.md), or (None, None)."""
+    import re
+    path = os.path.join(ROOT, "profiles", f"{kernel_class}_traffic_512x385x257.md")
+    try:
+        m = re.search(r"traffic_bytes_per_launch:\s*(\d+)", open(path).read())
+        return (int(m.group(1)), os.path.relpath(path, ROOT)) if m else (None, None)
+    except OSError:
+        return None, None
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -402,9 +414,10 @@ def run_gpu(args):
         roof = None
         if dcnt > 0 and dms > 0:
             achieved = dbytes / (dms / 1000.0) / 1e9
+            traffic, tsrc = profiled_traffic(name)
             roof = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                    "traffic": None, "algorithmic_bytes_per_launch": int(dbytes / dcnt),
+                    "traffic": traffic, "traffic_source": tsrc, "algorithmic_bytes_per_launch": int(dbytes / dcnt),
                     "avg_launch_us": round(dms * 1000.0 / dcnt, 3), "launches_per_step": dcnt,
                     "share_of_step": round(dms / ktot, 4)}
         per_class_gbs = {k: round(v[2] / (v[0] / 1000.0) / 1e9, 1) for k, v in kt.items()
