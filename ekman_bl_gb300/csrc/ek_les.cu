@@ -362,25 +362,32 @@ __global__ void k_les_extra(LesExtraArgs a) {
   };
   T G[4];
   if (vel) {
-    // the stress at (k + dk, j + dj) through the ghost map, addressed from c
-    // with small-integer offsets (64-bit index products are emulated)
-    auto tau = [&](const T *S, int dk, int dj) {
-      int kk = k + dk, jj = j + dj;
-      kk = (kk == 0) ? 1 : (kk == d.NZ + 1) ? d.NZ : kk;
-      jj = (jj == 0) ? 1 : (jj == d.NY + 1) ? d.NY : jj;
-      const bool in = (jj >= d.JS && jj <= d.JE && kk >= d.ZS && kk <= d.ZE);
-      const long long ok = (kk == k) ? 0LL : (kk > k ? (long long)sK : -(long long)sK);
-      const long long oj = (jj == j) ? 0LL : (jj > j ? (long long)sJ : -(long long)sJ);
-      const long long off = ok + oj;
-      return in ? S[(long long)c + off] : T(0.0);
-    };
+    // the stresses at (k, j) and its four neighbours through the ghost map:
+    // an offset from c and a flag per point, the same for the whole block row
+    long long off[5];
+    bool in[5];
+    {
+      const int dk[5] = {0, 1, -1, 0, 0}, dj[5] = {0, 0, 0, 1, -1};
+#pragma unroll
+      for (int n = 0; n < 5; ++n) {
+        int kk = k + dk[n], jj = j + dj[n];
+        kk = (kk == 0) ? 1 : (kk == d.NZ + 1) ? d.NZ : kk;
+        jj = (jj == 0) ? 1 : (jj == d.NY + 1) ? d.NY : jj;
+        in[n] = (jj >= d.JS && jj <= d.JE && kk >= d.ZS && kk <= d.ZE);
+        const long long ok = (kk == k) ? 0LL : (kk > k ? (long long)sK : -(long long)sK);
+        const long long oj = (jj == j) ? 0LL : (jj > j ? (long long)sJ : -(long long)sJ);
+        off[n] = ok + oj;
+      }
+    }
+    auto tau = [&](const T *S, int n) { return in[n] ? S[(long long)c + off[n]] : T(0.0); };
     auto w = [&](int t) -> T {
       if constexpr (kF) return a.tabf[mm + t * n2];
       else return a.m.pg[mm + t * n2];
     };
+    // w0 X + w1 X(k+1) + w2 X(k-1) + w3 X(j+1) + w4 X(j-1)
     auto div = [&](const T *S, int g0) {
-      return fma(w(g0 + 4), tau(S, 0, -1),
-                 fma(w(g0 + 3), tau(S, 0, 1), fma(w(g0 + 2), tau(S, -1, 0), fma(w(g0 + 1), tau(S, 1, 0), w(g0) * tau(S, 0, 0)))));
+      return fma(w(g0 + 4), tau(S, 4),
+                 fma(w(g0 + 3), tau(S, 3), fma(w(g0 + 2), tau(S, 2), fma(w(g0 + 1), tau(S, 1), w(g0) * tau(S, 0)))));
     };
     const T *U1, *U2, *U3, *t12, *t13, *t23;
     T *e1, *e2, *e3;

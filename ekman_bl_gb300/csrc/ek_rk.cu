@@ -307,90 +307,6 @@ __global__ void k_adi_tab(Dims d, Metrics m, double coef, double *tab) {
   }
 }
 
-// CN-ADI line solves: a block owns 32 consecutive x points (lanes) of one
-// line.  Its kAdiWarps warps build the right-hand side of every row in
-// parallel straight into shared memory, together with the line's Thomas
-// factors (precomputed on the host, I-independent); then warp 0 runs the
-// forward elimination and back substitution (THOMAS_REAL) from shared
-// memory, one lane per x point.
-//
-// y sweep (ZS = false), duct.F90:1640-1739 for U1 (TH 1334-1433, U2
-// 1877-1980, U3 2137-2233): R' = S/2 + J phi + coef d_zeta(G11 d_zeta phi),
-// S = R - J phi; the solution of each (I,K) line goes to phs.
-// z sweep (ZS = true), duct.F90:1741-1854 for U1 (TH 1437-1600, U2
-// 1983-2115, U3 2257-2392): R'' = S/2 + J phi* + coef d_eta(G22 d_eta phi*);
-// the solution of each (I,J) line goes into the field; rows J outside the
-// solved range take the y-sweep values.
-constexpr int kAdiWarps = 8;
-template <bool ZS>
-__global__ void __launch_bounds__(32 * kAdiWarps) k_adi(AdiArgs a) {
-  extern __shared__ double sm[];
-  const Dims &d = a.d;
-  const int lane = threadIdx.x, w = threadIdx.y;
-  const int i = blockIdx.x * 32 + lane;
-  const int line = ZS ? (int)blockIdx.y : a.zs + (int)blockIdx.y;
-  const int nrow = ZS ? d.NZ2 : d.NY2;
-  const bool act = (i < d.NX);
-  if (ZS && (line < a.js || line > a.je)) {
-    if (act)
-      for (int k = a.zs + w; k <= a.ze; k += kAdiWarps) a.out[d.ip(i, k, line)] = a.phs[d.ip(i, k, line)];
-    return;
-  }
-  double *g = sm;  // [row][lane]
-  double *sfa = sm + (size_t)nrow * 32, *sfib = sfa + nrow, *sfu = sfib + nrow;
-  {
-    const double *fa = a.fa + (size_t)line * nrow, *fib = a.fib + (size_t)line * nrow, *fu = a.fu + (size_t)line * nrow;
-    for (int r = w * 32 + lane; r < nrow; r += 32 * kAdiWarps) {
-      sfa[r] = fa[r];
-      sfib[r] = fib[r];
-      sfu[r] = fu[r];
-    }
-  }
-  const int r0 = ZS ? a.zs : a.js, r1 = ZS ? a.ze : a.je;
-  for (int r = w; r < nrow; r += kAdiWarps) {
-    double v = 0.0;
-    if (act) {
-      if (r >= r0 && r <= r1) {
-        const size_t n2 = (size_t)d.LDM * (d.NY + 3);
-        if (!ZS) {
-          const int k = line;
-          const size_t c = d.ip(i, k, r), sK = d.LDX, mm = d.m2(k, r);
-          v = fma(0.5, a.R[c],
-                  fma(a.tab[mm], a.phi_old[c], fma(a.tab[n2 + mm], a.phi_old[c + sK], a.tab[2 * n2 + mm] * a.phi_old[c - sK])));
-        } else {
-          const int j = line;
-          const size_t c = d.ip(i, r, j), sJ = (size_t)d.LDX * d.NZ2, mm = d.m2(r, j);
-          v = fma(0.5, a.R[c],
-                  fma(a.tab[3 * n2 + mm], a.phi_old[c],
-                      fma(a.tab[mm], a.phs[c], fma(a.tab[n2 + mm], a.phs[c + sJ], a.tab[2 * n2 + mm] * a.phs[c - sJ]))));
-        }
-      }
-      for (int b = 0; b < a.bc.n; ++b) {
-        const BcRow &br = a.bc.r[b];
-        if (br.row != r) continue;
-        if (br.kind == 0) v = br.val;
-        else if (br.kind == 1) v = ZS ? a.phs[d.ip(i, br.src, line)] : a.phi_old[d.ip(i, line, br.src)];
-        else v = br.val * a.bcw[br.src + line];
-      }
-    }
-    g[r * 32 + lane] = v;
-  }
-  __syncthreads();
-  if (w != 0 || !act) return;
-  auto at = [&](int r) { return ZS ? d.ip(i, r, line) : d.ip(i, line, r); };
-  double prev = g[lane];
-  for (int r = 1; r < nrow; ++r) {
-    prev = g[r * 32 + lane] + sfa[r] * prev;
-    g[r * 32 + lane] = prev;
-  }
-  double x = prev * sfib[nrow - 1];
-  a.out[at(nrow - 1)] = x;
-  for (int r = nrow - 2; r >= 0; --r) {
-    x = (g[r * 32 + lane] - sfu[r] * x) * sfib[r];
-    a.out[at(r)] = x;
-  }
-}
-
 // Per-cell weights of one LES ADI sweep (seven planes, ltab[t * n2 + m2(k, j)]):
 //   t0 = -c Gb(lo), t1 = -c Gb(up), t2 = J + c (Gb(up) + Gb(lo))   the plain row
 //   t3 = h Gm(lo),  t4 = h Gm(up)     eddy-viscosity face weights of the row
@@ -618,6 +534,71 @@ __global__ void __launch_bounds__(128) k_adi_les_ff(AdiArgs a) {
     const FF gg = ff2(gout[c]);
     x = (gg - ff2(su[c]) * x) * ff2(sb[c]);
     a.out[c] = (double)x;
+  }
+}
+
+// CN-ADI line solves, one thread per system (one x point of one line).
+// y sweep (ZS = false), duct.F90:1640-1739 for U1 (TH 1334-1433, U2
+// 1877-1980, U3 2137-2233): R' = S/2 + J phi + coef d_zeta(G11 d_zeta phi),
+// S = R - J phi; the solution of each (I,K) line goes to phs.
+// z sweep (ZS = true), duct.F90:1741-1854 for U1 (TH 1437-1600, U2
+// 1983-2115, U3 2257-2392): R'' = S/2 + J phi* + coef d_eta(G22 d_eta phi*);
+// the solution of each (I,J) line goes into the field; rows J outside the
+// solved range take the y-sweep values.
+// The thread forms each row's right-hand side from the per-cell weights
+// (k_adi_tab), runs the forward elimination of THOMAS_REAL with the line's
+// host factors (broadcast loads: a block's threads share the line) and parks
+// the modified right-hand side in the output, then back-substitutes.  (A
+// block of eight warps that built the rows in shared memory while one warp
+// ran the recurrences took twice as long: seven warps idled through the
+// sequential part.)
+template <bool ZS>
+__global__ void __launch_bounds__(128) k_adi_seq(AdiArgs a) {
+  const Dims &d = a.d;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int line = ZS ? (int)blockIdx.y : a.zs + (int)blockIdx.y;
+  if (i >= d.NX) return;
+  if (ZS && (line < a.js || line > a.je)) {
+    for (int k = a.zs; k <= a.ze; ++k) a.out[d.ip(i, k, line)] = a.phs[d.ip(i, k, line)];
+    return;
+  }
+  const int nrow = ZS ? d.NZ2 : d.NY2;
+  const int r0 = ZS ? a.zs : a.js, r1 = ZS ? a.ze : a.je;
+  const int n2 = d.LDM * (d.NY + 3);
+  const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
+  const size_t sA = ZS ? sK : sJ;
+  const size_t sX = ZS ? sJ : sK;
+  const double *R = a.R, *po = a.phi_old, *ps = a.phs;
+  const double *px = ZS ? ps : po;
+  const double *fa = a.fa + (size_t)line * nrow, *fib = a.fib + (size_t)line * nrow, *fu = a.fu + (size_t)line * nrow;
+  const size_t c0 = ZS ? d.ip(i, 0, line) : d.ip(i, line, 0);
+  const int m0 = ZS ? line * d.LDM : line, mstep = ZS ? 1 : d.LDM;
+  double prev = 0.0;
+  size_t c = c0;
+  for (int r = 0; r < nrow; ++r, c += sA) {
+    double v = 0.0;
+    if (r >= r0 && r <= r1) {
+      const double *tb = a.tab + (m0 + r * mstep);
+      if (!ZS) v = fma(0.5, R[c], fma(tb[0], px[c], fma(tb[n2], px[c + sX], tb[2 * n2] * px[c - sX])));
+      else v = fma(0.5, R[c], fma(tb[3 * n2], po[c], fma(tb[0], px[c], fma(tb[n2], px[c + sX], tb[2 * n2] * px[c - sX]))));
+    }
+    for (int b = 0; b < a.bc.n; ++b) {
+      const BcRow &br = a.bc.r[b];
+      if (br.row != r) continue;
+      if (br.kind == 0) v = br.val;
+      else if (br.kind == 1) v = ZS ? ps[d.ip(i, br.src, line)] : po[d.ip(i, line, br.src)];
+      else v = br.val * a.bcw[br.src + line];
+    }
+    prev = (r == 0) ? v : v + fa[r] * prev;
+    a.out[c] = prev;
+  }
+  c -= sA;
+  double x = prev * fib[nrow - 1];
+  a.out[c] = x;
+  for (int r = nrow - 2; r >= 0; --r) {
+    c -= sA;
+    x = (a.out[c] - fu[r] * x) * fib[r];
+    a.out[c] = x;
   }
 }
 
@@ -994,10 +975,8 @@ void launch_adi(Ctx &c, int field, int rk) {
   a.fu = c.adi[field][rk][0].u;
   a.bc = c.bc[field][0];
   {
-    const size_t smem = sizeof(double) * (32 + 3) * d.NY2;
-    dim3 grid((d.NX + 31) / 32, a.ze - a.zs + 1);
     KScope ks(c, KC_ADI_Y, 24.0 * d.NX * d.NY2 * (a.ze - a.zs + 1));
-    k_adi<false><<<grid, dim3(32, kAdiWarps), smem, c.stream>>>(a);
+    k_adi_seq<false><<<dim3((d.NX + 127) / 128, a.ze - a.zs + 1), 128, 0, c.stream>>>(a);
     after_launch(c);
   }
   // z sweep
@@ -1008,10 +987,8 @@ void launch_adi(Ctx &c, int field, int rk) {
   a.fu = c.adi[field][rk][1].u;
   a.bc = c.bc[field][1];
   {
-    const size_t smem = sizeof(double) * (32 + 3) * d.NZ2;
-    dim3 grid((d.NX + 31) / 32, d.NY2);
     KScope ks(c, KC_ADI_Z, 32.0 * d.NX * d.NZ2 * (a.je - a.js + 1));
-    k_adi<true><<<grid, dim3(32, kAdiWarps), smem, c.stream>>>(a);
+    k_adi_seq<true><<<dim3((d.NX + 127) / 128, d.NY2), 128, 0, c.stream>>>(a);
     after_launch(c);
   }
 }
@@ -1081,14 +1058,6 @@ int finish_divergence(Ctx &c, double *div_out) {
 }  // namespace ek
 
 namespace ek {
-// The ADI kernels keep one line of right-hand sides per thread in shared
-// memory ((32 + 3) x (NY+2) doubles), more than the default 48 KB for
-// tall grids.
-void rk_init_attributes() {
-  static bool done = false;
-  if (done) return;
-  EK_CUDA(cudaFuncSetAttribute(k_adi<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  EK_CUDA(cudaFuncSetAttribute(k_adi<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  done = true;
-}
+// The RK kernels use the default shared-memory limit.
+void rk_init_attributes() {}
 }  // namespace ek

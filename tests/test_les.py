@@ -273,3 +273,27 @@ def test_les_mixed_precision_tracks_oracle():
     ng, _ = g.les_state()
     no, _ = o.les_state()
     assert rel_l2(ng, no) < 1e-4
+
+
+@pytest.mark.gpu
+def test_les_with_sponge_and_variable_dt():
+    """LES together with sponge_th (SPONGE_TYPE 2, its CU2X reset at
+    TIME_STEP 2) and VARIABLE_DT (the CFL step after each RK_STEP 3), on the
+    non-orthogonal grid, against the oracle over three steps."""
+    p, xp, yp, st = les_case("sheared")
+    p.sponge_type, p.ny_s_t = 2, p.ny // 2
+    p.nz_s_r = p.nz - 3
+    p.nz_s_l = p.nz + 1 - p.nz_s_r
+    p.save_stats_int = 4
+    p.variable_dt, p.update_dt, p.cfl, p.delta_t_set = 1, 1, 2e-3, 1.0
+    sg, so = ekref.sponge_profiles(p, xp, yp)
+    g, o = gpu_for(p, xp, yp, st), oracle_for(p, xp, yp, st)
+    g.set_sponge(sg, so)
+    o.set_sponge(sg, so)
+    for n in range(3):
+        g.step(1)
+        o.step(1)
+        tg, ng, dg = g.get_time()
+        to, no, do = o.get_time()
+        assert ng == no and abs(dg - do) <= 1e-12 * do, n
+        compare(g, o, 1e-10, f"step {n + 1}")
