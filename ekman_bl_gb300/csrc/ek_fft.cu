@@ -117,11 +117,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const Dims &d = fc.d;
   const int nk = args.k1 - args.k0 + 1;
-  const long nlines = (long)nk * (args.j1 - args.j0 + 1);
-  const long line = (long)blockIdx.x * kWarpsPerBlock + warp;
-  if (line >= nlines) return;
-  const int k = args.k0 + (int)(line % nk);
-  const int j = args.j0 + (int)(line / nk);
+  // grid (ceil(nk / kWarpsPerBlock), nj): no index division (a 64-bit one
+  // is a long integer sequence with FP64 steps)
+  const int kw = (int)blockIdx.x * kWarpsPerBlock + warp;
+  if (kw >= nk) return;
+  const int k = args.k0 + kw;
+  const int j = args.j0 + (int)blockIdx.y;
   const int NX = d.NX, M = fc.M;
   V *z = smem_c + (size_t)warp * M;
   T *zr = reinterpret_cast<T *>(z);
@@ -244,11 +245,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const Dims &d = fc.d;
   const int nk = args.k1 - args.k0 + 1;
-  const long nlines = (long)nk * (args.j1 - args.j0 + 1);
-  const long line = (long)blockIdx.x * kWarpsPerBlock + warp;
-  if (line >= nlines) return;
-  const int k = args.k0 + (int)(line % nk);
-  const int j = args.j0 + (int)(line / nk);
+  // grid (ceil(nk / kWarpsPerBlock), nj): no index division (a 64-bit one
+  // is a long integer sequence with FP64 steps)
+  const int kw = (int)blockIdx.x * kWarpsPerBlock + warp;
+  if (kw >= nk) return;
+  const int k = args.k0 + kw;
+  const int j = args.j0 + (int)blockIdx.y;
   const int M = fc.M, NKX = d.NKX;
   V *z = smem_c + (size_t)warp * M;
   const cplx_t *src = args.src + d.ic(0, k, j);
@@ -332,7 +334,7 @@ void launch_r2c(Ctx &c, const R2cArgs &a) {
   const FftConst fc = make_const(c);
   const long nlines = (long)(a.k1 - a.k0 + 1) * (a.j1 - a.j0 + 1);
   if (nlines <= 0) return;
-  const unsigned grid = (unsigned)((nlines + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  const dim3 grid((unsigned)((a.k1 - a.k0 + 1 + kWarpsPerBlock - 1) / kWarpsPerBlock), (unsigned)(a.j1 - a.j0 + 1));
   const size_t smem = sizeof(double2) * fc.M * kWarpsPerBlock;
   const int nops = (a.pro == PRO_LOAD) ? 1 : (a.pro == PRO_PROD) ? 2 : 3;
   const double epi = (a.epi == EPI_STORE) ? 16.0 * (c.d.NX2P + 1) : 32.0 * (c.d.NKX + 1);
@@ -347,7 +349,7 @@ void launch_c2r(Ctx &c, const C2rArgs &a) {
   const FftConst fc = make_const(c);
   const long nlines = (long)(a.k1 - a.k0 + 1) * (a.j1 - a.j0 + 1);
   if (nlines <= 0) return;
-  const unsigned grid = (unsigned)((nlines + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  const dim3 grid((unsigned)((a.k1 - a.k0 + 1 + kWarpsPerBlock - 1) / kWarpsPerBlock), (unsigned)(a.j1 - a.j0 + 1));
   const size_t smem = sizeof(double2) * fc.M * kWarpsPerBlock;
   KScope ks(c, KC_C2R, nlines * (16.0 * (c.d.NKX + 1) * (a.src2 ? 2 : 1) + 8.0 * (c.d.NX + 2)));
   if (fft_lowp(c, a.lowp)) k_c2r<float><<<grid, 32 * kWarpsPerBlock, smem / 2, c.stream>>>(fc, a);
@@ -453,7 +455,7 @@ int run_standalone(bool forward, int nx, int nkx, long nlines, const double *in,
                    const double2 *tw) {
   if (nlines == 0) return EK_OK;
   const FftConst fc = standalone_const(nx, nkx, nlines, tw);
-  const unsigned grid = (unsigned)((nlines + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  const dim3 grid((unsigned)((nlines + kWarpsPerBlock - 1) / kWarpsPerBlock), 1u);
   const size_t smem = sizeof(double2) * fc.M * kWarpsPerBlock;
   if (forward) {
     R2cArgs a{};
