@@ -15,9 +15,10 @@ flush is needed between steps.  For N > 1 each rank
 runs an independent replica on its own GPU (the path does not shard) and
 the value is the sum over ranks.
 
-The line also carries "les": the LES case 1024 x 513 x 385 (dynamic
-Smagorinsky, les_chan / les_chan_th) timed over one C_DYN period of five
-steps with the same mixed-precision method, the plain FP64 path beside it,
+The line also carries "les": the LES case 1024 x 513 x 385 at Re = 2000,
+Ri = 0.15, dt = 1.5e-4 (dynamic Smagorinsky, les_chan / les_chan_th),
+timed over one C_DYN period of five steps with the same mixed-precision
+method, the plain FP64 path beside it,
 the LES kernels' share and roofline, and one oracle LES substep on the host
 cores (skip with --no-les).
 """

@@ -192,9 +192,11 @@ WORKLOADS = {
                                         1e-10, 0.01, 64.0, 0.35),
     "ekman_strat_512x385x257": Workload("ekman_strat_512x385x257", 512, 385, 257, 1000.0, 0.7, 0.1, 3.0e-4, 200,
                                         1e-8, 0.01, 128.0, 0.3),
-    # the LES case: twice the spanwise and about 1.3 and 1.5 times the vertical
-    # and streamwise points of the large stratified case at the same cell sizes
-    "ekman_les_1024x513x385": Workload("ekman_les_1024x513x385", 1024, 513, 385, 1000.0, 0.7, 0.1, 3.0e-4, 500,
+    # the LES case: Re = 2000, Ri = 0.15; twice the spanwise and about 1.3 and
+    # 1.5 times the vertical and streamwise points of the large stratified
+    # case at the same cell sizes in Ekman depths, and half its time step (the
+    # depth halves with Re, so the advective CFL stays at ~0.6)
+    "ekman_les_1024x513x385": Workload("ekman_les_1024x513x385", 1024, 513, 385, 2000.0, 0.7, 0.15, 1.5e-4, 500,
                                        1e-8, 0.01, 256.0, 0.3, les=1),
 }
 
