@@ -20,7 +20,10 @@ Ri = 0.15, dt = 1.5e-4 (dynamic Smagorinsky, les_chan / les_chan_th),
 timed over one C_DYN period of five steps with the same mixed-precision
 method, the plain FP64 path beside it,
 the LES kernels' share and roofline, and one oracle LES substep on the host
-cores (skip with --no-les).
+cores (skip with --no-les), and "ensemble": eight runs on uneven seeded grids
+(64..256 points per side) stepped together on the GPU, against the same
+members one after another and the plain path's members (skip with
+--no-ensemble).
 """
 from __future__ import annotations
 
@@ -124,7 +127,9 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------
-def setup_solver(device_index: int, mg_fast: int = 1, fft_fp32: int = 1, workload: str = WORKLOAD):
+def setup_solver(device_index: int, mg_fast: int = 1, fft_fp32: int = 1, workload=WORKLOAD):
+    """A solver of a named workload (or a Workload) on its own stream, with
+    the initial field projected; returns (w, p, xp, yp, state, solver, stream)."""
     import torch
 
     from ekman_bl_gb300 import build as ekbuild
@@ -133,7 +138,7 @@ def setup_solver(device_index: int, mg_fast: int = 1, fft_fp32: int = 1, workloa
 
     ekbuild.build()
     torch.cuda.set_device(device_index)
-    w = WORKLOADS[workload]
+    w = WORKLOADS[workload] if isinstance(workload, str) else workload
     w.mg_tol = MG_TOL
     p, xp, yp, state = workload_setup(w, EK_MG_STOP_RESIDUAL)
     p.mg_fast = mg_fast
@@ -321,6 +326,80 @@ def run_les(args, local):
     return out
 
 
+ENS_STEPS = 5
+
+
+def run_ensemble(args, local):
+    """The ensemble of eight stratified Ekman-layer runs on uneven grids
+    (NX in {64, 128, 256}, NY+2 and NZ+2 drawn from [64, 256] with a fixed
+    seed and rounded up to MUDPACK form), each with its own parameters,
+    metrics and state.  Times ENS_STEPS RK3 steps of every member with the
+    mixed-precision method: all members together (ekgpu_ensemble_step, one
+    stream and host thread per member), the same members one after another,
+    and the plain FP64 path's members together.  Member streams run
+    concurrently, so the times are host wall clock between device-wide
+    synchronisations."""
+    import torch
+
+    from ekman_bl_gb300.duct import ensemble_step
+    from ekman_bl_gb300.params import ensemble_workloads
+
+    def members(mixed):
+        out = []
+        for _, w in ensemble_workloads():
+            w.mg_tol = MG_TOL
+            out.append(setup_solver(local, mixed, mixed, workload=w)[5])
+        return out
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    ens = ensemble_workloads()
+    pts = [w.nx * w.ny2 * w.nz2 for _, w in ens]
+    ms_ = members(1)
+    ensemble_step(ms_, 1)  # warm-up (first solves set up their pinned stop flags)
+    n0 = sum(m.launch_count() for m in ms_)
+    sampler = ClockSampler(local)
+    sampler.__enter__()
+    try:
+        t_together = timed(lambda: ensemble_step(ms_, ENS_STEPS))
+    finally:
+        sampler.__exit__(None, None, None)
+    launches = sum(m.launch_count() for m in ms_) - n0
+    t_alone = timed(lambda: [m.step(ENS_STEPS) for m in ms_])
+    cyc = max(m.mg_stats()["max_cycles"] for m in ms_)
+    divs = [m.divergence() for m in ms_]
+    for m in ms_:
+        m.close()
+    pl = members(0)
+    ensemble_step(pl, 1)
+    t_plain = timed(lambda: ensemble_step(pl, ENS_STEPS))
+    for m in pl:
+        m.close()
+    nm = len(ens)
+    rate = nm * ENS_STEPS / t_together
+    return {"members": [w.name for _, w in ens], "drawn_ny2_nz2": [list(d) for d, _ in ens],
+            "points_total": int(sum(pts)), "seed": 0,
+            "method": "mixed precision as the main line, default line-solve layouts, every member on its own "
+                      "stream and host thread (ekgpu_ensemble_step)",
+            "value": round(rate, 3), "unit": "member RK3 steps/s", "steps_per_member": ENS_STEPS,
+            "ms_per_ensemble_step": round(t_together * 1000.0 / ENS_STEPS, 3),
+            "grid_point_steps_per_s": round(sum(pts) * ENS_STEPS / t_together, 1),
+            "one_after_another": {"value": round(nm * ENS_STEPS / t_alone, 3),
+                                  "ms_per_ensemble_step": round(t_alone * 1000.0 / ENS_STEPS, 3)},
+            "speedup_vs_one_after_another": round(t_alone / t_together, 3),
+            "plain_together": {"value": round(nm * ENS_STEPS / t_plain, 3),
+                               "ms_per_ensemble_step": round(t_plain * 1000.0 / ENS_STEPS, 3)},
+            "speedup_vs_plain": round(t_plain / t_together, 3),
+            "mg_corrections_per_substep_max": cyc, "max_divergence": max(divs),
+            "gpu_launches": int(launches), "clocks": sampler.summary(),
+            "timing": "host wall clock between device synchronisations (members run on 8 streams)"}
+
+
 def les_cpu_baseline():
     """The oracle's LES path on the host cores, bounded sample: one substep
     (RK_STEP 1 of the FIRST_TIME step, C_DYN recomputed) of the LES case."""
@@ -405,6 +484,7 @@ def run_gpu(args):
     plain_pois_ms, plain_pst, _ = time_poisson(plain, pstream, p)
     plain.close()
     les = None if args.no_les else run_les(args, local)
+    ensemble = None if args.no_ensemble else run_ensemble(args, local)
 
     result = None
     if rank == 0:
@@ -469,6 +549,7 @@ def run_gpu(args):
             "roofline": roof,
             "learned": learned,
             "les": les,
+            "ensemble": ensemble,
         }
         if world == 1 and not args.no_cpu_baseline:
             result["cpu_baseline"] = cpu_baseline(args)
@@ -550,6 +631,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip training and timing the learned guess")
     ap.add_argument("--no-les", action="store_true", help="skip the LES case")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the uneven-grid ensemble")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gpu":
         args.warmup = 3

@@ -7,6 +7,9 @@
 #include <cstring>
 #include <memory>
 #include <new>
+#include <system_error>
+#include <thread>
+#include <vector>
 
 #include "ek_internal.h"
 #include "ek_unet.h"
@@ -745,6 +748,45 @@ int ekgpu_step(ek_ctx *h, int nsteps) {
     }
     return (int)EK_OK;
   });
+}
+
+int ekgpu_ensemble_step(ek_ctx *const *members, int n, int nsteps, int *status) {
+  if (!members || n < 1 || nsteps < 0) return EK_ERR_ARG;
+  std::vector<ek_ctx *> m(members, members + n);
+  for (int i = 0; i < n; ++i)
+    if (!m[i]) return EK_ERR_ARG;
+  std::vector<ek_ctx *> sorted(m);
+  std::sort(sorted.begin(), sorted.end());
+  if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end()) return EK_ERR_ARG;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return EK_ERR_CUDA;
+  std::vector<int> st(n, EK_OK);
+  // member 0 on the calling thread, the others on their own threads (every
+  // context owns its stream, buffers and pinned stop flags, so the members
+  // share nothing but the device)
+  std::vector<std::thread> th;
+  th.reserve(n - 1);
+  for (int i = 1; i < n; ++i) {
+    try {
+      th.emplace_back([&, i] {
+        if (cudaSetDevice(dev) != cudaSuccess) {
+          st[i] = fail(m[i]->c, EK_ERR_CUDA, "ensemble: cudaSetDevice failed");
+          return;
+        }
+        st[i] = ekgpu_step(m[i], nsteps);
+      });
+    } catch (const std::system_error &) {
+      st[i] = ekgpu_step(m[i], nsteps);  // no thread to spare: step it here
+    }
+  }
+  st[0] = ekgpu_step(m[0], nsteps);
+  for (auto &t : th) t.join();
+  int r = EK_OK;
+  for (int i = 0; i < n; ++i) {
+    if (status) status[i] = st[i];
+    if (r == EK_OK && st[i] != EK_OK) r = st[i];
+  }
+  return r;
 }
 
 int ekgpu_rem_div(ek_ctx *h) {

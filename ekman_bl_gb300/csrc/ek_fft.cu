@@ -362,15 +362,15 @@ void launch_c2r(Ctx &c, const C2rArgs &a) {
 
 namespace ek {
 void fft_init_attributes() {
-  static bool done = false;
-  if (done) return;
+  static std::once_flag once;
+  std::call_once(once, [] {
   EK_CUDA(cudaFuncSetAttribute(k_r2c<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
   EK_CUDA(cudaFuncSetAttribute(k_c2r<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
   EK_CUDA(cudaFuncSetAttribute(k_r2c<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
   EK_CUDA(cudaFuncSetAttribute(k_c2r<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
   EK_CUDA(cudaFuncSetAttribute(k_r2c<FF>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
   EK_CUDA(cudaFuncSetAttribute(k_c2r<FF>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-  done = true;
+  });
 }
 }  // namespace ek
 

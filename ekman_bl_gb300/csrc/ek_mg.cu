@@ -28,6 +28,8 @@
 #include <algorithm>
 #include <cstdio>
 
+#include <mutex>
+
 #include "ek_internal.h"
 
 namespace ek {
@@ -765,13 +767,13 @@ int mg_solve_exact(Ctx &c, MgWork &w, int nprob, const double *kx2_dev, ek_mg_st
   return mg_exact_stats(c, w, nprob, st);
 }
 
-// k_coarse's shared-memory limit, set once (outside any stream capture).
+// k_coarse's shared-memory limit, set once per process (outside any stream
+// capture; contexts stepping on several host threads may get here together).
 void mg_exact_attributes() {
-  static bool attr_set = false;
-  if (!attr_set) {
+  static std::once_flag once;
+  std::call_once(once, [] {
     EK_CUDA(cudaFuncSetAttribute(k_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr_set = true;
-  }
+  });
 }
 
 // The launches of one exact solve on c.stream.  poll: stop issuing cycles

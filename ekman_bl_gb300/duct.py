@@ -25,7 +25,7 @@ _lib = None
 EXPORTS = [
     "ekgpu_default_params", "ekgpu_create", "ekgpu_destroy", "ekgpu_last_error", "ekgpu_set_stream",
     "ekgpu_set_metrics", "ekgpu_metrics_from_grid", "ekgpu_upload_state", "ekgpu_download_state",
-    "ekgpu_get_field", "ekgpu_put_field", "ekgpu_rk_substep", "ekgpu_step", "ekgpu_rem_div",
+    "ekgpu_get_field", "ekgpu_put_field", "ekgpu_rk_substep", "ekgpu_step", "ekgpu_ensemble_step", "ekgpu_rem_div",
     "ekgpu_poisson_batch", "ekgpu_poisson_batch_device", "ekgpu_last_divergence", "ekgpu_last_mg_stats",
     "ekgpu_launch_count", "ekgpu_set_timing", "ekgpu_get_timing", "ekgpu_timing_class_name",
     "ekgpu_fft_x_to_fourier", "ekgpu_fft_x_to_physical", "ekgpu_fft_x_to_fourier_noalloc",
@@ -108,6 +108,7 @@ def load_library():
     L.ekgpu_put_field.argtypes = [V, C.c_int, _D]
     L.ekgpu_rk_substep.argtypes = [V, C.c_int]
     L.ekgpu_step.argtypes = [V, C.c_int]
+    L.ekgpu_ensemble_step.argtypes = [C.POINTER(V), C.c_int, C.c_int, C.POINTER(C.c_int)]
     L.ekgpu_rem_div.argtypes = [V]
     L.ekgpu_poisson_batch.argtypes = [V, _D, _D, _D, C.c_int, C.POINTER(EkMgStats)]
     L.ekgpu_poisson_batch_device.argtypes = [V, V, V, V, C.c_int, C.POINTER(EkMgStats)]
@@ -461,6 +462,27 @@ class DuctSolver:
         if k < 0:
             self._check(k)
         return {self._L.ekgpu_timing_class_name(i).decode(): (ms[i], int(cnt[i]), by[i]) for i in range(k)}
+
+
+def ensemble_step(members, nsteps: int = 1, raise_on_error: bool = True) -> list:
+    """Advance an ensemble of independent runs (DuctSolvers of any sizes)
+    by nsteps RK3 steps each, concurrently on one GPU (ekgpu_ensemble_step:
+    each member on its own stream and host thread).  Returns the members'
+    status codes; with raise_on_error, raises the first failing member's
+    EkError after every member has finished."""
+    members = list(members)
+    L = load_library()
+    n = len(members)
+    handles = (C.c_void_p * max(n, 1))(*[m._h.value for m in members])
+    status = (C.c_int * max(n, 1))()
+    r = L.ekgpu_ensemble_step(handles, n, nsteps, status)
+    codes = [int(status[i]) for i in range(n)]
+    if r and raise_on_error:
+        for m, c in zip(members, codes):
+            if c:
+                m._check(c)
+        raise EkError(r, "ekgpu_ensemble_step: bad arguments")
+    return codes
 
 
 def fft_x(forward: bool, nx: int, nkx: int, nlines: int, in_ptr: int, out_ptr: int, stream_ptr: int | None = None):

@@ -201,6 +201,49 @@ WORKLOADS = {
 }
 
 
+def mudpack_form(n: int, pmax: int = 8) -> bool:
+    """True when n = p*2^(k-1) + 1 with 2 <= p <= pmax: MUDPACK's grid
+    form (mud2cr.f:134-135) with a coarsest grid of at most pmax + 1 points,
+    so that the multigrid has a full hierarchy."""
+    m = n - 1
+    while m > pmax and m % 2 == 0:
+        m //= 2
+    return 2 <= m <= pmax
+
+
+def mudpack_size(n: int, pmax: int = 8) -> int:
+    """The smallest n' >= n of MUDPACK form with p <= pmax (384 -> 385,
+    200 -> 225, 100 -> 113).  The reference's mud2cr only runs sides of
+    that form; a run on any other side is set up on the next one."""
+    m = max(n, 3)
+    while not mudpack_form(m, pmax):
+        m += 1
+    return m
+
+
+ENSEMBLE_MEMBERS = 8
+
+
+def ensemble_workloads(members: int = ENSEMBLE_MEMBERS, seed: int = 0, lo: int = 64, hi: int = 256):
+    """An ensemble of independent stratified Ekman-layer runs on uneven grids:
+    per member, NX from {64, 128, 256} (the transforms take powers of two)
+    and NY+2, NZ+2 drawn uniformly from [lo, hi] with numpy default_rng(seed),
+    then rounded up to MUDPACK form (mudpack_size).  Re = 400, Pr = 0.7,
+    Ri = 0.1, dt = 1e-3, cells of 0.4 Ekman depths and a spanwise period of
+    4 pi * NX/64 depths (the 64x65x65 case's cell sizes).  Returns
+    [(drawn (NY+2, NZ+2), Workload)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for m in range(members):
+        nx = int(rng.choice([64, 128, 256]))
+        ny2, nz2 = (int(v) for v in rng.integers(lo, hi + 1, size=2))
+        ny2r, nz2r = mudpack_size(ny2), mudpack_size(nz2)
+        w = Workload(f"ensemble{m}_{nx}x{ny2r}x{nz2r}", nx, ny2r, nz2r, 400.0, 0.7, 0.1, 1.0e-3, 100,
+                     1e-8, 0.01, 4.0 * math.pi * nx / 64, 0.4, seed=seed + m)
+        out.append(((ny2, nz2), w))
+    return out
+
+
 def make_grid(p: EkParams, ly: float, lz: float, stretch: float = 1.8):
     """GRID_YZ.dat-style points xpoint/ypoint(0:NZ+1, 0:NY+1) (column-major,
     K fastest): uniform streamwise z (period NZ*dz) and a tanh-stretched

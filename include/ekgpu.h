@@ -369,6 +369,19 @@ int ekgpu_rk_substep(ek_ctx *ctx, int rk_step);
  * (diablo.F90:152-154), repeated; advances params.time by DELTA_T per step. */
 int ekgpu_step(ek_ctx *ctx, int nsteps);
 
+/* An ensemble of independent runs, each with its own sizes, parameters and
+ * metrics (one context per member), advanced by nsteps RK3 steps together
+ * on one GPU.  The reference runs each member as its own MPI job; here every
+ * member steps on its own stream, from its own host thread, so the members'
+ * kernels share the GPU and one member's host waits (multigrid stop checks,
+ * statistics) overlap the others' work.  status[m] (optional, n entries)
+ * receives member m's ekgpu_step result; the call returns EK_OK when every
+ * member succeeded, else the first failing member's code (its message stays
+ * in that member's ekgpu_last_error).  A member that fails leaves the others
+ * running.  EK_ERR_ARG (no member touched) for n < 1, nsteps < 0, a null
+ * member or the same context twice. */
+int ekgpu_ensemble_step(ek_ctx *const *members, int n, int nsteps, int *status);
+
 /* The projection alone: REM_DIV_CURV (duct.F90:2472-2818) on the current
  * state, leaving phi in CR1 (as the reference leaves it in CR1X). */
 int ekgpu_rem_div(ek_ctx *ctx);
