@@ -271,15 +271,24 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
     if (kk == 0) v.im = 0.0;
     return Cx<T>::make((T)v.re, (T)v.im);
   };
-  // merge: Z'[k] = (X_k + conj X_{M-k}) + i (X_k - conj X_{M-k}) W^{-k}
+  // merge: Z'[k] = (X_k + conj X_{M-k}) + i (X_k - conj X_{M-k}) W^{-k}.
+  // The spectrum is staged in z first, so that each mode's prologue (FP64
+  // loads, the scale2 combination, the split into T) runs once; then each
+  // lane merges the pair (k, M-k) in place (X_M = 0: k = 0 pairs with zero).
+  for (int kk = lane; kk < M; kk += 32) z[kk] = X(kk);
+  __syncwarp();
   const V *twn = tw_n<T>(fc);
-  for (int kk = lane; kk < M; kk += 32) {
-    const V a = X(kk), b = X(M - kk);
+  auto merge = [&](V a, V b, V w) {
     const T sr = a.x + b.x, si = a.y - b.y;  // X_k + conj X_{M-k}
     const T dr = a.x - b.x, di = a.y + b.y;  // X_k - conj X_{M-k}
-    const V w = twn[kk];                     // conj taken below
     const T tr = dr * w.x + di * w.y, ti = di * w.x - dr * w.y;  // (d)*conj(w)
-    z[kk] = Cx<T>::make(sr - ti, si + tr);   // + i*t
+    return Cx<T>::make(sr - ti, si + tr);   // + i*t
+  };
+  for (int kk = lane; kk <= (M >> 1); kk += 32) {
+    const V a = z[kk];
+    const V b = (kk == 0) ? Cx<T>::make(T(0.0), T(0.0)) : z[M - kk];
+    z[kk] = merge(a, b, twn[kk]);
+    if (kk != 0 && 2 * kk != M) z[M - kk] = merge(b, a, twn[M - kk]);
   }
   __syncwarp();
   dif_fft(z, M, tw_m<T>(fc), true, lane);
