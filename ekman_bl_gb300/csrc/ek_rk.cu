@@ -334,6 +334,11 @@ __global__ void k_adi_les_tab(Dims d, Metrics m, const double *gb, const double 
   tab[6 * n2 + mm] = h * gr[xm];
 }
 
+// Rows per chunk of the line-solve kernels below: a thread issues every
+// load of a chunk's rows before its recurrence consumes them (the
+// x-dependent LES rows hold more values per row than the plain ones).
+constexpr int kAdiChunk = 8, kLesChunk = 4;
+
 // CN-ADI line solves with the LES eddy viscosity (duct.F90:1373-1386,
 // 1437-1450, 1489-1500, 1559-1569 for TH; 1667-1680, 1720-1731, 1771-1784,
 // 1821-1832 for U1; 1916-1929, 1963-1973, 2013-2026, 2081-2091 for U2 with
@@ -369,59 +374,94 @@ __global__ void __launch_bounds__(128) k_adi_les(AdiArgs a) {
   // addresses advance along the line: the point by sA, the cell by 1 (z) or LDM (y)
   const size_t c0 = ZS ? d.ip(i, 0, line) : d.ip(i, line, 0);
   const int m0 = ZS ? line * d.LDM : line, mstep = ZS ? 1 : d.LDM;
+  // chunked along y only (as in k_adi_seq)
+  constexpr int CH = ZS ? 1 : kLesChunk, CB = ZS ? 1 : kAdiChunk;
   double rBp = 1.0, gp = 0.0, Up = 0.0;
-  size_t c = c0;
-  for (int r = 0; r < nrow; ++r, c += sA) {
-    double L = 0.0, D = 1.0, U = 0.0, V = 0.0;
-    if (r >= r0 && r <= r1) {
-      const double *lt = a.ltab + (m0 + r * mstep), *tb = a.tab + (m0 + r * mstep);
-      const double nu0 = nut[c], nap = nut[c + sA], nam = nut[c - sA];
-      const double nxp = nut[c + sX], nxm = nut[c - sX];
-      const double f0 = px[c], fxp = px[c + sX], fxm = px[c - sX];
-      if (!ZS) V = fma(0.5, R[c], fma(tb[0], f0, fma(tb[n2], fxp, tb[2 * n2] * fxm)));
-      else V = fma(0.5, R[c], fma(tb[3 * n2], po[c], fma(tb[0], f0, fma(tb[n2], fxp, tb[2 * n2] * fxm))));
-      const double tp = lt[5 * n2] * (nxp + nu0), tm = lt[6 * n2] * (nu0 + nxm);
-      V = fma(tp, fxp - f0, fma(-tm, f0 - fxm, V));
-      const double slo = nu0 + nam, sup = nu0 + nap;
-      const double ml = lt[3 * n2], mu = lt[4 * n2];
-      L = fma(-ml, slo, lt[0]);
-      U = fma(-mu, sup, lt[n2]);
-      D = fma(mu, sup, fma(ml, slo, lt[2 * n2]));
+  // rows CH at a time: the rows of a chunk are built (every load
+  // issued) before the elimination runs through them
+  for (int rc = 0; rc < nrow; rc += CH) {
+    double Lv[CH], Dv[CH], Uv[CH], Vv[CH];
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int r = rc + u;
+      const size_t c = c0 + (size_t)r * sA;
+      double L = 0.0, D = 1.0, U = 0.0, V = 0.0;
+      if (r >= r0 && r <= r1) {
+        const double *lt = a.ltab + (m0 + r * mstep), *tb = a.tab + (m0 + r * mstep);
+        const double nu0 = nut[c], nap = nut[c + sA], nam = nut[c - sA];
+        const double nxp = nut[c + sX], nxm = nut[c - sX];
+        const double f0 = px[c], fxp = px[c + sX], fxm = px[c - sX];
+        if (!ZS) V = fma(0.5, R[c], fma(tb[0], f0, fma(tb[n2], fxp, tb[2 * n2] * fxm)));
+        else V = fma(0.5, R[c], fma(tb[3 * n2], po[c], fma(tb[0], f0, fma(tb[n2], fxp, tb[2 * n2] * fxm))));
+        const double tp = lt[5 * n2] * (nxp + nu0), tm = lt[6 * n2] * (nu0 + nxm);
+        V = fma(tp, fxp - f0, fma(-tm, f0 - fxm, V));
+        const double slo = nu0 + nam, sup = nu0 + nap;
+        const double ml = lt[3 * n2], mu = lt[4 * n2];
+        L = fma(-ml, slo, lt[0]);
+        U = fma(-mu, sup, lt[n2]);
+        D = fma(mu, sup, fma(ml, slo, lt[2 * n2]));
+      }
+      if (r < nrow)
+        for (int b = 0; b < a.bc.n; ++b) {
+          const BcRow &br = a.bc.r[b];
+          if (br.row != r) continue;
+          L = br.l;
+          D = br.dg;
+          U = br.u;
+          if (br.kind == 0) V = br.val;
+          else if (br.kind == 1) V = ZS ? ps[d.ip(i, br.src, line)] : po[d.ip(i, line, br.src)];
+          else V = br.val * a.bcw[br.src + line];
+        }
+      Lv[u] = L;
+      Dv[u] = D;
+      Uv[u] = U;
+      Vv[u] = V;
     }
-    for (int b = 0; b < a.bc.n; ++b) {
-      const BcRow &br = a.bc.r[b];
-      if (br.row != r) continue;
-      L = br.l;
-      D = br.dg;
-      U = br.u;
-      if (br.kind == 0) V = br.val;
-      else if (br.kind == 1) V = ZS ? ps[d.ip(i, br.src, line)] : po[d.ip(i, line, br.src)];
-      else V = br.val * a.bcw[br.src + line];
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int r = rc + u;
+      if (r >= nrow) break;
+      const size_t c = c0 + (size_t)r * sA;
+      double B, g;
+      if (r == 0) {
+        B = Dv[u];
+        g = Vv[u];
+      } else {
+        const double am = -Lv[u] * rBp;
+        B = fma(am, Up, Dv[u]);
+        g = fma(am, gp, Vv[u]);
+      }
+      const double rB = __drcp_rn(B);
+      a.out[c] = g;
+      a.scr_b[c] = rB;
+      a.scr_u[c] = Uv[u];
+      rBp = rB;
+      gp = g;
+      Up = Uv[u];
     }
-    double B, g;
-    if (r == 0) {
-      B = D;
-      g = V;
-    } else {
-      const double am = -L * rBp;
-      B = fma(am, Up, D);
-      g = fma(am, gp, V);
-    }
-    const double rB = __drcp_rn(B);
-    a.out[c] = g;
-    a.scr_b[c] = rB;
-    a.scr_u[c] = U;
-    rBp = rB;
-    gp = g;
-    Up = U;
   }
-  c -= sA;  // the last row
   double x = gp * rBp;
-  a.out[c] = x;
-  for (int r = nrow - 2; r >= 0; --r) {
-    c -= sA;
-    x = fma(-a.scr_u[c], x, a.out[c]) * a.scr_b[c];
-    a.out[c] = x;
+  a.out[c0 + (size_t)(nrow - 1) * sA] = x;
+  for (int rc = nrow - 2; rc >= 0; rc -= CB) {
+    double gv[CB], uv[CB], bv[CB];
+#pragma unroll
+    for (int u = 0; u < CB; ++u) {
+      const int r = rc - u;
+      if (r >= 0) {
+        const size_t c = c0 + (size_t)r * sA;
+        gv[u] = a.out[c];
+        uv[u] = a.scr_u[c];
+        bv[u] = a.scr_b[c];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < CB; ++u) {
+      const int r = rc - u;
+      if (r >= 0) {
+        x = fma(-uv[u], x, gv[u]) * bv[u];
+        a.out[c0 + (size_t)r * sA] = x;
+      }
+    }
   }
 }
 
@@ -476,64 +516,96 @@ __global__ void __launch_bounds__(128) k_adi_les_ff(AdiArgs a) {
   float2 *sb = reinterpret_cast<float2 *>(a.scr_b), *su = reinterpret_cast<float2 *>(a.scr_u);
   const size_t c0 = ZS ? d.ip(i, 0, line) : d.ip(i, line, 0);
   const int m0 = ZS ? line * d.LDM : line, mstep = ZS ? 1 : d.LDM;
+  // chunked along y only (as in k_adi_seq)
+  constexpr int CH = ZS ? 1 : kLesChunk, CB = ZS ? 1 : kAdiChunk;
   FF rBp(1.0f, 0.0f), gp(0.0f, 0.0f), Up(0.0f, 0.0f);
-  size_t c = c0;
-  for (int r = 0; r < nrow; ++r, c += sA) {
-    FF L(0.0f, 0.0f), D(1.0f, 0.0f), U(0.0f, 0.0f), V(0.0f, 0.0f);
-    if (r >= r0 && r <= r1) {
-      const float2 *t = a.ftab + (m0 + r * mstep);
-      const float nu0 = nut[c], nap = nut[c + sA], nam = nut[c - sA], nxp = nut[c + sX], nxm = nut[c - sX];
-      const FF f0(px[c]), fxp(px[c + sX]), fxm(px[c - sX]), rr(R[c]);
-      FF v = FF(0.5f * rr.hi, 0.5f * rr.lo);
-      if (!ZS) {
-        v = v + ff2(t[0]) * f0 + ff2(t[n2]) * fxp + ff2(t[2 * n2]) * fxm;
-      } else {
-        const FF p0(po[c]);
-        v = v + ff2(t[3 * n2]) * p0 + ff2(t[0]) * f0 + ff2(t[n2]) * fxp + ff2(t[2 * n2]) * fxm;
+  for (int rc = 0; rc < nrow; rc += CH) {
+    FF Lv[CH], Dv[CH], Uv[CH], Vv[CH];
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int r = rc + u;
+      const size_t c = c0 + (size_t)r * sA;
+      FF L(0.0f, 0.0f), D(1.0f, 0.0f), U(0.0f, 0.0f), V(0.0f, 0.0f);
+      if (r >= r0 && r <= r1) {
+        const float2 *t = a.ftab + (m0 + r * mstep);
+        const float nu0 = nut[c], nap = nut[c + sA], nam = nut[c - sA], nxp = nut[c + sX], nxm = nut[c - sX];
+        const FF f0(px[c]), fxp(px[c + sX]), fxm(px[c - sX]), rr(R[c]);
+        FF v = FF(0.5f * rr.hi, 0.5f * rr.lo);
+        if (!ZS) {
+          v = v + ff2(t[0]) * f0 + ff2(t[n2]) * fxp + ff2(t[2 * n2]) * fxm;
+        } else {
+          const FF p0(po[c]);
+          v = v + ff2(t[3 * n2]) * p0 + ff2(t[0]) * f0 + ff2(t[n2]) * fxp + ff2(t[2 * n2]) * fxm;
+        }
+        const FF tp = ff2(t[9 * n2]) * (ff1(nxp) + ff1(nu0)), tm = ff2(t[10 * n2]) * (ff1(nu0) + ff1(nxm));
+        V = v + tp * (fxp - f0) - tm * (f0 - fxm);
+        const FF slo = ff1(nu0) + ff1(nam), sup = ff1(nu0) + ff1(nap);
+        const FF ml = ff2(t[7 * n2]), mu = ff2(t[8 * n2]);
+        L = ff2(t[4 * n2]) - ml * slo;
+        U = ff2(t[5 * n2]) - mu * sup;
+        D = ff2(t[6 * n2]) + mu * sup + ml * slo;
       }
-      const FF tp = ff2(t[9 * n2]) * (ff1(nxp) + ff1(nu0)), tm = ff2(t[10 * n2]) * (ff1(nu0) + ff1(nxm));
-      V = v + tp * (fxp - f0) - tm * (f0 - fxm);
-      const FF slo = ff1(nu0) + ff1(nam), sup = ff1(nu0) + ff1(nap);
-      const FF ml = ff2(t[7 * n2]), mu = ff2(t[8 * n2]);
-      L = ff2(t[4 * n2]) - ml * slo;
-      U = ff2(t[5 * n2]) - mu * sup;
-      D = ff2(t[6 * n2]) + mu * sup + ml * slo;
+      if (r < nrow)
+        for (int b = 0; b < a.bc.n; ++b) {
+          const BcRow &br = a.bc.r[b];
+          if (br.row != r) continue;
+          L = FF(br.l);
+          D = FF(br.dg);
+          U = FF(br.u);
+          if (br.kind == 0) V = FF(br.val);
+          else if (br.kind == 1) V = FF(ZS ? ps[d.ip(i, br.src, line)] : po[d.ip(i, line, br.src)]);
+          else V = FF(br.val * a.bcw[br.src + line]);
+        }
+      Lv[u] = L;
+      Dv[u] = D;
+      Uv[u] = U;
+      Vv[u] = V;
     }
-    for (int b = 0; b < a.bc.n; ++b) {
-      const BcRow &br = a.bc.r[b];
-      if (br.row != r) continue;
-      L = FF(br.l);
-      D = FF(br.dg);
-      U = FF(br.u);
-      if (br.kind == 0) V = FF(br.val);
-      else if (br.kind == 1) V = FF(ZS ? ps[d.ip(i, br.src, line)] : po[d.ip(i, line, br.src)]);
-      else V = FF(br.val * a.bcw[br.src + line]);
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int r = rc + u;
+      if (r >= nrow) break;
+      const size_t c = c0 + (size_t)r * sA;
+      FF B, g;
+      if (r == 0) {
+        B = Dv[u];
+        g = Vv[u];
+      } else {
+        const FF am = -(Lv[u] * rBp);
+        B = Dv[u] + am * Up;
+        g = Vv[u] + am * gp;
+      }
+      const FF rB = ff_rcp(B);
+      gout[c] = make_float2(g.hi, g.lo);
+      sb[c] = make_float2(rB.hi, rB.lo);
+      su[c] = make_float2(Uv[u].hi, Uv[u].lo);
+      rBp = rB;
+      gp = g;
+      Up = Uv[u];
     }
-    FF B, g;
-    if (r == 0) {
-      B = D;
-      g = V;
-    } else {
-      const FF am = -(L * rBp);
-      B = D + am * Up;
-      g = V + am * gp;
-    }
-    const FF rB = ff_rcp(B);
-    gout[c] = make_float2(g.hi, g.lo);
-    sb[c] = make_float2(rB.hi, rB.lo);
-    su[c] = make_float2(U.hi, U.lo);
-    rBp = rB;
-    gp = g;
-    Up = U;
   }
-  c -= sA;
   FF x = gp * rBp;
-  a.out[c] = (double)x;
-  for (int r = nrow - 2; r >= 0; --r) {
-    c -= sA;
-    const FF gg = ff2(gout[c]);
-    x = (gg - ff2(su[c]) * x) * ff2(sb[c]);
-    a.out[c] = (double)x;
+  a.out[c0 + (size_t)(nrow - 1) * sA] = (double)x;
+  for (int rc = nrow - 2; rc >= 0; rc -= CB) {
+    float2 gv[CB], uv[CB], bv[CB];
+#pragma unroll
+    for (int u = 0; u < CB; ++u) {
+      const int r = rc - u;
+      if (r >= 0) {
+        const size_t c = c0 + (size_t)r * sA;
+        gv[u] = gout[c];
+        uv[u] = su[c];
+        bv[u] = sb[c];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < CB; ++u) {
+      const int r = rc - u;
+      if (r >= 0) {
+        x = (ff2(gv[u]) - ff2(uv[u]) * x) * ff2(bv[u]);
+        a.out[c0 + (size_t)r * sA] = (double)x;
+      }
+    }
   }
 }
 
@@ -548,10 +620,14 @@ __global__ void __launch_bounds__(128) k_adi_les_ff(AdiArgs a) {
 // The thread forms each row's right-hand side from the per-cell weights
 // (k_adi_tab), runs the forward elimination of THOMAS_REAL with the line's
 // host factors (broadcast loads: a block's threads share the line) and parks
-// the modified right-hand side in the output, then back-substitutes.  (A
-// block of eight warps that built the rows in shared memory while one warp
-// ran the recurrences took twice as long: seven warps idled through the
-// sequential part.)
+// the modified right-hand side in the output, then back-substitutes.  Along
+// y, rows go kAdiChunk at a time: every load of a chunk is issued before the
+// recurrence consumes it, so a thread keeps that many rows' loads in flight
+// instead of waiting out one memory latency per row.  (A block of eight
+// warps that built the rows in shared memory while one warp ran the
+// recurrences took twice as long: seven warps idled through the sequential
+// part.)  In the z sweep the output is the field itself: a row's old value
+// is loaded (with its chunk) before the row is stored.
 template <bool ZS>
 __global__ void __launch_bounds__(128) k_adi_seq(AdiArgs a) {
   const Dims &d = a.d;
@@ -573,32 +649,64 @@ __global__ void __launch_bounds__(128) k_adi_seq(AdiArgs a) {
   const double *fa = a.fa + (size_t)line * nrow, *fib = a.fib + (size_t)line * nrow, *fu = a.fu + (size_t)line * nrow;
   const size_t c0 = ZS ? d.ip(i, 0, line) : d.ip(i, line, 0);
   const int m0 = ZS ? line * d.LDM : line, mstep = ZS ? 1 : d.LDM;
+  // chunks along y; the z sweep (a field in place, rows LDX apart) measured
+  // slower with them, so it keeps one row at a time
+  constexpr int CH = ZS ? 1 : kAdiChunk;
   double prev = 0.0;
-  size_t c = c0;
-  for (int r = 0; r < nrow; ++r, c += sA) {
-    double v = 0.0;
-    if (r >= r0 && r <= r1) {
-      const double *tb = a.tab + (m0 + r * mstep);
-      if (!ZS) v = fma(0.5, R[c], fma(tb[0], px[c], fma(tb[n2], px[c + sX], tb[2 * n2] * px[c - sX])));
-      else v = fma(0.5, R[c], fma(tb[3 * n2], po[c], fma(tb[0], px[c], fma(tb[n2], px[c + sX], tb[2 * n2] * px[c - sX]))));
+  for (int rc = 0; rc < nrow; rc += CH) {
+    double vv[CH], av[CH];
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int r = rc + u;
+      double v = 0.0;
+      if (r < nrow) {
+        const size_t c = c0 + (size_t)r * sA;
+        if (r >= r0 && r <= r1) {
+          const double *tb = a.tab + (m0 + r * mstep);
+          if (!ZS) v = fma(0.5, R[c], fma(tb[0], px[c], fma(tb[n2], px[c + sX], tb[2 * n2] * px[c - sX])));
+          else v = fma(0.5, R[c], fma(tb[3 * n2], po[c], fma(tb[0], px[c], fma(tb[n2], px[c + sX], tb[2 * n2] * px[c - sX]))));
+        }
+        for (int b = 0; b < a.bc.n; ++b) {
+          const BcRow &br = a.bc.r[b];
+          if (br.row != r) continue;
+          if (br.kind == 0) v = br.val;
+          else if (br.kind == 1) v = ZS ? ps[d.ip(i, br.src, line)] : po[d.ip(i, line, br.src)];
+          else v = br.val * a.bcw[br.src + line];
+        }
+      }
+      vv[u] = v;
+      av[u] = (r < nrow) ? fa[r] : 0.0;
     }
-    for (int b = 0; b < a.bc.n; ++b) {
-      const BcRow &br = a.bc.r[b];
-      if (br.row != r) continue;
-      if (br.kind == 0) v = br.val;
-      else if (br.kind == 1) v = ZS ? ps[d.ip(i, br.src, line)] : po[d.ip(i, line, br.src)];
-      else v = br.val * a.bcw[br.src + line];
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int r = rc + u;
+      if (r < nrow) {
+        prev = (r == 0) ? vv[u] : vv[u] + av[u] * prev;
+        a.out[c0 + (size_t)r * sA] = prev;
+      }
     }
-    prev = (r == 0) ? v : v + fa[r] * prev;
-    a.out[c] = prev;
   }
-  c -= sA;
   double x = prev * fib[nrow - 1];
-  a.out[c] = x;
-  for (int r = nrow - 2; r >= 0; --r) {
-    c -= sA;
-    x = (a.out[c] - fu[r] * x) * fib[r];
-    a.out[c] = x;
+  a.out[c0 + (size_t)(nrow - 1) * sA] = x;
+  for (int rc = nrow - 2; rc >= 0; rc -= CH) {
+    double gv[CH], uv[CH], bv[CH];
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int r = rc - u;
+      if (r >= 0) {
+        gv[u] = a.out[c0 + (size_t)r * sA];
+        uv[u] = fu[r];
+        bv[u] = fib[r];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int r = rc - u;
+      if (r >= 0) {
+        x = (gv[u] - uv[u] * x) * bv[u];
+        a.out[c0 + (size_t)r * sA] = x;
+      }
+    }
   }
 }
 
