@@ -133,19 +133,35 @@ __global__ void k_spectral_rhs(SpecArgs a) {
     const size_t n2 = (size_t)d.LDM * (d.NY + 3), mm = d.m2(k, j);
     const cplx_t cs1 = pg_dot(a.m.pg, n2, 5, mm, p0, pkp, pkm, pjp, pjm);
     const cplx_t cs2 = pg_dot(a.m.pg, n2, 0, mm, p0, pkp, pkm, pjp, pjm);
-    const cplx_t ik = {0.0, a.kx[i]};
-    r1 = csub(r1, cmul(cscl(jac, cscl(a.T4, ik)), p0));
-    r2 = csub(r2, cscl(a.T4, cs2));
-    r3 = csub(r3, cscl(a.T4, cs1));
+    // - T4 J (i kx) p0, with the zero real part of i kx dropped: GB300's
+    // FP64 pipe is this kernel's limit, so every product that is known to
+    // vanish or can be shared is left out (the terms are those of
+    // duct.F90:371-409, regrouped: results agree to rounding)
+    const double s1 = (jac * a.T4) * a.kx[i];
+    r1.re = fma(s1, p0.im, r1.re);
+    r1.im = fma(-s1, p0.re, r1.im);
+    r2.re = fma(-a.T4, cs2.re, r2.re);
+    r2.im = fma(-a.T4, cs2.im, r2.im);
+    r3.re = fma(-a.T4, cs1.re, r3.re);
+    r3.im = fma(-a.T4, cs1.im, r3.im);
     if (i == 0 && a.forcing) r3.re = r3.re - a.T4 * a.px * jac;
     a.CR1[q] = r1;
     a.CR2[q] = r2;
     a.CR3[q] = r3;
     const double v = -a.nu * a.kx2[i] * jac;
     cplx_t f1 = cscl(v, cu1), f2 = cscl(v, cu2), f3 = cscl(v, cu3);
-    f3 = cadd(f3, cscl(jac, cscl(a.f0, cplx_t{cu1.re - a.ubc_top, cu1.im})));
-    f1 = csub(f1, cscl(jac, cscl(a.f0, cplx_t{cu3.re - a.wbulk0, cu3.im})));
-    if (a.th) f2 = csub(f2, cscl(jac * a.ri, a.CTH[q]));
+    // Coriolis on every kx (duct.F90:461-473), J f0 shared by both terms
+    const double jf = jac * a.f0;
+    f3.re = fma(jf, cu1.re - a.ubc_top, f3.re);
+    f3.im = fma(jf, cu1.im, f3.im);
+    f1.re = fma(-jf, cu3.re - a.wbulk0, f1.re);
+    f1.im = fma(-jf, cu3.im, f1.im);
+    if (a.th) {
+      const double jr = jac * a.ri;
+      const cplx_t cth = a.CTH[q];
+      f2.re = fma(-jr, cth.re, f2.re);
+      f2.im = fma(-jr, cth.im, f2.im);
+    }
     F1 = f1;
     F2 = f2;
     F3 = f3;
