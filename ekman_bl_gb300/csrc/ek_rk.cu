@@ -11,9 +11,6 @@ namespace {
 __device__ __forceinline__ cplx_t cadd(cplx_t a, cplx_t b) { return {a.re + b.re, a.im + b.im}; }
 __device__ __forceinline__ cplx_t csub(cplx_t a, cplx_t b) { return {a.re - b.re, a.im - b.im}; }
 __device__ __forceinline__ cplx_t cscl(double s, cplx_t a) { return {s * a.re, s * a.im}; }
-__device__ __forceinline__ cplx_t cmul(cplx_t a, cplx_t b) {
-  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
-}
 
 // x / b for several x sharing one divisor b: r = RN(1/b) once, then per
 // quotient q0 = RN(x r), e = x - b q0 (exact with an FMA), q = RN(q0 + e r),
@@ -780,9 +777,12 @@ __global__ void k_div_rhs(Dims d, const double *kx, const cplx_t *CU1, const cpl
     const cplx_t *CU3b = CU2b + d.nspec();
     const size_t q = d.ic(I, k, j);
     const size_t sK = d.LDC, sJ = (size_t)d.LDC * d.NZ2;
-    const cplx_t ikj = cmul(cplx_t{0.0, kx[I]}, cplx_t{jacm[d.m2(k, j)], 0.0});
-    const cplx_t dv = cadd(cadd(cmul(ikj, CU1[q]), csub(CU2b[q + sJ], CU2b[q])), csub(CU3b[q + sK], CU3b[q]));
-    v = (p & 1) ? dv.im : dv.re;
+    // only the part this problem needs: i kx J CU1 has real part
+    // -kx J Im CU1 and imaginary part kx J Re CU1 (the zero real part of
+    // i kx dropped; GB300's FP64 pipe is the limit here)
+    const double kj = kx[I] * jacm[d.m2(k, j)];
+    if (p & 1) v = (kj * CU1[q].re + (CU2b[q + sJ].im - CU2b[q].im)) + (CU3b[q + sK].im - CU3b[q].im);
+    else v = (-(kj * CU1[q].im) + (CU2b[q + sJ].re - CU2b[q].re)) + (CU3b[q + sK].re - CU3b[q].re);
   }
   const int nfx = d.NZ2;
   rhs[((size_t)j * nfx + k) * P + p] = v;
@@ -825,10 +825,16 @@ __global__ void k_correct_faces(Dims d, Metrics m, const cplx_t *CR1, cplx_t *CU
   const size_t q = d.ic(i, k, j);
   const size_t sK = d.LDC, sJ = (size_t)d.LDC * d.NZ2;
   auto P = [&](int dk, int dj) { return CR1[q + (long)dk * (long)sK + (long)dj * (long)sJ]; };
-  CU2b[q] = csub(csub(CU2b[q], cscl(m.g22[d.m3(k, j, 1)], csub(P(0, 0), P(0, -1)))),
-                 cscl(0.25 * m.g12[d.m3(k, j, 1)], csub(csub(cadd(P(1, 0), P(1, -1)), P(-1, 0)), P(-1, -1))));
-  CU3b[q] = csub(csub(CU3b[q], cscl(m.g11[d.m3(k, j, 2)], csub(P(0, 0), P(-1, 0)))),
-                 cscl(0.25 * m.g12[d.m3(k, j, 2)], csub(csub(cadd(P(0, 1), P(-1, 1)), P(0, -1)), P(-1, -1))));
+  // the same terms with each metric product fused into its subtraction
+  const cplx_t p00 = P(0, 0), p0m = P(0, -1), pm0 = P(-1, 0), pmm = P(-1, -1);
+  const cplx_t p10 = P(1, 0), p1m = P(1, -1), p01 = P(0, 1), pm1 = P(-1, 1);
+  const double a22 = m.g22[d.m3(k, j, 1)], a12 = 0.25 * m.g12[d.m3(k, j, 1)];
+  const double b11 = m.g11[d.m3(k, j, 2)], b12 = 0.25 * m.g12[d.m3(k, j, 2)];
+  const cplx_t u = CU2b[q], w = CU3b[q];
+  CU2b[q] = cplx_t{fma(-a12, ((p10.re + p1m.re) - pm0.re) - pmm.re, fma(-a22, p00.re - p0m.re, u.re)),
+                   fma(-a12, ((p10.im + p1m.im) - pm0.im) - pmm.im, fma(-a22, p00.im - p0m.im, u.im))};
+  CU3b[q] = cplx_t{fma(-b12, ((p01.re + pm1.re) - p0m.re) - pmm.re, fma(-b11, p00.re - pm0.re, w.re)),
+                   fma(-b12, ((p01.im + pm1.im) - p0m.im) - pmm.im, fma(-b11, p00.im - pm0.im, w.im))};
 }
 
 // Cell-centre correction (duct.F90:2729-2750).
@@ -864,8 +870,10 @@ __global__ void k_div_check(Dims d, const double *kx, const double *jacm, const 
   if (j >= d.JS && j <= d.JE && k >= d.ZS && k <= d.ZE) {
     const cplx_t *CU3b = CU2b + d.nspec();
     const size_t sK = d.LDC, sJ = (size_t)d.LDC * d.NZ2;
-    const cplx_t ikj = cmul(cplx_t{0.0, kx[i]}, cplx_t{jacm[d.m2(k, j)], 0.0});
-    v = cadd(cadd(cmul(ikj, CU1[q]), csub(CU2b[q + sJ], CU2b[q])), csub(CU3b[q + sK], CU3b[q]));
+    const double kj = kx[i] * jacm[d.m2(k, j)];
+    const cplx_t u1 = CU1[q], a0 = CU2b[q], a1 = CU2b[q + sJ], b0 = CU3b[q], b1 = CU3b[q + sK];
+    v.re = (-(kj * u1.im) + (a1.re - a0.re)) + (b1.re - b0.re);
+    v.im = (kj * u1.re + (a1.im - a0.im)) + (b1.im - b0.im);
   }
   CS[q] = v;
 }
