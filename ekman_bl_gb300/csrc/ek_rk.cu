@@ -250,22 +250,26 @@ __global__ void k_spectral_rhs(SpecArgs a) {
 
 // Contravariant face velocities U2b, U3b (duct.F90:721-732); U3b is stored
 // right after U2b.
-__global__ void k_face_velocity(Dims d, Metrics m, const double *U2, const double *U3, double *U2b, float *U2bf) {
+__global__ void k_face_velocity(Dims d, Metrics m, const double *U2, const double *U3, double *U2b, const float *U2f,
+                                const float *U3f, float *U2bf) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int k = d.ZS + blockIdx.y, j = d.JS + blockIdx.z;
   if (i >= d.NX) return;
   double *U3b = U2b + d.nphys();
   const size_t c = d.ip(i, k, j);
   const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
-  const double u2b = 0.5 * m.c22[d.m3(k, j, 1)] * (U2[c] + U2[c - sJ]) + 0.5 * m.c21[d.m3(k, j, 1)] * (U3[c] + U3[c - sJ]);
-  const double u3b = 0.5 * m.c11[d.m3(k, j, 2)] * (U3[c] + U3[c - sK]) + 0.5 * m.c12[d.m3(k, j, 2)] * (U2[c] + U2[c - sK]);
   if (U2bf) {
-    // only the FP32 flux transforms read the face velocities
-    U2bf[c] = d2f_bits(u2b);
-    U2bf[c + d.nphys()] = d2f_bits(u3b);
+    // only the FP32 flux transforms read the face velocities: the same sums
+    // in FP32 from the FP32 copies of U2, U3 (no FP64 instruction; the
+    // metrics are rounded on the integer pipe, the halving is exact)
+    const float h22 = 0.5f * d2f_bits(m.c22[d.m3(k, j, 1)]), h21 = 0.5f * d2f_bits(m.c21[d.m3(k, j, 1)]);
+    const float h11 = 0.5f * d2f_bits(m.c11[d.m3(k, j, 2)]), h12 = 0.5f * d2f_bits(m.c12[d.m3(k, j, 2)]);
+    const float u2 = U2f[c], u3 = U3f[c];
+    U2bf[c] = h22 * (u2 + U2f[c - sJ]) + h21 * (u3 + U3f[c - sJ]);
+    U2bf[c + d.nphys()] = h11 * (u3 + U3f[c - sK]) + h12 * (u2 + U2f[c - sK]);
   } else {
-    U2b[c] = u2b;
-    U3b[c] = u3b;
+    U2b[c] = 0.5 * m.c22[d.m3(k, j, 1)] * (U2[c] + U2[c - sJ]) + 0.5 * m.c21[d.m3(k, j, 1)] * (U3[c] + U3[c - sJ]);
+    U3b[c] = 0.5 * m.c11[d.m3(k, j, 2)] * (U3[c] + U3[c - sK]) + 0.5 * m.c12[d.m3(k, j, 2)] * (U2[c] + U2[c - sK]);
   }
 }
 
@@ -1000,8 +1004,9 @@ void launch_courant(Ctx &c) {
 void launch_face_velocity(Ctx &c) {
   const Dims &d = c.d;
   dim3 grid((d.NX + 127) / 128, d.ZE - d.ZS + 2, d.JE - d.JS + 2);
-  KScope ks(c, KC_FACE, 32.0 * d.NX * (d.ZE - d.ZS + 2) * (d.JE - d.JS + 2));
-  k_face_velocity<<<grid, 128, 0, c.stream>>>(d, c.m, c.U2, c.U3, c.U2b, c.p.fft_fp32 ? c.U2bf : nullptr);
+  // read U2, U3 and write U2b, U3b: FP64, or FP32 copies on the mixed path
+  KScope ks(c, KC_FACE, (c.p.fft_fp32 ? 16.0 : 32.0) * d.NX * (d.ZE - d.ZS + 2) * (d.JE - d.JS + 2));
+  k_face_velocity<<<grid, 128, 0, c.stream>>>(d, c.m, c.U2, c.U3, c.U2b, c.U2f, c.U3f, c.p.fft_fp32 ? c.U2bf : nullptr);
   after_launch(c);
 }
 
