@@ -163,14 +163,21 @@ int substep(Ctx &c, int rk) {
       launch_r2c(c, a);
     }
   }
-  // R = c2r(CR + beta h CF) (duct.F90:1127-1161)
+  // R = c2r(CR + beta h CF) (duct.F90:1127-1161); in the explicit-increment
+  // form S = R - J phi_old, in FP32, into R's slots
+  const bool sform = explicit_increment_form(c);
+  auto rdst = [&](C2rArgs &a, double *r) {
+    a.dst = sform ? nullptr : r;
+    a.dstf = sform ? reinterpret_cast<float *>(r) : nullptr;
+    a.lowp = sform ? 1 : 0;
+  };
   {
     C2rArgs a{};
     a.j0 = d.JS; a.j1 = d.JE; a.k0 = d.ZS; a.k1 = d.ZE;
     a.scale2 = TEMP5;
-    a.src = c.CR1; a.src2 = c.CF1; a.dst = c.R1; launch_c2r(c, a);
-    a.src = c.CR2; a.src2 = c.CF2; a.dst = c.R2; launch_c2r(c, a);
-    a.src = c.CR3; a.src2 = c.CF3; a.dst = c.R3; launch_c2r(c, a);
+    a.src = c.CR1; a.src2 = c.CF1; rdst(a, c.R1); launch_c2r(c, a);
+    a.src = c.CR2; a.src2 = c.CF2; rdst(a, c.R2); launch_c2r(c, a);
+    a.src = c.CR3; a.src2 = c.CF3; rdst(a, c.R3); launch_c2r(c, a);
   }
   if (th) {
     // scalar nonlinear terms (duct.F90:1165-1252) and RTH (1304-1326)
@@ -189,7 +196,7 @@ int substep(Ctx &c, int rk) {
     launch_r2c(c, a);
     C2rArgs b{};
     b.j0 = d.JST; b.j1 = d.JET; b.k0 = d.ZST; b.k1 = d.ZET;
-    b.scale2 = TEMP5; b.src = c.CRTH; b.src2 = c.CFTH; b.dst = c.RTH;
+    b.scale2 = TEMP5; b.src = c.CRTH; b.src2 = c.CFTH; rdst(b, c.RTH);
     launch_c2r(c, b);
     launch_adi(c, 0, rk);
     launch_th_corners(c);

@@ -416,6 +416,13 @@ void sing_graph_reset(Ctx &c);
 
 // LES (ek_les.cu)
 bool les_active(const Ctx &c);
+// The mixed path's explicit-increment form (fft_fp32 >= 1): CR keeps only
+// CR - J CU, its inverse transform S = R - J phi_old runs in FP32 into R's
+// slots, and the ADI right-hand sides fold the J phi_old halves into their
+// weights.  The same terms as RK_DUCT's R = c2r(CR + beta h CF) and
+// S = R - J phi_old (duct.F90:1127-1161, 1334-2392), without transforming
+// the large J CU part: the FP32 rounding then falls on the O(h) increment.
+inline bool explicit_increment_form(const Ctx &c) { return c.p.fft_fp32 >= 1; }
 void les_alloc(Ctx &c);
 void launch_les(Ctx &c, int rk);
 void launch_th_corners(Ctx &c);

@@ -34,6 +34,9 @@ struct SpecArgs {
   cplx_t *CU1, *CU2, *CU3, *CP, *CTH, *CF1, *CF2, *CF3, *CFTH, *CR1, *CR2, *CR3, *CRTH;
   double nu, nupr, T3, T4, px, f0, ubc_top, wbulk0, ri;
   int rk, th, cont_strat, forcing;
+  // 1: CR holds only the explicit increment CR - J CU (the mixed path,
+  // whose ADI takes S = R - J phi straight from its FP32 transform)
+  int cr_inc;
   const double *nut;  // LES: NU_T of the previous substep (KAPPA_T = NU_T/PR), else null
   double pr;
   // sponge_th
@@ -115,7 +118,8 @@ __global__ void k_spectral_rhs(SpecArgs a) {
   cplx_t F1{}, F2{}, F3{}, FT{};
   if (vel) {
     const cplx_t cu1 = a.CU1[q], cu2 = a.CU2[q], cu3 = a.CU3[q];
-    cplx_t r1 = cscl(jac, cu1), r2 = cscl(jac, cu2), r3 = cscl(jac, cu3);
+    const double jr = a.cr_inc ? 0.0 : jac;
+    cplx_t r1 = cscl(jr, cu1), r2 = cscl(jr, cu2), r3 = cscl(jr, cu3);
     if (a.rk > 1) {
       r1 = cadd(r1, cscl(a.T3, a.CF1[q]));
       r2 = cadd(r2, cscl(a.T3, a.CF2[q]));
@@ -165,7 +169,7 @@ __global__ void k_spectral_rhs(SpecArgs a) {
   }
   if (sca) {
     const cplx_t cth = a.CTH[q];
-    cplx_t rt = cscl(jac, cth);
+    cplx_t rt = cscl(a.cr_inc ? 0.0 : jac, cth);
     if (a.rk > 1) rt = cadd(rt, cscl(a.T3, a.CFTH[q]));
     a.CRTH[q] = rt;
     cplx_t ft = cscl(-a.nupr * jac * a.kx2[i], cth);
@@ -238,7 +242,12 @@ __global__ void k_spectral_rhs(SpecArgs a) {
       }
     }
     // CU2X(0,:,:) = 0 on the whole plane, after every use above
-    if (i == 0 && a.strat_per && a.reset) a.CU2[q] = cplx_t{0.0, 0.0};
+    if (i == 0 && a.strat_per && a.reset) {
+      // the explicit-increment form takes phi_old from the reset CU2, so CR
+      // keeps J times the part the reset removes (R itself still holds it)
+      if (a.cr_inc && vel) a.CR2[q] = cadd(a.CR2[q], cscl(jac, a.CU2[q]));
+      a.CU2[q] = cplx_t{0.0, 0.0};
+    }
   }
   if (vel) {
     a.CF1[q] = F1;
@@ -294,6 +303,10 @@ struct AdiArgs {
   // both tables split into float-float planes (0..3 right-hand side, 4..10 row)
   const float *nutf;
   const float2 *ftab;
+  // the explicit-increment form (mixed path): S = R - J phi_old in FP32 in
+  // R's slots, and the weights of k_adi_tab with the J phi_old halves folded
+  // in; null: R in FP64
+  const float *Sf;
 };
 
 // Right-hand-side weights of one ADI sweep per cell (tab[t * n2 + m2(k, j)]),
@@ -305,14 +318,16 @@ struct AdiArgs {
 //            t0 = J - c (G22(j+1) + G22(j)), t1 = c G22(j+1), t2 = c G22(j), t3 = -0.5 J
 // (c = NU H/2 [/PR]; the same algebra as duct.F90:1640-1660, 1877-1905, ...)
 template <bool ZS>
-__global__ void k_adi_tab(Dims d, Metrics m, double coef, double *tab) {
+__global__ void k_adi_tab(Dims d, Metrics m, double coef, int sform, double *tab) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
   if (k > d.NZ + 1 || j > d.NY + 1 || k < 1 || j < 1) return;
   const size_t n2 = (size_t)d.LDM * (d.NY + 3), mm = d.m2(k, j);
   const double jac = m.jac[mm];
+  // R/2 = S/2 + J phi_old/2: with S in place of R the y sweep's J/2 becomes J
+  // and the z sweep's -J phi_old/2 term cancels
   if (!ZS) {
     const double gp = m.g11[d.m3(k + 1, j, 2)], gm = m.g11[d.m3(k, j, 2)];
-    tab[mm] = 0.5 * jac - coef * (gp + gm);
+    tab[mm] = (sform ? jac : 0.5 * jac) - coef * (gp + gm);
     tab[n2 + mm] = coef * gp;
     tab[2 * n2 + mm] = coef * gm;
   } else {
@@ -320,7 +335,7 @@ __global__ void k_adi_tab(Dims d, Metrics m, double coef, double *tab) {
     tab[mm] = jac - coef * (gp + gm);
     tab[n2 + mm] = coef * gp;
     tab[2 * n2 + mm] = coef * gm;
-    tab[3 * n2 + mm] = -0.5 * jac;
+    tab[3 * n2 + mm] = sform ? 0.0 : -0.5 * jac;
   }
 }
 
@@ -408,8 +423,9 @@ __global__ void __launch_bounds__(128) k_adi_les(AdiArgs a) {
         const double nu0 = nut[c], nap = nut[c + sA], nam = nut[c - sA];
         const double nxp = nut[c + sX], nxm = nut[c - sX];
         const double f0 = px[c], fxp = px[c + sX], fxm = px[c - sX];
-        if (!ZS) V = fma(0.5, R[c], fma(tb[0], f0, fma(tb[n2], fxp, tb[2 * n2] * fxm)));
-        else V = fma(0.5, R[c], fma(tb[3 * n2], po[c], fma(tb[0], f0, fma(tb[n2], fxp, tb[2 * n2] * fxm))));
+        const double rv = a.Sf ? f2d_bits(a.Sf[c]) : R[c];
+        if (!ZS || a.Sf) V = fma(0.5, rv, fma(tb[0], f0, fma(tb[n2], fxp, tb[2 * n2] * fxm)));
+        else V = fma(0.5, rv, fma(tb[3 * n2], po[c], fma(tb[0], f0, fma(tb[n2], fxp, tb[2 * n2] * fxm))));
         const double tp = lt[5 * n2] * (nxp + nu0), tm = lt[6 * n2] * (nu0 + nxm);
         V = fma(tp, fxp - f0, fma(-tm, f0 - fxm, V));
         const double slo = nu0 + nam, sup = nu0 + nap;
@@ -546,9 +562,12 @@ __global__ void __launch_bounds__(128) k_adi_les_ff(AdiArgs a) {
       if (r >= r0 && r <= r1) {
         const float2 *t = a.ftab + (m0 + r * mstep);
         const float nu0 = nut[c], nap = nut[c + sA], nam = nut[c - sA], nxp = nut[c + sX], nxm = nut[c - sX];
-        const FF f0(px[c]), fxp(px[c + sX]), fxm(px[c - sX]), rr(R[c]);
+        const FF f0(px[c]), fxp(px[c + sX]), fxm(px[c - sX]);
+        const FF rr = a.Sf ? FF(a.Sf[c], 0.0f) : FF(R[c]);
         FF v = FF(0.5f * rr.hi, 0.5f * rr.lo);
         if (!ZS) {
+          v = v + ff2(t[0]) * f0 + ff2(t[n2]) * fxp + ff2(t[2 * n2]) * fxm;
+        } else if (a.Sf) {
           v = v + ff2(t[0]) * f0 + ff2(t[n2]) * fxp + ff2(t[2 * n2]) * fxm;
         } else {
           const FF p0(po[c]);
@@ -680,8 +699,9 @@ __global__ void __launch_bounds__(128) k_adi_seq(AdiArgs a) {
         const size_t c = c0 + (size_t)r * sA;
         if (r >= r0 && r <= r1) {
           const double *tb = a.tab + (m0 + r * mstep);
-          if (!ZS) v = fma(0.5, R[c], fma(tb[0], px[c], fma(tb[n2], px[c + sX], tb[2 * n2] * px[c - sX])));
-          else v = fma(0.5, R[c], fma(tb[3 * n2], po[c], fma(tb[0], px[c], fma(tb[n2], px[c + sX], tb[2 * n2] * px[c - sX]))));
+          const double rv = a.Sf ? f2d_bits(a.Sf[c]) : R[c];
+          if (!ZS || a.Sf) v = fma(0.5, rv, fma(tb[0], px[c], fma(tb[n2], px[c + sX], tb[2 * n2] * px[c - sX])));
+          else v = fma(0.5, rv, fma(tb[3 * n2], po[c], fma(tb[0], px[c], fma(tb[n2], px[c + sX], tb[2 * n2] * px[c - sX]))));
         }
         for (int b = 0; b < a.bc.n; ++b) {
           const BcRow &br = a.bc.r[b];
@@ -918,6 +938,7 @@ void launch_spectral_rhs(Ctx &c, int rk) {
   a.CF1 = c.CF1; a.CF2 = c.CF2; a.CF3 = c.CF3; a.CFTH = c.CFTH;
   a.CR1 = c.CR1; a.CR2 = c.CR2; a.CR3 = c.CR3; a.CRTH = c.CRTH;
   const ek_params &p = c.p;
+  a.cr_inc = explicit_increment_form(c) ? 1 : 0;
   a.nu = p.nu;
   a.nupr = p.nu / p.pr;
   a.T3 = c.ZETA_BAR[rk] * c.H_BAR[rk];
@@ -1020,6 +1041,8 @@ void launch_adi(Ctx &c, int field, int rk) {
   a.d = d;
   a.m = c.m;
   a.R = R;
+  const int sform = explicit_increment_form(c) ? 1 : 0;
+  a.Sf = sform ? reinterpret_cast<const float *>(R) : nullptr;
   a.phi_old = phi;
   a.phs = c.PHS;
   a.bcw = c.bc_weights;
@@ -1036,9 +1059,9 @@ void launch_adi(Ctx &c, int field, int rk) {
   a.tab = c.adi_tab;
   {
     const dim3 tg((unsigned)((d.NZ + 2 + 63) / 64), (unsigned)(d.NY + 2));
-    k_adi_tab<false><<<tg, 64, 0, c.stream>>>(d, c.m, coef, c.adi_tab);
+    k_adi_tab<false><<<tg, 64, 0, c.stream>>>(d, c.m, coef, sform, c.adi_tab);
     after_launch(c);
-    k_adi_tab<true><<<tg, 64, 0, c.stream>>>(d, c.m, coef, c.adi_tab + 4 * n2);
+    k_adi_tab<true><<<tg, 64, 0, c.stream>>>(d, c.m, coef, sform, c.adi_tab + 4 * n2);
     after_launch(c);
   }
   if (les_active(c)) {
