@@ -109,7 +109,9 @@ typedef struct ek_params {
   double cfl;                /* CFL                                                     */
   double delta_t_set;        /* DELTA_T_SET: the cap of the CFL time step               */
   int fft_fp32;              /* x-transforms in FP32 arithmetic (fields stay FP64): 0 none,
-                                1 the nonlinear product/flux transforms, 2 every transform */
+                                1 the nonlinear product/flux transforms and the explicit
+                                increment S = R - J phi_old that the ADI starts from (CR then
+                                holds CR - J CU), 2 every transform */
   int ff_arith;              /* 1: the x-transforms fft_fp32 leaves in FP64 use float-float
                                 arithmetic (~48 bits) on the FP32 pipe; fields stay FP64  */
   int les_model_type;        /* LES_MODEL_TYPE: only 2 (dynamic Smagorinsky, C_DYN from the
