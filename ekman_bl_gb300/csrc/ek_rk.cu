@@ -664,7 +664,7 @@ __global__ void __launch_bounds__(128) k_adi_les_ff(AdiArgs a) {
 // recurrences took twice as long: seven warps idled through the sequential
 // part.)  In the z sweep the output is the field itself: a row's old value
 // is loaded (with its chunk) before the row is stored.
-template <bool ZS>
+template <bool ZS, bool SF>
 __global__ void __launch_bounds__(128) k_adi_seq(AdiArgs a) {
   const Dims &d = a.d;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -699,8 +699,9 @@ __global__ void __launch_bounds__(128) k_adi_seq(AdiArgs a) {
         const size_t c = c0 + (size_t)r * sA;
         if (r >= r0 && r <= r1) {
           const double *tb = a.tab + (m0 + r * mstep);
-          const double rv = a.Sf ? f2d_bits(a.Sf[c]) : R[c];
-          if (!ZS || a.Sf) v = fma(0.5, rv, fma(tb[0], px[c], fma(tb[n2], px[c + sX], tb[2 * n2] * px[c - sX])));
+          // SF: the explicit increment S in FP32 (a.Sf), no phi_old term in z
+          const double rv = SF ? f2d_bits(a.Sf[c]) : R[c];
+          if (!ZS || SF) v = fma(0.5, rv, fma(tb[0], px[c], fma(tb[n2], px[c + sX], tb[2 * n2] * px[c - sX])));
           else v = fma(0.5, rv, fma(tb[3 * n2], po[c], fma(tb[0], px[c], fma(tb[n2], px[c + sX], tb[2 * n2] * px[c - sX]))));
         }
         for (int b = 0; b < a.bc.n; ++b) {
@@ -1136,7 +1137,9 @@ void launch_adi(Ctx &c, int field, int rk) {
   a.bc = c.bc[field][0];
   {
     KScope ks(c, KC_ADI_Y, 24.0 * d.NX * d.NY2 * (a.ze - a.zs + 1));
-    k_adi_seq<false><<<dim3((d.NX + 127) / 128, a.ze - a.zs + 1), 128, 0, c.stream>>>(a);
+    const dim3 grid((d.NX + 127) / 128, a.ze - a.zs + 1);
+    if (a.Sf) k_adi_seq<false, true><<<grid, 128, 0, c.stream>>>(a);
+    else k_adi_seq<false, false><<<grid, 128, 0, c.stream>>>(a);
     after_launch(c);
   }
   // z sweep
@@ -1148,7 +1151,9 @@ void launch_adi(Ctx &c, int field, int rk) {
   a.bc = c.bc[field][1];
   {
     KScope ks(c, KC_ADI_Z, 32.0 * d.NX * d.NZ2 * (a.je - a.js + 1));
-    k_adi_seq<true><<<dim3((d.NX + 127) / 128, d.NY2), 128, 0, c.stream>>>(a);
+    const dim3 grid((d.NX + 127) / 128, d.NY2);
+    if (a.Sf) k_adi_seq<true, true><<<grid, 128, 0, c.stream>>>(a);
+    else k_adi_seq<true, false><<<grid, 128, 0, c.stream>>>(a);
     after_launch(c);
   }
 }
