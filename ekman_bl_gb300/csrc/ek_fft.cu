@@ -38,6 +38,7 @@ struct FftConst {
   const float4 *tw_mff, *tw_nff;  // and split into float-float (re.hi, re.lo, im.hi, im.lo)
   const double *kx;
   Metrics m;
+  double inv_nx;  // 1/NX, divided once on the host
 };
 
 // T: the arithmetic type of a transform (double; float with the fields still
@@ -70,6 +71,11 @@ template <> __device__ __forceinline__ const float2 *tw_n<float>(const FftConst 
 template <> __device__ __forceinline__ const FF2 *tw_n<FF>(const FftConst &f) {
   return reinterpret_cast<const FF2 *>(f.tw_nff);
 }
+
+// an FP64 value in the arithmetic type T; to float on the integer pipe
+// (a plain cast is an F2F on the narrow FP64 pipe)
+template <typename T> __device__ __forceinline__ T from_f64(double x) { return (T)x; }
+template <> __device__ __forceinline__ float from_f64<float>(double x) { return d2f_bits(x); }
 
 template <typename V>
 __device__ __forceinline__ V cmul(V a, V b) {
@@ -132,7 +138,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
   if (args.pro == PRO_LOAD) {
     for (int n = lane; n < NX; n += 32) zr[n] = (T)args.a[base + n];
   } else if (args.pro == PRO_PROD) {
-    const T jac = (T)fc.m.jac[d.m2(k, j)];
+    const T jac = from_f64<T>(fc.m.jac[d.m2(k, j)]);
     if (fin)
       for (int n = lane; n < NX; n += 32) zr[n] = jac * (T)(double)args.af[base + n] * (T)(double)args.bf[base + n];
     else
@@ -140,9 +146,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
   } else if (fin) {
     // the flux stencil below on the FP32 copies
     const float *F = args.af, *U2b = args.bf, *U3b = args.bf + d.nphys();
-    const T g12a = (T)fc.m.g12[d.m3(k + 1, j, 2)], g12b = (T)fc.m.g12[d.m3(k, j, 2)];
-    const T g12c = (T)fc.m.g12[d.m3(k, j + 1, 1)], g12d = (T)fc.m.g12[d.m3(k, j, 1)];
-    const T qv = (T)(0.25 * args.visc);
+    const T g12a = from_f64<T>(fc.m.g12[d.m3(k + 1, j, 2)]), g12b = from_f64<T>(fc.m.g12[d.m3(k, j, 2)]);
+    const T g12c = from_f64<T>(fc.m.g12[d.m3(k, j + 1, 1)]), g12d = from_f64<T>(fc.m.g12[d.m3(k, j, 1)]);
+    const T qv = from_f64<T>(0.25 * args.visc);
     const T h = (T)0.5;
     const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
     for (int n = lane; n < NX; n += 32) {
@@ -163,9 +169,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
     const double *F = args.a;
     const double *U2b = args.b;  // U2b, followed in memory by U3b (see launch)
     const double *U3b = args.b + d.nphys();
-    const T g12a = (T)fc.m.g12[d.m3(k + 1, j, 2)], g12b = (T)fc.m.g12[d.m3(k, j, 2)];
-    const T g12c = (T)fc.m.g12[d.m3(k, j + 1, 1)], g12d = (T)fc.m.g12[d.m3(k, j, 1)];
-    const T qv = (T)(0.25 * args.visc);
+    const T g12a = from_f64<T>(fc.m.g12[d.m3(k + 1, j, 2)]), g12b = from_f64<T>(fc.m.g12[d.m3(k, j, 2)]);
+    const T g12c = from_f64<T>(fc.m.g12[d.m3(k, j + 1, 1)]), g12d = from_f64<T>(fc.m.g12[d.m3(k, j, 1)]);
+    const T qv = from_f64<T>(0.25 * args.visc);
     const T h = (T)0.5;
     const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
     for (int n = lane; n < NX; n += 32) {
@@ -181,7 +187,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
   }
   if (args.pro != PRO_LOAD && (args.extra || args.extraf)) {
     // LES additions: jac * tau for a product, the precomputed terms for a flux
-    const T es = (args.pro == PRO_PROD) ? (T)fc.m.jac[d.m2(k, j)] : (T)1.0;
+    const T es = (args.pro == PRO_PROD) ? from_f64<T>(fc.m.jac[d.m2(k, j)]) : (T)1.0;
     if (kF && args.extraf)
       for (int n = lane; n < NX; n += 32) zr[n] = zr[n] + es * (T)args.extraf[base + n];
     else if (args.extra)
@@ -191,7 +197,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
   dif_fft(z, M, tw_m<T>(fc), false, lane);
   // split: X[k] = E + W^k O, E = (Z_k + conj Z_{M-k})/2, O = -i (Z_k - conj Z_{M-k})/2
   cplx_t *dst = args.dst + d.ic(0, k, j);
-  const T inv = (T)(1.0 / NX);
+  const T inv = from_f64<T>(fc.inv_nx);
   const T h = (T)0.5;
   const int NKX = d.NKX;
   const V *twn = tw_n<T>(fc);
@@ -216,7 +222,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
       } else if (args.epi == EPI_ADD) {
         dst[kk] = cplx_t{o.re + f2d_bits((float)tr), o.im + f2d_bits((float)ti)};
       } else {
-        const T kv = (T)fc.kx[kk];
+        const T kv = from_f64<T>(fc.kx[kk]);
         dst[kk] = cplx_t{o.re - f2d_bits((float)(T(0) * tr - kv * ti)), o.im - f2d_bits((float)(T(0) * ti + kv * tr))};
       }
       continue;
@@ -269,7 +275,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
       v.im = kv * re;
     }
     if (kk == 0) v.im = 0.0;
-    return Cx<T>::make((T)v.re, (T)v.im);
+    return Cx<T>::make(from_f64<T>(v.re), from_f64<T>(v.im));
   };
   // merge: Z'[k] = (X_k + conj X_{M-k}) + i (X_k - conj X_{M-k}) W^{-k}.
   // The spectrum is staged in z first, so that each mode's prologue (FP64
@@ -326,6 +332,7 @@ FftConst make_const(Ctx &c) {
   f.tw_mff = c.tw_mff;
   f.tw_nff = c.tw_nff;
   f.kx = c.kx;
+  f.inv_nx = 1.0 / c.d.NX;
   f.m = c.m;
   return f;
 }
@@ -457,6 +464,7 @@ FftConst standalone_const(int nx, int nkx, long nlines, const double2 *tw) {
   f.logM = lg;
   f.tw_m = tw;
   f.tw_n = tw + f.M / 2;
+  f.inv_nx = 1.0 / nx;
   return f;
 }
 
