@@ -385,7 +385,7 @@ constexpr int kAdiChunk = 8, kLesChunk = 4;
 // back substitution reads them back.  Consecutive threads take consecutive x
 // points, so every access is coalesced; the work is FP64 arithmetic, about
 // two dozen operations and one reciprocal per row.
-template <bool ZS>
+template <bool ZS, bool SF>
 __global__ void __launch_bounds__(128) k_adi_les(AdiArgs a) {
   const Dims &d = a.d;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -423,8 +423,8 @@ __global__ void __launch_bounds__(128) k_adi_les(AdiArgs a) {
         const double nu0 = nut[c], nap = nut[c + sA], nam = nut[c - sA];
         const double nxp = nut[c + sX], nxm = nut[c - sX];
         const double f0 = px[c], fxp = px[c + sX], fxm = px[c - sX];
-        const double rv = a.Sf ? f2d_bits(a.Sf[c]) : R[c];
-        if (!ZS || a.Sf) V = fma(0.5, rv, fma(tb[0], f0, fma(tb[n2], fxp, tb[2 * n2] * fxm)));
+        const double rv = SF ? f2d_bits(a.Sf[c]) : R[c];
+        if (!ZS || SF) V = fma(0.5, rv, fma(tb[0], f0, fma(tb[n2], fxp, tb[2 * n2] * fxm)));
         else V = fma(0.5, rv, fma(tb[3 * n2], po[c], fma(tb[0], f0, fma(tb[n2], fxp, tb[2 * n2] * fxm))));
         const double tp = lt[5 * n2] * (nxp + nu0), tm = lt[6 * n2] * (nu0 + nxm);
         V = fma(tp, fxp - f0, fma(-tm, f0 - fxm, V));
@@ -526,7 +526,7 @@ __global__ void k_adi_ff_tab(int n2, const double *rhs_tab, const double *row_ta
 // of a row and joins the result.  The eliminated rows go to the scratch
 // fields (and the modified right-hand side into the output) as float pairs
 // in the same 8-byte slots.
-template <bool ZS>
+template <bool ZS, bool SF>
 __global__ void __launch_bounds__(128) k_adi_les_ff(AdiArgs a) {
   const Dims &d = a.d;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -563,11 +563,11 @@ __global__ void __launch_bounds__(128) k_adi_les_ff(AdiArgs a) {
         const float2 *t = a.ftab + (m0 + r * mstep);
         const float nu0 = nut[c], nap = nut[c + sA], nam = nut[c - sA], nxp = nut[c + sX], nxm = nut[c - sX];
         const FF f0(px[c]), fxp(px[c + sX]), fxm(px[c - sX]);
-        const FF rr = a.Sf ? FF(a.Sf[c], 0.0f) : FF(R[c]);
+        const FF rr = SF ? FF(a.Sf[c], 0.0f) : FF(R[c]);
         FF v = FF(0.5f * rr.hi, 0.5f * rr.lo);
         if (!ZS) {
           v = v + ff2(t[0]) * f0 + ff2(t[n2]) * fxp + ff2(t[2 * n2]) * fxm;
-        } else if (a.Sf) {
+        } else if (SF) {
           v = v + ff2(t[0]) * f0 + ff2(t[n2]) * fxp + ff2(t[2 * n2]) * fxm;
         } else {
           const FF p0(po[c]);
@@ -1110,8 +1110,10 @@ void launch_adi(Ctx &c, int field, int rk) {
       dim3 grid((d.NX + 127) / 128, a.ze - a.zs + 1);
       // algorithmic: read R, the field and NU_T, write the result
       KScope ks(c, KC_ADI_Y, 32.0 * d.NX * d.NY2 * (a.ze - a.zs + 1));
-      if (ff) k_adi_les_ff<false><<<grid, 128, 0, c.stream>>>(a);
-      else k_adi_les<false><<<grid, 128, 0, c.stream>>>(a);
+      if (ff && a.Sf) k_adi_les_ff<false, true><<<grid, 128, 0, c.stream>>>(a);
+      else if (ff) k_adi_les_ff<false, false><<<grid, 128, 0, c.stream>>>(a);
+      else if (a.Sf) k_adi_les<false, true><<<grid, 128, 0, c.stream>>>(a);
+      else k_adi_les<false, false><<<grid, 128, 0, c.stream>>>(a);
       after_launch(c);
     }
     a.tab = c.adi_tab + 4 * n2;
@@ -1123,8 +1125,10 @@ void launch_adi(Ctx &c, int field, int rk) {
       dim3 grid((d.NX + 127) / 128, d.NY2);
       // read R, the old field, the y-sweep result and NU_T, write the result
       KScope ks(c, KC_ADI_Z, 40.0 * d.NX * d.NZ2 * (a.je - a.js + 1));
-      if (ff) k_adi_les_ff<true><<<grid, 128, 0, c.stream>>>(a);
-      else k_adi_les<true><<<grid, 128, 0, c.stream>>>(a);
+      if (ff && a.Sf) k_adi_les_ff<true, true><<<grid, 128, 0, c.stream>>>(a);
+      else if (ff) k_adi_les_ff<true, false><<<grid, 128, 0, c.stream>>>(a);
+      else if (a.Sf) k_adi_les<true, true><<<grid, 128, 0, c.stream>>>(a);
+      else k_adi_les<true, false><<<grid, 128, 0, c.stream>>>(a);
       after_launch(c);
     }
     return;
