@@ -6,8 +6,8 @@ Workload: the stratified Ekman layer 512 x 385 x 257 (NX x NY+2 x NZ+2;
 NY = 384 rounded up to MUDPACK form), Re = 1000, Pr = 0.7, Ri = 0.1,
 dt = 3e-4, seeded synthetic fields (laminar Ekman spiral + 1% Gaussian
 noise), FP64 fields, every per-kx Poisson problem (171 complex ones) driven
-to a relative residual of 1e-8 (the singular kx = 0 mode keeps MUDPACK's
-own rule).  Prints one JSON line: RK3 steps/s of the batched
+to a relative residual of 1e-8 (the singular kx = 0 mode too, after its
+right-hand side is projected onto the operator's range).  Prints one JSON line: RK3 steps/s of the batched
 mixed-precision projection over K steps after W warm-up steps, timed with
 CUDA events on the solver's stream, and beside it the plain FP64 MUDPACK
 path on the same workload; the fields are larger than the 126 MB L2, so no
@@ -154,10 +154,11 @@ def setup_solver(device_index: int, mg_fast: int = 1, fft_fp32: int = 1, workloa
     return w, p, xp, yp, state, solver, stream
 
 
-def time_steps(solver, stream, steps, warmup, clocks_gpu=None):
+def time_steps(solver, stream, steps, warmup, clocks_gpu=None, counts=None):
     """W untimed steps, then exactly `steps` RK3 steps between CUDA events on
     the solver's stream; returns (ms, max MG cycles per substep, launches,
-    clock summary or None)."""
+    clock summary or None).  counts (a dict), when given, receives the real
+    Poisson problems solved and left above tolerance in the timed steps."""
     import torch
 
     for _ in range(warmup):
@@ -172,6 +173,7 @@ def time_steps(solver, stream, steps, warmup, clocks_gpu=None):
     try:
         torch.cuda.synchronize()
         n0 = solver.launch_count()
+        c0 = solver.mg_counters()
         with torch.cuda.stream(stream):
             start.record(stream)
             for _ in range(steps):
@@ -180,6 +182,9 @@ def time_steps(solver, stream, steps, warmup, clocks_gpu=None):
             end.record(stream)
         torch.cuda.synchronize()
         launches = solver.launch_count() - n0
+        if counts is not None:
+            c1 = solver.mg_counters()
+            counts["solved"], counts["not_converged"] = c1[0] - c0[0], c1[1] - c0[1]
     finally:
         if sampler:
             sampler.__exit__(None, None, None)
@@ -214,6 +219,27 @@ def time_poisson(solver, stream, p, nrep=3):
         e1.record(stream)
     torch.cuda.synchronize()
     return e0.elapsed_time(e1) / nrep, pst, ncomplex
+
+
+def end_to_end(solver, shape, steps):
+    """RK3 steps through the public C ABI with host buffers: every step
+    uploads the state from pinned host memory, steps, and downloads the
+    state.  Returns (seconds per step, bytes copied each way, steps)."""
+    import torch
+
+    pinned = [torch.empty(shape, dtype=torch.complex128, pin_memory=True).numpy() for _ in range(5)]
+    cur = solver.download()
+    for a, b in zip(pinned, cur):
+        a[...] = b
+    n = max(2, min(steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(n):
+        solver.upload(*pinned)
+        solver.step(1)
+        solver.download(out=pinned)
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / n, 5 * int(np.prod(shape)) * 16, n
 
 
 def replica_throughput(ms: float, steps: int, device: str = "cuda"):
@@ -442,7 +468,9 @@ def run_gpu(args):
     t_tune = time.perf_counter() - t_tune
     if world > 1:
         dist.barrier()
-    ms, mg_cycles, launches, clocks = time_steps(solver, stream, args.steps, args.warmup, clocks_gpu=local)
+    counts = {}
+    ms, mg_cycles, launches, clocks = time_steps(solver, stream, args.steps, args.warmup, clocks_gpu=local,
+                                                 counts=counts)
     if world > 1:
         dist.barrier()
     value, ms_max = replica_throughput(ms, args.steps)
@@ -457,31 +485,18 @@ def run_gpu(args):
     pois_ms, pst, ncomplex = time_poisson(solver, stream, p)
     solves_per_s = ncomplex / (pois_ms / 1000.0)
 
-    # end to end through the public C ABI with host buffers: H2D of the
-    # state from pinned memory, one RK3 step, D2H of the state
     shape = (p.ny + 2, p.nz + 2, p.nx // 2 + 1)
-    pinned = [torch.empty(shape, dtype=torch.complex128, pin_memory=True).numpy() for _ in range(5)]
-    cur = solver.download()
-    for a, b in zip(pinned, cur):
-        a[...] = b
-    n_e2e = max(2, min(args.steps, 5))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(n_e2e):
-        solver.upload(*pinned)
-        solver.step(1)
-        solver.download(out=pinned)
-    torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / n_e2e
-    bytes_state = 5 * int(np.prod(shape)) * 16
+    e2e_s, bytes_state, n_e2e = end_to_end(solver, shape, args.steps)
     learned = None if args.no_learned else run_learned(solver, stream, args)
     solver.close()
 
     # the plain FP64 GPU path (MUDPACK's smoother and cycles) at the same
     # tolerance, same workload, for the method-vs-plain ratio
     _, _, _, _, _, plain, pstream = setup_solver(local, mg_fast=0, fft_fp32=0)
-    pms, pcyc, _, _ = time_steps(plain, pstream, args.steps, args.warmup)
+    pcounts = {}
+    pms, pcyc, _, _ = time_steps(plain, pstream, args.steps, args.warmup, counts=pcounts)
     plain_pois_ms, plain_pst, _ = time_poisson(plain, pstream, p)
+    plain_e2e_s, _, plain_n_e2e = end_to_end(plain, shape, 2)
     plain.close()
     les = None if args.no_les else run_les(args, local)
     ensemble = None if args.no_ensemble else run_ensemble(args, local)
@@ -515,24 +530,37 @@ def run_gpu(args):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f64",
+            "dtype": "mixed: f64 state and spectral terms; f32 nonlinear-term transforms and V-cycles; "
+                     "float-float (~48-bit) state transforms, ADI-input transforms in f32, Poisson residual "
+                     "and update",
             "data": "synthetic (seeded laminar Ekman spiral + 1% Gaussian noise; no reference dataset exists)",
             "config": {"workload": WORKLOAD, "nx": p.nx, "ny_plus_2": p.ny + 2, "nz_plus_2": p.nz + 2,
                        "re": w.re, "pr": w.pr, "ri": w.ri, "delta_t": p.delta_t,
                        "method": "batched mixed-precision projection (no learned guess)",
-                       "precision": "fp64 fields; state-carrying transforms in float-float (~48-bit) "
-                                    "arithmetic, nonlinear-term transforms in FP32; Poisson: FP64 residual "
-                                    "refinement around FP32 V-cycles",
-                       "poisson": f"relative residual {MG_TOL:g} per problem; kx=0 by MUDPACK's rule",
+                       "precision": "FP64 fields, spectral right-hand side, ADI and projection; the "
+                                    "state-carrying x-transforms in float-float (~48-bit) arithmetic; the "
+                                    "nonlinear-term transforms and the transforms of the explicit increment "
+                                    "S = R - J phi in FP32; Poisson: float-float residual and update around "
+                                    "FP32 V-cycles",
+                       "poisson": f"relative residual {MG_TOL:g} per problem, kx=0 included (its right-hand "
+                                  f"side projected onto the operator's range, zero-mean solution)",
                        "mg_corrections_per_substep_max": mg_cycles,
+                       "poisson_problems_per_step": counts.get("solved", 0) / args.steps,
+                       "poisson_not_converged_per_step": counts.get("not_converged", 0) / args.steps,
                        "line_solve_layouts": {f"L{r['level']}{r['dir']}": f"{r['lanes']}x{r['seg']}" for r in tuned},
                        "autotune_s": round(t_tune, 2),
                        "l2": "fields (407 MB each, ~18 GB resident) exceed the 126 MB L2; no flush",
                        "parallelism": f"replicas x{world}"},
             "plain": {"value": round(plain_value, 4), "unit": "RK3 steps/s", "ms_per_step": round(pms / args.steps, 3),
-                      "method": "FP64 MUDPACK FMG + W(2,1), 4-colour GS", "mg_cycles_per_substep_max": pcyc,
+                      "dtype": "f64",
+                      "method": "FP64 MUDPACK FMG + W(2,1), 4-colour GS, every transform and kernel in FP64",
+                      "mg_cycles_per_substep_max": pcyc,
+                      "poisson_not_converged_per_step": pcounts.get("not_converged", 0) / args.steps,
                       "poisson_solves_per_s": round(ncomplex / (plain_pois_ms / 1000.0), 2),
-                      "poisson_max_cycles": plain_pst["max_cycles"]},
+                      "poisson_max_cycles": plain_pst["max_cycles"],
+                      "e2e": {"value": round(world / plain_e2e_s, 4), "unit": "RK3 steps/s",
+                              "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state,
+                              "steps": plain_n_e2e}},
             "speedup_vs_plain": round(value / (world * plain_value), 3),
             "poisson_solves_per_s": round(solves_per_s, 2),
             "poisson_batch": {"complex_problems": ncomplex, "ms": round(pois_ms, 3),

@@ -32,7 +32,7 @@ def _compile(src: str) -> str:
     if src.endswith(".cu"):
         cmd += ARCH
     else:
-        cmd += ["-x", "c++"]
+        cmd += ["-x", "c++", "-Xcompiler", "-fopenmp"]
     subprocess.run(cmd, check=True)
     return obj
 
@@ -52,7 +52,7 @@ def build(force: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(_compile, SOURCES))
     tmp = LIB + ".tmp"
-    subprocess.run([nvcc(), "-shared", "-o", tmp, *objs, *ARCH, "-lcudart"], check=True)
+    subprocess.run([nvcc(), "-shared", "-o", tmp, *objs, *ARCH, "-lcudart", "-lgomp"], check=True)
     os.replace(tmp, LIB)
     return LIB
 

@@ -108,6 +108,18 @@ void set_delta_t(Ctx &c, double dt) {
   build_adi_factors(c);
 }
 
+// What a substep reports for its projection solve.  Under the residual rule
+// a problem that reached mg_maxcy above the tolerance makes it
+// EK_ERR_NOT_CONVERGED (the substep is complete and its state valid).  Under
+// MUDPACK's relative-change rule the count stays in the statistics only, as
+// MULTIGRID_MUDPACK ignores mud2cr's ierror = -1 (mg_solver2d.F90:195-199,
+// mud2cr.f:204-207).
+int projection_status(const Ctx &c, int mg) {
+  if (mg == EK_OK) return EK_OK;
+  if (mg == EK_ERR_NOT_CONVERGED) return c.p.mg_stop == EK_MG_STOP_RESIDUAL ? EK_ERR_NOT_CONVERGED : EK_OK;
+  return mg;
+}
+
 void run_rem_div(Ctx &c, double temp4, bool update_p, int *mg_status) {
   const int P = 2 * (c.d.NKX + 1);
   launch_divergence_rhs(c, c.mgw.rhs[c.mg.ngrid - 1], P);
@@ -228,7 +240,8 @@ int substep(Ctx &c, int rk) {
   }
   int mg = EK_OK;
   run_rem_div(c, TEMP4, true, &mg);
-  return finish_divergence(c, nullptr);
+  const int dv = finish_divergence(c, nullptr);
+  return dv != EK_OK ? dv : projection_status(c, mg);
 }
 
 __global__ void k_transpose(const double *in, double *out, int P, long npt, int to_inner) {
@@ -473,18 +486,10 @@ void ekgpu_destroy(ek_ctx *h) {
   for (void *p : c.allocs) cudaFree(p);
   if (c.mg_cof_pool) cudaFree(c.mg_cof_pool);
   mg_work_free(c.mgw);
-  mg_work_free(c.mgs);
   guess_free(c);
   if (c.mgf_pool) cudaFree(c.mgf_pool);
   if (c.mg.ops_dev) cudaFree(c.mg.ops_dev);
   c.poll.destroy();
-  if (c.aux_stream) {
-    cudaStreamSynchronize(c.aux_stream);
-    cudaStreamDestroy(c.aux_stream);
-  }
-  sing_graph_reset(c);
-  if (c.ev_fork) cudaEventDestroy(c.ev_fork);
-  if (c.ev_join) cudaEventDestroy(c.ev_join);
   for (auto &r : c.trec) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : c.evpool) cudaEventDestroy(e);
   if (c.own_stream) cudaStreamDestroy(c.own_stream);
@@ -610,7 +615,6 @@ int ekgpu_set_metrics(ek_ctx *h, const ek_metrics *m) {
     if (!c.m.pg) c.m.pg = dalloc<double>(c, 11 * n2);
     launch_metric_tables(c);
     c.les.tab_ok = false;
-    sing_graph_reset(c);  // the multigrid plan is rebuilt below
     std::vector<double> jac(m->int_jacob, m->int_jacob + n2), g11(m->gmat_11, m->gmat_11 + 2 * n2),
         g12(m->gmat_12, m->gmat_12 + 2 * n2), g22(m->gmat_22, m->gmat_22 + 2 * n2), c22(m->cjob_22, m->cjob_22 + 2 * n2);
     // boundary rows and Thomas factors of every field, substep and direction
@@ -628,6 +632,13 @@ int ekgpu_set_metrics(ek_ctx *h, const ek_metrics *m) {
     MgPlan &P = c.mg;
     mg_build_plan_host(c, jac, g11, g12, g22);
     mg_build_schedule(P, c.p.mg_kcycle, c.p.mg_iprer, c.p.mg_ipost, c.p.mg_maxcy);
+    if (c.p.mg_stop == EK_MG_STOP_RESIDUAL) {
+      // left null vector of the kx = 0 operator (the well-posed kx = 0 solve)
+      std::vector<double> z;
+      if (!mg_left_null_host(P, z)) return fail(c, EK_ERR_ARG, "kx = 0 operator: zero pivot while finding its null vector");
+      if (!c.mg_z) c.mg_z = dalloc<double>(c, z.size());
+      EK_CUDA(cudaMemcpy(c.mg_z, z.data(), sizeof(double) * z.size(), cudaMemcpyHostToDevice));
+    }
     const int ncof = P.orth ? 4 : 8;
     P.lc = 1;
     for (int l = 1; l <= P.ngrid; ++l) {
@@ -735,6 +746,7 @@ int ekgpu_rk_substep(ek_ctx *h, int rk) {
     if (rk < 1 || rk > 3) return fail(c, EK_ERR_ARG, "rk_step must be 1, 2 or 3");
     const int st = substep(c, rk);
     if (st == EK_ERR_NAN) return fail(c, EK_ERR_NAN, "DIV is a NaN");
+    if (st == EK_ERR_NOT_CONVERGED) return fail(c, st, "a Poisson problem reached mg_maxcy above the tolerance");
     return st;
   });
 }
@@ -743,16 +755,21 @@ int ekgpu_step(ek_ctx *h, int nsteps) {
   return guarded(h, [&](Ctx &c) {
     if (!c.have_metrics) return fail(c, EK_ERR_STATE, "metrics not set");
     if (nsteps < 0) return fail(c, EK_ERR_ARG, "nsteps must be >= 0");
+    // a solve that misses its tolerance does not stop the run (the state
+    // stays valid); the call reports it once all steps are done
+    int late = EK_OK;
     for (int n = 0; n < nsteps; ++n) {
       c.p.time_step += 1;
       for (int rk = 1; rk <= 3; ++rk) {
         const int st = substep(c, rk);
         if (st == EK_ERR_NAN) return fail(c, EK_ERR_NAN, "DIV is a NaN");
-        if (st != EK_OK) return st;
+        if (st == EK_ERR_NOT_CONVERGED) late = st;
+        else if (st != EK_OK) return st;
       }
       c.p.time += c.p.delta_t;
       c.les.first_time = false;  // FIRST_TIME = .FALSE. after the first step (diablo.F90:157)
     }
+    if (late != EK_OK) return fail(c, late, "a Poisson problem reached mg_maxcy above the tolerance");
     return (int)EK_OK;
   });
 }
@@ -803,7 +820,10 @@ int ekgpu_rem_div(ek_ctx *h) {
     run_rem_div(c, 1.0, false, &mg);
     const int st = finish_divergence(c, nullptr);
     if (st == EK_ERR_NAN) return fail(c, EK_ERR_NAN, "DIV is a NaN");
-    return st;
+    if (st != EK_OK) return st;
+    const int ps = projection_status(c, mg);
+    if (ps == EK_ERR_NOT_CONVERGED) return fail(c, ps, "a Poisson problem reached mg_maxcy above the tolerance");
+    return ps;
   });
 }
 
@@ -841,6 +861,14 @@ int ekgpu_last_divergence(ek_ctx *h, double *div) {
   return guarded(h, [&](Ctx &c) {
     if (!div) return fail(c, EK_ERR_ARG, "div is NULL");
     *div = c.last_div;
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_mg_counters(ek_ctx *h, long long *solved, long long *not_converged) {
+  return guarded(h, [&](Ctx &c) {
+    if (solved) *solved = c.mg_solved_total;
+    if (not_converged) *not_converged = c.mg_nc_total;
     return (int)EK_OK;
   });
 }

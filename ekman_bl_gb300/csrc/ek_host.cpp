@@ -603,4 +603,130 @@ void mg_build_schedule(MgPlan &plan, int kcycle, int iprer, int ipost, int maxcy
   ops.swap(merged);
 }
 
+// ---------------------------------------------------------------------------
+// Left null vector of the finest kx = 0 operator.  With kx = 0 the problem is
+// periodic in x and pure Neumann in y, so A 1 = 0 and A^T has a one-
+// dimensional null space too.  The residual rule solves that mode as a well-
+// posed problem: b' = b - (z.b) z with A^T z = 0, |z| = 1, and a zero-mean
+// solution.  z is found once per metric set from A^T with the equation of
+// the centre point replaced by z = 1 there, factored as a band.
+namespace {
+
+// A general band matrix with kl sub- and ku super-diagonals, stored by
+// columns with room for the fill of row interchanges (LAPACK's band layout).
+struct BandMatrix {
+  long n;
+  int kl, ku, ld;
+  std::vector<double> a;
+  std::vector<long> piv;
+  BandMatrix(long n_, int kl_, int ku_) : n(n_), kl(kl_), ku(ku_), ld(2 * kl_ + ku_ + 1), a((size_t)ld * n_, 0.0) {}
+  double &at(long i, long j) { return a[(size_t)j * ld + (size_t)(kl + ku + i - j)]; }
+  // LU with partial pivoting, column by column; false on a zero pivot
+  bool factor() {
+    piv.assign(n, 0);
+    long last = 0;  // last column touched by an interchange so far
+    for (long j = 0; j < n; ++j) {
+      const long m = std::min<long>(kl, n - 1 - j);
+      long best = 0;
+      for (long t = 1; t <= m; ++t)
+        if (std::fabs(at(j + t, j)) > std::fabs(at(j + best, j))) best = t;
+      piv[j] = j + best;
+      last = std::max(last, std::min<long>(j + ku + best, n - 1));
+      if (best)
+        for (long c = j; c <= last; ++c) std::swap(at(j, c), at(j + best, c));
+      const double d = at(j, j);
+      if (d == 0.0) return false;
+      const double rd = 1.0 / d;
+      double *l = &at(j + 1, j);
+      for (long t = 0; t < m; ++t) l[t] *= rd;
+#pragma omp parallel for schedule(static) if (m * (last - j) > 32768)
+      for (long c = j + 1; c <= last; ++c) {
+        const double u = at(j, c);
+        if (u != 0.0) {
+          double *col = &at(j + 1, c);
+          for (long t = 0; t < m; ++t) col[t] -= l[t] * u;
+        }
+      }
+    }
+    return true;
+  }
+  void solve(std::vector<double> &x) {
+    for (long j = 0; j < n; ++j) {
+      std::swap(x[j], x[piv[j]]);
+      const long m = std::min<long>(kl, n - 1 - j);
+      for (long t = 1; t <= m; ++t) x[j + t] -= at(j + t, j) * x[j];
+    }
+    for (long j = n - 1; j >= 0; --j) {
+      x[j] /= at(j, j);
+      for (long i = std::max<long>(0, j - kl - ku); i < j; ++i) x[i] -= at(i, j) * x[j];
+    }
+  }
+};
+
+}  // namespace
+
+bool mg_left_null_host(const MgPlan &P, std::vector<double> &z) {
+  const int nx = P.nfx, ny = P.nfy;
+  const long n = (long)nx * ny;
+  const std::vector<double> &cf = P.cof_host[P.ngrid - 1];
+  auto C = [&](int i, int j, int l) { return cf[((size_t)(l - 1) * ny + (j - 1)) * nx + (i - 1)]; };
+  // place of unknown (i, j): rows j one after another; inside a row the
+  // periodic x ring is visited 1, nx, 2, nx-1, 3, ... so that the couplings
+  // through the ghost columns stay within three places of the diagonal
+  std::vector<long> place(nx + 2);
+  {
+    long k = 0;
+    place[1] = k++;
+    place[nx] = k++;
+    for (int lo = 2, hi = nx - 1; lo <= hi; ++lo, --hi) {
+      place[lo] = k++;
+      if (hi != lo) place[hi] = k++;
+    }
+  }
+  place[0] = place[nx - 1];  // ghost columns: e(0) = e(nx-1), e(nx+1) = e(2)
+  place[nx + 1] = place[2];
+  auto idx = [&](int i, int j) { return (long)(j - 1) * nx + place[i]; };
+  static const int di[8] = {1, 1, 0, -1, -1, -1, 0, 1}, dj[8] = {0, 1, 1, 1, 0, -1, -1, -1};
+  const long pin = idx((nx + 1) / 2, (ny + 1) / 2);
+  struct Entry { long r, c; double v; };
+  std::vector<Entry> ent;
+  ent.reserve((size_t)n * 9);
+  int kl = 0, ku = 0;
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      const long row_of_a = idx(i, j);
+      // A^T: A's coupling of (i, j) to its neighbour q lands in row q, column (i, j)
+      const double c9 = -C(i, j, 9) + C(i, j, 10);
+      if (row_of_a != pin) ent.push_back({row_of_a, row_of_a, c9});
+      for (int l = 0; l < 8; ++l) {
+        const int jj = j + dj[l];
+        const double v = C(i, j, l + 1);
+        if (jj < 1 || jj > ny || v == 0.0) continue;  // the y ghosts carry no coupling after the folding
+        const long q = idx(i + di[l], jj);
+        if (q == pin) continue;
+        ent.push_back({q, row_of_a, v});
+        kl = std::max<int>(kl, (int)(q - row_of_a));
+        ku = std::max<int>(ku, (int)(row_of_a - q));
+      }
+    }
+  BandMatrix M(n, kl, ku);
+  for (const Entry &e : ent) M.at(e.r, e.c) += e.v;
+  M.at(pin, pin) = 1.0;
+  if (!M.factor()) return false;
+  std::vector<double> x(n, 0.0);
+  x[pin] = 1.0;
+  M.solve(x);
+  z.assign(n, 0.0);
+  double ss = 0.0;
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      const double v = x[idx(i, j)];
+      z[(size_t)(j - 1) * nx + (i - 1)] = v;
+      ss += v * v;
+    }
+  const double inv = 1.0 / std::sqrt(ss);
+  for (double &v : z) v *= inv;
+  return true;
+}
+
 }  // namespace ek

@@ -278,7 +278,6 @@ struct Ctx {
   MgPlan mg;
   double *mg_cof_pool = nullptr;    // the levels' coefficients
   MgWork mgw;                       // the solves' work arrays
-  MgWork mgs;                       // mixed precision: the kx^2 = 0 problems, solved MUDPACK-exact
   std::vector<double> mg_kx2_host;  // host copy of mgw.kx2
   float *mgf_pool = nullptr;        // mixed-precision multigrid
   std::vector<MgLevelF> mgf_levels;
@@ -287,18 +286,15 @@ struct Ctx {
   float *mgf_bh = nullptr, *mgf_bl = nullptr;    // float-float finest rhs
   float *mgf_cfh = nullptr, *mgf_cfl = nullptr;  // float-float finest coefficients
   int mgf_pmax = 0;
+  // residual rule: left null vector of the finest kx = 0 operator (nfx*nfy,
+  // unit norm), for the well-posed kx = 0 solve
+  double *mg_z = nullptr;
   ek_mg_stats last_stats{};
+  // problems that missed the residual rule's tolerance, and problems solved,
+  // summed over every solve since the context was created
+  long long mg_nc_total = 0, mg_solved_total = 0;
   double last_mean_cycles = 0.0;  // mixed solver: mean corrections over the kx^2 != 0 problems
   StopPoll poll;
-  cudaStream_t aux_stream = nullptr;  // the kx^2 = 0 batch runs here, beside the FP32 cycles (high priority)
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  // the kx^2 = 0 batch's exact solve captured as one CUDA graph: valid for
-  // sing_ns problems in the work arrays and plan recorded in sing_key
-  cudaGraph_t sing_graph = nullptr;
-  cudaGraphExec_t sing_exec = nullptr;
-  int sing_ns = 0;
-  const void *sing_key[3] = {};
-  long long sing_launches = 0;
   // sponge_th: SPONGE_SIGMA(0:NY+1), SPONGE_SIGMA_OUT(0:NZ+1), and the
   // mode-0 mean of CU3X over the upper layer with the dynamic-branch flag
   double *sponge_sig = nullptr, *sponge_sig_out = nullptr, *sponge_red = nullptr;
@@ -377,6 +373,7 @@ int sponge_profiles_host(const ek_params *p, const double *xpoint, const double 
 void mg_build_plan_host(Ctx &c, const std::vector<double> &jac, const std::vector<double> &g11,
                         const std::vector<double> &g12, const std::vector<double> &g22);
 void mg_build_schedule(MgPlan &plan, int kcycle, int iprer, int ipost, int maxcy);
+bool mg_left_null_host(const MgPlan &P, std::vector<double> &z);
 
 // ---- device launch wrappers ----
 // FFT (ek_fft.cu)
@@ -412,7 +409,6 @@ void launch_metric_tables(Ctx &c);
 void launch_face_velocity(Ctx &c);
 void launch_adi(Ctx &c, int field, int rk);
 void mg_exact_attributes();
-void sing_graph_reset(Ctx &c);
 
 // LES (ek_les.cu)
 bool les_active(const Ctx &c);
@@ -438,7 +434,10 @@ int mg_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_host, e
 int mg_solve_exact(Ctx &c, MgWork &w, int nprob, const double *kx2_dev, ek_mg_stats *st, int max_cycles);
 void mg_exact_enqueue(Ctx &c, MgWork &w, int nprob, const double *kx2_dev, int max_cycles, bool poll);
 int mg_exact_stats(Ctx &c, MgWork &w, int nprob, ek_mg_stats *st);
-constexpr int kSingularMaxCycles = 6;  // MULTIGRID_MUDPACK's cap for the kx = 0 mode
+// The residual rule's well-posed kx^2 = 0 problems (finest level, problem
+// fastest): b <- b - (z.b) z before the solve, phi <- phi - mean(phi) after.
+void mg_null_project(Ctx &c, double *rhs_finest, int nprob, const double *kx2_dev);
+void mg_null_mean(Ctx &c, double *phi_finest, int nprob, const double *kx2_dev);
 void mg_alloc(Ctx &c, int pmax);
 void mg_work_alloc(Ctx &c, MgWork &w, int pmax);
 void mg_work_free(MgWork &w);

@@ -395,8 +395,8 @@ __global__ void __launch_bounds__(32 * kChkY) k_check_reduce(MgDev g) {
   }
 }
 
-// Relative change (MUDPACK) or, for the residual rule, relative residual;
-// problems with ce = 0 (kx = 0, singular) keep the relative-change test.
+// Relative change (MUDPACK) or, for the residual rule, relative residual
+// (kx^2 = 0 problems included: their right-hand side was made compatible).
 __global__ void k_check_finish(MgDev g, int iter, int last) {
   if (*g.alldone) return;
   __shared__ int active;
@@ -413,14 +413,6 @@ __global__ void k_check_finish(MgDev g, int iter, int last) {
     if (g.stop_rule == 0) {
       meas = relmax;
       conv = (g.tol > 0.0) && (relmax <= g.tol);
-    } else if (g.kx2[p] == 0.0) {
-      // singular mode: MULTIGRID_MUDPACK's own rule (REAL*4 1e-6, <= 6 cycles)
-      meas = relmax;
-      conv = relmax <= (double)1.0e-6f;
-      if (!conv && iter >= kSingularMaxCycles) {
-        g.done[p] = 2;  // stopped at the reference's cycle cap
-        continue;
-      }
     } else {
       const double bn = sqrt(g.red[4 * p + 2]);
       meas = (bn > 0.0) ? sqrt(g.red[4 * p + 3]) / bn : 0.0;
@@ -753,8 +745,13 @@ void mg_alloc(Ctx &c, int pmax) {
 }
 
 int mg_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_host, ek_mg_stats *st) {
-  if (c.p.mg_fast) return mgfast_solve(c, nprob, kx2_dev, kx2_host, st);
-  return mg_solve_exact(c, c.mgw, nprob, kx2_dev, st, 0);
+  const int r = c.p.mg_fast ? mgfast_solve(c, nprob, kx2_dev, kx2_host, st)
+                            : mg_solve_exact(c, c.mgw, nprob, kx2_dev, st, 0);
+  if (r == EK_OK || r == EK_ERR_NOT_CONVERGED) {
+    c.mg_solved_total += nprob;
+    c.mg_nc_total += c.last_stats.n_not_converged;
+  }
+  return r;
 }
 
 // One batched MUDPACK-exact solve in the work arrays w: the finest rhs must
@@ -763,8 +760,68 @@ int mg_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_host, e
 // after that many k-cycles (a batch whose problems all stop by then).
 int mg_solve_exact(Ctx &c, MgWork &w, int nprob, const double *kx2_dev, ek_mg_stats *st, int max_cycles) {
   if (nprob > w.pmax) return EK_ERR_ARG;
+  const bool wellposed = c.p.mg_stop == EK_MG_STOP_RESIDUAL;
+  if (wellposed) mg_null_project(c, w.rhs[c.mg.ngrid - 1], nprob, kx2_dev);
   mg_exact_enqueue(c, w, nprob, kx2_dev, max_cycles, true);
+  if (wellposed) mg_null_mean(c, w.phif, nprob, kx2_dev);
   return mg_exact_stats(c, w, nprob, st);
+}
+
+namespace {
+// Sum over a block of 256 threads (fixed order: deterministic).
+__device__ __forceinline__ double block_sum256(double v, double *sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = (threadIdx.x < 8) ? sh[threadIdx.x] : 0.0;
+    for (int o = 4; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) sh[8] = v;
+  }
+  __syncthreads();
+  const double r = sh[8];
+  __syncthreads();
+  return r;
+}
+
+// One block per problem; problems with kx^2 != 0 return at once.
+// b <- b - (z.b) z at the finest level (z has unit norm).
+__global__ void __launch_bounds__(256) k_null_project(double *rhs, int P, const double *z, int npt,
+                                                       const double *kx2) {
+  __shared__ double sh[9];
+  const int p = blockIdx.x;
+  if (kx2[p] != 0.0) return;
+  double s = 0.0;
+  for (int t = threadIdx.x; t < npt; t += 256) s += z[t] * rhs[(size_t)t * P + p];
+  s = block_sum256(s, sh);
+  for (int t = threadIdx.x; t < npt; t += 256) rhs[(size_t)t * P + p] -= s * z[t];
+}
+
+// phi <- phi - mean(phi) over the npt finest points.
+__global__ void __launch_bounds__(256) k_null_mean(double *phi, int P, int npt, const double *kx2) {
+  __shared__ double sh[9];
+  const int p = blockIdx.x;
+  if (kx2[p] != 0.0) return;
+  double s = 0.0;
+  for (int t = threadIdx.x; t < npt; t += 256) s += phi[(size_t)t * P + p];
+  const double m = block_sum256(s, sh) / (double)npt;
+  for (int t = threadIdx.x; t < npt; t += 256) phi[(size_t)t * P + p] -= m;
+}
+}  // namespace
+
+void mg_null_project(Ctx &c, double *rhs_finest, int nprob, const double *kx2_dev) {
+  if (!c.mg_z) throw CudaError("well-posed kx = 0 solve: the left null vector is missing");
+  const int npt = c.mg.nfx * c.mg.nfy;
+  KScope ks(c, KC_MG_SETUP, 0.0);
+  k_null_project<<<nprob, 256, 0, c.stream>>>(rhs_finest, nprob, c.mg_z, npt, kx2_dev);
+  after_launch(c);
+}
+
+void mg_null_mean(Ctx &c, double *phi_finest, int nprob, const double *kx2_dev) {
+  const int npt = c.mg.nfx * c.mg.nfy;
+  KScope ks(c, KC_MG_SETUP, 0.0);
+  k_null_mean<<<nprob, 256, 0, c.stream>>>(phi_finest, nprob, npt, kx2_dev);
+  after_launch(c);
 }
 
 // k_coarse's shared-memory limit, set once per process (outside any stream

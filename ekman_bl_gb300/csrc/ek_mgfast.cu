@@ -17,11 +17,12 @@
 // directions smooths both regions, so each cycle cuts the residual ~10x
 // where MUDPACK's point smoother (W-cycles) gets ~1.3x.
 //
-// Problems with kx^2 = 0 are singular (periodic x, Neumann y).  MUDPACK stops
-// them on its relative-change rule after at most maxcy cycles, usually before
-// they converge, so their result is MUDPACK's particular iterate; they are
-// gathered into a batch of their own and solved by the MUDPACK-exact path,
-// which gives the same result as a solve with mg_fast = 0.
+// Problems with kx^2 = 0 are singular (periodic x, Neumann y).  They are
+// solved as well-posed problems in the same batch: the right-hand side loses
+// its component along the operator's left null vector, the tolerance is the
+// same as for every other problem, and the solution has zero mean.  Inside
+// the FP32 cycle their coarsest-level correction is shifted to zero mean (a
+// constant is in the null space at every level and prolongs to a constant).
 #include <algorithm>
 
 #include "ek_internal.h"
@@ -189,27 +190,6 @@ __global__ void k_f_check(FastDev g, int iter, int last) {
   }
   __syncthreads();
   if (threadIdx.x == 0 && active == 0) *g.alldone = 1;
-}
-
-// The kx^2 = 0 subset: gather its finest rhs (problem fastest, P problems)
-// into a batch of ns problems, mark it done for the FP32 iteration, and
-// scatter its solutions back.
-__global__ void k_f_gather(const double *src, int P, double *dst, int ns, const int *idx, long npt) {
-  const long n = npt * ns;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-    const int q = (int)(t % ns);
-    dst[t] = src[(t / ns) * P + idx[q]];
-  }
-}
-__global__ void k_f_scatter(const double *src, int ns, double *dst, int P, const int *idx, long npt) {
-  const long n = npt * ns;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-    const int q = (int)(t % ns);
-    dst[(t / ns) * P + idx[q]] = src[t];
-  }
-}
-__global__ void k_f_mark(int *done, const int *idx, int ns) {
-  for (int q = threadIdx.x; q < ns; q += blockDim.x) done[idx[q]] = 1;
 }
 
 // Line Gauss-Seidel.  The 9-point operator couples each point to its eight
@@ -602,6 +582,15 @@ __global__ void k_f_coarsest(FastDev g, int sweeps) {
       for (int col = 1; col <= 2; ++col)
         for (int j = col; j <= L.ny; j += 2) xline_solve(L, P, p, j, kx2, orth);
     }
+    if (kx2 == 0.f) {
+      // singular: keep the correction at zero mean, ghosts included
+      float m = 0.f;
+      for (int j = 1; j <= L.ny; ++j)
+        for (int i = 1; i <= L.nx; ++i) m += E(L, P, i, j, p);
+      m = m / (float)(L.nx * L.ny);
+      for (int j = 1; j <= L.ny; ++j)
+        for (int i = 0; i <= L.nx + 1; ++i) E(L, P, i, j, p) -= m;
+    }
   }
 }
 
@@ -941,24 +930,6 @@ void mgfast_alloc(Ctx &c, int pmax) {
     EK_CUDA(cudaMemcpy(c.mgf_cfl, l.data(), sizeof(float) * l.size(), cudaMemcpyHostToDevice));
   }
   c.mgf_pmax = pmax;
-  if (!c.aux_stream) {
-    // highest priority: the kx^2 = 0 solve is a long chain of small launches
-    // that would otherwise queue behind the FP32 cycles' full-GPU kernels
-    int lo = 0, hi = 0;
-    EK_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-    EK_CUDA(cudaStreamCreateWithPriority(&c.aux_stream, cudaStreamNonBlocking, hi));
-    EK_CUDA(cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming));
-    EK_CUDA(cudaEventCreateWithFlags(&c.ev_join, cudaEventDisableTiming));
-  }
-  mg_exact_attributes();
-}
-
-void sing_graph_reset(Ctx &c) {
-  if (c.sing_exec) cudaGraphExecDestroy(c.sing_exec);
-  if (c.sing_graph) cudaGraphDestroy(c.sing_graph);
-  c.sing_exec = nullptr;
-  c.sing_graph = nullptr;
-  c.sing_ns = 0;
 }
 
 // Solve with the mixed-precision iteration; the finest rhs must be in
@@ -971,7 +942,8 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
   cudaStream_t s = c.stream;
   const int bs = 256;
   const long npt = (long)PL.nfx * PL.nfy;
-  // the singular subset, solved first by the MUDPACK-exact path
+  // the kx^2 = 0 problems (well posed by projection; the learned guess and
+  // its statistics leave them out)
   std::vector<double> kxh;
   if (!kx2_host) {
     kxh.resize(nprob);
@@ -979,87 +951,20 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
     EK_CUDA(cudaStreamSynchronize(s));
     kx2_host = kxh.data();
   }
-  std::vector<int> sing;
   std::vector<char> is_sing(nprob, 0);
+  int ns = 0;
   for (int p = 0; p < nprob; ++p)
     if (kx2_host[p] == 0.0) {
-      sing.push_back(p);
       is_sing[p] = 1;
+      ++ns;
     }
-  const int ns = (int)sing.size();
-  ek_mg_stats Ss{};
-  int rs = EK_OK;
-  if (ns > 0) {
-    MgWork &ws = c.mgs;
-    if (ns > ws.pmax) {
-      mg_work_alloc(c, ws, std::max(ns, 2));
-      EK_CUDA(cudaMemsetAsync(ws.kx2, 0, sizeof(double) * ws.pmax, s));
-    }
-    if (ws.idx_host != sing) {
-      EK_CUDA(cudaMemcpyAsync(ws.idx, sing.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s));
-      ws.idx_host = sing;
-    }
-    {
-      KScope ks(c, KC_MG_SETUP, 16.0 * npt * ns);
-      k_f_gather<<<nb(npt * ns, bs), bs, 0, s>>>(w.rhs[PL.ngrid - 1], nprob, ws.rhs[PL.ngrid - 1], ns, ws.idx, npt);
-      after_launch(c);
-    }
-    // the exact solve runs on the auxiliary stream, beside the FP32 cycles
-    EK_CUDA(cudaEventRecord(c.ev_fork, s));
-    EK_CUDA(cudaStreamWaitEvent(c.aux_stream, c.ev_fork, 0));
-    if (c.timing) {
-      // the per-kernel timer records events around each launch: no graph
-      c.stream = c.aux_stream;
-      try {
-        mg_exact_enqueue(c, ws, ns, ws.kx2, kSingularMaxCycles, false);
-      } catch (...) {
-        c.stream = s;
-        throw;
-      }
-      c.stream = s;
-    } else {
-      // its ~1,500 launches (a fixed schedule: no host polling) as one CUDA
-      // graph, captured the first time and again when the work arrays or the
-      // plan change
-      const void *key[3] = {ws.pool, PL.ops_dev, PL.lv.empty() ? nullptr : PL.lv[0].cof};
-      if (!c.sing_exec || c.sing_ns != ns || key[0] != c.sing_key[0] || key[1] != c.sing_key[1] ||
-          key[2] != c.sing_key[2]) {
-        sing_graph_reset(c);
-        const long long l0 = c.launches;
-        EK_CUDA(cudaStreamBeginCapture(c.aux_stream, cudaStreamCaptureModeThreadLocal));
-        c.stream = c.aux_stream;
-        try {
-          mg_exact_enqueue(c, ws, ns, ws.kx2, kSingularMaxCycles, false);
-        } catch (...) {
-          c.stream = s;
-          cudaGraph_t g = nullptr;
-          cudaStreamEndCapture(c.aux_stream, &g);
-          if (g) cudaGraphDestroy(g);
-          throw;
-        }
-        c.stream = s;
-        EK_CUDA(cudaStreamEndCapture(c.aux_stream, &c.sing_graph));
-        EK_CUDA(cudaGraphInstantiate(&c.sing_exec, c.sing_graph, 0));
-        c.sing_launches = c.launches - l0;
-        c.launches = l0;
-        c.sing_ns = ns;
-        for (int t = 0; t < 3; ++t) c.sing_key[t] = key[t];
-      }
-      EK_CUDA(cudaGraphLaunch(c.sing_exec, c.aux_stream));
-      c.launches += c.sing_launches;
-    }
-    EK_CUDA(cudaEventRecord(c.ev_join, c.aux_stream));
-  }
+  if (ns > 0) mg_null_project(c, w.rhs[PL.ngrid - 1], nprob, kx2_dev);
   FastDev g = make_fastdev(c, nprob, kx2_dev);
 
   {
     KScope ks(c, KC_MG_SETUP, 8.0 * (PL.nfx + 2) * (PL.nfy + 2) * nprob * 2);
     EK_CUDA(cudaMemsetAsync(w.flags, 0, sizeof(int) * (2 * w.pmax + 4), s));
     EK_CUDA(cudaMemsetAsync(w.red, 0, sizeof(double) * (6 * w.pmax + 8), s));
-    if (ns > 0) {
-      k_f_mark<<<1, 128, 0, s>>>(w.done, c.mgs.idx, ns);
-      after_launch(c);
-    }
     const size_t nph = (size_t)(PL.nfx + 2) * (PL.nfy + 2) * nprob;
     EK_CUDA(cudaMemsetAsync(g.phh, 0, sizeof(float) * nph, s));
     EK_CUDA(cudaMemsetAsync(g.phl, 0, sizeof(float) * nph, s));
@@ -1182,14 +1087,7 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
     k_f_phif<<<dim3(pch, PL.nfy), dim3(32, kRY), 0, s>>>(g);
     after_launch(c);
   }
-  if (ns > 0) {
-    EK_CUDA(cudaStreamWaitEvent(s, c.ev_join, 0));
-    rs = mg_exact_stats(c, c.mgs, ns, &Ss);
-    if (rs != EK_OK && rs != EK_ERR_NOT_CONVERGED) return rs;
-    KScope ks(c, KC_MG_SETUP, 16.0 * npt * ns);
-    k_f_scatter<<<nb(npt * ns, bs), bs, 0, s>>>(c.mgs.phif, ns, w.phif, nprob, c.mgs.idx, npt);
-    after_launch(c);
-  }
+  if (ns > 0) mg_null_mean(c, w.phif, nprob, kx2_dev);
   std::vector<int> cyc(nprob), done(nprob);
   std::vector<double> meas(6 * nprob);
   EK_CUDA(cudaMemcpyAsync(cyc.data(), w.cycles, sizeof(int) * nprob, cudaMemcpyDeviceToHost, s));
@@ -1198,20 +1096,14 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
   EK_CUDA(cudaStreamSynchronize(s));
   ek_mg_stats S{};
   S.nprob = nprob;
-  // cycle counts over the non-singular problems when there are any: the
-  // kx^2 = 0 ones always run MUDPACK's capped cycles
-  S.min_cycles = (nprob > ns) ? (1 << 30) : Ss.min_cycles;
-  S.max_cycles = (nprob > ns) ? 0 : Ss.max_cycles;
-  S.n_not_converged = Ss.n_not_converged;
-  S.max_relchange = Ss.max_relchange;
-  S.max_residual = Ss.max_residual;
+  S.min_cycles = nprob ? (1 << 30) : 0;
   double csum = 0.0, rsum = 0.0;
   for (int p = 0; p < nprob; ++p) {
-    if (is_sing[p]) continue;
     S.min_cycles = std::min(S.min_cycles, cyc[p]);
     S.max_cycles = std::max(S.max_cycles, cyc[p]);
     if (done[p] != 1) S.n_not_converged++;
     S.max_residual = std::max(S.max_residual, meas[6 * p + 4]);
+    if (is_sing[p]) continue;
     csum += cyc[p];
     rsum += guessed ? meas[6 * p + 5] : 1.0;
   }

@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import warnings
 
 import numpy as np
 
@@ -27,6 +28,7 @@ EXPORTS = [
     "ekgpu_set_metrics", "ekgpu_metrics_from_grid", "ekgpu_upload_state", "ekgpu_download_state",
     "ekgpu_get_field", "ekgpu_put_field", "ekgpu_rk_substep", "ekgpu_step", "ekgpu_ensemble_step", "ekgpu_rem_div",
     "ekgpu_poisson_batch", "ekgpu_poisson_batch_device", "ekgpu_last_divergence", "ekgpu_last_mg_stats",
+    "ekgpu_mg_counters",
     "ekgpu_launch_count", "ekgpu_set_timing", "ekgpu_get_timing", "ekgpu_timing_class_name",
     "ekgpu_fft_x_to_fourier", "ekgpu_fft_x_to_physical", "ekgpu_fft_x_to_fourier_noalloc",
     "ekgpu_sponge_profiles", "ekgpu_set_sponge", "ekgpu_set_time", "ekgpu_get_time",
@@ -114,6 +116,7 @@ def load_library():
     L.ekgpu_poisson_batch_device.argtypes = [V, V, V, V, C.c_int, C.POINTER(EkMgStats)]
     L.ekgpu_last_divergence.argtypes = [V, _D]
     L.ekgpu_last_mg_stats.argtypes = [V, C.POINTER(EkMgStats)]
+    L.ekgpu_mg_counters.argtypes = [V, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     L.ekgpu_launch_count.argtypes = [V]
     L.ekgpu_launch_count.restype = C.c_longlong
     L.ekgpu_set_timing.argtypes = [V, C.c_int]
@@ -405,17 +408,34 @@ class DuctSolver:
         self._check(self._L.ekgpu_put_field(self._h, f, as_ptr(a)))
 
     # -- the reference operations ---------------------------------------------
+    # EK_ERR_NOT_CONVERGED (a projection problem stopped at mg_maxcy above
+    # the residual rule's tolerance) leaves a complete, valid state: these
+    # calls return the code and warn instead of raising.
+    def _solve_status(self, st):
+        self._check(st, allow=(3,))
+        if st == 3:
+            warnings.warn(f"EK_ERR_NOT_CONVERGED: {self._L.ekgpu_last_error(self._h).decode()}", RuntimeWarning,
+                          stacklevel=3)
+        return st
+
     def rk_duct(self, rk_step: int):
         """RK_DUCT: one RK3 substep (duct.F90:237-2469)."""
-        return self._check(self._L.ekgpu_rk_substep(self._h, rk_step))
+        return self._solve_status(self._L.ekgpu_rk_substep(self._h, rk_step))
 
     def step(self, nsteps: int = 1):
         """nsteps times DO RK_STEP=1,3; CALL RK_DUCT (diablo.F90:152-154)."""
-        return self._check(self._L.ekgpu_step(self._h, nsteps))
+        return self._solve_status(self._L.ekgpu_step(self._h, nsteps))
 
     def rem_div_curv(self):
         """REM_DIV_CURV: projection of the current state (duct.F90:2472-2818)."""
-        return self._check(self._L.ekgpu_rem_div(self._h))
+        return self._solve_status(self._L.ekgpu_rem_div(self._h))
+
+    def mg_counters(self):
+        """(real Poisson problems solved, of them stopped at the cycle cap)
+        since the context was created."""
+        a, b = C.c_longlong(), C.c_longlong()
+        self._check(self._L.ekgpu_mg_counters(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def multigrid_mudpack(self, rhs: np.ndarray, kx2: np.ndarray):
         """Batched MULTIGRID_MUDPACK: rhs[nprob, NY+2, NZ+2] (MUDPACK grid,
@@ -479,9 +499,10 @@ def ensemble_step(members, nsteps: int = 1, raise_on_error: bool = True) -> list
     codes = [int(status[i]) for i in range(n)]
     if r and raise_on_error:
         for m, c in zip(members, codes):
-            if c:
+            if c and c != 3:  # NOT_CONVERGED leaves the member's state valid
                 m._check(c)
-        raise EkError(r, "ekgpu_ensemble_step: bad arguments")
+        if any(c not in (0, 3) for c in codes) or not codes:
+            raise EkError(r, "ekgpu_ensemble_step: bad arguments")
     return codes
 
 

@@ -170,7 +170,9 @@ class Workload:
         p.mg_stop = mg_stop
         p.mg_tol = MUDPACK_TOLMAX if mg_stop == EK_MG_STOP_RELCHANGE else self.mg_tol
         if mg_stop == EK_MG_STOP_RESIDUAL:
-            p.mg_maxcy = 60
+            # a cap well above the ~55 W-cycles MUDPACK's point smoother needs
+            # at 1e-8 on these grids (the mixed solver needs <= 7)
+            p.mg_maxcy = 100
         if self.les:
             p.les, p.create_new_flow = 1, 0
         return p

@@ -41,7 +41,8 @@ typedef enum ek_status {
   EK_ERR_CUDA = 2,           /* a CUDA call failed                              */
   EK_ERR_NOT_CONVERGED = 3,  /* multigrid hit its cycle cap; phi still returned */
   EK_ERR_NAN = 4,            /* divergence is NaN (reference: STOP 'DIV is a NaN', duct.F90:2811) */
-  EK_ERR_TIMEOUT = 5,        /* a bounded device wait expired                   */
+  EK_ERR_TIMEOUT = 5,        /* reserved: no kernel of this library waits on a flag,
+                                a peer or a barrier, so no call returns it        */
   EK_ERR_STATE = 6,          /* call order violated (e.g. step before metrics)  */
   EK_ERR_IO = 7              /* restart file missing, unreadable or malformed  */
 } ek_status;
@@ -54,9 +55,14 @@ enum { EK_YMIN = 0, EK_YMAX = 1, EK_ZMIN = 2, EK_ZMAX = 3 };
 enum {
   EK_MG_STOP_RELCHANGE = 0,  /* MUDPACK rule: max|phi_k - phi_{k-1}| / max|phi_k| <= tol (mud2cr.f:301-326) */
   EK_MG_STOP_RESIDUAL = 1    /* ||b - A phi||_2 / ||b||_2 <= tol, per real 2-D problem.  A problem with
-                                kx^2 = 0 (singular: periodic x, Neumann y; its right-hand side need
-                                not be compatible) keeps MULTIGRID_MUDPACK's own rule instead:
-                                REAL*4 1e-6 relative change, at most 6 cycles                      */
+                                kx^2 = 0 (singular: periodic x, Neumann y, A 1 = 0) is made well
+                                posed first -- not a reference behaviour, whose MUDPACK iterate for
+                                that mode is whatever 6 cycles leave: b loses its component along the
+                                left null vector z of the operator (A^T z = 0, computed once per
+                                metric set), b' = b - (z.b / z.z) z, the tolerance applies to
+                                ||b' - A phi|| / ||b'||, and phi is shifted to zero mean over the
+                                (NZ+2)(NY+2) points.  The part z.b of the divergence is the one no
+                                pressure can remove; it stays in the divergence check.             */
 };
 
 /* Run parameters: the values the Fortran driver reads from input.dat and
@@ -66,7 +72,8 @@ typedef struct ek_params {
   int nx, ny, nz;            /* NX (spanwise, Fourier), NY, NZ interior counts          */
   double lx;                 /* LX, spanwise period: KX(i) = 2*pi*i/LX                 */
   double nu;                 /* NU                                                      */
-  double delta_t;            /* DELTA_T (fixed; VARIABLE_DT is not supported)           */
+  double delta_t;            /* DELTA_T; with variable_dt = 1 COURANT_CURV_MPI resets it
+                                (read it back with ekgpu_get_time)                      */
   double f0;                 /* F_0, Coriolis parameter                                 */
   double wbulk0;             /* WBULK0 (geostrophic wind of the Coriolis term)          */
   int f_type;                /* F_TYPE: 1 constant PX0, 2 oscillatory                   */
@@ -88,9 +95,10 @@ typedef struct ek_params {
   double mg_tol;             /* tolmax: reference REAL*4 10.0**(-6) widened to REAL*8   */
   int quirk_phi_fp32;        /* Q1: CMPLX(P_TMP2,P_TMP) rounds phi to REAL*4 (duct.F90:2664) */
   int mg_fast;               /* 0: MUDPACK's own iteration (FP64, point smoother, the parity
-                                default); 1: mixed precision -- FP64 residual and update around FP32
-                                V-cycles with a y-line smoother, same discrete operator, needs
-                                mg_stop = EK_MG_STOP_RESIDUAL; mg_maxcy caps the corrections   */
+                                default); 1: mixed precision -- float-float residual and update
+                                around FP32 V-cycles with an alternating-direction line smoother,
+                                same discrete operator, needs mg_stop = EK_MG_STOP_RESIDUAL;
+                                mg_maxcy caps the corrections                                   */
   int sponge_type;           /* SPONGE_TYPE: 0 none, 1 parabolic, 2 exponential profiles;
                                 sponge_th (duct.F90:3196-3362) runs when != 0 and N_TH >= 1 */
   int les;                   /* LES: dynamic-Smagorinsky subgrid terms of les_chan /
@@ -364,11 +372,18 @@ int ekgpu_get_field(ek_ctx *ctx, int field, double *out);
 int ekgpu_put_field(ek_ctx *ctx, int field, const double *in);
 
 /* One RK substep rk_step in {1,2,3}: RK_DUCT (duct.F90:237-2469) including
- * REM_DIV_CURV and the pressure update (duct.F90:2455-2466). */
+ * REM_DIV_CURV and the pressure update (duct.F90:2455-2466).  Under
+ * EK_MG_STOP_RESIDUAL, EK_ERR_NOT_CONVERGED when a projection problem reached
+ * mg_maxcy above the tolerance: the substep is complete and its state valid.
+ * Under EK_MG_STOP_RELCHANGE such problems are counted (ekgpu_last_mg_stats,
+ * ekgpu_mg_counters) but the call returns EK_OK, as MULTIGRID_MUDPACK ignores
+ * mud2cr's ierror (mg_solver2d.F90:195-199). */
 int ekgpu_rk_substep(ek_ctx *ctx, int rk_step);
 
 /* nsteps full RK3 steps: the driver loop DO RK_STEP=1,3; CALL RK_DUCT
- * (diablo.F90:152-154), repeated; advances params.time by DELTA_T per step. */
+ * (diablo.F90:152-154), repeated; advances params.time by DELTA_T per step.
+ * A substep that returns EK_ERR_NOT_CONVERGED does not stop the loop; the
+ * call returns it after the last step. */
 int ekgpu_step(ek_ctx *ctx, int nsteps);
 
 /* An ensemble of independent runs, each with its own sizes, parameters and
@@ -385,7 +400,8 @@ int ekgpu_step(ek_ctx *ctx, int nsteps);
 int ekgpu_ensemble_step(ek_ctx *const *members, int n, int nsteps, int *status);
 
 /* The projection alone: REM_DIV_CURV (duct.F90:2472-2818) on the current
- * state, leaving phi in CR1 (as the reference leaves it in CR1X). */
+ * state, leaving phi in CR1 (as the reference leaves it in CR1X).  Status as
+ * for ekgpu_rk_substep. */
 int ekgpu_rem_div(ek_ctx *ctx);
 
 /* Batched per-kx Poisson: for each problem p, solve the 9-point operator of
@@ -411,6 +427,11 @@ int ekgpu_last_divergence(ek_ctx *ctx, double *div);
 
 /* Stats of the last multigrid call made by a substep or poisson call. */
 int ekgpu_last_mg_stats(ek_ctx *ctx, ek_mg_stats *stats);
+
+/* Real 2-D Poisson problems solved since the context was created, and how
+ * many of them stopped at the cycle cap before their rule was met (either
+ * rule).  No counterpart in the reference, which ignores mud2cr's ierror. */
+int ekgpu_mg_counters(ek_ctx *ctx, long long *solved, long long *not_converged);
 
 /* Context-free batched x-transforms on device memory: the
  * FFT_X_TO_FOURIER_OP / FFT_X_TO_PHYSICAL_OP pair the reference calls
@@ -441,7 +462,8 @@ int ekgpu_fft_x_to_physical(int nx, int nkx, long nlines, const double *in_dev, 
  * capture.  Every call rewrites the whole table before using it, so nothing
  * has to start at zero; but all calls share the one table, so calls that
  * overlap on the GPU (e.g. on two streams) race and must be ordered by the
- * caller. */
+ * caller.  The looked-up address is kept for the life of the process: do not
+ * use this library across a cudaDeviceReset. */
 int ekgpu_fft_x_to_fourier_noalloc(int nx, int nkx, long nlines, const double *in_dev, double *out_dev,
                                    void *stream);
 

@@ -86,6 +86,9 @@ void ekref_thomas_real(int nsys, int n, double *a, double *b, double *c, double 
 /* Apply the finest-level 9-point operator of dismd2cr (with ce = -kx2*J)
  * to phi(0:NZ+1,0:NY+1): out = A phi on the MUDPACK grid. */
 int ekref_mg_apply(ekref_ctx *ctx, double kx2, const double *phi, double *out);
+/* Left null vector z of the finest kx = 0 operator (A^T z = 0, |z| = 1),
+ * (NZ+2)*(NY+2) doubles in the MUDPACK grid layout. */
+int ekref_mg_left_null(ekref_ctx *ctx, double *z);
 
 #ifdef __cplusplus
 }

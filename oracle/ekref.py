@@ -59,6 +59,7 @@ def lib():
         L.ekref_fft_c2r.argtypes = [C.c_int, C.c_int, C.c_long, _D, _D]
         L.ekref_thomas_real.argtypes = [C.c_int, C.c_int, _D, _D, _D, _D]
         L.ekref_mg_apply.argtypes = [C.c_void_p, C.c_double, _D, _D]
+        L.ekref_mg_left_null.argtypes = [C.c_void_p, _D]
         L.ekref_save_stats.argtypes = [C.c_void_p, C.POINTER(EkStats)]
         L.ekref_les_metrics_from_grid.argtypes = [P, _D, _D] + [_D] * 6
         L.ekref_set_les_metrics.argtypes = [C.c_void_p] + [_D] * 6
@@ -203,6 +204,12 @@ class Oracle:
         out = np.zeros_like(phi)
         self._check(lib().ekref_mg_apply(self._h, kx2, as_ptr(phi), as_ptr(out)))
         return out
+
+    def mg_left_null(self):
+        """Left null vector z of the finest kx = 0 operator, [NY+2, NZ+2]."""
+        z = np.zeros((self.p.ny + 2, self.p.nz + 2))
+        self._check(lib().ekref_mg_left_null(self._h, as_ptr(z)))
+        return z
 
     def divergence(self):
         d = C.c_double()

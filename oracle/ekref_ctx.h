@@ -100,6 +100,9 @@ struct ekref_ctx {
   std::vector<double> U1, U2, U3, TH, R1, R2, R3, RTH, S1, S2, U2b, U3b;
   std::unique_ptr<FFT> fft;
   ekref::MudOpts mud{};
+  // left null vector of the finest kx = 0 operator (the residual rule's
+  // well-posed kx = 0 solve); built on first use, cleared with the metrics
+  std::vector<double> mg_z;
   double last_div = 0.0;
   ek_mg_stats last_stats{};
   // LES (les_chan / les_chan_th): the module arrays they keep between

@@ -361,11 +361,26 @@ void Mud2cr::kcymd2cr(int kcur) {
 }
 
 // mud2cr1 (mud2cr.f:211-338) with swk2 (mudcom.f:32-59).
-MudResult Mud2cr::solve(const double *rhsf, double *phif, bool singular) {
+MudResult Mud2cr::solve(const double *rhsf, double *phif, bool singular, const double *z) {
   MudResult r;
   const int nfx = nfx_, nfy = nfy_;
+  const size_t nf = (size_t)nfx * nfy;
   auto PF = [&](int i, int j) -> double & { return phif[(size_t)(j - 1) * nfx + (i - 1)]; };
   Level &F = lv_[ngrid_ - 1];
+  // the residual rule's well-posed kx = 0 problem: b' = b - (z.b / z.z) z
+  const bool wellposed = singular && o_.stop_rule == 1;
+  std::vector<double> bproj;
+  if (wellposed) {
+    double zb = 0.0, zz = 0.0;
+    for (size_t t = 0; t < nf; ++t) {
+      zb += z[t] * rhsf[t];
+      zz += z[t] * z[t];
+    }
+    const double a = (zz > 0.0) ? zb / zz : 0.0;
+    bproj.resize(nf);
+    for (size_t t = 0; t < nf; ++t) bproj[t] = rhsf[t] - a * z[t];
+    rhsf = bproj.data();
+  }
   for (int j = 1; j <= nfy; ++j)
     for (int i = 1; i <= nfx; ++i) {
       F.P(i, j) = PF(i, j);
@@ -392,12 +407,9 @@ MudResult Mud2cr::solve(const double *rhsf, double *phif, bool singular) {
       for (int i = 1; i <= nfx; ++i) bnorm += F.C(i, j, 10) * F.C(i, j, 10);
     bnorm = std::sqrt(bnorm);
   }
-  // Under the residual rule a singular problem keeps MULTIGRID_MUDPACK's own
-  // rule: REAL*4 10.0**(-6) relative change, at most 6 cycles
-  // (mg_solver2d.F90:146-199).
-  const bool rel = (o_.stop_rule == 0 || singular);
-  const double tol = (o_.stop_rule == 0) ? o_.tol : (double)1.0e-6f;
-  const int maxcy = (o_.stop_rule == 0 || !singular) ? o_.maxcy : std::min(o_.maxcy, 6);
+  const bool rel = (o_.stop_rule == 0);
+  const double tol = o_.tol;
+  const int maxcy = o_.maxcy;
   for (int iter = 1; iter <= maxcy; ++iter) {
     r.cycles = iter;
     kcymd2cr(kcur);
@@ -436,7 +448,122 @@ MudResult Mud2cr::solve(const double *rhsf, double *phif, bool singular) {
   }
   for (int j = 1; j <= nfy; ++j)
     for (int i = 1; i <= nfx; ++i) PF(i, j) = F.P(i, j);
+  if (wellposed) {
+    // the solution is defined up to a constant: zero mean
+    double m = 0.0;
+    for (size_t t = 0; t < nf; ++t) m += phif[t];
+    m = m / (double)nf;
+    for (size_t t = 0; t < nf; ++t) phif[t] = phif[t] - m;
+  }
   return r;
+}
+
+void Mud2cr::finest_coo(std::vector<int> &row, std::vector<int> &col, std::vector<double> &val) const {
+  const Level &F = lv_[ngrid_ - 1];
+  const int nx = nfx_, ny = nfy_;
+  static const int di[9] = {1, 1, 0, -1, -1, -1, 0, 1, 0}, dj[9] = {0, 1, 1, 1, 0, -1, -1, -1, 0};
+  row.clear();
+  col.clear();
+  val.clear();
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i)
+      for (int l = 0; l < 9; ++l) {
+        const double v = F.cof[((size_t)l * ny + (j - 1)) * nx + (i - 1)];
+        int ii = i + di[l];
+        const int jj = j + dj[l];
+        if (jj < 1 || jj > ny) continue;  // zero after the Neumann folding
+        if (v == 0.0) continue;
+        if (ii == 0) ii = nx - 1;
+        if (ii == nx + 1) ii = 2;
+        row.push_back((j - 1) * nx + (i - 1));
+        col.push_back((jj - 1) * nx + (ii - 1));
+        val.push_back(v);
+      }
+}
+
+std::vector<double> Mud2cr::left_null() const {
+  const int nx = nfx_, ny = nfy_;
+  const long n = (long)nx * ny;
+  // unknowns ordered row by row (j outer); inside a row the periodic ring
+  // 1, nx, 2, nx-1, 3, ... so that every x-coupling (the wrap included)
+  // spans at most 3 places and the band is nx + 3 wide
+  std::vector<int> pos(nx + 1);
+  const int L = nx - 2, left = (L + 1) / 2;
+  pos[1] = 0;
+  pos[nx] = 1;
+  for (int i = 2; i <= nx - 1; ++i) pos[i] = (i - 2 < left) ? 2 + 2 * (i - 2) : 3 + 2 * ((nx - 1) - i);
+  auto q = [&](int u) { return (long)(u / nx) * nx + pos[u % nx + 1]; };
+  std::vector<int> r, c;
+  std::vector<double> v;
+  finest_coo(r, c, v);
+  const long pin = q(((ny + 1) / 2 - 1) * nx + (nx + 1) / 2 - 1);
+  // M = A^T: entry (q(col), q(row)); the pinned equation becomes z = 1
+  int kl = 0, ku = 0;
+  for (size_t t = 0; t < v.size(); ++t) {
+    const long a = q(c[t]), b = q(r[t]);
+    if (a == pin) continue;
+    kl = std::max<int>(kl, (int)(a - b));
+    ku = std::max<int>(ku, (int)(b - a));
+  }
+  const int kv = kl + ku, ldab = 2 * kl + ku + 1;
+  std::vector<double> ab((size_t)ldab * n, 0.0);
+  auto AB = [&](long i, long j) -> double & { return ab[(size_t)j * ldab + (size_t)(kv + i - j)]; };
+  for (size_t t = 0; t < v.size(); ++t) {
+    const long a = q(c[t]), b = q(r[t]);
+    if (a == pin) continue;
+    AB(a, b) += v[t];
+  }
+  AB(pin, pin) = 1.0;
+  // LU with partial pivoting of the band (the unblocked LAPACK gbtf2 scheme)
+  std::vector<long> ipiv(n);
+  long ju = 0;
+  for (long j = 0; j < n; ++j) {
+    const long km = std::min<long>(kl, n - 1 - j);
+    long jp = 0;
+    double best = std::fabs(AB(j, j));
+    for (long t = 1; t <= km; ++t)
+      if (std::fabs(AB(j + t, j)) > best) {
+        best = std::fabs(AB(j + t, j));
+        jp = t;
+      }
+    ipiv[j] = j + jp;
+    ju = std::max(ju, std::min<long>(j + ku + jp, n - 1));
+    if (jp != 0)
+      for (long cc = j; cc <= ju; ++cc) std::swap(AB(j, cc), AB(j + jp, cc));
+    const double piv = AB(j, j);
+    if (piv == 0.0) continue;  // cannot happen for a connected grid
+    for (long t = 1; t <= km; ++t) AB(j + t, j) = AB(j + t, j) / piv;
+    const double *lcol = &AB(j + 1, j);
+#pragma omp parallel for schedule(static) if (km * (ju - j) > 20000)
+    for (long cc = j + 1; cc <= ju; ++cc) {
+      const double m = AB(j, cc);
+      if (m == 0.0) continue;
+      double *dst = &AB(j + 1, cc);
+      for (long t = 0; t < km; ++t) dst[t] = dst[t] - lcol[t] * m;
+    }
+  }
+  // solve M y = e_pin
+  std::vector<double> y(n, 0.0);
+  y[pin] = 1.0;
+  for (long j = 0; j < n; ++j) {
+    if (ipiv[j] != j) std::swap(y[j], y[ipiv[j]]);
+    const long km = std::min<long>(kl, n - 1 - j);
+    for (long t = 1; t <= km; ++t) y[j + t] = y[j + t] - AB(j + t, j) * y[j];
+  }
+  for (long j = n - 1; j >= 0; --j) {
+    y[j] = y[j] / AB(j, j);
+    const double yj = y[j];
+    for (long i = std::max<long>(0, j - kv); i < j; ++i) y[i] = y[i] - AB(i, j) * yj;
+  }
+  std::vector<double> z(n);
+  double zz = 0.0;
+  for (long u = 0; u < n; ++u) {
+    z[u] = y[q(u)];
+    zz += z[u] * z[u];
+  }
+  const double s = 1.0 / std::sqrt(zz);
+  for (long u = 0; u < n; ++u) z[u] = z[u] * s;
+  return z;
 }
 
 void Mud2cr::apply_finest(const double *phif, double *out) const {

@@ -36,11 +36,25 @@ class Mud2cr {
   void discretize(const CoefFn &coef);
   // intl=1 call: rhsf, phif are (nfx, nfy) column-major; phif is input guess
   // (the reference always passes zeros) and output solution.
-  // singular: the problem has ce = 0 (kx = 0, pure Neumann/periodic); under
-  // the residual rule it uses the relative-change test instead.
-  MudResult solve(const double *rhsf, double *phif, bool singular = false);
+  // singular: the problem has ce = 0 (kx = 0, pure Neumann/periodic).  Under
+  // the relative-change rule it runs as MUDPACK does.  Under the residual
+  // rule it is made well posed (not a reference behaviour): the right-hand
+  // side's component along the left null vector z of the finest operator
+  // (A^T z = 0, from left_null) is removed, b' = b - (z.b / z.z) z, the
+  // k-cycles run until ||b' - A phi|| <= tol ||b'||, and the solution is
+  // shifted to zero mean over the nfx x nfy points.  z must then be given.
+  MudResult solve(const double *rhsf, double *phif, bool singular = false, const double *z = nullptr);
   // out = A phi at the finest level on (1..nfx, 1..nfy).
   void apply_finest(const double *phif, double *out) const;
+  // The finest operator as coordinate triplets over the nfx*nfy unknowns
+  // (unknown (i, j) -> (j-1)*nfx + i-1): the periodic ghosts of columns 0
+  // and nfx+1 folded onto i = nfx-1 and i = 2, the y ghosts (zero couplings
+  // after the Neumann folding) dropped.
+  void finest_coo(std::vector<int> &row, std::vector<int> &col, std::vector<double> &val) const;
+  // Left null vector of the finest operator as last discretized (kx = 0):
+  // A^T z = 0 with |z|_2 = 1, by a banded LU with partial pivoting of A^T
+  // with the equation of the centre point replaced by z = 1 there.
+  std::vector<double> left_null() const;
   int nfx() const { return nfx_; }
   int nfy() const { return nfy_; }
   int ngrid() const { return ngrid_; }

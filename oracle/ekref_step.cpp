@@ -295,6 +295,7 @@ extern "C" int ekref_set_metrics(ekref_ctx *c, const ek_metrics *m) {
   cp2(c->cjob_11, m->cjob_11, 2 * n2); cp2(c->cjob_12, m->cjob_12, 2 * n2);
   cp2(c->cjob_21, m->cjob_21, 2 * n2); cp2(c->cjob_22, m->cjob_22, 2 * n2);
   cp2(c->th_bar, m->th_bar, n2);
+  c->mg_z.clear();
   c->have_metrics = true;
   return EK_OK;
 }
@@ -614,9 +615,23 @@ static ekref::CoefFn make_cofcr(const ekref_ctx *c, double kx2) {
 }
 
 // rhs/phi: nprob problems of (NZ+2)*(NY+2) doubles (MUDPACK grid, x = K fastest).
+// The left null vector of the finest kx = 0 operator, built once per metric set.
+static const double *mg_left_null(ekref_ctx *c) {
+  if (c->mg_z.empty()) {
+    ekref::Mud2cr mg(c->mud);
+    mg.discretize(make_cofcr(c, 0.0));
+    c->mg_z = mg.left_null();
+  }
+  return c->mg_z.data();
+}
+
 static int mg_batch(ekref_ctx *c, const double *rhs, double *phi, const double *kx2, int nprob, ek_mg_stats *st) {
   const size_t n = (size_t)(c->NZ + 2) * (c->NY + 2);
   std::vector<ekref::MudResult> res(nprob);
+  const double *z = nullptr;
+  if (c->mud.stop_rule == 1)
+    for (int p = 0; p < nprob; ++p)
+      if (kx2[p] == 0.0) z = mg_left_null(c);
 #pragma omp parallel
   {
     ekref::Mud2cr mg(c->mud);
@@ -624,7 +639,7 @@ static int mg_batch(ekref_ctx *c, const double *rhs, double *phi, const double *
     for (int p = 0; p < nprob; ++p) {
       mg.discretize(make_cofcr(c, kx2[p]));
       std::fill(phi + p * n, phi + (p + 1) * n, 0.0);  // P_TMP = 0
-      res[p] = mg.solve(rhs + p * n, phi + p * n, kx2[p] == 0.0);
+      res[p] = mg.solve(rhs + p * n, phi + p * n, kx2[p] == 0.0, z);
     }
   }
   ek_mg_stats s{};
@@ -653,6 +668,13 @@ extern "C" int ekref_mg_apply(ekref_ctx *c, double kx2, const double *phi, doubl
   ekref::Mud2cr mg(c->mud);
   mg.discretize(make_cofcr(c, kx2));
   mg.apply_finest(phi, out);
+  return EK_OK;
+}
+
+extern "C" int ekref_mg_left_null(ekref_ctx *c, double *z) {
+  if (!c->have_metrics) return fail(c, EK_ERR_STATE, "metrics not set");
+  const double *v = mg_left_null(c);
+  std::copy(v, v + c->mg_z.size(), z);
   return EK_OK;
 }
 

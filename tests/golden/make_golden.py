@@ -7,8 +7,8 @@ directions to 81 x 33 (both still MUDPACK sizes p*2^k+1), and the divergence
 values the reference printed after each projection (rundir_unst/log), kept as
 a magnitude check.
 
-Run in a container that has the reference mounted:
-    python tests/golden/make_golden.py /root/reference
+Run where the reference tree is available, with its root as the argument:
+    python tests/golden/make_golden.py <path of the ekman_bl tree>
 """
 import os
 import re
@@ -37,4 +37,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path of the ekman_bl tree>")
+    main(sys.argv[1])

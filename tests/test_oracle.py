@@ -92,6 +92,47 @@ def test_multigrid_reference_stopping_rule():
     assert code == 0 and st0["max_cycles"] == 1 and not phi.any()
 
 
+@pytest.mark.parametrize("case", ["small", "sheared", "refgrid"])
+def test_left_null_vector_of_the_kx0_operator(case):
+    """z with A^T z = 0 for the singular kx = 0 operator: z . (A phi) = 0
+    for any phi, |z| = 1; A 1 = 0 holds for the same operator."""
+    p, xp, yp, _ = {"small": small_case, "sheared": sheared_case, "refgrid": refgrid_case}[case]()
+    o = ekref.Oracle(p, ekref.metrics_from_grid(p, xp, yp))
+    z = o.mg_left_null()
+    assert abs(np.linalg.norm(z) - 1.0) < 1e-12
+    rng = np.random.default_rng(8)
+    for _ in range(3):
+        a = o.mg_apply(0.0, rng.standard_normal(z.shape))
+        assert abs((z * a).sum()) <= 1e-14 * np.linalg.norm(a)
+    assert np.abs(o.mg_apply(0.0, np.ones(z.shape))).max() < 1e-10
+
+
+@pytest.mark.parametrize("case", ["small", "sheared", "refgrid"])
+def test_wellposed_kx0_solve(case):
+    """Under the residual rule the kx = 0 problem is solved as a well-posed
+    one: b' = b - (z.b) z, ||b' - A phi|| <= tol ||b'||, zero-mean phi, the
+    same cycle cap as every problem.  Adding a compatible part to b moves phi
+    by the exact solution of that part."""
+    p, xp, yp, _ = {"small": small_case, "sheared": sheared_case, "refgrid": refgrid_case}[case]()
+    p.mg_stop, p.mg_tol, p.mg_maxcy = 1, 1e-10, 200
+    o = ekref.Oracle(p, ekref.metrics_from_grid(p, xp, yp))
+    z = o.mg_left_null()
+    rng = np.random.default_rng(9)
+    b = rng.standard_normal((1, p.ny + 2, p.nz + 2))
+    phi, st, code = o.poisson(b, np.array([0.0]))
+    assert code == 0 and st["n_not_converged"] == 0, st
+    bp = b[0] - (z * b[0]).sum() * z
+    r = bp - o.mg_apply(0.0, phi[0])
+    assert np.linalg.norm(r) <= 1.0001e-10 * np.linalg.norm(bp)
+    assert abs(phi[0].mean()) < 1e-12 * np.abs(phi[0]).max()
+    # a manufactured zero-mean solution comes back
+    want = rng.standard_normal(z.shape)
+    want -= want.mean()
+    got, st2, code2 = o.poisson(o.mg_apply(0.0, want)[None], np.array([0.0]))
+    assert code2 == 0
+    assert np.linalg.norm(got[0] - want) / np.linalg.norm(want) < 1e-7
+
+
 def test_oracle_steps_keep_divergence_small():
     p, xp, yp, st = small_case(32, 33, 33)
     m = ekref.metrics_from_grid(p, xp, yp)

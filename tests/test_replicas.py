@@ -1,5 +1,5 @@
 """bench.py's N > 1 path: N independent replicas (the duct step does not
-shard; SURVEY's multi-GPU decision), the whole-job value from the slowest
+shard: every rank steps its own copy of the run), the whole-job value from the slowest
 rank.  Two gloo ranks on the CPU stand in for two GPUs."""
 import os
 import socket
