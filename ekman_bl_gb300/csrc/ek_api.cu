@@ -244,6 +244,97 @@ int substep(Ctx &c, int rk) {
   return dv != EK_OK ? dv : projection_status(c, mg);
 }
 
+// ---- whole-step CUDA graphs ------------------------------------------------
+// ekgpu_step runs each RK3 step as one CUDA graph when the step's launches
+// depend on nothing but the context's plan and a few host-side choices (the
+// key below): the mixed solver (its correction cycles loop in conditional
+// while-nodes), a fixed time step, constant mean-pressure forcing, no learned
+// guess or pair collection, the per-kernel timer off.  Statistics and the
+// divergence of each substep are read once, after the step.
+bool step_graph_eligible(const Ctx &c) {
+  const ek_params &p = c.p;
+  return c.step_graphs && !c.timing && p.mg_fast && !p.variable_dt && p.f_type == 1 &&
+         !(c.guess.net && c.guess.use) && !c.guess.sink_x;
+}
+
+// The host-side choices a step's launches depend on: LES active, FIRST_TIME,
+// C_DYN due at RK_STEP 1 (MOD(TIME_STEP, 5) = 0), sponge_th's CU2X reset.
+unsigned long long step_graph_key(const Ctx &c) {
+  const ek_params &p = c.p;
+  const bool reset = p.sponge_type != 0 && p.save_stats_int > 0 && (2 * p.time_step) % p.save_stats_int == 0;
+  return (les_active(c) ? 1ull : 0ull) | (c.les.first_time ? 2ull : 0ull) | (p.time_step % 5 == 0 ? 4ull : 0ull) |
+         (reset ? 8ull : 0ull);
+}
+
+StepGraph &step_graph_capture(Ctx &c, unsigned long long key) {
+  StepGraph sg;
+  sg.key = key;
+  const cudaStream_t saved = c.stream;
+  const long long l0 = c.launches;
+  long long body = 0;
+  c.stream = c.cap_stream;
+  EK_CUDA(cudaStreamBeginCapture(c.cap_stream, cudaStreamCaptureModeThreadLocal));
+  try {
+    for (int rk = 1; rk <= 3; ++rk) {
+      c.graph_slot = rk - 1;
+      c.graph_body_launches = 0;
+      const int st = substep(c, rk);
+      if (st != EK_OK) throw CudaError("step graph: substep " + std::to_string(rk) + " returned " + std::to_string(st));
+      sg.body_launches[rk - 1] = c.graph_body_launches;
+      body += c.graph_body_launches;
+    }
+  } catch (...) {
+    c.graph_slot = -1;
+    c.stream = saved;
+    c.launches = l0;
+    cudaGraph_t junk = nullptr;
+    cudaStreamEndCapture(c.cap_stream, &junk);
+    if (junk) cudaGraphDestroy(junk);
+    throw;
+  }
+  c.graph_slot = -1;
+  c.stream = saved;
+  sg.fixed_launches = c.launches - l0 - body;
+  c.launches = l0;
+  EK_CUDA(cudaStreamEndCapture(c.cap_stream, &sg.graph));
+  if (cudaGraphInstantiate(&sg.exec, sg.graph, 0) != cudaSuccess) {
+    cudaGraphDestroy(sg.graph);
+    throw CudaError("step graph: cudaGraphInstantiate failed");
+  }
+  c.graphs.push_back(sg);
+  return c.graphs.back();
+}
+
+// One step from its graph; late becomes EK_ERR_NOT_CONVERGED when a solve
+// of the step missed the residual rule's tolerance.
+int step_graph_run(Ctx &c, const StepGraph &sg, int &late) {
+  EK_CUDA(cudaGraphLaunch(sg.exec, c.stream));
+  EK_CUDA(cudaMemcpyAsync(c.step_stats_host, c.step_stats_dev, 3 * sizeof(StepStats), cudaMemcpyDeviceToHost,
+                          c.stream));
+  EK_CUDA(cudaStreamSynchronize(c.stream));
+  long long n = sg.fixed_launches;
+  bool nan = false;
+  for (int k = 0; k < 3; ++k) {
+    const StepStats &S = c.step_stats_host[k];
+    n += (long long)S.max_cycles * sg.body_launches[k];
+    c.mg_solved_total += S.nprob;
+    c.mg_nc_total += S.n_not_converged;
+    if (S.n_not_converged && c.p.mg_stop == EK_MG_STOP_RESIDUAL) late = EK_ERR_NOT_CONVERGED;
+    if (S.div != S.div) nan = true;
+  }
+  c.launches += n;
+  const StepStats &L = c.step_stats_host[2];
+  ek_mg_stats st{};
+  st.nprob = L.nprob;
+  st.min_cycles = L.min_cycles;
+  st.max_cycles = L.max_cycles;
+  st.n_not_converged = L.n_not_converged;
+  st.max_residual = L.max_residual;
+  c.last_stats = st;
+  c.last_div = L.div;
+  return nan ? EK_ERR_NAN : EK_OK;
+}
+
 __global__ void k_transpose(const double *in, double *out, int P, long npt, int to_inner) {
   const long n = (long)P * npt;
   for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
@@ -262,6 +353,16 @@ __global__ void k_transpose(const double *in, double *out, int P, long npt, int 
 }  // namespace
 
 namespace ek {
+// Drop every captured step graph (the plan they were captured from changed).
+void step_graphs_clear(Ctx &c) {
+  for (StepGraph &g : c.graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (g.graph) cudaGraphDestroy(g.graph);
+  }
+  c.graphs.clear();
+  c.eager_since_plan = false;
+}
+
 // Sum the recorded per-kernel-class event pairs into kms/kcnt.
 void timing_resolve(Ctx &c) {
   if (c.trec.empty()) return;
@@ -378,6 +479,9 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
   try {
     EK_CUDA(cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking));
     c.stream = c.own_stream;
+    EK_CUDA(cudaStreamCreateWithFlags(&c.cap_stream, cudaStreamNonBlocking));
+    EK_CUDA(cudaStreamCreateWithFlags(&c.cap_stream2, cudaStreamNonBlocking));
+    EK_CUDA(cudaHostAlloc(&c.step_stats_host, 3 * sizeof(StepStats), cudaHostAllocDefault));
     rk_init_attributes();
     fft_init_attributes();
     if (p.les) les_init_attributes();
@@ -464,6 +568,7 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
       c.U3bf = c.U2bf + np;
     }
     c.div_part = dalloc<double>(c, d.NY2);
+    c.step_stats_dev = dalloc<StepStats>(c, 3);
     c.cfl_dt = dalloc<double>(c, 1);
     c.sponge_sig = dalloc<double>(c, d.NY2 + d.NZ2 + 4);
     c.sponge_sig_out = c.sponge_sig + d.NY2;
@@ -490,6 +595,10 @@ void ekgpu_destroy(ek_ctx *h) {
   if (c.mgf_pool) cudaFree(c.mgf_pool);
   if (c.mg.ops_dev) cudaFree(c.mg.ops_dev);
   c.poll.destroy();
+  step_graphs_clear(c);
+  if (c.cap_stream) cudaStreamDestroy(c.cap_stream);
+  if (c.cap_stream2) cudaStreamDestroy(c.cap_stream2);
+  if (c.step_stats_host) cudaFreeHost(c.step_stats_host);
   for (auto &r : c.trec) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : c.evpool) cudaEventDestroy(e);
   if (c.own_stream) cudaStreamDestroy(c.own_stream);
@@ -612,6 +721,7 @@ int ekgpu_set_metrics(ek_ctx *h, const ek_metrics *m) {
     up(c.m.c11, m->cjob_11, 2 * n2); up(c.m.c12, m->cjob_12, 2 * n2);
     up(c.m.c21, m->cjob_21, 2 * n2); up(c.m.c22, m->cjob_22, 2 * n2);
     up(c.m.thbar, m->th_bar, n2);
+    step_graphs_clear(c);  // the plan they were captured from is rebuilt below
     if (!c.m.pg) c.m.pg = dalloc<double>(c, 11 * n2);
     launch_metric_tables(c);
     c.les.tab_ok = false;
@@ -760,11 +870,25 @@ int ekgpu_step(ek_ctx *h, int nsteps) {
     int late = EK_OK;
     for (int n = 0; n < nsteps; ++n) {
       c.p.time_step += 1;
-      for (int rk = 1; rk <= 3; ++rk) {
-        const int st = substep(c, rk);
+      const bool graph = step_graph_eligible(c) && c.eager_since_plan;
+      if (graph) {
+        const unsigned long long key = step_graph_key(c);
+        const StepGraph *sg = nullptr;
+        for (const StepGraph &g : c.graphs)
+          if (g.key == key) sg = &g;
+        if (!sg) sg = &step_graph_capture(c, key);
+        const int st = step_graph_run(c, *sg, late);
         if (st == EK_ERR_NAN) return fail(c, EK_ERR_NAN, "DIV is a NaN");
-        if (st == EK_ERR_NOT_CONVERGED) late = st;
-        else if (st != EK_OK) return st;
+        if (st != EK_OK) return st;
+      } else {
+        for (int rk = 1; rk <= 3; ++rk) {
+          const int st = substep(c, rk);
+          if (st == EK_ERR_NAN) return fail(c, EK_ERR_NAN, "DIV is a NaN");
+          if (st == EK_ERR_NOT_CONVERGED) late = st;
+          else if (st != EK_OK) return st;
+        }
+        // lazily allocated buffers exist now, outside any capture
+        c.eager_since_plan = true;
       }
       c.p.time += c.p.delta_t;
       c.les.first_time = false;  // FIRST_TIME = .FALSE. after the first step (diablo.F90:157)
@@ -861,6 +985,13 @@ int ekgpu_last_divergence(ek_ctx *h, double *div) {
   return guarded(h, [&](Ctx &c) {
     if (!div) return fail(c, EK_ERR_ARG, "div is NULL");
     *div = c.last_div;
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_set_step_graph(ek_ctx *h, int on) {
+  return guarded(h, [&](Ctx &c) {
+    c.step_graphs = on != 0;
     return (int)EK_OK;
   });
 }
@@ -1090,6 +1221,7 @@ int ekgpu_mg_autotune(ek_ctx *h, int reps, char *report, int report_len) {
     if (!c.p.mg_fast) return fail(c, EK_ERR_STATE, "the autotuner tunes the mixed solver (mg_fast = 1)");
     if (!c.have_metrics) return fail(c, EK_ERR_STATE, "metrics not set");
     std::string rep;
+    step_graphs_clear(c);  // captured with the old layouts
     const int st = mgfast_autotune(c, reps < 1 ? 1 : reps, rep);
     if (st != EK_OK) return fail(c, st, "autotune failed");
     if (report && report_len > 0) {
@@ -1113,6 +1245,7 @@ int ekgpu_mg_set_layout(ek_ctx *h, int level, int dir, int lanes, int seg) {
     if ((int)u.size() < PL.ngrid + 1) u.resize(PL.ngrid + 1, 0);
     t[level] = lanes;
     u[level] = seg;
+    step_graphs_clear(c);  // captured with the old layouts
     return (int)EK_OK;
   });
 }

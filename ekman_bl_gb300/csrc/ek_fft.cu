@@ -429,18 +429,21 @@ bool fft_args_ok(int nx, int nkx, long nlines, const void *in, const void *out) 
 }
 
 // Twiddle tables of the context-free transforms: cudaMalloc'd once per
-// (device, nx) and kept for the life of the process.
+// (device, nx) and kept for the life of the process.  Their size in double2,
+// shared with the fixed table of the allocation-free entry point below.
+constexpr int twiddle_count(int nx) { return (nx / 2) / 2 + nx / 2 + 1; }
+std::mutex g_tw_mu;
+std::map<std::pair<int, int>, double2 *> g_tw_cache;
 double2 *cached_twiddles(int nx, cudaStream_t s) {
-  static std::mutex mu;
-  static std::map<std::pair<int, int>, double2 *> cache;
   int dev = 0;
   EK_CUDA(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lk(mu);
+  std::lock_guard<std::mutex> lk(g_tw_mu);
+  auto &cache = g_tw_cache;
   auto it = cache.find({dev, nx});
   if (it != cache.end()) return it->second;
   const int M = nx / 2;
   double2 *tw = nullptr;
-  EK_CUDA(cudaMalloc(&tw, sizeof(double2) * (M / 2 + M + 1)));
+  EK_CUDA(cudaMalloc(&tw, sizeof(double2) * twiddle_count(nx)));
   k_twiddles<<<4, 256, 0, s>>>(tw, tw + M / 2, nx);
   EK_CUDA(cudaPeekAtLastError());
   EK_CUDA(cudaStreamSynchronize(s));
@@ -512,6 +515,11 @@ const char *last_global_error() { return t_last_error.c_str(); }
 
 }  // namespace ek
 
+extern "C" int ekgpu_fft_table_count(void) {
+  std::lock_guard<std::mutex> lk(ek::g_tw_mu);
+  return (int)ek::g_tw_cache.size();
+}
+
 extern "C" int ekgpu_fft_x_to_fourier(int nx, int nkx, long nlines, const double *in_dev, double *out_dev,
                                       void *stream) {
   return ek::standalone(true, nx, nkx, nlines, in_dev, out_dev, stream);
@@ -532,6 +540,7 @@ namespace {
 // (12.3 KB, resident on every GPU that loads the library until exit).
 constexpr int kNoAllocMaxNx = 1024;
 constexpr int kNoAllocTw = kNoAllocMaxNx / 4 + kNoAllocMaxNx / 2 + 1;
+static_assert(kNoAllocTw == twiddle_count(kNoAllocMaxNx), "the fixed table must hold the cached layout at nx = 1024");
 static __device__ __align__(256) double2 g_noalloc_twiddles[kNoAllocTw];
 
 // Device address of g_noalloc_twiddles, looked up once per device (the host

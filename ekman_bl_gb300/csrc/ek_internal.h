@@ -129,6 +129,7 @@ struct MgWork {
   std::vector<double *> phi, rhs, inv9;
   double *scratch = nullptr, *phif = nullptr, *red = nullptr, *kx2 = nullptr;
   int *done = nullptr, *cycles = nullptr, *alldone = nullptr, *idx = nullptr;
+  int *iter = nullptr;        // mixed solver: corrections applied so far (device counter)
   std::vector<int> idx_host;  // host copy of idx (a subset's problem numbers)
 };
 
@@ -204,6 +205,25 @@ struct StopPoll {
     cudaEventSynchronize(ev[k1]);
     return host[k1] != 0;
   }
+};
+
+// Per-substep results of a step run as a CUDA graph, written on the device
+// and read once after the step: the projection solve's statistics and the
+// divergence check's mean |div|.
+struct StepStats {
+  int min_cycles, max_cycles, n_not_converged, nprob;
+  double max_residual, div;
+};
+// One RK3 step captured as a CUDA graph (ekgpu_step).  A graph holds every
+// launch of the three substeps; the mixed solver's correction cycles sit in
+// conditional while-nodes that its check kernel stops.  key: the host-side
+// choices a step's launches depend on (see step_graph_key).
+struct StepGraph {
+  unsigned long long key = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  long long fixed_launches = 0;  // kernels outside the while bodies
+  long long body_launches[3] = {};  // kernels of one correction cycle, per substep
 };
 
 class UNet;
@@ -315,6 +335,17 @@ struct Ctx {
   double *div_part = nullptr;
   double last_div = 0.0;
   std::vector<void *> allocs;
+  // whole-step CUDA graphs (ekgpu_step): capture streams, the graphs by
+  // variant, a counter of plan changes that invalidate them, whether a step
+  // was taken eagerly since (lazy allocations happen there, never inside a
+  // capture), and the substep slot being captured (-1: running eagerly)
+  bool step_graphs = true;
+  cudaStream_t cap_stream = nullptr, cap_stream2 = nullptr;
+  std::vector<StepGraph> graphs;
+  bool eager_since_plan = false;
+  int graph_slot = -1;
+  long long graph_body_launches = 0;  // kernels in the while body of the last captured solve
+  StepStats *step_stats_dev = nullptr, *step_stats_host = nullptr;  // 3 slots; host copy pinned
   // per-kernel timer
   bool timing = false;
   std::vector<TimerRec> trec;
@@ -425,6 +456,7 @@ void launch_th_corners(Ctx &c);
 void launch_divergence_rhs(Ctx &c, double *rhs_finest, int nprob);
 void launch_projection(Ctx &c, const double *phif, int nprob, double temp4, bool update_p);
 int finish_divergence(Ctx &c, double *div_out);
+void step_graphs_clear(Ctx &c);
 
 // multigrid (ek_mg.cu).  mg_solve: nprob problems whose finest rhs is in
 // c.mgw.rhs[ngrid-1]; the solution is left in c.mgw.phif.  kx2_host may be

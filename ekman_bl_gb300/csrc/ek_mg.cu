@@ -713,6 +713,7 @@ void mg_work_alloc(Ctx &c, MgWork &w, int pmax) {
   w.done = w.flags;
   w.cycles = w.flags + pmax;
   w.alldone = w.flags + 2 * pmax;
+  w.iter = w.flags + 2 * pmax + 1;
   w.idx = w.flags + 2 * pmax + 4;
   w.pmax = pmax;
 }
@@ -747,7 +748,7 @@ void mg_alloc(Ctx &c, int pmax) {
 int mg_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_host, ek_mg_stats *st) {
   const int r = c.p.mg_fast ? mgfast_solve(c, nprob, kx2_dev, kx2_host, st)
                             : mg_solve_exact(c, c.mgw, nprob, kx2_dev, st, 0);
-  if (r == EK_OK || r == EK_ERR_NOT_CONVERGED) {
+  if (c.graph_slot < 0 && (r == EK_OK || r == EK_ERR_NOT_CONVERGED)) {  // a captured solve counts after the step
     c.mg_solved_total += nprob;
     c.mg_nc_total += c.last_stats.n_not_converged;
   }

@@ -49,6 +49,7 @@ struct FastDev {
   double *phif;            // output (finest interior, problem fastest)
   double *red;             // 6 per problem: |b|^2, |r|^2, two unused, meas
   int *done, *cycles, *alldone;
+  int *iter;               // corrections applied so far
   double tol;
 };
 
@@ -170,10 +171,19 @@ __global__ void k_f_split(const double *b, float *bh, float *bl, size_t n) {
   }
 }
 
-// Decide per problem; iter = corrections applied so far.
-__global__ void k_f_check(FastDev g, int iter, int last) {
-  if (*g.alldone) return;
+// Decide per problem after a residual; iter = corrections applied so far
+// (the device counter plus incr).  A problem within the tolerance is done
+// (1); at iter = maxit the rest stop (2); when none is left, alldone.  In a
+// captured step graph the block also sets the condition of the while-node
+// that repeats the correction cycle: 1 while any problem is active.
+__global__ void k_f_check(FastDev g, int maxit, int incr, cudaGraphConditionalHandle cond, int use_cond) {
+  if (*g.alldone) {
+    if (use_cond && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
+    return;
+  }
   __shared__ int active;
+  const int iter = *g.iter + incr;
+  const bool last = iter >= maxit;
   if (threadIdx.x == 0) active = 0;
   __syncthreads();
   for (int p = threadIdx.x; p < g.P; p += blockDim.x) {
@@ -189,7 +199,48 @@ __global__ void k_f_check(FastDev g, int iter, int last) {
     else atomicAdd(&active, 1);
   }
   __syncthreads();
-  if (threadIdx.x == 0 && active == 0) *g.alldone = 1;
+  if (threadIdx.x == 0) {
+    *g.iter = iter;
+    if (active == 0) *g.alldone = 1;
+    if (use_cond) cudaGraphSetConditional(cond, active == 0 ? 0u : 1u);
+  }
+}
+
+// The solve's statistics on the device (a step run as a graph reads them
+// after the step): cycle range, problems stopped at the cap, largest final
+// relative residual.  One block.
+__global__ void k_f_stats(FastDev g, StepStats *out) {
+  __shared__ int smin[256], smax[256], snc[256];
+  __shared__ double sres[256];
+  int mn = 1 << 30, mx = 0, nc = 0;
+  double rs = 0.0;
+  for (int p = threadIdx.x; p < g.P; p += blockDim.x) {
+    mn = min(mn, g.cycles[p]);
+    mx = max(mx, g.cycles[p]);
+    nc += (g.done[p] != 1);
+    rs = fmax(rs, g.red[6 * p + 4]);
+  }
+  smin[threadIdx.x] = mn;
+  smax[threadIdx.x] = mx;
+  snc[threadIdx.x] = nc;
+  sres[threadIdx.x] = rs;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      smin[threadIdx.x] = min(smin[threadIdx.x], smin[threadIdx.x + w]);
+      smax[threadIdx.x] = max(smax[threadIdx.x], smax[threadIdx.x + w]);
+      snc[threadIdx.x] += snc[threadIdx.x + w];
+      sres[threadIdx.x] = fmax(sres[threadIdx.x], sres[threadIdx.x + w]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out->min_cycles = smin[0];
+    out->max_cycles = smax[0];
+    out->n_not_converged = snc[0];
+    out->nprob = g.P;
+    out->max_residual = sres[0];
+  }
 }
 
 // Line Gauss-Seidel.  The 9-point operator couples each point to its eight
@@ -866,6 +917,7 @@ FastDev make_fastdev(Ctx &c, int nprob, const double *kx2_dev) {
   g.done = w.done;
   g.cycles = w.cycles;
   g.alldone = w.alldone;
+  g.iter = w.iter;
   g.tol = c.p.mg_tol;
   return g;
 }
@@ -1035,18 +1087,17 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
   };
 
   const int maxit = c.p.mg_maxcy;
-  c.poll.init();
-  c.poll.reset();
-  for (int it = 0; it <= maxit; ++it) {
-    {
-      KScope ks(c, KC_MG_CHECK, 4.0 * nprob * (4.0 * npt + 2.0 * (PL.nfx + 2) * (PL.nfy + 2)));
-      k_f_resid_ff<<<dim3(pch, PL.nfy + 2), dim3(32, kRY), 0, s>>>(g);
-      after_launch(c);
-      k_f_check<<<1, 256, 0, s>>>(g, it, it == maxit ? 1 : 0);
-      after_launch(c);
-    }
-    if (it == maxit || c.poll.after_check(w.alldone, s)) break;
-    // one FP32 V(1,1) cycle on A e = r from e = 0
+  // r = b - A phi and the per-problem decision (incr: count one more
+  // correction); cond/use_cond: the while-node condition in a graph
+  auto check = [&](int incr, cudaGraphConditionalHandle cond, int use_cond) {
+    KScope ks(c, KC_MG_CHECK, 4.0 * nprob * (4.0 * npt + 2.0 * (PL.nfx + 2) * (PL.nfy + 2)));
+    k_f_resid_ff<<<dim3(pch, PL.nfy + 2), dim3(32, kRY), 0, s>>>(g);
+    after_launch(c);
+    k_f_check<<<1, 256, 0, s>>>(g, maxit, incr, cond, use_cond);
+    after_launch(c);
+  };
+  // one FP32 V(1,1) cycle on A e = r from e = 0, then phi += e
+  auto correction = [&]() {
     for (int l = PL.ngrid; l >= 1; --l) {
       const MgLevel &L = PL.lv[l - 1];
       if (l == 1) {
@@ -1076,11 +1127,60 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
       }
       relax(l, true);
     }
-    {
-      KScope ks(c, KC_MG_CHECK, 4.0 * nprob * npt * 5);
-      k_f_update_ff<<<dim3(pch, PL.nfy), dim3(32, kRY), 0, s>>>(g);
-      after_launch(c);
+    KScope ks(c, KC_MG_CHECK, 4.0 * nprob * npt * 5);
+    k_f_update_ff<<<dim3(pch, PL.nfy), dim3(32, kRY), 0, s>>>(g);
+    after_launch(c);
+  };
+  if (c.graph_slot < 0) {
+    // eager: the host stops issuing cycles once the done flag it polls is set
+    c.poll.init();
+    c.poll.reset();
+    check(0, 0, 0);
+    bool stop = c.poll.after_check(w.alldone, s);
+    for (int it = 1; it <= maxit && !stop; ++it) {
+      correction();
+      check(1, 0, 0);
+      stop = c.poll.after_check(w.alldone, s);
     }
+  } else {
+    // captured: the cycles repeat in a conditional while-node whose
+    // condition the check kernel sets, so no host decides between them
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    EK_CUDA(cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &ndeps));
+    if (cs != cudaStreamCaptureStatusActive) throw CudaError("mixed solve: step graph capture is not active");
+    cudaGraphConditionalHandle cond;
+    EK_CUDA(cudaGraphConditionalHandleCreate(&cond, cg, 1u, cudaGraphCondAssignDefault));
+    check(0, cond, 1);
+    EK_CUDA(cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &ndeps));
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    EK_CUDA(cudaGraphAddNode(&wnode, cg, deps, nullptr, ndeps, &np));
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    EK_CUDA(cudaStreamUpdateCaptureDependencies(s, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    const cudaStream_t outer = s;
+    s = c.cap_stream2;
+    const long long l0 = c.launches;
+    try {
+      EK_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+      correction();
+      check(1, cond, 1);
+      cudaGraph_t done_body = nullptr;
+      EK_CUDA(cudaStreamEndCapture(s, &done_body));
+    } catch (...) {
+      cudaGraph_t junk = nullptr;
+      cudaStreamEndCapture(c.cap_stream2, &junk);
+      s = outer;
+      throw;
+    }
+    s = outer;
+    c.graph_body_launches = c.launches - l0;
   }
   {
     KScope ks(c, KC_MG_SETUP, 16.0 * nprob * npt);
@@ -1088,6 +1188,12 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
     after_launch(c);
   }
   if (ns > 0) mg_null_mean(c, w.phif, nprob, kx2_dev);
+  if (c.graph_slot >= 0) {
+    // a captured step reads the statistics after the step
+    k_f_stats<<<1, 256, 0, s>>>(g, c.step_stats_dev + c.graph_slot);
+    after_launch(c);
+    return EK_OK;
+  }
   std::vector<int> cyc(nprob), done(nprob);
   std::vector<double> meas(6 * nprob);
   EK_CUDA(cudaMemcpyAsync(cyc.data(), w.cycles, sizeof(int) * nprob, cudaMemcpyDeviceToHost, s));

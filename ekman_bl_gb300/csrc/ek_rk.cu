@@ -1211,8 +1211,26 @@ void launch_projection(Ctx &c, const double *phif, int P, double temp4, bool upd
 }
 
 // Mean |div| from the per-line partial sums, in J order (duct.F90:2800).
+namespace {
+// The mean |div| from the per-line sums, in the order and arithmetic of the
+// host reduction below, written to a step graph's statistics slot.
+__global__ void k_div_final(const double *part, int n, double scale_den, double *out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0.0;
+  for (int t = 0; t < n; ++t) s += part[t];
+  *out = s / scale_den;
+}
+}  // namespace
+
 int finish_divergence(Ctx &c, double *div_out) {
   const Dims &d = c.d;
+  if (c.graph_slot >= 0) {
+    // a captured step reads the value after the step
+    k_div_final<<<1, 32, 0, c.stream>>>(c.div_part, d.NY - 2, (double)(d.NX + 1) * (double)d.NY * (double)d.NZ,
+                                         &c.step_stats_dev[c.graph_slot].div);
+    after_launch(c);
+    return EK_OK;
+  }
   std::vector<double> part(d.NY - 2);
   EK_CUDA(cudaMemcpyAsync(part.data(), c.div_part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, c.stream));
   EK_CUDA(cudaStreamSynchronize(c.stream));

@@ -28,9 +28,9 @@ EXPORTS = [
     "ekgpu_set_metrics", "ekgpu_metrics_from_grid", "ekgpu_upload_state", "ekgpu_download_state",
     "ekgpu_get_field", "ekgpu_put_field", "ekgpu_rk_substep", "ekgpu_step", "ekgpu_ensemble_step", "ekgpu_rem_div",
     "ekgpu_poisson_batch", "ekgpu_poisson_batch_device", "ekgpu_last_divergence", "ekgpu_last_mg_stats",
-    "ekgpu_mg_counters",
+    "ekgpu_mg_counters", "ekgpu_set_step_graph",
     "ekgpu_launch_count", "ekgpu_set_timing", "ekgpu_get_timing", "ekgpu_timing_class_name",
-    "ekgpu_fft_x_to_fourier", "ekgpu_fft_x_to_physical", "ekgpu_fft_x_to_fourier_noalloc",
+    "ekgpu_fft_x_to_fourier", "ekgpu_fft_x_to_physical", "ekgpu_fft_x_to_fourier_noalloc", "ekgpu_fft_table_count",
     "ekgpu_sponge_profiles", "ekgpu_set_sponge", "ekgpu_set_time", "ekgpu_get_time",
     "ekgpu_save_flow", "ekgpu_read_flow", "ekgpu_save_stats",
     "ekgpu_unet_create", "ekgpu_unet_destroy", "ekgpu_unet_last_error", "ekgpu_unet_num_params",
@@ -117,12 +117,14 @@ def load_library():
     L.ekgpu_last_divergence.argtypes = [V, _D]
     L.ekgpu_last_mg_stats.argtypes = [V, C.POINTER(EkMgStats)]
     L.ekgpu_mg_counters.argtypes = [V, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    L.ekgpu_set_step_graph.argtypes = [V, C.c_int]
     L.ekgpu_launch_count.argtypes = [V]
     L.ekgpu_launch_count.restype = C.c_longlong
     L.ekgpu_set_timing.argtypes = [V, C.c_int]
     L.ekgpu_get_timing.argtypes = [V, _D, C.POINTER(C.c_longlong), _D, C.c_int]
     L.ekgpu_timing_class_name.argtypes = [C.c_int]
     L.ekgpu_timing_class_name.restype = C.c_char_p
+    L.ekgpu_fft_table_count.argtypes = []
     for n in ("ekgpu_fft_x_to_fourier", "ekgpu_fft_x_to_physical", "ekgpu_fft_x_to_fourier_noalloc"):
         getattr(L, n).argtypes = [C.c_int, C.c_int, C.c_long, V, V, V]
     _lib = L
@@ -429,6 +431,11 @@ class DuctSolver:
     def rem_div_curv(self):
         """REM_DIV_CURV: projection of the current state (duct.F90:2472-2818)."""
         return self._solve_status(self._L.ekgpu_rem_div(self._h))
+
+    def set_step_graph(self, on: bool):
+        """Let step() run each RK3 step as one captured CUDA graph (default
+        on; applies to the mixed solver with a fixed time step)."""
+        self._check(self._L.ekgpu_set_step_graph(self._h, 1 if on else 0))
 
     def mg_counters(self):
         """(real Poisson problems solved, of them stopped at the cycle cap)

@@ -386,6 +386,18 @@ int ekgpu_rk_substep(ek_ctx *ctx, int rk_step);
  * call returns it after the last step. */
 int ekgpu_step(ek_ctx *ctx, int nsteps);
 
+/* Whether ekgpu_step may run each RK3 step as one CUDA graph (default on).
+ * No counterpart in the reference.  The graph path applies with mg_fast = 1,
+ * a fixed time step, F_TYPE = 1, no learned guess or pair collection and the
+ * per-kernel timer off; the first step after ekgpu_set_metrics, the autotuner
+ * or a layout change runs eagerly, later steps replay a graph captured once
+ * per variant (LES on/off, FIRST_TIME, C_DYN due, sponge reset), in which the
+ * mixed solver's correction cycles repeat in conditional while-nodes until
+ * its device-side check stops them.  Results are the same either way; the
+ * statistics and the divergence check are read once per step instead of
+ * once per substep. */
+int ekgpu_set_step_graph(ek_ctx *ctx, int on);
+
 /* An ensemble of independent runs, each with its own sizes, parameters and
  * metrics (one context per member), advanced by nsteps RK3 steps together
  * on one GPU.  The reference runs each member as its own MPI job; here every
@@ -445,6 +457,11 @@ int ekgpu_mg_counters(ek_ctx *ctx, long long *solved, long long *not_converged);
  * allocated once per (device, nx).  Asynchronous on the stream. */
 int ekgpu_fft_x_to_fourier(int nx, int nkx, long nlines, const double *in_dev, double *out_dev, void *stream);
 int ekgpu_fft_x_to_physical(int nx, int nkx, long nlines, const double *in_dev, double *out_dev, void *stream);
+
+/* Number of (device, nx) twiddle tables the two transforms above have
+ * allocated so far in this process (a diagnostic of their device memory; no
+ * counterpart in the reference). */
+int ekgpu_fft_table_count(void);
 
 /* ekgpu_fft_x_to_fourier without any device allocation.  No counterpart in
  * the reference: it exists for callers that are not allowed to allocate

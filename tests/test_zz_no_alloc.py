@@ -46,6 +46,22 @@ def test_noalloc_matches_regular_entry_point_twice():
         assert not a[:, nkx + 1:].any()
 
 
+def test_noalloc_allocates_no_table():
+    """A size no other call of this process used: the regular entry point
+    would allocate a twiddle table for it, the allocation-free one must not."""
+    torch = pytest.importorskip("torch")
+    ekbuild.build()
+    L = load_library()
+    L.ekgpu_fft_x_to_fourier_noalloc.argtypes = [C.c_int, C.c_int, C.c_long, C.c_void_p, C.c_void_p, C.c_void_p]
+    nx = 512
+    x = np.zeros((7, nx + 2))
+    x[:, :nx] = np.random.default_rng(5).standard_normal((7, nx))
+    before = L.ekgpu_fft_table_count()
+    st, _ = _transform(L.ekgpu_fft_x_to_fourier_noalloc, nx, nx // 3, x, torch)
+    assert st == 0
+    assert L.ekgpu_fft_table_count() == before
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch():
     ekbuild.build()
     L = load_library()
