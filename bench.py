@@ -48,14 +48,21 @@ MG_TOL = 1e-8
 METRIC = "RK3 steps/s and Poisson solves/s at 1e-8 residual: learned+batched vs plain, 1 GB300"
 
 
-def profiled_traffic(kernel_class: str):
-    """DRAM bytes per launch of a kernel class from its committed ncu summary
-    (profiles/<class>_traffic_512x385x257.md), or (None, None)."""
+# DRAM traffic per algorithmic byte of a kernel class, from a committed ncu
+# summary of a small case of the same kernel (one kernel, a few launches)
+TRAFFIC_PROFILES = {"mg_relax": "profiles/k_f_pline_dram_traffic_512x385x257_nx128.md"}
+
+
+def profiled_traffic_ratio(kernel_class: str):
+    """(measured DRAM bytes / algorithmic bytes, summary path) of a kernel
+    class, or (None, None) when no summary covers it."""
     import re
-    path = os.path.join(ROOT, "profiles", f"{kernel_class}_traffic_512x385x257.md")
+    rel = TRAFFIC_PROFILES.get(kernel_class)
+    if rel is None:
+        return None, None
     try:
-        m = re.search(r"traffic_bytes_per_launch:\s*(\d+)", open(path).read())
-        return (int(m.group(1)), os.path.relpath(path, ROOT)) if m else (None, None)
+        m = re.search(r"traffic_to_algorithmic:\s*([0-9.]+)", open(os.path.join(ROOT, rel)).read())
+        return (float(m.group(1)), rel) if m else (None, None)
     except OSError:
         return None, None
 
@@ -510,10 +517,15 @@ def run_gpu(args):
         roof = None
         if dcnt > 0 and dms > 0:
             achieved = dbytes / (dms / 1000.0) / 1e9
-            traffic, tsrc = profiled_traffic(name)
+            ratio, tsrc = profiled_traffic_ratio(name)
+            traffic = int(ratio * dbytes / dcnt) if ratio is not None else None
             roof = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                    "traffic": traffic, "traffic_source": tsrc, "algorithmic_bytes_per_launch": int(dbytes / dcnt),
+                    "traffic": traffic, "traffic_source": tsrc,
+                    "traffic_note": (f"DRAM bytes per algorithmic byte ({ratio}) of one finest-level sweep of the "
+                                     f"class's kernel, measured with ncu on the NX=128 case (fields above L2), "
+                                     f"times this class's algorithmic bytes per launch") if ratio else None,
+                    "algorithmic_bytes_per_launch": int(dbytes / dcnt),
                     "avg_launch_us": round(dms * 1000.0 / dcnt, 3), "launches_per_step": dcnt,
                     "share_of_step": round(dms / ktot, 4)}
         per_class_gbs = {k: round(v[2] / (v[0] / 1000.0) / 1e9, 1) for k, v in kt.items()
