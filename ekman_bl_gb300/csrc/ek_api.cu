@@ -3,9 +3,11 @@
 // RK_DUCT (src/duct.F90:237-2469), with every transform, stencil and solve
 // running on the GPU and the state resident in HBM.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <system_error>
 #include <thread>
@@ -266,14 +268,13 @@ unsigned long long step_graph_key(const Ctx &c) {
          (reset ? 8ull : 0ull);
 }
 
-StepGraph &step_graph_capture(Ctx &c, unsigned long long key) {
-  StepGraph sg;
-  sg.key = key;
+// The three substeps of one step, captured on stream s (which is capturing);
+// fills the launch counts of sg.
+void capture_substeps(Ctx &c, cudaStream_t s, StepGraph &sg) {
   const cudaStream_t saved = c.stream;
   const long long l0 = c.launches;
   long long body = 0;
-  c.stream = c.cap_stream;
-  EK_CUDA(cudaStreamBeginCapture(c.cap_stream, cudaStreamCaptureModeThreadLocal));
+  c.stream = s;
   try {
     for (int rk = 1; rk <= 3; ++rk) {
       c.graph_slot = rk - 1;
@@ -287,15 +288,26 @@ StepGraph &step_graph_capture(Ctx &c, unsigned long long key) {
     c.graph_slot = -1;
     c.stream = saved;
     c.launches = l0;
-    cudaGraph_t junk = nullptr;
-    cudaStreamEndCapture(c.cap_stream, &junk);
-    if (junk) cudaGraphDestroy(junk);
     throw;
   }
   c.graph_slot = -1;
   c.stream = saved;
   sg.fixed_launches = c.launches - l0 - body;
   c.launches = l0;
+}
+
+StepGraph &step_graph_capture(Ctx &c, unsigned long long key) {
+  StepGraph sg;
+  sg.key = key;
+  EK_CUDA(cudaStreamBeginCapture(c.cap_stream, cudaStreamCaptureModeThreadLocal));
+  try {
+    capture_substeps(c, c.cap_stream, sg);
+  } catch (...) {
+    cudaGraph_t junk = nullptr;
+    cudaStreamEndCapture(c.cap_stream, &junk);
+    if (junk) cudaGraphDestroy(junk);
+    throw;
+  }
   EK_CUDA(cudaStreamEndCapture(c.cap_stream, &sg.graph));
   if (cudaGraphInstantiate(&sg.exec, sg.graph, 0) != cudaSuccess) {
     cudaGraphDestroy(sg.graph);
@@ -305,6 +317,8 @@ StepGraph &step_graph_capture(Ctx &c, unsigned long long key) {
   return c.graphs.back();
 }
 
+int step_stats_apply(Ctx &c, const StepGraph &sg, int &late);
+
 // One step from its graph; late becomes EK_ERR_NOT_CONVERGED when a solve
 // of the step missed the residual rule's tolerance.
 int step_graph_run(Ctx &c, const StepGraph &sg, int &late) {
@@ -312,6 +326,12 @@ int step_graph_run(Ctx &c, const StepGraph &sg, int &late) {
   EK_CUDA(cudaMemcpyAsync(c.step_stats_host, c.step_stats_dev, 3 * sizeof(StepStats), cudaMemcpyDeviceToHost,
                           c.stream));
   EK_CUDA(cudaStreamSynchronize(c.stream));
+  return step_stats_apply(c, sg, late);
+}
+
+// The statistics a graph-run step left in the context's pinned slots: launch
+// count, multigrid totals and last stats, divergence, status.
+int step_stats_apply(Ctx &c, const StepGraph &sg, int &late) {
   long long n = sg.fixed_launches;
   bool nan = false;
   for (int k = 0; k < 3; ++k) {
@@ -335,6 +355,107 @@ int step_graph_run(Ctx &c, const StepGraph &sg, int &late) {
   return nan ? EK_ERR_NAN : EK_OK;
 }
 
+// ---- ensembles in one graph launch -------------------------------------------
+// Members that all take the graph path step together from one CUDA graph
+// per ensemble step: each member's three substeps are a branch of its own,
+// forked from and joined to the graph's root, so one cudaGraphLaunch runs
+// every member's kernels side by side.  Graphs are cached process-wide by
+// the members' (epoch, key) pairs; an epoch is never reused, so a graph of
+// a destroyed or re-planned member is never launched again.
+struct EnsembleGraph {
+  std::vector<unsigned long long> sig;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<StepGraph> parts;  // per member: its launch counts
+  std::vector<cudaEvent_t> ev;   // ordering against the members' own streams
+  ~EnsembleGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  }
+};
+std::mutex g_ens_mu;
+// most recent last; never destroyed at exit (the CUDA runtime may be gone by then)
+std::vector<std::unique_ptr<EnsembleGraph>> &g_ens = *new std::vector<std::unique_ptr<EnsembleGraph>>();
+constexpr size_t kEnsembleGraphsKept = 8;
+
+EnsembleGraph &ensemble_graph(const std::vector<ek_ctx *> &m, const std::vector<unsigned long long> &sig) {
+  for (auto &e : g_ens)
+    if (e->sig == sig) return *e;
+  const int n = (int)m.size();
+  auto eg = std::make_unique<EnsembleGraph>();
+  eg->sig = sig;
+  eg->parts.resize(n);
+  eg->ev.resize(n + 1);
+  for (cudaEvent_t &e : eg->ev) EK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  Ctx &c0 = m[0]->c;
+  const cudaStream_t root = c0.cap_stream;
+  EK_CUDA(cudaStreamBeginCapture(root, cudaStreamCaptureModeThreadLocal));
+  try {
+    EK_CUDA(cudaEventRecord(eg->ev[n], root));  // the fork
+    for (int i = 0; i < n; ++i) {
+      Ctx &c = m[i]->c;
+      if (i > 0) EK_CUDA(cudaStreamWaitEvent(c.cap_stream, eg->ev[n], 0));
+      capture_substeps(c, c.cap_stream, eg->parts[i]);
+      if (i > 0) {
+        EK_CUDA(cudaEventRecord(eg->ev[i], c.cap_stream));
+        EK_CUDA(cudaStreamWaitEvent(root, eg->ev[i], 0));
+      }
+    }
+  } catch (...) {
+    cudaGraph_t junk = nullptr;
+    cudaStreamEndCapture(root, &junk);
+    if (junk) cudaGraphDestroy(junk);
+    throw;
+  }
+  EK_CUDA(cudaStreamEndCapture(root, &eg->graph));
+  if (cudaGraphInstantiate(&eg->exec, eg->graph, 0) != cudaSuccess) throw CudaError("ensemble graph: instantiate failed");
+  if (g_ens.size() >= kEnsembleGraphsKept) g_ens.erase(g_ens.begin());
+  g_ens.push_back(std::move(eg));
+  return *g_ens.back();
+}
+
+// One step of every member from one graph launch; st[i] receives member i's
+// status.  Throws CudaError when the graph cannot be captured (nothing has
+// run then, and TIME_STEP is left as it was).
+void ensemble_graph_step(const std::vector<ek_ctx *> &m, std::vector<int> &st, std::vector<int> &late) {
+  const int n = (int)m.size();
+  std::lock_guard<std::mutex> lk(g_ens_mu);
+  for (ek_ctx *h : m) h->c.p.time_step += 1;
+  std::vector<unsigned long long> sig;
+  for (ek_ctx *h : m) {
+    sig.push_back(h->c.epoch);
+    sig.push_back(step_graph_key(h->c));
+  }
+  EnsembleGraph *eg = nullptr;
+  try {
+    eg = &ensemble_graph(m, sig);
+  } catch (...) {
+    for (ek_ctx *h : m) h->c.p.time_step -= 1;
+    throw;
+  }
+  Ctx &c0 = m[0]->c;
+  // after the work already queued on every member's stream
+  for (int i = 1; i < n; ++i) {
+    EK_CUDA(cudaEventRecord(eg->ev[i], m[i]->c.stream));
+    EK_CUDA(cudaStreamWaitEvent(c0.stream, eg->ev[i], 0));
+  }
+  EK_CUDA(cudaGraphLaunch(eg->exec, c0.stream));
+  for (ek_ctx *h : m)
+    EK_CUDA(cudaMemcpyAsync(h->c.step_stats_host, h->c.step_stats_dev, 3 * sizeof(StepStats), cudaMemcpyDeviceToHost,
+                            c0.stream));
+  EK_CUDA(cudaEventRecord(eg->ev[n], c0.stream));
+  for (int i = 1; i < n; ++i) EK_CUDA(cudaStreamWaitEvent(m[i]->c.stream, eg->ev[n], 0));
+  EK_CUDA(cudaStreamSynchronize(c0.stream));
+  for (int i = 0; i < n; ++i) {
+    Ctx &c = m[i]->c;
+    const int r = step_stats_apply(c, eg->parts[i], late[i]);
+    if (r == EK_ERR_NAN) st[i] = fail(c, EK_ERR_NAN, "DIV is a NaN");
+    c.p.time += c.p.delta_t;
+    c.les.first_time = false;
+  }
+}
+
 __global__ void k_transpose(const double *in, double *out, int P, long npt, int to_inner) {
   const long n = (long)P * npt;
   for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
@@ -354,13 +475,16 @@ __global__ void k_transpose(const double *in, double *out, int P, long npt, int 
 
 namespace ek {
 // Drop every captured step graph (the plan they were captured from changed).
+// The new epoch also retires every ensemble graph that holds this context.
 void step_graphs_clear(Ctx &c) {
+  static std::atomic<unsigned long long> next_epoch{1};
   for (StepGraph &g : c.graphs) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     if (g.graph) cudaGraphDestroy(g.graph);
   }
   c.graphs.clear();
   c.eager_since_plan = false;
+  c.epoch = next_epoch.fetch_add(1);
 }
 
 // Sum the recorded per-kernel-class event pairs into kms/kcnt.
@@ -482,6 +606,7 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
     EK_CUDA(cudaStreamCreateWithFlags(&c.cap_stream, cudaStreamNonBlocking));
     EK_CUDA(cudaStreamCreateWithFlags(&c.cap_stream2, cudaStreamNonBlocking));
     EK_CUDA(cudaHostAlloc(&c.step_stats_host, 3 * sizeof(StepStats), cudaHostAllocDefault));
+    step_graphs_clear(c);  // a fresh epoch
     rk_init_attributes();
     fft_init_attributes();
     if (p.les) les_init_attributes();
@@ -909,6 +1034,38 @@ int ekgpu_ensemble_step(ek_ctx *const *members, int n, int nsteps, int *status) 
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return EK_ERR_CUDA;
   std::vector<int> st(n, EK_OK);
+  // every member on the graph path: one graph launch per ensemble step
+  bool graph = n >= 2;
+  for (ek_ctx *h : m) graph = graph && step_graph_eligible(h->c) && h->c.have_metrics && h->c.eager_since_plan;
+  int done = 0;
+  if (graph) {
+    std::vector<int> late(n, EK_OK);
+    try {
+      for (; done < nsteps; ++done) {
+        ensemble_graph_step(m, st, late);
+        if (std::any_of(st.begin(), st.end(), [](int v) { return v != EK_OK; })) {
+          ++done;
+          break;
+        }
+      }
+    } catch (const CudaError &e) {
+      m[0]->c.err = e.msg;  // capture failed: the remaining steps run as below
+    }
+    for (int i = 0; i < n; ++i)
+      if (st[i] == EK_OK && late[i] != EK_OK) st[i] = fail(m[i]->c, late[i], "a Poisson problem reached mg_maxcy above the tolerance");
+    if (done == nsteps) {
+      int r = EK_OK;
+      for (int i = 0; i < n; ++i) {
+        if (status) status[i] = st[i];
+        if (r == EK_OK && st[i] != EK_OK) r = st[i];
+      }
+      return r;
+    }
+  }
+  // the remaining steps (all of them off the graph path) member by member;
+  // a member that failed above does not step again
+  std::vector<int> prior(st);
+  const int rest = nsteps - done;
   // member 0 on the calling thread, the others on their own threads (every
   // context owns its stream, buffers and pinned stop flags, so the members
   // share nothing but the device)
@@ -921,14 +1078,17 @@ int ekgpu_ensemble_step(ek_ctx *const *members, int n, int nsteps, int *status) 
           st[i] = fail(m[i]->c, EK_ERR_CUDA, "ensemble: cudaSetDevice failed");
           return;
         }
-        st[i] = ekgpu_step(m[i], nsteps);
+        if (prior[i] == EK_OK || prior[i] == EK_ERR_NOT_CONVERGED) st[i] = ekgpu_step(m[i], rest);
       });
     } catch (const std::system_error &) {
-      st[i] = ekgpu_step(m[i], nsteps);  // no thread to spare: step it here
+      // no thread to spare: step it here
+      if (prior[i] == EK_OK || prior[i] == EK_ERR_NOT_CONVERGED) st[i] = ekgpu_step(m[i], rest);
     }
   }
-  st[0] = ekgpu_step(m[0], nsteps);
+  if (prior[0] == EK_OK || prior[0] == EK_ERR_NOT_CONVERGED) st[0] = ekgpu_step(m[0], rest);
   for (auto &t : th) t.join();
+  for (int i = 0; i < n; ++i)
+    if (prior[i] != EK_OK && st[i] == EK_OK) st[i] = prior[i];
   int r = EK_OK;
   for (int i = 0; i < n; ++i) {
     if (status) status[i] = st[i];

@@ -340,6 +340,7 @@ struct Ctx {
   // was taken eagerly since (lazy allocations happen there, never inside a
   // capture), and the substep slot being captured (-1: running eagerly)
   bool step_graphs = true;
+  unsigned long long epoch = 0;  // process-unique; renewed whenever its step graphs are dropped
   cudaStream_t cap_stream = nullptr, cap_stream2 = nullptr;
   std::vector<StepGraph> graphs;
   bool eager_since_plan = false;

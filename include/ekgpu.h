@@ -400,10 +400,15 @@ int ekgpu_set_step_graph(ek_ctx *ctx, int on);
 
 /* An ensemble of independent runs, each with its own sizes, parameters and
  * metrics (one context per member), advanced by nsteps RK3 steps together
- * on one GPU.  The reference runs each member as its own MPI job; here every
- * member steps on its own stream, from its own host thread, so the members'
- * kernels share the GPU and one member's host waits (multigrid stop checks,
- * statistics) overlap the others' work.  status[m] (optional, n entries)
+ * on one GPU.  The reference runs each member as its own MPI job.  Here,
+ * when every member takes ekgpu_step's graph path and has stepped once
+ * since its plan was set, each ensemble step is one CUDA graph launch on
+ * member 0's stream (ordered after the work queued on every member's
+ * stream): every member's three substeps form a branch of that graph, so
+ * the members' kernels run side by side.  Otherwise every member steps on
+ * its own stream, from its own host thread, so the members' kernels share
+ * the GPU and one member's host waits overlap the others' work.  Results
+ * are the same either way.  status[m] (optional, n entries)
  * receives member m's ekgpu_step result; the call returns EK_OK when every
  * member succeeded, else the first failing member's code (its message stays
  * in that member's ekgpu_last_error).  A member that fails leaves the others

@@ -131,3 +131,35 @@ def test_graph_step_reports_nan():
         assert "NAN" in str(e.value)
     finally:
         g.close()
+
+
+def test_ensemble_graph_equals_members_stepped_alone():
+    """Members of different sizes stepped as one graph launch per ensemble
+    step equal the same members stepped one at a time without graphs."""
+    from ekman_bl_gb300.duct import ensemble_step
+    from test_ensemble import SIZES, _member
+    together, alone = [], []
+    for i, (nx, ny2, nz2) in enumerate(SIZES[:3]):
+        p, xp, yp, st = _member(i, nx, ny2, nz2)
+        _mixed(p)
+        for group, on in ((together, True), (alone, False)):
+            s = DuctSolver(p, metrics_from_grid(p, xp, yp))
+            s.set_step_graph(on)
+            s.upload(*st)
+            group.append(s)
+    try:
+        # the first call steps the members on their own threads (an eager
+        # step each, then their own graphs); the second one launches one
+        # graph per ensemble step
+        assert ensemble_step(together, 2) == [0, 0, 0]
+        n0 = sum(s.launch_count() for s in together)
+        assert ensemble_step(together, 3) == [0, 0, 0]
+        assert sum(s.launch_count() for s in together) > n0
+        for s in alone:
+            assert s.step(5) == 0
+        for a, b in zip(together, alone):
+            _same(a, b)
+            assert a.get_time() == b.get_time()
+    finally:
+        for s in together + alone:
+            s.close()
