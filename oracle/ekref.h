@@ -11,12 +11,16 @@
  * Only the tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg
  * may load this library.  It is never part of the product path.
  *
- * The reference itself cannot be compiled here (no Fortran compiler, no MPI,
- * no FFTW, and src/fft.F90 is missing from the tree), so parity of the
- * x-FFT convention is pinned by known-answer tests of our own, not by
- * reference output: forward = (1/NX) sum_n u_n exp(-2 pi i k n/NX) for
- * k = 0..NX/3 (higher modes zeroed), inverse = Hermitian sum over
- * k = 0..NX/3 (imaginary part of k=0 ignored), KX = 2 pi k/LX.
+ * The reference cannot be compiled here (no Fortran compiler, no MPI, no
+ * FFTW).  Its unmodified source is run instead through an interpreter of
+ * the Fortran subset it uses (tests/golden/fortran_interp.py), and this
+ * oracle is pinned against those runs: the MUDPACK solves bit for bit,
+ * REM_DIV_CURV plus two RK3 steps of RK_DUCT to rounding level on five
+ * cases (tests/test_golden_reference.py).  src/fft.F90 is missing from the
+ * tree, so the x-FFT convention is pinned by known-answer tests of our
+ * own: forward = (1/NX) sum_n u_n exp(-2 pi i k n/NX) for k = 0..NX/3
+ * (higher modes zeroed), inverse = Hermitian sum over k = 0..NX/3
+ * (imaginary part of k=0 ignored), KX = 2 pi k/LX.
  */
 #ifndef EKREF_H
 #define EKREF_H

@@ -503,7 +503,13 @@ class Runtime:
         self.commons = {}      # block -> bytearray
         self.funcs = {}        # name -> translated python function
         self.externals = {}    # name -> python callable (stubs)
+        self.files = {}        # file name -> text, for OPEN and list-directed READ
+        self.units_io = {}     # unit number -> iterator over the open file's records
         self.trace = False
+        # kind of CMPLX(x, y) without KIND=: default complex (REAL*4 parts),
+        # as the standard says; "c16" evaluates the source as if it had
+        # written KIND=8
+        self.cmplx_default = "c8"
 
     # -- loading ---------------------------------------------------------------
     def load(self, path, includes=None):
@@ -513,6 +519,29 @@ class Runtime:
                 self.modules[u.name] = u
             else:
                 self.units[u.name] = u
+
+    # -- list-directed input from in-memory files --------------------------------
+    def io_open(self, unit, name):
+        """OPEN of a file given in self.files; OPENs of other files (the
+        program's output files) are ignored like the WRITEs to them."""
+        if name in self.files:
+            self.units_io[int(unit)] = iter(self.files[name].splitlines())
+
+    def io_close(self, unit):
+        self.units_io.pop(int(unit), None)
+
+    def io_read(self, unit, n):
+        """The values of one list-directed READ: it starts a new record and
+        reads on into the following ones until it has n values."""
+        it = self.units_io.get(int(unit))
+        if it is None:
+            raise IOError(f"READ from unit {unit}, which has no input file open")
+        vals = []
+        while True:
+            line = next(it).strip()
+            vals += [v for v in re.split(r"[\s,]+", line) if v]
+            if len(vals) >= n:
+                return vals[:n]
 
     def provide(self, name, fn):
         """A procedure supplied in Python (a stub for MPI, or a routine whose
@@ -587,7 +616,8 @@ class Runtime:
             elif callable(a):
                 conv.append(a)
             else:
-                t = "i4" if isinstance(a, (int, np.integer)) else "c16" if isinstance(a, complex) else "r8"
+                t = ("l" if isinstance(a, (bool, np.bool_)) else "i4" if isinstance(a, (int, np.integer))
+                     else "c16" if isinstance(a, complex) else "r8")
                 conv.append(Seq(np.array([a], _DT[t]), t))
         return self.proc(name)(*conv)
 
@@ -1376,7 +1406,7 @@ class Translator:
         if name in ("cmplx", "dcmplx"):
             (a, ta, _) = ev[0]
             b, tb = (ev[1][0], ev[1][1]) if len(ev) > 1 else ("0.0", "r8")
-            to = "c16" if name == "dcmplx" else "c8"
+            to = "c16" if name == "dcmplx" else self.rt.cmplx_default
             if "kind" in kw:
                 to = "c16" if eval(kw["kind"][0]) == 8 else "c8"
             if to == "c16":
@@ -1394,6 +1424,9 @@ class Translator:
             return f"np.sum({c})", t, False
         if name == "maxval":
             return f"np.max({ev[0][0]})", ev[0][1], False
+        if name in ("ieee_is_nan", "isnan"):
+            c, t, _ = ev[0]
+            return (f"np.isnan({c})" if arr else f"_math.isnan({c})"), "l", arr
         if name == "minval":
             return f"np.min({ev[0][0]})", ev[0][1], False
         if name == "allocated":
@@ -1757,7 +1790,21 @@ class Translator:
         self.emit(f"{target} = {tl} + _trip({tl}, {th}, {ts}) * {ts}", ind)
 
     def stmt(self, s, ind):
-        if s in ("continue",) or re.match(r"^(write|print|open|close|format|flush|inquire|rewind|backspace)\b", s):
+        m = re.match(r"^(open|close)\s*\(", s)
+        if m:
+            ctl = split_top(s[s.index("(") + 1:match_paren(s, s.index("("))])
+            unit = next((c for c in ctl if "=" not in c), None)
+            unit = unit or next(c.split("=", 1)[1] for c in ctl if c.split("=", 1)[0].strip() == "unit")
+            if m.group(1) == "close":
+                self.emit(f"_rt.io_close({self.int_ex(parse_expr(unit))})", ind)
+                return
+            f = next((c.split("=", 1)[1].strip() for c in ctl if c.split("=", 1)[0].strip() == "file"), None)
+            if f and f[0] in "'\"" and f[-1] == f[0]:
+                self.emit(f"_rt.io_open({self.int_ex(parse_expr(unit))}, {f[1:-1]!r})", ind)
+            else:
+                self.emit("pass", ind)
+            return
+        if s in ("continue",) or re.match(r"^(write|print|format|flush|inquire|rewind|backspace)\b", s):
             self.emit("pass", ind)
             return
         m = re.match(r"^if\s*\(", s)
@@ -1809,8 +1856,23 @@ class Translator:
                 self.emit(f"{ref} = _FArr(np.zeros(({', '.join(exts)},), _DT[{sym.t!r}], order='F'), "
                           f"({', '.join(lbs)},), {sym.t!r})", ind)
             return
-        if re.match(r"^read\b", s):
-            raise NotImplementedError("READ statements")
+        if re.match(r"^read\s*\(", s):
+            i = s.index("(")
+            j = match_paren(s, i)
+            ctl = split_top(s[i + 1:j])
+            if len(ctl) != 2 or ctl[1].strip() != "*":
+                raise NotImplementedError(f"READ other than list-directed: {s!r}")
+            items = split_top(s[j + 1:].strip()) if s[j + 1:].strip() else []
+            if any(it.strip().startswith("(") for it in items):
+                raise NotImplementedError(f"implied DO in READ: {s!r}")
+            self.emit(f"_v = _rt.io_read({self.int_ex(parse_expr(ctl[0]))}, {len(items)})", ind)
+            for q, it in enumerate(items):
+                le = parse_expr(it.strip())
+                kind, sym, ref = self.resolve(le[1])
+                if sym is None:
+                    raise NameError(f"{self.unit.name}: unknown name {le[1]}")
+                self.assign(le, it, f"_from_text(_v[{q}], {sym.t!r})", sym.t, False, ind)
+            return
         # assignment
         i = _assign_split(s)
         if i is None:
@@ -1818,6 +1880,11 @@ class Translator:
         lhs, rhs = s[:i].strip(), s[i + 1:].strip()
         le = parse_expr(lhs)
         c, t, arr = self.ex(parse_expr(rhs))
+        self.assign(le, lhs, c, t, arr, ind)
+
+    def assign(self, le, lhs, c, t, arr, ind):
+        """Store the value c (type t, an array if arr) in the variable,
+        element or section le."""
         if le[0] == "name":
             kind, sym, ref = self.resolve(le[1])
             if kind is None:
@@ -1839,7 +1906,7 @@ class Translator:
             else:
                 self.emit(f"{ref}.a[{idx}] = {self.conv(c, t, sym.t)}", ind)
             return
-        raise NotImplementedError(f"assignment {s!r}")
+        raise NotImplementedError(f"assignment to {lhs!r}")
 
     def arr_conv(self, c, t, to, arr):
         if not arr:
@@ -1969,6 +2036,21 @@ _GLOBALS = {"np": np, "_math": math, "_cmath": __import__("cmath"), "_f32": np.f
             "_fint": _fint, "_nint": _nint, "_aint": _aint, "_sign": _sign, "_mod": _mod, "_trip": _trip,
             "_Goto": _Goto, "_Stop": _Stop, "_scalar_arg": _scalar_arg, "_array_arg": _array_arg,
             "_elem": _elem, "_section": _section, "_view": _view, "_view_rest": view_rest}
+
+
+def _from_text(tok, t):
+    """A list-directed input value for a variable of type t."""
+    if t in ("i4", "i8"):
+        return int(tok)
+    if t in ("r4", "r8"):
+        v = float(tok.replace("d", "e").replace("D", "E"))
+        return float(np.float32(v)) if t == "r4" else v
+    if t == "l":
+        return tok.lstrip(".").upper().startswith("T")
+    raise NotImplementedError(f"list-directed READ into type {t}")
+
+
+_GLOBALS["_from_text"] = _from_text
 
 
 def translate(rt, unit):

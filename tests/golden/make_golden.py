@@ -15,6 +15,18 @@ fortran_interp.py, so the oracle's restatement of the Poisson solver is
 checked against the reference itself.  Each file holds the metric arrays
 the solve used, the right-hand sides, kx^2 and the reference's phi.
 
+step_<case>.npz: the reference's time stepping -- REM_DIV_CURV
+(src/duct.F90:2472-2850), then per step DO RK_STEP = 1,3: CALL RK_DUCT
+(src/duct.F90:237-2460, with src/boundary.F90, src/mpi_duct.F90,
+src/ALLOCATION.F90, and JACOBI_TRANS and INIT_DUCT for the set-up) -- on
+the cases of tests/ekcases.golden_step_cases: the state after the steps
+(modes 0..NKX; the ones above are zero), the divergence printed after
+every projection, JACOBI_TRANS's metrics on the two curvilinear grids, and
+a SHA-256 of the inputs, so the test knows that it regenerated the same
+ones.  fft.F90 is missing from the reference tree:
+the x-transforms are the oracle's (1/NX forward, unnormalised inverse,
+modes above NKX zero), and MPI with one rank copies.
+
 Run where the reference tree is available, with its root as the argument:
     python tests/golden/make_golden.py <path of the ekman_bl tree>
 """
@@ -70,8 +82,53 @@ def mudpack_goldens(ref_root: str) -> None:
         print(f"wrote mudpack_{name}.npz", rhs.shape)
 
 
+def case_digest(st, th_bar):
+    """SHA-256 of a case's inputs: the state's bytes, then TH_BAR's."""
+    import hashlib
+    h = hashlib.sha256()
+    for a in st:
+        h.update(np.ascontiguousarray(a, np.complex128).tobytes())
+    if th_bar is not None:
+        h.update(np.ascontiguousarray(th_bar, np.float64).tobytes())
+    return h.hexdigest()
+
+
+def step_goldens(ref_root: str) -> None:
+    """Reference time steps: REM_DIV_CURV, then per step DO RK_STEP = 1,3:
+    RK_DUCT, on the cases of tests/ekcases.golden_step_cases."""
+    here = os.path.dirname(os.path.abspath(__file__))
+    sys.path.insert(0, here)
+    sys.path.insert(0, os.path.join(here, ".."))
+    sys.path.insert(0, os.path.join(here, "..", ".."))
+    import reference_run as rr
+    from ekcases import golden_step_cases
+    for name, (p, xp, yp, st, tb, steps) in golden_step_cases().items():
+        sponge = (p.ny_s_t, p.nz_s_r, p.nz_s_l) if p.sponge_type else None
+        rt = rr.runtime(ref_root, p.nx, p.ny, p.nz, sponge=sponge, phi64=not p.quirk_phi_fp32)
+        rr.duct_setup(rt, p, xp, yp, st, tb)
+        # JACOBI_TRANS's metrics on the curvilinear grids, in the oracle's layout
+        metrics = {}
+        if name in ("sheared", "refgrid"):
+            for nm in ("int_jacob", "gmat_11", "gmat_12", "gmat_22", "cjob_11", "cjob_12", "cjob_21", "cjob_22"):
+                a = rt.var("run_variable", nm).a
+                metrics[f"metric_{nm}"] = a.T if a.ndim == 2 else np.transpose(a, (2, 1, 0))
+        rr.record_divergence(rt)
+        rr.rem_div_curv(rt)
+        for _ in range(steps):
+            rr.rk_step(rt)
+        state = np.stack(rr.get_state(rt))
+        nkx = p.nx // 3
+        # the modes above NKX are kept only where they are not all zero
+        high = {"state_high": state[..., nkx + 1:]} if np.any(state[..., nkx + 1:]) else {}
+        np.savez_compressed(os.path.join(here, f"step_{name}.npz"), nx=p.nx, ny=p.ny, nz=p.nz, steps=steps,
+                            quirk_phi_fp32=p.quirk_phi_fp32, inputs_sha256=case_digest(st, tb),
+                            state=state[..., :nkx + 1], divergence=np.array(rt.divergence), **high, **metrics)
+        print(f"wrote step_{name}.npz", state.shape, len(rt.divergence), "divergences")
+
+
 if __name__ == "__main__":
     if len(sys.argv) != 2:
         sys.exit("usage: make_golden.py <path of the ekman_bl tree>")
     main(sys.argv[1])
     mudpack_goldens(sys.argv[1])
+    step_goldens(sys.argv[1])

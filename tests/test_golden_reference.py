@@ -12,12 +12,19 @@ restatement to the reference itself.
   with the reference's settings (FMG + at most 6 W(2,1) cycles, REAL*4 1e-6
   relative change) on the three test grids for kx^2 in {0, 0.3, 1, 7, 50}:
   the oracle's solve must agree bit for bit.
+- step_<case>.npz: REM_DIV_CURV and two time steps of RK_DUCT
+  (src/duct.F90:237-2850) on a uniform, a sheared and the reference's own
+  grid (the last with a read-in TH_BAR), with sponge_th on, and once with
+  phi kept in REAL*8: the oracle's state and divergences must agree to
+  rounding level.
 """
 import os
+import sys
 
 import numpy as np
 import pytest
 
+from ekcases import golden_step_cases
 from ekman_bl_gb300.params import default_params
 from oracle import ekref
 
@@ -42,3 +49,114 @@ def test_oracle_poisson_equals_reference_mudpack(case):
     for q, k in enumerate(g["kx2"]):
         ref = g["phi"][q]
         assert np.array_equal(phi[q], ref), (q, k, np.abs(phi[q] - ref).max(), np.abs(ref).max())
+
+
+def _step_case(name):
+    g = _fixture(f"step_{name}.npz")
+    sys.path.insert(0, GOLDEN)
+    from make_golden import case_digest
+    p, xp, yp, st, tb, steps = golden_step_cases()[name]
+    assert case_digest(st, tb) == str(g["inputs_sha256"]), "inputs changed: regenerate the fixture"
+    assert (p.nx, p.ny, p.nz, steps) == (int(g["nx"]), int(g["ny"]), int(g["nz"]), int(g["steps"]))
+    return g, p, xp, yp, st, tb, steps
+
+
+def _oracle_steps(p, xp, yp, st, tb, steps, by_substep):
+    m = ekref.metrics_from_grid(p, xp, yp)
+    if tb is not None:
+        m["th_bar"][:p.ny + 2, :p.nz + 2] = tb
+    o = ekref.Oracle(p, m)
+    try:
+        if p.sponge_type:
+            o.set_sponge(*ekref.sponge_profiles(p, xp, yp))
+        o.upload(*st)
+        o.set_time(p.time, p.time_step)
+        o.rem_div()
+        divs = [o.divergence()]
+        if by_substep:
+            # the driver loop spelled out: TIME_STEP + 1, RK_DUCT three times, TIME + DT
+            for _ in range(steps):
+                t, ts, dt = o.get_time()
+                o.set_time(t, ts + 1)
+                for rk in (1, 2, 3):
+                    o.rk_substep(rk)
+                    divs.append(o.divergence())
+                o.set_time(t + dt, ts + 1)
+        else:
+            o.step(steps)
+        return np.stack(o.download()), divs
+    finally:
+        o.close()
+
+
+@pytest.mark.parametrize("case", ["small", "sheared", "refgrid", "sponge", "small_phi64"])
+def test_oracle_steps_equal_reference_rk_duct(case):
+    """REM_DIV_CURV and two RK3 steps of the oracle against the reference's
+    own RK_DUCT.  The interpreter evaluates each Fortran expression in
+    source order while the oracle's C++ groups a few sums differently, so
+    the bar is rounding level: 1e-14 relative L2 for velocity and scalar,
+    1e-12 for the pressure, the divergence after every projection to 1e-10
+    relative.  ekref_step gives the same state as the substeps."""
+    g, p, xp, yp, st, tb, steps = _step_case(case)
+    got, divs = _oracle_steps(p, xp, yp, st, tb, steps, True)
+    assert np.array_equal(got, _oracle_steps(p, xp, yp, st, tb, steps, False)[0])
+    nkx = p.nx // 3
+    ref = g["state"]
+    for f, name in enumerate(("CU1", "CU2", "CU3", "CP", "CTH")):
+        den = np.linalg.norm(ref[f])
+        err = np.linalg.norm(got[f, ..., :nkx + 1] - ref[f]) / (den if den > 0 else 1.0)
+        # CP sums the Poisson solutions, whose conditioning (~1e3 here) lifts
+        # rounding-level differences in their right-hand sides
+        assert err <= (1e-12 if name == "CP" else 1e-14), (name, err)
+    high = g["state_high"] if "state_high" in g.files else np.zeros_like(got[..., nkx + 1:])
+    assert np.array_equal(got[..., nkx + 1:], high)
+    np.testing.assert_allclose(divs, g["divergence"], rtol=1e-10)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["small", "sheared", "refgrid", "sponge", "small_phi64"])
+def test_gpu_steps_against_reference_rk_duct(case):
+    """The library's FP64 path (MUDPACK's own iteration) against the same
+    fixtures.  With phi kept in REAL*8 the bar is the plain path's 1e-10;
+    where phi is rounded to REAL*4 as the reference does, last-bit
+    differences in phi can round the other way, so 1e-6 (the bar of the
+    quirk_phi_fp32 tests)."""
+    from ekman_bl_gb300 import build as ekbuild
+    from ekman_bl_gb300.duct import DuctSolver, metrics_from_grid, sponge_profiles
+    ekbuild.build()
+    g, p, xp, yp, st, tb, steps = _step_case(case)
+    m = metrics_from_grid(p, xp, yp)
+    if tb is not None:
+        m["th_bar"][:p.ny + 2, :p.nz + 2] = tb
+    s = DuctSolver(p, m)
+    try:
+        if p.sponge_type:
+            s.set_sponge(*sponge_profiles(p, xp, yp))
+        s.upload(*st)
+        s.set_time(p.time, p.time_step)
+        s.rem_div_curv()
+        s.step(steps)
+        got = np.stack(s.download())
+        div = s.divergence()
+    finally:
+        s.close()
+    tol = 1e-6 if p.quirk_phi_fp32 else 1e-10
+    nkx = p.nx // 3
+    for f, name in enumerate(("CU1", "CU2", "CU3", "CP", "CTH")):
+        ref = g["state"][f]
+        err = np.linalg.norm(got[f, ..., :nkx + 1] - ref) / np.linalg.norm(ref)
+        assert err <= (100 * tol if name == "CP" else tol), (name, err)
+    assert div == pytest.approx(float(g["divergence"][-1]), rel=1e-3 if p.quirk_phi_fp32 else 1e-7)
+
+
+@pytest.mark.parametrize("case", ["sheared", "refgrid"])
+def test_metrics_equal_reference_jacobi_trans(case):
+    """JACOBI_TRANS (src/diablo.F90:1088-1570) as the reference computes it
+    from the grid file: the oracle's metrics and the library's host routine
+    are equal bit for bit."""
+    from ekman_bl_gb300.duct import metrics_from_grid
+    g, p, xp, yp, st, tb, steps = _step_case(case)
+    for m in (ekref.metrics_from_grid(p, xp, yp), metrics_from_grid(p, xp, yp)):
+        for k in ("int_jacob", "gmat_11", "gmat_12", "gmat_22", "cjob_11", "cjob_12", "cjob_21", "cjob_22"):
+            ref = g[f"metric_{k}"]
+            assert np.array_equal(m[k], ref), (k, np.abs(m[k] - ref).max())

@@ -18,26 +18,14 @@ import math
 import numpy as np
 import pytest
 
-from ekcases import rel_l2, refgrid_case, sheared_case, small_case
+from ekcases import les_case, rel_l2, refgrid_case, sheared_case, small_case
 from ekman_bl_gb300.duct import les_metrics_from_grid, metrics_from_grid
-from ekman_bl_gb300.params import EK_F_CF1, EK_F_CF2, EK_F_CF3, EK_F_CFTH, EK_F_CR1, ekman_state, spectral_shape
+from ekman_bl_gb300.params import EK_F_CF1, EK_F_CF2, EK_F_CF3, EK_F_CFTH, EK_F_CR1, spectral_shape
 from oracle import ekref
 
 ALPHA = 2.44950  # les_chan.F90 PARAMETER alpha
 
 
-def les_case(case="small", noise=0.3, seed=4):
-    base = {"small": small_case, "sheared": sheared_case, "refgrid": refgrid_case}[case]
-    p, xp, yp, _ = base()
-    st = ekman_state(p, yp, noise, seed)
-    if case != "refgrid":
-        # a nonzero scalar and Kelvin-Helmholtz-like shear for a lively subgrid field
-        st = list(st)
-        rng = np.random.default_rng(seed + 1)
-        sub = (p.ny, p.nz, p.nx // 3)
-        st[4][1:p.ny + 1, 1:p.nz + 1, 1:p.nx // 3 + 1] += noise * (rng.standard_normal(sub) + 1j * rng.standard_normal(sub))
-    p.les, p.les_model_type, p.les_model_type_th, p.create_new_flow = 1, 2, 1, 0
-    return p, xp, yp, tuple(st)
 
 
 def oracle_for(p, xp, yp, st):

@@ -12,24 +12,11 @@ import math
 import numpy as np
 import pytest
 
-from ekcases import rel_l2, small_case
+from ekcases import rel_l2, small_case, sponge_case
 from ekman_bl_gb300.duct import DuctSolver, metrics_from_grid, sponge_profiles
 from oracle import ekref
 
 
-def sponge_case(sponge_type, dynamic=True, save_stats_int=4):
-    p, xp, yp, st = small_case()
-    p.sponge_type = sponge_type
-    p.ny_s_t = p.ny // 2
-    p.nz_s_r = p.nz - 3           # streamwise sponge on the last 4 K and first ones
-    p.nz_s_l = p.nz + 1 - p.nz_s_r
-    p.save_stats_int = save_stats_int
-    p.time_step = 0
-    st = [a.copy() for a in st]
-    if not dynamic:
-        # upper layer of CU3X(0,K,J) exactly WBULK0: |mean - WBULK0| = 0
-        st[2][p.ny_s_t:, :, 0] = p.wbulk0
-    return p, xp, yp, st
 
 
 def formula_profiles(p, xp, yp):

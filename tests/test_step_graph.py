@@ -12,12 +12,10 @@ a capped solve and for a NaN divergence.
 import numpy as np
 import pytest
 
-from ekcases import small_case
+from ekcases import les_case, small_case, sponge_case
 from ekman_bl_gb300 import build as ekbuild
 from ekman_bl_gb300.duct import DuctSolver, les_metrics_from_grid, metrics_from_grid, sponge_profiles
 from ekman_bl_gb300.params import EK_MG_STOP_RESIDUAL
-from test_les import les_case
-from test_sponge import sponge_case
 
 pytestmark = pytest.mark.gpu
 
