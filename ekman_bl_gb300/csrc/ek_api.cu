@@ -117,6 +117,9 @@ void set_delta_t(Ctx &c, double dt) {
 // MULTIGRID_MUDPACK ignores mud2cr's ierror = -1 (mg_solver2d.F90:195-199,
 // mud2cr.f:204-207).
 int projection_status(const Ctx &c, int mg) {
+  // REM_DIV_CURV ends with IF (DELTA_T .LT. 1.0E-4) STOP 'DELTA_T is zero'
+  // (duct.F90:2812): the bound is the REAL*4 literal 1.0E-4
+  if (c.p.delta_t < static_cast<double>(1.0e-4f)) return EK_ERR_DT;
   if (mg == EK_OK) return EK_OK;
   if (mg == EK_ERR_NOT_CONVERGED) return c.p.mg_stop == EK_MG_STOP_RESIDUAL ? EK_ERR_NOT_CONVERGED : EK_OK;
   return mg;
@@ -255,7 +258,10 @@ int substep(Ctx &c, int rk) {
 // divergence of each substep are read once, after the step.
 bool step_graph_eligible(const Ctx &c) {
   const ek_params &p = c.p;
+  // a time step below the reference's bound stops the run after the first
+  // substep's projection, which the eager path reports
   return c.step_graphs && !c.timing && p.mg_fast && !p.variable_dt && p.f_type == 1 &&
+         p.delta_t >= static_cast<double>(1.0e-4f) &&
          !(c.guess.net && c.guess.use) && !c.guess.sink_x;
 }
 
@@ -981,6 +987,7 @@ int ekgpu_rk_substep(ek_ctx *h, int rk) {
     if (rk < 1 || rk > 3) return fail(c, EK_ERR_ARG, "rk_step must be 1, 2 or 3");
     const int st = substep(c, rk);
     if (st == EK_ERR_NAN) return fail(c, EK_ERR_NAN, "DIV is a NaN");
+    if (st == EK_ERR_DT) return fail(c, EK_ERR_DT, "DELTA_T is zero");
     if (st == EK_ERR_NOT_CONVERGED) return fail(c, st, "a Poisson problem reached mg_maxcy above the tolerance");
     return st;
   });
@@ -1009,6 +1016,7 @@ int ekgpu_step(ek_ctx *h, int nsteps) {
         for (int rk = 1; rk <= 3; ++rk) {
           const int st = substep(c, rk);
           if (st == EK_ERR_NAN) return fail(c, EK_ERR_NAN, "DIV is a NaN");
+          if (st == EK_ERR_DT) return fail(c, EK_ERR_DT, "DELTA_T is zero");
           if (st == EK_ERR_NOT_CONVERGED) late = st;
           else if (st != EK_OK) return st;
         }
@@ -1106,6 +1114,7 @@ int ekgpu_rem_div(ek_ctx *h) {
     if (st == EK_ERR_NAN) return fail(c, EK_ERR_NAN, "DIV is a NaN");
     if (st != EK_OK) return st;
     const int ps = projection_status(c, mg);
+    if (ps == EK_ERR_DT) return fail(c, ps, "DELTA_T is zero");
     if (ps == EK_ERR_NOT_CONVERGED) return fail(c, ps, "a Poisson problem reached mg_maxcy above the tolerance");
     return ps;
   });

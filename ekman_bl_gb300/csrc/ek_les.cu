@@ -43,7 +43,10 @@ namespace ek {
 
 namespace {
 
-constexpr double kAlpha = 2.44950;  // les_chan.F90 PARAMETER alpha (test-filter width ratio)
+// les_chan.F90:30,37 REAL*8 alpha; PARAMETER (alpha=2.44950): the test-filter
+// width ratio.  The literal is default REAL, so the parameter holds 2.4495
+// rounded to single precision (2.4495000839...), not the decimal value.
+constexpr double kAlpha = static_cast<double>(2.44950f);
 constexpr int kLineThreads = 256;
 // planes of the FP32 weight table: pg[0..9] (eta and zeta differences),
 // 1/J, then the GMAT_12, GMAT_12_y, GMAT_12_z faces (K+1,J,2), (K,J,2),

@@ -21,7 +21,7 @@ EK_MG_STOP_RELCHANGE, EK_MG_STOP_RESIDUAL = 0, 1
 
 STATUS = {0: "EK_OK", 1: "EK_ERR_ARG", 2: "EK_ERR_CUDA", 3: "EK_ERR_NOT_CONVERGED",
           4: "EK_ERR_NAN", 5: "EK_ERR_TIMEOUT", 6: "EK_ERR_STATE",
-          7: "EK_ERR_IO"}
+          7: "EK_ERR_IO", 8: "EK_ERR_DT"}
 
 # REAL*4 literal 10.0**(-6) of mg_solver2d.F90:188, widened to REAL*8.
 MUDPACK_TOLMAX = float(np.float32(10.0) ** np.float32(-6))

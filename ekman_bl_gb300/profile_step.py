@@ -31,6 +31,8 @@ def main():
     ap.add_argument("--layout", default="", help="LANESxSEG for every line solve (e.g. 8x8) instead of tuning")
     ap.add_argument("--les", action="store_true",
                     help="dynamic-Smagorinsky LES on (CREATE_NEW_FLOW = .FALSE.: subgrid terms from the first step)")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="issue every launch from the host (no whole-step CUDA graph), for per-kernel profiling")
     ap.add_argument("--guess", action="store_true",
                     help="train the learned initial guess on one warm-up step (50 Adam steps) and use it (needs --mixed)")
     args = ap.parse_args()
@@ -50,6 +52,8 @@ def main():
     if args.les:
         p.les, p.create_new_flow = 1, 0
     s = DuctSolver(p, metrics_from_grid(p, xp, yp))
+    if args.no_graph:
+        s.set_step_graph(False)
     if p.les:
         s.set_les_metrics(les_metrics_from_grid(p, xp, yp))
     s.upload(*state)

@@ -44,7 +44,10 @@ typedef enum ek_status {
   EK_ERR_TIMEOUT = 5,        /* reserved: no kernel of this library waits on a flag,
                                 a peer or a barrier, so no call returns it        */
   EK_ERR_STATE = 6,          /* call order violated (e.g. step before metrics)  */
-  EK_ERR_IO = 7              /* restart file missing, unreadable or malformed  */
+  EK_ERR_IO = 7,             /* restart file missing, unreadable or malformed  */
+  EK_ERR_DT = 8              /* DELTA_T below 1.0E-4 after a projection (reference:
+                                STOP 'DELTA_T is zero', duct.F90:2812; the bound is
+                                the REAL*4 literal, 9.99999974737875e-05)       */
 } ek_status;
 
 /* Boundary-wall index into the *_bc arrays, in input.dat order

@@ -28,7 +28,9 @@ using namespace ekref_detail;
 
 namespace {
 
-constexpr double kAlpha = 2.44950;  // les_chan.F90 PARAMETER (alpha = 2.44950)
+// les_chan.F90:30,37 REAL*8 alpha; PARAMETER (alpha = 2.44950): a default-REAL
+// literal, so alpha is 2.4495 rounded to single precision, widened.
+constexpr double kAlpha = static_cast<double>(2.44950f);
 constexpr double kBeta = 1.0;       // PARAMETER (beta = 1.d0)
 
 inline cplx cdiv_r(cplx a, double r) { return {a.re / r, a.im / r}; }

@@ -793,6 +793,8 @@ extern "C" int ekref_rem_div(ekref_ctx *c) {
   div = div / ((double)(c->NXP) * (double)NY * (double)NZ);
   c->last_div = div;
   if (std::isnan(div)) return fail(c, EK_ERR_NAN, "DIV is a NaN");
+  // IF (DELTA_T .LT. 1.0E-4) STOP 'DELTA_T is zero' (duct.F90:2812), a REAL*4 bound
+  if (c->p.delta_t < static_cast<double>(1.0e-4f)) return fail(c, EK_ERR_DT, "DELTA_T is zero");
   return st == EK_ERR_NOT_CONVERGED ? EK_OK : st;  // the reference ignores ierror
 }
 

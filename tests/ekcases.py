@@ -47,12 +47,12 @@ def refgrid_case(nx=16, seed=2, stride=1):
     return p, xp, yp, st
 
 
-def sponge_case(sponge_type, dynamic=True, save_stats_int=4):
+def sponge_case(sponge_type, dynamic=True, save_stats_int=4, nx=16):
     """small_case with sponge_th on (SPONGE_TYPE 1 parabolic, 2 exponential):
     a top sponge from NY_S_T = NY/2 and streamwise sponges on the last and
     first four K.  dynamic=False puts WBULK0 exactly in the top layer of the
     mean streamwise flow, so the dynamic mean-flow branch stays idle."""
-    p, xp, yp, st = small_case()
+    p, xp, yp, st = small_case(nx=nx)
     p.sponge_type = sponge_type
     p.ny_s_t = p.ny // 2
     p.nz_s_r = p.nz - 3           # streamwise sponge on the last 4 K and first ones
@@ -66,11 +66,12 @@ def sponge_case(sponge_type, dynamic=True, save_stats_int=4):
     return p, xp, yp, st
 
 
-def les_case(case="small", noise=0.3, seed=4):
+def les_case(case="small", noise=0.3, seed=4, **grid):
     """A test grid with the dynamic Smagorinsky terms on from the first step
-    (CREATE_NEW_FLOW = 0) and a noisier state."""
+    (CREATE_NEW_FLOW = 0) and a noisier state; grid goes to the grid's case
+    function (nx, stride)."""
     base = {"small": small_case, "sheared": sheared_case, "refgrid": refgrid_case}[case]
-    p, xp, yp, _ = base()
+    p, xp, yp, _ = base(**grid)
     st = ekman_state(p, yp, noise, seed)
     if case != "refgrid":
         # a nonzero scalar and Kelvin-Helmholtz-like shear for a lively subgrid field
@@ -89,6 +90,14 @@ def rel_l2(a, b):
     return np.linalg.norm((a - b).ravel()) / (den if den > 0 else 1.0)
 
 
+def cfl_case(cfl, delta_t_set, nx=16):
+    """small_case under VARIABLE_DT: COURANT_CURV_MPI after every step's
+    RK_STEP = 3 ADI (UPDATE_DT = 1)."""
+    p, xp, yp, st = small_case(nx=nx)
+    p.variable_dt, p.update_dt, p.cfl, p.delta_t_set = 1, 1, cfl, delta_t_set
+    return p, xp, yp, st
+
+
 def th_bar_profile(p, xpoint, ypoint):
     """A read-in background scalar TH_BAR [J, K] for runs without
     CONT_STRAT (JACOBI_TRANS reads it from density_data_input.dat): linear
@@ -103,12 +112,17 @@ def golden_step_cases():
     """The runs of the reference's RK_DUCT kept as fixtures (step_<name>.npz):
     name -> (p, xpoint, ypoint, state, th_bar or None, steps).  p has
     quirk_phi_fp32 = 1, the reference's own rounding of phi, except in
-    small_phi64."""
+    small_phi64.  les_small's five steps cover C_DYN computed with
+    FIRST_TIME, kept, and recomputed at TIME_STEP 5."""
     out = {}
     for name, case, steps in (("small", small_case, 2), ("sheared", lambda: sheared_case(nx=8), 2),
                               ("refgrid", lambda: refgrid_case(8, stride=2), 2),
-                              ("sponge", lambda: sponge_case(2, True, save_stats_int=4), 2),
-                              ("small_phi64", small_case, 2)):
+                              ("sponge", lambda: sponge_case(2, True, save_stats_int=4, nx=8), 2),
+                              ("small_phi64", lambda: small_case(nx=8), 2),
+                              ("cfl", lambda: cfl_case(0.2, 1.0, nx=8), 2),
+                              ("les_small", lambda: les_case("small"), 5),
+                              ("les_sheared", lambda: les_case("sheared", nx=8), 2),
+                              ("les_refgrid", lambda: les_case("refgrid", nx=8, stride=2), 2)):
         p, xp, yp, st = case()
         p.quirk_phi_fp32 = 0 if name.endswith("phi64") else 1
         tb = None if p.cont_strat else th_bar_profile(p, xp, yp)

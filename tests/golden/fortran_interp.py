@@ -1696,6 +1696,24 @@ class Translator:
                     continue
                 if ended:
                     ended.clear()
+                m = re.match(r"^select\s*case\s*\((.*)\)$", s)
+                if m:
+                    arms = []
+                    stop = lambda l, t: re.match(r"^(case\b|end\s*select$)", t)
+                    if parse_block(stop):
+                        raise NotImplementedError("statements between SELECT CASE and its first CASE")
+                    while True:
+                        lab2, s2, n2 = body[pos]
+                        pos += 1
+                        if re.match(r"^end\s*select$", s2):
+                            break
+                        mc = re.match(r"^case\s*(default$|\((.*)\)$)", s2)
+                        if not mc:
+                            raise NotImplementedError(f"statement {s2!r}")
+                        sel = None if mc.group(1) == "default" else split_top(mc.group(2))
+                        arms.append((sel, parse_block(stop)))
+                    out.append(("select", lab, m.group(1), arms, n))
+                    continue
                 m = re.match(r"^do\s+while\s*\((.*)\)$", s)
                 if m:
                     blk = parse_block(lambda l, t: re.match(r"^end\s*do$", t))
@@ -1744,7 +1762,16 @@ class Translator:
         k = nd[0]
         try:
             if k == "s":
-                self.stmt(nd[2], ind)
+                mark = len(self.lines)
+                try:
+                    self.stmt(nd[2], ind)
+                except NotImplementedError as e:
+                    # a statement outside the subset (string building for
+                    # output file names, system calls): an error only if
+                    # it is executed
+                    del self.lines[mark:]
+                    msg = f"{self.unit.path}:{nd[-1]}: {e}"
+                    self.emit(f"raise NotImplementedError({msg!r})", ind)
             elif k == "if":
                 _, lab, arms, els, n = nd
                 for i, (cond, blk) in enumerate(arms):
@@ -1754,6 +1781,34 @@ class Translator:
                 if els is not None:
                     self.emit("else:", ind)
                     self.block(els, ind + 1)
+            elif k == "select":
+                _, lab, expr, arms, n = nd
+                c, t, _ = self.ex(parse_expr(expr))
+                v = f"_sel{n}"
+                self.emit(f"{v} = {c}", ind)
+                first, default = True, None
+                for sel, blk in arms:
+                    if sel is None:
+                        default = blk
+                        continue
+                    tests = []
+                    for item in sel:
+                        if ":" in item:
+                            lo, hi = (x.strip() for x in item.split(":", 1))
+                            parts = ([f"{v} >= {self.ex(parse_expr(lo))[0]}"] if lo else []) + \
+                                    ([f"{v} <= {self.ex(parse_expr(hi))[0]}"] if hi else [])
+                            tests.append("(" + " and ".join(parts) + ")")
+                        else:
+                            tests.append(f"{v} == {self.ex(parse_expr(item))[0]}")
+                    self.emit(f"{'if' if first else 'elif'} {' or '.join(tests)}:", ind)
+                    self.block(blk, ind + 1)
+                    first = False
+                if default is not None:
+                    if first:
+                        self.block(default, ind)
+                    else:
+                        self.emit("else:", ind)
+                        self.block(default, ind + 1)
             elif k == "while":
                 _, lab, cond, blk, n = nd
                 c, t, _ = self.ex(parse_expr(cond))
@@ -1822,7 +1877,7 @@ class Translator:
         if s == "return":
             self.emit(self.return_code(), ind)
             return
-        m = re.match(r"^stop\b\s*(.*)$", s)
+        m = re.match(r"^(?:stop|pause)\b\s*(.*)$", s)
         if m:
             self.emit(f"raise _Stop({m.group(1)!r})", ind)
             return

@@ -21,9 +21,10 @@ step_<case>.npz: the reference's time stepping -- REM_DIV_CURV
 src/ALLOCATION.F90, and JACOBI_TRANS and INIT_DUCT for the set-up) -- on
 the cases of tests/ekcases.golden_step_cases: the state after the steps
 (modes 0..NKX; the ones above are zero), the divergence printed after
-every projection, JACOBI_TRANS's metrics on the two curvilinear grids, and
-a SHA-256 of the inputs, so the test knows that it regenerated the same
-ones.  fft.F90 is missing from the reference tree:
+every projection, TIME and DELTA_T, C_DYN of the LES runs, JACOBI_TRANS's
+metrics on the two curvilinear grids (the LES ones on the LES runs of
+those grids), and a SHA-256 of the inputs, so the test knows that it
+regenerated the same ones.  fft.F90 is missing from the reference tree:
 the x-transforms are the oracle's (1/NX forward, unnormalised inverse,
 modes above NKX zero), and MPI with one rank copies.
 
@@ -93,9 +94,10 @@ def case_digest(st, th_bar):
     return h.hexdigest()
 
 
-def step_goldens(ref_root: str) -> None:
+def step_goldens(ref_root: str, only=None) -> None:
     """Reference time steps: REM_DIV_CURV, then per step DO RK_STEP = 1,3:
-    RK_DUCT, on the cases of tests/ekcases.golden_step_cases."""
+    RK_DUCT, on the cases of tests/ekcases.golden_step_cases (those named
+    in only, if given)."""
     here = os.path.dirname(os.path.abspath(__file__))
     sys.path.insert(0, here)
     sys.path.insert(0, os.path.join(here, ".."))
@@ -103,26 +105,37 @@ def step_goldens(ref_root: str) -> None:
     import reference_run as rr
     from ekcases import golden_step_cases
     for name, (p, xp, yp, st, tb, steps) in golden_step_cases().items():
+        if only and name not in only:
+            continue
         sponge = (p.ny_s_t, p.nz_s_r, p.nz_s_l) if p.sponge_type else None
         rt = rr.runtime(ref_root, p.nx, p.ny, p.nz, sponge=sponge, phi64=not p.quirk_phi_fp32)
         rr.duct_setup(rt, p, xp, yp, st, tb)
         # JACOBI_TRANS's metrics on the curvilinear grids, in the oracle's layout
         metrics = {}
+        names = []
         if name in ("sheared", "refgrid"):
-            for nm in ("int_jacob", "gmat_11", "gmat_12", "gmat_22", "cjob_11", "cjob_12", "cjob_21", "cjob_22"):
-                a = rt.var("run_variable", nm).a
-                metrics[f"metric_{nm}"] = a.T if a.ndim == 2 else np.transpose(a, (2, 1, 0))
+            names = [("run_variable", nm) for nm in ("int_jacob", "gmat_11", "gmat_12", "gmat_22", "cjob_11",
+                                                     "cjob_12", "cjob_21", "cjob_22")]
+        if name in ("les_sheared", "les_refgrid"):
+            names = [("les_chan_var", f"gmat_{a}_{d}") for a in ("11", "12", "22") for d in ("y", "z")]
+        for mod, nm in names:
+            a = rt.var(mod, nm).a
+            metrics[f"metric_{nm}"] = a.T if a.ndim == 2 else np.transpose(a, (2, 1, 0))
         rr.record_divergence(rt)
         rr.rem_div_curv(rt)
         for _ in range(steps):
             rr.rk_step(rt)
         state = np.stack(rr.get_state(rt))
+        extra = {"time": rt.var("run_variable", "time")[0], "delta_t": rt.var("time_step_var", "delta_t")[0]}
+        if p.les:
+            extra["c_dyn"] = rt.var("les_chan_var", "c_dyn").a.T.copy()
         nkx = p.nx // 3
         # the modes above NKX are kept only where they are not all zero
         high = {"state_high": state[..., nkx + 1:]} if np.any(state[..., nkx + 1:]) else {}
         np.savez_compressed(os.path.join(here, f"step_{name}.npz"), nx=p.nx, ny=p.ny, nz=p.nz, steps=steps,
                             quirk_phi_fp32=p.quirk_phi_fp32, inputs_sha256=case_digest(st, tb),
-                            state=state[..., :nkx + 1], divergence=np.array(rt.divergence), **high, **metrics)
+                            state=state[..., :nkx + 1], divergence=np.array(rt.divergence), **high, **metrics,
+                            **extra)
         print(f"wrote step_{name}.npz", state.shape, len(rt.divergence), "divergences")
 
 

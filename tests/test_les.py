@@ -23,7 +23,9 @@ from ekman_bl_gb300.duct import les_metrics_from_grid, metrics_from_grid
 from ekman_bl_gb300.params import EK_F_CF1, EK_F_CF2, EK_F_CF3, EK_F_CFTH, EK_F_CR1, spectral_shape
 from oracle import ekref
 
-ALPHA = 2.44950  # les_chan.F90 PARAMETER alpha
+# les_chan.F90:37 PARAMETER (alpha=2.44950) into a REAL*8: the literal is
+# default REAL, so alpha is 2.4495 rounded to single precision
+ALPHA = float(np.float32(2.44950))
 
 
 
