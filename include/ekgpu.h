@@ -47,7 +47,9 @@ typedef enum ek_status {
   EK_ERR_IO = 7,             /* restart file missing, unreadable or malformed  */
   EK_ERR_DT = 8              /* DELTA_T below 1.0E-4 after a projection (reference:
                                 STOP 'DELTA_T is zero', duct.F90:2812; the bound is
-                                the REAL*4 literal, 9.99999974737875e-05)       */
+                                the REAL*4 literal, 9.99999974737875e-05).  The
+                                substep is complete; its CP update, which the
+                                reference would not reach, is included.        */
 } ek_status;
 
 /* Boundary-wall index into the *_bc arrays, in input.dat order
