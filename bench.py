@@ -45,6 +45,27 @@ if ROOT not in sys.path:
 
 WORKLOAD = "ekman_strat_512x385x257"
 MG_TOL = 1e-8
+# the mixed method's state path: 1 float-float transforms and ADI, 2 FP32
+# transforms and ADI on increments (ek_params.ff_arith)
+FF_ARITH = 2
+STATE_DTYPE = {
+    1: "mixed: f64 spectral state and spectral terms; float-float (~48-bit) physical fields, state transforms "
+       "and ADI; f32 nonlinear-term transforms and V-cycles; float-float Poisson residual and update",
+    2: "mixed: f64 spectral state and spectral terms; f32 physical fields, with the ADI and the state "
+       "transforms in f32 on increments (CU += FFT(increment)); f32 nonlinear-term transforms and V-cycles; "
+       "float-float Poisson residual and update",
+}
+STATE_PRECISION = {
+    1: "FP64 spectral fields, spectral right-hand side and projection; physical fields as float-float planes "
+       "(~48-bit): state-carrying x-transforms and ADI in float-float; the nonlinear-term transforms and the "
+       "transforms of the explicit increment S = R - J phi in FP32; Poisson: float-float residual and update "
+       "around FP32 V-cycles",
+    2: "FP64 spectral fields, spectral right-hand side and projection; physical fields in FP32; each ADI sweep "
+       "solves in FP32 for the increment of its field (the J phi terms cancel algebraically) and the FP32 "
+       "transform of the total increment is added to the FP64 spectral state; the nonlinear-term transforms "
+       "and the transforms of the explicit increment S = R - J phi in FP32; Poisson: float-float residual "
+       "and update around FP32 V-cycles",
+}
 METRIC = "RK3 steps/s and Poisson solves/s at 1e-8 residual: learned+batched vs plain, 1 GB300"
 
 
@@ -134,9 +155,10 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------
-def setup_solver(device_index: int, mg_fast: int = 1, fft_fp32: int = 1, workload=WORKLOAD):
+def setup_solver(device_index: int, mg_fast: int = 1, fft_fp32: int = 1, workload=WORKLOAD, ff_arith=None):
     """A solver of a named workload (or a Workload) on its own stream, with
-    the initial field projected; returns (w, p, xp, yp, state, solver, stream)."""
+    the initial field projected; returns (w, p, xp, yp, state, solver, stream).
+    ff_arith: the state path of the mixed method (default FF_ARITH)."""
     import torch
 
     from ekman_bl_gb300 import build as ekbuild
@@ -150,7 +172,7 @@ def setup_solver(device_index: int, mg_fast: int = 1, fft_fp32: int = 1, workloa
     p, xp, yp, state = workload_setup(w, EK_MG_STOP_RESIDUAL)
     p.mg_fast = mg_fast
     p.fft_fp32 = fft_fp32
-    p.ff_arith = 1 if fft_fp32 else 0
+    p.ff_arith = (FF_ARITH if ff_arith is None else ff_arith) if fft_fp32 else 0
     solver = DuctSolver(p, metrics_from_grid(p, xp, yp))
     if p.les:
         solver.set_les_metrics(les_metrics_from_grid(p, xp, yp))
@@ -542,18 +564,12 @@ def run_gpu(args):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "mixed: f64 state and spectral terms; f32 nonlinear-term transforms and V-cycles; "
-                     "float-float (~48-bit) state transforms, ADI-input transforms in f32, Poisson residual "
-                     "and update",
+            "dtype": STATE_DTYPE[FF_ARITH],
             "data": "synthetic (seeded laminar Ekman spiral + 1% Gaussian noise; no reference dataset exists)",
             "config": {"workload": WORKLOAD, "nx": p.nx, "ny_plus_2": p.ny + 2, "nz_plus_2": p.nz + 2,
                        "re": w.re, "pr": w.pr, "ri": w.ri, "delta_t": p.delta_t,
                        "method": "batched mixed-precision projection (no learned guess)",
-                       "precision": "FP64 fields, spectral right-hand side, ADI and projection; the "
-                                    "state-carrying x-transforms in float-float (~48-bit) arithmetic; the "
-                                    "nonlinear-term transforms and the transforms of the explicit increment "
-                                    "S = R - J phi in FP32; Poisson: float-float residual and update around "
-                                    "FP32 V-cycles",
+                       "precision": STATE_PRECISION[FF_ARITH],
                        "poisson": f"relative residual {MG_TOL:g} per problem, kx=0 included (its right-hand "
                                   f"side projected onto the operator's range, zero-mean solution)",
                        "mg_corrections_per_substep_max": mg_cycles,

@@ -93,10 +93,20 @@ void build_adi_factors(Ctx &c) {
           F.a = dalloc<double>(c, a.size());
           F.ib = dalloc<double>(c, ib.size());
           F.u = dalloc<double>(c, u.size());
+          if (c.p.ff_arith) {
+            F.a2 = dalloc<float2>(c, a.size());
+            F.ib2 = dalloc<float2>(c, ib.size());
+            F.u2 = dalloc<float2>(c, u.size());
+          }
         }
         EK_CUDA(cudaMemcpyAsync(F.a, a.data(), sizeof(double) * a.size(), cudaMemcpyHostToDevice, c.stream));
         EK_CUDA(cudaMemcpyAsync(F.ib, ib.data(), sizeof(double) * ib.size(), cudaMemcpyHostToDevice, c.stream));
         EK_CUDA(cudaMemcpyAsync(F.u, u.data(), sizeof(double) * u.size(), cudaMemcpyHostToDevice, c.stream));
+        if (F.a2) {
+          split_ff(c, F.a, F.a2, a.size());
+          split_ff(c, F.ib, F.ib2, ib.size());
+          split_ff(c, F.u, F.u2, u.size());
+        }
         EK_CUDA(cudaStreamSynchronize(c.stream));
       }
 }
@@ -144,14 +154,28 @@ int substep(Ctx &c, int rk) {
   launch_spectral_rhs(c, rk);
   // FP32 copies of the physical fields for the nonlinear terms (fft_fp32)
   const bool f32 = p.fft_fp32 != 0;
+  // float-float physical fields: the FP32 copy is the high part, the low
+  // part goes to the FP64 buffer's first half, no FP64 field is written
+  const bool ffp = ff_fields(c);
+  // increment form: the state's inverse transforms are FP32, into the FP32
+  // copies only
+  const bool inc = inc_fields(c);
   // to physical space (duct.F90:656-673)
   {
     C2rArgs a{};
     a.j0 = 0; a.j1 = d.NY + 1; a.k0 = 0; a.k1 = d.NZ + 1;
-    a.src = c.CU1; a.dst = c.U1; a.dstf = f32 ? c.U1f : nullptr; launch_c2r(c, a);
-    a.src = c.CU2; a.dst = c.U2; a.dstf = f32 ? c.U2f : nullptr; launch_c2r(c, a);
-    a.src = c.CU3; a.dst = c.U3; a.dstf = f32 ? c.U3f : nullptr; launch_c2r(c, a);
-    if (th) { a.src = c.CTH; a.dst = c.TH; a.dstf = f32 ? c.THf : nullptr; launch_c2r(c, a); }
+    a.lowp = inc ? 1 : 0;
+    auto to_phys = [&](const cplx_t *src, double *dst, float *dstf) {
+      a.src = src;
+      a.dst = (ffp || inc) ? nullptr : dst;
+      a.dstf = f32 ? dstf : nullptr;
+      a.dstlo = ffp ? ff_lo(dst) : nullptr;
+      launch_c2r(c, a);
+    };
+    to_phys(c.CU1, c.U1, c.U1f);
+    to_phys(c.CU2, c.U2, c.U2f);
+    to_phys(c.CU3, c.U3, c.U3f);
+    if (th) to_phys(c.CTH, c.TH, c.THf);
   }
   // les_chan / les_chan_th (duct.F90:641-654): NU_T and the stress terms
   // that the transforms below add to CF1..CF3 and CFTH
@@ -238,10 +262,26 @@ int substep(Ctx &c, int rk) {
     R2cArgs a{};
     a.j0 = 0; a.j1 = d.NY + 1; a.k0 = 0; a.k1 = d.NZ + 1;
     a.pro = PRO_LOAD; a.epi = EPI_STORE;
-    a.a = c.U1; a.dst = c.CU1; launch_r2c(c, a);
-    a.a = c.U2; a.dst = c.CU2; launch_r2c(c, a);
-    a.a = c.U3; a.dst = c.CU3; launch_r2c(c, a);
-    if (th) { a.a = c.TH; a.dst = c.CTH; launch_r2c(c, a); }
+    auto to_fourier = [&](double *src, const float *srcf, cplx_t *dst, double *R) {
+      if (inc) {
+        // CU += the FP32 transform of the ADI's total increment
+        a.lowp = 1;
+        a.epi = EPI_ADD;
+        a.a = nullptr;
+        a.af = inc_plane(c, R);
+        a.alo = nullptr;
+      } else {
+        a.a = ffp ? nullptr : src;
+        a.af = ffp ? srcf : nullptr;
+        a.alo = ffp ? ff_lo(src) : nullptr;
+      }
+      a.dst = dst;
+      launch_r2c(c, a);
+    };
+    to_fourier(c.U1, c.U1f, c.CU1, c.R1);
+    to_fourier(c.U2, c.U2f, c.CU2, c.R2);
+    to_fourier(c.U3, c.U3f, c.CU3, c.R3);
+    if (th) to_fourier(c.TH, c.THf, c.CTH, c.RTH);
   }
   int mg = EK_OK;
   run_rem_div(c, TEMP4, true, &mg);
@@ -583,7 +623,7 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
   if (p.sponge_type < 0 || p.sponge_type > 2) return reject("SPONGE_TYPE must be 0, 1 or 2");
   if (p.sponge_type != 0 && p.save_stats_int < 1) return reject("SAVE_STATS_INT must be >= 1 with a sponge");
   if (p.fft_fp32 < 0 || p.fft_fp32 > 2) return reject("fft_fp32 must be 0, 1 or 2");
-  if (p.ff_arith < 0 || p.ff_arith > 1) return reject("ff_arith must be 0 or 1");
+  if (p.ff_arith < 0 || p.ff_arith > 2) return reject("ff_arith must be 0, 1 or 2");
   if (p.variable_dt && (p.update_dt < 1 || !(p.cfl > 0.0) || !(p.delta_t_set > 0.0)))
     return reject("VARIABLE_DT needs UPDATE_DT >= 1, CFL > 0 and DELTA_T_SET > 0");
   if (p.sponge_type != 0 && p.ny_s_t <= p.ny && p.ny_s_t < 0) return reject("NY_S_T must be >= 0");

@@ -19,6 +19,7 @@
 //            EPI_SUB_IK dst -= i kx X      (duct.F90:712-718)
 // so no product or transform temporary ever reaches HBM.
 #include <map>
+#include <type_traits>
 #include <mutex>
 #include <utility>
 
@@ -115,7 +116,90 @@ __device__ __forceinline__ void dif_fft(V *z, int M, const V *tw, bool conj_tw, 
   }
 }
 
-template <typename T>
+// One value exchanged with the lane whose index differs in the bits of m.
+__device__ __forceinline__ float2 shfl_x(float2 v, int m) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+template <typename V>
+__device__ __forceinline__ V csub(V a, V b) {
+  V r;
+  r.x = a.x - b.x;
+  r.y = a.y - b.y;
+  return r;
+}
+template <typename V>
+__device__ __forceinline__ V caddv(V a, V b) {
+  V r;
+  r.x = a.x + b.x;
+  r.y = a.y + b.y;
+  return r;
+}
+
+// The same radix-2 DIF (same butterflies, same twiddles, bit-reversed
+// output in z) with the warp's M = 32 E points held in registers: lane l
+// keeps points l + 32 t, t < E.  The log2(E) stages whose pairs are 32 or
+// more apart run between a lane's own registers; the five stages below run
+// between lanes through shuffles, where a lane's twiddle depends only on the
+// lane.  Shared memory is touched once to load and once to store, instead
+// of twice per stage.
+template <int E, typename V>
+__device__ __forceinline__ void dif_fft_reg(V *z, const V *tw, bool conj_tw, int lane) {
+  constexpr int M = 32 * E;
+  V v[E];
+#pragma unroll
+  for (int t = 0; t < E; ++t) v[t] = z[lane + 32 * t];
+#pragma unroll
+  for (int h = E / 2; h >= 1; h >>= 1) {
+    // span s = 32 h: pairs (t, t + h) within each block of 2h registers
+    const int stride = M / (64 * h);  // M / (2 s)
+#pragma unroll
+    for (int t = 0; t < E; ++t) {
+      if (t & h) continue;
+      const V a = v[t], b = v[t + h];
+      v[t] = caddv(a, b);
+      const int tt = lane + 32 * (t & (h - 1));  // n mod s
+      V dlt = csub(a, b);
+      if (tt != 0) {
+        V w = tw[tt * stride];
+        if (conj_tw) w.y = -w.y;
+        dlt = cmul(dlt, w);
+      }
+      v[t + h] = dlt;
+    }
+  }
+#pragma unroll
+  for (int s = 16; s >= 1; s >>= 1) {
+    const bool upper = (lane & s) != 0;
+    const int tt = lane & (s - 1);
+    V w = tw[tt * (M / (2 * s))];
+    if (conj_tw) w.y = -w.y;
+#pragma unroll
+    for (int t = 0; t < E; ++t) {
+      const V p = shfl_x(v[t], s);
+      if (!upper) {
+        v[t] = caddv(v[t], p);
+      } else {
+        V dlt = csub(p, v[t]);
+        if (tt != 0) dlt = cmul(dlt, w);
+        v[t] = dlt;
+      }
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < E; ++t) z[lane + 32 * t] = v[t];
+  __syncwarp();
+}
+
+// The register form for M = 32 E (E > 0, chosen per launch so that each
+// size gets its own register budget), the shared-memory loop otherwise.
+template <int E, typename V>
+__device__ __forceinline__ void dif_fft_any(V *z, int M, const V *tw, bool conj_tw, int lane) {
+  __syncwarp();
+  if constexpr (E > 0) dif_fft_reg<E>(z, tw, conj_tw, lane);
+  else dif_fft(z, M, tw, conj_tw, lane);
+}
+
+template <typename T, int E>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArgs args) {
   using V = typename Cx<T>::V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -136,7 +220,19 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
   constexpr bool kF = sizeof(T) == 4;
   const bool fin = kF && args.af != nullptr;  // FP32 copies of the inputs
   if (args.pro == PRO_LOAD) {
-    for (int n = lane; n < NX; n += 32) zr[n] = (T)args.a[base + n];
+    if constexpr (std::is_same_v<T, FF>) {
+      if (args.alo) {
+        // a float-float field: the pair as it is, no FP64 split
+        for (int n = lane; n < NX; n += 32) zr[n] = FF(args.af[base + n], args.alo[base + n]);
+      } else {
+        for (int n = lane; n < NX; n += 32) zr[n] = (T)args.a[base + n];
+      }
+    } else if (fin) {
+      // an FP32 field (the increment of the state)
+      for (int n = lane; n < NX; n += 32) zr[n] = (T)args.af[base + n];
+    } else {
+      for (int n = lane; n < NX; n += 32) zr[n] = (T)args.a[base + n];
+    }
   } else if (args.pro == PRO_PROD) {
     const T jac = from_f64<T>(fc.m.jac[d.m2(k, j)]);
     if (fin)
@@ -194,7 +290,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
       for (int n = lane; n < NX; n += 32) zr[n] = zr[n] + es * (T)args.extra[base + n];
   }
   __syncwarp();
-  dif_fft(z, M, tw_m<T>(fc), false, lane);
+  dif_fft_any<E>(z, M, tw_m<T>(fc), false, lane);
   // split: X[k] = E + W^k O, E = (Z_k + conj Z_{M-k})/2, O = -i (Z_k - conj Z_{M-k})/2
   cplx_t *dst = args.dst + d.ic(0, k, j);
   const T inv = from_f64<T>(fc.inv_nx);
@@ -243,7 +339,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
   }
 }
 
-template <typename T>
+template <typename T, int E>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArgs args) {
   using V = typename Cx<T>::V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -297,11 +393,24 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
     if (kk != 0 && 2 * kk != M) z[M - kk] = merge(b, a, twn[M - kk]);
   }
   __syncwarp();
-  dif_fft(z, M, tw_m<T>(fc), true, lane);
+  dif_fft_any<E>(z, M, tw_m<T>(fc), true, lane);
   const T *zr = reinterpret_cast<const T *>(z);
   double *dst = args.dst ? args.dst + d.ip(0, k, j) : nullptr;
   float *dstf = args.dstf ? args.dstf + d.ip(0, k, j) : nullptr;
   const int NX = d.NX;
+  if constexpr (std::is_same_v<T, FF>) {
+    if (args.dstlo) {
+      // float-float planes: the high part is also the field's FP32 copy
+      float *dlo = args.dstlo + d.ip(0, k, j);
+      for (int n = lane; n < NX + 2; n += 32) {
+        FF v(0.0f, 0.0f);
+        if (n < NX) v = zr[2 * brev(n >> 1, fc.logM) + (n & 1)];
+        dstf[n] = v.hi;
+        dlo[n] = v.lo;
+      }
+      return;
+    }
+  }
   for (int n = lane; n < NX + 2; n += 32) {
     T v = T(0.0);
     if (n < NX) {
@@ -315,6 +424,44 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
       if (dst) dst[n] = (double)v;
       if (dstf) dstf[n] = d2f_bits((double)v);
     }
+  }
+}
+
+// Launch a transform.  The register form of the FFT pays in the FP32
+// inverse transform (measured on 512 x 385 x 257: 0.34 -> 0.23 ms per
+// launch); in the forward transforms, whose stencil prologues want many
+// warps in flight, and in the FP64 and float-float ones, its extra registers
+// cost more than the shared-memory passes it saves, so they keep the loop.
+template <typename T>
+void run_r2c(dim3 grid, size_t smem, cudaStream_t s, const FftConst &fc, const R2cArgs &a) {
+  k_r2c<T, 0><<<grid, 32 * kWarpsPerBlock, smem, s>>>(fc, a);
+}
+template <typename T>
+void run_c2r(dim3 grid, size_t smem, cudaStream_t s, const FftConst &fc, const C2rArgs &a) {
+  const unsigned nt = 32 * kWarpsPerBlock;
+  if constexpr (std::is_same_v<T, float>) {
+    switch (fc.M) {
+      case 32: k_c2r<T, 1><<<grid, nt, smem, s>>>(fc, a); return;
+      case 64: k_c2r<T, 2><<<grid, nt, smem, s>>>(fc, a); return;
+      case 128: k_c2r<T, 4><<<grid, nt, smem, s>>>(fc, a); return;
+      case 256: k_c2r<T, 8><<<grid, nt, smem, s>>>(fc, a); return;
+      case 512: k_c2r<T, 16><<<grid, nt, smem, s>>>(fc, a); return;
+      default: break;
+    }
+  }
+  k_c2r<T, 0><<<grid, nt, smem, s>>>(fc, a);
+}
+template <typename T>
+void smem_attributes() {
+  const int b = 96 * 1024;
+  EK_CUDA(cudaFuncSetAttribute(k_r2c<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+  EK_CUDA(cudaFuncSetAttribute(k_c2r<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+  if constexpr (std::is_same_v<T, float>) {
+    EK_CUDA(cudaFuncSetAttribute(k_c2r<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    EK_CUDA(cudaFuncSetAttribute(k_c2r<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    EK_CUDA(cudaFuncSetAttribute(k_c2r<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    EK_CUDA(cudaFuncSetAttribute(k_c2r<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    EK_CUDA(cudaFuncSetAttribute(k_c2r<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
   }
 }
 
@@ -355,9 +502,9 @@ void launch_r2c(Ctx &c, const R2cArgs &a) {
   const int nops = (a.pro == PRO_LOAD) ? 1 : (a.pro == PRO_PROD) ? 2 : 3;
   const double epi = (a.epi == EPI_STORE) ? 16.0 * (c.d.NX2P + 1) : 32.0 * (c.d.NKX + 1);
   KScope ks(c, KC_R2C, nlines * (8.0 * c.d.NX * nops + epi));
-  if (fft_lowp(c, a.lowp)) k_r2c<float><<<grid, 32 * kWarpsPerBlock, smem / 2, c.stream>>>(fc, a);
-  else if (fft_ff(c, a.lowp)) k_r2c<FF><<<grid, 32 * kWarpsPerBlock, smem, c.stream>>>(fc, a);
-  else k_r2c<double><<<grid, 32 * kWarpsPerBlock, smem, c.stream>>>(fc, a);
+  if (fft_lowp(c, a.lowp)) run_r2c<float>(grid, smem / 2, c.stream, fc, a);
+  else if (fft_ff(c, a.lowp)) run_r2c<FF>(grid, smem, c.stream, fc, a);
+  else run_r2c<double>(grid, smem, c.stream, fc, a);
   after_launch(c);
 }
 
@@ -368,9 +515,9 @@ void launch_c2r(Ctx &c, const C2rArgs &a) {
   const dim3 grid((unsigned)((a.k1 - a.k0 + 1 + kWarpsPerBlock - 1) / kWarpsPerBlock), (unsigned)(a.j1 - a.j0 + 1));
   const size_t smem = sizeof(double2) * fc.M * kWarpsPerBlock;
   KScope ks(c, KC_C2R, nlines * (16.0 * (c.d.NKX + 1) * (a.src2 ? 2 : 1) + 8.0 * (c.d.NX + 2)));
-  if (fft_lowp(c, a.lowp)) k_c2r<float><<<grid, 32 * kWarpsPerBlock, smem / 2, c.stream>>>(fc, a);
-  else if (fft_ff(c, a.lowp)) k_c2r<FF><<<grid, 32 * kWarpsPerBlock, smem, c.stream>>>(fc, a);
-  else k_c2r<double><<<grid, 32 * kWarpsPerBlock, smem, c.stream>>>(fc, a);
+  if (fft_lowp(c, a.lowp)) run_c2r<float>(grid, smem / 2, c.stream, fc, a);
+  else if (fft_ff(c, a.lowp)) run_c2r<FF>(grid, smem, c.stream, fc, a);
+  else run_c2r<double>(grid, smem, c.stream, fc, a);
   after_launch(c);
 }
 
@@ -380,12 +527,9 @@ namespace ek {
 void fft_init_attributes() {
   static std::once_flag once;
   std::call_once(once, [] {
-  EK_CUDA(cudaFuncSetAttribute(k_r2c<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-  EK_CUDA(cudaFuncSetAttribute(k_c2r<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-  EK_CUDA(cudaFuncSetAttribute(k_r2c<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-  EK_CUDA(cudaFuncSetAttribute(k_c2r<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-  EK_CUDA(cudaFuncSetAttribute(k_r2c<FF>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-  EK_CUDA(cudaFuncSetAttribute(k_c2r<FF>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+  smem_attributes<double>();
+  smem_attributes<float>();
+  smem_attributes<FF>();
   });
 }
 }  // namespace ek
@@ -484,13 +628,13 @@ int run_standalone(bool forward, int nx, int nkx, long nlines, const double *in,
     a.pro = PRO_LOAD;
     a.epi = EPI_STORE;
     a.k0 = 0; a.k1 = (int)nlines - 1; a.j0 = 0; a.j1 = 0;
-    k_r2c<double><<<grid, 32 * kWarpsPerBlock, smem, s>>>(fc, a);
+    run_r2c<double>(grid, smem, s, fc, a);
   } else {
     C2rArgs a{};
     a.src = reinterpret_cast<const cplx_t *>(in);
     a.dst = out;
     a.k0 = 0; a.k1 = (int)nlines - 1; a.j0 = 0; a.j1 = 0;
-    k_c2r<double><<<grid, 32 * kWarpsPerBlock, smem, s>>>(fc, a);
+    run_c2r<double>(grid, smem, s, fc, a);
   }
   EK_CUDA(cudaPeekAtLastError());
   return EK_OK;

@@ -110,6 +110,9 @@ struct BcSet {
 struct AdiFactors {
   double *a, *ib, *u;
   int nline, nrow;
+  // the same factors split into float-float pairs (hi, lo), for the
+  // float-float sweeps of the mixed path (null until ff_arith needs them)
+  float2 *a2 = nullptr, *ib2 = nullptr, *u2 = nullptr;
 };
 
 // One multigrid level (MUDPACK level k; index k-1).
@@ -331,6 +334,7 @@ struct Ctx {
   double *adi_scr = nullptr;      // LES ADI: 1/B and the upper diagonal of the eliminated rows (two fields)
   double *adi_les_tab = nullptr;  // LES ADI: per-cell row weights of the two sweeps (k_adi_les_tab)
   float2 *adi_ff_tab = nullptr;   // LES ADI, float-float: both sweeps' weights as float pairs
+  float2 *adi_tab2 = nullptr;     // the weights of adi_tab as float pairs (float-float fields)
   // divergence check
   double *div_part = nullptr;
   double last_div = 0.0;
@@ -422,6 +426,9 @@ struct R2cArgs {
   int j0, j1, k0, k1;
   int lowp;               // a nonlinear-term transform (FP32 arithmetic when fft_fp32 = 1)
   const float *af, *bf;   // FP32 copies of a, b read by the FP32 kernel when given
+  // PRO_LOAD of a field held as float-float planes (the float-float kernel
+  // reads the pair af + alo and no FP64 a)
+  const float *alo;
 };
 void launch_r2c(Ctx &c, const R2cArgs &a);
 struct C2rArgs {
@@ -432,6 +439,9 @@ struct C2rArgs {
   int j0, j1, k0, k1;
   int lowp;                  // as R2cArgs::lowp
   float *dstf;               // also write an FP32 copy of dst when given (dst may then be null)
+  // the float-float kernel with dstlo set writes its result as two float
+  // planes, high part to dstf and low part to dstlo, and no FP64 dst
+  float *dstlo;
 };
 void launch_c2r(Ctx &c, const C2rArgs &a);
 
@@ -451,6 +461,27 @@ bool les_active(const Ctx &c);
 // S = R - J phi_old (duct.F90:1127-1161, 1334-2392), without transforming
 // the large J CU part: the FP32 rounding then falls on the O(h) increment.
 inline bool explicit_increment_form(const Ctx &c) { return c.p.fft_fp32 >= 1; }
+// The mixed path's float-float physical fields: with ff_arith and the
+// nonlinear-term transforms in FP32 (and no LES in the substep), the
+// physical U1, U2, U3, TH live as float-float pairs -- the high part is the
+// FP32 copy the nonlinear terms read (U1f ...), the low part sits in the
+// first half of the FP64 buffer (U1 ...) -- from the inverse transform at
+// the substep's start, through the float-float ADI, to the forward transform
+// at its end, so none of those kernels splits or joins an FP64 value per
+// physical point.
+bool ff_fields(const Ctx &c);
+inline float *ff_lo(double *field) { return reinterpret_cast<float *>(field); }
+// The increment form of the state path (ff_arith = 2, nonlinear-term
+// transforms in FP32, no LES in the substep): the inverse transforms of the
+// state are FP32 (the fields' FP32 copies), each ADI sweep solves in FP32 for
+// the increment of its field over the field it starts from, and the forward
+// transform of the total increment (in the second half of the field's R
+// buffer) is added to the FP64 spectral state.  Every FP32 rounding then
+// falls on an O(h) increment or on an O(h) viscous term, never on the state.
+bool inc_fields(const Ctx &c);
+// the total ADI increment of a field: the second float half of its R buffer
+inline float *inc_plane(Ctx &c, double *R) { return reinterpret_cast<float *>(R) + c.d.nphys(); }
+void split_ff(Ctx &c, const double *in, float2 *out, size_t n);
 void les_alloc(Ctx &c);
 void launch_les(Ctx &c, int rk);
 void launch_th_corners(Ctx &c);

@@ -307,6 +307,18 @@ struct AdiArgs {
   // R's slots, and the weights of k_adi_tab with the J phi_old halves folded
   // in; null: R in FP64
   const float *Sf;
+  // float-float fields (k_adi_ffs): the old field, the y-sweep result and
+  // the output as high/low float planes; the right-hand-side weights and the
+  // line's Thomas factors as float pairs
+  const float *po_h, *po_l, *ps_h, *ps_l;
+  float *out_h, *out_l;
+  const float2 *tab2, *fa2, *fib2, *fu2;
+  // increment form (k_adi_inc): the field's FP32 copy, the y sweep's
+  // increment and the sweep's output (y: that increment; z: the total);
+  // brk: on the rows that copy another row (periodic ghosts) the FP32
+  // transform of the spectral difference phi_old(src) - phi_old(row)
+  const float *phf, *dsf, *brk;
+  float *incf;
 };
 
 // Right-hand-side weights of one ADI sweep per cell (tab[t * n2 + m2(k, j)]),
@@ -318,24 +330,41 @@ struct AdiArgs {
 //            t0 = J - c (G22(j+1) + G22(j)), t1 = c G22(j+1), t2 = c G22(j), t3 = -0.5 J
 // (c = NU H/2 [/PR]; the same algebra as duct.F90:1640-1660, 1877-1905, ...)
 template <bool ZS>
-__global__ void k_adi_tab(Dims d, Metrics m, double coef, int sform, double *tab) {
+__global__ void k_adi_tab(Dims d, Metrics m, double coef, int sform, double *tab, float2 *tab2) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
   if (k > d.NZ + 1 || j > d.NY + 1 || k < 1 || j < 1) return;
   const size_t n2 = (size_t)d.LDM * (d.NY + 3), mm = d.m2(k, j);
   const double jac = m.jac[mm];
+  double w[4];
   // R/2 = S/2 + J phi_old/2: with S in place of R the y sweep's J/2 becomes J
   // and the z sweep's -J phi_old/2 term cancels
   if (!ZS) {
     const double gp = m.g11[d.m3(k + 1, j, 2)], gm = m.g11[d.m3(k, j, 2)];
-    tab[mm] = (sform ? jac : 0.5 * jac) - coef * (gp + gm);
-    tab[n2 + mm] = coef * gp;
-    tab[2 * n2 + mm] = coef * gm;
+    w[0] = (sform ? jac : 0.5 * jac) - coef * (gp + gm);
+    w[1] = coef * gp;
+    w[2] = coef * gm;
   } else {
     const double gp = m.g22[d.m3(k, j + 1, 1)], gm = m.g22[d.m3(k, j, 1)];
-    tab[mm] = jac - coef * (gp + gm);
-    tab[n2 + mm] = coef * gp;
-    tab[2 * n2 + mm] = coef * gm;
-    tab[3 * n2 + mm] = sform ? 0.0 : -0.5 * jac;
+    w[0] = jac - coef * (gp + gm);
+    w[1] = coef * gp;
+    w[2] = coef * gm;
+    w[3] = sform ? 0.0 : -0.5 * jac;
+  }
+  for (int t = 0; t < (ZS ? 4 : 3); ++t) {
+    tab[t * n2 + mm] = w[t];
+    // the float-float sweeps read the same weights as float pairs
+    if (tab2) {
+      const FF f(w[t]);
+      tab2[t * n2 + mm] = make_float2(f.hi, f.lo);
+    }
+  }
+}
+
+// A double array split into float-float pairs (hi, lo).
+__global__ void k_split_ff(size_t n, const double *in, float2 *out) {
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    const FF f(in[q]);
+    out[q] = make_float2(f.hi, f.lo);
   }
 }
 
@@ -369,7 +398,7 @@ __global__ void k_adi_les_tab(Dims d, Metrics m, const double *gb, const double 
 // Rows per chunk of the line-solve kernels below: a thread issues every
 // load of a chunk's rows before its recurrence consumes them (the
 // x-dependent LES rows hold more values per row than the plain ones).
-constexpr int kAdiChunk = 8, kLesChunk = 4;
+constexpr int kAdiChunk = 8, kLesChunk = 4, kIncChunkZ = 4;
 
 // CN-ADI line solves with the LES eddy viscosity (duct.F90:1373-1386,
 // 1437-1450, 1489-1500, 1559-1569 for TH; 1667-1680, 1720-1731, 1771-1784,
@@ -748,8 +777,287 @@ __global__ void __launch_bounds__(128) k_adi_seq(AdiArgs a) {
   }
 }
 
-// Corner copies after the TH solve (duct.F90:1606-1624).
-__global__ void k_th_corners(Dims d, double *TH, int zmax1, int zmin6) {
+// k_adi_seq (explicit-increment form) on float-float fields, for the mixed
+// path: the old field, the y-sweep result and the new field are float-float
+// planes and every row runs in float-float arithmetic (about 48 bits) on the
+// FP32 pipe, from the same per-cell weights and host Thomas factors split
+// into float pairs; the only FP64 work left is a boundary row's constant.
+template <bool ZS>
+__global__ void __launch_bounds__(128) k_adi_ffs(AdiArgs a) {
+  const Dims &d = a.d;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int line = ZS ? (int)blockIdx.y : a.zs + (int)blockIdx.y;
+  if (i >= d.NX) return;
+  if (ZS && (line < a.js || line > a.je)) {
+    for (int k = a.zs; k <= a.ze; ++k) {
+      const size_t c = d.ip(i, k, line);
+      a.out_h[c] = a.ps_h[c];
+      a.out_l[c] = a.ps_l[c];
+    }
+    return;
+  }
+  const int nrow = ZS ? d.NZ2 : d.NY2;
+  const int r0 = ZS ? a.zs : a.js, r1 = ZS ? a.ze : a.je;
+  const int n2 = d.LDM * (d.NY + 3);
+  const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
+  const size_t sA = ZS ? sK : sJ;
+  const size_t sX = ZS ? sJ : sK;
+  // the y sweep reads the old field, the z sweep the y sweep's result
+  const float *xh = ZS ? a.ps_h : a.po_h, *xl = ZS ? a.ps_l : a.po_l;
+  const float2 *fa = a.fa2 + (size_t)line * nrow, *fib = a.fib2 + (size_t)line * nrow;
+  const float2 *fu = a.fu2 + (size_t)line * nrow;
+  const size_t c0 = ZS ? d.ip(i, 0, line) : d.ip(i, line, 0);
+  const int m0 = ZS ? line * d.LDM : line, mstep = ZS ? 1 : d.LDM;
+  constexpr int CH = ZS ? 1 : kAdiChunk;
+  FF prev(0.0f, 0.0f);
+  for (int rc = 0; rc < nrow; rc += CH) {
+    FF vv[CH];
+    float2 av[CH];
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int r = rc + u;
+      FF v(0.0f, 0.0f);
+      if (r < nrow) {
+        const size_t c = c0 + (size_t)r * sA;
+        if (r >= r0 && r <= r1) {
+          const float2 *tb = a.tab2 + (m0 + r * mstep);
+          v = FF(0.5f * a.Sf[c], 0.0f) + ff2(tb[0]) * FF(xh[c], xl[c]) + ff2(tb[n2]) * FF(xh[c + sX], xl[c + sX]) +
+              ff2(tb[2 * n2]) * FF(xh[c - sX], xl[c - sX]);
+        }
+        for (int b = 0; b < a.bc.n; ++b) {
+          const BcRow &br = a.bc.r[b];
+          if (br.row != r) continue;
+          if (br.kind == 0) {
+            v = FF(br.val);
+          } else if (br.kind == 1) {
+            const size_t q = ZS ? d.ip(i, br.src, line) : d.ip(i, line, br.src);
+            v = FF(xh[q], xl[q]);
+          } else {
+            v = FF(br.val * a.bcw[br.src + line]);
+          }
+        }
+      }
+      vv[u] = v;
+      av[u] = (r < nrow) ? fa[r] : make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int r = rc + u;
+      if (r < nrow) {
+        prev = (r == 0) ? vv[u] : vv[u] + ff2(av[u]) * prev;
+        const size_t c = c0 + (size_t)r * sA;
+        a.out_h[c] = prev.hi;
+        a.out_l[c] = prev.lo;
+      }
+    }
+  }
+  FF x = prev * ff2(fib[nrow - 1]);
+  {
+    const size_t c = c0 + (size_t)(nrow - 1) * sA;
+    a.out_h[c] = x.hi;
+    a.out_l[c] = x.lo;
+  }
+  for (int rc = nrow - 2; rc >= 0; rc -= CH) {
+    FF gv[CH];
+    float2 uv[CH], bv[CH];
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int r = rc - u;
+      if (r >= 0) {
+        const size_t c = c0 + (size_t)r * sA;
+        gv[u] = FF(a.out_h[c], a.out_l[c]);
+        uv[u] = fu[r];
+        bv[u] = fib[r];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int r = rc - u;
+      if (r >= 0) {
+        x = (gv[u] - ff2(uv[u]) * x) * ff2(bv[u]);
+        const size_t c = c0 + (size_t)r * sA;
+        a.out_h[c] = x.hi;
+        a.out_l[c] = x.lo;
+      }
+    }
+  }
+}
+
+// The ADI in increment form, FP32 (the mixed path with ff_arith = 2).  Each
+// sweep's tridiagonal system M phi_new = v (the rows of k_adi_seq: interior
+// rows (J - c A_line) with v = S/2 + (J + c A_across) phi_base, the boundary
+// rows of APPLY_BC_*, identity rows elsewhere) is solved for the increment
+// over its base field, M (phi_new - phi_base) = v - M phi_base.  For an
+// interior row that right-hand side is S/2 + c (A_k + A_j) phi_base: the
+// J phi terms cancel algebraically, so nothing of size J phi is rounded to
+// FP32, only the O(h) increment S and the O(c) viscous differences.  The y
+// sweep's base is phi_old (the field's FP32 copy) and its output the
+// increment d*; the z sweep's base is phi* = phi_old + d* (d* = 0 on the
+// lines the y sweep leaves alone) and its output the total increment
+// phi_new - phi_old, whose FP32 forward transform is added to the spectral
+// state.  The same host Thomas factors and per-cell weights, rounded to
+// FP32, drive the elimination.
+template <bool ZS>
+__global__ void __launch_bounds__(128) k_adi_inc(AdiArgs a) {
+  const Dims &d = a.d;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int line = ZS ? (int)blockIdx.y : a.zs + (int)blockIdx.y;
+  if (i >= d.NX) return;
+  const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
+  const float *ph = a.phf, *ds = a.dsf;
+  float *out = a.incf;
+  // the base field of the sweep at point q (row k along z)
+  auto base = [&](size_t q, int k) -> float {
+    return (ZS && k >= a.zs && k <= a.ze) ? ph[q] + ds[q] : ph[q];
+  };
+  if (ZS && (line < a.js || line > a.je)) {
+    // phi_new = phi* on the y sweep's lines, phi_old elsewhere
+    for (int k = 0; k < d.NZ2; ++k) {
+      const size_t q = d.ip(i, k, line);
+      out[q] = (k >= a.zs && k <= a.ze) ? ds[q] : 0.0f;
+    }
+    return;
+  }
+  const int nrow = ZS ? d.NZ2 : d.NY2;
+  const int r0 = ZS ? a.zs : a.js, r1 = ZS ? a.ze : a.je;
+  const int n2 = d.LDM * (d.NY + 3);
+  const size_t sA = ZS ? sK : sJ;
+  const float2 *fa = a.fa2 + (size_t)line * nrow, *fib = a.fib2 + (size_t)line * nrow;
+  const float2 *fu = a.fu2 + (size_t)line * nrow;
+  // per-cell weights c G11(k+1), c G11(k) (the y table) and c G22(j+1),
+  // c G22(j) (the z table), high parts of the float pairs
+  const float2 *wk = a.tab2, *wj = a.tab2 + 4 * (size_t)n2;
+  const size_t c0 = ZS ? d.ip(i, 0, line) : d.ip(i, line, 0);
+  const size_t sX = ZS ? sJ : sK;
+  // rows go CH at a time: the chunk's base values along the line (rows
+  // rc-1 .. rc+CH) are loaded once and shared by neighbouring rows, and
+  // every load of the chunk is issued before the recurrence consumes it
+  constexpr int CH = ZS ? kIncChunkZ : kAdiChunk;
+  auto base_row = [&](int r) -> float {
+    if (r < 0 || r >= nrow) return 0.0f;
+    return base(c0 + (size_t)r * sA, ZS ? r : line);
+  };
+  float prev = 0.0f;
+  for (int rc = 0; rc < nrow; rc += CH) {
+    float vv[CH], av[CH], bp[CH + 2];
+#pragma unroll
+    for (int u = 0; u < CH + 2; ++u) bp[u] = base_row(rc - 1 + u);
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int r = rc + u;
+      float v = 0.0f;
+      if (r < nrow) {
+        const size_t q = c0 + (size_t)r * sA;
+        const int k = ZS ? r : line, j = ZS ? line : r;
+        const float p0 = bp[u + 1];
+        if (r >= r0 && r <= r1) {
+          const int m = d.m2(k, j);
+          // along the line: bp; across it: rows of the neighbouring lines
+          const float pap = bp[u + 2], pam = bp[u];
+          const float pxp = base(q + sX, k), pxm = base(q - sX, k);
+          const float pkp = ZS ? pap : pxp, pkm = ZS ? pam : pxm;
+          const float pjp = ZS ? pxp : pap, pjm = ZS ? pxm : pam;
+          v = 0.5f * a.Sf[q] + (wk[n2 + m].x * (pkp - p0) - wk[2 * n2 + m].x * (p0 - pkm)) +
+              (wj[n2 + m].x * (pjp - p0) - wj[2 * n2 + m].x * (p0 - pjm));
+        } else {
+          v = -p0;  // identity row: phi_new = 0
+        }
+        for (int b = 0; b < a.bc.n; ++b) {
+          const BcRow &br = a.bc.r[b];
+          if (br.row != r) continue;
+          if (br.kind == 1) {
+            // the lagged copy (an identity row): phi_base(src) - phi_base(row)
+            // = (phi_old(src) - phi_old(row)) + (d*(src) - d*(row)) in z,
+            // the first part from the spectral difference, so the FP32
+            // roundings of the two old values never enter the ghost rows
+            float dv = a.brk[q];
+            if (ZS) {
+              const size_t qs = d.ip(i, br.src, line);
+              if (br.src >= a.zs && br.src <= a.ze) dv += ds[qs];
+              if (k >= a.zs && k <= a.ze) dv -= ds[q];
+            }
+            v = dv;
+            continue;
+          }
+          const float vb = (br.kind == 0) ? (float)br.val : (float)(br.val * a.bcw[br.src + line]);
+          float mrow = (float)br.dg * p0;
+          if (r > 0) mrow += (float)br.l * bp[u];
+          if (r + 1 < nrow) mrow += (float)br.u * bp[u + 2];
+          v = vb - mrow;
+        }
+      }
+      vv[u] = v;
+      av[u] = (r < nrow) ? fa[r].x : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int r = rc + u;
+      if (r < nrow) {
+        prev = (r == 0) ? vv[u] : fmaf(av[u], prev, vv[u]);
+        out[c0 + (size_t)r * sA] = prev;  // parked until the back substitution
+      }
+    }
+  }
+  // back substitution; the z sweep adds d* to its increment for the total
+  float x = prev * fib[nrow - 1].x;
+  {
+    const size_t q = c0 + (size_t)(nrow - 1) * sA;
+    const int k = ZS ? nrow - 1 : line;
+    out[q] = (ZS && k >= a.zs && k <= a.ze) ? x + ds[q] : x;
+  }
+  for (int rc = nrow - 2; rc >= 0; rc -= CH) {
+    float gv[CH], uv[CH], bv[CH];
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int r = rc - u;
+      if (r >= 0) {
+        gv[u] = out[c0 + (size_t)r * sA];
+        uv[u] = fu[r].x;
+        bv[u] = fib[r].x;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int r = rc - u;
+      if (r >= 0) {
+        x = (gv[u] - uv[u] * x) * bv[u];
+        const size_t q = c0 + (size_t)r * sA;
+        const int k = ZS ? r : line;
+        out[q] = (ZS && k >= a.zs && k <= a.ze) ? x + ds[q] : x;
+      }
+    }
+  }
+}
+
+// TH corner copies (duct.F90:1606-1624) in increment form: the corner's new
+// value is its neighbour's, so its increment is phi_old(nb) + d(nb) -
+// phi_old(corner).
+__global__ void k_th_corners_inc(Dims d, const float *TH, float *dTH, int zmax1, int zmin6) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.NX) return;
+  const int NZ = d.NZ, NY = d.NY;
+  auto cp = [&](int kd, int jd, int ks, int js) {
+    const size_t q = d.ip(i, kd, jd), s = d.ip(i, ks, js);
+    dTH[q] = (TH[s] + dTH[s]) - TH[q];
+  };
+  if (zmax1) {
+    cp(NZ + 1, NY + 1, NZ, NY + 1);
+    cp(NZ + 1, 0, NZ, 0);
+    cp(0, NY + 1, 1, NY + 1);
+    cp(0, 0, 1, 0);
+  }
+  if (zmin6) {
+    cp(NZ + 1, NY + 1, 1, NY + 1);
+    cp(NZ + 1, 0, 1, 0);
+    cp(0, NY + 1, NZ, NY + 1);
+    cp(0, 0, NZ, 0);
+  }
+}
+
+// Corner copies after the TH solve (duct.F90:1606-1624); T = double, or
+// float for each plane of a float-float field.
+template <typename T>
+__global__ void k_th_corners(Dims d, T *TH, int zmax1, int zmin6) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.NX) return;
   const int NZ = d.NZ, NY = d.NY;
@@ -981,20 +1289,32 @@ void launch_spectral_rhs(Ctx &c, int rk) {
 // K = ZSTART..ZEND, J = JSTART..JEND of CFL*DX/|U1|, CFL*J/|U2b|, CFL*J/|U3b|
 // (face velocities as duct.F90:3631-3636), starting from 999.  All terms
 // are positive, so the minimum of their bit patterns is the minimum.
-__global__ void k_courant(Dims d, Metrics m, const double *U1, const double *U2, const double *U3, double cfl,
-                          double dx, unsigned long long *out) {
+// a physical field value: FP64, or the sum of a float-float field's planes
+__device__ __forceinline__ double fld(const double *U, const float *H, const float *L, size_t c) {
+  return H ? f2d_bits(H[c]) + f2d_bits(L[c]) : U[c];
+}
+
+__global__ void k_courant(Dims d, Metrics m, const double *U1, const double *U2, const double *U3, const float *H1,
+                          const float *L1, const float *H2, const float *L2, const float *H3, const float *L3,
+                          double cfl, double dx, unsigned long long *out) {
   __shared__ unsigned long long s[256];
   unsigned long long best = (unsigned long long)__double_as_longlong(999.0);
   const int ni = d.NX + 2, nk = d.ZE - d.ZS + 1, nj = d.JE - d.JS + 1;
   const long n = (long)ni * nk * nj;
   for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
     const int i = (int)(t % ni), k = d.ZS + (int)((t / ni) % nk), j = d.JS + (int)(t / ((long)ni * nk));
+    // the padding points x = NX, NX+1 hold zero velocity (infinite steps,
+    // no effect on the minimum); plane forms do not keep them
+    if (H1 && i >= d.NX) continue;
     const size_t c = d.ip(i, k, j);
     const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
-    const double u2b = 0.5 * m.c22[d.m3(k, j, 1)] * (U2[c] + U2[c - sJ]) + 0.5 * m.c21[d.m3(k, j, 1)] * (U3[c] + U3[c - sJ]);
-    const double u3b = 0.5 * m.c11[d.m3(k, j, 2)] * (U3[c] + U3[c - sK]) + 0.5 * m.c12[d.m3(k, j, 2)] * (U2[c] + U2[c - sK]);
+    const double u2 = fld(U2, H2, L2, c), u3 = fld(U3, H3, L3, c);
+    const double u2b = 0.5 * m.c22[d.m3(k, j, 1)] * (u2 + fld(U2, H2, L2, c - sJ)) +
+                       0.5 * m.c21[d.m3(k, j, 1)] * (u3 + fld(U3, H3, L3, c - sJ));
+    const double u3b = 0.5 * m.c11[d.m3(k, j, 2)] * (u3 + fld(U3, H3, L3, c - sK)) +
+                       0.5 * m.c12[d.m3(k, j, 2)] * (u2 + fld(U2, H2, L2, c - sK));
     const double jac = m.jac[d.m2(k, j)];
-    const double dtx = cfl * dx / fabs(U1[c]);
+    const double dtx = cfl * dx / fabs(fld(U1, H1, L1, c));
     const double dty = cfl * jac / fabs(u2b);
     const double dtz = cfl * jac / fabs(u3b);
     for (double v : {dtx, dty, dtz}) {
@@ -1018,7 +1338,14 @@ void launch_courant(Ctx &c) {
   KScope ks(c, KC_FACE, 8.0 * 5 * (double)(d.NX + 2) * (d.ZE - d.ZS + 1) * (d.JE - d.JS + 1));
   k_set_double<<<1, 1, 0, c.stream>>>(c.cfl_dt, 999.0);
   after_launch(c);
-  k_courant<<<2 * 152, 256, 0, c.stream>>>(d, c.m, c.U1, c.U2, c.U3, c.p.cfl, c.p.lx / c.p.nx,
+  // float-float fields: the two planes; increment form: phi_old's FP32 copy
+  // plus the ADI's total increment
+  const bool ffp = ff_fields(c), inc = inc_fields(c);
+  const bool pl = ffp || inc;
+  float *l1 = inc ? inc_plane(c, c.R1) : ff_lo(c.U1), *l2 = inc ? inc_plane(c, c.R2) : ff_lo(c.U2);
+  float *l3 = inc ? inc_plane(c, c.R3) : ff_lo(c.U3);
+  k_courant<<<2 * 152, 256, 0, c.stream>>>(d, c.m, c.U1, c.U2, c.U3, pl ? c.U1f : nullptr, l1, pl ? c.U2f : nullptr,
+                                          l2, pl ? c.U3f : nullptr, l3, c.p.cfl, c.p.lx / c.p.nx,
                                           reinterpret_cast<unsigned long long *>(c.cfl_dt));
   after_launch(c);
 }
@@ -1058,11 +1385,17 @@ void launch_adi(Ctx &c, int field, int rk) {
     c.allocs.push_back(c.adi_tab);
   }
   a.tab = c.adi_tab;
+  const bool ffp = ff_fields(c), inc = inc_fields(c);
+  if ((ffp || inc) && !c.adi_tab2) {
+    EK_CUDA(cudaMalloc(&c.adi_tab2, sizeof(float2) * 8 * n2));
+    c.allocs.push_back(c.adi_tab2);
+  }
   {
     const dim3 tg((unsigned)((d.NZ + 2 + 63) / 64), (unsigned)(d.NY + 2));
-    k_adi_tab<false><<<tg, 64, 0, c.stream>>>(d, c.m, coef, sform, c.adi_tab);
+    k_adi_tab<false><<<tg, 64, 0, c.stream>>>(d, c.m, coef, sform, c.adi_tab, (ffp || inc) ? c.adi_tab2 : nullptr);
     after_launch(c);
-    k_adi_tab<true><<<tg, 64, 0, c.stream>>>(d, c.m, coef, sform, c.adi_tab + 4 * n2);
+    k_adi_tab<true><<<tg, 64, 0, c.stream>>>(d, c.m, coef, sform, c.adi_tab + 4 * n2,
+                                               (ffp || inc) ? c.adi_tab2 + 4 * n2 : nullptr);
     after_launch(c);
   }
   if (les_active(c)) {
@@ -1133,6 +1466,108 @@ void launch_adi(Ctx &c, int field, int rk) {
     }
     return;
   }
+  if (inc) {
+    float *phf = (field == 0) ? c.THf : (field == 1) ? c.U1f : (field == 2) ? c.U2f : c.U3f;
+    const cplx_t *cu = (field == 0) ? c.CTH : (field == 1) ? c.CU1 : (field == 2) ? c.CU2 : c.CU3;
+    float *dstar = ff_lo(c.PHS);
+    float *brk = ff_lo(c.PHS) + d.nphys();
+    // copy rows: the FP32 transform of CU(src) - CU(row) on their lines
+    auto brackets = [&](const BcSet &bs, int dir) {
+      for (int b = 0; b < bs.n; ++b) {
+        const BcRow &br = bs.r[b];
+        if (br.kind != 1) continue;
+        C2rArgs t{};
+        const long shift = (dir == 0) ? (long)d.ic(0, 0, br.src) - (long)d.ic(0, 0, br.row)
+                                      : (long)d.ic(0, br.src, 0) - (long)d.ic(0, br.row, 0);
+        t.src = cu + shift;
+        t.src2 = cu;
+        t.scale2 = -1.0;
+        t.dstf = brk;
+        t.lowp = 1;
+        if (dir == 0) {
+          t.j0 = t.j1 = br.row;
+          t.k0 = 0;
+          t.k1 = d.NZ + 1;
+        } else {
+          t.k0 = t.k1 = br.row;
+          t.j0 = 0;
+          t.j1 = d.NY + 1;
+        }
+        launch_c2r(c, t);
+      }
+    };
+    brackets(c.bc[field][0], 0);
+    a.phf = phf;
+    a.dsf = dstar;
+    a.brk = brk;
+    a.incf = dstar;
+    a.tab2 = c.adi_tab2;
+    a.fa2 = c.adi[field][rk][0].a2;
+    a.fib2 = c.adi[field][rk][0].ib2;
+    a.fu2 = c.adi[field][rk][0].u2;
+    a.bc = c.bc[field][0];
+    {
+      // read S and the FP32 field (8 bytes), write the increment (4)
+      KScope ks(c, KC_ADI_Y, 12.0 * d.NX * d.NY2 * (a.ze - a.zs + 1));
+      const dim3 grid((d.NX + 127) / 128, a.ze - a.zs + 1);
+      k_adi_inc<false><<<grid, 128, 0, c.stream>>>(a);
+      after_launch(c);
+    }
+    brackets(c.bc[field][1], 1);
+    a.incf = inc_plane(c, const_cast<double *>(R));
+    a.fa2 = c.adi[field][rk][1].a2;
+    a.fib2 = c.adi[field][rk][1].ib2;
+    a.fu2 = c.adi[field][rk][1].u2;
+    a.bc = c.bc[field][1];
+    {
+      // read S, the FP32 field and the y increment, write the total increment
+      KScope ks(c, KC_ADI_Z, 16.0 * d.NX * d.NZ2 * d.NY2);
+      const dim3 grid((d.NX + 127) / 128, d.NY2);
+      k_adi_inc<true><<<grid, 128, 0, c.stream>>>(a);
+      after_launch(c);
+    }
+    return;
+  }
+  if (ffp) {
+    // float-float fields: the high planes are the FP32 copies, the low ones
+    // the first half of the FP64 buffers; PHS holds the y sweep's planes
+    float *hi = (field == 0) ? c.THf : (field == 1) ? c.U1f : (field == 2) ? c.U2f : c.U3f;
+    float *lo = ff_lo(phi);
+    float *ph = ff_lo(c.PHS), *pl = ff_lo(c.PHS) + d.nphys();
+    a.po_h = hi;
+    a.po_l = lo;
+    a.ps_h = ph;
+    a.ps_l = pl;
+    a.out_h = ph;
+    a.out_l = pl;
+    a.tab2 = c.adi_tab2;
+    a.fa2 = c.adi[field][rk][0].a2;
+    a.fib2 = c.adi[field][rk][0].ib2;
+    a.fu2 = c.adi[field][rk][0].u2;
+    a.bc = c.bc[field][0];
+    {
+      // read S (4 bytes) and the old field (8), write the planes (8)
+      KScope ks(c, KC_ADI_Y, 20.0 * d.NX * d.NY2 * (a.ze - a.zs + 1));
+      const dim3 grid((d.NX + 127) / 128, a.ze - a.zs + 1);
+      k_adi_ffs<false><<<grid, 128, 0, c.stream>>>(a);
+      after_launch(c);
+    }
+    a.out_h = hi;
+    a.out_l = lo;
+    a.tab2 = c.adi_tab2 + 4 * n2;
+    a.fa2 = c.adi[field][rk][1].a2;
+    a.fib2 = c.adi[field][rk][1].ib2;
+    a.fu2 = c.adi[field][rk][1].u2;
+    a.bc = c.bc[field][1];
+    {
+      // read S and the y-sweep planes, write the field's planes
+      KScope ks(c, KC_ADI_Z, 20.0 * d.NX * d.NZ2 * (a.je - a.js + 1));
+      const dim3 grid((d.NX + 127) / 128, d.NY2);
+      k_adi_ffs<true><<<grid, 128, 0, c.stream>>>(a);
+      after_launch(c);
+    }
+    return;
+  }
   // y sweep
   a.out = c.PHS;
   a.fa = c.adi[field][rk][0].a;
@@ -1166,7 +1601,15 @@ void launch_th_corners(Ctx &c) {
   const int zmax1 = c.p.th_bc[EK_ZMAX] == 1, zmin6 = c.p.th_bc[EK_ZMIN] == 6;
   if (!zmax1 && !zmin6) return;
   KScope ks(c, KC_ADI_Z, 64.0 * c.d.NX);
-  k_th_corners<<<(c.d.NX + 127) / 128, 128, 0, c.stream>>>(c.d, c.TH, zmax1, zmin6);
+  if (inc_fields(c)) {
+    k_th_corners_inc<<<(c.d.NX + 127) / 128, 128, 0, c.stream>>>(c.d, c.THf, inc_plane(c, c.RTH), zmax1, zmin6);
+  } else if (ff_fields(c)) {
+    k_th_corners<float><<<(c.d.NX + 127) / 128, 128, 0, c.stream>>>(c.d, c.THf, zmax1, zmin6);
+    after_launch(c);
+    k_th_corners<float><<<(c.d.NX + 127) / 128, 128, 0, c.stream>>>(c.d, ff_lo(c.TH), zmax1, zmin6);
+  } else {
+    k_th_corners<double><<<(c.d.NX + 127) / 128, 128, 0, c.stream>>>(c.d, c.TH, zmax1, zmin6);
+  }
   after_launch(c);
 }
 
@@ -1204,6 +1647,9 @@ void launch_projection(Ctx &c, const double *phif, int P, double temp4, bool upd
   ca.j1 = d.NY - 1;
   ca.k0 = 2;
   ca.k1 = d.NZ - 1;
+  // the check's transform is linear in the (small) divergence itself: on the
+  // mixed path FP32 arithmetic keeps it to ~1e-7 relative, widened exactly
+  ca.lowp = explicit_increment_form(c) ? 1 : 0;
   launch_c2r(c, ca);
   KScope ks(c, KC_DIVERGENCE, 8.0 * (d.NX + 2) * (d.NZ - 2) * (d.NY - 2));
   k_div_sum<<<d.NY - 2, 256, 0, c.stream>>>(d, c.SPH, c.div_part);
@@ -1247,4 +1693,16 @@ int finish_divergence(Ctx &c, double *div_out) {
 namespace ek {
 // The RK kernels use the default shared-memory limit.
 void rk_init_attributes() {}
+}  // namespace ek
+
+namespace ek {
+bool ff_fields(const Ctx &c) { return c.p.ff_arith == 1 && c.p.fft_fp32 == 1 && !les_active(c); }
+bool inc_fields(const Ctx &c) { return c.p.ff_arith == 2 && c.p.fft_fp32 == 1 && !les_active(c); }
+
+void split_ff(Ctx &c, const double *in, float2 *out, size_t n) {
+  if (n == 0) return;
+  const unsigned nb = (unsigned)std::min<size_t>((n + 255) / 256, 4 * 152);
+  k_split_ff<<<nb, 256, 0, c.stream>>>(n, in, out);
+  after_launch(c);
+}
 }  // namespace ek

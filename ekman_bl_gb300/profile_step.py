@@ -27,6 +27,7 @@ def main():
     ap.add_argument("--mixed", action="store_true",
                     help="mixed-precision method: mg_fast = 1, fft_fp32 = 1 (needs --tol > 0)")
     ap.add_argument("--ff", action="store_true", help="float-float state-carrying transforms (ff_arith = 1)")
+    ap.add_argument("--ff-arith", type=int, default=-1, help="ff_arith (0, 1, 2); overrides --ff")
     ap.add_argument("--autotune", action="store_true", help="tune the line-solve layouts first, as bench.py does")
     ap.add_argument("--layout", default="", help="LANESxSEG for every line solve (e.g. 8x8) instead of tuning")
     ap.add_argument("--les", action="store_true",
@@ -49,6 +50,8 @@ def main():
         p.mg_fast, p.fft_fp32 = 1, 1
     if args.ff:
         p.ff_arith = 1
+    if args.ff_arith >= 0:
+        p.ff_arith = args.ff_arith
     if args.les:
         p.les, p.create_new_flow = 1, 0
     s = DuctSolver(p, metrics_from_grid(p, xp, yp))

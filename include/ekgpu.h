@@ -126,7 +126,14 @@ typedef struct ek_params {
                                 increment S = R - J phi_old that the ADI starts from (CR then
                                 holds CR - J CU), 2 every transform */
   int ff_arith;              /* 1: the x-transforms fft_fp32 leaves in FP64 use float-float
-                                arithmetic (~48 bits) on the FP32 pipe; fields stay FP64  */
+                                arithmetic (~48 bits) on the FP32 pipe; with fft_fp32 = 1
+                                (and no LES in the substep) the physical fields are then
+                                float-float planes and the ADI runs in float-float too.
+                                2 (fft_fp32 = 1): the state's inverse transforms and the ADI
+                                run in FP32 on increments -- each sweep solves for the
+                                change of its field, whose FP32 forward transform is added
+                                to the FP64 spectral state (LES substeps as with 1).
+                                The spectral fields stay FP64 in every mode.              */
   int les_model_type;        /* LES_MODEL_TYPE: only 2 (dynamic Smagorinsky, C_DYN from the
                                 test filter every 5 steps) is supported                   */
   int les_model_type_th;     /* LES_MODEL_TYPE_TH: only 1 (KAPPA_T = NU_T/PR) is supported */

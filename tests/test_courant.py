@@ -112,3 +112,31 @@ def test_library_stops_below_the_dt_bound(fast):
         assert g.get_time()[1] == 1
     finally:
         g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ff", [1, 2])
+def test_cfl_steps_mixed_path(ff):
+    """VARIABLE_DT on the mixed-precision path, whose physical fields are
+    float-float planes (ff_arith = 1) or an FP32 field plus its FP32
+    increment (ff_arith = 2) when COURANT_CURV_MPI reads them: DELTA_T
+    within 1e-6 of the FP64 oracle's over three steps (it follows the mixed
+    state's ~1e-7 difference), the state within the mixed bar."""
+    p, xp, yp, st = cfl_case(0.2, 1.0)
+    q = type(p).from_buffer_copy(p)
+    q.mg_stop, q.mg_tol, q.mg_maxcy, q.mg_fast, q.fft_fp32, q.ff_arith = EK_MG_STOP_RESIDUAL, 1e-10, 60, 1, 1, ff
+    p.mg_stop, p.mg_tol, p.mg_maxcy = EK_MG_STOP_RESIDUAL, 1e-10, 200
+    g = DuctSolver(q, metrics_from_grid(q, xp, yp))
+    o = ekref.Oracle(p, ekref.metrics_from_grid(p, xp, yp))
+    try:
+        g.upload(*st)
+        o.upload(*st)
+        for _ in range(3):
+            g.step(1)
+            o.step(1)
+            assert g.get_time()[2] == pytest.approx(o.get_time()[2], rel=1e-6)
+        for name, x, y in zip(("CU1", "CU2", "CU3", "CTH"), *[[a[i] for i in (0, 1, 2, 4)] for a in (g.download(), o.download())]):
+            assert rel_l2(x, y) < 1e-5, name
+    finally:
+        g.close()
+        o.close()

@@ -41,20 +41,23 @@ def _oracle(p, xp, yp):
 
 def test_mixed_method_one_step_at_512x385x257():
     """The bench's method and workload: NX = 512, NY+2 = 385, NZ+2 = 257,
-    Re = 1000, Ri = 0.1, dt = 3e-4, every Poisson problem to 1e-8."""
+    Re = 1000, Ri = 0.1, dt = 3e-4, every Poisson problem to 1e-8; both
+    forms of the state path (ff_arith = 1 float-float, 2 FP32 increments)
+    against one step of the oracle."""
     w = dataclasses.replace(WORKLOADS["ekman_strat_512x385x257"], mg_tol=1e-8)
     p, xp, yp, st = workload_setup(w, EK_MG_STOP_RESIDUAL)
-    q = workload_setup(w, EK_MG_STOP_RESIDUAL)[0]
-    q.mg_fast, q.fft_fp32, q.ff_arith = 1, 1, 1
-    g = DuctSolver(q, metrics_from_grid(q, xp, yp))
-    try:
-        g.upload(*st)
-        assert g.rem_div_curv() == 0
-        assert g.step(1) == 0
-        gs = g.download()
-        gdiv, gmg = g.divergence(), g.mg_stats()
-    finally:
-        g.close()
+    runs = {}
+    for ff in (1, 2):
+        q = workload_setup(w, EK_MG_STOP_RESIDUAL)[0]
+        q.mg_fast, q.fft_fp32, q.ff_arith = 1, 1, ff
+        g = DuctSolver(q, metrics_from_grid(q, xp, yp))
+        try:
+            g.upload(*st)
+            assert g.rem_div_curv() == 0
+            assert g.step(1) == 0
+            runs[ff] = (g.download(), g.divergence(), g.mg_stats())
+        finally:
+            g.close()
     o = _oracle(p, xp, yp)
     try:
         o.upload(*st)
@@ -64,12 +67,13 @@ def test_mixed_method_one_step_at_512x385x257():
         odiv = o.divergence()
     finally:
         o.close()
-    errs = {n: rel_l2(a, b) for n, a, b in zip(STATE, gs, os_)}
-    print("mixed vs FP64 oracle after one step at 512x385x257:", errs, "div", gdiv, odiv, gmg)
-    for n in ("CU1", "CU2", "CU3", "CTH"):
-        assert errs[n] <= 1e-5, (n, errs[n])
-    assert gmg["n_not_converged"] == 0 and gmg["max_residual"] <= 1e-8, gmg
-    assert np.isfinite(gdiv) and gdiv <= 3.0 * odiv + 1e-12, (gdiv, odiv)
+    for ff, (gs, gdiv, gmg) in runs.items():
+        errs = {n: rel_l2(a, b) for n, a, b in zip(STATE, gs, os_)}
+        print(f"mixed (ff_arith={ff}) vs FP64 oracle after one step at 512x385x257:", errs, "div", gdiv, odiv, gmg)
+        for n in ("CU1", "CU2", "CU3", "CTH"):
+            assert errs[n] <= 1e-5, (ff, n, errs[n])
+        assert gmg["n_not_converged"] == 0 and gmg["max_residual"] <= 1e-8, gmg
+        assert np.isfinite(gdiv) and gdiv <= 3.0 * odiv + 1e-12, (gdiv, odiv)
 
 
 def test_plain_fp64_three_steps_at_256x257x193():

@@ -273,8 +273,8 @@ def test_les_with_sponge_and_variable_dt():
     p.nz_s_r = p.nz - 3
     p.nz_s_l = p.nz + 1 - p.nz_s_r
     p.save_stats_int = 4
-    # CFL 0.2: steps near 3e-4, above the 1.0E-4 at which REM_DIV_CURV stops
-    p.variable_dt, p.update_dt, p.cfl, p.delta_t_set = 1, 1, 0.2, 1.0
+    # CFL 1: steps near 4e-4, above the 1.0E-4 at which REM_DIV_CURV stops
+    p.variable_dt, p.update_dt, p.cfl, p.delta_t_set = 1, 1, 1.0, 1.0
     sg, so = ekref.sponge_profiles(p, xp, yp)
     g, o = gpu_for(p, xp, yp, st), oracle_for(p, xp, yp, st)
     g.set_sponge(sg, so)

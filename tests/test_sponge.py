@@ -118,7 +118,8 @@ def test_sponge_changes_the_flow():
 
 
 @pytest.mark.gpu
-def test_sponge_mixed_path_with_reset_matches_oracle():
+@pytest.mark.parametrize("ff", [1, 2])
+def test_sponge_mixed_path_with_reset_matches_oracle(ff):
     """The mixed path (FP32 nonlinear and explicit-increment transforms,
     float-float state transforms, mixed multigrid) through the stratified
     z-periodic branch and its reset of CU2X(0,:,:) at TIME_STEP = 2, from a
@@ -135,7 +136,7 @@ def test_sponge_mixed_path_with_reset_matches_oracle():
     p.mg_stop, p.mg_tol, p.mg_maxcy = 1, 1e-10, 200
     o = ekref.Oracle(p, ekref.metrics_from_grid(p, xp, yp))
     q = sponge_case(2, True)[0]
-    q.mg_stop, q.mg_tol, q.mg_maxcy, q.mg_fast, q.fft_fp32, q.ff_arith = 1, 1e-10, 60, 1, 1, 1
+    q.mg_stop, q.mg_tol, q.mg_maxcy, q.mg_fast, q.fft_fp32, q.ff_arith = 1, 1e-10, 60, 1, 1, ff
     g = DuctSolver(q, metrics_from_grid(q, xp, yp))
     g.set_sponge(sg, so)
     o.set_sponge(sg, so)

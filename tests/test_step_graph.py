@@ -25,14 +25,14 @@ def _build():
     ekbuild.build()
 
 
-def _mixed(p):
-    p.mg_stop, p.mg_tol, p.mg_maxcy, p.mg_fast, p.fft_fp32, p.ff_arith = EK_MG_STOP_RESIDUAL, 1e-10, 60, 1, 1, 1
+def _mixed(p, ff=1):
+    p.mg_stop, p.mg_tol, p.mg_maxcy, p.mg_fast, p.fft_fp32, p.ff_arith = EK_MG_STOP_RESIDUAL, 1e-10, 60, 1, 1, ff
     return p
 
 
-def _pair(case, graph_first=True):
+def _pair(case, ff=1):
     p, xp, yp, st = case
-    _mixed(p)
+    _mixed(p, ff)
     out = []
     for on in (True, False):
         g = DuctSolver(p, metrics_from_grid(p, xp, yp))
@@ -55,8 +55,11 @@ def _same(a, b):
         assert sa[k] == sb[k], (k, sa, sb)
 
 
-@pytest.mark.parametrize("variant", ["plain", "sponge", "les"])
+@pytest.mark.parametrize("variant", ["plain", "sponge", "les", "plain_inc", "sponge_inc"])
 def test_graph_steps_equal_eager_steps(variant):
+    """(_inc: the state path in FP32 increment form, ff_arith = 2.)"""
+    ff = 2 if variant.endswith("_inc") else 1
+    variant = variant.replace("_inc", "")
     if variant == "plain":
         case = small_case()
     elif variant == "sponge":
@@ -65,7 +68,7 @@ def test_graph_steps_equal_eager_steps(variant):
         case = (p, xp, yp, st)
     else:
         case = les_case("small")
-    g, e = _pair(case)
+    g, e = _pair(case, ff)
     try:
         for _ in range(7):  # the LES C_DYN recomputation falls on TIME_STEP 5
             assert g.step(1) == 0 and e.step(1) == 0
