@@ -267,6 +267,7 @@ int substep(Ctx &c, int rk) {
         // CU += the FP32 transform of the ADI's total increment
         a.lowp = 1;
         a.epi = EPI_ADD;
+        a.zero_hi = 1;
         a.a = nullptr;
         a.af = inc_plane(c, R);
         a.alo = nullptr;

@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
   const V *twn = tw_n<T>(fc);
   for (int kk = lane; kk <= d.NX2P; kk += 32) {
     if (kk > NKX) {
-      if (args.epi == EPI_STORE) dst[kk] = cplx_t{0.0, 0.0};
+      if (args.epi == EPI_STORE || args.zero_hi) dst[kk] = cplx_t{0.0, 0.0};
       continue;
     }
     const V zk = z[brev(kk & (M - 1), fc.logM)];

@@ -429,6 +429,9 @@ struct R2cArgs {
   // PRO_LOAD of a field held as float-float planes (the float-float kernel
   // reads the pair af + alo and no FP64 a)
   const float *alo;
+  // EPI_ADD: also zero the modes above NX/3, as a state's forward transform
+  // does (EPI_STORE always does)
+  int zero_hi;
 };
 void launch_r2c(Ctx &c, const R2cArgs &a);
 struct C2rArgs {
@@ -470,6 +473,8 @@ inline bool explicit_increment_form(const Ctx &c) { return c.p.fft_fp32 >= 1; }
 // at its end, so none of those kernels splits or joins an FP64 value per
 // physical point.
 bool ff_fields(const Ctx &c);
+// the spectral kernels' sizes: NX2P lowered to NKX on the mixed path
+Dims spec_dims(const Ctx &c);
 inline float *ff_lo(double *field) { return reinterpret_cast<float *>(field); }
 // The increment form of the state path (ff_arith = 2, nonlinear-term
 // transforms in FP32, no LES in the substep): the inverse transforms of the

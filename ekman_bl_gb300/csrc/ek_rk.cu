@@ -1274,8 +1274,9 @@ void launch_spectral_rhs(Ctx &c, int rk) {
   a.tgt3 = p.wbulk0;
   a.strat_per = (p.v_bc[EK_ZMAX] == 6 && p.u_bc[EK_ZMAX] == 6 && p.w_bc[EK_ZMAX] == 6 && p.ri_tau != 0.0) ? 1 : 0;
   a.reset = (a.strat_per && p.save_stats_int > 0 && (2 * p.time_step) % p.save_stats_int == 0) ? 1 : 0;
-  dim3 grid((c.d.NX2P + 1 + 63) / 64, c.d.NZ2, c.d.NY2);
-  KScope ks(c, KC_SPECTRAL, 16.0 * c.d.nspec() * (5 + (rk > 1 ? 4 : 0) + 8));
+  a.d = spec_dims(c);
+  dim3 grid((a.d.NX2P + 1 + 63) / 64, c.d.NZ2, c.d.NY2);
+  KScope ks(c, KC_SPECTRAL, 16.0 * c.d.nspec() * (a.d.NX2P + 1.0) / c.d.LDC * (5 + (rk > 1 ? 4 : 0) + 8));
   if (a.sponge) {
     const int nys = (p.ny_s_t > p.ny) ? (2 * p.ny) / 3 : p.ny_s_t;
     k_sponge_mean<<<1, 256, 0, c.stream>>>(c.d, c.CU3, nys, p.wbulk0, c.sponge_red);
@@ -1615,9 +1616,11 @@ void launch_th_corners(Ctx &c) {
 
 void launch_divergence_rhs(Ctx &c, double *rhs, int P) {
   const Dims &d = c.d;
-  KScope ks(c, KC_DIVERGENCE, 16.0 * d.nspec() * 4 + (16.0 * d.nspec() * 3 + 8.0 * P * d.NZ2 * d.NY2));
-  dim3 g1((d.NX2P + 1 + 63) / 64, d.NZ2, d.NY2);
-  k_rem_faces<<<g1, 64, 0, c.stream>>>(d, c.m, c.CU2, c.CU3, c.CU2b);
+  const Dims ds = spec_dims(c);
+  const double fm = (ds.NX2P + 1.0) / d.LDC;  // share of the modes processed
+  KScope ks(c, KC_DIVERGENCE, 16.0 * d.nspec() * fm * 4 + (16.0 * d.nspec() * 3 + 8.0 * P * d.NZ2 * d.NY2));
+  dim3 g1((ds.NX2P + 1 + 63) / 64, d.NZ2, d.NY2);
+  k_rem_faces<<<g1, 64, 0, c.stream>>>(ds, c.m, c.CU2, c.CU3, c.CU2b);
   after_launch(c);
   dim3 g2((P + 63) / 64, d.NZ2, d.NY2);
   k_div_rhs<<<g2, 64, 0, c.stream>>>(d, c.kx, c.CU1, c.CU2b, c.m.jac, rhs, P);
@@ -1626,18 +1629,20 @@ void launch_divergence_rhs(Ctx &c, double *rhs, int P) {
 
 void launch_projection(Ctx &c, const double *phif, int P, double temp4, bool update_p) {
   const Dims &d = c.d;
-  dim3 g0((d.NX2P + 1 + 63) / 64, d.NZ2, d.NY2);
+  const Dims ds = spec_dims(c);
+  const double fm = (ds.NX2P + 1.0) / d.LDC;
+  dim3 g0((ds.NX2P + 1 + 63) / 64, d.NZ2, d.NY2);
   {
-  KScope ks(c, KC_PROJECTION, 16.0 * d.nspec() * (1 + 1 + (update_p ? 2 : 0)) + 16.0 * d.nspec() * (5 + 7 + 4));
-  k_phi_to_cr1<<<g0, 64, 0, c.stream>>>(d, phif, P, c.CR1, c.CP, temp4, 1.0 / temp4, update_p ? 1 : 0,
+  KScope ks(c, KC_PROJECTION, (16.0 * d.nspec() * (1 + 1 + (update_p ? 2 : 0)) + 16.0 * d.nspec() * (5 + 7 + 4)) * fm);
+  k_phi_to_cr1<<<g0, 64, 0, c.stream>>>(ds, phif, P, c.CR1, c.CP, temp4, 1.0 / temp4, update_p ? 1 : 0,
                                        c.p.quirk_phi_fp32);
   after_launch(c);
-  dim3 g1((d.NX2P + 1 + 63) / 64, d.ZE - d.ZS + 1, d.JE - d.JS + 1);
-  k_correct_faces<<<g1, 64, 0, c.stream>>>(d, c.m, c.CR1, c.CU2b);
+  dim3 g1((ds.NX2P + 1 + 63) / 64, d.ZE - d.ZS + 1, d.JE - d.JS + 1);
+  k_correct_faces<<<g1, 64, 0, c.stream>>>(ds, c.m, c.CR1, c.CU2b);
   after_launch(c);
-  k_correct_cells<<<g1, 64, 0, c.stream>>>(d, c.m, c.kx, c.CR1, c.CU1, c.CU2, c.CU3);
+  k_correct_cells<<<g1, 64, 0, c.stream>>>(ds, c.m, c.kx, c.CR1, c.CU1, c.CU2, c.CU3);
   after_launch(c);
-  k_div_check<<<g0, 64, 0, c.stream>>>(d, c.kx, c.m.jac, c.CU1, c.CU2b, c.CS);
+  k_div_check<<<g0, 64, 0, c.stream>>>(ds, c.kx, c.m.jac, c.CU1, c.CU2b, c.CS);
   after_launch(c);
   }
   C2rArgs ca{};
@@ -1704,5 +1709,18 @@ void split_ff(Ctx &c, const double *in, float2 *out, size_t n) {
   const unsigned nb = (unsigned)std::min<size_t>((n + 255) / 256, 4 * 152);
   k_split_ff<<<nb, 256, 0, c.stream>>>(n, in, out);
   after_launch(c);
+}
+}  // namespace ek
+
+namespace ek {
+// The modes the spectral kernels process: all NX/2+1 on the plain path, as
+// the reference does; on the mixed path the ones up to NX/3 only.  The x
+// transforms read and write no mode above NX/3, and no spectral operation
+// couples modes, so those modes of CF and CR (which the reference's
+// Coriolis term on every kx fills) never reach a field that is kept.
+Dims spec_dims(const Ctx &c) {
+  Dims d = c.d;
+  if (explicit_increment_form(c)) d.NX2P = d.NKX;
+  return d;
 }
 }  // namespace ek
