@@ -1315,6 +1315,14 @@ int ekgpu_unet_forward(ek_unet *u, const float *x_dev, int n, float *y_dev, void
     if (!x_dev || !y_dev || n < 1 || n > net.max_n) return (int)EK_ERR_ARG;
     net.forward(x_dev, n, y_dev, (cudaStream_t)stream);
     EK_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    if (net.tcgen05() && net.tc_error((cudaStream_t)stream)) return (int)EK_ERR_TIMEOUT;
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_unet_set_tcgen05(ek_unet *u, int on) {
+  return unet_guarded(u, [&](ek::UNet &net) {
+    net.set_tcgen05(on != 0);
     return (int)EK_OK;
   });
 }

@@ -118,8 +118,13 @@ __global__ void k_spectral_rhs(SpecArgs a) {
   cplx_t F1{}, F2{}, F3{}, FT{};
   if (vel) {
     const cplx_t cu1 = a.CU1[q], cu2 = a.CU2[q], cu3 = a.CU3[q];
-    const double jr = a.cr_inc ? 0.0 : jac;
-    cplx_t r1 = cscl(jr, cu1), r2 = cscl(jr, cu2), r3 = cscl(jr, cu3);
+    // the explicit-increment form leaves J CU out of CR (no products spent on it)
+    cplx_t r1{}, r2{}, r3{};
+    if (!a.cr_inc) {
+      r1 = cscl(jac, cu1);
+      r2 = cscl(jac, cu2);
+      r3 = cscl(jac, cu3);
+    }
     if (a.rk > 1) {
       r1 = cadd(r1, cscl(a.T3, a.CF1[q]));
       r2 = cadd(r2, cscl(a.T3, a.CF2[q]));
@@ -169,7 +174,7 @@ __global__ void k_spectral_rhs(SpecArgs a) {
   }
   if (sca) {
     const cplx_t cth = a.CTH[q];
-    cplx_t rt = cscl(a.cr_inc ? 0.0 : jac, cth);
+    cplx_t rt = a.cr_inc ? cplx_t{0.0, 0.0} : cscl(jac, cth);
     if (a.rk > 1) rt = cadd(rt, cscl(a.T3, a.CFTH[q]));
     a.CRTH[q] = rt;
     cplx_t ft = cscl(-a.nupr * jac * a.kx2[i], cth);
@@ -398,7 +403,7 @@ __global__ void k_adi_les_tab(Dims d, Metrics m, const double *gb, const double 
 // Rows per chunk of the line-solve kernels below: a thread issues every
 // load of a chunk's rows before its recurrence consumes them (the
 // x-dependent LES rows hold more values per row than the plain ones).
-constexpr int kAdiChunk = 8, kLesChunk = 4, kIncChunkZ = 4;
+constexpr int kAdiChunk = 8, kLesChunk = 4, kIncChunkY = 8, kIncChunkZ = 4;
 
 // CN-ADI line solves with the LES eddy viscosity (duct.F90:1373-1386,
 // 1437-1450, 1489-1500, 1559-1569 for TH; 1667-1680, 1720-1731, 1771-1784,
@@ -932,7 +937,7 @@ __global__ void __launch_bounds__(128) k_adi_inc(AdiArgs a) {
   // rows go CH at a time: the chunk's base values along the line (rows
   // rc-1 .. rc+CH) are loaded once and shared by neighbouring rows, and
   // every load of the chunk is issued before the recurrence consumes it
-  constexpr int CH = ZS ? kIncChunkZ : kAdiChunk;
+  constexpr int CH = ZS ? kIncChunkZ : kIncChunkY;
   auto base_row = [&](int r) -> float {
     if (r < 0 || r >= nrow) return 0.0f;
     return base(c0 + (size_t)r * sA, ZS ? r : line);

@@ -262,6 +262,212 @@ __global__ void __launch_bounds__(NT) k_conv_gemm(ConvArgs a) {
       }
 }
 
+// ---------------------------------------------------------------------------
+// Forward convolution on the 5th-generation tensor cores (tcgen05), for the
+// layers with cin and cout multiples of 16 (cout <= 256): one CTA of 128
+// threads computes a 128-pixel x cout tile as one GEMM D = A B^T with
+// M = 128 pixels, N = cout, K = 9 cin.  The threads stage the whole K extent
+// of A (the shifted input rows, BF16) and of B (the weights, rounded to
+// BF16) in shared memory in the canonical no-swizzle K-major layout: 8-row x
+// 16-byte core matrices, 128 contiguous bytes each, the K-adjacent ones 128
+// bytes apart (leading byte offset) and the next 8 rows K*2 bytes apart
+// (stride byte offset).  One elected thread issues the K/16 tcgen05.mma
+// instructions (kind::f16, BF16 x BF16 -> FP32) into a TMEM accumulator of
+// the CTA and commits them to an mbarrier; every warp then reads its 32
+// rows of D from TMEM (tcgen05.ld 32x32b) for the epilogue (bias, ReLU,
+// BF16 store).  The wait on the mbarrier is bounded: if it runs out the
+// kernel flags the error, waits once more (bounded) for the MMAs it issued,
+// frees its TMEM and leaves the tile unwritten.
+namespace tc {
+
+constexpr int kM = 128;
+constexpr long kWaitLimit = 1L << 24;
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+// shared memory matrix descriptor: start, leading and stride byte offsets
+// (>> 4), version 1, no swizzle
+__device__ __forceinline__ unsigned long long sdesc(unsigned addr, unsigned lbo, unsigned sbo) {
+  return (unsigned long long)((addr >> 4) & 0x3fffu) | ((unsigned long long)((lbo >> 4) & 0x3fffu) << 16) |
+         ((unsigned long long)((sbo >> 4) & 0x3fffu) << 32) | (1ull << 46);
+}
+// instruction descriptor of kind::f16: FP32 accumulator, A and B BF16 and
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24
+__host__ __device__ constexpr unsigned idesc_bf16(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(n >> 3) << 17) | ((unsigned)(m >> 4) << 24);
+}
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned phase, long limit) {
+  for (long it = 0; it < limit; ++it) {
+    unsigned done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(phase)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+}  // namespace tc
+
+__global__ void __launch_bounds__(128, 1) k_conv_fwd_tc(ConvArgs a, int ncols, int *err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const int cin = a.cin, cout = a.cout;
+  const int K = 9 * cin, KC = K / 8;
+  unsigned char *As = smem;
+  unsigned char *Bs = smem + (size_t)tc::kM * K * 2;
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(Bs + (size_t)cout * K * 2);
+  unsigned *tslot = reinterpret_cast<unsigned *>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const long M = (long)a.g.N * a.g.H * a.g.W;
+  const long ntile = (M + tc::kM - 1) / tc::kM;
+
+  // TMEM: one warp allocates ncols (a power of two >= 32) columns, kept for
+  // every tile of this CTA
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tc::smem_u32(tslot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(tc::smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  // B once per CTA: row co = the weights W[co][tap][ci] rounded to BF16
+  for (int q = tid; q < cout * KC; q += 128) {
+    const int co = q / KC, kc = q - co * KC;
+    const float4 *w = reinterpret_cast<const float4 *>(a.w + (size_t)co * K + (size_t)kc * 8);
+    const float4 w0 = w[0], w1 = w[1];
+    const unsigned off = (unsigned)(co >> 3) * (unsigned)KC * 128u + (unsigned)kc * 128u + (unsigned)(co & 7) * 16u;
+    *reinterpret_cast<uint4 *>(Bs + off) =
+        make_uint4((unsigned)f2bf(w0.x) | ((unsigned)f2bf(w0.y) << 16), (unsigned)f2bf(w0.z) | ((unsigned)f2bf(w0.w) << 16),
+                   (unsigned)f2bf(w1.x) | ((unsigned)f2bf(w1.y) << 16), (unsigned)f2bf(w1.z) | ((unsigned)f2bf(w1.w) << 16));
+  }
+  const unsigned barad = tc::smem_u32(bar);
+  const unsigned rowoff = (unsigned)(tid >> 3) * (unsigned)KC * 128u + (unsigned)(tid & 7) * 16u;
+  const unsigned arow = tc::smem_u32(As) + rowoff;
+  bool ok = true;
+  unsigned phase = 0;
+  for (long tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const long m = tile * tc::kM + tid;
+    // A: thread tid stages row tid (pixel m): per tap its cin channels as
+    // 16-byte asynchronous copies (8 channels each) from x1, then x2, all in
+    // flight together
+    if (m < M) {
+      int n, y, x;
+      pix(a.g, m, n, y, x);
+      for (int tap = 0; tap < 9; ++tap) {
+        const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+        const unsigned short *s1 = a.x1 + a.g.at(n, yy, xx, a.c1);
+        for (int c = 0; c < a.c1 / 8; ++c) {
+          const int kc = (tap * cin) / 8 + c;
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(arow + (unsigned)kc * 128u), "l"(s1 + 8 * c)
+                       : "memory");
+        }
+        if (a.c2) {
+          const unsigned short *s2 = a.x2 + a.g.at(n, yy, xx, a.c2);
+          for (int c = 0; c < a.c2 / 8; ++c) {
+            const int kc = (tap * cin + a.c1) / 8 + c;
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(arow + (unsigned)kc * 128u),
+                         "l"(s2 + 8 * c)
+                         : "memory");
+          }
+        }
+      }
+    } else {
+      for (int kc = 0; kc < KC; ++kc) *reinterpret_cast<uint4 *>(As + rowoff + (unsigned)kc * 128u) = make_uint4(0, 0, 0, 0);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    // the stores must be visible to the tensor cores' async proxy
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const unsigned tmem = *tslot;
+    if (tid == 0) {
+      const unsigned idesc = tc::idesc_bf16(tc::kM, cout);
+      const unsigned a0 = tc::smem_u32(As), b0 = tc::smem_u32(Bs);
+      const unsigned sbo = (unsigned)KC * 128u;
+      for (int ks = 0; ks < K / 16; ++ks) {
+        const unsigned long long da = tc::sdesc(a0 + (unsigned)ks * 256u, 128u, sbo);
+        const unsigned long long db = tc::sdesc(b0 + (unsigned)ks * 256u, 128u, sbo);
+        const unsigned acc = ks > 0 ? 1u : 0u;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(idesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(barad)
+                   : "memory");
+    }
+    bool done = tc::mbar_wait(barad, phase, tc::kWaitLimit);
+    if (!done) {
+      atomicExch(err, 1);
+      done = tc::mbar_wait(barad, phase, tc::kWaitLimit);
+    }
+    phase ^= 1u;
+    // every warp of the CTA takes the same branch (tcgen05.ld is .aligned)
+    ok = __syncthreads_and(done) != 0;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (!ok) break;
+    // warp w reads rows 32w..32w+31 (lane = its thread), 32 columns a load
+    const unsigned tw = tmem + ((unsigned)(warp * 32) << 16);
+    for (int c0 = 0; c0 < cout; c0 += 32) {
+      unsigned r[32];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+          "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          : "r"(tw + (unsigned)c0)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      if (m < M) {
+        int n, y, x;
+        pix(a.g, m, n, y, x);
+        unsigned short *out = a.y + a.g.at(n, y, x, cout) + c0;
+        const int nc = min(32, cout - c0);
+#pragma unroll
+        for (int j = 0; j < 32; j += 8) {
+          if (j >= nc) break;
+          unsigned pk[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            float v0 = __uint_as_float(r[j + 2 * e]) + a.bias[c0 + j + 2 * e];
+            float v1 = __uint_as_float(r[j + 2 * e + 1]) + a.bias[c0 + j + 2 * e + 1];
+            if (a.relu) {
+              v0 = fmaxf(v0, 0.f);
+              v1 = fmaxf(v1, 0.f);
+            }
+            pk[e] = (unsigned)f2bf(v0) | ((unsigned)f2bf(v1) << 16);
+          }
+          *reinterpret_cast<uint4 *>(out + j) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        }
+      }
+    }
+    // the next tile's MMAs overwrite the accumulator and A: every thread's
+    // TMEM reads and A copies of this tile end here
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(*tslot), "r"(ncols) : "memory");
+  }
+}
+
 // bias gradient: db[co] += sum over pixels of dZ[p][co]
 __global__ void k_bias_grad(Img g, const float *dz, int cout, float *db) {
   const long npx = (long)g.N * g.H * g.W;
@@ -452,6 +658,7 @@ UNet::UNet(int cin_, int C_, int max_n_, int h_, int w_) : cin(cin_), C(C_), max
       }
     }
     y_ = (float *)alloc(sizeof(float) * (size_t)max_n * h * w, bufs_);
+    tc_err_ = (int *)alloc(sizeof(int), bufs_);
   } catch (...) {
     for (void *p : bufs_) cudaFree(p);
     bufs_.clear();
@@ -530,7 +737,28 @@ void UNet::run_forward(const float *x, int n, float *y, cudaStream_t s) {
     a.y32 = out32;
     a.relu = Ly.relu;
     const long M = (long)n * a.g.H * a.g.W;
-    k_conv_gemm<PASS_FWD><<<dim3((unsigned)((M + BM - 1) / BM), (unsigned)((Ly.cout + BN - 1) / BN)), NT, 0, s>>>(a);
+    if (tc_ && !out32 && Ly.cin % 16 == 0 && Ly.c1 % 8 == 0 && Ly.c2 % 8 == 0 && Ly.cout % 16 == 0 &&
+        Ly.cout <= 256) {
+      const size_t smem = (size_t)(tc::kM + Ly.cout) * 9 * Ly.cin * 2 + 16;
+      int ncols = 32;
+      while (ncols < Ly.cout) ncols *= 2;
+      static bool attr = false;
+      if (!attr) {
+        EK_CUDA(cudaFuncSetAttribute(k_conv_fwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+        attr = true;
+      }
+      if (smem > 220 * 1024) throw CudaError("unet: tcgen05 tile does not fit in shared memory");
+      // persistent CTAs: as many as fit on the SMs (by shared memory), each
+      // stages the weights once and loops over 128-pixel tiles
+      static int nsm = 0;
+      if (!nsm) EK_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, 0));
+      const long ntile = (M + tc::kM - 1) / tc::kM;
+      const long per_sm = std::max<long>(1, (long)(220 * 1024) / (long)smem);
+      const long nblk = std::min<long>(ntile, (long)nsm * per_sm);
+      k_conv_fwd_tc<<<(unsigned)nblk, 128, smem, s>>>(a, ncols, tc_err_);
+    } else {
+      k_conv_gemm<PASS_FWD><<<dim3((unsigned)((M + BM - 1) / BM), (unsigned)((Ly.cout + BN - 1) / BN)), NT, 0, s>>>(a);
+    }
     K.check();
   };
   auto pool = [&](int lev, const unsigned short *src, unsigned short *dst) {
@@ -562,6 +790,13 @@ void UNet::run_forward(const float *x, int n, float *y, cudaStream_t s) {
 }
 
 void UNet::forward(const float *x, int n, float *y, cudaStream_t s) { run_forward(x, n, y, s); }
+
+int UNet::tc_error(cudaStream_t s) {
+  int v = 0;
+  EK_CUDA(cudaMemcpyAsync(&v, tc_err_, sizeof(int), cudaMemcpyDeviceToHost, s));
+  EK_CUDA(cudaStreamSynchronize(s));
+  return v;
+}
 
 double UNet::forward_backward(const float *x, const float *t, int n, int hv, int wv, float *y, cudaStream_t s) {
   if (!y) y = y_;

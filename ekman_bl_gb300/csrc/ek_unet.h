@@ -36,6 +36,13 @@ class UNet {
   const float *grads() const { return grad_; }
   long launches() const { return launches_; }
   double forward_flops(int n) const;  // 2 x multiply-adds of the convolutions
+  // the forward convolutions whose channel counts allow it on the tcgen05
+  // kernel (default), else all on the mma.sync one
+  void set_tcgen05(bool on) { tc_ = on; }
+  bool tcgen05() const { return tc_; }
+  // 1 when a tcgen05 convolution's bounded wait ran out (sticky); reads the
+  // device flag (synchronises the stream)
+  int tc_error(cudaStream_t s);
 
   int cin, C, max_n, h, w;
 
@@ -50,6 +57,8 @@ class UNet {
   float *param_ = nullptr, *grad_ = nullptr, *m_ = nullptr, *v_ = nullptr;
   long step_ = 0;
   long launches_ = 0;
+  bool tc_ = true;
+  int *tc_err_ = nullptr;
   // activations (BF16, bordered): xin, t[l], s[l], p[l], u[l], v[l], d[l]
   unsigned short *xin_ = nullptr;
   unsigned short *t_[kLevels] = {}, *s_[kLevels] = {}, *p_[kLevels] = {};

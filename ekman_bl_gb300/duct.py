@@ -34,7 +34,8 @@ EXPORTS = [
     "ekgpu_sponge_profiles", "ekgpu_set_sponge", "ekgpu_set_time", "ekgpu_get_time",
     "ekgpu_save_flow", "ekgpu_read_flow", "ekgpu_save_stats",
     "ekgpu_unet_create", "ekgpu_unet_destroy", "ekgpu_unet_last_error", "ekgpu_unet_num_params",
-    "ekgpu_unet_set_params", "ekgpu_unet_get_params", "ekgpu_unet_forward", "ekgpu_unet_train_step",
+    "ekgpu_unet_set_params", "ekgpu_unet_get_params", "ekgpu_unet_forward", "ekgpu_unet_set_tcgen05",
+    "ekgpu_unet_train_step",
     "ekgpu_unet_gradient", "ekgpu_guess_geometry", "ekgpu_set_poisson_guess", "ekgpu_set_pair_sink",
     "ekgpu_pair_count", "ekgpu_last_guess_stats", "ekgpu_mg_autotune", "ekgpu_mg_set_layout", "ekgpu_mg_levels",
     "ekgpu_les_metrics_from_grid", "ekgpu_set_les_metrics", "ekgpu_les_set_first_time", "ekgpu_les_get",
@@ -92,6 +93,7 @@ def load_library():
     L.ekgpu_unet_set_params.argtypes = [V, F]
     L.ekgpu_unet_get_params.argtypes = [V, F]
     L.ekgpu_unet_forward.argtypes = [V, V, C.c_int, V, V]
+    L.ekgpu_unet_set_tcgen05.argtypes = [V, C.c_int]
     L.ekgpu_unet_train_step.argtypes = [V, V, V, C.c_int, C.c_int, C.c_int, C.c_double, _D, V]
     L.ekgpu_unet_gradient.argtypes = [V, V, V, C.c_int, C.c_int, C.c_int, _D, V, F, V]
     L.ekgpu_guess_geometry.argtypes = [V, C.c_int] + [C.POINTER(C.c_int)] * 4
@@ -571,6 +573,11 @@ class UNet:
     def forward(self, x_ptr: int, n: int, y_ptr: int, stream: int | None = None):
         self._check(self._L.ekgpu_unet_forward(self._h, C.c_void_p(x_ptr), n, C.c_void_p(y_ptr),
                                                C.c_void_p(stream or 0)))
+
+    def set_tcgen05(self, on: bool):
+        """Forward convolutions on the tcgen05 tensor-core kernel where their
+        channel counts allow it (the default), or all on the mma.sync one."""
+        self._check(self._L.ekgpu_unet_set_tcgen05(self._h, int(bool(on))))
 
     def train_step(self, x_ptr: int, t_ptr: int, n: int, hv: int, wv: int, lr: float,
                    stream: int | None = None) -> float:

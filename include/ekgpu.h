@@ -41,8 +41,9 @@ typedef enum ek_status {
   EK_ERR_CUDA = 2,           /* a CUDA call failed                              */
   EK_ERR_NOT_CONVERGED = 3,  /* multigrid hit its cycle cap; phi still returned */
   EK_ERR_NAN = 4,            /* divergence is NaN (reference: STOP 'DIV is a NaN', duct.F90:2811) */
-  EK_ERR_TIMEOUT = 5,        /* reserved: no kernel of this library waits on a flag,
-                                a peer or a barrier, so no call returns it        */
+  EK_ERR_TIMEOUT = 5,        /* a tensor-core convolution of the U-Net gave up its
+                                bounded wait for its MMAs (ekgpu_unet_forward,
+                                _train_step, _gradient); no other kernel waits  */
   EK_ERR_STATE = 6,          /* call order violated (e.g. step before metrics)  */
   EK_ERR_IO = 7,             /* restart file missing, unreadable or malformed  */
   EK_ERR_DT = 8              /* DELTA_T below 1.0E-4 after a projection (reference:
@@ -354,6 +355,10 @@ int ekgpu_unet_set_params(ek_unet *net, const float *params);   /* host; resets 
 int ekgpu_unet_get_params(ek_unet *net, float *params);         /* host               */
 /* y[n][h][w] = net(x[n][h][w][cin]); device pointers; stream may be NULL */
 int ekgpu_unet_forward(ek_unet *net, const float *x_dev, int n, float *y_dev, void *stream);
+/* Forward convolutions with cin and cout multiples of 16 run on the tcgen05
+ * tensor-core kernel (on by default); 0 puts every layer on the mma.sync
+ * kernel.  No counterpart in the reference (method tuning). */
+int ekgpu_unet_set_tcgen05(ek_unet *net, int on);
 /* one Adam step (beta 0.9/0.999, eps 1e-8) on the mean-square error against
  * t[n][h][w] over the top-left hv x wv pixels of each image */
 int ekgpu_unet_train_step(ek_unet *net, const float *x_dev, const float *t_dev, int n, int hv, int wv,
