@@ -468,6 +468,72 @@ __global__ void __launch_bounds__(128, 1) k_conv_fwd_tc(ConvArgs a, int ncols, i
   }
 }
 
+// The two thin convolutions of the network, on the CUDA cores with the same
+// arithmetic as the tensor-core GEMMs (weights rounded to BF16, BF16
+// activations, FP32 accumulation): the first (cin = cin of the network, a
+// 9 cin-long K) and the last (cout = 1).  As GEMMs their K or N fills a
+// small part of a tensor-core tile.
+// first layer: one thread per pixel, all cout outputs (cout <= 64, cin <= 4)
+__global__ void k_conv_first(ConvArgs a) {
+  extern __shared__ float wsh[];  // [9 cin][cout] rounded weights, then bias
+  const int cin = a.cin, cout = a.cout, K = 9 * cin;
+  for (int q = threadIdx.x; q < K * cout; q += blockDim.x) {
+    const int co = q % cout, k = q / cout;
+    wsh[q] = bf2f(f2bf(a.w[(size_t)co * K + k]));
+  }
+  for (int q = threadIdx.x; q < cout; q += blockDim.x) wsh[K * cout + q] = a.bias[q];
+  __syncthreads();
+  const long M = (long)a.g.N * a.g.H * a.g.W;
+  for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < M; m += (long)gridDim.x * blockDim.x) {
+    int n, y, x;
+    pix(a.g, m, n, y, x);
+    float acc[64];
+#pragma unroll
+    for (int co = 0; co < 64; ++co) acc[co] = 0.f;
+    for (int tap = 0; tap < 9; ++tap) {
+      const unsigned short *src = a.x1 + a.g.at(n, y + tap / 3 - 1, x + tap % 3 - 1, cin);
+      for (int ci = 0; ci < cin; ++ci) {
+        const float v = bf2f(src[ci]);
+        const float *wr = wsh + (tap * cin + ci) * cout;
+#pragma unroll
+        for (int co = 0; co < 64; ++co)
+          if (co < cout) acc[co] = fmaf(v, wr[co], acc[co]);
+      }
+    }
+    unsigned short *out = a.y + a.g.at(n, y, x, cout);
+#pragma unroll
+    for (int co = 0; co < 64; ++co) {
+      if (co >= cout) break;
+      float v = acc[co] + wsh[K * cout + co];
+      if (a.relu) v = fmaxf(v, 0.f);
+      out[co] = f2bf(v);
+    }
+  }
+}
+
+// last layer: one output channel in FP32, one thread per pixel
+__global__ void k_conv_last(ConvArgs a) {
+  extern __shared__ float wsh[];  // [9 cin] rounded weights
+  const int cin = a.cin, K = 9 * cin;
+  for (int q = threadIdx.x; q < K; q += blockDim.x) wsh[q] = bf2f(f2bf(a.w[q]));
+  __syncthreads();
+  const float b = a.bias[0];
+  const long M = (long)a.g.N * a.g.H * a.g.W;
+  for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < M; m += (long)gridDim.x * blockDim.x) {
+    int n, y, x;
+    pix(a.g, m, n, y, x);
+    float acc = 0.f;
+    for (int tap = 0; tap < 9; ++tap) {
+      const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+      const float *wr = wsh + tap * cin;
+      for (int ci = 0; ci < cin; ++ci) acc = fmaf(act_in(a, n, yy, xx, ci), wr[ci], acc);
+    }
+    float v = acc + b;
+    if (a.relu) v = fmaxf(v, 0.f);
+    a.y32[m] = v;
+  }
+}
+
 // bias gradient: db[co] += sum over pixels of dZ[p][co]
 __global__ void k_bias_grad(Img g, const float *dz, int cout, float *db) {
   const long npx = (long)g.N * g.H * g.W;
@@ -756,6 +822,10 @@ void UNet::run_forward(const float *x, int n, float *y, cudaStream_t s) {
       const long per_sm = std::max<long>(1, (long)(220 * 1024) / (long)smem);
       const long nblk = std::min<long>(ntile, (long)nsm * per_sm);
       k_conv_fwd_tc<<<(unsigned)nblk, 128, smem, s>>>(a, ncols, tc_err_);
+    } else if (tc_ && out32 && Ly.cout == 1 && !Ly.c2) {
+      k_conv_last<<<gsz(M, 256), 256, sizeof(float) * 9 * Ly.cin, s>>>(a);
+    } else if (tc_ && !out32 && Ly.cin <= 4 && Ly.cout <= 64 && !Ly.c2) {
+      k_conv_first<<<gsz(M, 128), 128, sizeof(float) * (9 * Ly.cin + 1) * Ly.cout, s>>>(a);
     } else {
       k_conv_gemm<PASS_FWD><<<dim3((unsigned)((M + BM - 1) / BM), (unsigned)((Ly.cout + BN - 1) / BN)), NT, 0, s>>>(a);
     }
