@@ -327,7 +327,7 @@ def run_learned(solver, stream, args):
             "starting_residual_ratio": round(rho, 4),
             "guess_ms_per_step": round(g_ms, 3),
             "unet_forward_tflops": round(g_flops / (g_ms / 1000.0) / 1e12, 2) if g_ms > 0 else None,
-            "network": f"U-Net 4 levels x {LEARN_CHANNELS} channels, 3x3, BF16 mma.sync, FP32 accumulate, on the "
+            "network": f"U-Net 4 levels x {LEARN_CHANNELS} channels, 3x3, BF16 tcgen05 tensor cores (direct FP32 first and last layers), FP32 accumulate, on the "
                        f"finest multigrid grid averaged {LEARN_FACTOR}x{LEARN_FACTOR}",
             "training": {"pairs": npairs, "collect_s": round(collect_s, 2), **{k: (round(v, 5) if isinstance(v, float)
                                                                                  else v) for k, v in rep.items()}}}
