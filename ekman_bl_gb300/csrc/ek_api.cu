@@ -191,16 +191,17 @@ int substep(Ctx &c, int rk) {
     const float *uf[3] = {c.U1f, c.U2f, c.U3f};
     cplx_t *cf[3] = {c.CF1, c.CF2, c.CF3};
     a.lowp = 1;
+    // each component's product and flux terms in one launch
+    a.fuse_flux = 1;
     for (int f = 0; f < 3; ++f) {
       a.pro = PRO_PROD; a.a = c.U1; a.b = uu[f]; a.epi = EPI_SUB_IK; a.dst = cf[f];
       a.af = f32 ? c.U1f : nullptr; a.bf = f32 ? uf[f] : nullptr;
       a.extra = les ? c.les.t[f] : nullptr;  // + J tau_1f
       a.extraf = les ? c.les.tf[f] : nullptr;
-      launch_r2c(c, a);
-      a.pro = PRO_FLUX; a.a = uu[f]; a.b = c.U2b; a.visc = p.nu; a.epi = EPI_ADD;
-      a.af = f32 ? uf[f] : nullptr; a.bf = f32 ? c.U2bf : nullptr;
-      a.extra = les ? c.les.ext[f] : nullptr;  // + NU_T cross term - stress divergence
-      a.extraf = les ? c.les.extf[f] : nullptr;
+      a.a2 = uu[f]; a.b2 = c.U2b; a.visc2 = p.nu;
+      a.a2f = f32 ? uf[f] : nullptr; a.b2f = f32 ? c.U2bf : nullptr;
+      a.extra2 = les ? c.les.ext[f] : nullptr;  // + NU_T cross term - stress divergence
+      a.extraf2 = les ? c.les.extf[f] : nullptr;
       launch_r2c(c, a);
     }
   }
@@ -229,11 +230,11 @@ int substep(Ctx &c, int rk) {
     a.af = f32 ? c.THf : nullptr; a.bf = f32 ? c.U1f : nullptr;
     a.extra = les ? c.les.tth : nullptr;  // + J (-KAPPA_T dTH/dx)
     a.extraf = les ? c.les.tthf : nullptr;
-    launch_r2c(c, a);
-    a.pro = PRO_FLUX; a.a = c.TH; a.b = c.U2b; a.visc = p.nu / p.pr; a.epi = EPI_ADD;
-    a.af = f32 ? c.THf : nullptr; a.bf = f32 ? c.U2bf : nullptr;
-    a.extra = les ? c.les.ext[3] : nullptr;  // + KAPPA_T cross term
-    a.extraf = les ? c.les.extf[3] : nullptr;
+    a.fuse_flux = 1;
+    a.a2 = c.TH; a.b2 = c.U2b; a.visc2 = p.nu / p.pr;
+    a.a2f = f32 ? c.THf : nullptr; a.b2f = f32 ? c.U2bf : nullptr;
+    a.extra2 = les ? c.les.ext[3] : nullptr;  // + KAPPA_T cross term
+    a.extraf2 = les ? c.les.extf[3] : nullptr;
     launch_r2c(c, a);
     C2rArgs b{};
     b.j0 = d.JST; b.j1 = d.JET; b.k0 = d.ZST; b.k1 = d.ZET;
@@ -894,7 +895,7 @@ int ekgpu_set_metrics(ek_ctx *h, const ek_metrics *m) {
     up(c.m.c21, m->cjob_21, 2 * n2); up(c.m.c22, m->cjob_22, 2 * n2);
     up(c.m.thbar, m->th_bar, n2);
     step_graphs_clear(c);  // the plan they were captured from is rebuilt below
-    if (!c.m.pg) c.m.pg = dalloc<double>(c, 11 * n2);
+    if (!c.m.pg) c.m.pg = dalloc<double>(c, 13 * n2);
     launch_metric_tables(c);
     c.les.tab_ok = false;
     std::vector<double> jac(m->int_jacob, m->int_jacob + n2), g11(m->gmat_11, m->gmat_11 + 2 * n2),
@@ -1464,6 +1465,14 @@ int ekgpu_mg_set_layout(ek_ctx *h, int level, int dir, int lanes, int seg) {
     t[level] = lanes;
     u[level] = seg;
     step_graphs_clear(c);  // captured with the old layouts
+    return (int)EK_OK;
+  });
+}
+
+int ekgpu_mg_tail_levels(ek_ctx *h, int *ltop) {
+  return guarded(h, [&](Ctx &c) {
+    if (!ltop) return fail(c, EK_ERR_ARG, "ltop is NULL");
+    *ltop = mgfast_tail_levels(c);
     return (int)EK_OK;
   });
 }

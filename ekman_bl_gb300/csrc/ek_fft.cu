@@ -199,6 +199,50 @@ __device__ __forceinline__ void dif_fft_any(V *z, int M, const V *tw, bool conj_
   else dif_fft(z, M, tw, conj_tw, lane);
 }
 
+// The flux form of the eta/zeta convection plus the GMAT_12 cross diffusion
+// of field a (duct.F90:735-761; the TH version at 1210-1241 has visc =
+// NU/PR) along one x-line, into zr: from the FP32 copies (fin) or FP64.
+// b is U2b, followed in memory by U3b (see the launch).
+template <typename T>
+__device__ __forceinline__ void flux_line(T *zr, const FftConst &fc, int k, int j, size_t base, int lane, bool fin,
+                                          const double *a, const double *b, const float *af, const float *bf,
+                                          double visc) {
+  const Dims &d = fc.d;
+  const int NX = d.NX;
+  const T g12a = from_f64<T>(fc.m.g12[d.m3(k + 1, j, 2)]), g12b = from_f64<T>(fc.m.g12[d.m3(k, j, 2)]);
+  const T g12c = from_f64<T>(fc.m.g12[d.m3(k, j + 1, 1)]), g12d = from_f64<T>(fc.m.g12[d.m3(k, j, 1)]);
+  const T qv = from_f64<T>(0.25 * visc);
+  const T h = (T)0.5;
+  const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
+  if (fin) {
+    const float *F = af, *U2b = bf, *U3b = bf + d.nphys();
+    for (int n = lane; n < NX; n += 32) {
+      const size_t c = base + n;
+      const T f = (T)(double)F[c], fkp = (T)(double)F[c + sK], fkm = (T)(double)F[c - sK];
+      const T fjp = (T)(double)F[c + sJ], fjm = (T)(double)F[c - sJ];
+      const T fpp = (T)(double)F[c + sK + sJ], fpm = (T)(double)F[c + sK - sJ];
+      const T fmp = (T)(double)F[c - sK + sJ], fmm = (T)(double)F[c - sK - sJ];
+      T s1 = h * (T)(double)U2b[c + sJ] * (f + fjp) - h * (T)(double)U2b[c] * (f + fjm);
+      T s2 = h * (T)(double)U3b[c + sK] * (f + fkp) - h * (T)(double)U3b[c] * (f + fkm);
+      s1 = -s1 + qv * (g12a * (fpp + fjp - fjm - fpm) - g12b * (fmp + fjp - fjm - fmm));
+      s2 = -s2 + qv * (g12c * (fpp + fkp - fmp - fkm) - g12d * (fkp + fpm - fkm - fmm));
+      zr[n] = s1 + s2;
+    }
+  } else {
+    const double *F = a, *U2b = b, *U3b = b + d.nphys();
+    for (int n = lane; n < NX; n += 32) {
+      const size_t c = base + n;
+      const T f = (T)F[c], fkp = (T)F[c + sK], fkm = (T)F[c - sK], fjp = (T)F[c + sJ], fjm = (T)F[c - sJ];
+      const T fpp = (T)F[c + sK + sJ], fpm = (T)F[c + sK - sJ], fmp = (T)F[c - sK + sJ], fmm = (T)F[c - sK - sJ];
+      T s1 = h * (T)U2b[c + sJ] * (f + fjp) - h * (T)U2b[c] * (f + fjm);
+      T s2 = h * (T)U3b[c + sK] * (f + fkp) - h * (T)U3b[c] * (f + fkm);
+      s1 = -s1 + qv * (g12a * (fpp + fjp - fjm - fpm) - g12b * (fmp + fjp - fjm - fmm));
+      s2 = -s2 + qv * (g12c * (fpp + fkp - fmp - fkm) - g12d * (fkp + fpm - fkm - fmm));
+      zr[n] = s1 + s2;
+    }
+  }
+}
+
 template <typename T, int E>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArgs args) {
   using V = typename Cx<T>::V;
@@ -239,47 +283,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
       for (int n = lane; n < NX; n += 32) zr[n] = jac * (T)(double)args.af[base + n] * (T)(double)args.bf[base + n];
     else
       for (int n = lane; n < NX; n += 32) zr[n] = jac * (T)args.a[base + n] * (T)args.b[base + n];
-  } else if (fin) {
-    // the flux stencil below on the FP32 copies
-    const float *F = args.af, *U2b = args.bf, *U3b = args.bf + d.nphys();
-    const T g12a = from_f64<T>(fc.m.g12[d.m3(k + 1, j, 2)]), g12b = from_f64<T>(fc.m.g12[d.m3(k, j, 2)]);
-    const T g12c = from_f64<T>(fc.m.g12[d.m3(k, j + 1, 1)]), g12d = from_f64<T>(fc.m.g12[d.m3(k, j, 1)]);
-    const T qv = from_f64<T>(0.25 * args.visc);
-    const T h = (T)0.5;
-    const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
-    for (int n = lane; n < NX; n += 32) {
-      const size_t c = base + n;
-      const T f = (T)(double)F[c], fkp = (T)(double)F[c + sK], fkm = (T)(double)F[c - sK];
-      const T fjp = (T)(double)F[c + sJ], fjm = (T)(double)F[c - sJ];
-      const T fpp = (T)(double)F[c + sK + sJ], fpm = (T)(double)F[c + sK - sJ];
-      const T fmp = (T)(double)F[c - sK + sJ], fmm = (T)(double)F[c - sK - sJ];
-      T s1 = h * (T)(double)U2b[c + sJ] * (f + fjp) - h * (T)(double)U2b[c] * (f + fjm);
-      T s2 = h * (T)(double)U3b[c + sK] * (f + fkp) - h * (T)(double)U3b[c] * (f + fkm);
-      s1 = -s1 + qv * (g12a * (fpp + fjp - fjm - fpm) - g12b * (fmp + fjp - fjm - fmm));
-      s2 = -s2 + qv * (g12c * (fpp + fkp - fmp - fkm) - g12d * (fkp + fpm - fkm - fmm));
-      zr[n] = s1 + s2;
-    }
   } else {
-    // flux form of the eta/zeta convection plus the GMAT_12 cross diffusion
-    // (duct.F90:735-761; the TH version at 1210-1241 has visc = NU/PR)
-    const double *F = args.a;
-    const double *U2b = args.b;  // U2b, followed in memory by U3b (see launch)
-    const double *U3b = args.b + d.nphys();
-    const T g12a = from_f64<T>(fc.m.g12[d.m3(k + 1, j, 2)]), g12b = from_f64<T>(fc.m.g12[d.m3(k, j, 2)]);
-    const T g12c = from_f64<T>(fc.m.g12[d.m3(k, j + 1, 1)]), g12d = from_f64<T>(fc.m.g12[d.m3(k, j, 1)]);
-    const T qv = from_f64<T>(0.25 * args.visc);
-    const T h = (T)0.5;
-    const size_t sK = d.LDX, sJ = (size_t)d.LDX * d.NZ2;
-    for (int n = lane; n < NX; n += 32) {
-      const size_t c = base + n;
-      const T f = (T)F[c], fkp = (T)F[c + sK], fkm = (T)F[c - sK], fjp = (T)F[c + sJ], fjm = (T)F[c - sJ];
-      const T fpp = (T)F[c + sK + sJ], fpm = (T)F[c + sK - sJ], fmp = (T)F[c - sK + sJ], fmm = (T)F[c - sK - sJ];
-      T s1 = h * (T)U2b[c + sJ] * (f + fjp) - h * (T)U2b[c] * (f + fjm);
-      T s2 = h * (T)U3b[c + sK] * (f + fkp) - h * (T)U3b[c] * (f + fkm);
-      s1 = -s1 + qv * (g12a * (fpp + fjp - fjm - fpm) - g12b * (fmp + fjp - fjm - fmm));
-      s2 = -s2 + qv * (g12c * (fpp + fkp - fmp - fkm) - g12d * (fkp + fpm - fkm - fmm));
-      zr[n] = s1 + s2;
-    }
+    flux_line<T>(zr, fc, k, j, base, lane, fin, args.a, args.b, args.af, args.bf, args.visc);
   }
   if (args.pro != PRO_LOAD && (args.extra || args.extraf)) {
     // LES additions: jac * tau for a product, the precomputed terms for a flux
@@ -289,8 +294,22 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
     else if (args.extra)
       for (int n = lane; n < NX; n += 32) zr[n] = zr[n] + es * (T)args.extra[base + n];
   }
+  // with fuse_flux the same line's flux term (PRO_FLUX of a2 against b2, and
+  // its LES addition) goes through a second transform in the same warp
+  const bool fuse = args.fuse_flux != 0;
+  V *z2 = smem_c + (size_t)(kWarpsPerBlock + warp) * M;
+  if (fuse) {
+    T *zr2 = reinterpret_cast<T *>(z2);
+    const bool fin2 = kF && args.a2f != nullptr;
+    flux_line<T>(zr2, fc, k, j, base, lane, fin2, args.a2, args.b2, args.a2f, args.b2f, args.visc2);
+    if (kF && args.extraf2)
+      for (int n = lane; n < NX; n += 32) zr2[n] = zr2[n] + (T)1.0 * (T)args.extraf2[base + n];
+    else if (args.extra2)
+      for (int n = lane; n < NX; n += 32) zr2[n] = zr2[n] + (T)1.0 * (T)args.extra2[base + n];
+  }
   __syncwarp();
   dif_fft_any<E>(z, M, tw_m<T>(fc), false, lane);
+  if (fuse) dif_fft_any<E>(z2, M, tw_m<T>(fc), false, lane);
   // split: X[k] = E + W^k O, E = (Z_k + conj Z_{M-k})/2, O = -i (Z_k - conj Z_{M-k})/2
   cplx_t *dst = args.dst + d.ic(0, k, j);
   const T inv = from_f64<T>(fc.inv_nx);
@@ -302,13 +321,33 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
       if (args.epi == EPI_STORE || args.zero_hi) dst[kk] = cplx_t{0.0, 0.0};
       continue;
     }
-    const V zk = z[brev(kk & (M - 1), fc.logM)];
-    const V zm = z[brev((M - kk) & (M - 1), fc.logM)];
-    const T er = h * (zk.x + zm.x), ei = h * (zk.y - zm.y);
-    const T orr = h * (zk.y + zm.y), oi = -h * (zk.x - zm.x);
+    const int ik = brev(kk & (M - 1), fc.logM), im = brev((M - kk) & (M - 1), fc.logM);
     const V w = twn[kk];
-    const T tr = (er + (w.x * orr - w.y * oi)) * inv;
-    const T ti = (ei + (w.x * oi + w.y * orr)) * inv;
+    auto split = [&](const V *zz, T &tr, T &ti) {
+      const V zk = zz[ik], zm = zz[im];
+      const T er = h * (zk.x + zm.x), ei = h * (zk.y - zm.y);
+      const T orr = h * (zk.y + zm.y), oi = -h * (zk.x - zm.x);
+      tr = (er + (w.x * orr - w.y * oi)) * inv;
+      ti = (ei + (w.x * oi + w.y * orr)) * inv;
+    };
+    T tr, ti;
+    split(z, tr, ti);
+    if (fuse) {
+      // dst -= i kx X, then dst += X2: the two launches' FP64 updates in order
+      T tr2, ti2;
+      split(z2, tr2, ti2);
+      const cplx_t o = dst[kk];
+      if constexpr (kF) {
+        const T kv = from_f64<T>(fc.kx[kk]);
+        const cplx_t o1{o.re - f2d_bits((float)(T(0) * tr - kv * ti)), o.im - f2d_bits((float)(T(0) * ti + kv * tr))};
+        dst[kk] = cplx_t{o1.re + f2d_bits((float)tr2), o1.im + f2d_bits((float)ti2)};
+      } else {
+        const double xr = (double)tr, xi = (double)ti, kv = fc.kx[kk];
+        const cplx_t o1{o.re - (0.0 * xr - kv * xi), o.im - (0.0 * xi + kv * xr)};
+        dst[kk] = cplx_t{o1.re + (double)tr2, o1.im + (double)ti2};
+      }
+      continue;
+    }
     if constexpr (kF) {
       // the FP32 result enters the FP64 field with one exact widening and
       // one FP64 add per component
@@ -498,11 +537,21 @@ void launch_r2c(Ctx &c, const R2cArgs &a) {
   const long nlines = (long)(a.k1 - a.k0 + 1) * (a.j1 - a.j0 + 1);
   if (nlines <= 0) return;
   const dim3 grid((unsigned)((a.k1 - a.k0 + 1 + kWarpsPerBlock - 1) / kWarpsPerBlock), (unsigned)(a.j1 - a.j0 + 1));
-  const size_t smem = sizeof(double2) * fc.M * kWarpsPerBlock;
-  const int nops = (a.pro == PRO_LOAD) ? 1 : (a.pro == PRO_PROD) ? 2 : 3;
+  if (a.fuse_flux && (a.pro != PRO_PROD || a.epi != EPI_SUB_IK))
+    throw CudaError("r2c: a fused flux goes with a product and dst -= i kx X");
+  // a fused launch holds both lines' spectra
+  const size_t smem = sizeof(double2) * fc.M * kWarpsPerBlock * (a.fuse_flux ? 2 : 1);
+  // algorithmic bytes: the input planes read (the flux's field, U2b and U3b;
+  // a fused launch reads its product's second factor once, as the flux's
+  // field) at the size of the copy the kernel reads, and the spectrum
+  // (an FP32 kernel reading FP32 copies: 4 bytes an element; FP64 fields,
+  // or float-float planes as hi and lo: 8)
+  const bool lp = fft_lowp(c, a.lowp);
+  const double elt = (lp && a.af) ? 4.0 : 8.0;
+  const int nops = (a.pro == PRO_LOAD) ? 1 : (a.pro == PRO_PROD) ? (a.fuse_flux ? 4 : 2) : 3;
   const double epi = (a.epi == EPI_STORE) ? 16.0 * (c.d.NX2P + 1) : 32.0 * (c.d.NKX + 1);
-  KScope ks(c, KC_R2C, nlines * (8.0 * c.d.NX * nops + epi));
-  if (fft_lowp(c, a.lowp)) run_r2c<float>(grid, smem / 2, c.stream, fc, a);
+  KScope ks(c, KC_R2C, nlines * (elt * c.d.NX * nops + epi));
+  if (lp) run_r2c<float>(grid, smem / 2, c.stream, fc, a);
   else if (fft_ff(c, a.lowp)) run_r2c<FF>(grid, smem, c.stream, fc, a);
   else run_r2c<double>(grid, smem, c.stream, fc, a);
   after_launch(c);
@@ -514,7 +563,10 @@ void launch_c2r(Ctx &c, const C2rArgs &a) {
   if (nlines <= 0) return;
   const dim3 grid((unsigned)((a.k1 - a.k0 + 1 + kWarpsPerBlock - 1) / kWarpsPerBlock), (unsigned)(a.j1 - a.j0 + 1));
   const size_t smem = sizeof(double2) * fc.M * kWarpsPerBlock;
-  KScope ks(c, KC_C2R, nlines * (16.0 * (c.d.NKX + 1) * (a.src2 ? 2 : 1) + 8.0 * (c.d.NX + 2)));
+  // algorithmic bytes: the spectra read, the planes written (FP64, FP32 copy
+  // and float-float low part as given)
+  const double out = (a.dst ? 8.0 : 0.0) + (a.dstf ? 4.0 : 0.0) + (a.dstlo ? 4.0 : 0.0);
+  KScope ks(c, KC_C2R, nlines * (16.0 * (c.d.NKX + 1) * (a.src2 ? 2 : 1) + out * (c.d.NX + 2)));
   if (fft_lowp(c, a.lowp)) run_c2r<float>(grid, smem / 2, c.stream, fc, a);
   else if (fft_ff(c, a.lowp)) run_c2r<FF>(grid, smem, c.stream, fc, a);
   else run_c2r<double>(grid, smem, c.stream, fc, a);

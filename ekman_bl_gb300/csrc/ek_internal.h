@@ -83,7 +83,10 @@ struct Metrics {
   // per-cell coefficient planes (metric-only, built by launch_metric_tables):
   // pg[0..4] the pressure-gradient weights of the CJOB_12/CJOB_22 combination
   // and pg[5..9] of the CJOB_11/CJOB_21 one, for (p0, p(k+1), p(k-1),
-  // p(j+1), p(j-1)), each with its 0.5; pg[10] = 1/INT_JACOB
+  // p(j+1), p(j-1)), each with its 0.5; pg[10] = 1/INT_JACOB; pg[11] and
+  // pg[12] the background-stratification terms of the scalar right-hand
+  // side that depend on (K, J) only: the coefficient of CU2 and the TH_BAR
+  // diffusion bracket that KAPPA/4 multiplies
   double *pg = nullptr;
   // LES variants GMAT_*_y / GMAT_*_z (face layout; null without LES)
   double *g11y = nullptr, *g12y = nullptr, *g22y = nullptr, *g11z = nullptr, *g12z = nullptr, *g22z = nullptr;
@@ -306,9 +309,12 @@ struct Ctx {
   std::vector<MgLevelF> mgf_levels;
   float *mgf_scratch = nullptr;
   float *mgf_phh = nullptr, *mgf_phl = nullptr;  // float-float finest iterate
+  float *mgf_phh2 = nullptr, *mgf_phl2 = nullptr;  // its second buffer (alternate corrections)
   float *mgf_bh = nullptr, *mgf_bl = nullptr;    // float-float finest rhs
   float *mgf_cfh = nullptr, *mgf_cfl = nullptr;  // float-float finest coefficients
   int mgf_pmax = 0;
+  float *mgf_tailfac = nullptr;  // Thomas factors of the coarse levels' lines (k_f_vtail), per problem
+  size_t mgf_tailfac_n = 0;
   // residual rule: left null vector of the finest kx = 0 operator (nfx*nfy,
   // unit norm), for the well-posed kx = 0 solve
   double *mg_z = nullptr;
@@ -432,6 +438,14 @@ struct R2cArgs {
   // EPI_ADD: also zero the modes above NX/3, as a state's forward transform
   // does (EPI_STORE always does)
   int zero_hi;
+  // PRO_PROD with EPI_SUB_IK and fuse_flux = 1: the same launch also
+  // transforms the flux term of a2 against b2 (PRO_FLUX with visc2, plus
+  // extra2/extraf2) and adds it, dst = dst - i kx X + X2, as the two
+  // launches would in turn
+  int fuse_flux;
+  const double *a2, *b2, *extra2;
+  const float *a2f, *b2f, *extraf2;
+  double visc2;
 };
 void launch_r2c(Ctx &c, const R2cArgs &a);
 struct C2rArgs {
@@ -512,6 +526,8 @@ void mg_work_alloc(Ctx &c, MgWork &w, int pmax);
 void mg_work_free(MgWork &w);
 int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_host, ek_mg_stats *st);
 void mgfast_alloc(Ctx &c, int pmax);
+// the coarse levels 1..ltop the mixed solver runs in one launch per cycle
+int mgfast_tail_levels(const Ctx &c);
 int mgfast_autotune(Ctx &c, int reps, std::string &report);
 
 // restart files (ek_io.cpp): SAVE_FLOW / READ_FLOW records from and into the state

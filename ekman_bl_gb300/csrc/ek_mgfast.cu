@@ -41,7 +41,8 @@ struct FastDev {
   LvF lv[24];
   float *scr;              // finest-size scratch x P (residual / correction)
   double *rhs;              // FP64 finest rhs
-  float *phh, *phl;         // float-float finest iterate, with ghosts
+  float *phh, *phl;         // float-float finest iterate, with ghosts (buffer 0)
+  float *phh2, *phl2;       // buffer 1: problem p's iterate after n corrections is in buffer n & 1
   float *bh, *bl;           // float-float finest rhs
   const float *cfh, *cfl;   // float-float finest coefficients
   int nfx, nfy;
@@ -58,53 +59,89 @@ __device__ __forceinline__ float &E(const LvF &L, int P, int i, int j, int p) {
 }
 
 // r = b - A phi at the finest level in float-float (about 48 bits, on the
-// FP32 pipe); r32 = r; e_finest = 0 (ghosts included); per-problem |b|^2 and
-// |r|^2.  Block row jr = j for j = 0..ny+1, lanes over 32 problems.
+// FP32 pipe); r32 = r; per-problem |b|^2 and |r|^2.  With `update` the
+// correction of the cycle just run is applied first, phi' = phi + e (the
+// float-float sum), and written to the other iterate buffer, ghosts
+// included; r is then the residual of phi'.  The iterate of problem p is in
+// buffer cycles[p] & 1 (corrections applied so far).  Block row j = 1..ny,
+// lanes over 32 problems; each warp walks a contiguous run of i with the
+// values at i-1, i, i+1 of row j kept in registers.
 constexpr int kRY = 8;
-__global__ void __launch_bounds__(32 * kRY) k_f_resid_ff(FastDev g) {
+// (at most 64 registers: four blocks an SM; its loads need the warps)
+template <bool UPDATE, bool ORTH>
+__global__ void __launch_bounds__(32 * kRY, 4) k_f_resid_ff(FastDev g) {
   if (*g.alldone) return;
   const int P = g.P;
   const int p = blockIdx.x * 32 + threadIdx.x;
   const int ty = threadIdx.y;
-  const int nx = g.nfx, ny = g.nfy, j = (int)blockIdx.y;
+  const int nx = g.nfx, ny = g.nfy, j = 1 + (int)blockIdx.y;
   const size_t npt = (size_t)nx * ny;
-  const LvF &F = g.lv[g.ngrid - 1];
   float sb = 0.f, sr = 0.f;
   const bool act = (p < P) && !g.done[p];
   if (act) {
-    for (int i = ty; i <= nx + 1; i += kRY) F.e[((size_t)j * (nx + 2) + i) * P + p] = 0.f;
-    if (j >= 1 && j <= ny) {
-      const size_t si = P, sj = (size_t)(nx + 2) * P;
-      const FF kx2(g.kx2[p]);
-      for (int i = 1 + ty; i <= nx; i += kRY) {
-        const size_t pt = (size_t)(j - 1) * nx + (i - 1);
-        const size_t q = ((size_t)j * (nx + 2) + i) * P + p;
-        auto PH = [&](long o) { return FF(g.phh[q + o], g.phl[q + o]); };
-        auto CF = [&](int l) { return FF(g.cfh[l * npt + pt], g.cfl[l * npt + pt]); };
-        FF s = CF(0) * PH((long)si);
-        if (!g.orth) s = s + CF(1) * PH((long)(si + sj));
-        s = s + CF(2) * PH((long)sj);
-        if (!g.orth) s = s + CF(3) * PH((long)sj - (long)si);
-        s = s + CF(4) * PH(-(long)si);
-        if (!g.orth) s = s + CF(5) * PH(-(long)(si + sj));
-        s = s + CF(6) * PH(-(long)sj);
-        if (!g.orth) s = s + CF(7) * PH((long)si - (long)sj);
-        const FF c9 = ((-kx2 * CF(10)) - CF(8)) + CF(9);
-        s = s + c9 * PH(0);
-        const FF b(g.bh[pt * P + p], g.bl[pt * P + p]);
-        const FF r = b - s;
-        const float r32 = __fadd_rn(r.hi, r.lo);
-        sb = fmaf(b.hi, b.hi, sb);
-        sr = fmaf(r32, r32, sr);
-        F.r[pt * P + p] = r32;
+    const int par = g.cycles[p] & 1;
+    const float *__restrict__ sh = par ? g.phh2 : g.phh;
+    const float *__restrict__ sl = par ? g.phl2 : g.phl;
+    float *__restrict__ dh = par ? g.phh : g.phh2;
+    float *__restrict__ dl = par ? g.phl : g.phl2;
+    const float *__restrict__ ef = g.lv[g.ngrid - 1].e;
+    const size_t si = P, sj = (size_t)(nx + 2) * P;
+    const FF kx2(g.kx2[p]);
+    auto V = [&](size_t q) {
+      FF v(sh[q], sl[q]);
+      if (UPDATE) v = v + FF(ef[q], 0.f);
+      return v;
+    };
+    const int per = (nx + kRY - 1) / kRY;
+    const int i0 = 1 + ty * per, i1 = min(nx, i0 + per - 1);
+    const size_t row = (size_t)j * (nx + 2) * P + p;
+    FF wm, wc;
+    if (i0 <= i1) {
+      wm = V(row + (size_t)(i0 - 1) * si);
+      wc = V(row + (size_t)i0 * si);
+    }
+    for (int i = i0; i <= i1; ++i) {
+      const size_t pt = (size_t)(j - 1) * nx + (i - 1);
+      const size_t q = row + (size_t)i * si;
+      auto CF = [&](int l) { return FF(g.cfh[l * npt + pt], g.cfl[l * npt + pt]); };
+      const FF wp = V(q + si), wn = V(q + sj), ws = V(q - sj);
+      FF s = CF(0) * wp;
+      if (!ORTH) s = s + CF(1) * V(q + si + sj);
+      s = s + CF(2) * wn;
+      if (!ORTH) s = s + CF(3) * V(q + sj - si);
+      s = s + CF(4) * wm;
+      if (!ORTH) s = s + CF(5) * V(q - si - sj);
+      s = s + CF(6) * ws;
+      if (!ORTH) s = s + CF(7) * V(q + si - sj);
+      const FF c9 = ((-kx2 * CF(10)) - CF(8)) + CF(9);
+      s = s + c9 * wc;
+      const FF b(g.bh[pt * P + p], g.bl[pt * P + p]);
+      const FF r = b - s;
+      const float r32 = __fadd_rn(r.hi, r.lo);
+      sb = fmaf(b.hi, b.hi, sb);
+      sr = fmaf(r32, r32, sr);
+      g.lv[g.ngrid - 1].r[pt * P + p] = r32;
+      if (UPDATE) {
+        dh[q] = wc.hi;
+        dl[q] = wc.lo;
+        if (i == nx - 1) {
+          dh[row] = wc.hi;
+          dl[row] = wc.lo;
+        }
+        if (i == 2) {
+          dh[row + (size_t)(nx + 1) * si] = wc.hi;
+          dl[row + (size_t)(nx + 1) * si] = wc.lo;
+        }
       }
+      wm = wc;
+      wc = wp;
     }
   }
   __shared__ float red[2][kRY][32];
   red[0][ty][threadIdx.x] = sb;
   red[1][ty][threadIdx.x] = sr;
   __syncthreads();
-  if (ty == 0 && act && j >= 1 && j <= ny) {
+  if (ty == 0 && act) {
     for (int y = 1; y < kRY; ++y) {
       sb += red[0][y][threadIdx.x];
       sr += red[1][y][threadIdx.x];
@@ -254,7 +291,10 @@ __global__ void k_f_stats(FastDev g, StepStats *out) {
 // c7 = 0 and c3 = 0 after MUDPACK's Neumann folding.  c' is kept in cp, d'
 // overwrites e until the back substitution.
 constexpr int kChunk = 8;
-__device__ __forceinline__ void yline_solve(const LvF &L, int P, int p, int i, float kx2, bool orth) {
+// zero_nbr: the neighbouring lines hold zero (the first sweep of a cycle
+// from e = 0), so their terms are left out and their stale values unread
+__device__ __forceinline__ void yline_solve(const LvF &L, int P, int p, int i, float kx2, bool orth,
+                                            bool zero_nbr = false) {
   const int nx = L.nx, ny = L.ny;
   const size_t npt = (size_t)nx * ny;
   const size_t si = P, sj = (size_t)(nx + 2) * P;
@@ -270,10 +310,13 @@ __device__ __forceinline__ void yline_solve(const LvF &L, int P, int p, int i, f
       if (j > ny) break;
       const size_t pt = (size_t)(j - 1) * nx + (i - 1);
       const float *ep = &L.e[((size_t)j * (nx + 2) + i) * P + p];
-      float d = L.r[pt * P + p] - cf[pt] * ep[si] - cf[4 * npt + pt] * ep[-(long)si];
-      if (orth == false)
-        d = d - cf[npt + pt] * ep[si + sj] - cf[3 * npt + pt] * ep[sj - si] - cf[5 * npt + pt] * ep[-(long)(si + sj)] -
-            cf[7 * npt + pt] * ep[si - sj];
+      float d = L.r[pt * P + p];
+      if (!zero_nbr) {
+        d = d - cf[pt] * ep[si] - cf[4 * npt + pt] * ep[-(long)si];
+        if (orth == false)
+          d = d - cf[npt + pt] * ep[si + sj] - cf[3 * npt + pt] * ep[sj - si] -
+              cf[5 * npt + pt] * ep[-(long)(si + sj)] - cf[7 * npt + pt] * ep[si - sj];
+      }
       dv[u] = d;
       av[u] = cf[6 * npt + pt];
       cv[u] = cf[2 * npt + pt];
@@ -383,7 +426,7 @@ __device__ __forceinline__ void xline_solve(const LvF &L, int P, int p, int j, f
 }
 
 // y-lines i = i0, i0+istep, ... (ncol of them), all problems
-__global__ void __launch_bounds__(64) k_f_yline(FastDev g, int level, int i0, int istep, int ncol) {
+__global__ void __launch_bounds__(64) k_f_yline(FastDev g, int level, int i0, int istep, int ncol, int zero_nbr) {
   if (*g.alldone) return;
   const LvF L = g.lv[level - 1];
   const int P = g.P;
@@ -391,7 +434,7 @@ __global__ void __launch_bounds__(64) k_f_yline(FastDev g, int level, int i0, in
   for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
     const int p = (int)(t % P);
     if (g.done[p]) continue;
-    yline_solve(L, P, p, i0 + istep * (int)(t / P), (float)g.kx2[p], g.orth != 0);
+    yline_solve(L, P, p, i0 + istep * (int)(t / P), (float)g.kx2[p], g.orth != 0, zero_nbr != 0);
   }
 }
 
@@ -424,7 +467,9 @@ enum { SH_A, SH_B, SH_C, SH_D, SH_YF, SH_VF, SH_WF, SH_YL, SH_VL, SH_WL, SH_S, S
 // 4-row segments are capped at 48 registers, so that two or three blocks
 // share an SM (their per-thread arrays are half as large)
 template <bool XL, bool ORTH, int LANES, int SEG>
-__global__ void __launch_bounds__(1024) __maxnreg__(SEG == 4 ? 48 : 64) k_f_pline(FastDev g, int level, int l0, int lstep, int mb, int me) {
+// zero_e: the first sweep of a cycle from e = 0 (y-lines only): the
+// neighbouring lines' terms are left out and their stale values unread.
+__global__ void __launch_bounds__(1024) __maxnreg__(SEG == 4 ? 48 : 64) k_f_pline(FastDev g, int level, int l0, int lstep, int mb, int me, int zero_e) {
   constexpr int kSegMax = SEG;
   if (*g.alldone) return;
   extern __shared__ float sh[];
@@ -461,9 +506,9 @@ __global__ void __launch_bounds__(1024) __maxnreg__(SEG == 4 ? 48 : 64) k_f_plin
     } else {
       a = cp[6 * npt];
       c = cp[2 * npt];
-      dd = dd - cp[0] * ep[si] - cp[4 * npt] * *(ep - si);
+      if (!zero_e) dd = dd - cp[0] * ep[si] - cp[4 * npt] * *(ep - si);
     }
-    if (!ORTH)
+    if (!ORTH && !zero_e)
       dd = dd - cp[npt] * ep[si + sj] - cp[3 * npt] * ep[sj - si] - cp[5 * npt] * *(ep - (si + sj)) -
            cp[7 * npt] * *(ep - (sj - si));
     d = dd;
@@ -651,6 +696,57 @@ __global__ void k_f_coarsest(FastDev g, int sweeps) {
 // index needs a division.
 constexpr int kRowWarps = 8;
 
+// The level operations below act on one point of one problem: arrays with
+// the problem index fastest (stride P, problem p), as the batched kernels
+// keep them in global memory, or P = 1, p = 0 for one problem's arrays in
+// shared memory (k_f_vtail).  One definition serves both, so a level gives
+// the same numbers in either.
+
+// residual of the correction equation at point (i, j) of a level (FP32)
+__device__ __forceinline__ void f_resid_at(const float *__restrict__ cf, const float *__restrict__ ee,
+                                           const float *__restrict__ rr, float *__restrict__ scr, int nx, int ny,
+                                           int P, int p, int i, int j, float kx2, bool orth) {
+  const size_t npt = (size_t)nx * ny;
+  const size_t si = P, sj = (size_t)(nx + 2) * P;
+  const size_t pt = (size_t)(j - 1) * nx + (i - 1);
+  const float *ep = &ee[((size_t)j * (nx + 2) + i) * P + p];
+  float s = cf[pt] * ep[si] + cf[2 * npt + pt] * ep[sj] + cf[4 * npt + pt] * ep[-(long)si] +
+            cf[6 * npt + pt] * ep[-(long)sj];
+  if (!orth)
+    s += cf[npt + pt] * ep[si + sj] + cf[3 * npt + pt] * ep[sj - si] + cf[5 * npt + pt] * ep[-(long)(si + sj)] +
+         cf[7 * npt + pt] * ep[si - sj];
+  const float c9 = ((-kx2 * cf[10 * npt + pt]) - cf[8 * npt + pt]) + cf[9 * npt + pt];
+  s += c9 * ep[0];
+  scr[((size_t)j * (nx + 2) + i) * P + p] = rr[pt * P + p] - s;
+}
+
+// full weighting (res2, mudcom.f:120-257) of the fine residual in scr to the
+// coarse rhs at (ic, jc), and e_coarse = 0 there (ghosts included: ic =
+// 0..ncx+1, jc = 0..ncy+1)
+__device__ __forceinline__ void f_restrict_at(const float *__restrict__ scr, float *__restrict__ ce,
+                                              float *__restrict__ cr, int nx, int ny, int ncx, int ncy, int P, int p,
+                                              int ic, int jc) {
+  const int ix = (ncx == nx) ? 0 : 1, jy = (ncy == ny) ? 0 : 1;
+  ce[((size_t)jc * (ncx + 2) + ic) * P + p] = 0.f;
+  if (ic < 1 || ic > ncx || jc < 1 || jc > ncy) return;
+  const int i = ic + ix * (ic - 1), j = jc + jy * (jc - 1);
+  int im1 = i - 1, ip1 = i + 1, jm1 = j - 1, jp1 = j + 1;
+  if (ic == 1 || ic == ncx) {
+    im1 = max(i - 1, 2);
+    ip1 = min(i + 1, nx - 1);
+    if (i == 1) im1 = nx - 1;
+    if (i == nx) ip1 = 2;
+  }
+  if (jc == 1 || jc == ncy) {
+    jm1 = max(j - 1, 2);
+    jp1 = min(j + 1, ny - 1);
+  }
+  auto R = [&](int a, int b) { return scr[((size_t)b * (nx + 2) + a) * P + p]; };
+  cr[((size_t)(jc - 1) * ncx + (ic - 1)) * P + p] =
+      (R(im1, jm1) + R(ip1, jm1) + R(im1, jp1) + R(ip1, jp1) + 2.f * (R(im1, j) + R(ip1, j) + R(i, jm1) + R(i, jp1)) +
+       4.f * R(i, j)) * .0625f;
+}
+
 // residual of the correction equation at a level (FP32) into the scratch
 __global__ void __launch_bounds__(32 * kRowWarps) k_f_resid32(FastDev g, int level) {
   if (*g.alldone) return;
@@ -659,28 +755,11 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_f_resid32(FastDev g, int lev
   const int p = blockIdx.x * 32 + threadIdx.x;
   if (p >= P || g.done[p]) return;
   const int nx = L.nx, j = 1 + (int)blockIdx.y;
-  const size_t npt = (size_t)nx * L.ny;
-  const size_t si = P, sj = (size_t)(nx + 2) * P;
   const float kx2 = (float)g.kx2[p];
-  // restrict-qualified copies: the stores cannot alias the loads, so the
-  // unrolled iterations' loads are issued together
-  const float *__restrict__ cf = L.cof;
-  const float *__restrict__ ee = L.e;
-  const float *__restrict__ rr = L.r;
-  float *__restrict__ scr = g.scr;
+  const bool orth = g.orth != 0;
 #pragma unroll 4
-  for (int i = 1 + (int)threadIdx.y; i <= nx; i += kRowWarps) {
-    const size_t pt = (size_t)(j - 1) * nx + (i - 1);
-    const float *ep = &ee[((size_t)j * (nx + 2) + i) * P + p];
-    float s = cf[pt] * ep[si] + cf[2 * npt + pt] * ep[sj] + cf[4 * npt + pt] * ep[-(long)si] +
-              cf[6 * npt + pt] * ep[-(long)sj];
-    if (!g.orth)
-      s += cf[npt + pt] * ep[si + sj] + cf[3 * npt + pt] * ep[sj - si] + cf[5 * npt + pt] * ep[-(long)(si + sj)] +
-           cf[7 * npt + pt] * ep[si - sj];
-    const float c9 = ((-kx2 * cf[10 * npt + pt]) - cf[8 * npt + pt]) + cf[9 * npt + pt];
-    s += c9 * ep[0];
-    scr[((size_t)j * (nx + 2) + i) * P + p] = rr[pt * P + p] - s;
-  }
+  for (int i = 1 + (int)threadIdx.y; i <= nx; i += kRowWarps)
+    f_resid_at(L.cof, L.e, L.r, g.scr, nx, L.ny, P, p, i, j, kx2, orth);
 }
 
 // full weighting (res2, mudcom.f:120-257) to the coarse rhs; e_coarse = 0
@@ -691,33 +770,10 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_f_restrict(FastDev g, int le
   const int P = g.P;
   const int p = blockIdx.x * 32 + threadIdx.x;
   if (p >= P || g.done[p]) return;
-  const int nx = F.nx, ny = F.ny, ncx = C.nx, ncy = C.ny;
-  const int ix = (ncx == nx) ? 0 : 1, jy = (ncy == ny) ? 0 : 1;
   const int jc = (int)blockIdx.y;
-  const float *__restrict__ scr = g.scr;
-  float *__restrict__ ce = C.e;
-  float *__restrict__ cr = C.r;
 #pragma unroll 4
-  for (int ic = (int)threadIdx.y; ic <= ncx + 1; ic += kRowWarps) {
-    ce[((size_t)jc * (ncx + 2) + ic) * P + p] = 0.f;
-    if (ic < 1 || ic > ncx || jc < 1 || jc > ncy) continue;
-    const int i = ic + ix * (ic - 1), j = jc + jy * (jc - 1);
-    int im1 = i - 1, ip1 = i + 1, jm1 = j - 1, jp1 = j + 1;
-    if (ic == 1 || ic == ncx) {
-      im1 = max(i - 1, 2);
-      ip1 = min(i + 1, nx - 1);
-      if (i == 1) im1 = nx - 1;
-      if (i == nx) ip1 = 2;
-    }
-    if (jc == 1 || jc == ncy) {
-      jm1 = max(j - 1, 2);
-      jp1 = min(j + 1, ny - 1);
-    }
-    auto R = [&](int a, int b) { return scr[((size_t)b * (nx + 2) + a) * P + p]; };
-    cr[((size_t)(jc - 1) * ncx + (ic - 1)) * P + p] =
-        (R(im1, jm1) + R(ip1, jm1) + R(im1, jp1) + R(ip1, jp1) + 2.f * (R(im1, j) + R(ip1, j) + R(i, jm1) + R(i, jp1)) +
-         4.f * R(i, j)) * .0625f;
-  }
+  for (int ic = (int)threadIdx.y; ic <= C.nx + 1; ic += kRowWarps)
+    f_restrict_at(g.scr, C.e, C.r, F.nx, F.ny, C.nx, C.ny, P, p, ic, jc);
 }
 
 // cubic/linear prolongation (prolon1/prolon2, mudcom.f:261-499) of the
@@ -736,6 +792,41 @@ __device__ __forceinline__ float prolon1f(int i, int ncx, int nx, bool cubic, F 
   return (-q(nx - 4) + 9.f * (q(nx - 2) + q(nx)) - q(3)) * .0625f;
 }
 
+// fine row j = 2 rr + 1 (y coarsened) or rr + 1, point i: stage 1 into scr
+__device__ __forceinline__ void f_prolong_x_at(const float *__restrict__ ce, float *__restrict__ scr, int nx, int ny,
+                                               int ncx, int ncy, int P, int p, int i, int rr) {
+  const bool ycoarse = ncy < ny;
+  const bool cubic = ncx >= 4;
+  const int j = ycoarse ? 2 * rr + 1 : rr + 1;
+  const int jc = ycoarse ? j / 2 + 1 : j;
+  auto pc = [&](int ic) { return ce[((size_t)jc * (ncx + 2) + ic) * P + p]; };
+  scr[((size_t)j * (nx + 2) + i) * P + p] = prolon1f(i, ncx, nx, cubic, pc);
+}
+
+// stage 2 at fine point (i, j): the rows between (cubic or linear in y), then
+// e += correction, with the periodic ghosts written together with their
+// sources
+__device__ __forceinline__ void f_prolong_y_at(const float *__restrict__ scr, float *__restrict__ ef, int nx, int ny,
+                                               int ncy, int P, int p, int i, int j) {
+  const bool ycoarse = ncy < ny;
+  const bool cubic = ncy >= 4;
+  const size_t rowj = (size_t)j * (nx + 2) * P + p;
+  auto Q = [&](int jj) { return scr[((size_t)jj * (nx + 2) + i) * P + p]; };
+  float v;
+  if (ycoarse && !(j & 1)) {
+    if (!cubic) v = 0.5f * (Q(j - 1) + Q(j + 1));
+    else if (j >= 4 && j <= ny - 3) v = (-Q(j - 3) + 9.f * (Q(j - 1) + Q(j + 1)) - Q(j + 3)) * .0625f;
+    else if (j == 2) v = (5.f * Q(1) + 15.f * Q(3) - 5.f * Q(5) + Q(7)) * .0625f;
+    else v = (5.f * Q(ny) + 15.f * Q(ny - 2) - 5.f * Q(ny - 4) + Q(ny - 6)) * .0625f;
+  } else {
+    v = Q(j);
+  }
+  const float ne = ef[rowj + (size_t)i * P] + v;
+  ef[rowj + (size_t)i * P] = ne;
+  if (i == nx - 1) ef[rowj] = ne;
+  if (i == 2) ef[rowj + (size_t)(nx + 1) * P] = ne;
+}
+
 // block row rr: fine row j = 2 rr + 1 (y coarsened) or rr + 1
 __global__ void __launch_bounds__(32 * kRowWarps) k_f_prolong_x(FastDev g, int level) {
   if (*g.alldone) return;
@@ -743,82 +834,303 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_f_prolong_x(FastDev g, int l
   const int P = g.P;
   const int p = blockIdx.x * 32 + threadIdx.x;
   if (p >= P || g.done[p]) return;
-  const int nx = F.nx, ny = F.ny, ncx = C.nx, ncy = C.ny;
-  const bool ycoarse = ncy < ny;
-  const bool cubic = ncx >= 4;
   const int rr = (int)blockIdx.y;
-  const int j = ycoarse ? 2 * rr + 1 : rr + 1;
-  const int jc = ycoarse ? j / 2 + 1 : j;
-  const float *__restrict__ ce = C.e;
-  float *__restrict__ scr = g.scr;
-  auto pc = [&](int ic) { return ce[((size_t)jc * (ncx + 2) + ic) * P + p]; };
 #pragma unroll 4
-  for (int i = 1 + (int)threadIdx.y; i <= nx; i += kRowWarps)
-    scr[((size_t)j * (nx + 2) + i) * P + p] = prolon1f(i, ncx, nx, cubic, pc);
+  for (int i = 1 + (int)threadIdx.y; i <= F.nx; i += kRowWarps) f_prolong_x_at(C.e, g.scr, F.nx, F.ny, C.nx, C.ny, P, p, i, rr);
 }
 
-// stage 2: the rows between (cubic or linear in y), then e += correction,
-// with the periodic ghosts written together with their sources (block row
-// j - 1)
+// block row j - 1
 __global__ void __launch_bounds__(32 * kRowWarps) k_f_prolong_y(FastDev g, int level) {
   if (*g.alldone) return;
   const LvF F = g.lv[level - 1], C = g.lv[level - 2];
   const int P = g.P;
   const int p = blockIdx.x * 32 + threadIdx.x;
   if (p >= P || g.done[p]) return;
-  const int nx = F.nx, ny = F.ny, ncy = C.ny;
-  const bool ycoarse = ncy < ny;
-  const bool cubic = ncy >= 4;
   const int j = 1 + (int)blockIdx.y;
-  const float *__restrict__ scr = g.scr;
-  float *__restrict__ ef = F.e;
-  const size_t rowj = (size_t)j * (nx + 2) * P + p;
 #pragma unroll 4
-  for (int i = 1 + (int)threadIdx.y; i <= nx; i += kRowWarps) {
-    auto Q = [&](int jj) { return scr[((size_t)jj * (nx + 2) + i) * P + p]; };
-    float v;
-    if (ycoarse && !(j & 1)) {
-      if (!cubic) v = 0.5f * (Q(j - 1) + Q(j + 1));
-      else if (j >= 4 && j <= ny - 3) v = (-Q(j - 3) + 9.f * (Q(j - 1) + Q(j + 1)) - Q(j + 3)) * .0625f;
-      else if (j == 2) v = (5.f * Q(1) + 15.f * Q(3) - 5.f * Q(5) + Q(7)) * .0625f;
-      else v = (5.f * Q(ny) + 15.f * Q(ny - 2) - 5.f * Q(ny - 4) + Q(ny - 6)) * .0625f;
-    } else {
-      v = Q(j);
+  for (int i = 1 + (int)threadIdx.y; i <= F.nx; i += kRowWarps) f_prolong_y_at(g.scr, F.e, F.nx, F.ny, C.ny, P, p, i, j);
+}
+
+// The coarse end of a V(1,1) cycle in one launch: levels ltop, ltop-1, ..., 1
+// of one problem per block, with the level arrays in shared memory and the
+// (problem-independent) coefficients read through L1.  Each level down: the
+// pre-smoothing sweep, the residual, the restriction; the coarsest level's
+// `sweeps` alternating sweeps (and, for kx^2 = 0, its zero-mean shift); each
+// level up: the prolongation and the post-smoothing sweep -- the operations
+// and order of the per-level launches, with every line solved by one thread
+// (lines of one colour are independent).  On the coarse levels a per-level
+// launch does a few microseconds of work behind a launch and a grid-wide
+// dependency; here the levels follow each other behind block barriers.
+//
+// A line's Thomas factors (m = 1 / (b - a c'), c' = c m, per row) depend on
+// the problem's kx^2 and the level coefficients only, so k_f_tail_factors
+// computes them once per solve; a sweep then runs the recurrences
+// d' = (d - a d') m and x = d' - c' x, with no division on the chain.
+// In: the restricted rhs of level ltop (global); out: its correction e,
+// ghosts included (global).
+constexpr int kTailThreads = 64;
+constexpr int kTailMax = 12;
+struct TailPlan {
+  int ltop, sweeps;
+  int nfac;  // factor floats per problem: (c', m) of the y-lines and of the x-lines, every level
+  int fac0, scr, total;  // shared-memory offsets (floats): factor block, transfer scratch; total floats
+  int nx[kTailMax], ny[kTailMax];
+  int e[kTailMax], r[kTailMax];  // shared-memory offsets of e and r of level l + 1
+  int f[kTailMax];               // offset of level l + 1's y-line factors in the factor block (x-lines follow)
+};
+
+TailPlan make_tail_plan(const MgPlan &PL, int ltop) {
+  TailPlan t{};
+  t.ltop = ltop;
+  t.sweeps = std::max(8, (PL.lv[0].nx + PL.lv[0].ny) / 2);
+  int off = 0, fo = 0;
+  for (int l = 0; l < ltop; ++l) {
+    const int nx = PL.lv[l].nx, ny = PL.lv[l].ny;
+    t.nx[l] = nx;
+    t.ny[l] = ny;
+    t.e[l] = off;
+    off += (nx + 2) * (ny + 2);
+    t.r[l] = off;
+    off += nx * ny;
+    t.f[l] = fo;
+    fo += 4 * nx * ny;
+  }
+  t.scr = off;
+  off += (t.nx[ltop - 1] + 2) * (t.ny[ltop - 1] + 2);
+  off = (off + 3) & ~3;  // the factor block is copied as float4
+  t.fac0 = off;
+  t.nfac = fo;
+  t.total = off + fo;
+  return t;
+}
+
+// one level of one problem in shared memory (P = 1, p = 0)
+struct TailLv {
+  int nx, ny;
+  float *e, *r;
+  const float2 *fy, *fx;  // (c', m) per point, point (i, j) at (j-1) nx + (i-1)
+  const float *cof;
+};
+__device__ __forceinline__ TailLv tail_level_at(const TailPlan &t, const FastDev &g, float *sm, int l) {
+  TailLv L;
+  L.nx = t.nx[l];
+  L.ny = t.ny[l];
+  L.e = sm + t.e[l];
+  L.r = sm + t.r[l];
+  L.fy = reinterpret_cast<const float2 *>(sm + t.fac0 + t.f[l]);
+  L.fx = L.fy + (size_t)L.nx * L.ny;
+  L.cof = g.lv[l].cof;
+  return L;
+}
+
+// y-line at column i with precomputed factors (the rows of yline_solve)
+__device__ __forceinline__ void tail_yline(const TailLv &L, int i, bool orth) {
+  const int nx = L.nx, ny = L.ny, npt = nx * ny, sj = nx + 2;
+  const float *__restrict__ cf = L.cof;
+  const float *__restrict__ r = L.r;
+  const float2 *__restrict__ fy = L.fy;
+  float *__restrict__ e = L.e;
+  float dprev = 0.f;
+  for (int j0 = 1; j0 <= ny; j0 += kChunk) {
+    float dv[kChunk], av[kChunk], mv[kChunk];
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      const int j = j0 + u;
+      if (j > ny) break;
+      const int pt = (j - 1) * nx + (i - 1), q = j * sj + i;
+      float d = r[pt] - cf[pt] * e[q + 1] - cf[4 * npt + pt] * e[q - 1];
+      if (orth == false)
+        d = d - cf[npt + pt] * e[q + 1 + sj] - cf[3 * npt + pt] * e[q + sj - 1] - cf[5 * npt + pt] * e[q - 1 - sj] -
+            cf[7 * npt + pt] * e[q + 1 - sj];
+      dv[u] = d;
+      av[u] = cf[6 * npt + pt];
+      mv[u] = fy[pt].y;
     }
-    const float ne = ef[rowj + (size_t)i * P] + v;
-    ef[rowj + (size_t)i * P] = ne;
-    if (i == nx - 1) ef[rowj] = ne;
-    if (i == 2) ef[rowj + (size_t)(nx + 1) * P] = ne;
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      const int j = j0 + u;
+      if (j > ny) break;
+      dprev = (dv[u] - av[u] * dprev) * mv[u];
+      e[j * sj + i] = dprev;
+    }
+  }
+  float x = 0.f;
+  for (int j = ny; j >= 1; --j) {
+    x = e[j * sj + i] - fy[(j - 1) * nx + (i - 1)].x * x;
+    e[j * sj + i] = x;
+    if (i == nx - 1) e[j * sj] = x;
+    if (i == 2) e[j * sj + nx + 1] = x;
   }
 }
 
-// phi += e at the finest level in float-float, with the periodic ghosts of
-// phi (block row j - 1, lanes over 32 problems).
-__global__ void __launch_bounds__(32 * kRY) k_f_update_ff(FastDev g) {
+// x-line at row j with precomputed factors (the rows of xline_solve)
+__device__ __forceinline__ void tail_xline(const TailLv &L, int j, bool orth) {
+  const int nx = L.nx, ny = L.ny, npt = nx * ny, sj = nx + 2;
+  const float *__restrict__ cf = L.cof;
+  const float *__restrict__ r = L.r;
+  const float2 *__restrict__ fx = L.fx;
+  float *__restrict__ erow = L.e + j * sj;
+  const float g0 = erow[0], g1 = erow[nx + 1];
+  const int rb = (j - 1) * nx;
+  float dprev = 0.f;
+  for (int i0 = 1; i0 <= nx; i0 += kChunk) {
+    float dv[kChunk], av[kChunk], mv[kChunk];
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      const int i = i0 + u;
+      if (i > nx) break;
+      const int pt = rb + (i - 1);
+      float d = r[pt] - cf[2 * npt + pt] * erow[i + sj] - cf[6 * npt + pt] * erow[i - sj];
+      if (orth == false)
+        d = d - cf[npt + pt] * erow[i + 1 + sj] - cf[3 * npt + pt] * erow[i + sj - 1] -
+            cf[5 * npt + pt] * erow[i - 1 - sj] - cf[7 * npt + pt] * erow[i + 1 - sj];
+      float a = cf[4 * npt + pt];
+      if (i == 1) { d -= a * g0; a = 0.f; }
+      if (i == nx) d -= cf[pt] * g1;
+      dv[u] = d;
+      av[u] = a;
+      mv[u] = fx[pt].y;
+    }
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      const int i = i0 + u;
+      if (i > nx) break;
+      dprev = (dv[u] - av[u] * dprev) * mv[u];
+      erow[i] = dprev;
+    }
+  }
+  float x = 0.f;
+  for (int i = nx; i >= 1; --i) {
+    x = erow[i] - fx[rb + (i - 1)].x * x;
+    erow[i] = x;
+    if (i == nx - 1) erow[0] = x;
+    if (i == 2) erow[nx + 1] = x;
+  }
+}
+
+// one alternating-direction zebra sweep (the order of the per-level relax)
+__device__ __forceinline__ void tail_relax(const TailLv &L, bool orth, bool post) {
+  for (int k = 0; k < 2; ++k) {
+    const int col = post ? 2 - k : 1 + k;
+    LinePhase ph[2];
+    const int nph = line_phases(L.nx, col, ph);
+    for (int q = 0; q < nph; ++q) {
+      for (int c = threadIdx.x; c < ph[q].ncol; c += blockDim.x) tail_yline(L, ph[q].i0 + ph[q].istep * c, orth);
+      __syncthreads();
+    }
+  }
+  for (int k = 0; k < 2; ++k) {
+    const int col = post ? 2 - k : 1 + k;
+    const int nrow = (L.ny >= col) ? (L.ny - col) / 2 + 1 : 0;
+    for (int c = threadIdx.x; c < nrow; c += blockDim.x) tail_xline(L, col + 2 * c, orth);
+    __syncthreads();
+  }
+}
+
+// Thomas factors of every line of the levels 1..ltop, per problem (one block
+// per problem), into fac[p * nfac ...] in the shared-memory layout of the
+// factor block; the same m and c' as yline_solve / xline_solve compute
+__global__ void __launch_bounds__(kTailThreads) k_f_tail_factors(FastDev g, TailPlan t, float *fac) {
+  const int p = (int)blockIdx.x;
+  if (p >= g.P) return;
+  const float kx2 = (float)g.kx2[p];
+  float *fb = fac + (size_t)p * t.nfac;
+  for (int l = 0; l < t.ltop; ++l) {
+    const int nx = t.nx[l], ny = t.ny[l], npt = nx * ny;
+    const float *__restrict__ cf = g.lv[l].cof;
+    float2 *fy = reinterpret_cast<float2 *>(fb + t.f[l]);
+    float2 *fx = fy + npt;
+    for (int i = 1 + threadIdx.x; i <= nx; i += blockDim.x) {
+      float cprev = 0.f;
+      for (int j = 1; j <= ny; ++j) {
+        const int pt = (j - 1) * nx + (i - 1);
+        const float b = ((-kx2 * cf[10 * npt + pt]) - cf[8 * npt + pt]) + cf[9 * npt + pt];
+        const float m = 1.f / (b - cf[6 * npt + pt] * cprev);
+        cprev = cf[2 * npt + pt] * m;
+        fy[pt] = make_float2(cprev, m);
+      }
+    }
+    for (int j = 1 + threadIdx.x; j <= ny; j += blockDim.x) {
+      float cprev = 0.f;
+      for (int i = 1; i <= nx; ++i) {
+        const int pt = (j - 1) * nx + (i - 1);
+        const float b = ((-kx2 * cf[10 * npt + pt]) - cf[8 * npt + pt]) + cf[9 * npt + pt];
+        const float a = (i == 1) ? 0.f : cf[4 * npt + pt];
+        const float c = (i == nx) ? 0.f : cf[pt];
+        const float m = 1.f / (b - a * cprev);
+        cprev = c * m;
+        fx[pt] = make_float2(cprev, m);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kTailThreads) k_f_vtail(FastDev g, TailPlan t, const float *fac) {
   if (*g.alldone) return;
+  const int p = (int)blockIdx.x;
+  if (p >= g.P || g.done[p]) return;
+  extern __shared__ __align__(16) float tsh[];
   const int P = g.P;
-  const int p = blockIdx.x * 32 + threadIdx.x;
-  if (p >= P || g.done[p]) return;
-  const int nx = g.nfx, j = 1 + (int)blockIdx.y;
-  const LvF &F = g.lv[g.ngrid - 1];
-  const float *__restrict__ ef = F.e;
-  float *__restrict__ ph = g.phh;
-  float *__restrict__ pl = g.phl;
-  const size_t rowj = (size_t)j * (nx + 2) * P + p;
-#pragma unroll 4
-  for (int i = 1 + (int)threadIdx.y; i <= nx; i += kRY) {
-    const size_t q = rowj + (size_t)i * P;
-    const FF v = FF(ph[q], pl[q]) + FF(ef[q], 0.f);
-    ph[q] = v.hi;
-    pl[q] = v.lo;
-    if (i == nx - 1) {
-      ph[rowj] = v.hi;
-      pl[rowj] = v.lo;
+  const float kx2 = (float)g.kx2[p];
+  const bool orth = g.orth != 0;
+  const int ltop = t.ltop;
+  float *const scr = tsh + t.scr;
+  {
+    // this problem's factors (contiguous), the rhs of level ltop, e = 0
+    const float4 *src = reinterpret_cast<const float4 *>(fac + (size_t)p * t.nfac);
+    float4 *dst = reinterpret_cast<float4 *>(tsh + t.fac0);
+    for (int v = threadIdx.x; v < t.nfac / 4; v += blockDim.x) dst[v] = src[v];
+    const TailLv T = tail_level_at(t, g, tsh, ltop - 1);
+    const LvF &G = g.lv[ltop - 1];
+    const int ne = (T.nx + 2) * (T.ny + 2), nr = T.nx * T.ny;
+    for (int v = threadIdx.x; v < ne; v += blockDim.x) T.e[v] = 0.f;
+    for (int v = threadIdx.x; v < nr; v += blockDim.x) T.r[v] = G.r[(size_t)v * P + p];
+  }
+  __syncthreads();
+  for (int l = ltop; l >= 2; --l) {
+    const TailLv F = tail_level_at(t, g, tsh, l - 1), C = tail_level_at(t, g, tsh, l - 2);
+    tail_relax(F, orth, false);
+    for (int v = threadIdx.x; v < F.nx * F.ny; v += blockDim.x)
+      f_resid_at(F.cof, F.e, F.r, scr, F.nx, F.ny, 1, 0, 1 + v % F.nx, 1 + v / F.nx, kx2, orth);
+    __syncthreads();
+    for (int v = threadIdx.x; v < (C.nx + 2) * (C.ny + 2); v += blockDim.x)
+      f_restrict_at(scr, C.e, C.r, F.nx, F.ny, C.nx, C.ny, 1, 0, v % (C.nx + 2), v / (C.nx + 2));
+    __syncthreads();
+  }
+  {
+    const TailLv L = tail_level_at(t, g, tsh, 0);
+    for (int sw = 0; sw < t.sweeps; ++sw) tail_relax(L, orth, false);
+    if (kx2 == 0.f) {
+      // singular: keep the correction at zero mean, ghosts included (the
+      // sum in k_f_coarsest's order)
+      __shared__ float mean;
+      if (threadIdx.x == 0) {
+        float m = 0.f;
+        for (int j = 1; j <= L.ny; ++j)
+          for (int i = 1; i <= L.nx; ++i) m += L.e[j * (L.nx + 2) + i];
+        mean = m / (float)(L.nx * L.ny);
+      }
+      __syncthreads();
+      for (int v = threadIdx.x; v < L.ny * (L.nx + 2); v += blockDim.x) L.e[(L.nx + 2) + v] -= mean;
+      __syncthreads();
     }
-    if (i == 2) {
-      ph[rowj + (size_t)(nx + 1) * P] = v.hi;
-      pl[rowj + (size_t)(nx + 1) * P] = v.lo;
-    }
+  }
+  for (int l = 2; l <= ltop; ++l) {
+    const TailLv F = tail_level_at(t, g, tsh, l - 1), C = tail_level_at(t, g, tsh, l - 2);
+    const int nrr = (C.ny < F.ny) ? (F.ny + 1) / 2 : F.ny;
+    for (int v = threadIdx.x; v < F.nx * nrr; v += blockDim.x)
+      f_prolong_x_at(C.e, scr, F.nx, F.ny, C.nx, C.ny, 1, 0, 1 + v % F.nx, v / F.nx);
+    __syncthreads();
+    for (int v = threadIdx.x; v < F.nx * F.ny; v += blockDim.x)
+      f_prolong_y_at(scr, F.e, F.nx, F.ny, C.ny, 1, 0, 1 + v % F.nx, 1 + v / F.nx);
+    __syncthreads();
+    tail_relax(F, orth, true);
+  }
+  {
+    const TailLv T = tail_level_at(t, g, tsh, ltop - 1);
+    const LvF &G = g.lv[ltop - 1];
+    const int ne = (T.nx + 2) * (T.ny + 2);
+    for (int v = threadIdx.x; v < ne; v += blockDim.x) G.e[(size_t)v * P + p] = T.e[v];
   }
 }
 
@@ -829,9 +1141,12 @@ __global__ void __launch_bounds__(32 * kRY) k_f_phif(FastDev g) {
   const int p = blockIdx.x * 32 + threadIdx.x;
   if (p >= P) return;
   const int nx = g.nfx, j = 1 + (int)blockIdx.y;
+  const int par = g.cycles[p] & 1;
+  const float *__restrict__ ph = par ? g.phh2 : g.phh;
+  const float *__restrict__ pl = par ? g.phl2 : g.phl;
   for (int i = 1 + (int)threadIdx.y; i <= nx; i += kRY) {
     const size_t q = ((size_t)j * (nx + 2) + i) * P + p;
-    g.phif[((size_t)(j - 1) * nx + (i - 1)) * P + p] = (double)FF(g.phh[q], g.phl[q]);
+    g.phif[((size_t)(j - 1) * nx + (i - 1)) * P + p] = (double)FF(ph[q], pl[q]);
   }
 }
 
@@ -850,7 +1165,9 @@ bool pline_fits(int n, int lanes, int seg) {
 }
 
 void launch_pline(const FastDev &g, int l, bool xl, int l0, int lstep, int nline, int n, int lanes, int seg,
-                  cudaStream_t s) {
+                  cudaStream_t s, bool zero_e = false) {
+  if (zero_e && xl) throw CudaError("line solve: the zero-neighbour sweep is a y-line sweep");
+  const int z = zero_e ? 1 : 0;
   const int K = pline_segments(n, seg);
   // the kernel indexes with 32-bit offsets
   if ((size_t)(g.nfx + 2) * (g.nfy + 2) * g.P >= (1ull << 31) || 11ull * g.nfx * g.nfy >= (1ull << 31))
@@ -858,7 +1175,7 @@ void launch_pline(const FastDev &g, int l, bool xl, int l0, int lstep, int nline
   if (!pline_fits(n, lanes, seg)) {
     const unsigned b = (unsigned)(((long)nline * g.P + 63) / 64);
     if (xl) k_f_xline<<<b, 64, 0, s>>>(g, l, l0, nline);
-    else k_f_yline<<<b, 64, 0, s>>>(g, l, l0, lstep, nline);
+    else k_f_yline<<<b, 64, 0, s>>>(g, l, l0, lstep, nline, z);
     return;
   }
   const int mb = (n - K + 1) / K, me = (n - K + 1) % K;
@@ -867,11 +1184,11 @@ void launch_pline(const FastDev &g, int l, bool xl, int l0, int lstep, int nline
 #define EK_PLINE(W, S)                                                                             \
   do {                                                                                             \
     if (g.orth) {                                                                                  \
-      if (xl) k_f_pline<true, true, W, S><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);        \
-      else k_f_pline<false, true, W, S><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);          \
+      if (xl) k_f_pline<true, true, W, S><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me, z);        \
+      else k_f_pline<false, true, W, S><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me, z);          \
     } else {                                                                                       \
-      if (xl) k_f_pline<true, false, W, S><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);       \
-      else k_f_pline<false, false, W, S><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me);         \
+      if (xl) k_f_pline<true, false, W, S><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me, z);       \
+      else k_f_pline<false, false, W, S><<<grid, blk, smem, s>>>(g, l, l0, lstep, mb, me, z);         \
     }                                                                                              \
   } while (0)
   if (seg == 4) {
@@ -905,6 +1222,8 @@ FastDev make_fastdev(Ctx &c, int nprob, const double *kx2_dev) {
   g.rhs = w.rhs[PL.ngrid - 1];
   g.phh = c.mgf_phh;
   g.phl = c.mgf_phl;
+  g.phh2 = c.mgf_phh2;
+  g.phl2 = c.mgf_phl2;
   g.bh = c.mgf_bh;
   g.bl = c.mgf_bl;
   g.cfh = c.mgf_cfh;
@@ -922,6 +1241,33 @@ FastDev make_fastdev(Ctx &c, int nprob, const double *kx2_dev) {
   return g;
 }
 
+// shared memory of k_f_vtail: at most this much.  Measured on the
+// 512 x 385 x 257 workload (levels 3x4 .. 257x385): the levels up to 17 x 25
+// in the tail (17 KB) beat up to 33 x 49 (62 KB) by 0.8 ms a step -- a level
+// of ~1,600 points is cheaper as batched launches than on one block's
+// thread chain, and the smaller blocks leave L1 to the coefficients.
+constexpr size_t kTailSmem = 24 * 1024;
+// the levels 1..ltop that k_f_vtail runs: the largest ltop below the finest
+// level whose arrays fit kTailSmem bytes (0: none fits, k_f_coarsest)
+int tail_level(const MgPlan &PL) {
+  int ltop = 0;
+  while (ltop + 1 < PL.ngrid && ltop + 1 <= kTailMax &&
+         make_tail_plan(PL, ltop + 1).total * sizeof(float) <= kTailSmem)
+    ++ltop;
+  return ltop;
+}
+
+void launch_resid_ff(const FastDev &g, bool update, unsigned pch, cudaStream_t s) {
+  const dim3 grid(pch, (unsigned)g.nfy), blk(32, kRY);
+  if (update) {
+    if (g.orth) k_f_resid_ff<true, true><<<grid, blk, 0, s>>>(g);
+    else k_f_resid_ff<true, false><<<grid, blk, 0, s>>>(g);
+  } else {
+    if (g.orth) k_f_resid_ff<false, true><<<grid, blk, 0, s>>>(g);
+    else k_f_resid_ff<false, false><<<grid, blk, 0, s>>>(g);
+  }
+}
+
 unsigned nb(long n, int bs) {
   long b = (n + bs - 1) / bs;
   if (b < 1) b = 1;
@@ -930,6 +1276,8 @@ unsigned nb(long n, int bs) {
 }
 
 }  // namespace
+
+int mgfast_tail_levels(const Ctx &c) { return c.mg.ngrid > 0 ? tail_level(c.mg) : 0; }
 
 // FP32 copies of the level coefficients and the FP32 work arrays.
 void mgfast_alloc(Ctx &c, int pmax) {
@@ -949,7 +1297,12 @@ void mgfast_alloc(Ctx &c, int pmax) {
   const size_t nph = (size_t)(PL.nfx + 2) * (PL.nfy + 2), nf = (size_t)PL.nfx * PL.nfy;
   tot += nph * pmax;
   const size_t ff_off = tot;
-  tot += 2 * nph * pmax + 2 * nf * pmax + 22 * nf;
+  tot += 4 * nph * pmax + 2 * nf * pmax + 22 * nf;
+  const int ltop = tail_level(PL);
+  const size_t nfac = ltop ? (size_t)make_tail_plan(PL, ltop).nfac * pmax : 0;
+  tot = (tot + 3) & ~(size_t)3;  // float4 reads of each problem's factor block
+  const size_t fac_off = tot;
+  tot += nfac;
   EK_CUDA(cudaMalloc(&c.mgf_pool, tot * sizeof(float)));
   c.mgf_levels.assign(PL.ngrid, {});
   for (int l = 0; l < PL.ngrid; ++l) {
@@ -966,10 +1319,17 @@ void mgfast_alloc(Ctx &c, int pmax) {
   c.mgf_scratch = c.mgf_pool + scr_off;
   c.mgf_phh = c.mgf_pool + ff_off;
   c.mgf_phl = c.mgf_phh + nph * pmax;
-  c.mgf_bh = c.mgf_phl + nph * pmax;
+  c.mgf_phh2 = c.mgf_phl + nph * pmax;
+  c.mgf_phl2 = c.mgf_phh2 + nph * pmax;
+  c.mgf_bh = c.mgf_phl2 + nph * pmax;
   c.mgf_bl = c.mgf_bh + nf * pmax;
   c.mgf_cfh = c.mgf_bl + nf * pmax;
   c.mgf_cfl = c.mgf_cfh + 11 * nf;
+  c.mgf_tailfac = nfac ? c.mgf_pool + fac_off : nullptr;
+  c.mgf_tailfac_n = nfac;
+  // every context's tail fits kTailSmem, so one process-wide limit serves all
+  // (set here, never during a stream capture)
+  EK_CUDA(cudaFuncSetAttribute(k_f_vtail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailSmem));
   {
     // the finest coefficients split into float-float pairs
     const std::vector<double> &cf = PL.cof_host[PL.ngrid - 1];
@@ -1020,6 +1380,11 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
     const size_t nph = (size_t)(PL.nfx + 2) * (PL.nfy + 2) * nprob;
     EK_CUDA(cudaMemsetAsync(g.phh, 0, sizeof(float) * nph, s));
     EK_CUDA(cudaMemsetAsync(g.phl, 0, sizeof(float) * nph, s));
+    EK_CUDA(cudaMemsetAsync(g.phh2, 0, sizeof(float) * nph, s));
+    EK_CUDA(cudaMemsetAsync(g.phl2, 0, sizeof(float) * nph, s));
+    // the finest correction: its ghost rows stay zero from here on, and each
+    // cycle's first sweep leaves its other values unread
+    EK_CUDA(cudaMemsetAsync(g.lv[PL.ngrid - 1].e, 0, sizeof(float) * nph, s));
     const size_t nf = (size_t)PL.nfx * PL.nfy * nprob;
     k_f_split<<<nb((long)nf, bs), bs, 0, s>>>(g.rhs, g.bh, g.bl, nf);
     after_launch(c);
@@ -1043,7 +1408,7 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
       EK_CUDA(cudaMalloc(&G.alpha, sizeof(float) * nprob));
       G.alpha_cap = nprob;
     }
-    k_f_resid_ff<<<dim3(pch, PL.nfy + 2), dim3(32, kRY), 0, s>>>(g);
+    launch_resid_ff(g, false, pch, s);
     after_launch(c);
     k_f_guess_rb<<<dim3(pch, PL.nfy), dim3(32, kRY), 0, s>>>(g);
     after_launch(c);
@@ -1054,13 +1419,13 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
   }
 
   // one partitioned line launch, in the layout tuned for (level, direction)
-  auto pline = [&](int l, bool xl, int l0, int lstep, int nline, int n) {
+  auto pline = [&](int l, bool xl, int l0, int lstep, int nline, int n, bool zero_e) {
     int lanes = default_lanes(n), seg = 8;
     const std::vector<int> &tl = xl ? PL.lanes_x : PL.lanes_y;
     const std::vector<int> &ts = xl ? PL.seg_x : PL.seg_y;
     if (l < (int)tl.size() && tl[l] > 0) lanes = tl[l];
     if (l < (int)ts.size() && ts[l] > 0) seg = ts[l];
-    launch_pline(g, l, xl, l0, lstep, nline, n, lanes, seg, s);
+    launch_pline(g, l, xl, l0, lstep, nline, n, lanes, seg, s, zero_e);
     after_launch(c);
   };
 
@@ -1070,7 +1435,12 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
   // sweep takes the colours in the reverse order.  (Post-smoothing with
   // x-lines only needs 8-9 corrections instead of 6-7 on the 256x257x193
   // grid, so it costs more than it saves.)
-  auto relax = [&](int l, bool post) {
+  // zero_first: e holds stale values that the cycle starts from zero
+  // (the finest level, whose e is not cleared between cycles): the first
+  // colour's y-lines take their neighbours as zero.  Needs odd nx (one
+  // phase per colour, and no line of the first colour reads a line of the
+  // same colour), which every level above the coarsest has.
+  auto relax = [&](int l, bool post, bool zero_first) {
     const MgLevel &L = PL.lv[l - 1];
     KScope ks(c, KC_MG_RELAX, 4.0 * nprob * L.nx * L.ny * 10);
     for (int k = 0; k < 2; ++k) {
@@ -1078,11 +1448,11 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
       LinePhase ph[2];
       const int nph = line_phases(L.nx, col, ph);
       for (int q = 0; q < nph; ++q)
-        if (ph[q].ncol > 0) pline(l, false, ph[q].i0, ph[q].istep, ph[q].ncol, L.ny);
+        if (ph[q].ncol > 0) pline(l, false, ph[q].i0, ph[q].istep, ph[q].ncol, L.ny, zero_first && k == 0);
     }
     for (int k = 0; k < 2; ++k) {
       const int col = post ? 2 - k : 1 + k;
-      pline(l, true, col, 2, (L.ny - col) / 2 + 1, L.nx);
+      pline(l, true, col, 2, (L.ny - col) / 2 + 1, L.nx, false);
     }
   };
 
@@ -1090,16 +1460,42 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
   // r = b - A phi and the per-problem decision (incr: count one more
   // correction); cond/use_cond: the while-node condition in a graph
   auto check = [&](int incr, cudaGraphConditionalHandle cond, int use_cond) {
-    KScope ks(c, KC_MG_CHECK, 4.0 * nprob * (4.0 * npt + 2.0 * (PL.nfx + 2) * (PL.nfy + 2)));
-    k_f_resid_ff<<<dim3(pch, PL.nfy + 2), dim3(32, kRY), 0, s>>>(g);
+    // bytes: b (2), r; phi (2), and with the update e and phi' (2)
+    KScope ks(c, KC_MG_CHECK, 4.0 * nprob * npt * (incr ? 8.0 : 5.0));
+    launch_resid_ff(g, incr != 0, pch, s);
     after_launch(c);
     k_f_check<<<1, 256, 0, s>>>(g, maxit, incr, cond, use_cond);
     after_launch(c);
   };
-  // one FP32 V(1,1) cycle on A e = r from e = 0, then phi += e
+  // the levels 1..ltop run as one k_f_vtail launch
+  const int ltop = tail_level(PL);
+  const TailPlan tplan = ltop ? make_tail_plan(PL, ltop) : TailPlan{};
+  const size_t tail_bytes = ltop ? tplan.total * sizeof(float) : 0;
+  if (ltop) {
+    if ((size_t)tplan.nfac * nprob > c.mgf_tailfac_n) throw CudaError("mixed solve: tail factor buffer too small");
+    KScope ks(c, KC_MG_SETUP, 4.0 * nprob * tplan.nfac);
+    k_f_tail_factors<<<(unsigned)nprob, kTailThreads, 0, s>>>(g, tplan, c.mgf_tailfac);
+    after_launch(c);
+  }
+  // one FP32 V(1,1) cycle on A e = r from e = 0 (phi += e follows in the
+  // next check's residual kernel).  The finest e is not cleared: the first
+  // sweep reads none of it (odd nx, the MUDPACK grids' rule), else it is
+  // cleared here.
+  const bool fine_zero = PL.ngrid >= 2 && PL.lv[PL.ngrid - 1].nx % 2 == 1;
   auto correction = [&]() {
+    if (!fine_zero) {
+      const size_t nph = (size_t)(PL.nfx + 2) * (PL.nfy + 2) * nprob;
+      EK_CUDA(cudaMemsetAsync(g.lv[PL.ngrid - 1].e, 0, sizeof(float) * nph, s));
+    }
     for (int l = PL.ngrid; l >= 1; --l) {
       const MgLevel &L = PL.lv[l - 1];
+      if (l == ltop) {
+        // bytes: level ltop's rhs in and its correction out
+        KScope ks(c, KC_MG_COARSE, 4.0 * nprob * (L.nx * L.ny + (L.nx + 2.0) * (L.ny + 2)));
+        k_f_vtail<<<(unsigned)nprob, kTailThreads, tail_bytes, s>>>(g, tplan, c.mgf_tailfac);
+        after_launch(c);
+        break;
+      }
       if (l == 1) {
         const int sweeps = std::max(8, (L.nx + L.ny) / 2);
         KScope ks(c, KC_MG_RELAX, 4.0 * nprob * L.nx * L.ny * 10 * sweeps);
@@ -1107,7 +1503,7 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
         after_launch(c);
         break;
       }
-      relax(l, false);
+      relax(l, false, l == PL.ngrid && fine_zero);
       const MgLevel &C = PL.lv[l - 2];
       KScope ks(c, KC_MG_TRANSFER, 4.0 * nprob * (4.0 * L.nx * L.ny + 2.0 * (C.nx + 2) * (C.ny + 2)));
       k_f_resid32<<<dim3(pch, L.ny), dim3(32, kRowWarps), 0, s>>>(g, l);
@@ -1115,7 +1511,7 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
       k_f_restrict<<<dim3(pch, C.ny + 2), dim3(32, kRowWarps), 0, s>>>(g, l);
       after_launch(c);
     }
-    for (int l = 2; l <= PL.ngrid; ++l) {
+    for (int l = std::max(2, ltop + 1); l <= PL.ngrid; ++l) {
       const MgLevel &L = PL.lv[l - 1];
       {
         KScope ks(c, KC_MG_TRANSFER, 4.0 * nprob * 4.0 * L.nx * L.ny);
@@ -1125,11 +1521,8 @@ int mgfast_solve(Ctx &c, int nprob, const double *kx2_dev, const double *kx2_hos
         k_f_prolong_y<<<dim3(pch, L.ny), dim3(32, kRowWarps), 0, s>>>(g, l);
         after_launch(c);
       }
-      relax(l, true);
+      relax(l, true, false);
     }
-    KScope ks(c, KC_MG_CHECK, 4.0 * nprob * npt * 5);
-    k_f_update_ff<<<dim3(pch, PL.nfy), dim3(32, kRY), 0, s>>>(g);
-    after_launch(c);
   };
   if (c.graph_slot < 0) {
     // eager: the host stops issuing cycles once the done flag it polls is set
@@ -1244,7 +1637,8 @@ int mgfast_autotune(Ctx &c, int reps, std::string &report) {
   report = "[";
   bool first = true;
   try {
-    for (int l = 2; l <= PL.ngrid; ++l) {
+    // the levels k_f_vtail runs have no line-solve launches to tune
+    for (int l = std::max(2, tail_level(PL) + 1); l <= PL.ngrid; ++l) {
       const MgLevel &L = PL.lv[l - 1];
       for (int dir = 0; dir < 2; ++dir) {
         const bool xl = dir == 1;

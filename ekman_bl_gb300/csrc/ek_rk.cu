@@ -87,14 +87,31 @@ __device__ __forceinline__ cplx_t pg_dot(const double *pg, size_t n2, int g0, si
 
 // The pressure-gradient weights and 1/J per cell, K = 1..NZ, J = 1..NY: the
 // metric combinations that the spectral right-hand side and the projection
-// would otherwise rebuild for every kx mode
+// would otherwise rebuild for every kx mode.  Planes 11 and 12 hold the
+// TH_BAR terms of the scalar right-hand side (duct.F90:589-618), which
+// depend on (K, J) only: the coefficient g of CU2 and the bracket that
+// KAPPA/4 multiplies, each evaluated in the order of the per-mode formula
+// it replaces, so the right-hand side is unchanged bit for bit.
+constexpr int kPgPlanes = 13;
 __global__ void k_metric_tables(Dims d, Metrics m) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
   const size_t n2 = (size_t)d.LDM * (d.NY + 3);
   if (k > d.NZ + 2 || j > d.NY + 2) return;
   const size_t mm = d.m2(k, j);
-  double w[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double w[kPgPlanes] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   if (k >= 1 && k <= d.NZ && j >= 1 && j <= d.NY) {
+    const double *TB = m.thbar;
+    auto tb = [&](int kk, int jj) { return TB[d.m2(kk, jj)]; };
+    w[11] = 0.5 * m.c12[d.m3(k + 1, j, 2)] * (tb(k, j) + tb(k + 1, j)) -
+            0.5 * m.c12[d.m3(k, j, 2)] * (tb(k, j) + tb(k - 1, j)) +
+            0.5 * m.c22[d.m3(k, j + 1, 1)] * (tb(k, j) + tb(k, j + 1)) -
+            0.5 * m.c22[d.m3(k, j, 1)] * (tb(k, j) + tb(k, j - 1));
+    w[12] = (+m.g12[d.m3(k + 1, j, 2)] * (tb(k + 1, j + 1) + tb(k, j + 1) - tb(k, j - 1) - tb(k + 1, j - 1)) -
+             m.g12[d.m3(k, j, 2)] * (tb(k - 1, j + 1) + tb(k, j + 1) - tb(k, j - 1) - tb(k - 1, j - 1)) +
+             m.g12[d.m3(k, j + 1, 1)] * (tb(k + 1, j + 1) + tb(k + 1, j) - tb(k - 1, j + 1) - tb(k - 1, j)) -
+             m.g12[d.m3(k, j, 1)] * (tb(k + 1, j) + tb(k + 1, j - 1) - tb(k - 1, j) - tb(k - 1, j - 1)) +
+             4.0 * (m.g11[d.m3(k + 1, j, 2)] * (tb(k + 1, j) - tb(k, j)) - m.g11[d.m3(k, j, 2)] * (tb(k, j) - tb(k - 1, j))) +
+             4.0 * (m.g22[d.m3(k, j + 1, 1)] * (tb(k, j + 1) - tb(k, j)) - m.g22[d.m3(k, j, 1)] * (tb(k, j) - tb(k, j - 1))));
     const double e = 0.5 * m.c12[d.m3(k + 1, j, 2)], f = 0.5 * m.c12[d.m3(k, j, 2)];
     const double g = 0.5 * m.c22[d.m3(k, j + 1, 1)], h = 0.5 * m.c22[d.m3(k, j, 1)];
     const double a = 0.5 * m.c11[d.m3(k + 1, j, 2)], b = 0.5 * m.c11[d.m3(k, j, 2)];
@@ -103,7 +120,7 @@ __global__ void k_metric_tables(Dims d, Metrics m) {
     w[5] = ((a - b) + c) - dd; w[6] = a; w[7] = -b; w[8] = c; w[9] = -dd;
     w[10] = 1.0 / m.jac[mm];
   }
-  for (int t = 0; t < 11; ++t) m.pg[t * n2 + mm] = w[t];
+  for (int t = 0; t < kPgPlanes; ++t) m.pg[t * n2 + mm] = w[t];
 }
 
 __global__ void k_spectral_rhs(SpecArgs a) {
@@ -181,25 +198,13 @@ __global__ void k_spectral_rhs(SpecArgs a) {
     if (a.cont_strat) {
       ft = cadd(ft, cscl(jac, a.CU2[q]));
     } else {
-      const double *TB = a.m.thbar;
-      auto tb = [&](int kk, int jj) { return TB[d.m2(kk, jj)]; };
-      const double g = 0.5 * a.m.c12[d.m3(k + 1, j, 2)] * (tb(k, j) + tb(k + 1, j)) -
-                       0.5 * a.m.c12[d.m3(k, j, 2)] * (tb(k, j) + tb(k - 1, j)) +
-                       0.5 * a.m.c22[d.m3(k, j + 1, 1)] * (tb(k, j) + tb(k, j + 1)) -
-                       0.5 * a.m.c22[d.m3(k, j, 1)] * (tb(k, j) + tb(k, j - 1));
-      ft = csub(ft, cscl(g, a.CU2[q]));
+      // the TH_BAR terms from their per-cell planes (k_metric_tables)
+      const size_t n2 = (size_t)d.LDM * (d.NY + 3), mm = d.m2(k, j);
+      ft = csub(ft, cscl(a.m.pg[11 * n2 + mm], a.CU2[q]));
       // with LES the coefficient is NU/PR + KAPPA_T at the physical point whose
       // x index is the mode index (duct.F90:610-618)
       const double kap = a.nut ? a.nupr + a.nut[d.ip(i, k, j)] / a.pr : a.nupr;
-      const double dd =
-          0.25 * kap *
-          (+a.m.g12[d.m3(k + 1, j, 2)] * (tb(k + 1, j + 1) + tb(k, j + 1) - tb(k, j - 1) - tb(k + 1, j - 1)) -
-           a.m.g12[d.m3(k, j, 2)] * (tb(k - 1, j + 1) + tb(k, j + 1) - tb(k, j - 1) - tb(k - 1, j - 1)) +
-           a.m.g12[d.m3(k, j + 1, 1)] * (tb(k + 1, j + 1) + tb(k + 1, j) - tb(k - 1, j + 1) - tb(k - 1, j)) -
-           a.m.g12[d.m3(k, j, 1)] * (tb(k + 1, j) + tb(k + 1, j - 1) - tb(k - 1, j) - tb(k - 1, j - 1)) +
-           4.0 * (a.m.g11[d.m3(k + 1, j, 2)] * (tb(k + 1, j) - tb(k, j)) - a.m.g11[d.m3(k, j, 2)] * (tb(k, j) - tb(k - 1, j))) +
-           4.0 * (a.m.g22[d.m3(k, j + 1, 1)] * (tb(k, j + 1) - tb(k, j)) - a.m.g22[d.m3(k, j, 1)] * (tb(k, j) - tb(k, j - 1))));
-      ft.re = ft.re + dd;
+      ft.re = ft.re + 0.25 * kap * a.m.pg[12 * n2 + mm];
     }
     FT = ft;
   }

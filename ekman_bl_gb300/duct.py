@@ -37,7 +37,7 @@ EXPORTS = [
     "ekgpu_unet_set_params", "ekgpu_unet_get_params", "ekgpu_unet_forward", "ekgpu_unet_set_tcgen05",
     "ekgpu_unet_train_step",
     "ekgpu_unet_gradient", "ekgpu_guess_geometry", "ekgpu_set_poisson_guess", "ekgpu_set_pair_sink",
-    "ekgpu_pair_count", "ekgpu_last_guess_stats", "ekgpu_mg_autotune", "ekgpu_mg_set_layout", "ekgpu_mg_levels",
+    "ekgpu_pair_count", "ekgpu_last_guess_stats", "ekgpu_mg_autotune", "ekgpu_mg_set_layout", "ekgpu_mg_levels", "ekgpu_mg_tail_levels",
     "ekgpu_les_metrics_from_grid", "ekgpu_set_les_metrics", "ekgpu_les_set_first_time", "ekgpu_les_get",
 ]
 
@@ -104,6 +104,7 @@ def load_library():
     L.ekgpu_mg_autotune.argtypes = [V, C.c_int, C.c_char_p, C.c_int]
     L.ekgpu_mg_set_layout.argtypes = [V, C.c_int, C.c_int, C.c_int, C.c_int]
     L.ekgpu_mg_levels.argtypes = [V, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]
+    L.ekgpu_mg_tail_levels.argtypes = [V, C.POINTER(C.c_int)]
     L.ekgpu_les_metrics_from_grid.argtypes = [P, _D, _D] + [_D] * 6
     L.ekgpu_set_les_metrics.argtypes = [V] + [_D] * 6
     L.ekgpu_les_set_first_time.argtypes = [V, C.c_int]
@@ -363,6 +364,13 @@ class DuctSolver:
         """Problems per block (8/16/32) and segment rows (4/8) of the line
         solves at one level and direction (0 y-lines, 1 x-lines); 0 = default."""
         self._check(self._L.ekgpu_mg_set_layout(self._h, level, direction, lanes, seg))
+
+    def mg_tail_levels(self) -> int:
+        """ltop: the mixed solver's coarse levels 1..ltop run as one launch per
+        cycle (no line-solve layouts to tune there); 0 = none."""
+        n = C.c_int()
+        self._check(self._L.ekgpu_mg_tail_levels(self._h, C.byref(n)))
+        return n.value
 
     def mg_levels(self):
         """[(nx, ny)] of the multigrid levels, coarsest first."""

@@ -319,6 +319,7 @@ int ekgpu_save_stats(ek_ctx *ctx, ek_stats *stats);
 
 /* ---- Tile-shape autotuner of the mixed solver's line solves ----------------
  * (No counterpart in the reference.)  For every multigrid level l = 2..ngrid
+ * above the coarse levels that run as one launch (ekgpu_mg_tail_levels)
  * and both line directions, time one zebra sweep in each valid layout -- 8,
  * 16 or 32 problems per block, line segments of 8 or 4 rows -- `reps` times
  * on the context's own work arrays, and use the fastest from then on.  Each
@@ -332,6 +333,11 @@ int ekgpu_mg_autotune(ek_ctx *ctx, int reps, char *report, int report_len);
 int ekgpu_mg_set_layout(ek_ctx *ctx, int level, int dir, int lanes, int seg);
 /* The multigrid levels: ngrid and the sizes nx[l-1] x ny[l-1], l = 1..ngrid. */
 int ekgpu_mg_levels(ek_ctx *ctx, int *ngrid, int *nx, int *ny, int cap);
+/* The mixed solver runs its coarse levels 1..ltop as one launch per cycle,
+ * each problem's levels in shared memory (ltop = 0: none).  Those levels have
+ * no line-solve launches, so the autotuner times levels max(2, ltop+1)..ngrid
+ * only and their layouts are not used. */
+int ekgpu_mg_tail_levels(ek_ctx *ctx, int *ltop);
 
 /* ---- Learned initial guess of the per-kx Poisson problems -------------------
  * (No counterpart in the reference: its solves always start from zero.)

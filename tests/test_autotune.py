@@ -71,7 +71,12 @@ def test_autotune_picks_valid_layouts_and_changes_nothing():
     a0 = g.download()
     rep = g.mg_autotune(reps=2)
     levels = g.mg_levels()
-    assert len(rep) == 2 * (len(levels) - 1)
+    # the coarse levels 1..ltop run as one launch per cycle, with no layouts
+    ltop = g.mg_tail_levels()
+    assert 1 <= ltop < len(levels)
+    first = max(2, ltop + 1)
+    assert len(rep) == 2 * (len(levels) - first + 1)
+    assert sorted({row["level"] for row in rep}) == list(range(first, len(levels) + 1))
     for row in rep:
         assert row["lanes"] in (8, 16, 32) and row["seg"] in (4, 8)
         assert f'{row["lanes"]}x{row["seg"]}' in row["us"]
