@@ -389,11 +389,12 @@ def run_ensemble(args, local):
     (NX in {64, 128, 256}, NY+2 and NZ+2 drawn from [64, 256] with a fixed
     seed and rounded up to MUDPACK form), each with its own parameters,
     metrics and state.  Times ENS_STEPS RK3 steps of every member with the
-    mixed-precision method: all members together (ekgpu_ensemble_step, one
-    stream and host thread per member), the same members one after another,
-    and the plain FP64 path's members together.  Member streams run
-    concurrently, so the times are host wall clock between device-wide
-    synchronisations."""
+    mixed-precision method: all members together (ekgpu_ensemble_step: each
+    ensemble step is one CUDA graph launch whose parallel branches are the
+    members' step graphs), the same members one after another (each with its
+    own step graph), and the plain FP64 path's members together (one stream
+    and host thread per member).  Members run concurrently, so the times are
+    host wall clock between device-wide synchronisations."""
     import torch
 
     from ekman_bl_gb300.duct import ensemble_step
@@ -439,8 +440,8 @@ def run_ensemble(args, local):
     rate = nm * ENS_STEPS / t_together
     return {"members": [w.name for _, w in ens], "drawn_ny2_nz2": [list(d) for d, _ in ens],
             "points_total": int(sum(pts)), "seed": 0,
-            "method": "mixed precision as the main line, default line-solve layouts, every member on its own "
-                      "stream and host thread (ekgpu_ensemble_step)",
+            "method": "mixed precision as the main line, default line-solve layouts; each ensemble step one CUDA "
+                      "graph launch with every member's step graph as a parallel branch (ekgpu_ensemble_step)",
             "value": round(rate, 3), "unit": "member RK3 steps/s", "steps_per_member": ENS_STEPS,
             "ms_per_ensemble_step": round(t_together * 1000.0 / ENS_STEPS, 3),
             "grid_point_steps_per_s": round(sum(pts) * ENS_STEPS / t_together, 1),
