@@ -240,50 +240,85 @@ int substep(Ctx &c, int rk) {
     b.j0 = d.JST; b.j1 = d.JET; b.k0 = d.ZST; b.k1 = d.ZET;
     b.scale2 = TEMP5; b.src = c.CRTH; b.src2 = c.CFTH; rdst(b, c.RTH);
     launch_c2r(c, b);
-    launch_adi(c, 0, rk);
-    launch_th_corners(c);
   }
-  launch_adi(c, 1, rk);
-  launch_adi(c, 2, rk);
-  launch_adi(c, 3, rk);
-  // COURANT_CURV_MPI (duct.F90:2417-2419): the new DELTA_T applies from the
-  // next substep; this one's projection keeps TEMP4
-  if (p.variable_dt && rk == 3 && p.update_dt > 0 && p.time_step % p.update_dt == 0) {
-    launch_courant(c);
-    double dt = 0.0;
-    EK_CUDA(cudaMemcpyAsync(&dt, c.cfl_dt, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-    EK_CUDA(cudaStreamSynchronize(c.stream));
-    if (dt > 0.0) {
-      const double nd = (dt >= p.delta_t_set) ? p.delta_t_set : dt;
-      if (nd != p.delta_t) set_delta_t(c, nd);
-    }
-  }
-  // back to Fourier space (duct.F90:2421-2451)
-  {
+  // back to Fourier space (duct.F90:2421-2451), one field
+  auto to_fourier = [&](int f) {
+    double *src = (f == 0) ? c.TH : (f == 1) ? c.U1 : (f == 2) ? c.U2 : c.U3;
+    const float *srcf = (f == 0) ? c.THf : (f == 1) ? c.U1f : (f == 2) ? c.U2f : c.U3f;
+    cplx_t *dst = (f == 0) ? c.CTH : (f == 1) ? c.CU1 : (f == 2) ? c.CU2 : c.CU3;
+    double *R = (f == 0) ? c.RTH : (f == 1) ? c.R1 : (f == 2) ? c.R2 : c.R3;
     R2cArgs a{};
     a.j0 = 0; a.j1 = d.NY + 1; a.k0 = 0; a.k1 = d.NZ + 1;
     a.pro = PRO_LOAD; a.epi = EPI_STORE;
-    auto to_fourier = [&](double *src, const float *srcf, cplx_t *dst, double *R) {
-      if (inc) {
-        // CU += the FP32 transform of the ADI's total increment
-        a.lowp = 1;
-        a.epi = EPI_ADD;
-        a.zero_hi = 1;
-        a.a = nullptr;
-        a.af = inc_plane(c, R);
-        a.alo = nullptr;
-      } else {
-        a.a = ffp ? nullptr : src;
-        a.af = ffp ? srcf : nullptr;
-        a.alo = ffp ? ff_lo(src) : nullptr;
+    if (inc) {
+      // CU += the FP32 transform of the ADI's total increment
+      a.lowp = 1;
+      a.epi = EPI_ADD;
+      a.zero_hi = 1;
+      a.a = nullptr;
+      a.af = inc_plane(c, R);
+      a.alo = nullptr;
+    } else {
+      a.a = ffp ? nullptr : src;
+      a.af = ffp ? srcf : nullptr;
+      a.alo = ffp ? ff_lo(src) : nullptr;
+    }
+    a.dst = dst;
+    launch_r2c(c, a);
+  };
+  // COURANT_CURV_MPI (duct.F90:2417-2419) reads every field after its ADI
+  const bool courant = p.variable_dt && rk == 3 && p.update_dt > 0 && p.time_step % p.update_dt == 0;
+  // In the increment form each field's ADI (with TH's corner copies) and
+  // its forward transform run on a stream of their own, forked from and
+  // joined back to the step's stream: the fields share no array there, and
+  // their line solves are latency-bound, so the four fill each other's idle
+  // issue slots.  (Not under the per-kernel timer, whose events need one
+  // stream, nor when COURANT_CURV_MPI sits between the ADI and the
+  // transforms.)
+  const bool fork = inc && !c.timing && !courant;
+  const int f0 = th ? 0 : 1;
+  if (fork) {
+    const cudaStream_t main = c.stream;
+    EK_CUDA(cudaEventRecord(c.field_ev[4], main));
+    try {
+      for (int f = f0; f < 4; ++f) {
+        EK_CUDA(cudaStreamWaitEvent(c.field_stream[f], c.field_ev[4], 0));
+        c.stream = c.field_stream[f];
+        launch_adi(c, f, rk);
+        if (f == 0) launch_th_corners(c);
+        to_fourier(f);
+        EK_CUDA(cudaEventRecord(c.field_ev[f], c.stream));
+        c.stream = main;
       }
-      a.dst = dst;
-      launch_r2c(c, a);
-    };
-    to_fourier(c.U1, c.U1f, c.CU1, c.R1);
-    to_fourier(c.U2, c.U2f, c.CU2, c.R2);
-    to_fourier(c.U3, c.U3f, c.CU3, c.R3);
-    if (th) to_fourier(c.TH, c.THf, c.CTH, c.RTH);
+    } catch (...) {
+      c.stream = main;
+      throw;
+    }
+    for (int f = f0; f < 4; ++f) EK_CUDA(cudaStreamWaitEvent(main, c.field_ev[f], 0));
+  } else {
+    if (th) {
+      launch_adi(c, 0, rk);
+      launch_th_corners(c);
+    }
+    launch_adi(c, 1, rk);
+    launch_adi(c, 2, rk);
+    launch_adi(c, 3, rk);
+    // the new DELTA_T applies from the next substep; this one's projection
+    // keeps TEMP4
+    if (courant) {
+      launch_courant(c);
+      double dt = 0.0;
+      EK_CUDA(cudaMemcpyAsync(&dt, c.cfl_dt, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+      EK_CUDA(cudaStreamSynchronize(c.stream));
+      if (dt > 0.0) {
+        const double nd = (dt >= p.delta_t_set) ? p.delta_t_set : dt;
+        if (nd != p.delta_t) set_delta_t(c, nd);
+      }
+    }
+    to_fourier(1);
+    to_fourier(2);
+    to_fourier(3);
+    if (th) to_fourier(0);
   }
   int mg = EK_OK;
   run_rem_div(c, TEMP4, true, &mg);
@@ -653,6 +688,8 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
     c.stream = c.own_stream;
     EK_CUDA(cudaStreamCreateWithFlags(&c.cap_stream, cudaStreamNonBlocking));
     EK_CUDA(cudaStreamCreateWithFlags(&c.cap_stream2, cudaStreamNonBlocking));
+    for (int f = 0; f < 4; ++f) EK_CUDA(cudaStreamCreateWithFlags(&c.field_stream[f], cudaStreamNonBlocking));
+    for (int f = 0; f < 5; ++f) EK_CUDA(cudaEventCreateWithFlags(&c.field_ev[f], cudaEventDisableTiming));
     EK_CUDA(cudaHostAlloc(&c.step_stats_host, 3 * sizeof(StepStats), cudaHostAllocDefault));
     step_graphs_clear(c);  // a fresh epoch
     rk_init_attributes();
@@ -771,6 +808,10 @@ void ekgpu_destroy(ek_ctx *h) {
   step_graphs_clear(c);
   if (c.cap_stream) cudaStreamDestroy(c.cap_stream);
   if (c.cap_stream2) cudaStreamDestroy(c.cap_stream2);
+  for (int f = 0; f < 4; ++f)
+    if (c.field_stream[f]) cudaStreamDestroy(c.field_stream[f]);
+  for (int f = 0; f < 5; ++f)
+    if (c.field_ev[f]) cudaEventDestroy(c.field_ev[f]);
   if (c.step_stats_host) cudaFreeHost(c.step_stats_host);
   for (auto &r : c.trec) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : c.evpool) cudaEventDestroy(e);

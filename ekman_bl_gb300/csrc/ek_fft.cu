@@ -467,13 +467,25 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
 }
 
 // Launch a transform.  The register form of the FFT pays in the FP32
-// inverse transform (measured on 512 x 385 x 257: 0.34 -> 0.23 ms per
-// launch); in the forward transforms, whose stencil prologues want many
-// warps in flight, and in the FP64 and float-float ones, its extra registers
-// cost more than the shared-memory passes it saves, so they keep the loop.
+// transforms (measured on 512 x 385 x 257: the inverse 0.34 -> 0.23 ms per
+// launch; the forward ones, since each launch fuses a component's product
+// and flux transforms, 13.9 -> 11.7 ms a step); in the FP64 and float-float
+// ones its extra registers cost more than the shared-memory passes it
+// saves, so they keep the loop.
 template <typename T>
 void run_r2c(dim3 grid, size_t smem, cudaStream_t s, const FftConst &fc, const R2cArgs &a) {
-  k_r2c<T, 0><<<grid, 32 * kWarpsPerBlock, smem, s>>>(fc, a);
+  const unsigned nt = 32 * kWarpsPerBlock;
+  if constexpr (std::is_same_v<T, float>) {
+    switch (fc.M) {
+      case 32: k_r2c<T, 1><<<grid, nt, smem, s>>>(fc, a); return;
+      case 64: k_r2c<T, 2><<<grid, nt, smem, s>>>(fc, a); return;
+      case 128: k_r2c<T, 4><<<grid, nt, smem, s>>>(fc, a); return;
+      case 256: k_r2c<T, 8><<<grid, nt, smem, s>>>(fc, a); return;
+      case 512: k_r2c<T, 16><<<grid, nt, smem, s>>>(fc, a); return;
+      default: break;
+    }
+  }
+  k_r2c<T, 0><<<grid, nt, smem, s>>>(fc, a);
 }
 template <typename T>
 void run_c2r(dim3 grid, size_t smem, cudaStream_t s, const FftConst &fc, const C2rArgs &a) {
@@ -497,6 +509,11 @@ void smem_attributes() {
   EK_CUDA(cudaFuncSetAttribute(k_c2r<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
   if constexpr (std::is_same_v<T, float>) {
     EK_CUDA(cudaFuncSetAttribute(k_c2r<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    EK_CUDA(cudaFuncSetAttribute(k_r2c<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    EK_CUDA(cudaFuncSetAttribute(k_r2c<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    EK_CUDA(cudaFuncSetAttribute(k_r2c<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    EK_CUDA(cudaFuncSetAttribute(k_r2c<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    EK_CUDA(cudaFuncSetAttribute(k_r2c<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
     EK_CUDA(cudaFuncSetAttribute(k_c2r<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
     EK_CUDA(cudaFuncSetAttribute(k_c2r<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
     EK_CUDA(cudaFuncSetAttribute(k_c2r<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));

@@ -341,6 +341,15 @@ struct Ctx {
   double *adi_les_tab = nullptr;  // LES ADI: per-cell row weights of the two sweeps (k_adi_les_tab)
   float2 *adi_ff_tab = nullptr;   // LES ADI, float-float: both sweeps' weights as float pairs
   float2 *adi_tab2 = nullptr;     // the weights of adi_tab as float pairs (float-float fields)
+  // the increment-form ADI of the four fields runs on four concurrent
+  // streams (forked from and joined to the step's stream): each field's own
+  // sweep weights and scratch (the y sweep's increment and the copy rows'
+  // brackets), allocated in an eager step
+  double *adi_tab_f[4] = {nullptr, nullptr, nullptr, nullptr};
+  float2 *adi_tab2_f[4] = {nullptr, nullptr, nullptr, nullptr};
+  float *inc_scr[4] = {nullptr, nullptr, nullptr, nullptr};  // 2 x nphys floats each
+  cudaStream_t field_stream[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t field_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   // divergence check
   double *div_part = nullptr;
   double last_div = 0.0;

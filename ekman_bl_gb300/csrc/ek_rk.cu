@@ -1221,6 +1221,26 @@ __global__ void k_div_check(Dims d, const double *kx, const double *jacm, const 
   CS[q] = v;
 }
 
+// The same sums from the FP32 plane of the mixed path's FP32 transform (its
+// values are exactly the FP32 results the FP64 plane would hold widened):
+// each thread accumulates in float-float on the FP32 pipe, then the block
+// reduces in FP64 as above.  GB300's FP64 pipe made the FP64 sums of 50 M
+// values a 0.3 ms kernel.
+__global__ void k_div_sum_f(Dims d, const float *S, double *part) {
+  const int j = 2 + blockIdx.x;
+  __shared__ double red[256];
+  FF s(0.0f, 0.0f);
+  for (int k = 2; k <= d.NZ - 1; ++k)
+    for (int i = 1 + threadIdx.x; i <= d.NX + 1; i += blockDim.x) s = s + FF(fabsf(S[d.ip(i, k, j)]), 0.0f);
+  red[threadIdx.x] = (double)s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
 // Sum of |div| over I = 1..NXP, K = 2..NZ-1 per line J (duct.F90:2790-2798);
 // one block per J, fixed summation order.
 __global__ void k_div_sum(Dims d, const double *S, double *part) {
@@ -1395,18 +1415,33 @@ void launch_adi(Ctx &c, int field, int rk) {
     EK_CUDA(cudaMalloc(&c.adi_tab, sizeof(double) * 8 * n2));
     c.allocs.push_back(c.adi_tab);
   }
-  a.tab = c.adi_tab;
   const bool ffp = ff_fields(c), inc = inc_fields(c);
   if ((ffp || inc) && !c.adi_tab2) {
     EK_CUDA(cudaMalloc(&c.adi_tab2, sizeof(float2) * 8 * n2));
     c.allocs.push_back(c.adi_tab2);
   }
+  // the increment form keeps each field's weights and scratch apart, so the
+  // four fields' sweeps may run concurrently
+  if (inc && !c.adi_tab_f[field]) {
+    EK_CUDA(cudaMalloc(&c.adi_tab_f[field], sizeof(double) * 8 * n2));
+    c.allocs.push_back(c.adi_tab_f[field]);
+    EK_CUDA(cudaMalloc(&c.adi_tab2_f[field], sizeof(float2) * 8 * n2));
+    c.allocs.push_back(c.adi_tab2_f[field]);
+    if (field == 0) {
+      c.inc_scr[0] = ff_lo(c.PHS);
+    } else {
+      EK_CUDA(cudaMalloc(&c.inc_scr[field], sizeof(float) * 2 * d.nphys()));
+      c.allocs.push_back(c.inc_scr[field]);
+    }
+  }
+  double *tab = inc ? c.adi_tab_f[field] : c.adi_tab;
+  float2 *tab2 = inc ? c.adi_tab2_f[field] : c.adi_tab2;
+  a.tab = tab;
   {
     const dim3 tg((unsigned)((d.NZ + 2 + 63) / 64), (unsigned)(d.NY + 2));
-    k_adi_tab<false><<<tg, 64, 0, c.stream>>>(d, c.m, coef, sform, c.adi_tab, (ffp || inc) ? c.adi_tab2 : nullptr);
+    k_adi_tab<false><<<tg, 64, 0, c.stream>>>(d, c.m, coef, sform, tab, (ffp || inc) ? tab2 : nullptr);
     after_launch(c);
-    k_adi_tab<true><<<tg, 64, 0, c.stream>>>(d, c.m, coef, sform, c.adi_tab + 4 * n2,
-                                               (ffp || inc) ? c.adi_tab2 + 4 * n2 : nullptr);
+    k_adi_tab<true><<<tg, 64, 0, c.stream>>>(d, c.m, coef, sform, tab + 4 * n2, (ffp || inc) ? tab2 + 4 * n2 : nullptr);
     after_launch(c);
   }
   if (les_active(c)) {
@@ -1480,8 +1515,8 @@ void launch_adi(Ctx &c, int field, int rk) {
   if (inc) {
     float *phf = (field == 0) ? c.THf : (field == 1) ? c.U1f : (field == 2) ? c.U2f : c.U3f;
     const cplx_t *cu = (field == 0) ? c.CTH : (field == 1) ? c.CU1 : (field == 2) ? c.CU2 : c.CU3;
-    float *dstar = ff_lo(c.PHS);
-    float *brk = ff_lo(c.PHS) + d.nphys();
+    float *dstar = c.inc_scr[field];
+    float *brk = c.inc_scr[field] + d.nphys();
     // copy rows: the FP32 transform of CU(src) - CU(row) on their lines
     auto brackets = [&](const BcSet &bs, int dir) {
       for (int b = 0; b < bs.n; ++b) {
@@ -1512,7 +1547,7 @@ void launch_adi(Ctx &c, int field, int rk) {
     a.dsf = dstar;
     a.brk = brk;
     a.incf = dstar;
-    a.tab2 = c.adi_tab2;
+    a.tab2 = tab2;
     a.fa2 = c.adi[field][rk][0].a2;
     a.fib2 = c.adi[field][rk][0].ib2;
     a.fu2 = c.adi[field][rk][0].u2;
@@ -1663,11 +1698,17 @@ void launch_projection(Ctx &c, const double *phif, int P, double temp4, bool upd
   ca.k0 = 2;
   ca.k1 = d.NZ - 1;
   // the check's transform is linear in the (small) divergence itself: on the
-  // mixed path FP32 arithmetic keeps it to ~1e-7 relative, widened exactly
-  ca.lowp = explicit_increment_form(c) ? 1 : 0;
+  // mixed path FP32 arithmetic keeps it to ~1e-7 relative, into an FP32 plane
+  const bool lp = explicit_increment_form(c);
+  ca.lowp = lp ? 1 : 0;
+  if (lp) {
+    ca.dst = nullptr;
+    ca.dstf = reinterpret_cast<float *>(c.SPH);
+  }
   launch_c2r(c, ca);
-  KScope ks(c, KC_DIVERGENCE, 8.0 * (d.NX + 2) * (d.NZ - 2) * (d.NY - 2));
-  k_div_sum<<<d.NY - 2, 256, 0, c.stream>>>(d, c.SPH, c.div_part);
+  KScope ks(c, KC_DIVERGENCE, (lp ? 4.0 : 8.0) * (d.NX + 2) * (d.NZ - 2) * (d.NY - 2));
+  if (lp) k_div_sum_f<<<d.NY - 2, 256, 0, c.stream>>>(d, reinterpret_cast<const float *>(c.SPH), c.div_part);
+  else k_div_sum<<<d.NY - 2, 256, 0, c.stream>>>(d, c.SPH, c.div_part);
   after_launch(c);
 }
 
