@@ -182,29 +182,27 @@ int substep(Ctx &c, int rk) {
   const bool les = les_active(c);
   if (les) launch_les(c, rk);
   launch_face_velocity(c);
-  // nonlinear and cross-diffusion terms, fused with their forward FFTs
-  // (duct.F90:683-1121)
-  {
+  // nonlinear and cross-diffusion terms of velocity component f (0..2),
+  // fused with their forward FFTs (duct.F90:683-1121)
+  auto nl_velocity = [&](int f) {
     R2cArgs a{};
     a.j0 = d.JS; a.j1 = d.JE; a.k0 = d.ZS; a.k1 = d.ZE;
     const double *uu[3] = {c.U1, c.U2, c.U3};
     const float *uf[3] = {c.U1f, c.U2f, c.U3f};
     cplx_t *cf[3] = {c.CF1, c.CF2, c.CF3};
     a.lowp = 1;
-    // each component's product and flux terms in one launch
+    // the component's product and flux terms in one launch
     a.fuse_flux = 1;
-    for (int f = 0; f < 3; ++f) {
-      a.pro = PRO_PROD; a.a = c.U1; a.b = uu[f]; a.epi = EPI_SUB_IK; a.dst = cf[f];
-      a.af = f32 ? c.U1f : nullptr; a.bf = f32 ? uf[f] : nullptr;
-      a.extra = les ? c.les.t[f] : nullptr;  // + J tau_1f
-      a.extraf = les ? c.les.tf[f] : nullptr;
-      a.a2 = uu[f]; a.b2 = c.U2b; a.visc2 = p.nu;
-      a.a2f = f32 ? uf[f] : nullptr; a.b2f = f32 ? c.U2bf : nullptr;
-      a.extra2 = les ? c.les.ext[f] : nullptr;  // + NU_T cross term - stress divergence
-      a.extraf2 = les ? c.les.extf[f] : nullptr;
-      launch_r2c(c, a);
-    }
-  }
+    a.pro = PRO_PROD; a.a = c.U1; a.b = uu[f]; a.epi = EPI_SUB_IK; a.dst = cf[f];
+    a.af = f32 ? c.U1f : nullptr; a.bf = f32 ? uf[f] : nullptr;
+    a.extra = les ? c.les.t[f] : nullptr;  // + J tau_1f
+    a.extraf = les ? c.les.tf[f] : nullptr;
+    a.a2 = uu[f]; a.b2 = c.U2b; a.visc2 = p.nu;
+    a.a2f = f32 ? uf[f] : nullptr; a.b2f = f32 ? c.U2bf : nullptr;
+    a.extra2 = les ? c.les.ext[f] : nullptr;  // + NU_T cross term - stress divergence
+    a.extraf2 = les ? c.les.extf[f] : nullptr;
+    launch_r2c(c, a);
+  };
   // R = c2r(CR + beta h CF) (duct.F90:1127-1161); in the explicit-increment
   // form S = R - J phi_old, in FP32, into R's slots
   const bool sform = explicit_increment_form(c);
@@ -213,16 +211,16 @@ int substep(Ctx &c, int rk) {
     a.dstf = sform ? reinterpret_cast<float *>(r) : nullptr;
     a.lowp = sform ? 1 : 0;
   };
-  {
+  auto r_velocity = [&](int f) {
+    const cplx_t *cr[3] = {c.CR1, c.CR2, c.CR3}, *cf[3] = {c.CF1, c.CF2, c.CF3};
+    double *rr[3] = {c.R1, c.R2, c.R3};
     C2rArgs a{};
     a.j0 = d.JS; a.j1 = d.JE; a.k0 = d.ZS; a.k1 = d.ZE;
     a.scale2 = TEMP5;
-    a.src = c.CR1; a.src2 = c.CF1; rdst(a, c.R1); launch_c2r(c, a);
-    a.src = c.CR2; a.src2 = c.CF2; rdst(a, c.R2); launch_c2r(c, a);
-    a.src = c.CR3; a.src2 = c.CF3; rdst(a, c.R3); launch_c2r(c, a);
-  }
-  if (th) {
-    // scalar nonlinear terms (duct.F90:1165-1252) and RTH (1304-1326)
+    a.src = cr[f]; a.src2 = cf[f]; rdst(a, rr[f]); launch_c2r(c, a);
+  };
+  // scalar nonlinear terms (duct.F90:1165-1252) and RTH (1304-1326)
+  auto th_explicit = [&]() {
     R2cArgs a{};
     a.j0 = d.JST; a.j1 = d.JET; a.k0 = d.ZST; a.k1 = d.ZET;
     a.lowp = 1;
@@ -240,7 +238,7 @@ int substep(Ctx &c, int rk) {
     b.j0 = d.JST; b.j1 = d.JET; b.k0 = d.ZST; b.k1 = d.ZET;
     b.scale2 = TEMP5; b.src = c.CRTH; b.src2 = c.CFTH; rdst(b, c.RTH);
     launch_c2r(c, b);
-  }
+  };
   // back to Fourier space (duct.F90:2421-2451), one field
   auto to_fourier = [&](int f) {
     double *src = (f == 0) ? c.TH : (f == 1) ? c.U1 : (f == 2) ? c.U2 : c.U3;
@@ -268,13 +266,14 @@ int substep(Ctx &c, int rk) {
   };
   // COURANT_CURV_MPI (duct.F90:2417-2419) reads every field after its ADI
   const bool courant = p.variable_dt && rk == 3 && p.update_dt > 0 && p.time_step % p.update_dt == 0;
-  // In the increment form each field's ADI (with TH's corner copies) and
-  // its forward transform run on a stream of their own, forked from and
-  // joined back to the step's stream: the fields share no array there, and
-  // their line solves are latency-bound, so the four fill each other's idle
-  // issue slots.  (Not under the per-kernel timer, whose events need one
-  // stream, nor when COURANT_CURV_MPI sits between the ADI and the
-  // transforms.)
+  // In the increment form each field's chain -- its explicit terms, ADI
+  // (with TH's corner copies) and forward transform -- runs on a stream of
+  // its own, forked from and joined back to the step's stream: the chains
+  // share no array (every one reads the FP32 physical fields and face
+  // velocities, none writes them), and the transforms of one fill the
+  // latency-bound line solves of another.  (Not under the per-kernel timer,
+  // whose events need one stream, nor when COURANT_CURV_MPI sits between the
+  // ADI and the transforms.)
   const bool fork = inc && !c.timing && !courant;
   const int f0 = th ? 0 : 1;
   if (fork) {
@@ -284,6 +283,11 @@ int substep(Ctx &c, int rk) {
       for (int f = f0; f < 4; ++f) {
         EK_CUDA(cudaStreamWaitEvent(c.field_stream[f], c.field_ev[4], 0));
         c.stream = c.field_stream[f];
+        if (f == 0) th_explicit();
+        else {
+          nl_velocity(f - 1);
+          r_velocity(f - 1);
+        }
         launch_adi(c, f, rk);
         if (f == 0) launch_th_corners(c);
         to_fourier(f);
@@ -296,7 +300,10 @@ int substep(Ctx &c, int rk) {
     }
     for (int f = f0; f < 4; ++f) EK_CUDA(cudaStreamWaitEvent(main, c.field_ev[f], 0));
   } else {
+    for (int f = 0; f < 3; ++f) nl_velocity(f);
+    for (int f = 0; f < 3; ++f) r_velocity(f);
     if (th) {
+      th_explicit();
       launch_adi(c, 0, rk);
       launch_th_corners(c);
     }
