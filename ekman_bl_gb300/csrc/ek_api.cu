@@ -151,7 +151,6 @@ int substep(Ctx &c, int rk) {
   const bool th = p.n_th > 0;
   const double TEMP4 = c.H_BAR[rk];
   const double TEMP5 = c.BETA_BAR[rk] * c.H_BAR[rk];
-  launch_spectral_rhs(c, rk);
   // FP32 copies of the physical fields for the nonlinear terms (fft_fp32)
   const bool f32 = p.fft_fp32 != 0;
   // float-float physical fields: the FP32 copy is the high part, the low
@@ -160,6 +159,7 @@ int substep(Ctx &c, int rk) {
   // increment form: the state's inverse transforms are FP32, into the FP32
   // copies only
   const bool inc = inc_fields(c);
+  launch_spectral_rhs(c, rk);
   // to physical space (duct.F90:656-673)
   {
     C2rArgs a{};
@@ -276,6 +276,9 @@ int substep(Ctx &c, int rk) {
   // ADI and the transforms.)
   const bool fork = inc && !c.timing && !courant;
   const int f0 = th ? 0 : 1;
+  // the previous substep's divergence check reads CU1 and the face
+  // velocities, which the chains below and the projection write
+  div_join(c);
   if (fork) {
     const cudaStream_t main = c.stream;
     EK_CUDA(cudaEventRecord(c.field_ev[4], main));
@@ -374,10 +377,12 @@ void capture_substeps(Ctx &c, cudaStream_t s, StepGraph &sg) {
       sg.body_launches[rk - 1] = c.graph_body_launches;
       body += c.graph_body_launches;
     }
+    div_join(c);  // the last substep's check ends inside the graph
   } catch (...) {
     c.graph_slot = -1;
     c.stream = saved;
     c.launches = l0;
+    c.div_pending = false;
     throw;
   }
   c.graph_slot = -1;
@@ -697,6 +702,8 @@ int ekgpu_create(const ek_params *pp, ek_ctx **out) {
     EK_CUDA(cudaStreamCreateWithFlags(&c.cap_stream2, cudaStreamNonBlocking));
     for (int f = 0; f < 4; ++f) EK_CUDA(cudaStreamCreateWithFlags(&c.field_stream[f], cudaStreamNonBlocking));
     for (int f = 0; f < 5; ++f) EK_CUDA(cudaEventCreateWithFlags(&c.field_ev[f], cudaEventDisableTiming));
+    EK_CUDA(cudaStreamCreateWithFlags(&c.div_stream, cudaStreamNonBlocking));
+    for (int f = 0; f < 2; ++f) EK_CUDA(cudaEventCreateWithFlags(&c.div_ev[f], cudaEventDisableTiming));
     EK_CUDA(cudaHostAlloc(&c.step_stats_host, 3 * sizeof(StepStats), cudaHostAllocDefault));
     step_graphs_clear(c);  // a fresh epoch
     rk_init_attributes();
@@ -819,6 +826,9 @@ void ekgpu_destroy(ek_ctx *h) {
     if (c.field_stream[f]) cudaStreamDestroy(c.field_stream[f]);
   for (int f = 0; f < 5; ++f)
     if (c.field_ev[f]) cudaEventDestroy(c.field_ev[f]);
+  if (c.div_stream) cudaStreamDestroy(c.div_stream);
+  for (int f = 0; f < 2; ++f)
+    if (c.div_ev[f]) cudaEventDestroy(c.div_ev[f]);
   if (c.step_stats_host) cudaFreeHost(c.step_stats_host);
   for (auto &r : c.trec) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : c.evpool) cudaEventDestroy(e);

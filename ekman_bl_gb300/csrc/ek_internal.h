@@ -350,6 +350,12 @@ struct Ctx {
   float *inc_scr[4] = {nullptr, nullptr, nullptr, nullptr};  // 2 x nphys floats each
   cudaStream_t field_stream[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t field_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  // a captured step runs each substep's divergence check on a side stream
+  // (div_ev[0] forks it, div_ev[1] marks its end); div_pending: a check is
+  // in flight that the work writing CU1 or the face velocities must wait for
+  cudaStream_t div_stream = nullptr;
+  cudaEvent_t div_ev[2] = {nullptr, nullptr};
+  bool div_pending = false;
   // divergence check
   double *div_part = nullptr;
   double last_div = 0.0;
@@ -405,6 +411,11 @@ struct KScope {
   }
 };
 void timing_resolve(Ctx &c);
+// a captured step's divergence check in flight on the side stream: make the
+// step's stream wait for it
+void div_join(Ctx &c);
+// a captured step's mean |div| into its statistics slot (on c.stream)
+void div_final(Ctx &c);
 
 // ---- host helpers (ek_host.cpp) ----
 int metrics_from_grid_host(const ek_params *p, const double *xpoint, const double *ypoint, double *int_jacob,

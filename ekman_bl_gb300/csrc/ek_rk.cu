@@ -1674,6 +1674,7 @@ void launch_divergence_rhs(Ctx &c, double *rhs, int P) {
 
 void launch_projection(Ctx &c, const double *phif, int P, double temp4, bool update_p) {
   const Dims &d = c.d;
+  const bool side = c.graph_slot >= 0 && !c.timing;
   const Dims ds = spec_dims(c);
   const double fm = (ds.NX2P + 1.0) / d.LDC;
   dim3 g0((ds.NX2P + 1 + 63) / 64, d.NZ2, d.NY2);
@@ -1687,8 +1688,21 @@ void launch_projection(Ctx &c, const double *phif, int P, double temp4, bool upd
   after_launch(c);
   k_correct_cells<<<g1, 64, 0, c.stream>>>(ds, c.m, c.kx, c.CR1, c.CU1, c.CU2, c.CU3);
   after_launch(c);
-  k_div_check<<<g0, 64, 0, c.stream>>>(ds, c.kx, c.m.jac, c.CU1, c.CU2b, c.CS);
-  after_launch(c);
+  if (!side) {
+    k_div_check<<<g0, 64, 0, c.stream>>>(ds, c.kx, c.m.jac, c.CU1, c.CU2b, c.CS);
+    after_launch(c);
+  }
+  }
+  const cudaStream_t main = c.stream;
+  if (side) {
+    // a captured step checks the divergence on the side stream, alongside
+    // the next substep's right-hand side and transforms; the work that next
+    // writes CU1 or the face velocities waits for it (div_join)
+    EK_CUDA(cudaEventRecord(c.div_ev[0], main));
+    EK_CUDA(cudaStreamWaitEvent(c.div_stream, c.div_ev[0], 0));
+    c.stream = c.div_stream;
+    k_div_check<<<g0, 64, 0, c.stream>>>(ds, c.kx, c.m.jac, c.CU1, c.CU2b, c.CS);
+    after_launch(c);
   }
   C2rArgs ca{};
   ca.src = c.CS;
@@ -1710,6 +1724,12 @@ void launch_projection(Ctx &c, const double *phif, int P, double temp4, bool upd
   if (lp) k_div_sum_f<<<d.NY - 2, 256, 0, c.stream>>>(d, reinterpret_cast<const float *>(c.SPH), c.div_part);
   else k_div_sum<<<d.NY - 2, 256, 0, c.stream>>>(d, c.SPH, c.div_part);
   after_launch(c);
+  if (side) {
+    div_final(c);
+    EK_CUDA(cudaEventRecord(c.div_ev[1], c.stream));
+    c.stream = main;
+    c.div_pending = true;
+  }
 }
 
 // Mean |div| from the per-line partial sums, in J order (duct.F90:2800).
@@ -1724,13 +1744,26 @@ __global__ void k_div_final(const double *part, int n, double scale_den, double 
 }
 }  // namespace
 
+// a captured step's mean |div| into its statistics slot
+void div_final(Ctx &c) {
+  const Dims &d = c.d;
+  k_div_final<<<1, 32, 0, c.stream>>>(c.div_part, d.NY - 2, (double)(d.NX + 1) * (double)d.NY * (double)d.NZ,
+                                       &c.step_stats_dev[c.graph_slot].div);
+  after_launch(c);
+}
+
+void div_join(Ctx &c) {
+  if (!c.div_pending) return;
+  EK_CUDA(cudaStreamWaitEvent(c.stream, c.div_ev[1], 0));
+  c.div_pending = false;
+}
+
 int finish_divergence(Ctx &c, double *div_out) {
   const Dims &d = c.d;
   if (c.graph_slot >= 0) {
-    // a captured step reads the value after the step
-    k_div_final<<<1, 32, 0, c.stream>>>(c.div_part, d.NY - 2, (double)(d.NX + 1) * (double)d.NY * (double)d.NZ,
-                                         &c.step_stats_dev[c.graph_slot].div);
-    after_launch(c);
+    // a captured step reads the value after the step (the side stream's
+    // check has written it already)
+    if (!c.div_pending) div_final(c);
     return EK_OK;
   }
   std::vector<double> part(d.NY - 2);
