@@ -318,6 +318,8 @@ struct Ctx {
   // residual rule: left null vector of the finest kx = 0 operator (nfx*nfy,
   // unit norm), for the well-posed kx = 0 solve
   double *mg_z = nullptr;
+  // per-chunk partial sums of the kx = 0 projections (pmax x kNullChunks)
+  double *mg_null_part = nullptr;
   ek_mg_stats last_stats{};
   // problems that missed the residual rule's tolerance, and problems solved,
   // summed over every solve since the context was created
@@ -541,6 +543,7 @@ int mg_exact_stats(Ctx &c, MgWork &w, int nprob, ek_mg_stats *st);
 // fastest): b <- b - (z.b) z before the solve, phi <- phi - mean(phi) after.
 void mg_null_project(Ctx &c, double *rhs_finest, int nprob, const double *kx2_dev);
 void mg_null_mean(Ctx &c, double *phi_finest, int nprob, const double *kx2_dev);
+constexpr int kNullChunks = 64;  // blocks per kx = 0 problem of the null-space projections
 void mg_alloc(Ctx &c, int pmax);
 void mg_work_alloc(Ctx &c, MgWork &w, int pmax);
 void mg_work_free(MgWork &w);
