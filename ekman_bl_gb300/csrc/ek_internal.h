@@ -311,7 +311,7 @@ struct Ctx {
   float *mgf_phh = nullptr, *mgf_phl = nullptr;  // float-float finest iterate
   float *mgf_phh2 = nullptr, *mgf_phl2 = nullptr;  // its second buffer (alternate corrections)
   float *mgf_bh = nullptr, *mgf_bl = nullptr;    // float-float finest rhs
-  float *mgf_cfh = nullptr, *mgf_cfl = nullptr;  // float-float finest coefficients
+  float2 *mgf_cf2 = nullptr;  // float-float finest coefficients, (hi, lo) interleaved
   int mgf_pmax = 0;
   float *mgf_tailfac = nullptr;  // Thomas factors of the coarse levels' lines (k_f_vtail), per problem
   size_t mgf_tailfac_n = 0;

@@ -44,7 +44,7 @@ struct FastDev {
   float *phh, *phl;         // float-float finest iterate, with ghosts (buffer 0)
   float *phh2, *phl2;       // buffer 1: problem p's iterate after n corrections is in buffer n & 1
   float *bh, *bl;           // float-float finest rhs
-  const float *cfh, *cfl;   // float-float finest coefficients
+  const float2 *cf2;        // float-float finest coefficients, (hi, lo) interleaved
   int nfx, nfy;
   const double *kx2;
   double *phif;            // output (finest interior, problem fastest)
@@ -103,7 +103,10 @@ __global__ void __launch_bounds__(32 * kRY, 4) k_f_resid_ff(FastDev g) {
     for (int i = i0; i <= i1; ++i) {
       const size_t pt = (size_t)(j - 1) * nx + (i - 1);
       const size_t q = row + (size_t)i * si;
-      auto CF = [&](int l) { return FF(g.cfh[l * npt + pt], g.cfl[l * npt + pt]); };
+      auto CF = [&](int l) {
+        const float2 v = g.cf2[l * npt + pt];
+        return FF(v.x, v.y);
+      };
       const FF wp = V(q + si), wn = V(q + sj), ws = V(q - sj);
       FF s = CF(0) * wp;
       if (!ORTH) s = s + CF(1) * V(q + si + sj);
@@ -1226,8 +1229,7 @@ FastDev make_fastdev(Ctx &c, int nprob, const double *kx2_dev) {
   g.phl2 = c.mgf_phl2;
   g.bh = c.mgf_bh;
   g.bl = c.mgf_bl;
-  g.cfh = c.mgf_cfh;
-  g.cfl = c.mgf_cfl;
+  g.cf2 = c.mgf_cf2;
   g.nfx = PL.nfx;
   g.nfy = PL.nfy;
   g.kx2 = kx2_dev;
@@ -1297,7 +1299,7 @@ void mgfast_alloc(Ctx &c, int pmax) {
   const size_t nph = (size_t)(PL.nfx + 2) * (PL.nfy + 2), nf = (size_t)PL.nfx * PL.nfy;
   tot += nph * pmax;
   const size_t ff_off = tot;
-  tot += 4 * nph * pmax + 2 * nf * pmax + 22 * nf;
+  tot += 4 * nph * pmax + 2 * nf * pmax + 22 * nf + 1;
   const int ltop = tail_level(PL);
   const size_t nfac = ltop ? (size_t)make_tail_plan(PL, ltop).nfac * pmax : 0;
   tot = (tot + 3) & ~(size_t)3;  // float4 reads of each problem's factor block
@@ -1323,8 +1325,13 @@ void mgfast_alloc(Ctx &c, int pmax) {
   c.mgf_phl2 = c.mgf_phh2 + nph * pmax;
   c.mgf_bh = c.mgf_phl2 + nph * pmax;
   c.mgf_bl = c.mgf_bh + nf * pmax;
-  c.mgf_cfh = c.mgf_bl + nf * pmax;
-  c.mgf_cfl = c.mgf_cfh + 11 * nf;
+  // 8-byte aligned for the float2 loads: the address itself decides (the
+  // pool holds one float of slack)
+  {
+    float *cfb = c.mgf_bl + nf * pmax;
+    if (reinterpret_cast<uintptr_t>(cfb) & 7) ++cfb;
+    c.mgf_cf2 = reinterpret_cast<float2 *>(cfb);
+  }
   c.mgf_tailfac = nfac ? c.mgf_pool + fac_off : nullptr;
   c.mgf_tailfac_n = nfac;
   // every context's tail fits kTailSmem, so one process-wide limit serves all
@@ -1333,13 +1340,12 @@ void mgfast_alloc(Ctx &c, int pmax) {
   {
     // the finest coefficients split into float-float pairs
     const std::vector<double> &cf = PL.cof_host[PL.ngrid - 1];
-    std::vector<float> h(cf.size()), l(cf.size());
+    std::vector<float2> hl(cf.size());
     for (size_t t = 0; t < cf.size(); ++t) {
-      h[t] = (float)cf[t];
-      l[t] = (float)(cf[t] - (double)h[t]);
+      const float h = (float)cf[t];
+      hl[t] = make_float2(h, (float)(cf[t] - (double)h));
     }
-    EK_CUDA(cudaMemcpy(c.mgf_cfh, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice));
-    EK_CUDA(cudaMemcpy(c.mgf_cfl, l.data(), sizeof(float) * l.size(), cudaMemcpyHostToDevice));
+    EK_CUDA(cudaMemcpy(c.mgf_cf2, hl.data(), sizeof(float2) * hl.size(), cudaMemcpyHostToDevice));
   }
   c.mgf_pmax = pmax;
 }
