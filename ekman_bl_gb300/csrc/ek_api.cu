@@ -817,6 +817,7 @@ void ekgpu_destroy(ek_ctx *h) {
   mg_work_free(c.mgw);
   guess_free(c);
   if (c.mgf_pool) cudaFree(c.mgf_pool);
+  if (c.mgf_cf4_pool) cudaFree(c.mgf_cf4_pool);
   if (c.mg_null_part) cudaFree(c.mg_null_part);
   if (c.mg.ops_dev) cudaFree(c.mg.ops_dev);
   c.poll.destroy();

@@ -148,6 +148,11 @@ struct MgOp {
 // FP32 arrays of one level for the mixed-precision multigrid (ek_mgfast.cu).
 struct MgLevelF {
   float *e = nullptr, *r = nullptr, *cp = nullptr, *cof = nullptr;
+  // the same coefficients packed per point for the level residual's vector
+  // loads (planes c[l] of cof): [3 pt] = (c0, c2, c4, c6), the couplings
+  // along the axes; [3 pt + 1] = (c8, c9, c10, 0), the diagonal's parts;
+  // [3 pt + 2] = (c1, c3, c5, c7), the corner couplings
+  float4 *cf4 = nullptr;
 };
 
 struct MgPlan {
@@ -306,6 +311,7 @@ struct Ctx {
   MgWork mgw;                       // the solves' work arrays
   std::vector<double> mg_kx2_host;  // host copy of mgw.kx2
   float *mgf_pool = nullptr;        // mixed-precision multigrid
+  float4 *mgf_cf4_pool = nullptr;   // its packed level coefficients
   std::vector<MgLevelF> mgf_levels;
   float *mgf_scratch = nullptr;
   float *mgf_phh = nullptr, *mgf_phl = nullptr;  // float-float finest iterate

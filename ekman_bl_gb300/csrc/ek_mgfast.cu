@@ -35,6 +35,7 @@ namespace {
 struct LvF {
   int nx, ny;
   float *e, *r, *cof, *cp;  // e: (0:nx+1,0:ny+1)xP; r: nx*ny*P; cof: 11*nx*ny; cp: line-solve scratch nx*ny*P
+  const float4 *cf4;        // cof packed per point (MgLevelF::cf4), for the level residual
 };
 struct FastDev {
   int P, ngrid, orth;
@@ -750,6 +751,26 @@ __device__ __forceinline__ void f_restrict_at(const float *__restrict__ scr, flo
        4.f * R(i, j)) * .0625f;
 }
 
+// the same residual from the packed coefficients (the same products and
+// sums, in the same order): two or three vector loads for seven or eleven
+// scalar ones
+__device__ __forceinline__ void f_resid_at4(const float4 *__restrict__ cf4, const float *__restrict__ ee,
+                                            const float *__restrict__ rr, float *__restrict__ scr, int nx, int P,
+                                            int p, int i, int j, float kx2, bool orth) {
+  const size_t si = P, sj = (size_t)(nx + 2) * P;
+  const size_t pt = (size_t)(j - 1) * nx + (i - 1);
+  const float *ep = &ee[((size_t)j * (nx + 2) + i) * P + p];
+  const float4 q0 = cf4[3 * pt], q1 = cf4[3 * pt + 1];
+  float s = q0.x * ep[si] + q0.y * ep[sj] + q0.z * ep[-(long)si] + q0.w * ep[-(long)sj];
+  if (!orth) {
+    const float4 q2 = cf4[3 * pt + 2];
+    s += q2.x * ep[si + sj] + q2.y * ep[sj - si] + q2.z * ep[-(long)(si + sj)] + q2.w * ep[si - sj];
+  }
+  const float c9 = ((-kx2 * q1.z) - q1.x) + q1.y;
+  s += c9 * ep[0];
+  scr[((size_t)j * (nx + 2) + i) * P + p] = rr[pt * P + p] - s;
+}
+
 // residual of the correction equation at a level (FP32) into the scratch
 __global__ void __launch_bounds__(32 * kRowWarps) k_f_resid32(FastDev g, int level) {
   if (*g.alldone) return;
@@ -762,7 +783,7 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_f_resid32(FastDev g, int lev
   const bool orth = g.orth != 0;
 #pragma unroll 4
   for (int i = 1 + (int)threadIdx.y; i <= nx; i += kRowWarps)
-    f_resid_at(L.cof, L.e, L.r, g.scr, nx, L.ny, P, p, i, j, kx2, orth);
+    f_resid_at4(L.cf4, L.e, L.r, g.scr, nx, P, p, i, j, kx2, orth);
 }
 
 // full weighting (res2, mudcom.f:120-257) to the coarse rhs; e_coarse = 0
@@ -1219,7 +1240,7 @@ FastDev make_fastdev(Ctx &c, int nprob, const double *kx2_dev) {
   g.orth = PL.orth ? 1 : 0;
   for (int l = 0; l < PL.ngrid; ++l) {
     const MgLevelF &F = c.mgf_levels[l];
-    g.lv[l] = LvF{PL.lv[l].nx, PL.lv[l].ny, F.e, F.r, F.cof, F.cp};
+    g.lv[l] = LvF{PL.lv[l].nx, PL.lv[l].ny, F.e, F.r, F.cof, F.cp, F.cf4};
   }
   g.scr = c.mgf_scratch;
   g.rhs = w.rhs[PL.ngrid - 1];
@@ -1307,6 +1328,14 @@ void mgfast_alloc(Ctx &c, int pmax) {
   tot += nfac;
   EK_CUDA(cudaMalloc(&c.mgf_pool, tot * sizeof(float)));
   c.mgf_levels.assign(PL.ngrid, {});
+  // the packed coefficients (3 float4 per point and level)
+  if (c.mgf_cf4_pool) {
+    cudaFree(c.mgf_cf4_pool);
+    c.mgf_cf4_pool = nullptr;
+  }
+  size_t n4 = 0;
+  for (int l = 0; l < PL.ngrid; ++l) n4 += 3 * (size_t)PL.lv[l].nx * PL.lv[l].ny;
+  EK_CUDA(cudaMalloc(&c.mgf_cf4_pool, n4 * sizeof(float4)));
   for (int l = 0; l < PL.ngrid; ++l) {
     const MgLevel &L = PL.lv[l];
     float *b = c.mgf_pool + off[l];
@@ -1317,6 +1346,20 @@ void mgfast_alloc(Ctx &c, int pmax) {
     F.cof = F.cp + (size_t)L.nx * L.ny * pmax;
     std::vector<float> cf(PL.cof_host[l].begin(), PL.cof_host[l].end());
     EK_CUDA(cudaMemcpy(F.cof, cf.data(), sizeof(float) * cf.size(), cudaMemcpyHostToDevice));
+    {
+      const size_t npt = (size_t)L.nx * L.ny;
+      size_t o4 = 0;
+      for (int q = 0; q < l; ++q) o4 += 3 * (size_t)PL.lv[q].nx * PL.lv[q].ny;
+      F.cf4 = c.mgf_cf4_pool + o4;
+      std::vector<float4> pk(3 * npt);
+      for (size_t pt = 0; pt < npt; ++pt) {
+        auto C = [&](int t) { return cf[t * npt + pt]; };
+        pk[3 * pt] = make_float4(C(0), C(2), C(4), C(6));
+        pk[3 * pt + 1] = make_float4(C(8), C(9), C(10), 0.f);
+        pk[3 * pt + 2] = make_float4(C(1), C(3), C(5), C(7));
+      }
+      EK_CUDA(cudaMemcpy(F.cf4, pk.data(), sizeof(float4) * pk.size(), cudaMemcpyHostToDevice));
+    }
   }
   c.mgf_scratch = c.mgf_pool + scr_off;
   c.mgf_phh = c.mgf_pool + ff_off;

@@ -1229,10 +1229,17 @@ __global__ void k_div_check(Dims d, const double *kx, const double *jacm, const 
 __global__ void k_div_sum_f(Dims d, const float *S, double *part) {
   const int j = 2 + blockIdx.x;
   __shared__ double red[256];
-  FF s(0.0f, 0.0f);
-  for (int k = 2; k <= d.NZ - 1; ++k)
-    for (int i = 1 + threadIdx.x; i <= d.NX + 1; i += blockDim.x) s = s + FF(fabsf(S[d.ip(i, k, j)]), 0.0f);
-  red[threadIdx.x] = (double)s;
+  // four accumulators over consecutive K, so four dependent chains interleave
+  FF s[4] = {FF(0.0f, 0.0f), FF(0.0f, 0.0f), FF(0.0f, 0.0f), FF(0.0f, 0.0f)};
+  for (int i = 1 + threadIdx.x; i <= d.NX + 1; i += blockDim.x) {
+    int k = 2;
+    for (; k + 3 <= d.NZ - 1; k += 4) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) s[u] = s[u] + FF(fabsf(S[d.ip(i, k + u, j)]), 0.0f);
+    }
+    for (; k <= d.NZ - 1; ++k) s[0] = s[0] + FF(fabsf(S[d.ip(i, k, j)]), 0.0f);
+  }
+  red[threadIdx.x] = (double)((s[0] + s[1]) + (s[2] + s[3]));
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];

@@ -164,3 +164,27 @@ def test_ensemble_graph_equals_members_stepped_alone():
     finally:
         for s in together + alone:
             s.close()
+
+
+@pytest.mark.parametrize("variant", ["plain", "sponge"])
+def test_concurrent_branches_equal_one_chain(variant):
+    """The increment form's concurrent branches (each field's chain on its own
+    stream, a captured step's divergence check on a side stream) against the
+    same steps as one chain of launches (the per-kernel timer forces that),
+    bit for bit: the branches share no array, so no ordering between them
+    can change a result.  The sponge case crosses sponge_th's CU2X reset."""
+    if variant == "plain":
+        case = small_case()
+    else:
+        p, xp, yp, st = sponge_case(2, True, save_stats_int=4)
+        case = (p, xp, yp, st)
+    g, e = _pair(case, 2)
+    try:
+        e.set_step_graph(False)
+        e.set_timing(True)
+        for _ in range(5):
+            assert g.step(1) == 0 and e.step(1) == 0
+            _same(g, e)
+    finally:
+        g.close()
+        e.close()
