@@ -185,10 +185,34 @@ __device__ __forceinline__ void dif_fft_reg(V *z, const V *tw, bool conj_tw, int
       }
     }
   }
+  // v[t] holds DIF position p = lane + 32 t, i.e. frequency brev(p) =
+  // rev5(lane) E + revE(t); it goes to its natural-order slot with one pad
+  // element every E (fslot), so that this store and the readers' runs of
+  // consecutive frequencies fall in distinct banks (the bit-reversed order
+  // puts a warp's 32 frequencies E elements apart)
+  const int r5 = (int)(__brev((unsigned)lane) >> 27);
 #pragma unroll
-  for (int t = 0; t < E; ++t) z[lane + 32 * t] = v[t];
+  for (int t = 0; t < E; ++t) {
+    int rt = 0;
+#pragma unroll
+    for (int b = 1, q = E >> 1; b < E; b <<= 1, q >>= 1)
+      if (t & b) rt |= q;
+    z[r5 * (E + 1) + rt] = v[t];
+  }
   __syncwarp();
 }
+
+// Where frequency f of a transform of M = 32 E points sits after
+// dif_fft_any<E>: natural order with a pad element every E (the register
+// form), bit-reversed order (the shared-memory loop, E = 0).
+template <int E>
+__device__ __forceinline__ int fslot(int f, int logM) {
+  if constexpr (E > 0) return f + f / E;
+  else return (int)brev((unsigned)f, logM);
+}
+// Per-warp stride of the spectra in shared memory: room for the pad slots
+template <int E>
+__device__ __forceinline__ int fstride(int M) { return (E > 0) ? M + 32 : M; }
 
 // The register form for M = 32 E (E > 0, chosen per launch so that each
 // size gets its own register budget), the shared-memory loop otherwise.
@@ -258,7 +282,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
   const int k = args.k0 + kw;
   const int j = args.j0 + (int)blockIdx.y;
   const int NX = d.NX, M = fc.M;
-  V *z = smem_c + (size_t)warp * M;
+  V *z = smem_c + (size_t)warp * fstride<E>(M);
   T *zr = reinterpret_cast<T *>(z);
   const size_t base = d.ip(0, k, j);
   constexpr bool kF = sizeof(T) == 4;
@@ -297,7 +321,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
   // with fuse_flux the same line's flux term (PRO_FLUX of a2 against b2, and
   // its LES addition) goes through a second transform in the same warp
   const bool fuse = args.fuse_flux != 0;
-  V *z2 = smem_c + (size_t)(kWarpsPerBlock + warp) * M;
+  V *z2 = smem_c + (size_t)(kWarpsPerBlock + warp) * fstride<E>(M);
   if (fuse) {
     T *zr2 = reinterpret_cast<T *>(z2);
     const bool fin2 = kF && args.a2f != nullptr;
@@ -321,7 +345,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_r2c(FftConst fc, R2cArg
       if (args.epi == EPI_STORE || args.zero_hi) dst[kk] = cplx_t{0.0, 0.0};
       continue;
     }
-    const int ik = brev(kk & (M - 1), fc.logM), im = brev((M - kk) & (M - 1), fc.logM);
+    const int ik = fslot<E>(kk & (M - 1), fc.logM), im = fslot<E>((M - kk) & (M - 1), fc.logM);
     const V w = twn[kk];
     auto split = [&](const V *zz, T &tr, T &ti) {
       const V zk = zz[ik], zm = zz[im];
@@ -393,7 +417,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
   const int k = args.k0 + kw;
   const int j = args.j0 + (int)blockIdx.y;
   const int M = fc.M, NKX = d.NKX;
-  V *z = smem_c + (size_t)warp * M;
+  V *z = smem_c + (size_t)warp * fstride<E>(M);
   const cplx_t *src = args.src + d.ic(0, k, j);
   const cplx_t *src2 = args.src2 ? args.src2 + d.ic(0, k, j) : nullptr;
   auto X = [&](int kk) -> V {
@@ -443,7 +467,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
       float *dlo = args.dstlo + d.ip(0, k, j);
       for (int n = lane; n < NX + 2; n += 32) {
         FF v(0.0f, 0.0f);
-        if (n < NX) v = zr[2 * brev(n >> 1, fc.logM) + (n & 1)];
+        if (n < NX) v = zr[2 * fslot<E>(n >> 1, fc.logM) + (n & 1)];
         dstf[n] = v.hi;
         dlo[n] = v.lo;
       }
@@ -454,7 +478,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_c2r(FftConst fc, C2rArg
     T v = T(0.0);
     if (n < NX) {
       const int m = n >> 1;
-      v = zr[2 * brev(m, fc.logM) + (n & 1)];
+      v = zr[2 * fslot<E>(m, fc.logM) + (n & 1)];
     }
     if constexpr (sizeof(T) == 4) {
       if (dst) dst[n] = f2d_bits((float)v);
@@ -568,7 +592,9 @@ void launch_r2c(Ctx &c, const R2cArgs &a) {
   const int nops = (a.pro == PRO_LOAD) ? 1 : (a.pro == PRO_PROD) ? (a.fuse_flux ? 4 : 2) : 3;
   const double epi = (a.epi == EPI_STORE) ? 16.0 * (c.d.NX2P + 1) : 32.0 * (c.d.NKX + 1);
   KScope ks(c, KC_R2C, nlines * (elt * c.d.NX * nops + epi));
-  if (lp) run_r2c<float>(grid, smem / 2, c.stream, fc, a);
+  // FP32 spectra: 8 bytes an element, with the register form's pad slots
+  const size_t smem_f = sizeof(float2) * (fc.M + 32) * kWarpsPerBlock * (a.fuse_flux ? 2 : 1);
+  if (lp) run_r2c<float>(grid, smem_f, c.stream, fc, a);
   else if (fft_ff(c, a.lowp)) run_r2c<FF>(grid, smem, c.stream, fc, a);
   else run_r2c<double>(grid, smem, c.stream, fc, a);
   after_launch(c);
@@ -584,7 +610,8 @@ void launch_c2r(Ctx &c, const C2rArgs &a) {
   // and float-float low part as given)
   const double out = (a.dst ? 8.0 : 0.0) + (a.dstf ? 4.0 : 0.0) + (a.dstlo ? 4.0 : 0.0);
   KScope ks(c, KC_C2R, nlines * (16.0 * (c.d.NKX + 1) * (a.src2 ? 2 : 1) + out * (c.d.NX + 2)));
-  if (fft_lowp(c, a.lowp)) run_c2r<float>(grid, smem / 2, c.stream, fc, a);
+  const size_t smem_f = sizeof(float2) * (fc.M + 32) * kWarpsPerBlock;
+  if (fft_lowp(c, a.lowp)) run_c2r<float>(grid, smem_f, c.stream, fc, a);
   else if (fft_ff(c, a.lowp)) run_c2r<FF>(grid, smem, c.stream, fc, a);
   else run_c2r<double>(grid, smem, c.stream, fc, a);
   after_launch(c);
